@@ -1,0 +1,615 @@
+// fvx_particles.cu -- all-pairs vortex-particle sweeps (velocity, stretching,
+// velocity gradient, vorticity) with the Winckelmans or Gaussian-erf core.
+//
+// Replaces src/fluxvortex/kernel.py:69-190 (NumPy, 512 x 512 chunks) and its
+// unused Warp ports src/fluxvortex/warp_vpm.py:20-141 (one thread per pair,
+// one atomic per pair and component).
+//
+// Closed forms used (C = -1/(4 pi) folded into alpha on staging; d = x_t - x_s;
+// f(r) = g(r/sigma)/r^3 and fpr = f'(r)/r, both finite at r = 0):
+//   u      += f (d x a)                                      kernel.py:103-114
+//   J_ij   += fpr (d x a)_i d_j + f eps_ijl a_l              kernel.py:156-188
+//   S       = J . G_t = f (G_t x a) + fpr (d . G_t)(d x a)   particles.py:148-151
+//   omega_i = eps_ijk J_kj = fpr (d (d . a) - a r^2) - 2 f a particles.py:219-225
+// Winckelmans: f = (r^2 + 2.5 s^2) q^-5/2, fpr = -(3 r^2 + 10.5 s^2) q^-7/2,
+//   q = r^2 + s^2 (kernel.py:42-55 rewritten without r_bar = r/sigma).
+// Gaussian-erf: for r/sigma >= 0.5 the kernel.py:16-31 formula; below it the
+//   Taylor series of g(r)/r^3 (the reference's erf - c r exp form cancels
+//   there and is pure rounding noise at its r = 1e-12 self-pair clamp).
+//
+// Layout and tiling: a CTA owns 128 (FP64) or 256 (FP32, two per thread)
+// targets held in registers.  Source tiles of 128 particles (AoS pos, alpha,
+// sigma exactly as the caller stores them) are staged by 1-D TMA bulk copies
+// (cp.async.bulk) into a double-buffered raw area, then converted by all
+// threads into a compute tile (alpha pre-scaled by C, sigma^2 and the core's
+// second constant precomputed; FP32 positions re-centred on the CTA's first
+// target in FP64 before rounding).  Every thread then sweeps the tile reading
+// shared memory by broadcast.  FP32 sums are kept per tile and folded into a
+// two-sum (hi, lo) pair per component.  When targets alone cannot fill the
+// SMs the source range is split over gridDim.y; partial sums go to scratch
+// and a second kernel adds them in fixed order.
+#include <type_traits>
+
+#include "fvx_common.cuh"
+
+namespace fvx {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kSrcTile = 128;
+constexpr double kC = -0.07957747154594767;  // -1/(4 pi)
+constexpr double kSqrt2OverPi = 0.79788456080286535588;
+constexpr double kInvSqrt2 = 0.70710678118654752440;
+
+template <int MODE>
+struct ModeInfo;
+template <>
+struct ModeInfo<FVX_PAIR_VELOCITY> {
+  static constexpr int ncomp = 3, na = 3;
+  static constexpr bool need_fpr = false, need_tg = false;
+};
+template <>
+struct ModeInfo<FVX_PAIR_STRETCH> {
+  static constexpr int ncomp = 3, na = 3;
+  static constexpr bool need_fpr = true, need_tg = true;
+};
+template <>
+struct ModeInfo<FVX_PAIR_VELOCITY_STRETCH> {
+  static constexpr int ncomp = 6, na = 3;
+  static constexpr bool need_fpr = true, need_tg = true;
+};
+template <>
+struct ModeInfo<FVX_PAIR_JACOBIAN> {
+  static constexpr int ncomp = 9, na = 9;
+  static constexpr bool need_fpr = true, need_tg = false;
+};
+template <>
+struct ModeInfo<FVX_PAIR_VORTICITY> {
+  static constexpr int ncomp = 3, na = 3;
+  static constexpr bool need_fpr = true, need_tg = false;
+};
+
+// ---- regularising cores -----------------------------------------------------
+// Series coefficients of h(rho) = g(rho)/rho^3 for the Gaussian-erf core:
+// g(rho) = sqrt(2/pi) int_0^rho t^2 exp(-t^2/2) dt, so
+// h = sqrt(2/pi) sum_k a_k rho^(2k), a_k = (-1)^k / (2^k k! (2k+3)).
+#define FVX_GA0 (1.0 / 3.0)
+#define FVX_GA1 (-1.0 / 10.0)
+#define FVX_GA2 (1.0 / 56.0)
+#define FVX_GA3 (-1.0 / 432.0)
+#define FVX_GA4 (1.0 / 4224.0)
+#define FVX_GA5 (-1.0 / 49920.0)
+#define FVX_GA6 (1.0 / 691200.0)
+#define FVX_GA7 (-1.0 / 10967040.0)
+#define FVX_GA8 (1.0 / 196116480.0)
+#define FVX_GA9 (-1.0 / 3901685760.0)
+#define FVX_GA10 (1.0 / 85463500800.0)
+
+// Staged per-source constants: s2 = sigma^2, k2 = 2.5 sigma^2 (Winckelmans)
+// or 1/sigma (Gaussian).
+template <int KERNEL, bool NEED_FPR>
+__device__ __forceinline__ void core_f64(double r2, double s2, double k2, double& f,
+                                         double& fpr) {
+  if (KERNEL == FVX_KERNEL_WINCKELMANS) {
+    double q = r2 + s2;
+    double t = rsqrt(q);
+    double t2 = t * t;
+    double t5 = t2 * t2 * t;
+    f = (r2 + k2) * t5;
+    if (NEED_FPR) fpr = -(3.0 * r2 + 10.5 * s2) * (t5 * t2);
+  } else {
+    const double inv_s = k2;
+    const double x = r2 * inv_s * inv_s;  // rho^2
+    if (x < 0.25) {
+      double h = FVX_GA10;
+      h = fma(h, x, FVX_GA9);
+      h = fma(h, x, FVX_GA8);
+      h = fma(h, x, FVX_GA7);
+      h = fma(h, x, FVX_GA6);
+      h = fma(h, x, FVX_GA5);
+      h = fma(h, x, FVX_GA4);
+      h = fma(h, x, FVX_GA3);
+      h = fma(h, x, FVX_GA2);
+      h = fma(h, x, FVX_GA1);
+      h = fma(h, x, FVX_GA0);
+      const double is3 = inv_s * inv_s * inv_s;
+      f = kSqrt2OverPi * h * is3;
+      if (NEED_FPR) {
+        double d = 20.0 * FVX_GA10;
+        d = fma(d, x, 18.0 * FVX_GA9);
+        d = fma(d, x, 16.0 * FVX_GA8);
+        d = fma(d, x, 14.0 * FVX_GA7);
+        d = fma(d, x, 12.0 * FVX_GA6);
+        d = fma(d, x, 10.0 * FVX_GA5);
+        d = fma(d, x, 8.0 * FVX_GA4);
+        d = fma(d, x, 6.0 * FVX_GA3);
+        d = fma(d, x, 4.0 * FVX_GA2);
+        d = fma(d, x, 2.0 * FVX_GA1);
+        fpr = kSqrt2OverPi * d * is3 * inv_s * inv_s;
+      }
+    } else {
+      double r = sqrt(r2);
+      double rho = r * inv_s;
+      double e = exp(-0.5 * x);
+      double g = erf(rho * kInvSqrt2) - kSqrt2OverPi * rho * e;
+      double ir = 1.0 / r;
+      double ir3 = ir * ir * ir;
+      f = g * ir3;
+      if (NEED_FPR) {
+        double dg = kSqrt2OverPi * x * e;
+        fpr = (dg * inv_s - 3.0 * g * ir) * ir3 * ir;
+      }
+    }
+  }
+}
+
+template <int KERNEL, bool NEED_FPR>
+__device__ __forceinline__ void core_f32(float r2, float s2, float k2, float& f, float& fpr) {
+  if (KERNEL == FVX_KERNEL_WINCKELMANS) {
+    float q = r2 + s2;
+    float t = rsqrtf(q);
+    float t2 = t * t;
+    float t5 = t2 * t2 * t;
+    f = (r2 + k2) * t5;
+    if (NEED_FPR) fpr = -(3.0f * r2 + 10.5f * s2) * (t5 * t2);
+  } else {
+    const float inv_s = k2;
+    const float x = r2 * inv_s * inv_s;
+    if (x < 0.25f) {
+      float h = static_cast<float>(FVX_GA6);
+      h = fmaf(h, x, static_cast<float>(FVX_GA5));
+      h = fmaf(h, x, static_cast<float>(FVX_GA4));
+      h = fmaf(h, x, static_cast<float>(FVX_GA3));
+      h = fmaf(h, x, static_cast<float>(FVX_GA2));
+      h = fmaf(h, x, static_cast<float>(FVX_GA1));
+      h = fmaf(h, x, static_cast<float>(FVX_GA0));
+      const float is3 = inv_s * inv_s * inv_s;
+      f = static_cast<float>(kSqrt2OverPi) * h * is3;
+      if (NEED_FPR) {
+        float d = static_cast<float>(12.0 * FVX_GA6);
+        d = fmaf(d, x, static_cast<float>(10.0 * FVX_GA5));
+        d = fmaf(d, x, static_cast<float>(8.0 * FVX_GA4));
+        d = fmaf(d, x, static_cast<float>(6.0 * FVX_GA3));
+        d = fmaf(d, x, static_cast<float>(4.0 * FVX_GA2));
+        d = fmaf(d, x, static_cast<float>(2.0 * FVX_GA1));
+        fpr = static_cast<float>(kSqrt2OverPi) * d * is3 * inv_s * inv_s;
+      }
+    } else {
+      float ir = rsqrtf(r2);
+      float r = r2 * ir;
+      float rho = r * inv_s;
+      float e = expf(-0.5f * x);
+      float g = erff(rho * static_cast<float>(kInvSqrt2)) -
+                static_cast<float>(kSqrt2OverPi) * rho * e;
+      float ir3 = ir * ir * ir;
+      f = g * ir3;
+      if (NEED_FPR) {
+        float dg = static_cast<float>(kSqrt2OverPi) * x * e;
+        fpr = (dg * inv_s - 3.0f * g * ir) * ir3 * ir;
+      }
+    }
+  }
+}
+
+// ---- per-pair accumulation ----------------------------------------------------
+template <int MODE, typename T>
+__device__ __forceinline__ void accumulate(T* acc, T dx, T dy, T dz, T r2, T ax, T ay, T az,
+                                           T f, T fpr, T gx, T gy, T gz) {
+  const T cx = dy * az - dz * ay;
+  const T cy = dz * ax - dx * az;
+  const T cz = dx * ay - dy * ax;
+  if (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_VELOCITY_STRETCH) {
+    acc[0] += f * cx;
+    acc[1] += f * cy;
+    acc[2] += f * cz;
+  }
+  if (MODE == FVX_PAIR_STRETCH || MODE == FVX_PAIR_VELOCITY_STRETCH) {
+    constexpr int o = MODE == FVX_PAIR_STRETCH ? 0 : 3;
+    const T w = fpr * (dx * gx + dy * gy + dz * gz);
+    acc[o + 0] += f * (gy * az - gz * ay) + w * cx;
+    acc[o + 1] += f * (gz * ax - gx * az) + w * cy;
+    acc[o + 2] += f * (gx * ay - gy * ax) + w * cz;
+  }
+  if (MODE == FVX_PAIR_JACOBIAN) {
+    const T px = fpr * cx, py = fpr * cy, pz = fpr * cz;
+    acc[0] += px * dx;
+    acc[1] += px * dy + f * az;
+    acc[2] += px * dz - f * ay;
+    acc[3] += py * dx - f * az;
+    acc[4] += py * dy;
+    acc[5] += py * dz + f * ax;
+    acc[6] += pz * dx + f * ay;
+    acc[7] += pz * dy - f * ax;
+    acc[8] += pz * dz;
+  }
+  if (MODE == FVX_PAIR_VORTICITY) {
+    const T da = dx * ax + dy * ay + dz * az;
+    const T f2 = f + f;
+    acc[0] += fpr * (dx * da - ax * r2) - f2 * ax;
+    acc[1] += fpr * (dy * da - ay * r2) - f2 * ay;
+    acc[2] += fpr * (dz * da - az * r2) - f2 * az;
+  }
+}
+
+struct RawSrc {
+  double pos[kSrcTile * 3];
+  double alpha[kSrcTile * 3];
+  double sigma[kSrcTile];
+};
+
+template <typename T>
+struct SrcTile {
+  T x[kSrcTile], y[kSrcTile], z[kSrcTile];
+  T ax[kSrcTile], ay[kSrcTile], az[kSrcTile];
+  T s2[kSrcTile], k2[kSrcTile];
+};
+
+struct PairArgs {
+  const double* tgt;
+  const double* tgt_gamma;
+  int64_t n_tgt;
+  const double* pos;
+  const double* alpha;
+  const double* sigma;
+  int64_t n_src;
+  int64_t chunk;  // sources per split (even)
+  double* out_a;
+  double* out_b;
+  double* partial;  // (S, M, ncomp) when gridDim.y > 1
+  int use_tma;
+};
+
+__device__ void issue_src(const PairArgs& A, RawSrc& raw, int64_t j0, int cnt, uint64_t* bar) {
+  BulkPlan pp = plan_bulk(A.pos, j0, cnt, 24, A.use_tma);
+  BulkPlan pa = plan_bulk(A.alpha, j0, cnt, 24, A.use_tma);
+  BulkPlan ps = plan_bulk(A.sigma, j0, cnt, 8, A.use_tma);
+  mbar_arrive_expect_tx(bar, pp.bulk_bytes + pa.bulk_bytes + ps.bulk_bytes);
+  if (pp.bulk_bytes) bulk_g2s(raw.pos, A.pos + 3 * j0, pp.bulk_bytes, bar);
+  if (pa.bulk_bytes) bulk_g2s(raw.alpha, A.alpha + 3 * j0, pa.bulk_bytes, bar);
+  if (ps.bulk_bytes) bulk_g2s(raw.sigma, A.sigma + j0, ps.bulk_bytes, bar);
+}
+
+__device__ void tail_src(const PairArgs& A, RawSrc& raw, int64_t j0, int cnt) {
+  BulkPlan p = plan_bulk(A.pos, j0, cnt, 24, A.use_tma);
+  if (p.tail_bytes) plain_copy8(raw.pos, A.pos + 3 * j0, p.bulk_bytes, p.tail_bytes);
+  p = plan_bulk(A.alpha, j0, cnt, 24, A.use_tma);
+  if (p.tail_bytes) plain_copy8(raw.alpha, A.alpha + 3 * j0, p.bulk_bytes, p.tail_bytes);
+  p = plan_bulk(A.sigma, j0, cnt, 8, A.use_tma);
+  if (p.tail_bytes) plain_copy8(raw.sigma, A.sigma + j0, p.bulk_bytes, p.tail_bytes);
+}
+
+template <typename T>
+__device__ __forceinline__ void two_sum_fold(T& hi, T& lo, T p) {
+  T s = hi + p;
+  T bp = s - hi;
+  T err = (hi - (s - bp)) + (p - bp);
+  hi = s;
+  lo += err;
+}
+
+template <int MODE, int KERNEL, bool F32>
+__global__ void __launch_bounds__(kThreads) pairs_kernel(PairArgs A) {
+  using T = typename std::conditional<F32, float, double>::type;
+  constexpr int TPT = F32 ? 2 : 1;  // targets per thread
+  constexpr int NC = ModeInfo<MODE>::ncomp;
+  constexpr bool NEED_FPR = ModeInfo<MODE>::need_fpr;
+  constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
+
+  __shared__ __align__(128) RawSrc raw[2];
+  __shared__ __align__(16) SrcTile<T> tile;
+  __shared__ __align__(8) uint64_t bar[2];
+
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * (kThreads * TPT);
+  // Re-centring origin: the CTA's first target (FP32 only).
+  double ox = 0.0, oy = 0.0, oz = 0.0;
+  if (F32) {
+    ox = A.tgt[3 * base + 0];
+    oy = A.tgt[3 * base + 1];
+    oz = A.tgt[3 * base + 2];
+  }
+  T tx[TPT], ty[TPT], tz[TPT], gx[TPT], gy[TPT], gz[TPT];
+  bool act[TPT];
+#pragma unroll
+  for (int j = 0; j < TPT; ++j) {
+    const int64_t i = base + threadIdx.x + j * kThreads;
+    act[j] = i < A.n_tgt;
+    double px = 0, py = 0, pz = 0, qx = 0, qy = 0, qz = 0;
+    if (act[j]) {
+      px = A.tgt[3 * i + 0] - ox;
+      py = A.tgt[3 * i + 1] - oy;
+      pz = A.tgt[3 * i + 2] - oz;
+      if (NEED_TG) {
+        qx = A.tgt_gamma[3 * i + 0];
+        qy = A.tgt_gamma[3 * i + 1];
+        qz = A.tgt_gamma[3 * i + 2];
+      }
+    }
+    tx[j] = static_cast<T>(px);
+    ty[j] = static_cast<T>(py);
+    tz[j] = static_cast<T>(pz);
+    gx[j] = static_cast<T>(qx);
+    gy[j] = static_cast<T>(qy);
+    gz[j] = static_cast<T>(qz);
+  }
+
+  const int64_t jb = static_cast<int64_t>(blockIdx.y) * A.chunk;
+  const int64_t je = min(jb + A.chunk, A.n_src);
+  const int ntiles = jb < je ? static_cast<int>((je - jb + kSrcTile - 1) / kSrcTile) : 0;
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  T hi[TPT][NC], lo[TPT][NC];
+#pragma unroll
+  for (int j = 0; j < TPT; ++j)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) hi[j][c] = lo[j][c] = T(0);
+
+  uint32_t phase[2] = {0u, 0u};
+  bool ok = true;
+  if (ntiles > 0 && threadIdx.x == 0)
+    issue_src(A, raw[0], jb, static_cast<int>(min64(kSrcTile, je - jb)), &bar[0]);
+  int t = 0;
+  for (; t < ntiles; ++t) {
+    const int buf = t & 1;
+    const int64_t j0 = jb + static_cast<int64_t>(t) * kSrcTile;
+    const int n = static_cast<int>(min64(kSrcTile, je - j0));
+    if (t + 1 < ntiles && threadIdx.x == 0) {
+      const int64_t j1 = j0 + kSrcTile;
+      issue_src(A, raw[buf ^ 1], j1, static_cast<int>(min64(kSrcTile, je - j1)),
+                &bar[buf ^ 1]);
+    }
+    const bool got = mbar_wait(&bar[buf], phase[buf]);
+    if (!__syncthreads_and(got)) {
+      ok = false;
+      break;
+    }
+    phase[buf] ^= 1u;
+    tail_src(A, raw[buf], j0, n);
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += kThreads) {
+      const double sg = raw[buf].sigma[k];
+      tile.x[k] = static_cast<T>(raw[buf].pos[3 * k + 0] - ox);
+      tile.y[k] = static_cast<T>(raw[buf].pos[3 * k + 1] - oy);
+      tile.z[k] = static_cast<T>(raw[buf].pos[3 * k + 2] - oz);
+      tile.ax[k] = static_cast<T>(kC * raw[buf].alpha[3 * k + 0]);
+      tile.ay[k] = static_cast<T>(kC * raw[buf].alpha[3 * k + 1]);
+      tile.az[k] = static_cast<T>(kC * raw[buf].alpha[3 * k + 2]);
+      tile.s2[k] = static_cast<T>(sg * sg);
+      tile.k2[k] = static_cast<T>(KERNEL == FVX_KERNEL_WINCKELMANS ? 2.5 * sg * sg : 1.0 / sg);
+    }
+    __syncthreads();
+    T part[TPT][NC];
+#pragma unroll
+    for (int j = 0; j < TPT; ++j)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) part[j][c] = T(0);
+#pragma unroll 2
+    for (int k = 0; k < n; ++k) {
+      const T sx = tile.x[k], sy = tile.y[k], sz = tile.z[k];
+      const T ax = tile.ax[k], ay = tile.ay[k], az = tile.az[k];
+      const T s2 = tile.s2[k], k2 = tile.k2[k];
+#pragma unroll
+      for (int j = 0; j < TPT; ++j) {
+        const T dx = tx[j] - sx, dy = ty[j] - sy, dz = tz[j] - sz;
+        const T r2 = dx * dx + dy * dy + dz * dz;
+        T f, fpr = T(0);
+        if constexpr (F32)
+          core_f32<KERNEL, NEED_FPR>(r2, s2, k2, f, fpr);
+        else
+          core_f64<KERNEL, NEED_FPR>(r2, s2, k2, f, fpr);
+        accumulate<MODE, T>(part[j], dx, dy, dz, r2, ax, ay, az, f, fpr, gx[j], gy[j], gz[j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < TPT; ++j)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        if constexpr (F32)
+          two_sum_fold(hi[j][c], lo[j][c], part[j][c]);
+        else
+          hi[j][c] += part[j][c];
+      }
+    __syncthreads();
+  }
+  if (!ok) {
+    flag_status(kStatusTimeout);
+    if (threadIdx.x == 0 && t + 1 < ntiles) mbar_wait(&bar[(t + 1) & 1], phase[(t + 1) & 1]);
+    return;
+  }
+#pragma unroll
+  for (int j = 0; j < TPT; ++j) {
+    if (!act[j]) continue;
+    const int64_t i = base + threadIdx.x + j * kThreads;
+    double v[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+      v[c] = static_cast<double>(hi[j][c]) + static_cast<double>(lo[j][c]);
+    if (gridDim.y > 1) {
+      double* o = A.partial + (static_cast<int64_t>(blockIdx.y) * A.n_tgt + i) * NC;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) o[c] = v[c];
+    } else {
+      constexpr int NA = ModeInfo<MODE>::na;
+#pragma unroll
+      for (int c = 0; c < NA; ++c) A.out_a[i * NA + c] = v[c];
+#pragma unroll
+      for (int c = NA; c < NC; ++c) A.out_b[i * (NC - NA) + (c - NA)] = v[c];
+    }
+  }
+}
+
+__global__ void reduce_pairs_kernel(const double* __restrict__ partial, int64_t n_tgt, int nc,
+                                    int na, int splits, double* __restrict__ out_a,
+                                    double* __restrict__ out_b) {
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t n_vals = n_tgt * nc;
+  if (idx >= n_vals) return;
+  double s = 0.0;
+  for (int k = 0; k < splits; ++k) s += partial[static_cast<int64_t>(k) * n_vals + idx];
+  const int64_t i = idx / nc;
+  const int c = static_cast<int>(idx - i * nc);
+  if (c < na)
+    out_a[i * na + c] = s;
+  else
+    out_b[i * (nc - na) + (c - na)] = s;
+}
+
+int mode_ncomp(int mode) {
+  switch (mode) {
+    case FVX_PAIR_VELOCITY:
+    case FVX_PAIR_STRETCH:
+    case FVX_PAIR_VORTICITY:
+      return 3;
+    case FVX_PAIR_VELOCITY_STRETCH:
+      return 6;
+    case FVX_PAIR_JACOBIAN:
+      return 9;
+    default:
+      return -1;
+  }
+}
+
+int mode_na(int mode) { return mode == FVX_PAIR_VELOCITY_STRETCH ? 3 : mode_ncomp(mode); }
+
+int pair_splits(int precision, int64_t n_tgt, int64_t n_src, int64_t* chunk) {
+  const int per_cta = kThreads * (precision == FVX_PREC_F32C ? 2 : 1);
+  const int64_t gx = (n_tgt + per_cta - 1) / per_cta;
+  const int64_t want = 2LL * device_sm_count();
+  int64_t s = gx >= want ? 1 : (want + gx - 1) / gx;
+  // keep at least two source tiles per split
+  int64_t maxs = (n_src + 2 * kSrcTile - 1) / (2 * kSrcTile);
+  if (s > maxs) s = maxs;
+  if (s < 1) s = 1;
+  int64_t c = (n_src + s - 1) / s;
+  c = (c + 1) & ~int64_t(1);
+  s = (n_src + c - 1) / c;
+  *chunk = c;
+  return static_cast<int>(s);
+}
+
+template <int MODE, int KERNEL>
+void launch_mode(int precision, dim3 grid, cudaStream_t stream, const PairArgs& A) {
+  if (precision == FVX_PREC_F32C)
+    pairs_kernel<MODE, KERNEL, true><<<grid, kThreads, 0, stream>>>(A);
+  else
+    pairs_kernel<MODE, KERNEL, false><<<grid, kThreads, 0, stream>>>(A);
+}
+
+template <int KERNEL>
+void launch_kernel(int mode, int precision, dim3 grid, cudaStream_t stream, const PairArgs& A) {
+  switch (mode) {
+    case FVX_PAIR_VELOCITY:
+      launch_mode<FVX_PAIR_VELOCITY, KERNEL>(precision, grid, stream, A);
+      break;
+    case FVX_PAIR_STRETCH:
+      launch_mode<FVX_PAIR_STRETCH, KERNEL>(precision, grid, stream, A);
+      break;
+    case FVX_PAIR_VELOCITY_STRETCH:
+      launch_mode<FVX_PAIR_VELOCITY_STRETCH, KERNEL>(precision, grid, stream, A);
+      break;
+    case FVX_PAIR_JACOBIAN:
+      launch_mode<FVX_PAIR_JACOBIAN, KERNEL>(precision, grid, stream, A);
+      break;
+    default:
+      launch_mode<FVX_PAIR_VORTICITY, KERNEL>(precision, grid, stream, A);
+      break;
+  }
+}
+
+}  // namespace
+
+size_t particle_pairs_scratch(int mode, int precision, int64_t n_tgt, int64_t n_src) {
+  const int nc = mode_ncomp(mode);
+  if (nc < 0 || n_tgt <= 0 || n_src <= 0) return 0;
+  int64_t chunk = 0;
+  const int s = pair_splits(precision, n_tgt, n_src, &chunk);
+  return s > 1 ? sizeof(double) * static_cast<size_t>(nc) * n_tgt * s : 0;
+}
+
+int particle_pairs_launch(int mode, int kernel, int precision, const double* tgt,
+                          const double* tgt_gamma, int64_t n_tgt, const double* pos,
+                          const double* alpha, const double* sigma, int64_t n_src,
+                          double* out_a, double* out_b, void* scratch, size_t scratch_bytes,
+                          cudaStream_t stream) {
+  const int nc = mode_ncomp(mode);
+  FVX_ARG_CHECK(nc > 0, "unknown pair mode %d", mode);
+  FVX_ARG_CHECK(kernel == FVX_KERNEL_GAUSSIANERF || kernel == FVX_KERNEL_WINCKELMANS,
+                "unknown kernel %d", kernel);
+  FVX_ARG_CHECK(precision == FVX_PREC_F64 || precision == FVX_PREC_F32C,
+                "unknown precision %d", precision);
+  FVX_ARG_CHECK(n_tgt >= 0 && n_src >= 0, "negative size");
+  if (n_tgt == 0) return FVX_OK;
+  const int na = mode_na(mode);
+  FVX_ARG_CHECK(tgt && out_a, "null targets/output");
+  FVX_ARG_CHECK(na == nc || out_b, "mode needs out_b");
+  const bool need_tg = mode == FVX_PAIR_STRETCH || mode == FVX_PAIR_VELOCITY_STRETCH;
+  FVX_ARG_CHECK(!need_tg || tgt_gamma, "mode needs target strengths");
+  if (n_src == 0) {
+    FVX_CUDA_TRY(cudaMemsetAsync(out_a, 0, sizeof(double) * na * n_tgt, stream));
+    if (nc > na) FVX_CUDA_TRY(cudaMemsetAsync(out_b, 0, sizeof(double) * (nc - na) * n_tgt, stream));
+    return FVX_OK;
+  }
+  FVX_ARG_CHECK(pos && alpha && sigma, "null source array");
+  int64_t chunk = 0;
+  const int splits = pair_splits(precision, n_tgt, n_src, &chunk);
+  const size_t need = splits > 1 ? sizeof(double) * static_cast<size_t>(nc) * n_tgt * splits : 0;
+  if (need > 0 && (scratch == nullptr || scratch_bytes < need)) {
+    set_last_error("particle_pairs needs %zu scratch bytes, got %zu", need, scratch_bytes);
+    return FVX_ERR_SCRATCH;
+  }
+  PairArgs A;
+  A.tgt = tgt;
+  A.tgt_gamma = tgt_gamma;
+  A.n_tgt = n_tgt;
+  A.pos = pos;
+  A.alpha = alpha;
+  A.sigma = sigma;
+  A.n_src = n_src;
+  A.chunk = chunk;
+  A.out_a = out_a;
+  A.out_b = out_b;
+  A.partial = static_cast<double*>(scratch);
+  A.use_tma = aligned16(pos) && aligned16(alpha) && aligned16(sigma);
+  const int per_cta = kThreads * (precision == FVX_PREC_F32C ? 2 : 1);
+  const int64_t gx = (n_tgt + per_cta - 1) / per_cta;
+  FVX_ARG_CHECK(gx < (1LL << 31), "too many targets");
+  dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(splits));
+  if (kernel == FVX_KERNEL_WINCKELMANS)
+    launch_kernel<FVX_KERNEL_WINCKELMANS>(mode, precision, grid, stream, A);
+  else
+    launch_kernel<FVX_KERNEL_GAUSSIANERF>(mode, precision, grid, stream, A);
+  FVX_LAUNCH_CHECK();
+  if (splits > 1) {
+    const int64_t nv = n_tgt * nc;
+    reduce_pairs_kernel<<<static_cast<unsigned>((nv + 255) / 256), 256, 0, stream>>>(
+        static_cast<const double*>(scratch), n_tgt, nc, na, splits, out_a, out_b);
+    FVX_LAUNCH_CHECK();
+  }
+  return FVX_OK;
+}
+
+}  // namespace fvx
+
+extern "C" {
+
+size_t fvx_particle_pairs_scratch_bytes(int mode, int precision, int64_t n_targets,
+                                        int64_t n_sources) {
+  return fvx::particle_pairs_scratch(mode, precision, n_targets, n_sources);
+}
+
+int fvx_particle_pairs(int mode, int kernel, int precision, const double* tgt_pos,
+                       const double* tgt_gamma, int64_t n_targets, const double* src_pos,
+                       const double* src_gamma, const double* src_sigma, int64_t n_sources,
+                       double* out_a, double* out_b, void* scratch, size_t scratch_bytes,
+                       void* stream) {
+  return fvx::particle_pairs_launch(mode, kernel, precision, tgt_pos, tgt_gamma, n_targets,
+                                    src_pos, src_gamma, src_sigma, n_sources, out_a, out_b,
+                                    scratch, scratch_bytes, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+/*
+ * fluxvortex_gb300.h -- C ABI of the GB300 (sm_103a) vortex-induction library.
+ *
+ * Conventions
+ *   - Every entry returns an int status: FVX_OK (0) or an FVX_ERR_* code; the
+ *     message of the last failure on the calling thread is fvx_last_error().
+ *   - "Device" entries take device pointers and a cudaStream_t (passed as
+ *     void*, NULL = legacy default stream); they are stream-ordered and return
+ *     without synchronising.  "Host" entries (fvx_host_*) take host pointers,
+ *     copy in, run, copy out and synchronise, like the NumPy functions they
+ *     replace.
+ *   - Point/vector arrays are (n, 3) float64, C-contiguous (AoS), exactly as
+ *     the reference passes NumPy arrays; scalar-per-element arrays are (n,).
+ *   - Device pointers should be 16-byte aligned (cudaMalloc / torch
+ *     allocations are); unaligned inputs are accepted but staged without TMA.
+ *
+ * Reference interfaces replaced (paths inside the FLUXVortex project):
+ *   - src/fluxvortex/warp_kernels.py:251-382, the five PteraSoftware
+ *     `_aerodynamics_functions` Biot-Savart functions swapped in by
+ *     src/fluxvortex/warp_patch.py:43-58;
+ *   - src/fluxvortex/kernel.py:69-190, velocity_from_particles and
+ *     jacobian_from_particles (and the unused Warp ports of them,
+ *     src/fluxvortex/warp_vpm.py:20-173);
+ *   - src/fluxvortex/particles.py:85-246, VortexParticleField.advect_rk3 and
+ *     _relax_pedrizzetti.
+ */
+#ifndef FLUXVORTEX_GB300_H
+#define FLUXVORTEX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define FVX_OK 0
+#define FVX_ERR_ARG 1        /* bad shape, pointer, enum or size */
+#define FVX_ERR_CUDA 2       /* CUDA runtime error (message has details) */
+#define FVX_ERR_CAPACITY 3   /* a fixed capacity would be exceeded */
+#define FVX_ERR_TIMEOUT 4    /* a bounded device wait ran out */
+#define FVX_ERR_SCRATCH 5    /* scratch buffer missing or too small */
+
+/* ---- enums --------------------------------------------------------------- */
+/* Leg sets of a ring given by corners BR, FR, FL, BL:
+ *   RING       BR->FR, FR->FL, FL->BL, BL->BR   (warp_kernels.py:268-273)
+ *   CHORDWISE  BR->FR, FL->BL                   (warp_kernels.py:296-299)
+ *   HORSESHOE  BR->FR, FR->FL, FL->BL           (warp_kernels.py:350-354) */
+#define FVX_LEGS_RING 0
+#define FVX_LEGS_CHORDWISE 1
+#define FVX_LEGS_HORSESHOE 2
+
+/* Regularising cores of kernel.py:10-62. */
+#define FVX_KERNEL_GAUSSIANERF 0
+#define FVX_KERNEL_WINCKELMANS 1
+
+/* Arithmetic of a particle sweep: FP64 throughout, or FP32 pair arithmetic on
+ * tile-recentred coordinates with compensated (two-sum) FP32 accumulation. */
+#define FVX_PREC_F64 0
+#define FVX_PREC_F32C 1
+
+/* What a particle sweep accumulates per target (C = -1/(4 pi), d = x_t - x_s):
+ *   VELOCITY          u (M,3)                        kernel.py:69-116
+ *   STRETCH           S = J . Gamma_t (M,3)          particles.py:148-151
+ *   VELOCITY_STRETCH  u -> out_a, S -> out_b, same state
+ *   JACOBIAN          J[t,i,j] = du_i/dx_j (M,3,3)   kernel.py:119-190
+ *   VORTICITY         omega_i = eps_ijk J_kj (M,3)   particles.py:219-225 */
+#define FVX_PAIR_VELOCITY 0
+#define FVX_PAIR_STRETCH 1
+#define FVX_PAIR_VELOCITY_STRETCH 2
+#define FVX_PAIR_JACOBIAN 3
+#define FVX_PAIR_VORTICITY 4
+
+/* ---- library ------------------------------------------------------------- */
+const char* fvx_version(void);
+const char* fvx_last_error(void);
+/* Reads and clears the device status word (bit 1 = a bounded wait timed out,
+ * 2 = non-finite value guarded, 4 = device capacity hit); synchronises
+ * `stream`. */
+int fvx_status_read_and_clear(unsigned* bits, void* stream);
+
+/* ---- line-vortex segments (ring / chordwise / horseshoe) --------------------
+ * Replaces warp_kernels.py:251-302 and :335-357 (collapsed) and :305-332,
+ * :360-382 (expanded).  ages may be NULL (zero ages, as the horseshoe
+ * wrappers force, warp_kernels.py:348,373).  singularity_counts, if not NULL,
+ * is a device int64[4] incremented per (point, leg) pair skipped by the tests
+ * of warp_kernels.py:52 (zero-length leg), :72 (point at leg start), :74
+ * (point at leg end) and :81 (point on the leg's line).  Empty inputs
+ * (n_points == 0 or n_vortices == 0) write zeros (warp_kernels.py:193-194). */
+size_t fvx_segments_collapsed_scratch_bytes(int64_t n_points, int64_t n_vortices, int leg_set);
+int fvx_segments_collapsed(const double* points, int64_t n_points, const double* br,
+                           const double* fr, const double* fl, const double* bl,
+                           const double* strengths, const double* r_c0s, const double* ages,
+                           double nu, int64_t n_vortices, int leg_set, double* out /*(N,3)*/,
+                           int64_t* singularity_counts, void* scratch, size_t scratch_bytes,
+                           void* stream);
+int fvx_segments_expanded(const double* points, int64_t n_points, const double* br,
+                          const double* fr, const double* fl, const double* bl,
+                          const double* strengths, const double* r_c0s, const double* ages,
+                          double nu, int64_t n_vortices, int leg_set, double* out /*(N,M,3)*/,
+                          int64_t* singularity_counts, void* stream);
+
+/* Host-pointer forms: same arguments with host arrays; output written to the
+ * caller's host buffer; singularity_counts (host int64[4], may be NULL) is
+ * incremented.  Synchronous, like the NumPy functions. */
+typedef struct fvx_context fvx_context;
+int fvx_context_create(int device, fvx_context** ctx);
+void fvx_context_destroy(fvx_context* ctx);
+int fvx_host_segments_collapsed(fvx_context* ctx, const double* points, int64_t n_points,
+                                const double* br, const double* fr, const double* fl,
+                                const double* bl, const double* strengths, const double* r_c0s,
+                                const double* ages, double nu, int64_t n_vortices, int leg_set,
+                                double* out, int64_t* singularity_counts);
+int fvx_host_segments_expanded(fvx_context* ctx, const double* points, int64_t n_points,
+                               const double* br, const double* fr, const double* fl,
+                               const double* bl, const double* strengths, const double* r_c0s,
+                               const double* ages, double nu, int64_t n_vortices, int leg_set,
+                               double* out, int64_t* singularity_counts);
+
+/* ---- vortex particles -------------------------------------------------------
+ * One all-pairs sweep of n_sources particles (pos (N,3), alpha = vector
+ * strength (N,3), sigma (N,)) over n_targets points tgt_pos (M,3).  tgt_gamma
+ * (M,3) is required by STRETCH and VELOCITY_STRETCH only.  Outputs per the
+ * FVX_PAIR_* table above; out_b is used by VELOCITY_STRETCH only.  The self
+ * pair (d = 0) follows kernel.py's r -> 1e-12 clamp limit; the Gaussian-erf
+ * core is evaluated without the cancellation of kernel.py:16-18 (series below
+ * r/sigma = 0.5). */
+size_t fvx_particle_pairs_scratch_bytes(int mode, int precision, int64_t n_targets,
+                                        int64_t n_sources);
+int fvx_particle_pairs(int mode, int kernel, int precision, const double* tgt_pos,
+                       const double* tgt_gamma, int64_t n_targets, const double* src_pos,
+                       const double* src_gamma, const double* src_sigma, int64_t n_sources,
+                       double* out_a, double* out_b, void* scratch, size_t scratch_bytes,
+                       void* stream);
+int fvx_host_particle_pairs(fvx_context* ctx, int mode, int kernel, int precision,
+                            const double* tgt_pos, const double* tgt_gamma, int64_t n_targets,
+                            const double* src_pos, const double* src_gamma,
+                            const double* src_sigma, int64_t n_sources, double* out_a,
+                            double* out_b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLUXVORTEX_GB300_H */

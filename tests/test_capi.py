@@ -1,0 +1,60 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every entry point
+that include/*.h declares.  No compute calls (CPU only)."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+from fluxvortex_gb300 import _capi, build
+from tests.conftest import ROOT
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\b(fvx_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+def test_library_builds_and_loads():
+    path = build.build()
+    assert os.path.exists(path)
+    lib = _capi.load()
+    assert b"sm_103a" in lib.fvx_version()
+
+
+def test_every_declared_symbol_is_exported():
+    lib = ctypes.CDLL(build.build())
+    declared = _declared()
+    assert len(declared) >= 10
+    missing = [n for n in sorted(declared) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_ctypes_table_covers_header():
+    declared = _declared()
+    assert set(_capi.SIGNATURES) >= declared, declared - set(_capi.SIGNATURES)
+
+
+def test_argument_errors_are_reported_without_device_work():
+    lib = _capi.load()
+    # unknown leg set: rejected before any CUDA call
+    st = lib.fvx_segments_collapsed(None, 0, None, None, None, None, None, None, None, 0.0, 0,
+                                    7, None, None, None, 0, None)
+    assert st == _capi.FVX_ERR_ARG
+    assert b"leg set" in lib.fvx_last_error()
+    st = lib.fvx_particle_pairs(9, 0, 0, None, None, 1, None, None, None, 1, None, None, None,
+                                0, None)
+    assert st == _capi.FVX_ERR_ARG
+    with pytest.raises(_capi.FvxError):
+        _capi.check(st)
+
+
+def test_scratch_query_is_host_only():
+    lib = _capi.load()
+    assert lib.fvx_segments_collapsed_scratch_bytes(0, 10, 0) == 0
+    assert lib.fvx_particle_pairs_scratch_bytes(0, 0, 0, 10) == 0
