@@ -30,6 +30,7 @@ PAIR_VELOCITY, PAIR_STRETCH, PAIR_VELOCITY_STRETCH, PAIR_JACOBIAN, PAIR_VORTICIT
 SIGNATURES = {
     "fvx_version": (ctypes.c_char_p, []),
     "fvx_last_error": (ctypes.c_char_p, []),
+    "fvx_launch_count": (ctypes.c_ulonglong, []),
     "fvx_status_read_and_clear": (I32, [P, P]),
     "fvx_segments_collapsed_scratch_bytes": (SZ, [I64, I64, I32]),
     "fvx_segments_collapsed": (I32, [P, I64, P, P, P, P, P, P, P, D, I64, I32, P, P, P, SZ, P]),
@@ -41,6 +42,11 @@ SIGNATURES = {
     "fvx_particle_pairs_scratch_bytes": (SZ, [I32, I32, I64, I64]),
     "fvx_particle_pairs": (I32, [I32, I32, I32, P, P, I64, P, P, P, I64, P, P, P, SZ, P]),
     "fvx_host_particle_pairs": (I32, [P, I32, I32, I32, P, P, I64, P, P, P, I64, P, P]),
+    "fvx_vpm_stage_position": (I32, [I64, D, D, D, P, P, P, P, P, P]),
+    "fvx_vpm_stage_strength": (I32, [I64, D, D, D, D, P, P, P, P, P, P]),
+    "fvx_vpm_finalize": (I32, [I64, D, P, P, P, P]),
+    "fvx_vpm_relax": (I32, [I64, D, P, P, P]),
+    "fvx_probe_fp32_fma": (I32, [I32, I32, P, P]),
 }
 
 _lock = threading.Lock()

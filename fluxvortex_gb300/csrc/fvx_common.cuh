@@ -16,6 +16,9 @@ int device_sm_count();
 // Thread-local error message of the last failing C-ABI call.
 void set_last_error(const char* fmt, ...);
 
+// Counts kernel launches issued by the library (all threads).
+void note_launch();
+
 // Device status word: kernels OR bits in here instead of trapping.  The host
 // reads and clears it with fvx_status_read_and_clear().  Without relocatable
 // device code every translation unit has its own copy (internal linkage);
@@ -155,6 +158,8 @@ __device__ __forceinline__ void plain_copy8(void* dst, const void* src, uint32_t
     }                                                                             \
   } while (0)
 
+// Follows every kernel launch of the library: checks it and counts it (the
+// count is what fvx_launch_count() reports).
 #define FVX_LAUNCH_CHECK()                                                       \
   do {                                                                           \
     cudaError_t _e = cudaGetLastError();                                         \
@@ -163,6 +168,7 @@ __device__ __forceinline__ void plain_copy8(void* dst, const void* src, uint32_t
                             cudaGetErrorString(_e), __FILE__, __LINE__);         \
       return FVX_ERR_CUDA;                                                       \
     }                                                                            \
+    ::fvx::note_launch();                                                        \
   } while (0)
 
 #define FVX_ARG_CHECK(cond, ...)                 \

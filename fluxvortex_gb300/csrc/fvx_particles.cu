@@ -17,8 +17,8 @@
 //   Taylor series of g(r)/r^3 (the reference's erf - c r exp form cancels
 //   there and is pure rounding noise at its r = 1e-12 self-pair clamp).
 //
-// Layout and tiling: a CTA owns 128 (FP64) or 256 (FP32, two per thread)
-// targets held in registers.  Source tiles of 128 particles (AoS pos, alpha,
+// Layout and tiling: a CTA owns 128 (FP64) or 256-512 (FP32, two or four per
+// thread) targets held in registers.  Source tiles of 128 particles (AoS pos, alpha,
 // sigma exactly as the caller stores them) are staged by 1-D TMA bulk copies
 // (cp.async.bulk) into a double-buffered raw area, then converted by all
 // threads into a compute tile (alpha pre-scaled by C, sigma^2 and the core's
@@ -237,11 +237,22 @@ struct RawSrc {
   double sigma[kSrcTile];
 };
 
+// Compute tile: two 4-vectors per source so that a thread fetches a source
+// with two 128-bit shared loads (FP32) and reuses it for all its targets.
+template <typename T>
+struct alignas(4 * sizeof(T)) Vec4 {
+  T x, y, z, w;
+};
 template <typename T>
 struct SrcTile {
-  T x[kSrcTile], y[kSrcTile], z[kSrcTile];
-  T ax[kSrcTile], ay[kSrcTile], az[kSrcTile];
-  T s2[kSrcTile], k2[kSrcTile];
+  Vec4<T> p[kSrcTile];  // x, y, z, sigma^2
+  Vec4<T> a[kSrcTile];  // C*alpha_x, C*alpha_y, C*alpha_z, k2
+};
+
+// Targets per thread: more register blocking for the 3-component modes.
+template <int MODE, bool F32>
+struct Blocking {
+  static constexpr int tpt = !F32 ? 1 : (ModeInfo<MODE>::ncomp <= 3 ? 4 : 2);
 };
 
 struct PairArgs {
@@ -290,7 +301,7 @@ __device__ __forceinline__ void two_sum_fold(T& hi, T& lo, T p) {
 template <int MODE, int KERNEL, bool F32>
 __global__ void __launch_bounds__(kThreads) pairs_kernel(PairArgs A) {
   using T = typename std::conditional<F32, float, double>::type;
-  constexpr int TPT = F32 ? 2 : 1;  // targets per thread
+  constexpr int TPT = Blocking<MODE, F32>::tpt;  // targets per thread
   constexpr int NC = ModeInfo<MODE>::ncomp;
   constexpr bool NEED_FPR = ModeInfo<MODE>::need_fpr;
   constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
@@ -373,14 +384,17 @@ __global__ void __launch_bounds__(kThreads) pairs_kernel(PairArgs A) {
     __syncthreads();
     for (int k = threadIdx.x; k < n; k += kThreads) {
       const double sg = raw[buf].sigma[k];
-      tile.x[k] = static_cast<T>(raw[buf].pos[3 * k + 0] - ox);
-      tile.y[k] = static_cast<T>(raw[buf].pos[3 * k + 1] - oy);
-      tile.z[k] = static_cast<T>(raw[buf].pos[3 * k + 2] - oz);
-      tile.ax[k] = static_cast<T>(kC * raw[buf].alpha[3 * k + 0]);
-      tile.ay[k] = static_cast<T>(kC * raw[buf].alpha[3 * k + 1]);
-      tile.az[k] = static_cast<T>(kC * raw[buf].alpha[3 * k + 2]);
-      tile.s2[k] = static_cast<T>(sg * sg);
-      tile.k2[k] = static_cast<T>(KERNEL == FVX_KERNEL_WINCKELMANS ? 2.5 * sg * sg : 1.0 / sg);
+      Vec4<T> pv, av;
+      pv.x = static_cast<T>(raw[buf].pos[3 * k + 0] - ox);
+      pv.y = static_cast<T>(raw[buf].pos[3 * k + 1] - oy);
+      pv.z = static_cast<T>(raw[buf].pos[3 * k + 2] - oz);
+      pv.w = static_cast<T>(sg * sg);
+      av.x = static_cast<T>(kC * raw[buf].alpha[3 * k + 0]);
+      av.y = static_cast<T>(kC * raw[buf].alpha[3 * k + 1]);
+      av.z = static_cast<T>(kC * raw[buf].alpha[3 * k + 2]);
+      av.w = static_cast<T>(KERNEL == FVX_KERNEL_WINCKELMANS ? 2.5 * sg * sg : 1.0 / sg);
+      tile.p[k] = pv;
+      tile.a[k] = av;
     }
     __syncthreads();
     T part[TPT][NC];
@@ -390,9 +404,10 @@ __global__ void __launch_bounds__(kThreads) pairs_kernel(PairArgs A) {
       for (int c = 0; c < NC; ++c) part[j][c] = T(0);
 #pragma unroll 2
     for (int k = 0; k < n; ++k) {
-      const T sx = tile.x[k], sy = tile.y[k], sz = tile.z[k];
-      const T ax = tile.ax[k], ay = tile.ay[k], az = tile.az[k];
-      const T s2 = tile.s2[k], k2 = tile.k2[k];
+      const Vec4<T> pv = tile.p[k];
+      const Vec4<T> av = tile.a[k];
+      const T sx = pv.x, sy = pv.y, sz = pv.z, s2 = pv.w;
+      const T ax = av.x, ay = av.y, az = av.z, k2 = av.w;
 #pragma unroll
       for (int j = 0; j < TPT; ++j) {
         const T dx = tx[j] - sx, dy = ty[j] - sy, dz = tz[j] - sz;
@@ -476,8 +491,13 @@ int mode_ncomp(int mode) {
 
 int mode_na(int mode) { return mode == FVX_PAIR_VELOCITY_STRETCH ? 3 : mode_ncomp(mode); }
 
-int pair_splits(int precision, int64_t n_tgt, int64_t n_src, int64_t* chunk) {
-  const int per_cta = kThreads * (precision == FVX_PREC_F32C ? 2 : 1);
+int targets_per_cta(int mode, int precision) {
+  if (precision != FVX_PREC_F32C) return kThreads;
+  return kThreads * (mode_ncomp(mode) <= 3 ? 4 : 2);
+}
+
+int pair_splits(int mode, int precision, int64_t n_tgt, int64_t n_src, int64_t* chunk) {
+  const int per_cta = targets_per_cta(mode, precision);
   const int64_t gx = (n_tgt + per_cta - 1) / per_cta;
   const int64_t want = 2LL * device_sm_count();
   int64_t s = gx >= want ? 1 : (want + gx - 1) / gx;
@@ -527,7 +547,7 @@ size_t particle_pairs_scratch(int mode, int precision, int64_t n_tgt, int64_t n_
   const int nc = mode_ncomp(mode);
   if (nc < 0 || n_tgt <= 0 || n_src <= 0) return 0;
   int64_t chunk = 0;
-  const int s = pair_splits(precision, n_tgt, n_src, &chunk);
+  const int s = pair_splits(mode, precision, n_tgt, n_src, &chunk);
   return s > 1 ? sizeof(double) * static_cast<size_t>(nc) * n_tgt * s : 0;
 }
 
@@ -556,7 +576,7 @@ int particle_pairs_launch(int mode, int kernel, int precision, const double* tgt
   }
   FVX_ARG_CHECK(pos && alpha && sigma, "null source array");
   int64_t chunk = 0;
-  const int splits = pair_splits(precision, n_tgt, n_src, &chunk);
+  const int splits = pair_splits(mode, precision, n_tgt, n_src, &chunk);
   const size_t need = splits > 1 ? sizeof(double) * static_cast<size_t>(nc) * n_tgt * splits : 0;
   if (need > 0 && (scratch == nullptr || scratch_bytes < need)) {
     set_last_error("particle_pairs needs %zu scratch bytes, got %zu", need, scratch_bytes);
@@ -575,7 +595,7 @@ int particle_pairs_launch(int mode, int kernel, int precision, const double* tgt
   A.out_b = out_b;
   A.partial = static_cast<double*>(scratch);
   A.use_tma = aligned16(pos) && aligned16(alpha) && aligned16(sigma);
-  const int per_cta = kThreads * (precision == FVX_PREC_F32C ? 2 : 1);
+  const int per_cta = targets_per_cta(mode, precision);
   const int64_t gx = (n_tgt + per_cta - 1) / per_cta;
   FVX_ARG_CHECK(gx < (1LL << 31), "too many targets");
   dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(splits));

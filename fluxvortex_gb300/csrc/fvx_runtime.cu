@@ -8,6 +8,7 @@
 // inputs into one pinned staging block, issues a single host-to-device copy,
 // runs the kernels, and issues a single device-to-host copy, on a stream and
 // a workspace that persist for the life of the context.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -26,6 +27,11 @@ std::vector<StatusReader>& status_readers() {
 }  // namespace
 
 void register_status_reader(StatusReader fn) { status_readers().push_back(fn); }
+
+namespace {
+std::atomic<unsigned long long> g_launches{0};
+}
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 namespace {
 thread_local char t_err[512] = "";
@@ -213,6 +219,8 @@ extern "C" {
 const char* fvx_version(void) { return "fluxvortex_gb300 0.1.0 (sm_103a)"; }
 
 const char* fvx_last_error(void) { return fvx::t_err; }
+
+unsigned long long fvx_launch_count(void) { return fvx::g_launches.load(); }
 
 int fvx_status_read_and_clear(unsigned* bits, void* stream) {
   FVX_ARG_CHECK(bits != nullptr, "null bits");

@@ -1,0 +1,180 @@
+"""Device-resident VortexParticleField (mirror of src/fluxvortex/particles.py).
+
+Same public surface as the reference class (particles.py:15-246):
+``add_particle``, ``add_particles_batch``, ``positions``/``gammas``/
+``sigmas``, ``induce_velocity_at``, ``advect_rk3`` and the Pedrizzetti
+relaxation run after every step.  The particle store lives in HBM as
+capacity-sized FP64 AoS tensors (pos, gamma, sigma, age, RK3 registers);
+every step is a fixed sequence of stream-ordered launches of the C ABI:
+
+  per RK3 stage: velocity sweep -> stage_position -> [stretch sweep ->
+  stage_strength];  then finalize (NaN/Inf guard, age) and, if rlxf > 0, a
+  vorticity sweep with the Gaussian-erf core (as particles.py:219 always
+  uses) -> relax.
+
+``precision="f32c"`` runs the sweeps in FP32 with compensated accumulation;
+positions, strengths and the time integration stay FP64.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _capi
+
+RK3_COEFFS = ((0.0, 1.0 / 3.0), (-5.0 / 9.0, 15.0 / 16.0), (-153.0 / 128.0, 8.0 / 15.0))
+
+
+class VortexParticleField:
+    """Structure of FP64 device arrays holding up to ``max_particles`` particles."""
+
+    def __init__(self, max_particles=50000, nu=0.0, rlxf=0.3, kernel="gaussianerf",
+                 precision="f64", device="cuda", relax_kernel="gaussianerf"):
+        self.max_particles = int(max_particles)
+        self.nu = float(nu)
+        self.rlxf = float(rlxf)
+        self.kernel = kernel
+        self.relax_kernel = relax_kernel
+        self.precision = precision
+        self.device = torch.device(device)
+        cap = self.max_particles
+        z3 = lambda: torch.zeros((cap, 3), dtype=torch.float64, device=self.device)  # noqa: E731
+        z1 = lambda: torch.zeros(cap, dtype=torch.float64, device=self.device)  # noqa: E731
+        self._pos, self._gamma, self._sigma, self._age = z3(), z3(), z1(), z1()
+        self._rk_X, self._rk_G, self._rk_s = z3(), z3(), z1()
+        self._u, self._S, self._w = z3(), z3(), z3()
+        self._scratch = torch.empty(1, dtype=torch.uint8, device=self.device)
+        self.np = 0
+        self._lib = _capi.load()
+        # Optional profiling hook: when a list, every sweep appends
+        # (mode, kernel, n_targets, n_sources, start_event, end_event).
+        self.sweep_events = None
+
+    # ---- particle management (particles.py:35-66) ----------------------------
+    def add_particle(self, X, Gamma, sigma):
+        self.add_particles_batch(np.asarray(X, dtype=np.float64).reshape(1, 3),
+                                 np.asarray(Gamma, dtype=np.float64).reshape(1, 3),
+                                 np.asarray([sigma], dtype=np.float64))
+
+    def add_particles_batch(self, positions, gammas, sigmas):
+        n = int(positions.shape[0])
+        if self.np + n > self.max_particles:
+            raise RuntimeError(
+                f"Particle field would overflow ({self.np}+{n} > {self.max_particles})")
+        sl = slice(self.np, self.np + n)
+        t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=self.device)  # noqa: E731
+        self._pos[sl] = t(positions).reshape(n, 3)
+        self._gamma[sl] = t(gammas).reshape(n, 3)
+        self._sigma[sl] = t(sigmas).reshape(n)
+        self._age[sl] = 0.0
+        self.np += n
+
+    @property
+    def positions(self):
+        return self._pos[: self.np].cpu().numpy().copy()
+
+    @property
+    def gammas(self):
+        return self._gamma[: self.np].cpu().numpy().copy()
+
+    @property
+    def sigmas(self):
+        return self._sigma[: self.np].cpu().numpy().copy()
+
+    @property
+    def ages(self):
+        return self._age[: self.np].cpu().numpy().copy()
+
+    # ---- sweeps ----------------------------------------------------------------
+    def _stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def _ensure_scratch(self, nbytes):
+        if self._scratch.numel() < nbytes:
+            self._scratch = torch.empty(int(nbytes * 5 // 4) + 256, dtype=torch.uint8,
+                                        device=self.device)
+
+    def _sweep(self, mode, tgt, tgt_gamma, n_tgt, out_a, out_b=None, kernel=None):
+        lib = self._lib
+        pid = _capi.PRECISIONS[self.precision]
+        kid = _capi.KERNELS[kernel or self.kernel]
+        n = self.np
+        nbytes = lib.fvx_particle_pairs_scratch_bytes(mode, pid, n_tgt, n)
+        self._ensure_scratch(nbytes)
+        ev = None
+        if self.sweep_events is not None:
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev[0].record()
+        _capi.check(lib.fvx_particle_pairs(
+            mode, kid, pid, tgt.data_ptr(), None if tgt_gamma is None else tgt_gamma.data_ptr(),
+            n_tgt, self._pos.data_ptr(), self._gamma.data_ptr(), self._sigma.data_ptr(), n,
+            out_a.data_ptr(), None if out_b is None else out_b.data_ptr(),
+            self._scratch.data_ptr(), self._scratch.numel(), self._stream()))
+        if ev is not None:
+            ev[1].record()
+            self.sweep_events.append((mode, kernel or self.kernel, n_tgt, n, ev[0], ev[1]))
+
+    def induce_velocity_at(self, target_points):
+        """Velocity induced by all particles at target points (particles.py:72)."""
+        is_t = isinstance(target_points, torch.Tensor)
+        if self.np == 0:
+            return torch.zeros_like(target_points) if is_t else np.zeros_like(target_points)
+        t = torch.as_tensor(target_points, dtype=torch.float64, device=self.device).contiguous()
+        M = t.shape[0]
+        u = torch.empty((M, 3), dtype=torch.float64, device=self.device)
+        self._sweep(_capi.PAIR_VELOCITY, t, None, M, u)
+        return u if is_t else u.cpu().numpy()
+
+    # ---- RK3 + rVPM (particles.py:85-199) --------------------------------------
+    def _extra_velocity(self, fn, n):
+        if fn is None:
+            return None
+        v = fn(self._pos[:n])
+        return torch.as_tensor(v, dtype=torch.float64, device=self.device).reshape(n, 3).contiguous()
+
+    def advect_rk3(self, dt, U_inf_func, bound_velocity_func=None, stretch=True, free_wake=True):
+        """Advance one time step.  ``U_inf_func`` is either a constant freestream
+        3-vector (kept on the device path) or a callable X -> (N,3) as in the
+        reference; ``bound_velocity_func`` likewise (callable or None)."""
+        n = self.np
+        if n == 0:
+            return
+        lib, st = self._lib, self._stream()
+        dt = float(dt)
+        if callable(U_inf_func):
+            u_inf_host = np.zeros(3)
+            inf_fn = U_inf_func
+        else:
+            u_inf_host = np.ascontiguousarray(U_inf_func, dtype=np.float64).reshape(3)
+            inf_fn = None
+        for a, b in RK3_COEFFS:
+            if free_wake:
+                self._sweep(_capi.PAIR_VELOCITY, self._pos, None, n, self._u)
+            extra = None
+            if inf_fn is not None or bound_velocity_func is not None:
+                eb = self._extra_velocity(bound_velocity_func, n)
+                ei = self._extra_velocity(inf_fn, n)
+                extra = eb if ei is None else (ei if eb is None else eb + ei)
+            _capi.check(lib.fvx_vpm_stage_position(
+                n, a, b, dt, u_inf_host.ctypes.data, self._u.data_ptr() if free_wake else None,
+                None if extra is None else extra.data_ptr(), self._pos.data_ptr(),
+                self._rk_X.data_ptr(), st))
+            if stretch:
+                self._sweep(_capi.PAIR_STRETCH, self._pos, self._gamma, n, self._S)
+                _capi.check(lib.fvx_vpm_stage_strength(
+                    n, a, b, dt, self.nu, self._S.data_ptr(), self._gamma.data_ptr(),
+                    self._sigma.data_ptr(), self._rk_G.data_ptr(), self._rk_s.data_ptr(), st))
+        _capi.check(lib.fvx_vpm_finalize(n, dt, self._pos.data_ptr(), self._gamma.data_ptr(),
+                                         self._age.data_ptr(), st))
+        self._relax_pedrizzetti()
+
+    def _relax_pedrizzetti(self):
+        """particles.py:202-246; the vorticity uses ``relax_kernel``
+        (Gaussian-erf, as the reference always does)."""
+        n = self.np
+        if self.rlxf <= 0 or n == 0:
+            return
+        self._sweep(_capi.PAIR_VORTICITY, self._pos, None, n, self._w, kernel=self.relax_kernel)
+        _capi.check(self._lib.fvx_vpm_relax(n, self.rlxf, self._w.data_ptr(),
+                                            self._gamma.data_ptr(), self._stream()))
+

@@ -75,6 +75,8 @@ extern "C" {
 /* ---- library ------------------------------------------------------------- */
 const char* fvx_version(void);
 const char* fvx_last_error(void);
+/* Number of kernels this library has launched in the process so far. */
+unsigned long long fvx_launch_count(void);
 /* Reads and clears the device status word (bit 1 = a bounded wait timed out,
  * 2 = non-finite value guarded, 4 = device capacity hit); synchronises
  * `stream`. */
@@ -138,6 +140,35 @@ int fvx_host_particle_pairs(fvx_context* ctx, int mode, int kernel, int precisio
                             const double* src_pos, const double* src_gamma,
                             const double* src_sigma, int64_t n_sources, double* out_a,
                             double* out_b);
+
+/* ---- vortex-particle integrator stages (particles.py:85-246) ---------------
+ * Element-wise FP64 kernels over a device AoS particle store of n particles;
+ * the caller runs the all-pairs sweeps (fvx_particle_pairs) between them.
+ * stage_position: U = (u_part + u_extra) + u_inf (u_part, u_extra may be
+ *   NULL; u_inf is a host double[3]), |U| clamped to 50, rk_x = a rk_x + dt U,
+ *   pos += b rk_x.
+ * stage_strength: rVPM update from stretch S = J . Gamma (Z = 0.2 S.G/|G|^2,
+ *   |Z| <= 10/dt), viscous core growth nu / sigma, |G|^2 <= 1e4,
+ *   sigma in [1e-6, 5].
+ * finalize: zero the strength of particles with a non-finite position or
+ *   strength (status bit 2), age += dt.
+ * relax: Pedrizzetti realignment of gamma toward omega with factor rlxf. */
+int fvx_vpm_stage_position(int64_t n, double a, double b, double dt, const double* u_inf,
+                           const double* u_part, const double* u_extra, double* pos,
+                           double* rk_x, void* stream);
+int fvx_vpm_stage_strength(int64_t n, double a, double b, double dt, double nu,
+                           const double* stretch, double* gamma, double* sigma, double* rk_g,
+                           double* rk_s, void* stream);
+int fvx_vpm_finalize(int64_t n, double dt, const double* pos, double* gamma, double* age,
+                     void* stream);
+int fvx_vpm_relax(int64_t n, double rlxf, const double* omega, double* gamma, void* stream);
+
+/* ---- diagnostics -------------------------------------------------------------
+ * Launches blocks_per_sm x SMs CTAs of 256 threads, each running `iters`
+ * rounds of 8 independent FP32 FMAs (16 flop per round per thread): the
+ * measured FP32 CUDA-core peak used as the particle sweeps' roofline.  No
+ * reference counterpart (measurement only). */
+int fvx_probe_fp32_fma(int blocks_per_sm, int iters, float* sink, void* stream);
 
 #ifdef __cplusplus
 }

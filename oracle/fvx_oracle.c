@@ -249,7 +249,7 @@ int orc_particle_velocity(int64_t n_tgt, const double *tgt, int64_t n_src,
                           const double *sig, int kernel, double *out)
 {
     const double C = -1.0 / (4.0 * ORC_PI);
-#pragma omp parallel for schedule(dynamic, 16)
+#pragma omp parallel for schedule(dynamic, 1)
     for (int64_t i = 0; i < n_tgt; ++i) {
         double u0 = 0.0, u1 = 0.0, u2 = 0.0;
         const double *t = tgt + 3 * i;
@@ -283,7 +283,7 @@ int orc_particle_jacobian(int64_t n_tgt, const double *tgt, int64_t n_src,
                           const double *sig, int kernel, double *out)
 {
     const double C = -1.0 / (4.0 * ORC_PI);
-#pragma omp parallel for schedule(dynamic, 16)
+#pragma omp parallel for schedule(dynamic, 1)
     for (int64_t i = 0; i < n_tgt; ++i) {
         double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         const double *t = tgt + 3 * i;
@@ -325,7 +325,7 @@ int orc_particle_velocity_stretch(int64_t n_tgt, const double *tgt,
                                   double *s_out)
 {
     const double C = -1.0 / (4.0 * ORC_PI);
-#pragma omp parallel for schedule(dynamic, 16)
+#pragma omp parallel for schedule(dynamic, 1)
     for (int64_t i = 0; i < n_tgt; ++i) {
         double u[3] = {0, 0, 0};
         double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
