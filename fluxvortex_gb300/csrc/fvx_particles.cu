@@ -127,6 +127,13 @@ __device__ __forceinline__ void core_f64(double r2, double s2, double k2, double
         d = fma(d, x, 2.0 * FVX_GA1);
         fpr = kSqrt2OverPi * d * is3 * inv_s * inv_s;
       }
+    } else if (x > 90.0) {
+      // rho > 9.4: 1 - erf(rho/sqrt2) and rho exp(-rho^2/2) are below 1e-18,
+      // so g = 1 (and g' ~ 0) in FP64: the core is the singular kernel.
+      const double ir = rsqrt(r2);
+      const double ir2 = ir * ir;
+      f = ir2 * ir;
+      if (NEED_FPR) fpr = -3.0 * f * ir2;
     } else {
       double r = sqrt(r2);
       double rho = r * inv_s;
@@ -174,6 +181,12 @@ __device__ __forceinline__ void core_f32(float r2, float s2, float k2, float& f,
         d = fmaf(d, x, static_cast<float>(2.0 * FVX_GA1));
         fpr = static_cast<float>(kSqrt2OverPi) * d * is3 * inv_s * inv_s;
       }
+    } else if (x > 50.0f) {
+      // rho > 7.1: g = 1 and g' ~ 0 to FP32 round-off (terms below 1e-9)
+      const float ir = rsqrtf(r2);
+      const float ir2 = ir * ir;
+      f = ir2 * ir;
+      if (NEED_FPR) fpr = -3.0f * f * ir2;
     } else {
       float ir = rsqrtf(r2);
       float r = r2 * ir;
@@ -195,22 +208,26 @@ __device__ __forceinline__ void core_f32(float r2, float s2, float k2, float& f,
 template <int MODE, typename T>
 __device__ __forceinline__ void accumulate(T* acc, T dx, T dy, T dz, T r2, T ax, T ay, T az,
                                            T f, T fpr, T gx, T gy, T gz) {
-  const T cx = dy * az - dz * ay;
-  const T cy = dz * ax - dx * az;
-  const T cz = dx * ay - dy * ax;
   if (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_VELOCITY_STRETCH) {
-    acc[0] += f * cx;
-    acc[1] += f * cy;
-    acc[2] += f * cz;
+    // u += (f d) x a
+    const T ex = f * dx, ey = f * dy, ez = f * dz;
+    acc[0] += ey * az - ez * ay;
+    acc[1] += ez * ax - ex * az;
+    acc[2] += ex * ay - ey * ax;
   }
   if (MODE == FVX_PAIR_STRETCH || MODE == FVX_PAIR_VELOCITY_STRETCH) {
+    // S += f (G x a) + w (d x a) = (f G + w d) x a,  w = fpr (d . G)
     constexpr int o = MODE == FVX_PAIR_STRETCH ? 0 : 3;
     const T w = fpr * (dx * gx + dy * gy + dz * gz);
-    acc[o + 0] += f * (gy * az - gz * ay) + w * cx;
-    acc[o + 1] += f * (gz * ax - gx * az) + w * cy;
-    acc[o + 2] += f * (gx * ay - gy * ax) + w * cz;
+    const T vx = f * gx + w * dx, vy = f * gy + w * dy, vz = f * gz + w * dz;
+    acc[o + 0] += vy * az - vz * ay;
+    acc[o + 1] += vz * ax - vx * az;
+    acc[o + 2] += vx * ay - vy * ax;
   }
   if (MODE == FVX_PAIR_JACOBIAN) {
+    const T cx = dy * az - dz * ay;
+    const T cy = dz * ax - dx * az;
+    const T cz = dx * ay - dy * ax;
     const T px = fpr * cx, py = fpr * cy, pz = fpr * cz;
     acc[0] += px * dx;
     acc[1] += px * dy + f * az;
@@ -223,11 +240,12 @@ __device__ __forceinline__ void accumulate(T* acc, T dx, T dy, T dz, T r2, T ax,
     acc[8] += pz * dz;
   }
   if (MODE == FVX_PAIR_VORTICITY) {
-    const T da = dx * ax + dy * ay + dz * az;
-    const T f2 = f + f;
-    acc[0] += fpr * (dx * da - ax * r2) - f2 * ax;
-    acc[1] += fpr * (dy * da - ay * r2) - f2 * ay;
-    acc[2] += fpr * (dz * da - az * r2) - f2 * az;
+    // omega += d (fpr (d . a)) - a (fpr r^2 + 2 f)
+    const T s1 = fpr * (dx * ax + dy * ay + dz * az);
+    const T s2 = fpr * r2 + (f + f);
+    acc[0] += dx * s1 - ax * s2;
+    acc[1] += dy * s1 - ay * s2;
+    acc[2] += dz * s1 - az * s2;
   }
 }
 
