@@ -34,6 +34,7 @@ SIGNATURES = {
     "fvx_status_read_and_clear": (I32, [P, P]),
     "fvx_segments_collapsed_scratch_bytes": (SZ, [I64, I64, I32]),
     "fvx_segments_collapsed": (I32, [P, I64, P, P, P, P, P, P, P, D, I64, I32, P, P, P, SZ, P]),
+    "fvx_segments_collapsed_noalloc": (I32, [P, I64, P, P, P, P, P, P, P, D, I64, I32, P, P, P]),
     "fvx_segments_expanded": (I32, [P, I64, P, P, P, P, P, P, P, D, I64, I32, P, P, P]),
     "fvx_context_create": (I32, [I32, P]),
     "fvx_context_destroy": (None, [P]),

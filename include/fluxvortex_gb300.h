@@ -97,6 +97,24 @@ int fvx_segments_collapsed(const double* points, int64_t n_points, const double*
                            double nu, int64_t n_vortices, int leg_set, double* out /*(N,3)*/,
                            int64_t* singularity_counts, void* scratch, size_t scratch_bytes,
                            void* stream);
+/* Scratch-free form of fvx_segments_collapsed, for callers that may not
+ * allocate device memory while they run (a host that owns the GPU memory
+ * budget and passes only input/output buffers; a fixed-rate stepping loop
+ * where an allocation's device-wide synchronisation would stall it).  Same
+ * arguments and results as fvx_segments_collapsed without the scratch pair:
+ * its partial sums live in a 1 MiB array built into the library (held on
+ * every GPU that loads it until the process exits).  Calls whose partial sums
+ * need more than 1 MiB return FVX_ERR_CAPACITY before launching anything.
+ * The first call on each device looks the array's address up
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race.  This entry
+ * point has no counterpart in the reference. */
+int fvx_segments_collapsed_noalloc(const double* points, int64_t n_points, const double* br,
+                                   const double* fr, const double* fl, const double* bl,
+                                   const double* strengths, const double* r_c0s,
+                                   const double* ages, double nu, int64_t n_vortices,
+                                   int leg_set, double* out, int64_t* singularity_counts,
+                                   void* stream);
 int fvx_segments_expanded(const double* points, int64_t n_points, const double* br,
                           const double* fr, const double* fl, const double* bl,
                           const double* strengths, const double* r_c0s, const double* ages,
