@@ -48,6 +48,16 @@ SIGNATURES = {
     "fvx_vpm_finalize": (I32, [I64, D, P, P, P, P]),
     "fvx_vpm_relax": (I32, [I64, D, P, P, P]),
     "fvx_probe_fp32_fma": (I32, [I32, I32, P, P]),
+    "fvx_uvlm_kinematics": (I32, [I64, P, D, D, D, D, D, P, P]),
+    "fvx_uvlm_lattice": (I32, [P, I32, I32, P, P, P, P, P, P, P, P, P, P, P]),
+    "fvx_uvlm_aic": (I32, [I32, I32, P, P, P, P, P, P, D, D, P, P]),
+    "fvx_uvlm_rhs": (I32, [I32, P, P, P, P, P, D, D, D, D, D, P, P]),
+    "fvx_lu_solve_batched": (I32, [I32, I32, P, P, P]),
+    "fvx_uvlm_loads": (I32, [I32, I32, P, P, P, P, P, P, P, P, P, P, D, D, D, D, D, D, D, P, P,
+                             P, P]),
+    "fvx_uvlm_wake_rings": (I32, [I32, I32, P, P, P, D, P, P, P, P, P, P, P, P]),
+    "fvx_uvlm_shed": (I32, [I32, I32, I32, P, P, P, P, P, P, D, P, P, P, P]),
+    "fvx_uvlm_convert": (I32, [I32, I32, I32, P, P, I32, D, I64, P, P, P, P, P, P]),
 }
 
 _lock = threading.Lock()

@@ -1,0 +1,599 @@
+// fvx_uvlm.cu -- panel side of the hybrid panel-particle step, FP64.
+//
+// Kernels for one step of a ring-vortex UVLM with a hybrid ring/particle
+// wake, in the order the reference's solver runs it (PteraSoftware's step,
+// overridden by tests/experiment_hybrid_panel_particle.py:114-204):
+//   kinematics      base vertex grid -> vertices at time t (heave + flapping)
+//   lattice         quarter-chord ring corners, 3/4-chord collocation points,
+//                   normals, areas, bound-leg centres/vectors, TE back edge
+//   aic             AIC[i,j] = (unit ring j at collocation i) . n_i, the
+//                   expanded ring Biot-Savart fused with the normal product
+//   rhs             -((U_inf - v_body) + V_wake) . n
+//   lu_solve        batched FP64 Gaussian elimination with partial pivoting
+//                   (one CTA per system; the AIC system is tiny and stays in L2)
+//   loads           Kutta-Joukowski on the bound legs + unsteady term, reduced
+//                   to CL and CDi in fixed order (deterministic)
+//   wake_rings      ring-wake vertex lattice -> the five-function ring layout
+//   shed            prescribed-wake convection + new trailing-edge row
+//   convert         HybridSolver._convert_old_wake_to_particles (:145-204):
+//                   rows >= N_keep -> 4 particles per ring, appended on the
+//                   device with a block-wide compaction
+// All per-step inputs are device arrays; the host only sequences launches.
+#include "fvx_common.cuh"
+#include "fvx_segment_math.cuh"
+
+namespace fvx {
+namespace {
+
+constexpr int kT = 128;
+
+__device__ __forceinline__ void load3(const double* p, int64_t i, double v[3]) {
+  v[0] = p[3 * i];
+  v[1] = p[3 * i + 1];
+  v[2] = p[3 * i + 2];
+}
+__device__ __forceinline__ void store3(double* p, int64_t i, const double v[3]) {
+  p[3 * i] = v[0];
+  p[3 * i + 1] = v[1];
+  p[3 * i + 2] = v[2];
+}
+
+struct Motion {
+  double heave_amp, flap_amp, omega, y0, t;
+};
+
+// Body-point velocity at current position p: heave rate on z, flapping about
+// the x axis through y0 mirrored per half wing.
+__device__ __forceinline__ void body_velocity(const Motion& m, const double p[3], double v[3]) {
+  const double h = m.heave_amp * sin(m.omega * m.t);
+  const double hdot = m.heave_amp * m.omega * cos(m.omega * m.t);
+  const double thdot = m.flap_amp * m.omega * cos(m.omega * m.t);
+  const double dy = p[1] - m.y0;
+  const double s = dy >= 0.0 ? 1.0 : -1.0;
+  const double Z = p[2] - h;
+  v[0] = 0.0;
+  v[1] = -s * thdot * Z;
+  v[2] = s * thdot * dy + hdot;
+}
+
+__global__ void kinematics_kernel(int64_t nv, const double* __restrict__ base, Motion m,
+                                  double* __restrict__ out) {
+  int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= nv) return;
+  double v[3];
+  load3(base, i, v);
+  if (m.flap_amp != 0.0) {
+    const double th = m.flap_amp * sin(m.omega * m.t);
+    const double dy = v[1] - m.y0;
+    const double s = dy > 0.0 ? 1.0 : (dy < 0.0 ? -1.0 : 0.0);
+    const double y = fabs(dy), z = v[2];
+    const double c = cos(th), sn = sin(th);
+    v[1] = m.y0 + s * (y * c - z * sn);
+    v[2] = y * sn + z * c;
+  }
+  if (m.heave_amp != 0.0) v[2] += m.heave_amp * sin(m.omega * m.t);
+  store3(out, i, v);
+}
+
+struct LatticeOut {
+  double *br, *fr, *fl, *bl, *colloc, *normal, *area, *leg_center, *leg_vec, *te_back;
+};
+
+// quarter-chord lattice point of vertex (i, j)
+__device__ __forceinline__ void vq(const double* v, int nc, int ns, int i, int j, double o[3]) {
+  const int w = ns + 1;
+  double a[3], b[3];
+  if (i < nc) {
+    load3(v, static_cast<int64_t>(i) * w + j, a);
+    load3(v, static_cast<int64_t>(i + 1) * w + j, b);
+    for (int c = 0; c < 3; ++c) o[c] = a[c] + 0.25 * (b[c] - a[c]);
+  } else {
+    load3(v, static_cast<int64_t>(nc) * w + j, a);
+    load3(v, static_cast<int64_t>(nc - 1) * w + j, b);
+    for (int c = 0; c < 3; ++c) o[c] = a[c] + 0.25 * (a[c] - b[c]);
+  }
+}
+
+__global__ void lattice_kernel(const double* __restrict__ v, int nc, int ns, LatticeOut o) {
+  const int P = nc * ns;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int w = ns + 1;
+  if (k <= ns && k < w) {  // trailing-edge back edge
+    double tb[3];
+    vq(v, nc, ns, nc, k, tb);
+    store3(o.te_back, k, tb);
+  }
+  if (k >= P) return;
+  const int i = k / ns, j = k % ns;
+  double fl[3], fr[3], br[3], bl[3];
+  vq(v, nc, ns, i, j, fl);
+  vq(v, nc, ns, i, j + 1, fr);
+  vq(v, nc, ns, i + 1, j + 1, br);
+  vq(v, nc, ns, i + 1, j, bl);
+  store3(o.fl, k, fl);
+  store3(o.fr, k, fr);
+  store3(o.br, k, br);
+  store3(o.bl, k, bl);
+  double a0[3], a1[3], b0[3], b1[3];  // vertices (i,j), (i,j+1), (i+1,j), (i+1,j+1)
+  load3(v, static_cast<int64_t>(i) * w + j, a0);
+  load3(v, static_cast<int64_t>(i) * w + j + 1, a1);
+  load3(v, static_cast<int64_t>(i + 1) * w + j, b0);
+  load3(v, static_cast<int64_t>(i + 1) * w + j + 1, b1);
+  double cp[3], d1[3], d2[3], lc[3], lv[3];
+  for (int c = 0; c < 3; ++c) {
+    const double vc0 = a0[c] + 0.75 * (b0[c] - a0[c]);
+    const double vc1 = a1[c] + 0.75 * (b1[c] - a1[c]);
+    cp[c] = 0.5 * (vc0 + vc1);
+    d1[c] = b1[c] - a0[c];
+    d2[c] = a1[c] - b0[c];
+    lc[c] = 0.5 * (fr[c] + fl[c]);
+    lv[c] = fl[c] - fr[c];
+  }
+  double cr[3] = {d1[1] * d2[2] - d1[2] * d2[1], d1[2] * d2[0] - d1[0] * d2[2],
+                  d1[0] * d2[1] - d1[1] * d2[0]};
+  const double nrm = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+  double n[3] = {cr[0] / nrm, cr[1] / nrm, cr[2] / nrm};
+  store3(o.colloc, k, cp);
+  store3(o.normal, k, n);
+  o.area[k] = 0.5 * nrm;
+  store3(o.leg_center, k, lc);
+  store3(o.leg_vec, k, lv);
+}
+
+// AIC[i, j] for B independent systems laid out back to back.
+__global__ void aic_kernel(int P, const double* __restrict__ colloc,
+                           const double* __restrict__ normal, const double* __restrict__ br,
+                           const double* __restrict__ fr, const double* __restrict__ fl,
+                           const double* __restrict__ bl, double rc0, double nu,
+                           double* __restrict__ aic) {
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t PP = static_cast<int64_t>(P) * P;
+  const int64_t b = blockIdx.y;
+  if (idx >= PP) return;
+  const int i = static_cast<int>(idx / P), j = static_cast<int>(idx % P);
+  const int64_t ii = b * P + i, jj = b * P + j;
+  seg::VortexRec R;
+  seg::prep_vortex<FVX_LEGS_RING>(R, br + 3 * jj, fr + 3 * jj, fl + 3 * jj, bl + 3 * jj, 1.0, rc0,
+                                  0.0, nu);
+  double vx = 0.0, vy = 0.0, vz = 0.0;
+  int cnt[4] = {0, 0, 0, 0};
+  seg::vortex_velocity<FVX_LEGS_RING>(R, colloc[3 * ii], colloc[3 * ii + 1], colloc[3 * ii + 2],
+                                      vx, vy, vz, cnt);
+  aic[b * PP + idx] = vx * normal[3 * ii] + vy * normal[3 * ii + 1] + vz * normal[3 * ii + 2];
+}
+
+// rhs_i = -((U_inf - v_body) + (v1 + v2)) . n   (v1, v2 may be null)
+__global__ void rhs_kernel(int P, const double* __restrict__ colloc,
+                           const double* __restrict__ normal, const double* __restrict__ v1,
+                           const double* __restrict__ v2, double ux, double uy, double uz,
+                           Motion m, double* __restrict__ rhs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  double p[3], vb[3], n[3];
+  load3(colloc, i, p);
+  load3(normal, i, n);
+  body_velocity(m, p, vb);
+  double w[3] = {0.0, 0.0, 0.0};
+  if (v1) load3(v1, i, w);
+  if (v2) {
+    w[0] += v2[3 * i];
+    w[1] += v2[3 * i + 1];
+    w[2] += v2[3 * i + 2];
+  }
+  const double a0 = (ux - vb[0]) + w[0], a1 = (uy - vb[1]) + w[1], a2 = (uz - vb[2]) + w[2];
+  rhs[i] = -(a0 * n[0] + a1 * n[1] + a2 * n[2]);
+}
+
+// In-place solve of A x = b for B systems (A: B x P x P row-major, b: B x P);
+// Gaussian elimination with partial pivoting (first maximum wins).  x -> b.
+__global__ void __launch_bounds__(256) lu_solve_kernel(int P, double* __restrict__ A,
+                                                       double* __restrict__ b) {
+  const int64_t PP = static_cast<int64_t>(P) * P;
+  double* a = A + blockIdx.x * PP;
+  double* x = b + static_cast<int64_t>(blockIdx.x) * P;
+  __shared__ double s_val[256];
+  __shared__ int s_idx[256];
+  __shared__ int s_piv;
+  for (int k = 0; k < P; ++k) {
+    // pivot search in column k, rows k..P-1
+    double best = -1.0;
+    int bi = P;
+    for (int r = k + threadIdx.x; r < P; r += blockDim.x) {
+      const double v = fabs(a[static_cast<int64_t>(r) * P + k]);
+      if (v > best) {
+        best = v;
+        bi = r;
+      }
+    }
+    s_val[threadIdx.x] = best;
+    s_idx[threadIdx.x] = bi;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        const double v2 = s_val[threadIdx.x + s];
+        const int i2 = s_idx[threadIdx.x + s];
+        if (v2 > s_val[threadIdx.x] || (v2 == s_val[threadIdx.x] && i2 < s_idx[threadIdx.x])) {
+          s_val[threadIdx.x] = v2;
+          s_idx[threadIdx.x] = i2;
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      s_piv = s_idx[0];
+      if (!(s_val[0] > 0.0)) flag_status(kStatusNonFinite);
+    }
+    __syncthreads();
+    const int piv = s_piv;
+    if (piv != k && piv < P) {
+      for (int c = threadIdx.x; c < P; c += blockDim.x) {
+        const double t = a[static_cast<int64_t>(k) * P + c];
+        a[static_cast<int64_t>(k) * P + c] = a[static_cast<int64_t>(piv) * P + c];
+        a[static_cast<int64_t>(piv) * P + c] = t;
+      }
+      if (threadIdx.x == 0) {
+        const double t = x[k];
+        x[k] = x[piv];
+        x[piv] = t;
+      }
+    }
+    __syncthreads();
+    const double akk = a[static_cast<int64_t>(k) * P + k];
+    // eliminate below: one warp per row, lanes over columns
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = k + 1 + warp; r < P; r += nw) {
+      const double l = a[static_cast<int64_t>(r) * P + k] / akk;
+      for (int c = k + 1 + lane; c < P; c += 32)
+        a[static_cast<int64_t>(r) * P + c] -= l * a[static_cast<int64_t>(k) * P + c];
+      if (lane == 0) x[r] -= l * x[k];
+    }
+    __syncthreads();
+  }
+  // back substitution, one row at a time with a block reduction
+  for (int k = P - 1; k >= 0; --k) {
+    double s = 0.0;
+    for (int c = k + 1 + threadIdx.x; c < P; c += blockDim.x)
+      s += a[static_cast<int64_t>(k) * P + c] * x[c];
+    s_val[threadIdx.x] = s;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+      if (threadIdx.x < st) s_val[threadIdx.x] += s_val[threadIdx.x + st];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) x[k] = (x[k] - s_val[0]) / a[static_cast<int64_t>(k) * P + k];
+    __syncthreads();
+  }
+}
+
+struct LoadsArgs {
+  int nc, ns;
+  const double* gamma;
+  const double* gamma_prev;  // null: no unsteady term (first step)
+  const double* leg_center;
+  const double* leg_vec;
+  const double* area;
+  const double* normal;
+  const double* v1;  // induced velocities at the leg centres (summed, any may be null)
+  const double* v2;
+  const double* v3;
+  double ux, uy, uz, rho, dt;
+  Motion m;
+  double* cl_out;   // cl_out[0], cdi_out[0] written
+  double* cdi_out;
+  double* force;    // optional (P,3) per-panel force
+};
+
+__global__ void __launch_bounds__(256) loads_kernel(LoadsArgs a) {
+  const int P = a.nc * a.ns;
+  double F[3] = {0.0, 0.0, 0.0}, S = 0.0;
+  for (int k = threadIdx.x; k < P; k += blockDim.x) {
+    const int i = k / a.ns;
+    const double g = a.gamma[k];
+    const double geff = i > 0 ? g - a.gamma[k - a.ns] : g;
+    double p[3], vb[3], l[3], n[3];
+    load3(a.leg_center, k, p);
+    load3(a.leg_vec, k, l);
+    load3(a.normal, k, n);
+    body_velocity(a.m, p, vb);
+    double w[3] = {0.0, 0.0, 0.0};
+    if (a.v1) load3(a.v1, k, w);
+    if (a.v2) {
+      w[0] += a.v2[3 * k];
+      w[1] += a.v2[3 * k + 1];
+      w[2] += a.v2[3 * k + 2];
+    }
+    if (a.v3) {
+      w[0] += a.v3[3 * k];
+      w[1] += a.v3[3 * k + 1];
+      w[2] += a.v3[3 * k + 2];
+    }
+    const double V0 = (a.ux - vb[0]) + w[0], V1 = (a.uy - vb[1]) + w[1],
+                 V2 = (a.uz - vb[2]) + w[2];
+    const double cx = V1 * l[2] - V2 * l[1], cy = V2 * l[0] - V0 * l[2],
+                 cz = V0 * l[1] - V1 * l[0];
+    const double dg = a.gamma_prev ? (g - a.gamma_prev[k]) / a.dt : 0.0;
+    const double ua = a.rho * dg * a.area[k];
+    const double f0 = a.rho * geff * cx - ua * n[0];
+    const double f1 = a.rho * geff * cy - ua * n[1];
+    const double f2 = a.rho * geff * cz - ua * n[2];
+    if (a.force) {
+      a.force[3 * k] = f0;
+      a.force[3 * k + 1] = f1;
+      a.force[3 * k + 2] = f2;
+    }
+    F[0] += f0;
+    F[1] += f1;
+    F[2] += f2;
+    S += a.area[k];
+  }
+  __shared__ double red[4][256];
+  red[0][threadIdx.x] = F[0];
+  red[1][threadIdx.x] = F[1];
+  red[2][threadIdx.x] = F[2];
+  red[3][threadIdx.x] = S;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int c = 0; c < 4; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double V = sqrt(a.ux * a.ux + a.uy * a.uy + a.uz * a.uz);
+    const double eD[3] = {a.ux / V, a.uy / V, a.uz / V};
+    const double eL[3] = {-eD[2], 0.0, eD[0]};
+    const double qS = 0.5 * a.rho * V * V * red[3][0];
+    a.cl_out[0] = (red[0][0] * eL[0] + red[1][0] * eL[1] + red[2][0] * eL[2]) / qS;
+    a.cdi_out[0] = (red[0][0] * eD[0] + red[1][0] * eD[1] + red[2][0] * eD[2]) / qS;
+  }
+}
+
+// Ring wake (R rows x ns rings) from the vertex lattice W ((R+1) x (ns+1)).
+__global__ void wake_rings_kernel(int R, int ns, const double* __restrict__ W,
+                                  const double* __restrict__ gam, const double* __restrict__ age,
+                                  double rc0, double* br, double* fr, double* fl, double* bl,
+                                  double* strength, double* rc0s, double* ages) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= R * ns) return;
+  const int r = k / ns, j = k % ns, w = ns + 1;
+  double p[3];
+  load3(W, static_cast<int64_t>(r) * w + j, p);
+  store3(fl, k, p);
+  load3(W, static_cast<int64_t>(r) * w + j + 1, p);
+  store3(fr, k, p);
+  load3(W, static_cast<int64_t>(r + 1) * w + j + 1, p);
+  store3(br, k, p);
+  load3(W, static_cast<int64_t>(r + 1) * w + j, p);
+  store3(bl, k, p);
+  strength[k] = gam[k];
+  rc0s[k] = rc0;
+  ages[k] = age[r];
+}
+
+// New wake from the old one: row 0 = trailing edge of the next step, rows
+// m >= 1 = old rows convected by U_inf dt; strengths shift by one row and take
+// the trailing-edge ring strengths; ages shift and grow by dt.
+__global__ void shed_kernel(int R_old, int nc, int ns, const double* __restrict__ W_old,
+                            const double* __restrict__ gam_old,
+                            const double* __restrict__ age_old,
+                            const double* __restrict__ te_next, const double* __restrict__ gamma,
+                            double dx, double dy, double dz, double dt, double* __restrict__ W_new,
+                            double* __restrict__ gam_new, double* __restrict__ age_new) {
+  const int w = ns + 1;
+  const int nverts = (R_old + 2) * w;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nverts) {
+    const int r = k / w, j = k % w;
+    double p[3];
+    if (r == 0) {
+      load3(te_next, j, p);
+    } else {
+      load3(W_old, static_cast<int64_t>(r - 1) * w + j, p);
+      p[0] += dx;
+      p[1] += dy;
+      p[2] += dz;
+    }
+    store3(W_new, k, p);
+  }
+  if (k < (R_old + 1) * ns) {
+    const int r = k / ns, j = k % ns;
+    gam_new[k] = r == 0 ? gamma[(nc - 1) * ns + j] : gam_old[(r - 1) * ns + j];
+  }
+  if (k < R_old + 1) age_new[k] = k == 0 ? 0.0 : age_old[k - 1] + dt;
+}
+
+// Rows r >= n_keep of the wake lattice -> particles appended at *count.
+__global__ void __launch_bounds__(256) convert_kernel(int R, int n_keep, int ns,
+                                                      const double* __restrict__ W,
+                                                      const double* __restrict__ gam,
+                                                      int sigma_rule, double sigma_vdt,
+                                                      int64_t capacity, int64_t* count,
+                                                      double* pos, double* alpha, double* sigma,
+                                                      double* age) {
+  __shared__ int s_scan[256];
+  __shared__ int64_t s_base;
+  if (threadIdx.x == 0) s_base = *count;
+  __syncthreads();
+  const int nrings = (R - n_keep) * ns;
+  const int w = ns + 1;
+  for (int c0 = 0; c0 < nrings; c0 += blockDim.x) {
+    const int k = c0 + threadIdx.x;
+    double q[4][3], al[4][3];
+    int emit = 0, mask = 0;
+    double sg = sigma_vdt;
+    if (k < nrings) {
+      const int r = n_keep + k / ns, j = k % ns;
+      const double g = gam[r * ns + j];
+      double fl[3], fr[3], bl[3], br[3];
+      load3(W, static_cast<int64_t>(r) * w + j, fl);
+      load3(W, static_cast<int64_t>(r) * w + j + 1, fr);
+      load3(W, static_cast<int64_t>(r + 1) * w + j, bl);
+      load3(W, static_cast<int64_t>(r + 1) * w + j + 1, br);
+      const double* A[4] = {fr, fl, bl, br};  // legs front, left, back, right
+      const double* B[4] = {fl, bl, br, fr};
+      if (sigma_rule == 1) {
+        double e = 0.0;
+        for (int l = 0; l < 4; ++l) {
+          const double d0 = A[l][0] - B[l][0], d1 = A[l][1] - B[l][1], d2 = A[l][2] - B[l][2];
+          e += sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        }
+        sg = 1.3 * 0.25 * e;
+      }
+      if (!(fabs(g) < 1e-15)) {
+        for (int l = 0; l < 4; ++l) {
+          double s2 = 0.0;
+          for (int c = 0; c < 3; ++c) {
+            al[l][c] = g * (B[l][c] - A[l][c]);
+            q[l][c] = 0.5 * (A[l][c] + B[l][c]);
+            s2 += al[l][c] * al[l][c];
+          }
+          if (s2 > 1e-30) {
+            mask |= 1 << l;
+            ++emit;
+          }
+        }
+      }
+    }
+    // block-wide exclusive scan of emit (ring-major order)
+    s_scan[threadIdx.x] = emit;
+    __syncthreads();
+    for (int off = 1; off < blockDim.x; off <<= 1) {
+      int v = threadIdx.x >= off ? s_scan[threadIdx.x - off] : 0;
+      __syncthreads();
+      s_scan[threadIdx.x] += v;
+      __syncthreads();
+    }
+    const int incl = s_scan[threadIdx.x];
+    const int total = s_scan[blockDim.x - 1];
+    int64_t o = s_base + incl - emit;
+    for (int l = 0; l < 4; ++l) {
+      if (!((mask >> l) & 1)) continue;
+      if (o < capacity) {
+        store3(pos, o, q[l]);
+        store3(alpha, o, al[l]);
+        sigma[o] = sg;
+        age[o] = 0.0;
+      } else {
+        flag_status(kStatusCapacity);
+      }
+      ++o;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_base += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *count = s_base < capacity ? s_base : capacity;
+}
+
+unsigned nblk(int64_t n, int t = kT) { return static_cast<unsigned>((n + t - 1) / t); }
+
+}  // namespace
+}  // namespace fvx
+
+using fvx::Motion;
+
+extern "C" {
+
+int fvx_uvlm_kinematics(int64_t n_verts, const double* base, double heave_amp, double flap_amp,
+                        double omega, double y0, double t, double* out, void* stream) {
+  FVX_ARG_CHECK(n_verts >= 0 && base && out, "bad kinematics arguments");
+  if (n_verts == 0) return FVX_OK;
+  Motion m{heave_amp, flap_amp, omega, y0, t};
+  fvx::kinematics_kernel<<<fvx::nblk(n_verts), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(
+      n_verts, base, m, out);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_uvlm_lattice(const double* verts, int nc, int ns, double* br, double* fr, double* fl,
+                     double* bl, double* colloc, double* normal, double* area,
+                     double* leg_center, double* leg_vec, double* te_back, void* stream) {
+  FVX_ARG_CHECK(nc >= 2 && ns >= 1 && verts, "lattice needs nc >= 2, ns >= 1");
+  fvx::LatticeOut o{br, fr, fl, bl, colloc, normal, area, leg_center, leg_vec, te_back};
+  const int n = nc * ns > ns + 1 ? nc * ns : ns + 1;
+  fvx::lattice_kernel<<<fvx::nblk(n), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(verts, nc,
+                                                                                      ns, o);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_uvlm_aic(int n_systems, int P, const double* colloc, const double* normal,
+                 const double* br, const double* fr, const double* fl, const double* bl,
+                 double rc0, double nu, double* aic, void* stream) {
+  FVX_ARG_CHECK(n_systems >= 1 && P >= 1 && n_systems <= 65535, "bad AIC sizes");
+  const int64_t PP = static_cast<int64_t>(P) * P;
+  dim3 grid(fvx::nblk(PP), n_systems);
+  fvx::aic_kernel<<<grid, fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(
+      P, colloc, normal, br, fr, fl, bl, rc0, nu, aic);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_uvlm_rhs(int P, const double* colloc, const double* normal, const double* v1,
+                 const double* v2, const double* u_inf, double heave_amp, double flap_amp,
+                 double omega, double y0, double t, double* rhs, void* stream) {
+  FVX_ARG_CHECK(P >= 1 && colloc && normal && u_inf && rhs, "bad rhs arguments");
+  Motion m{heave_amp, flap_amp, omega, y0, t};
+  fvx::rhs_kernel<<<fvx::nblk(P), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(
+      P, colloc, normal, v1, v2, u_inf[0], u_inf[1], u_inf[2], m, rhs);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_lu_solve_batched(int n_systems, int P, double* A, double* b, void* stream) {
+  FVX_ARG_CHECK(n_systems >= 1 && P >= 1 && A && b, "bad solve arguments");
+  fvx::lu_solve_kernel<<<n_systems, 256, 0, static_cast<cudaStream_t>(stream)>>>(P, A, b);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_uvlm_loads(int nc, int ns, const double* gamma, const double* gamma_prev,
+                   const double* leg_center, const double* leg_vec, const double* area,
+                   const double* normal, const double* v1, const double* v2, const double* v3,
+                   const double* u_inf, double rho, double dt, double heave_amp, double flap_amp,
+                   double omega, double y0, double t, double* cl, double* cdi, double* force,
+                   void* stream) {
+  FVX_ARG_CHECK(nc >= 1 && ns >= 1 && gamma && u_inf && cl && cdi, "bad loads arguments");
+  fvx::LoadsArgs a{nc,        ns,   gamma, gamma_prev, leg_center, leg_vec, area, normal, v1,
+                   v2,        v3,   u_inf[0], u_inf[1], u_inf[2],  rho,     dt,
+                   Motion{heave_amp, flap_amp, omega, y0, t}, cl, cdi, force};
+  fvx::loads_kernel<<<1, 256, 0, static_cast<cudaStream_t>(stream)>>>(a);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_uvlm_wake_rings(int R, int ns, const double* W, const double* gam, const double* age,
+                        double rc0, double* br, double* fr, double* fl, double* bl,
+                        double* strength, double* rc0s, double* ages, void* stream) {
+  FVX_ARG_CHECK(R >= 0 && ns >= 1, "bad wake sizes");
+  if (R == 0) return FVX_OK;
+  fvx::wake_rings_kernel<<<fvx::nblk(R * ns), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(
+      R, ns, W, gam, age, rc0, br, fr, fl, bl, strength, rc0s, ages);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_uvlm_shed(int R_old, int nc, int ns, const double* W_old, const double* gam_old,
+                  const double* age_old, const double* te_next, const double* gamma,
+                  const double* u_inf, double dt, double* W_new, double* gam_new,
+                  double* age_new, void* stream) {
+  FVX_ARG_CHECK(R_old >= 0 && nc >= 1 && ns >= 1 && u_inf, "bad shed arguments");
+  const int n = (R_old + 2) * (ns + 1);
+  fvx::shed_kernel<<<fvx::nblk(n), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(
+      R_old, nc, ns, W_old, gam_old, age_old, te_next, gamma, u_inf[0] * dt, u_inf[1] * dt,
+      u_inf[2] * dt, dt, W_new, gam_new, age_new);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_uvlm_convert(int R, int n_keep, int ns, const double* W, const double* gam,
+                     int sigma_rule, double sigma_vdt, int64_t capacity, int64_t* count,
+                     double* pos, double* alpha, double* sigma, double* age, void* stream) {
+  FVX_ARG_CHECK(R >= 0 && n_keep >= 0 && ns >= 1 && count, "bad convert arguments");
+  if (R <= n_keep) return FVX_OK;
+  fvx::convert_kernel<<<1, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      R, n_keep, ns, W, gam, sigma_rule, sigma_vdt, capacity, count, pos, alpha, sigma, age);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+}  // extern "C"

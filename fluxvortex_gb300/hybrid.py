@@ -1,0 +1,209 @@
+"""Device-resident hybrid panel-particle step (mirror of the reference's HybridSolver).
+
+One ``HybridStep.step()`` runs, on the GPU and in the order of the
+reference's solver (tests/experiment_hybrid_panel_particle.py:87-204 on top
+of PteraSoftware's step):
+
+  kinematics -> lattice -> AIC (expanded ring Biot-Savart . n) ->
+  wake on collocation (ring rows + particles) -> rhs -> FP64 LU solve ->
+  loads (bound legs, CL / CDi) -> shed + convect the ring wake ->
+  rows >= N_keep to particles -> particle RK3 (VortexParticleField)
+
+Every stage is a C-ABI kernel over device arrays; the host keeps only the
+wake row count and reads the particle count once per step.  Particle sweeps
+run in FP64 or FP32-compensated (``precision``); the panel side, the AIC
+solve and the time integration stay FP64.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _capi
+from .geometry import HybridConfig
+from .particles import VortexParticleField
+
+
+class HybridStep:
+    def __init__(self, cfg: HybridConfig, precision: str = "f64", device="cuda"):
+        self.cfg = cfg
+        self.precision = precision
+        self.device = torch.device(device)
+        self.lib = _capi.load()
+        nc, ns = cfg.verts.shape[0] - 1, cfg.verts.shape[1] - 1
+        self.nc, self.ns, self.P = nc, ns, nc * ns
+        d = dict(dtype=torch.float64, device=self.device)
+        P = self.P
+        self.base = torch.as_tensor(cfg.verts.reshape(-1, 3), **d).contiguous()
+        self.verts = torch.empty_like(self.base)
+        self.verts_next = torch.empty_like(self.base)
+        z3 = lambda n: torch.zeros((n, 3), **d)  # noqa: E731
+        self.L = {k: z3(P) for k in ("br", "fr", "fl", "bl", "colloc", "normal", "leg_center",
+                                     "leg_vec")}
+        self.L["area"] = torch.zeros(P, **d)
+        self.te = z3(ns + 1)
+        self.te_next = z3(ns + 1)
+        self.Ln = {k: z3(P) for k in self.L if k != "area"}
+        self.Ln["area"] = torch.zeros(P, **d)
+        self.aic = torch.zeros((P, P), **d)
+        self.rhs = torch.zeros(P, **d)
+        self.gamma = torch.zeros(P, **d)
+        self.gamma_prev = torch.zeros(P, **d)
+        self.force = z3(P)
+        # ring wake: vertex lattice (R+1 rows) ping-pong, row strengths, ages
+        rows = cfg.n_keep + 2
+        self.W = [z3(rows * (ns + 1)), z3(rows * (ns + 1))]
+        self.wg = [torch.zeros(rows * ns, **d), torch.zeros(rows * ns, **d)]
+        self.wa = [torch.zeros(rows, **d), torch.zeros(rows, **d)]
+        self.cur = 0
+        self.R = 0
+        nr = (cfg.n_keep + 1) * ns
+        self.wr = {k: z3(nr) for k in ("br", "fr", "fl", "bl")}
+        self.wr_s = torch.zeros(nr, **d)
+        self.wr_rc = torch.zeros(nr, **d)
+        self.wr_age = torch.zeros(nr, **d)
+        self.v_ring_c, self.v_part_c = z3(P), z3(P)
+        self.v_ring_l, self.v_part_l, self.v_bound_l = z3(P), z3(P), z3(P)
+        self.seg_scratch = torch.empty(1, dtype=torch.uint8, device=self.device)
+        self.field = VortexParticleField(cfg.max_particles, nu=cfg.nu, rlxf=cfg.rlxf,
+                                         kernel=cfg.kernel, precision=precision, device=device)
+        self.count = torch.zeros(1, dtype=torch.int64, device=self.device)
+        self.u_inf = np.ascontiguousarray(cfg.u_inf, dtype=np.float64)
+        self.omega = 2.0 * np.pi / cfg.kin.period
+        self.cl_hist = torch.zeros(0, **d)
+        self._cl = torch.zeros(4096, **d)
+        self._cdi = torch.zeros(4096, **d)
+        self.k = 0
+        # initial wake lattice: the trailing edge at t = 0
+        self._kin(0.0, self.verts)
+        self._lattice(self.verts, self.L, self.te)
+        self.W[0][: ns + 1].copy_(self.te)
+
+    # ---- helpers ------------------------------------------------------------
+    def _st(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def _kin(self, t, out):
+        k = self.cfg.kin
+        _capi.check(self.lib.fvx_uvlm_kinematics(self.base.shape[0], self.base.data_ptr(),
+                                                 k.heave_amp, k.flap_amp, self.omega, k.y0, t,
+                                                 out.data_ptr(), self._st()))
+
+    def _lattice(self, verts, L, te):
+        _capi.check(self.lib.fvx_uvlm_lattice(
+            verts.data_ptr(), self.nc, self.ns, L["br"].data_ptr(), L["fr"].data_ptr(),
+            L["fl"].data_ptr(), L["bl"].data_ptr(),
+            L["colloc"].data_ptr() if "colloc" in L else None,
+            L["normal"].data_ptr(), L["area"].data_ptr(), L["leg_center"].data_ptr(),
+            L["leg_vec"].data_ptr(), te.data_ptr(), self._st()))
+
+    def _rings_at(self, pts, n_pts, out, strengths, n_rings, corners, rc0s, ages):
+        """Collapsed ring Biot-Savart of n_rings rings at n_pts points -> out."""
+        lib = self.lib
+        nb = lib.fvx_segments_collapsed_scratch_bytes(n_pts, n_rings, _capi.LEGS_RING)
+        if self.seg_scratch.numel() < nb:
+            self.seg_scratch = torch.empty(nb + 256, dtype=torch.uint8, device=self.device)
+        _capi.check(lib.fvx_segments_collapsed(
+            pts.data_ptr(), n_pts, corners["br"].data_ptr(), corners["fr"].data_ptr(),
+            corners["fl"].data_ptr(), corners["bl"].data_ptr(), strengths.data_ptr(),
+            rc0s.data_ptr(), None if ages is None else ages.data_ptr(), self.cfg.nu, n_rings,
+            _capi.LEGS_RING, out.data_ptr(), None, self.seg_scratch.data_ptr(),
+            self.seg_scratch.numel(), self._st()))
+
+    # ---- one step -----------------------------------------------------------
+    def step(self):
+        cfg, lib, st = self.cfg, self.lib, self._st()
+        kin = cfg.kin
+        P, ns = self.P, self.ns
+        t = self.k * cfg.dt
+        mot = (kin.heave_amp, kin.flap_amp, self.omega, kin.y0, t)
+        self._kin(t, self.verts)
+        self._lattice(self.verts, self.L, self.te)
+        L = self.L
+        # 1. AIC
+        _capi.check(lib.fvx_uvlm_aic(1, P, L["colloc"].data_ptr(), L["normal"].data_ptr(),
+                                     L["br"].data_ptr(), L["fr"].data_ptr(), L["fl"].data_ptr(),
+                                     L["bl"].data_ptr(), cfg.rc0, cfg.nu, self.aic.data_ptr(), st))
+        # 2-3. wake on collocation: ring rows + particles
+        R = self.R
+        Wc, gc, ac = self.W[self.cur], self.wg[self.cur], self.wa[self.cur]
+        nr = R * ns
+        if R:
+            _capi.check(lib.fvx_uvlm_wake_rings(R, ns, Wc.data_ptr(), gc.data_ptr(), ac.data_ptr(),
+                                                cfg.rc0, self.wr["br"].data_ptr(),
+                                                self.wr["fr"].data_ptr(), self.wr["fl"].data_ptr(),
+                                                self.wr["bl"].data_ptr(), self.wr_s.data_ptr(),
+                                                self.wr_rc.data_ptr(), self.wr_age.data_ptr(), st))
+            self._rings_at(L["colloc"], P, self.v_ring_c, self.wr_s, nr, self.wr, self.wr_rc,
+                           self.wr_age)
+        npart = self.field.np
+        if npart:
+            self.field._sweep(_capi.PAIR_VELOCITY, L["colloc"], None, P, self.v_part_c)
+        _capi.check(lib.fvx_uvlm_rhs(P, L["colloc"].data_ptr(), L["normal"].data_ptr(),
+                                     self.v_ring_c.data_ptr() if R else None,
+                                     self.v_part_c.data_ptr() if npart else None,
+                                     self.u_inf.ctypes.data, *mot, self.rhs.data_ptr(), st))
+        # 4. strengths (in place: rhs -> Gamma)
+        self.gamma.copy_(self.rhs)
+        _capi.check(lib.fvx_lu_solve_batched(1, P, self.aic.data_ptr(), self.gamma.data_ptr(), st))
+        # 5. loads at the bound-leg centres
+        if R:
+            self._rings_at(L["leg_center"], P, self.v_ring_l, self.wr_s, nr, self.wr, self.wr_rc,
+                           self.wr_age)
+        if npart:
+            self.field._sweep(_capi.PAIR_VELOCITY, L["leg_center"], None, P, self.v_part_l)
+        self._rings_at(L["leg_center"], P, self.v_bound_l, self.gamma, P, L,
+                       self._rc0_bound(), None)
+        k = self.k
+        if k >= self._cl.numel():
+            self._cl = torch.cat([self._cl, torch.zeros_like(self._cl)])
+            self._cdi = torch.cat([self._cdi, torch.zeros_like(self._cdi)])
+        _capi.check(lib.fvx_uvlm_loads(
+            self.nc, ns, self.gamma.data_ptr(), self.gamma_prev.data_ptr() if k else None,
+            L["leg_center"].data_ptr(), L["leg_vec"].data_ptr(), L["area"].data_ptr(),
+            L["normal"].data_ptr(), self.v_ring_l.data_ptr() if R else None,
+            self.v_part_l.data_ptr() if npart else None, self.v_bound_l.data_ptr(),
+            self.u_inf.ctypes.data, cfg.rho, cfg.dt, *mot, self._cl[k:].data_ptr(),
+            self._cdi[k:].data_ptr(), self.force.data_ptr(), st))
+        # 6. next wake: trailing edge at t + dt, convected rows
+        self._kin(t + cfg.dt, self.verts_next)
+        self._lattice(self.verts_next, self.Ln, self.te_next)
+        nxt = 1 - self.cur
+        _capi.check(lib.fvx_uvlm_shed(R, self.nc, ns, Wc.data_ptr(), gc.data_ptr(), ac.data_ptr(),
+                                      self.te_next.data_ptr(), self.gamma.data_ptr(),
+                                      self.u_inf.ctypes.data, cfg.dt, self.W[nxt].data_ptr(),
+                                      self.wg[nxt].data_ptr(), self.wa[nxt].data_ptr(), st))
+        self.cur = nxt
+        R += 1
+        # 7. rows >= N_keep -> particles
+        if R > cfg.n_keep:
+            f = self.field
+            self.count.fill_(f.np)
+            _capi.check(lib.fvx_uvlm_convert(
+                R, cfg.n_keep, ns, self.W[nxt].data_ptr(), self.wg[nxt].data_ptr(),
+                1 if cfg.sigma_rule == "edge" else 0, cfg.speed * cfg.dt, f.max_particles,
+                self.count.data_ptr(), f._pos.data_ptr(), f._gamma.data_ptr(),
+                f._sigma.data_ptr(), f._age.data_ptr(), st))
+            f.np = int(self.count.item())
+            R = cfg.n_keep
+        self.R = R
+        # 8. particles
+        if self.field.np:
+            self.field.advect_rk3(cfg.dt, self.u_inf, stretch=cfg.stretch,
+                                  free_wake=cfg.free_vpm)
+        self.gamma_prev.copy_(self.gamma)
+        self.k += 1
+
+    def _rc0_bound(self):
+        if not hasattr(self, "_rcb"):
+            self._rcb = torch.full((self.P,), self.cfg.rc0, dtype=torch.float64,
+                                   device=self.device)
+        return self._rcb
+
+    @property
+    def cl(self):
+        return self._cl[: self.k].cpu().numpy()
+
+    @property
+    def cdi(self):
+        return self._cdi[: self.k].cpu().numpy()

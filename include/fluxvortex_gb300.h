@@ -181,6 +181,65 @@ int fvx_vpm_finalize(int64_t n, double dt, const double* pos, double* gamma, dou
                      void* stream);
 int fvx_vpm_relax(int64_t n, double rlxf, const double* omega, double* gamma, void* stream);
 
+/* ---- panel side of the hybrid panel-particle step (FP64) ------------------------
+ * Replaces the PteraSoftware solver stages that HybridSolver runs around the
+ * Biot-Savart calls (tests/experiment_hybrid_panel_particle.py:114-204 and the
+ * PS step order of idea-stage/architecture_analysis.md:7-27).  A wing is a
+ * vertex grid verts[(nc+1)*(ns+1)][3] (chordwise rows LE->TE, spanwise columns
+ * left->right); P = nc*ns panels.  Motion: heave h(t) = heave_amp sin(omega t)
+ * and flapping theta(t) = flap_amp sin(omega t) about the x axis through y0.
+ *
+ * kinematics: vertices at time t.
+ * lattice: quarter-chord ring corners (br, fr, fl, bl: (P,3)), 3/4-chord
+ *   collocation points, unit normals, areas, bound-leg centres and FR->FL
+ *   vectors (P,3), trailing-edge back edge te_back (ns+1,3).
+ * aic: AIC[b][i][j] = (unit ring j at collocation i) . n_i for n_systems
+ *   systems stored back to back (expanded ring Biot-Savart fused with n).
+ * rhs: rhs_i = -((u_inf - v_body) + v1 + v2) . n_i (v1, v2 may be NULL).
+ * lu_solve_batched: solves A x = b in place (x -> b) for n_systems P x P
+ *   systems, partial pivoting; a zero pivot sets status bit 2.
+ * loads: Kutta-Joukowski force on each bound leg, rho (G_ij - G_i-1,j) (V x l),
+ *   V = u_inf - v_body + v1 + v2 + v3, minus rho dG/dt A n (gamma_prev NULL:
+ *   no unsteady term); writes CL and CDi (device scalars) and optionally the
+ *   per-panel forces.
+ * wake_rings: ring-wake vertex lattice W[(R+1)*(ns+1)][3] with row strengths
+ *   gam[R*ns] and row ages age[R] -> the ring layout of the Biot-Savart entries.
+ * shed: W_new = [te_next; W_old + u_inf dt], gam_new = [TE ring strengths;
+ *   gam_old], age_new = [0; age_old + dt].
+ * convert: rows r >= n_keep of W -> 4 particles per ring at leg midpoints
+ *   with alpha = Gamma (b - a), skipping |Gamma| < 1e-15 and |alpha|^2 <= 1e-30
+ *   (experiment_hybrid_panel_particle.py:173-200); sigma = sigma_vdt
+ *   (sigma_rule 0) or 1.3 x the ring's mean edge (sigma_rule 1); appended at
+ *   *count (device int64), clipped at capacity (status bit 4). */
+int fvx_uvlm_kinematics(int64_t n_verts, const double* base, double heave_amp, double flap_amp,
+                        double omega, double y0, double t, double* out, void* stream);
+int fvx_uvlm_lattice(const double* verts, int nc, int ns, double* br, double* fr, double* fl,
+                     double* bl, double* colloc, double* normal, double* area,
+                     double* leg_center, double* leg_vec, double* te_back, void* stream);
+int fvx_uvlm_aic(int n_systems, int P, const double* colloc, const double* normal,
+                 const double* br, const double* fr, const double* fl, const double* bl,
+                 double rc0, double nu, double* aic, void* stream);
+int fvx_uvlm_rhs(int P, const double* colloc, const double* normal, const double* v1,
+                 const double* v2, const double* u_inf, double heave_amp, double flap_amp,
+                 double omega, double y0, double t, double* rhs, void* stream);
+int fvx_lu_solve_batched(int n_systems, int P, double* A, double* b, void* stream);
+int fvx_uvlm_loads(int nc, int ns, const double* gamma, const double* gamma_prev,
+                   const double* leg_center, const double* leg_vec, const double* area,
+                   const double* normal, const double* v1, const double* v2, const double* v3,
+                   const double* u_inf, double rho, double dt, double heave_amp, double flap_amp,
+                   double omega, double y0, double t, double* cl, double* cdi, double* force,
+                   void* stream);
+int fvx_uvlm_wake_rings(int R, int ns, const double* W, const double* gam, const double* age,
+                        double rc0, double* br, double* fr, double* fl, double* bl,
+                        double* strength, double* rc0s, double* ages, void* stream);
+int fvx_uvlm_shed(int R_old, int nc, int ns, const double* W_old, const double* gam_old,
+                  const double* age_old, const double* te_next, const double* gamma,
+                  const double* u_inf, double dt, double* W_new, double* gam_new,
+                  double* age_new, void* stream);
+int fvx_uvlm_convert(int R, int n_keep, int ns, const double* W, const double* gam,
+                     int sigma_rule, double sigma_vdt, int64_t capacity, int64_t* count,
+                     double* pos, double* alpha, double* sigma, double* age, void* stream);
+
 /* ---- diagnostics -------------------------------------------------------------
  * Launches blocks_per_sm x SMs CTAs of 256 threads, each running `iters`
  * rounds of 8 independent FP32 FMAs (16 flop per round per thread): the
