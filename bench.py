@@ -1,23 +1,24 @@
 #!/usr/bin/env python
-"""Benchmark of the vortex-particle + panel induction step on one GB300.
+"""Benchmark of the VPM+panel step (hybrid panel-particle induction) on one GB300.
 
-Workload: the synthetic wake of ``fluxvortex_gb300.workloads.slab_wake`` at
-2^20 (~1e6) particles, Winckelmans core sigma = 0.02c, plus the 4096
-collocation points of a 64 x 64 wing grid.  One step =
-  wake-on-collocation induction (4096 targets x N particles) +
-  one VortexParticleField.advect_rk3 step with free wake and stretching
-  (3 x [velocity sweep, position update, stretching sweep, strength update])
-  + NaN guard + Pedrizzetti relaxation (Gaussian-erf vorticity sweep),
-all resident in HBM.  Sweeps run FP32 with compensated accumulation; the
-time integration is FP64.
+Workload (``Step``): the heaving NACA 0012 wing of the reference's hybrid
+experiment (120 panels, N_keep = 10 ring rows) with its particle wake seeded
+to 2^20 (~1e6) particles by a seeded 20c x 10c x 2c slab behind the trailing
+edge (``fluxvortex_gb300.workloads.slab_wake``).  One step = lattice + AIC +
+wake-on-collocation (ring rows + every particle) + FP64 LU solve + loads
+(CL, CDi) + shedding + row-to-particle conversion + one RK3 particle step
+with free wake and stretching (3 velocity + 3 stretching all-pairs sweeps),
+all resident in HBM.  Sweeps run FP32 with compensated accumulation
+(``--precision f32c``) or FP64; panel side and time integration are FP64.
 
 Output: one JSON line (rank 0).  ``value`` = steps/s of the whole job
-(device-timed, inputs resident); ``e2e`` = the same through the host-facing
-API (particle state copied in from pinned host memory and the new state plus
-the collocation velocities copied back every step); ``fp64_direct`` = the
+(device-timed, inputs resident, L2 flushed before every step); ``e2e`` = the
+same through the host-facing API (particle state copied in from pinned host
+memory, new state and CL/CDi copied back, every step); ``fp64_direct`` = the
 same step with FP64 sweeps, timed on a target sample and scaled (all-pairs
-cost is linear in the target count); ``cpu_baseline`` = the FP64 C oracle on
-the host cores on a bounded target sample, scaled likewise.
+cost is linear in the target count), plus the CL/CDi error of the mixed form
+against FP64 sweeps at the same state; ``cpu_baseline`` = the FP64 C oracle
+on the host cores on a bounded target sample, scaled likewise.
 
 ``--impl reference`` times the reference's CPU path for this step (its
 arithmetic restated in C + OpenMP, all host cores) on a bounded sample.
@@ -49,6 +50,8 @@ FLOP_PER_PAIR = {
     ("velocity", "gaussianerf"): 40,
     ("stretch", "gaussianerf"): 67,
 }
+WORKLOAD = ("VPM+panel step: heaving NACA0012 wing 120 panels + {n} seeded wake particles, "
+            "RK3 free wake with stretching")
 MODE_NAMES = {0: "velocity", 1: "stretch", 2: "velocity_stretch", 3: "jacobian", 4: "vorticity"}
 
 
@@ -114,27 +117,33 @@ def stop_clock_sampler(handle, gpu_index=0):
 
 # ---------------------------------------------------------------------------
 class Step:
-    """The benchmarked step on one device (state resident in HBM)."""
+    """The benchmarked VPM+panel step on one device (state resident in HBM).
 
-    def __init__(self, n, precision, device):
+    Geometry: the heaving NACA 0012 wing (chord 1, half span 5 mirrored,
+    nc=10 x ns=6 per half, V=10, h0/c=0.1, k=0.5, 40 steps per cycle,
+    N_keep=10 ring rows).  Its particle wake is seeded with the slab wake of
+    ``workloads.slab_wake(n)`` (2^20 particles behind the trailing edge) and
+    grows by one converted ring row (48 particles) per step.  A step: lattice,
+    AIC, wake-on-collocation (rings + all particles), FP64 LU solve, loads
+    (CL, CDi), shedding, conversion, and one RK3 particle step with free wake
+    and stretching (3 velocity + 3 stretching sweeps over all particles)."""
+
+    def __init__(self, n, precision, device, steps_hint=64):
         import torch
-        from fluxvortex_gb300.particles import VortexParticleField
+        from fluxvortex_gb300.geometry import heaving_wing
+        from fluxvortex_gb300.hybrid import HybridStep
         from fluxvortex_gb300.workloads import slab_wake
         pos, gam, sig, colloc = slab_wake(n)
         self.host = dict(pos=pos, gamma=gam, sigma=sig, colloc=colloc)
-        self.field = VortexParticleField(max_particles=n, nu=0.0, rlxf=0.3, kernel="winckelmans",
-                                         precision=precision, device=device)
-        self.field.add_particles_batch(pos, gam, sig)
-        self.colloc = torch.as_tensor(colloc, device=device)
-        self.u_colloc = torch.empty_like(self.colloc)
-        self.u_inf = [10.0, 0.0, 0.0]
-        self.dt = 0.02       # 0.2 chord per step at 10 m/s
+        self.cfg = heaving_wing(n_keep=10, free_vpm=True, stretch=True, rlxf=0.0,
+                                max_particles=n + 48 * (steps_hint + 8))
+        self.hs = HybridStep(self.cfg, precision=precision, device=device)
+        self.hs.field.add_particles_batch(pos, gam, sig)
+        self.field = self.hs.field
         self.device = device
 
     def run(self):
-        self.field._sweep(0, self.colloc, None, self.colloc.shape[0], self.u_colloc)
-        self.field.advect_rk3(self.dt, self.u_inf, stretch=True, free_wake=True)
-
+        self.hs.step()
 
 def sample_sweeps(field, n_t, precision, reps=1):
     """Times each sweep kind of one step on the first n_t particles as targets
@@ -149,8 +158,7 @@ def sample_sweeps(field, n_t, precision, reps=1):
     old = field.precision
     field.precision = precision
     kinds = {"velocity": (_capi.PAIR_VELOCITY, None, "winckelmans"),
-             "stretch": (_capi.PAIR_STRETCH, tg, "winckelmans"),
-             "vorticity": (_capi.PAIR_VORTICITY, None, "gaussianerf")}
+             "stretch": (_capi.PAIR_STRETCH, tg, "winckelmans")}
     sec = {}
     for name, (mode, tgm, kern) in kinds.items():
         field._sweep(mode, t, tgm, n_t, out, kernel=kern)          # warm-up
@@ -164,10 +172,9 @@ def sample_sweeps(field, n_t, precision, reps=1):
         sec[name] = s.elapsed_time(e) / reps / 1e3
     field.precision = old
     full = n / n_t
-    # 3 velocity + 3 stretching + 1 vorticity sweeps over all N targets, plus
-    # the collocation sweep (4096 targets)
-    return (3 * sec["velocity"] + 3 * sec["stretch"] + sec["vorticity"]) * full + \
-        sec["velocity"] * 4096 / n_t
+    # 3 velocity + 3 stretching sweeps over all N targets, plus the
+    # collocation and bound-leg sweeps (2 x 120 panel targets)
+    return (3 * sec["velocity"] + 3 * sec["stretch"]) * full + sec["velocity"] * 240 / n_t
 
 
 def cpu_oracle_step_seconds(host, n_t, threads=None):
@@ -186,14 +193,11 @@ def cpu_oracle_step_seconds(host, n_t, threads=None):
     t0 = time.perf_counter()
     O.velocity_and_stretching(t, tg, pos, gam, sig, "winckelmans")
     t_vs = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    O.jacobian_from_particles(t, tg, pos, gam, sig, "gaussianerf")
-    t_j = time.perf_counter() - t0
     scale = n / n_t
-    # step: 3 velocity + 3 stretching (a velocity+stretch pass bounds the
-    # stretching pass) + 1 vorticity (Jacobian) + collocation (4096 targets)
-    step = (3 * t_vel + 3 * t_vs + t_j) * scale + t_vel * 4096 / n_t
-    return step, O.num_threads(), dict(velocity_s=t_vel, stretch_s=t_vs, jacobian_s=t_j,
+    # step: 3 velocity + 3 stretching sweeps (a velocity+stretching pass bounds
+    # the stretching pass) + collocation and bound-leg sweeps (240 targets)
+    step = (3 * t_vel + 3 * t_vs) * scale + t_vel * 240 / n_t
+    return step, O.num_threads(), dict(velocity_s=t_vel, stretch_s=t_vs,
                                        targets=n_t, sources=n)
 
 
@@ -214,15 +218,14 @@ def run_reference(args, rank, world):
         times.append(s)
     step_s = statistics.median(times)
     v = 1.0 / step_s
-    sample = (f"{n_t} targets x {args.n} sources per sweep kind (velocity, velocity+stretching, "
-              f"Gaussian-erf Jacobian), scaled to the full step by N/targets")
+    sample = (f"{n_t} targets x {args.n} sources per sweep kind (velocity, velocity+stretching),"
+              f" scaled to the full step by N/targets")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"slab wake, {args.n} particles + 4096 collocation points, "
-                               "one RK3 free-wake step with stretching and relaxation"},
+        "config": {"workload": WORKLOAD.format(n=args.n)},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -305,12 +308,11 @@ def run_ours(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32c sweeps / f64 integration" if args.precision == "f32c" else "f64",
-        "data": "synthetic (seeded slab wake, BASELINE config-3 shapes)",
-        "config": {"workload": f"slab wake, {args.n} particles + 4096 collocation points, "
-                               "one RK3 free-wake step with stretching and relaxation",
-                   "particles": args.n, "collocation_points": 4096,
+        "data": "synthetic (heaving-wing geometry; wake seeded with a 20c x 10c x 2c slab of particles)",
+        "config": {"workload": WORKLOAD.format(n=args.n), "particles": args.n,
+                   "panels": step.hs.P, "n_keep": step.cfg.n_keep,
                    "precision": args.precision, "kernel": "winckelmans",
-                   "relax_kernel": "gaussianerf", "l2": "flushed (256 MB write) before each step",
+                   "l2": "flushed (256 MB write) before each step",
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": int(launches),
         "clocks": clk,
@@ -330,16 +332,12 @@ def run_ours(args, rank, world):
                                  "sample": f"{n_t} targets x {args.n} sources per sweep kind",
                                  "same_sample_f32c_step_s": f32_s,
                                  "speedup_vs_fp64": f64_s * 1e3 / ms_max}
-        # wake-on-collocation accuracy of the mixed form against FP64
-        u32 = step.u_colloc.clone()
-        step.field.precision = "f64"
-        u64 = torch.empty_like(u32)
-        step.field._sweep(0, step.colloc, None, step.colloc.shape[0], u64)
-        step.field.precision = args.precision
-        step.field._sweep(0, step.colloc, None, step.colloc.shape[0], u32)
-        torch.cuda.synchronize()
-        err = float((u32 - u64).abs().max() / u64.abs().max())
-        result["fp64_direct"]["colloc_velocity_rel_err"] = err
+        # CL / CDi of the mixed form against FP64 particle sweeps, same state
+        cl64, cdi64 = step.hs.panel_loads("f64")
+        cl32, cdi32 = step.hs.panel_loads(args.precision)
+        result["fp64_direct"]["cl_rel_err_same_state"] = abs(cl32 - cl64) / abs(cl64)
+        result["fp64_direct"]["cdi_rel_err_same_state"] = abs(cdi32 - cdi64) / abs(cdi64)
+        result["fp64_direct"]["cl"] = cl64
         cores = os.cpu_count() or 1
         cpu_s, thr, detail = cpu_oracle_step_seconds(step.host, 64, cores)
         result["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": UNIT, "cores": thr,
@@ -349,14 +347,14 @@ def run_ours(args, rank, world):
                                             "scaled to the full step by N/targets"}
 
     if not args.no_e2e:
-        # End to end through the host-facing API: pinned host state in, step,
-        # new state + collocation velocities out, every step.
+        # End to end through the host-facing API: the particle state in from
+        # pinned host memory, the step, the new state and CL / CDi out.
         f = step.field
         n = f.np
         hp = torch.empty((n, 3), dtype=torch.float64).pin_memory()
         hg = torch.empty((n, 3), dtype=torch.float64).pin_memory()
         hs = torch.empty(n, dtype=torch.float64).pin_memory()
-        hu = torch.empty((4096, 3), dtype=torch.float64).pin_memory()
+        hc = torch.empty(2, dtype=torch.float64).pin_memory()
         hp.copy_(f._pos[:n])
         hg.copy_(f._gamma[:n])
         hs.copy_(f._sigma[:n])
@@ -370,10 +368,13 @@ def run_ours(args, rank, world):
             f._gamma[:n].copy_(hg, non_blocking=True)
             f._sigma[:n].copy_(hs, non_blocking=True)
             step.run()
-            hp.copy_(f._pos[:n], non_blocking=True)
-            hg.copy_(f._gamma[:n], non_blocking=True)
-            hs.copy_(f._sigma[:n], non_blocking=True)
-            hu.copy_(step.u_colloc, non_blocking=True)
+            m = f.np
+            kk = step.hs.k - 1
+            hp[:n].copy_(f._pos[:n], non_blocking=True)
+            hg[:n].copy_(f._gamma[:n], non_blocking=True)
+            hs[:n].copy_(f._sigma[:n], non_blocking=True)
+            hc[0:1].copy_(step.hs._cl[kk:kk + 1], non_blocking=True)
+            hc[1:2].copy_(step.hs._cdi[kk:kk + 1], non_blocking=True)
         e.record()
         torch.cuda.synchronize()
         e2e_ms = s.elapsed_time(e) / e2e_steps
@@ -381,7 +382,7 @@ def run_ours(args, rank, world):
         if world > 1:
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
         h2d = n * (3 + 3 + 1) * 8
-        d2h = n * (3 + 3 + 1) * 8 + 4096 * 3 * 8
+        d2h = n * (3 + 3 + 1) * 8 + 2 * 8
         result["e2e"] = {"value": world * 1e3 / float(t.item()), "unit": UNIT,
                          "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 

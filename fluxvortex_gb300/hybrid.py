@@ -111,7 +111,34 @@ class HybridStep:
             self.seg_scratch.numel(), self._st()))
 
     # ---- one step -----------------------------------------------------------
+    def panel_loads(self, precision=None):
+        """Stages 1-5 (AIC, wake on collocation, solve, loads) at the current
+        state without advancing it; returns (CL, CDi).  ``precision``
+        overrides the particle sweeps' precision for this evaluation."""
+        old = self.field.precision
+        if precision is not None:
+            self.field.precision = precision
+        try:
+            self._panel(self._tmp_cl())
+        finally:
+            self.field.precision = old
+        v = self._tmp.cpu().numpy()
+        return float(v[0]), float(v[1])
+
+    def _tmp_cl(self):
+        if not hasattr(self, "_tmp"):
+            self._tmp = torch.zeros(2, dtype=torch.float64, device=self.device)
+        return self._tmp
+
     def step(self):
+        k = self.k
+        if k >= self._cl.numel():
+            self._cl = torch.cat([self._cl, torch.zeros_like(self._cl)])
+            self._cdi = torch.cat([self._cdi, torch.zeros_like(self._cdi)])
+        self._panel(None)
+        self._advance()
+
+    def _panel(self, out2):
         cfg, lib, st = self.cfg, self.lib, self._st()
         kin = cfg.kin
         P, ns = self.P, self.ns
@@ -155,16 +182,22 @@ class HybridStep:
         self._rings_at(L["leg_center"], P, self.v_bound_l, self.gamma, P, L,
                        self._rc0_bound(), None)
         k = self.k
-        if k >= self._cl.numel():
-            self._cl = torch.cat([self._cl, torch.zeros_like(self._cl)])
-            self._cdi = torch.cat([self._cdi, torch.zeros_like(self._cdi)])
+        cl_p = self._cl[k:].data_ptr() if out2 is None else out2[0:].data_ptr()
+        cdi_p = self._cdi[k:].data_ptr() if out2 is None else out2[1:].data_ptr()
         _capi.check(lib.fvx_uvlm_loads(
             self.nc, ns, self.gamma.data_ptr(), self.gamma_prev.data_ptr() if k else None,
             L["leg_center"].data_ptr(), L["leg_vec"].data_ptr(), L["area"].data_ptr(),
             L["normal"].data_ptr(), self.v_ring_l.data_ptr() if R else None,
             self.v_part_l.data_ptr() if npart else None, self.v_bound_l.data_ptr(),
-            self.u_inf.ctypes.data, cfg.rho, cfg.dt, *mot, self._cl[k:].data_ptr(),
-            self._cdi[k:].data_ptr(), self.force.data_ptr(), st))
+            self.u_inf.ctypes.data, cfg.rho, cfg.dt, *mot, cl_p, cdi_p, self.force.data_ptr(),
+            st))
+
+    def _advance(self):
+        cfg, lib, st = self.cfg, self.lib, self._st()
+        ns = self.ns
+        t = self.k * cfg.dt
+        R = self.R
+        Wc, gc, ac = self.W[self.cur], self.wg[self.cur], self.wa[self.cur]
         # 6. next wake: trailing edge at t + dt, convected rows
         self._kin(t + cfg.dt, self.verts_next)
         self._lattice(self.verts_next, self.Ln, self.te_next)
