@@ -328,10 +328,15 @@ def run_ours(args, rank, world):
         n_t = 4096
         f64_s = sample_sweeps(step.field, n_t, "f64")
         f32_s = sample_sweeps(step.field, n_t, args.precision)
-        result["fp64_direct"] = {"step_s_extrapolated": f64_s, "steps_per_s": 1.0 / f64_s,
+        # The sample runs the sweeps on n_t targets only; calibrate its scale-up
+        # with the mixed-precision form, whose full step is measured above.
+        calib = (ms_max / 1e3) / f32_s
+        result["fp64_direct"] = {"step_s_extrapolated": f64_s * calib,
+                                 "steps_per_s": 1.0 / (f64_s * calib),
                                  "sample": f"{n_t} targets x {args.n} sources per sweep kind",
-                                 "same_sample_f32c_step_s": f32_s,
-                                 "speedup_vs_fp64": f64_s * 1e3 / ms_max}
+                                 "sample_scale_up_step_s": f64_s,
+                                 "calibration": calib,
+                                 "speedup_vs_fp64": f64_s * calib * 1e3 / ms_max}
         # CL / CDi of the mixed form against FP64 particle sweeps, same state
         cl64, cdi64 = step.hs.panel_loads("f64")
         cl32, cdi32 = step.hs.panel_loads(args.precision)
