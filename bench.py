@@ -63,6 +63,9 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=1 << 20, help="particles")
     p.add_argument("--precision", default="f32c", choices=["f32c", "f64"])
+    p.add_argument("--far-field", default="direct", choices=["direct", "tree"],
+                   help="particle self-sweeps: direct all-pairs or the treecode")
+    p.add_argument("--leaf", type=int, default=64, help="treecode particles per leaf")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-baselines", action="store_true")
     return p.parse_args()
@@ -128,7 +131,7 @@ class Step:
     (CL, CDi), shedding, conversion, and one RK3 particle step with free wake
     and stretching (3 velocity + 3 stretching sweeps over all particles)."""
 
-    def __init__(self, n, precision, device, steps_hint=64):
+    def __init__(self, n, precision, device, steps_hint=64, far_field="direct", leaf=64):
         import torch
         from fluxvortex_gb300.geometry import heaving_wing
         from fluxvortex_gb300.hybrid import HybridStep
@@ -136,8 +139,11 @@ class Step:
         pos, gam, sig, colloc = slab_wake(n)
         self.host = dict(pos=pos, gamma=gam, sigma=sig, colloc=colloc)
         self.cfg = heaving_wing(n_keep=10, free_vpm=True, stretch=True, rlxf=0.0,
-                                max_particles=n + 48 * (steps_hint + 8))
+                                max_particles=n + 48 * (steps_hint + 8),
+                                far_field=None if far_field == "direct" else far_field)
         self.hs = HybridStep(self.cfg, precision=precision, device=device)
+        if self.hs.field.tree is not None:
+            self.hs.field.tree.leaf_target = leaf
         self.hs.field.add_particles_batch(pos, gam, sig)
         self.field = self.hs.field
         self.device = device
@@ -242,7 +248,7 @@ def run_ours(args, rank, world):
     device = torch.device("cuda", local)
     lib = _capi.load()
 
-    step = Step(args.n, args.precision, device)
+    step = Step(args.n, args.precision, device, far_field=args.far_field, leaf=args.leaf)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)   # > L2 (129 MB)
 
     def barrier():

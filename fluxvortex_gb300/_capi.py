@@ -48,6 +48,9 @@ SIGNATURES = {
     "fvx_vpm_finalize": (I32, [I64, D, P, P, P, P]),
     "fvx_vpm_relax": (I32, [I64, D, P, P, P]),
     "fvx_probe_fp32_fma": (I32, [I32, I32, P, P]),
+    "fvx_tree_create": (I32, [P]),
+    "fvx_tree_destroy": (None, [P]),
+    "fvx_tree_sweep": (I32, [P, I32, I32, P, P, P, P, I64, D, I32, P, P, P, P]),
     "fvx_uvlm_kinematics": (I32, [I64, P, D, D, D, D, D, P, P]),
     "fvx_uvlm_lattice": (I32, [P, I32, I32, P, P, P, P, P, P, P, P, P, P, P]),
     "fvx_uvlm_aic": (I32, [I32, I32, P, P, P, P, P, P, D, D, P, P]),

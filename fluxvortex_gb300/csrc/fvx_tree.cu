@@ -1,0 +1,1105 @@
+// fvx_tree.cu -- cell-binned treecode for the particle self-induction sweeps.
+//
+// The reference sums every particle pair directly (src/fluxvortex/kernel.py:
+// 69-190, O(N^2) per sweep).  This treecode replaces a self-sweep over N
+// particles by
+//   near field: direct FP32 pair sums (same core arithmetic as fvx_particles)
+//               between each target leaf and the leaves its interaction list
+//               keeps near, with compensated accumulation;
+//   far field:  a quadrupole expansion of the vector potential
+//               Psi_m = (1/4pi) sum a_m/|x - x_s| about each accepted cell's
+//               centre (u = curl Psi, J_in = eps_ijm d_n d_j Psi_m), FP32.
+//
+// Build (every sweep state, all on the device):
+//   bbox -> host picks the grid (tree_params.grid_params: power-of-two root
+//   cube aligned to the leaf size) -> 30-bit Morton keys -> stable LSD radix
+//   sort (4 x 8-bit digits, per-block histograms, warp-match ranking) ->
+//   leaf cells = runs of equal keys, coarser levels = runs of equal key >> 3
+//   among the finer level's cells -> sorted FP32 particle records relative to
+//   their leaf centre -> leaf moments (one warp per leaf) -> M2M shifts up the
+//   levels -> interaction lists per target leaf (depth-first traversal, exact
+//   acceptance test |dc|^2 > 3/4 (h_T + h_S)^2 / theta^2 in FP64) -> eval.
+// Because cell centres are exact binary fractions, centre differences are
+// exact in FP32 and pair offsets are (c_T - c_S) + (o_t - o_s) with small
+// in-cell offsets o.
+#include <type_traits>
+
+#include "fvx_common.cuh"
+#include "fvx_pair_math.cuh"
+
+namespace fvx {
+namespace tree {
+
+constexpr int kScanBlock = 2048;   // elements per scan block (1024 threads x 2)
+constexpr int kSortItems = 1024;   // keys per radix-sort block (256 threads x 4)
+constexpr int kEvalThreads = 64;   // eval CTA; 2 targets per thread
+constexpr int kFarTile = 32;       // far cells staged per tile
+constexpr int kNearTile = 128;     // source particles staged per tile
+constexpr int kRecFloats = 40;     // far-cell record
+constexpr double kC = -0.07957747154594767;  // -1/(4 pi)
+
+// ---- scan: exclusive / inclusive prefix sums of int32 ------------------------
+__global__ void scan_block_kernel(const int* __restrict__ in, int n, int* __restrict__ out,
+                                  int* __restrict__ block_sums, int inclusive) {
+  __shared__ int s[kScanBlock];
+  const int base = blockIdx.x * kScanBlock;
+  for (int k = threadIdx.x; k < kScanBlock; k += blockDim.x) {
+    const int i = base + k;
+    s[k] = i < n ? in[i] : 0;
+  }
+  __syncthreads();
+  // Hillis-Steele on kScanBlock elements with kScanBlock / 2 threads
+  for (int off = 1; off < kScanBlock; off <<= 1) {
+    int v0 = 0, v1 = 0;
+    const int k0 = threadIdx.x, k1 = threadIdx.x + blockDim.x;
+    if (k0 >= off) v0 = s[k0 - off];
+    if (k1 >= off) v1 = s[k1 - off];
+    __syncthreads();
+    s[k0] += v0;
+    s[k1] += v1;
+    __syncthreads();
+  }
+  for (int k = threadIdx.x; k < kScanBlock; k += blockDim.x) {
+    const int i = base + k;
+    if (i < n) out[i] = inclusive ? s[k] : s[k] - (i < n ? in[i] : 0);
+  }
+  if (threadIdx.x == 0 && block_sums) block_sums[blockIdx.x] = s[kScanBlock - 1];
+}
+
+__global__ void scan_add_kernel(int* __restrict__ out, int n, const int* __restrict__ offs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += offs[i / kScanBlock];
+}
+
+// total of an inclusive scan -> *total
+__global__ void scan_total_kernel(const int* __restrict__ incl, int n, int* __restrict__ total) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *total = n > 0 ? incl[n - 1] : 0;
+}
+
+}  // namespace tree
+
+// Device-wide scan of n <= 2048*2048 ints (in -> out); tmp holds >= 2*2048 ints.
+int scan_ints(const int* in, int n, int* out, int inclusive, int* tmp, cudaStream_t s) {
+  using namespace tree;
+  if (n <= 0) return FVX_OK;
+  const int nb = (n + kScanBlock - 1) / kScanBlock;
+  FVX_ARG_CHECK(nb <= kScanBlock, "scan of %d elements exceeds 2^22", n);
+  int* bsum = tmp;
+  int* bsum_ex = tmp + kScanBlock;
+  scan_block_kernel<<<nb, kScanBlock / 2, 0, s>>>(in, n, out, bsum, inclusive);
+  FVX_LAUNCH_CHECK();
+  if (nb > 1) {
+    scan_block_kernel<<<1, kScanBlock / 2, 0, s>>>(bsum, nb, bsum_ex, nullptr, 0);
+    FVX_LAUNCH_CHECK();
+    scan_add_kernel<<<(n + 255) / 256, 256, 0, s>>>(out, n, bsum_ex);
+    FVX_LAUNCH_CHECK();
+  }
+  return FVX_OK;
+}
+
+namespace tree {
+
+// ---- bounding box -------------------------------------------------------------
+__global__ void bbox_partial_kernel(int64_t n, const double* __restrict__ pos,
+                                    double* __restrict__ partial) {
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    for (int c = 0; c < 3; ++c) {
+      const double v = pos[3 * i + c];
+      lo[c] = fmin(lo[c], v);
+      hi[c] = fmax(hi[c], v);
+    }
+  }
+  __shared__ double s[6][256];
+  for (int c = 0; c < 3; ++c) {
+    s[c][threadIdx.x] = lo[c];
+    s[3 + c][threadIdx.x] = hi[c];
+  }
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int c = 0; c < 3; ++c) {
+        s[c][threadIdx.x] = fmin(s[c][threadIdx.x], s[c][threadIdx.x + st]);
+        s[3 + c][threadIdx.x] = fmax(s[3 + c][threadIdx.x], s[3 + c][threadIdx.x + st]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) partial[blockIdx.x * 6 + threadIdx.x] = s[threadIdx.x][0];
+}
+
+__global__ void bbox_final_kernel(int nb, const double* __restrict__ partial,
+                                  double* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  double r[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
+  for (int b = 0; b < nb; ++b)
+    for (int c = 0; c < 3; ++c) {
+      r[c] = fmin(r[c], partial[b * 6 + c]);
+      r[3 + c] = fmax(r[3 + c], partial[b * 6 + 3 + c]);
+    }
+  for (int c = 0; c < 6; ++c) out[c] = r[c];
+}
+
+// ---- Morton keys ----------------------------------------------------------------
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {
+  v &= 0x3FFu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+__device__ __forceinline__ uint32_t compact10(uint32_t v) {
+  v &= 0x09249249u;
+  v = (v | (v >> 2)) & 0x030C30C3u;
+  v = (v | (v >> 4)) & 0x0300F00Fu;
+  v = (v | (v >> 8)) & 0x030000FFu;
+  v = (v | (v >> 16)) & 0x000003FFu;
+  return v;
+}
+
+__global__ void keys_kernel(int64_t n, const double* __restrict__ pos, double ox, double oy,
+                            double oz, double inv_h, int L, uint32_t* __restrict__ keys,
+                            int* __restrict__ idx) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const int top = (1 << L) - 1;
+  const double o[3] = {ox, oy, oz};
+  uint32_t q[3];
+  for (int c = 0; c < 3; ++c) {
+    double f = floor((pos[3 * i + c] - o[c]) * inv_h);
+    int v = f < 0.0 ? 0 : (f > top ? top : static_cast<int>(f));
+    q[c] = static_cast<uint32_t>(v);
+  }
+  keys[i] = spread10(q[0]) | (spread10(q[1]) << 1) | (spread10(q[2]) << 2);
+  idx[i] = static_cast<int>(i);
+}
+
+// ---- stable LSD radix sort, 8-bit digits ------------------------------------------
+__global__ void __launch_bounds__(256) radix_hist_kernel(const uint32_t* __restrict__ keys, int n,
+                                                         int shift, int nblk,
+                                                         int* __restrict__ table) {
+  __shared__ int h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int base = blockIdx.x * kSortItems;
+  for (int k = threadIdx.x; k < kSortItems; k += 256) {
+    const int i = base + k;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1);
+  }
+  __syncthreads();
+  table[threadIdx.x * nblk + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(256) radix_scatter_kernel(
+    const uint32_t* __restrict__ keys, const int* __restrict__ idx, int n, int shift, int nblk,
+    const int* __restrict__ offs, uint32_t* __restrict__ keys_out, int* __restrict__ idx_out) {
+  __shared__ int run[256];
+  __shared__ int whist[8][256];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  run[threadIdx.x] = offs[threadIdx.x * nblk + blockIdx.x];
+  const unsigned lt = (1u << lane) - 1u;
+  const int base = blockIdx.x * kSortItems;
+  for (int it = 0; it < kSortItems / 256; ++it) {
+    for (int w = 0; w < 8; ++w) whist[w][threadIdx.x] = 0;
+    __syncthreads();
+    const int i = base + it * 256 + warp * 32 + lane;
+    const bool valid = i < n;
+    const uint32_t key = valid ? keys[i] : 0u;
+    const int val = valid ? idx[i] : 0;
+    const unsigned digit = valid ? ((key >> shift) & 255u) : 256u;
+    const unsigned peers = __match_any_sync(0xffffffffu, digit);
+    const int rank = __popc(peers & lt);
+    const int leader = 31 - __clz(peers);
+    if (valid && lane == leader) whist[warp][digit] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      int off = run[digit] + rank;
+      for (int w = 0; w < warp; ++w) off += whist[w][digit];
+      keys_out[off] = key;
+      idx_out[off] = val;
+    }
+    __syncthreads();
+    int tot = 0;
+    for (int w = 0; w < 8; ++w) tot += whist[w][threadIdx.x];
+    run[threadIdx.x] += tot;
+    __syncthreads();
+  }
+}
+
+// ---- cells ----------------------------------------------------------------------
+// flag[i] = 1 where the level key (key >> shift) changes
+__global__ void flags_kernel(const uint32_t* __restrict__ keys, const int* __restrict__ n_ptr,
+                             int n_cap, int shift, int* __restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = n_ptr ? *n_ptr : n_cap;
+  if (i >= n_cap) return;
+  if (i >= n) {
+    flag[i] = 0;
+    return;
+  }
+  flag[i] = (i == 0 || (keys[i] >> shift) != (keys[i - 1] >> shift)) ? 1 : 0;
+}
+
+struct Level {
+  int* start;     // first sorted particle of each cell
+  int* count;     // particles in each cell
+  uint32_t* key;  // level key (Morton prefix)
+  int* child_lo;  // first child cell (level l+1 local id)
+  int* child_hi;  // one past the last child
+};
+
+// leaf cells from the particle flags (cid = inclusive scan of flags)
+__global__ void leaf_cells_kernel(const uint32_t* __restrict__ keys, int n,
+                                  const int* __restrict__ flag, const int* __restrict__ cid,
+                                  Level lv, int* __restrict__ n_cells) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = cid[i] - 1;
+  if (flag[i]) {
+    lv.start[c] = i;
+    lv.key[c] = keys[i];
+  }
+  if (i == n - 1) *n_cells = c + 1;
+}
+
+__global__ void cell_counts_kernel(Level lv, const int* __restrict__ n_cells, int n_total) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = *n_cells;
+  if (c >= nc) return;
+  const int end = c + 1 < nc ? lv.start[c + 1] : n_total;
+  lv.count[c] = end - lv.start[c];
+}
+
+// parent flags over the children cells of level l+1 (keys >> 3)
+__global__ void parent_flags_kernel(Level child, const int* __restrict__ n_child, int cap,
+                                    int* __restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cap) return;
+  const int n = *n_child;
+  if (i >= n) {
+    flag[i] = 0;
+    return;
+  }
+  flag[i] = (i == 0 || (child.key[i] >> 3) != (child.key[i - 1] >> 3)) ? 1 : 0;
+}
+
+__global__ void parent_cells_kernel(Level child, const int* __restrict__ n_child,
+                                    const int* __restrict__ flag, const int* __restrict__ pid,
+                                    Level par, int* __restrict__ n_par) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = *n_child;
+  if (i >= n) return;
+  const int p = pid[i] - 1;
+  if (flag[i]) {
+    par.start[p] = child.start[i];
+    par.key[p] = child.key[i] >> 3;
+    par.child_lo[p] = i;
+  }
+  if (i == n - 1 || flag[i + 1]) par.child_hi[p] = i + 1;
+  if (i == n - 1) *n_par = p + 1;
+}
+
+// parent particle count = (last child's end) - (first child's start)
+__global__ void parent_counts_kernel(Level child, Level par, const int* __restrict__ n_par) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= *n_par) return;
+  const int lc = par.child_hi[p] - 1;
+  par.count[p] = child.start[lc] + child.count[lc] - par.start[p];
+}
+
+// ---- sorted particle records -----------------------------------------------------
+struct Grid {
+  double ox, oy, oz, h;
+  int L;
+};
+
+__device__ __forceinline__ void cell_center(uint32_t key, double hl, const Grid& g, double c[3]) {
+  c[0] = g.ox + (static_cast<double>(compact10(key)) + 0.5) * hl;
+  c[1] = g.oy + (static_cast<double>(compact10(key >> 1)) + 0.5) * hl;
+  c[2] = g.oz + (static_cast<double>(compact10(key >> 2)) + 0.5) * hl;
+}
+// centre relative to the grid origin (exact in FP32)
+__device__ __forceinline__ float3 cell_center_rel(uint32_t key, float hl) {
+  return make_float3((static_cast<float>(compact10(key)) + 0.5f) * hl,
+                     (static_cast<float>(compact10(key >> 1)) + 0.5f) * hl,
+                     (static_cast<float>(compact10(key >> 2)) + 0.5f) * hl);
+}
+
+template <int KERNEL>
+__global__ void gather_kernel(int n, const int* __restrict__ perm, const int* __restrict__ leaf_of,
+                              const uint32_t* __restrict__ leaf_key, Grid g,
+                              const double* __restrict__ pos, const double* __restrict__ alpha,
+                              const double* __restrict__ sigma, const double* __restrict__ tgam,
+                              float4* __restrict__ sp, float4* __restrict__ sa,
+                              float4* __restrict__ sg) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int j = perm[i];
+  const int leaf = leaf_of[i] - 1;
+  double c[3];
+  cell_center(leaf_key[leaf], g.h, g, c);
+  const double s = sigma[j];
+  sp[i] = make_float4(static_cast<float>(pos[3 * j] - c[0]), static_cast<float>(pos[3 * j + 1] - c[1]),
+                      static_cast<float>(pos[3 * j + 2] - c[2]), static_cast<float>(s * s));
+  sa[i] = make_float4(static_cast<float>(kC * alpha[3 * j]), static_cast<float>(kC * alpha[3 * j + 1]),
+                      static_cast<float>(kC * alpha[3 * j + 2]),
+                      static_cast<float>(KERNEL == FVX_KERNEL_WINCKELMANS ? 2.5 * s * s : 1.0 / s));
+  if (tgam)
+    sg[i] = make_float4(static_cast<float>(tgam[3 * j]), static_cast<float>(tgam[3 * j + 1]),
+                        static_cast<float>(tgam[3 * j + 2]), 0.f);
+}
+
+// ---- moments ----------------------------------------------------------------------
+// record: [cx cy cz h | M0(3) t(3) | M1(9) | M2 (3 x 6 unique: xx xy xz yy yz zz) | pad 2]
+__device__ __forceinline__ int m2i(int j, int k) {
+  // unique index of the symmetric pair (j, k)
+  const int a = j < k ? j : k, b = j < k ? k : j;
+  return a == 0 ? b : (a == 1 ? 2 + b : 5);
+}
+
+// one warp per leaf, moments of the C-scaled strengths about the leaf centre
+__global__ void leaf_moments_kernel(Level lv, const int* __restrict__ n_leaves, float hl,
+                                    const float4* __restrict__ sp, const float4* __restrict__ sa,
+                                    float* __restrict__ rec) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= *n_leaves) return;
+  float m[30];
+#pragma unroll
+  for (int q = 0; q < 30; ++q) m[q] = 0.f;
+  const int s = lv.start[warp], e = s + lv.count[warp];
+  for (int i = s + lane; i < e; i += 32) {
+    const float4 p = sp[i];
+    const float4 a = sa[i];
+    const float d[3] = {p.x, p.y, p.z}, al[3] = {a.x, a.y, a.z};
+#pragma unroll
+    for (int mm = 0; mm < 3; ++mm) {
+      m[mm] += al[mm];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) m[3 + 3 * mm + j] += al[mm] * d[j];
+      m[12 + 6 * mm + 0] += al[mm] * d[0] * d[0];
+      m[12 + 6 * mm + 1] += al[mm] * d[0] * d[1];
+      m[12 + 6 * mm + 2] += al[mm] * d[0] * d[2];
+      m[12 + 6 * mm + 3] += al[mm] * d[1] * d[1];
+      m[12 + 6 * mm + 4] += al[mm] * d[1] * d[2];
+      m[12 + 6 * mm + 5] += al[mm] * d[2] * d[2];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 30; ++q)
+    for (int o = 16; o > 0; o >>= 1) m[q] += __shfl_xor_sync(0xffffffffu, m[q], o);
+  if (lane == 0) {
+    float* r = rec + static_cast<int64_t>(warp) * kRecFloats;
+    const float3 c = cell_center_rel(lv.key[warp], hl);
+    r[0] = c.x;
+    r[1] = c.y;
+    r[2] = c.z;
+    r[3] = hl;
+    for (int mm = 0; mm < 3; ++mm) {
+      r[4 + mm] = m[mm];
+      r[7 + mm] = m[12 + 6 * mm + 0] + m[12 + 6 * mm + 3] + m[12 + 6 * mm + 5];  // trace
+    }
+    for (int q = 0; q < 9; ++q) r[10 + q] = m[3 + q];
+    for (int q = 0; q < 18; ++q) r[19 + q] = m[12 + q];
+    r[37] = r[38] = r[39] = 0.f;
+  }
+}
+
+// parent moments from children (shift by s = c_child - c_parent, exact)
+__global__ void m2m_kernel(Level par, const int* __restrict__ n_par, float hl,
+                           const float* __restrict__ child_rec, float* __restrict__ par_rec) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= *n_par) return;
+  const float3 cp = cell_center_rel(par.key[p], hl);
+  float M0[3] = {0, 0, 0}, M1[9], M2[18];
+  for (int q = 0; q < 9; ++q) M1[q] = 0.f;
+  for (int q = 0; q < 18; ++q) M2[q] = 0.f;
+  for (int c = par.child_lo[p]; c < par.child_hi[p]; ++c) {
+    const float* r = child_rec + static_cast<int64_t>(c) * kRecFloats;
+    const float s[3] = {r[0] - cp.x, r[1] - cp.y, r[2] - cp.z};
+    for (int m = 0; m < 3; ++m) {
+      const float m0 = r[4 + m];
+      M0[m] += m0;
+      for (int j = 0; j < 3; ++j) M1[3 * m + j] += r[10 + 3 * m + j] + m0 * s[j];
+      for (int j = 0; j < 3; ++j)
+        for (int k = j; k < 3; ++k) {
+          const int u = m2i(j, k);
+          M2[6 * m + u] += r[19 + 6 * m + u] + r[10 + 3 * m + j] * s[k] +
+                           r[10 + 3 * m + k] * s[j] + m0 * s[j] * s[k];
+        }
+    }
+  }
+  float* r = par_rec + static_cast<int64_t>(p) * kRecFloats;
+  r[0] = cp.x;
+  r[1] = cp.y;
+  r[2] = cp.z;
+  r[3] = hl;
+  for (int m = 0; m < 3; ++m) {
+    r[4 + m] = M0[m];
+    r[7 + m] = M2[6 * m + 0] + M2[6 * m + 3] + M2[6 * m + 5];
+  }
+  for (int q = 0; q < 9; ++q) r[10 + q] = M1[q];
+  for (int q = 0; q < 18; ++q) r[19 + q] = M2[q];
+  r[37] = r[38] = r[39] = 0.f;
+}
+
+// ---- interaction lists --------------------------------------------------------------
+struct TreeView {
+  int L;
+  double h;          // leaf size
+  double mac_k;      // 3/4 / theta^2
+  int base[11];      // global id of the first cell of each level
+  int ncell[11];     // cells per level (device copy below)
+  const int* start;  // global cell arrays (concatenated levels)
+  const int* count;
+  const uint32_t* key;
+  const int* child_lo;  // level-local ids of the children (level l+1)
+  const int* child_hi;
+};
+
+template <bool FILL>
+__global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
+                                const int* __restrict__ far_off, int* __restrict__ near_cnt,
+                                int* __restrict__ far_cnt, int* __restrict__ near_idx,
+                                int* __restrict__ far_idx, int near_cap, int far_cap,
+                                unsigned* __restrict__ overflow) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nleaf = T.ncell[T.L];
+  if (t >= nleaf) return;
+  const int gT = T.base[T.L] + t;
+  const uint32_t kT = T.key[gT];
+  // centre of T in units of h/2 (exact integers)
+  const long long tx = 2LL * compact10(kT) + 1, ty = 2LL * compact10(kT >> 1) + 1,
+                  tz = 2LL * compact10(kT >> 2) + 1;
+  int stack[96];
+  int sp = 0;
+  for (int c = T.ncell[0] - 1; c >= 0; --c) stack[sp++] = T.base[0] + c;
+  int nn = 0, nf = 0;
+  int no = FILL ? near_off[t] : 0, fo = FILL ? far_off[t] : 0;
+  while (sp > 0) {
+    const int g = stack[--sp];
+    int l = 0;
+    while (l < T.L && g >= T.base[l + 1]) ++l;
+    const uint32_t k = T.key[g];
+    const long long sc = 1LL << (T.L - l);  // cell size in units of h
+    const long long sx = (2LL * compact10(k) + 1) * sc, sy = (2LL * compact10(k >> 1) + 1) * sc,
+                    sz = (2LL * compact10(k >> 2) + 1) * sc;
+    const double dx = static_cast<double>(tx - sx) * (0.5 * T.h);
+    const double dy = static_cast<double>(ty - sy) * (0.5 * T.h);
+    const double dz = static_cast<double>(tz - sz) * (0.5 * T.h);
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    const double hs = T.h + static_cast<double>(sc) * T.h;
+    if (d2 > T.mac_k * (hs * hs)) {
+      if (FILL && fo + nf < far_cap) far_idx[fo + nf] = g;
+      ++nf;
+    } else if (l == T.L) {
+      if (FILL && no + nn < near_cap) near_idx[no + nn] = g - T.base[T.L];
+      ++nn;
+    } else {
+      const int lo = T.child_lo[g], hi = T.child_hi[g];
+      for (int c = hi - 1; c >= lo; --c) {
+        if (sp < 96) {
+          stack[sp++] = T.base[l + 1] + c;
+        } else {
+          atomicOr(overflow, 1u);
+        }
+      }
+    }
+  }
+  if (!FILL) {
+    near_cnt[t] = nn;
+    far_cnt[t] = nf;
+  } else if (no + nn > near_cap || fo + nf > far_cap) {
+    atomicOr(overflow, 2u);
+  }
+}
+
+// ---- evaluation -----------------------------------------------------------------------
+struct EvalArgs {
+  float h;  // leaf size
+  const int* leaf_start;
+  const int* leaf_count;
+  const uint32_t* leaf_key;
+  const int* near_off;
+  const int* near_cnt;
+  const int* near_idx;
+  const int* far_off;
+  const int* far_cnt;
+  const int* far_idx;
+  const float* rec;  // global cell records
+  const float4* sp;
+  const float4* sa;
+  const float4* sg;
+  const int* perm;
+  double* out_a;
+  double* out_b;
+};
+
+template <typename T>
+__device__ __forceinline__ void fold(T& hi, T& lo, T p) {
+  T s = hi + p;
+  T bp = s - hi;
+  T err = (hi - (s - bp)) + (p - bp);
+  hi = s;
+  lo += err;
+}
+
+// Far field of one cell record R at offset r = x - c (moments of C-scaled
+// strengths; see the derivation in oracle/treecode.py): adds to acc.
+template <int MODE>
+__device__ __forceinline__ void m2p(float* acc, const float* R, float rx, float ry, float rz,
+                                    float gx, float gy, float gz) {
+  const float r[3] = {rx, ry, rz};
+  const float r2 = rx * rx + ry * ry + rz * rz;
+  const float ir = rsqrtf(r2);
+  const float ir2 = ir * ir;
+  const float ir3 = ir * ir2, ir5 = ir3 * ir2, ir7 = ir5 * ir2;
+  const float* M0 = R + 4;
+  const float* tr = R + 7;
+  const float* M1 = R + 10;
+  const float* M2 = R + 19;
+  float a[3], w[3][3], q[3], s[3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    a[m] = M1[3 * m] * rx + M1[3 * m + 1] * ry + M1[3 * m + 2] * rz;
+    const float* Q = M2 + 6 * m;  // xx xy xz yy yz zz
+    w[m][0] = Q[0] * rx + Q[1] * ry + Q[2] * rz;
+    w[m][1] = Q[1] * rx + Q[3] * ry + Q[4] * rz;
+    w[m][2] = Q[2] * rx + Q[4] * ry + Q[5] * rz;
+    q[m] = w[m][0] * rx + w[m][1] * ry + w[m][2] * rz;
+    s[m] = -M0[m] * ir3 - 3.f * ir5 * a[m] - 7.5f * ir7 * q[m] + 1.5f * ir5 * tr[m];
+  }
+  if (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_VELOCITY_STRETCH) {
+    float X[3][3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) X[m][j] = s[m] * r[j] + ir3 * M1[3 * m + j] + 3.f * ir5 * w[m][j];
+    acc[0] += X[1][2] - X[2][1];
+    acc[1] += X[2][0] - X[0][2];
+    acc[2] += X[0][1] - X[1][0];
+  }
+  if (MODE == FVX_PAIR_STRETCH || MODE == FVX_PAIR_VELOCITY_STRETCH ||
+      MODE == FVX_PAIR_VORTICITY) {
+    const float ir9 = ir7 * ir2;
+    float P[3], V[3][3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      P[m] = 3.f * M0[m] * ir5 + 15.f * ir7 * a[m] + 52.5f * ir9 * q[m] - 7.5f * ir7 * tr[m];
+#pragma unroll
+      for (int n = 0; n < 3; ++n) V[m][n] = 3.f * ir5 * M1[3 * m + n] + 15.f * ir7 * w[m][n];
+    }
+    if (MODE == FVX_PAIR_VORTICITY) {
+      const float rP = rx * P[0] + ry * P[1] + rz * P[2];
+      const float trV = V[0][0] + V[1][1] + V[2][2];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const float Vr = V[0][i] * rx + V[1][i] * ry + V[2][i] * rz;
+        // sum_j M2_j(i,j)
+        const float m2 = M2[6 * 0 + m2i(i, 0)] + M2[6 * 1 + m2i(i, 1)] + M2[6 * 2 + m2i(i, 2)];
+        acc[i] -= r[i] * rP + s[i] - Vr - r[i] * trV + 3.f * ir5 * m2;
+      }
+    } else {
+      constexpr int o = MODE == FVX_PAIR_STRETCH ? 0 : 3;
+      const float g[3] = {gx, gy, gz};
+      const float rG = rx * gx + ry * gy + rz * gz;
+      float hm[3][3];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const float VG = V[m][0] * gx + V[m][1] * gy + V[m][2] * gz;
+        const float* Q = M2 + 6 * m;
+        const float MG[3] = {Q[0] * gx + Q[1] * gy + Q[2] * gz, Q[1] * gx + Q[3] * gy + Q[4] * gz,
+                             Q[2] * gx + Q[4] * gy + Q[5] * gz};
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          hm[m][j] = rG * r[j] * P[m] + g[j] * s[m] - (VG * r[j] + V[m][j] * rG) +
+                     3.f * ir5 * MG[j];
+      }
+      acc[o + 0] -= hm[2][1] - hm[1][2];
+      acc[o + 1] -= hm[0][2] - hm[2][0];
+      acc[o + 2] -= hm[1][0] - hm[0][1];
+    }
+  }
+}
+
+template <int MODE, int KERNEL>
+__global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
+  using namespace pair;
+  constexpr int NC = ModeInfo<MODE>::ncomp;
+  constexpr int NA = ModeInfo<MODE>::na;
+  constexpr bool NEED_FPR = ModeInfo<MODE>::need_fpr;
+  constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
+  constexpr int TPT = 2;
+  __shared__ float4 s_p[kNearTile];
+  __shared__ float4 s_a[kNearTile];
+  __shared__ float s_rec[kFarTile * kRecFloats];
+
+  const int t = blockIdx.x;
+  const int tstart = A.leaf_start[t], tcount = A.leaf_count[t];
+  const float3 cT = cell_center_rel(A.leaf_key[t], A.h);
+  const int nno = A.near_off[t], nnc = A.near_cnt[t];
+  const int fno = A.far_off[t], fnc = A.far_cnt[t];
+
+  for (int chunk = 0; chunk < tcount; chunk += kEvalThreads * TPT) {
+    float ox[TPT], oy[TPT], oz[TPT], gx[TPT], gy[TPT], gz[TPT];
+    float hi[TPT][NC], lo[TPT][NC];
+    bool act[TPT];
+#pragma unroll
+    for (int j = 0; j < TPT; ++j) {
+      const int k = chunk + threadIdx.x + j * kEvalThreads;
+      act[j] = k < tcount;
+      float4 p = make_float4(0.f, 0.f, 0.f, 0.f), g = p;
+      if (act[j]) {
+        p = A.sp[tstart + k];
+        if (NEED_TG) g = A.sg[tstart + k];
+      }
+      ox[j] = p.x;
+      oy[j] = p.y;
+      oz[j] = p.z;
+      gx[j] = g.x;
+      gy[j] = g.y;
+      gz[j] = g.z;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) hi[j][c] = lo[j][c] = 0.f;
+    }
+    // near field: direct pairs with every near leaf
+    for (int q = 0; q < nnc; ++q) {
+      const int S = A.near_idx[nno + q];
+      const int ss = A.leaf_start[S], sn = A.leaf_count[S];
+      const float3 cS = cell_center_rel(A.leaf_key[S], A.h);
+      const float dcx = cT.x - cS.x, dcy = cT.y - cS.y, dcz = cT.z - cS.z;
+      float tx[TPT], ty[TPT], tz[TPT];
+#pragma unroll
+      for (int j = 0; j < TPT; ++j) {
+        tx[j] = ox[j] + dcx;
+        ty[j] = oy[j] + dcy;
+        tz[j] = oz[j] + dcz;
+      }
+      for (int k0 = 0; k0 < sn; k0 += kNearTile) {
+        const int nt = min(kNearTile, sn - k0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < nt; k += kEvalThreads) {
+          s_p[k] = A.sp[ss + k0 + k];
+          s_a[k] = A.sa[ss + k0 + k];
+        }
+        __syncthreads();
+        float part[TPT][NC];
+#pragma unroll
+        for (int j = 0; j < TPT; ++j)
+#pragma unroll
+          for (int c = 0; c < NC; ++c) part[j][c] = 0.f;
+        for (int k = 0; k < nt; ++k) {
+          const float4 pv = s_p[k];
+          const float4 av = s_a[k];
+#pragma unroll
+          for (int j = 0; j < TPT; ++j) {
+            const float dx = tx[j] - pv.x, dy = ty[j] - pv.y, dz = tz[j] - pv.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            float f, fpr = 0.f;
+            core_f32<KERNEL, NEED_FPR>(r2, pv.w, av.w, f, fpr);
+            accumulate<MODE, float>(part[j], dx, dy, dz, r2, av.x, av.y, av.z, f, fpr, gx[j],
+                                    gy[j], gz[j]);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < TPT; ++j)
+#pragma unroll
+          for (int c = 0; c < NC; ++c) fold(hi[j][c], lo[j][c], part[j][c]);
+      }
+    }
+    // far field: multipole expansions of the accepted cells
+    for (int f0 = 0; f0 < fnc; f0 += kFarTile) {
+      const int nt = min(kFarTile, fnc - f0);
+      __syncthreads();
+      for (int x = threadIdx.x; x < nt * kRecFloats; x += kEvalThreads) {
+        const int c = x / kRecFloats, o = x - c * kRecFloats;
+        s_rec[x] = A.rec[static_cast<int64_t>(A.far_idx[fno + f0 + c]) * kRecFloats + o];
+      }
+      __syncthreads();
+      float part[TPT][NC];
+#pragma unroll
+      for (int j = 0; j < TPT; ++j)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) part[j][c] = 0.f;
+      for (int c = 0; c < nt; ++c) {
+        const float* R = s_rec + c * kRecFloats;
+        const float dcx = cT.x - R[0], dcy = cT.y - R[1], dcz = cT.z - R[2];
+#pragma unroll
+        for (int j = 0; j < TPT; ++j)
+          m2p<MODE>(part[j], R, ox[j] + dcx, oy[j] + dcy, oz[j] + dcz, gx[j], gy[j], gz[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < TPT; ++j)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) fold(hi[j][c], lo[j][c], part[j][c]);
+    }
+#pragma unroll
+    for (int j = 0; j < TPT; ++j) {
+      if (!act[j]) continue;
+      const int i = A.perm[tstart + chunk + threadIdx.x + j * kEvalThreads];
+#pragma unroll
+      for (int c = 0; c < NA; ++c)
+        A.out_a[static_cast<int64_t>(i) * NA + c] =
+            static_cast<double>(hi[j][c]) + static_cast<double>(lo[j][c]);
+#pragma unroll
+      for (int c = NA; c < NC; ++c)
+        A.out_b[static_cast<int64_t>(i) * (NC - NA) + (c - NA)] =
+            static_cast<double>(hi[j][c]) + static_cast<double>(lo[j][c]);
+    }
+  }
+}
+
+}  // namespace tree
+
+// ---- host orchestration --------------------------------------------------------------
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+int grow(DevBuf& b, size_t bytes) {
+  if (bytes <= b.cap) return FVX_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+  size_t c = bytes + bytes / 4 + 4096;
+  FVX_CUDA_TRY(cudaMalloc(&b.p, c));
+  b.cap = c;
+  return FVX_OK;
+}
+
+template <typename T>
+T* P(DevBuf& b, size_t off = 0) {
+  return reinterpret_cast<T*>(static_cast<char*>(b.p) + off);
+}
+
+// Same arithmetic as fluxvortex_gb300/tree_params.py:grid_params.
+void grid_params(const double lo[3], const double hi[3], int64_t n, int leaf_target, int* L_out,
+                 double* h_out, double origin[3]) {
+  double ext[3], emax = 0.0;
+  for (int c = 0; c < 3; ++c) {
+    ext[c] = fmax(hi[c] - lo[c], 1e-12);
+    emax = fmax(emax, ext[c]);
+  }
+  double vol = 1.0;
+  for (int c = 0; c < 3; ++c) vol *= fmax(ext[c], emax * 1e-3);
+  const double h_target = pow(vol * leaf_target / static_cast<double>(n > 0 ? n : 1), 1.0 / 3.0);
+  int e = 0;
+  const double m = frexp(h_target, &e);
+  double h = m < 0.7071067811865476 ? ldexp(1.0, e - 1) : ldexp(1.0, e);
+  int L = 1;
+  for (;;) {
+    double span = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      origin[c] = floor(lo[c] / h) * h;
+      span = fmax(span, hi[c] - origin[c]);
+    }
+    L = 1;
+    while (h * static_cast<double>(1 << L) <= span) ++L;
+    if (L <= 10) break;
+    h *= 2.0;
+  }
+  *L_out = L;
+  *h_out = h;
+}
+
+}  // namespace
+
+}  // namespace fvx
+
+struct fvx_tree {
+  int device = 0;
+  fvx::DevBuf keys0, keys1, idx0, idx1, table, scan_tmp, flags, cid, levels, counts, rec, sp, sa,
+      sg, lists_meta, near_list, far_list, bbox;
+  int64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+namespace fvx {
+namespace {
+
+template <int KERNEL>
+void launch_gather(int n, const int* perm, const int* leaf_of, const uint32_t* leaf_key,
+                   tree::Grid g, const double* pos, const double* alpha, const double* sigma,
+                   const double* tgam, float4* sp, float4* sa, float4* sg, cudaStream_t s) {
+  tree::gather_kernel<KERNEL><<<(n + 255) / 256, 256, 0, s>>>(n, perm, leaf_of, leaf_key, g, pos,
+                                                             alpha, sigma, tgam, sp, sa, sg);
+}
+
+template <int KERNEL>
+void launch_eval(int mode, int nleaf, const tree::EvalArgs& A, cudaStream_t s) {
+  using namespace tree;
+  switch (mode) {
+    case FVX_PAIR_VELOCITY:
+      eval_kernel<FVX_PAIR_VELOCITY, KERNEL><<<nleaf, kEvalThreads, 0, s>>>(A);
+      break;
+    case FVX_PAIR_STRETCH:
+      eval_kernel<FVX_PAIR_STRETCH, KERNEL><<<nleaf, kEvalThreads, 0, s>>>(A);
+      break;
+    case FVX_PAIR_VELOCITY_STRETCH:
+      eval_kernel<FVX_PAIR_VELOCITY_STRETCH, KERNEL><<<nleaf, kEvalThreads, 0, s>>>(A);
+      break;
+    default:
+      eval_kernel<FVX_PAIR_VORTICITY, KERNEL><<<nleaf, kEvalThreads, 0, s>>>(A);
+      break;
+  }
+}
+
+}  // namespace
+
+int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const double* alpha,
+               const double* sigma, const double* tgt_gamma, int64_t n64, double theta,
+               int leaf_target, double* out_a, double* out_b, int64_t* stats, cudaStream_t s) {
+  using namespace tree;
+  FVX_ARG_CHECK(T != nullptr, "null tree handle");
+  FVX_ARG_CHECK(mode == FVX_PAIR_VELOCITY || mode == FVX_PAIR_STRETCH ||
+                    mode == FVX_PAIR_VELOCITY_STRETCH || mode == FVX_PAIR_VORTICITY,
+                "treecode supports the velocity, stretch, velocity+stretch and vorticity sweeps");
+  FVX_ARG_CHECK(kernel == FVX_KERNEL_WINCKELMANS || kernel == FVX_KERNEL_GAUSSIANERF,
+                "unknown kernel %d", kernel);
+  FVX_ARG_CHECK(theta > 0.0 && theta < 1.0 && leaf_target >= 1, "bad theta / leaf size");
+  FVX_ARG_CHECK(n64 >= 0 && n64 <= (int64_t(1) << 22), "treecode supports up to 2^22 particles");
+  const int n = static_cast<int>(n64);
+  if (n == 0) return FVX_OK;
+  const bool need_tg = mode == FVX_PAIR_STRETCH || mode == FVX_PAIR_VELOCITY_STRETCH;
+  FVX_ARG_CHECK(pos && alpha && sigma && out_a && (!need_tg || tgt_gamma) &&
+                    (mode != FVX_PAIR_VELOCITY_STRETCH || out_b),
+                "null array");
+  int rc;
+  // 1. bounding box -> grid
+  const int nbb = 256;
+  if ((rc = grow(T->bbox, sizeof(double) * (6 * nbb + 6)))) return rc;
+  bbox_partial_kernel<<<nbb, 256, 0, s>>>(n, pos, P<double>(T->bbox));
+  FVX_LAUNCH_CHECK();
+  bbox_final_kernel<<<1, 32, 0, s>>>(nbb, P<double>(T->bbox), P<double>(T->bbox) + 6 * nbb);
+  FVX_LAUNCH_CHECK();
+  double lohi[6];
+  FVX_CUDA_TRY(cudaMemcpyAsync(lohi, P<double>(T->bbox) + 6 * nbb, sizeof(lohi),
+                               cudaMemcpyDeviceToHost, s));
+  FVX_CUDA_TRY(cudaStreamSynchronize(s));
+  int L;
+  double h, origin[3];
+  grid_params(lohi, lohi + 3, n, leaf_target, &L, &h, origin);
+  // level capacities and bases
+  int cap[11], base[12];
+  cap[L] = n;
+  for (int l = L - 1; l >= 0; --l) {
+    const int64_t full = int64_t(1) << (3 * l);
+    cap[l] = static_cast<int>(full < cap[l + 1] ? full : cap[l + 1]);
+  }
+  base[0] = 0;
+  for (int l = 0; l <= L; ++l) base[l + 1] = base[l] + cap[l];
+  const int total_cells = base[L + 1];
+  const int nblk = (n + kSortItems - 1) / kSortItems;
+  if ((rc = grow(T->keys0, 4 * size_t(n))) || (rc = grow(T->keys1, 4 * size_t(n))) ||
+      (rc = grow(T->idx0, 4 * size_t(n))) || (rc = grow(T->idx1, 4 * size_t(n))) ||
+      (rc = grow(T->table, 4 * size_t(256) * nblk * 2)) ||
+      (rc = grow(T->scan_tmp, 4 * size_t(2 * kScanBlock))) ||
+      (rc = grow(T->flags, 4 * size_t(n))) || (rc = grow(T->cid, 4 * size_t(n))) ||
+      (rc = grow(T->levels, 4 * size_t(total_cells) * 5)) ||
+      (rc = grow(T->counts, 4 * 16)) ||
+      (rc = grow(T->rec, 4 * size_t(total_cells) * kRecFloats)) ||
+      (rc = grow(T->sp, 16 * size_t(n))) || (rc = grow(T->sa, 16 * size_t(n))) ||
+      (rc = grow(T->sg, 16 * size_t(n))))
+    return rc;
+  // 2. keys + stable radix sort (4 passes: result back in keys0/idx0)
+  keys_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, pos, origin[0], origin[1], origin[2], 1.0 / h, L,
+                                              P<uint32_t>(T->keys0), P<int>(T->idx0));
+  FVX_LAUNCH_CHECK();
+  uint32_t *ka = P<uint32_t>(T->keys0), *kb = P<uint32_t>(T->keys1);
+  int *ia = P<int>(T->idx0), *ib = P<int>(T->idx1);
+  int* table = P<int>(T->table);
+  int* table_ex = table + 256 * nblk;
+  for (int pass = 0; pass < 4; ++pass) {
+    const int shift = 8 * pass;
+    radix_hist_kernel<<<nblk, 256, 0, s>>>(ka, n, shift, nblk, table);
+    FVX_LAUNCH_CHECK();
+    if ((rc = scan_ints(table, 256 * nblk, table_ex, 0, P<int>(T->scan_tmp), s))) return rc;
+    radix_scatter_kernel<<<nblk, 256, 0, s>>>(ka, ia, n, shift, nblk, table_ex, kb, ib);
+    FVX_LAUNCH_CHECK();
+    uint32_t* tk = ka;
+    ka = kb;
+    kb = tk;
+    int* ti = ia;
+    ia = ib;
+    ib = ti;
+  }
+  const uint32_t* keys = ka;  // sorted
+  const int* perm = ia;
+  // 3. cells: leaves from particles, parents from children
+  int* lvb = P<int>(T->levels);
+  auto level = [&](int l) {
+    Level v;
+    v.start = lvb + base[l];
+    v.count = lvb + total_cells + base[l];
+    v.key = reinterpret_cast<uint32_t*>(lvb + 2 * total_cells + base[l]);
+    v.child_lo = lvb + 3 * total_cells + base[l];
+    v.child_hi = lvb + 4 * total_cells + base[l];
+    return v;
+  };
+  int* ncells_d = P<int>(T->counts);
+  int* flag = P<int>(T->flags);
+  int* cid = P<int>(T->cid);
+  flags_kernel<<<(n + 255) / 256, 256, 0, s>>>(keys, nullptr, n, 0, flag);
+  FVX_LAUNCH_CHECK();
+  if ((rc = scan_ints(flag, n, cid, 1, P<int>(T->scan_tmp), s))) return rc;
+  Level leaves = level(L);
+  leaf_cells_kernel<<<(n + 255) / 256, 256, 0, s>>>(keys, n, flag, cid, leaves, ncells_d + L);
+  FVX_LAUNCH_CHECK();
+  cell_counts_kernel<<<(n + 255) / 256, 256, 0, s>>>(leaves, ncells_d + L, n);
+  FVX_LAUNCH_CHECK();
+  // parent levels reuse flag (as flags) and the scan buffer; the leaf ids of
+  // the particles (cid) are kept for the gather
+  int* pflag = P<int>(T->keys1);  // free after the sort
+  int* pid = P<int>(T->idx1);
+  for (int l = L - 1; l >= 0; --l) {
+    Level ch = level(l + 1), par = level(l);
+    const int cc = cap[l + 1];
+    parent_flags_kernel<<<(cc + 255) / 256, 256, 0, s>>>(ch, ncells_d + l + 1, cc, pflag);
+    FVX_LAUNCH_CHECK();
+    if ((rc = scan_ints(pflag, cc, pid, 1, P<int>(T->scan_tmp), s))) return rc;
+    parent_cells_kernel<<<(cc + 255) / 256, 256, 0, s>>>(ch, ncells_d + l + 1, pflag, pid, par,
+                                                         ncells_d + l);
+    FVX_LAUNCH_CHECK();
+    parent_counts_kernel<<<(cap[l] + 255) / 256, 256, 0, s>>>(ch, par, ncells_d + l);
+    FVX_LAUNCH_CHECK();
+  }
+  int ncells[11];
+  FVX_CUDA_TRY(cudaMemcpyAsync(ncells, ncells_d, sizeof(int) * (L + 1), cudaMemcpyDeviceToHost, s));
+  FVX_CUDA_TRY(cudaStreamSynchronize(s));
+  const int nleaf = ncells[L];
+  // 4. sorted FP32 records
+  Grid g{origin[0], origin[1], origin[2], h, L};
+  float4 *sp = P<float4>(T->sp), *sa = P<float4>(T->sa), *sg = P<float4>(T->sg);
+  if (kernel == FVX_KERNEL_WINCKELMANS)
+    launch_gather<FVX_KERNEL_WINCKELMANS>(n, perm, cid, leaves.key, g, pos, alpha, sigma,
+                                          need_tg ? tgt_gamma : nullptr, sp, sa, sg, s);
+  else
+    launch_gather<FVX_KERNEL_GAUSSIANERF>(n, perm, cid, leaves.key, g, pos, alpha, sigma,
+                                          need_tg ? tgt_gamma : nullptr, sp, sa, sg, s);
+  FVX_LAUNCH_CHECK();
+  // 5. moments: leaves, then M2M up the levels
+  float* rec = P<float>(T->rec);
+  leaf_moments_kernel<<<(nleaf * 32 + 255) / 256, 256, 0, s>>>(
+      leaves, ncells_d + L, static_cast<float>(h), sp, sa, rec + int64_t(base[L]) * kRecFloats);
+  FVX_LAUNCH_CHECK();
+  for (int l = L - 1; l >= 0; --l) {
+    const float hl = static_cast<float>(h * static_cast<double>(1 << (L - l)));
+    m2m_kernel<<<(ncells[l] + 127) / 128, 128, 0, s>>>(
+        level(l), ncells_d + l, hl, rec + int64_t(base[l + 1]) * kRecFloats,
+        rec + int64_t(base[l]) * kRecFloats);
+    FVX_LAUNCH_CHECK();
+  }
+  // 6. interaction lists
+  TreeView V;
+  V.L = L;
+  V.h = h;
+  V.mac_k = 0.75 / (theta * theta);
+  for (int l = 0; l <= L + 1 && l < 11; ++l) V.base[l] = base[l];
+  for (int l = 0; l <= L; ++l) V.ncell[l] = ncells[l];
+  V.start = lvb;
+  V.count = lvb + total_cells;
+  V.key = reinterpret_cast<const uint32_t*>(lvb + 2 * total_cells);
+  V.child_lo = lvb + 3 * total_cells;
+  V.child_hi = lvb + 4 * total_cells;
+  if ((rc = grow(T->lists_meta, 4 * size_t(nleaf) * 4 + 64))) return rc;
+  int* near_cnt = P<int>(T->lists_meta);
+  int* far_cnt = near_cnt + nleaf;
+  int* near_off = far_cnt + nleaf;
+  int* far_off = near_off + nleaf;
+  unsigned* ovf = reinterpret_cast<unsigned*>(far_off + nleaf);
+  FVX_CUDA_TRY(cudaMemsetAsync(ovf, 0, 16, s));
+  traverse_kernel<false><<<(nleaf + 127) / 128, 128, 0, s>>>(
+      V, nullptr, nullptr, near_cnt, far_cnt, nullptr, nullptr, 0, 0, ovf);
+  FVX_LAUNCH_CHECK();
+  if ((rc = scan_ints(near_cnt, nleaf, near_off, 0, P<int>(T->scan_tmp), s))) return rc;
+  if ((rc = scan_ints(far_cnt, nleaf, far_off, 0, P<int>(T->scan_tmp), s))) return rc;
+  int tail[4];
+  FVX_CUDA_TRY(cudaMemcpyAsync(&tail[0], near_cnt + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
+  FVX_CUDA_TRY(cudaMemcpyAsync(&tail[1], near_off + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
+  FVX_CUDA_TRY(cudaMemcpyAsync(&tail[2], far_cnt + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
+  FVX_CUDA_TRY(cudaMemcpyAsync(&tail[3], far_off + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
+  FVX_CUDA_TRY(cudaStreamSynchronize(s));
+  const int64_t near_total = int64_t(tail[0]) + tail[1];
+  const int64_t far_total = int64_t(tail[2]) + tail[3];
+  FVX_ARG_CHECK(near_total < (int64_t(1) << 31) && far_total < (int64_t(1) << 31),
+                "interaction lists too long");
+  if ((rc = grow(T->near_list, 4 * size_t(near_total + 1))) ||
+      (rc = grow(T->far_list, 4 * size_t(far_total + 1))))
+    return rc;
+  traverse_kernel<true><<<(nleaf + 127) / 128, 128, 0, s>>>(
+      V, near_off, far_off, nullptr, nullptr, P<int>(T->near_list), P<int>(T->far_list),
+      static_cast<int>(near_total), static_cast<int>(far_total), ovf);
+  FVX_LAUNCH_CHECK();
+  // 7. evaluation
+  EvalArgs A;
+  A.h = static_cast<float>(h);
+  A.leaf_start = leaves.start;
+  A.leaf_count = leaves.count;
+  A.leaf_key = leaves.key;
+  A.near_off = near_off;
+  A.near_cnt = near_cnt;
+  A.near_idx = P<int>(T->near_list);
+  A.far_off = far_off;
+  A.far_cnt = far_cnt;
+  A.far_idx = P<int>(T->far_list);
+  A.rec = rec;
+  A.sp = sp;
+  A.sa = sa;
+  A.sg = sg;
+  A.perm = perm;
+  A.out_a = out_a;
+  A.out_b = out_b;
+  if (kernel == FVX_KERNEL_WINCKELMANS)
+    launch_eval<FVX_KERNEL_WINCKELMANS>(mode, nleaf, A, s);
+  else
+    launch_eval<FVX_KERNEL_GAUSSIANERF>(mode, nleaf, A, s);
+  FVX_LAUNCH_CHECK();
+  unsigned ovf_h = 0;
+  FVX_CUDA_TRY(cudaMemcpyAsync(&ovf_h, ovf, 4, cudaMemcpyDeviceToHost, s));
+  T->stats[0] = L;
+  T->stats[1] = nleaf;
+  T->stats[2] = near_total;
+  T->stats[3] = far_total;
+  T->stats[4] = total_cells;
+  if (stats) {
+    FVX_CUDA_TRY(cudaStreamSynchronize(s));
+    T->stats[5] = ovf_h;
+    for (int k = 0; k < 8; ++k) stats[k] = T->stats[k];
+    FVX_ARG_CHECK(ovf_h == 0, "treecode traversal overflow (code %u)", ovf_h);
+  }
+  return FVX_OK;
+}
+
+}  // namespace fvx
+
+extern "C" {
+
+int fvx_tree_create(fvx_tree** out) {
+  FVX_ARG_CHECK(out != nullptr, "null handle pointer");
+  *out = new fvx_tree();
+  cudaGetDevice(&(*out)->device);
+  return FVX_OK;
+}
+
+void fvx_tree_destroy(fvx_tree* T) {
+  if (!T) return;
+  fvx::DevBuf* bufs[] = {&T->keys0, &T->keys1,      &T->idx0,      &T->idx1,      &T->table,
+                         &T->scan_tmp, &T->flags,   &T->cid,       &T->levels,    &T->counts,
+                         &T->rec,   &T->sp,         &T->sa,        &T->sg,        &T->lists_meta,
+                         &T->near_list, &T->far_list, &T->bbox};
+  for (auto* b : bufs)
+    if (b->p) cudaFree(b->p);
+  delete T;
+}
+
+int fvx_tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const double* alpha,
+                   const double* sigma, const double* tgt_gamma, int64_t n, double theta,
+                   int leaf_target, double* out_a, double* out_b, int64_t* stats, void* stream) {
+  return fvx::tree_sweep(T, mode, kernel, pos, alpha, sigma, tgt_gamma, n, theta, leaf_target,
+                         out_a, out_b, stats, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -166,6 +166,7 @@ class HybridConfig:
     rlxf: float = 0.0
     kernel: str = "winckelmans"
     max_particles: int = 200000
+    far_field: str = None          # None: direct self-sweeps; "tree": treecode
 
     @property
     def speed(self):

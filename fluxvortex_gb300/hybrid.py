@@ -66,7 +66,8 @@ class HybridStep:
         self.v_ring_l, self.v_part_l, self.v_bound_l = z3(P), z3(P), z3(P)
         self.seg_scratch = torch.empty(1, dtype=torch.uint8, device=self.device)
         self.field = VortexParticleField(cfg.max_particles, nu=cfg.nu, rlxf=cfg.rlxf,
-                                         kernel=cfg.kernel, precision=precision, device=device)
+                                         kernel=cfg.kernel, precision=precision, device=device,
+                                         far_field=cfg.far_field)
         self.count = torch.zeros(1, dtype=torch.int64, device=self.device)
         self.u_inf = np.ascontiguousarray(cfg.u_inf, dtype=np.float64)
         self.omega = 2.0 * np.pi / cfg.kin.period

@@ -29,7 +29,8 @@ class VortexParticleField:
     """Structure of FP64 device arrays holding up to ``max_particles`` particles."""
 
     def __init__(self, max_particles=50000, nu=0.0, rlxf=0.3, kernel="gaussianerf",
-                 precision="f64", device="cuda", relax_kernel="gaussianerf"):
+                 precision="f64", device="cuda", relax_kernel="gaussianerf", far_field=None,
+                 theta=0.5, leaf_target=64):
         self.max_particles = int(max_particles)
         self.nu = float(nu)
         self.rlxf = float(rlxf)
@@ -49,6 +50,14 @@ class VortexParticleField:
         # Optional profiling hook: when a list, every sweep appends
         # (mode, kernel, n_targets, n_sources, start_event, end_event).
         self.sweep_events = None
+        # far_field="tree": the self-sweeps (every particle a target) use the
+        # cell-binned treecode; sweeps at other targets stay direct.
+        self.tree = None
+        if far_field == "tree":
+            from .tree import TreeSweeper
+            self.tree = TreeSweeper(theta=theta, leaf_target=leaf_target)
+        elif far_field not in (None, "direct"):
+            raise ValueError(f"unknown far_field {far_field!r}")
 
     # ---- particle management (particles.py:35-66) ----------------------------
     def add_particle(self, X, Gamma, sigma):
@@ -105,6 +114,16 @@ class VortexParticleField:
         if self.sweep_events is not None:
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev[0].record()
+        if (self.tree is not None and tgt is self._pos and n_tgt == n
+                and mode in (_capi.PAIR_VELOCITY, _capi.PAIR_STRETCH,
+                             _capi.PAIR_VELOCITY_STRETCH, _capi.PAIR_VORTICITY)):
+            self.tree.sweep(mode, kernel or self.kernel, self._pos, self._gamma, self._sigma, n,
+                            out_a, out_b, tgt_gamma=tgt_gamma)
+            if ev is not None:
+                ev[1].record()
+                self.sweep_events.append((mode, "tree/" + (kernel or self.kernel), n_tgt, n,
+                                          ev[0], ev[1]))
+            return
         _capi.check(lib.fvx_particle_pairs(
             mode, kid, pid, tgt.data_ptr(), None if tgt_gamma is None else tgt_gamma.data_ptr(),
             n_tgt, self._pos.data_ptr(), self._gamma.data_ptr(), self._sigma.data_ptr(), n,

@@ -181,6 +181,25 @@ int fvx_vpm_finalize(int64_t n, double dt, const double* pos, double* gamma, dou
                      void* stream);
 int fvx_vpm_relax(int64_t n, double rlxf, const double* omega, double* gamma, void* stream);
 
+/* ---- cell-binned treecode for particle self-induction sweeps ----------------------
+ * Approximates fvx_particle_pairs with targets = sources = the n particles
+ * (the self-sweeps of particles.py:122,148,219).  Near leaves: direct FP32
+ * pairs (compensated); accepted cells (|dc|^2 > 3/4 (h_T + h_S)^2/theta^2):
+ * quadrupole expansion of the vector potential, FP32.  Modes VELOCITY,
+ * STRETCH (tgt_gamma = the particles' own strengths), VELOCITY_STRETCH and
+ * VORTICITY.  The handle owns its device workspace (grown on demand) and the
+ * call synchronises `stream` three times (bounding box, cell counts, list
+ * sizes).  stats (host int64[8], may be NULL; also checks traversal overflow):
+ * levels, leaves, near leaf pairs, far cell interactions, cells.  The
+ * reference has no tree (its sweeps are direct); its notes call for one
+ * (docs/phase0A_findings.md:33-35). */
+typedef struct fvx_tree fvx_tree;
+int fvx_tree_create(fvx_tree** tree);
+void fvx_tree_destroy(fvx_tree* tree);
+int fvx_tree_sweep(fvx_tree* tree, int mode, int kernel, const double* pos, const double* alpha,
+                   const double* sigma, const double* tgt_gamma, int64_t n, double theta,
+                   int leaf_target, double* out_a, double* out_b, int64_t* stats, void* stream);
+
 /* ---- panel side of the hybrid panel-particle step (FP64) ------------------------
  * Replaces the PteraSoftware solver stages that HybridSolver runs around the
  * Biot-Savart calls (tests/experiment_hybrid_panel_particle.py:114-204 and the

@@ -1,0 +1,90 @@
+"""Treecode self-sweeps on the GPU.
+
+1. Against the oracle's FP64 restatement of the same algorithm
+   (oracle/treecode.py: same grid, sort, cells, lists, quadrupole far field):
+   differences come from FP32 arithmetic only -> 2e-5 relative.
+2. Against the direct FP64 sum: the approximation error of theta = 0.5 with
+   quadrupole cells -> 1e-3 relative (velocity), 1e-2 (stretching,
+   vorticity: one derivative more).
+3. Degenerate inputs: one particle, fewer particles than a leaf, a planar sheet."""
+import numpy as np
+import pytest
+import torch
+
+from fluxvortex_gb300 import _capi
+from fluxvortex_gb300 import kernel as K
+from fluxvortex_gb300.tree import TreeSweeper
+from fluxvortex_gb300.workloads import slab_wake
+from oracle import treecode as OT
+from tests.conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a, cuda):
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=cuda)
+
+
+def _tree(mode, kernel, pos, gam, sig, cuda, leaf_target, theta=0.5, tg=None):
+    n = pos.shape[0]
+    ts = TreeSweeper(theta=theta, leaf_target=leaf_target)
+    a = torch.empty((n, 3), dtype=torch.float64, device=cuda)
+    b = torch.empty((n, 3), dtype=torch.float64, device=cuda) if mode == 2 else None
+    stats = ts.sweep(mode, kernel, _dev(pos, cuda), _dev(gam, cuda), _dev(sig, cuda), n, a, b,
+                     tgt_gamma=None if tg is None else _dev(tg, cuda), check=True)
+    torch.cuda.synchronize()
+    return a.cpu().numpy(), (None if b is None else b.cpu().numpy()), stats.copy()
+
+
+@pytest.mark.parametrize("kernel", ["winckelmans", "gaussianerf"])
+def test_tree_matches_oracle_algorithm(cuda, kernel):
+    pos, gam, sig, _ = slab_wake(3000, seed=5)
+    tr = OT.build(pos, theta=0.5, leaf_target=16)
+    OT.moments(tr, pos, gam)
+    u, J = OT.evaluate(tr, pos, gam, sig, kernel=kernel)
+    S = np.einsum("tij,tj->ti", J, gam)
+    w = np.stack([J[:, 2, 1] - J[:, 1, 2], J[:, 0, 2] - J[:, 2, 0], J[:, 1, 0] - J[:, 0, 1]], 1)
+    gu, _, st = _tree(_capi.PAIR_VELOCITY, kernel, pos, gam, sig, cuda, 16)
+    assert st[0] == tr["L"] and st[1] == len(tr["levels"][-1]["start"])
+    lst = OT.lists(tr)
+    assert st[2] == sum(len(a) for a, _ in lst) and st[3] == sum(len(b) for _, b in lst)
+    assert rel_err(gu, u) < 2e-5
+    gs, _, _ = _tree(_capi.PAIR_STRETCH, kernel, pos, gam, sig, cuda, 16, tg=gam)
+    assert rel_err(gs, S) < 2e-5
+    gw, _, _ = _tree(_capi.PAIR_VORTICITY, kernel, pos, gam, sig, cuda, 16)
+    assert rel_err(gw, w) < 2e-5
+    ga, gb, _ = _tree(_capi.PAIR_VELOCITY_STRETCH, kernel, pos, gam, sig, cuda, 16, tg=gam)
+    assert rel_err(ga, u) < 2e-5 and rel_err(gb, S) < 2e-5
+
+
+def test_tree_accuracy_vs_direct_fp64(cuda):
+    pos, gam, sig, _ = slab_wake(1 << 16, seed=9)
+    u64, _ = K.particle_pairs(_capi.PAIR_VELOCITY, _dev(pos, cuda), None, _dev(pos, cuda),
+                              _dev(gam, cuda), _dev(sig, cuda), "winckelmans", "f64")
+    s64, _ = K.particle_pairs(_capi.PAIR_STRETCH, _dev(pos, cuda), _dev(gam, cuda),
+                              _dev(pos, cuda), _dev(gam, cuda), _dev(sig, cuda), "winckelmans",
+                              "f64")
+    gu, _, st = _tree(_capi.PAIR_VELOCITY, "winckelmans", pos, gam, sig, cuda, 64)
+    gs, _, _ = _tree(_capi.PAIR_STRETCH, "winckelmans", pos, gam, sig, cuda, 64, tg=gam)
+    assert st[3] > 0 and st[2] > 0
+    assert rel_err(gu, u64.cpu().numpy()) < 1e-3
+    assert rel_err(gs, s64.cpu().numpy()) < 1e-2
+
+
+@pytest.mark.parametrize("case", ["one", "few", "sheet"])
+def test_tree_degenerate_inputs(cuda, case):
+    rng = np.random.default_rng(3)
+    if case == "one":
+        pos = np.array([[0.3, -0.2, 0.1]])
+    elif case == "few":
+        pos = rng.uniform(0, 1, (5, 3))
+    else:
+        pos = np.c_[rng.uniform(0, 4, (4000, 2)), np.full(4000, 0.25)]
+    n = pos.shape[0]
+    gam = rng.normal(0, 1e-3, (n, 3))
+    sig = np.full(n, 0.05)
+    gu, _, _ = _tree(_capi.PAIR_VELOCITY, "winckelmans", pos, gam, sig, cuda, 64)
+    ud, _ = K.particle_pairs(_capi.PAIR_VELOCITY, pos, None, pos, gam, sig, "winckelmans", "f64")
+    assert np.all(np.isfinite(gu))
+    if np.abs(ud).max() > 0:
+        assert rel_err(gu, ud) < 1e-3
