@@ -22,6 +22,7 @@
 // Because cell centres are exact binary fractions, centre differences are
 // exact in FP32 and pair offsets are (c_T - c_S) + (o_t - o_s) with small
 // in-cell offsets o.
+#include <cstring>
 #include <type_traits>
 
 #include "fvx_common.cuh"
@@ -32,7 +33,7 @@ namespace tree {
 
 constexpr int kScanBlock = 2048;   // elements per scan block (1024 threads x 2)
 constexpr int kSortItems = 1024;   // keys per radix-sort block (256 threads x 4)
-constexpr int kEvalThreads = 64;   // eval CTA; 2 targets per thread
+constexpr int kEvalThreads = 32;   // eval CTA (one warp); 2 targets per thread
 constexpr int kFarTile = 32;       // far cells staged per tile
 constexpr int kNearTile = 128;     // source particles staged per tile
 constexpr int kRecFloats = 40;     // far-cell record
@@ -476,6 +477,8 @@ __global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
   int sp = 0;
   for (int c = T.ncell[0] - 1; c >= 0; --c) stack[sp++] = T.base[0] + c;
   int nn = 0, nf = 0;
+  long long near_pairs = 0;
+  const int cT_count = T.count[gT];
   int no = FILL ? near_off[t] : 0, fo = FILL ? far_off[t] : 0;
   while (sp > 0) {
     const int g = stack[--sp];
@@ -495,6 +498,7 @@ __global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
       ++nf;
     } else if (l == T.L) {
       if (FILL && no + nn < near_cap) near_idx[no + nn] = g - T.base[T.L];
+      near_pairs += static_cast<long long>(cT_count) * T.count[g];
       ++nn;
     } else {
       const int lo = T.child_lo[g], hi = T.child_hi[g];
@@ -510,8 +514,12 @@ __global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
   if (!FILL) {
     near_cnt[t] = nn;
     far_cnt[t] = nf;
-  } else if (no + nn > near_cap || fo + nf > far_cap) {
-    atomicOr(overflow, 2u);
+  } else {
+    if (no + nn > near_cap || fo + nf > far_cap) atomicOr(overflow, 2u);
+    // work counters: near particle pairs, far (target particle, cell) pairs
+    unsigned long long* work = reinterpret_cast<unsigned long long*>(overflow + 2);
+    atomicAdd(work, static_cast<unsigned long long>(near_pairs));
+    atomicAdd(work + 1, static_cast<unsigned long long>(cT_count) * nf);
   }
 }
 
@@ -815,6 +823,7 @@ struct fvx_tree {
   fvx::DevBuf keys0, keys1, idx0, idx1, table, scan_tmp, flags, cid, levels, counts, rec, sp, sa,
       sg, lists_meta, near_list, far_list, bbox;
   int64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the last evaluation launch
 };
 
 namespace fvx {
@@ -1009,8 +1018,8 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   int* far_cnt = near_cnt + nleaf;
   int* near_off = far_cnt + nleaf;
   int* far_off = near_off + nleaf;
-  unsigned* ovf = reinterpret_cast<unsigned*>(far_off + nleaf);
-  FVX_CUDA_TRY(cudaMemsetAsync(ovf, 0, 16, s));
+  unsigned* ovf = reinterpret_cast<unsigned*>(far_off + nleaf);  // + 2 x u64 work counters
+  FVX_CUDA_TRY(cudaMemsetAsync(ovf, 0, 24, s));
   traverse_kernel<false><<<(nleaf + 127) / 128, 128, 0, s>>>(
       V, nullptr, nullptr, near_cnt, far_cnt, nullptr, nullptr, 0, 0, ovf);
   FVX_LAUNCH_CHECK();
@@ -1052,13 +1061,19 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   A.perm = perm;
   A.out_a = out_a;
   A.out_b = out_b;
+  if (!T->ev0) {
+    FVX_CUDA_TRY(cudaEventCreate(&T->ev0));
+    FVX_CUDA_TRY(cudaEventCreate(&T->ev1));
+  }
+  FVX_CUDA_TRY(cudaEventRecord(T->ev0, s));
   if (kernel == FVX_KERNEL_WINCKELMANS)
     launch_eval<FVX_KERNEL_WINCKELMANS>(mode, nleaf, A, s);
   else
     launch_eval<FVX_KERNEL_GAUSSIANERF>(mode, nleaf, A, s);
   FVX_LAUNCH_CHECK();
-  unsigned ovf_h = 0;
-  FVX_CUDA_TRY(cudaMemcpyAsync(&ovf_h, ovf, 4, cudaMemcpyDeviceToHost, s));
+  FVX_CUDA_TRY(cudaEventRecord(T->ev1, s));
+  unsigned ovf_h[6] = {0, 0, 0, 0, 0, 0};
+  FVX_CUDA_TRY(cudaMemcpyAsync(ovf_h, ovf, 24, cudaMemcpyDeviceToHost, s));
   T->stats[0] = L;
   T->stats[1] = nleaf;
   T->stats[2] = near_total;
@@ -1066,9 +1081,13 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   T->stats[4] = total_cells;
   if (stats) {
     FVX_CUDA_TRY(cudaStreamSynchronize(s));
-    T->stats[5] = ovf_h;
+    unsigned long long work[2];
+    memcpy(work, ovf_h + 2, sizeof(work));
+    T->stats[5] = ovf_h[0];
+    T->stats[6] = static_cast<int64_t>(work[0]);
+    T->stats[7] = static_cast<int64_t>(work[1]);
     for (int k = 0; k < 8; ++k) stats[k] = T->stats[k];
-    FVX_ARG_CHECK(ovf_h == 0, "treecode traversal overflow (code %u)", ovf_h);
+    FVX_ARG_CHECK(ovf_h[0] == 0, "treecode traversal overflow (code %u)", ovf_h[0]);
   }
   return FVX_OK;
 }
@@ -1086,6 +1105,8 @@ int fvx_tree_create(fvx_tree** out) {
 
 void fvx_tree_destroy(fvx_tree* T) {
   if (!T) return;
+  if (T->ev0) cudaEventDestroy(T->ev0);
+  if (T->ev1) cudaEventDestroy(T->ev1);
   fvx::DevBuf* bufs[] = {&T->keys0, &T->keys1,      &T->idx0,      &T->idx1,      &T->table,
                          &T->scan_tmp, &T->flags,   &T->cid,       &T->levels,    &T->counts,
                          &T->rec,   &T->sp,         &T->sa,        &T->sg,        &T->lists_meta,
@@ -1100,6 +1121,15 @@ int fvx_tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const d
                    int leaf_target, double* out_a, double* out_b, int64_t* stats, void* stream) {
   return fvx::tree_sweep(T, mode, kernel, pos, alpha, sigma, tgt_gamma, n, theta, leaf_target,
                          out_a, out_b, stats, static_cast<cudaStream_t>(stream));
+}
+
+int fvx_tree_last_eval_ms(fvx_tree* T, float* ms) {
+  FVX_ARG_CHECK(T && ms, "null argument");
+  *ms = 0.f;
+  if (!T->ev0) return FVX_OK;
+  FVX_CUDA_TRY(cudaEventSynchronize(T->ev1));
+  FVX_CUDA_TRY(cudaEventElapsedTime(ms, T->ev0, T->ev1));
+  return FVX_OK;
 }
 
 }  // extern "C"

@@ -50,6 +50,7 @@ class VortexParticleField:
         # Optional profiling hook: when a list, every sweep appends
         # (mode, kernel, n_targets, n_sources, start_event, end_event).
         self.sweep_events = None
+        self.tree_events = []     # (mode, kernel, stats, eval_ms) when profiling
         # far_field="tree": the self-sweeps (every particle a target) use the
         # cell-binned treecode; sweeps at other targets stay direct.
         self.tree = None
@@ -117,12 +118,15 @@ class VortexParticleField:
         if (self.tree is not None and tgt is self._pos and n_tgt == n
                 and mode in (_capi.PAIR_VELOCITY, _capi.PAIR_STRETCH,
                              _capi.PAIR_VELOCITY_STRETCH, _capi.PAIR_VORTICITY)):
-            self.tree.sweep(mode, kernel or self.kernel, self._pos, self._gamma, self._sigma, n,
-                            out_a, out_b, tgt_gamma=tgt_gamma)
+            stats = self.tree.sweep(mode, kernel or self.kernel, self._pos, self._gamma,
+                                    self._sigma, n, out_a, out_b, tgt_gamma=tgt_gamma,
+                                    check=ev is not None)
             if ev is not None:
                 ev[1].record()
                 self.sweep_events.append((mode, "tree/" + (kernel or self.kernel), n_tgt, n,
                                           ev[0], ev[1]))
+                self.tree_events.append((mode, kernel or self.kernel, stats.copy(),
+                                         self.tree.last_eval_ms()))
             return
         _capi.check(lib.fvx_particle_pairs(
             mode, kid, pid, tgt.data_ptr(), None if tgt_gamma is None else tgt_gamma.data_ptr(),

@@ -48,3 +48,8 @@ class TreeSweeper:
             self.theta, self.leaf_target, out_a.data_ptr(),
             None if out_b is None else out_b.data_ptr(), stats, st))
         return self.stats
+
+    def last_eval_ms(self):
+        ms = ctypes.c_float(0.0)
+        _capi.check(self.lib.fvx_tree_last_eval_ms(self.handle, ctypes.byref(ms)))
+        return float(ms.value)

@@ -199,6 +199,9 @@ void fvx_tree_destroy(fvx_tree* tree);
 int fvx_tree_sweep(fvx_tree* tree, int mode, int kernel, const double* pos, const double* alpha,
                    const double* sigma, const double* tgt_gamma, int64_t n, double theta,
                    int leaf_target, double* out_a, double* out_b, int64_t* stats, void* stream);
+/* Device time of the last sweep's evaluation kernel (waits for it).  stats
+ * of the same sweep: [6] near particle pairs, [7] far (target, cell) pairs. */
+int fvx_tree_last_eval_ms(fvx_tree* tree, float* ms);
 
 /* ---- panel side of the hybrid panel-particle step (FP64) ------------------------
  * Replaces the PteraSoftware solver stages that HybridSolver runs around the
