@@ -52,6 +52,8 @@ SIGNATURES = {
     "fvx_tree_destroy": (None, [P]),
     "fvx_tree_sweep": (I32, [P, I32, I32, P, P, P, P, I64, D, I32, P, P, P, P]),
     "fvx_tree_last_eval_ms": (I32, [P, P]),
+    "fvx_mlp_forward": (I32, [P, I32, P, P, P, P, P, I32, P]),
+    "fvx_tc_gemm_probe": (I32, [P, P, I32, I32, P, I32, P]),
     "fvx_uvlm_kinematics": (I32, [I64, P, D, D, D, D, D, P, P]),
     "fvx_uvlm_lattice": (I32, [P, I32, I32, P, P, P, P, P, P, P, P, P, P, P]),
     "fvx_uvlm_aic": (I32, [I32, I32, P, P, P, P, P, P, D, D, P, P]),

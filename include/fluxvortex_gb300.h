@@ -262,6 +262,20 @@ int fvx_uvlm_convert(int R, int n_keep, int ns, const double* W, const double* g
                      int sigma_rule, double sigma_vdt, int64_t capacity, int64_t* count,
                      double* pos, double* alpha, double* sigma, double* age, void* stream);
 
+/* ---- learned far-field operator: BF16 tensor-core MLP (tcgen05) ---------------
+ * 48 inputs -> 3 x 128 SiLU -> 16 outputs; W packed [out][in] BF16 (W1 128x48,
+ * W2 128x128, W3 128x128, W4 16x128), bias packed FP32 (3 x 128 + 16).
+ * fvx_mlp_forward: Y[rows][16] FP32 from X[rows][48] BF16; z_store
+ * (3 x rows x 128 FP32) and h_store (3 x rows x 128 BF16), if not NULL,
+ * receive the hidden pre-activations and activations for training.
+ * stride_mode selects the descriptor stride convention (0 in production).
+ * fvx_tc_gemm_probe: C[128][N] = A[128][K] B[N][K]^T on one CTA (layout check).
+ * No reference counterpart (the operator is new). */
+int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, float* Y,
+                    float* z_store, void* h_store, int stride_mode, void* stream);
+int fvx_tc_gemm_probe(const void* A, const void* B, int N, int K, float* C, int stride_mode,
+                      void* stream);
+
 /* ---- diagnostics -------------------------------------------------------------
  * Launches blocks_per_sm x SMs CTAs of 256 threads, each running `iters`
  * rounds of 8 independent FP32 FMAs (16 flop per round per thread): the
