@@ -16,6 +16,7 @@ P = ctypes.c_void_p
 I64 = ctypes.c_int64
 I32 = ctypes.c_int
 D = ctypes.c_double
+F = ctypes.c_float
 SZ = ctypes.c_size_t
 
 FVX_OK, FVX_ERR_ARG, FVX_ERR_CUDA, FVX_ERR_CAPACITY, FVX_ERR_TIMEOUT, FVX_ERR_SCRATCH = range(6)
@@ -52,7 +53,14 @@ SIGNATURES = {
     "fvx_tree_destroy": (None, [P]),
     "fvx_tree_sweep": (I32, [P, I32, I32, P, P, P, P, I64, D, I32, P, P, P, P]),
     "fvx_tree_last_eval_ms": (I32, [P, P]),
-    "fvx_mlp_forward": (I32, [P, I32, P, P, P, P, P, I32, P]),
+    "fvx_tree_set_learned": (I32, [P, P, P, D]),
+    "fvx_tree_sample_pairs": (I32, [P, I32, P, P, P, P]),
+    "fvx_mlp_forward": (I32, [P, I32, P, P, P, P, P, P]),
+    "fvx_mlp_gemm": (I32, [P, I32, I32, P, I32, I32, P, I32, I32, I32, I32, I32, I32, P]),
+    "fvx_mlp_loss_grad": (I32, [I32, P, P, P, P, P, P]),
+    "fvx_mlp_silu_back": (I32, [I32, I32, P, P, P, P, P]),
+    "fvx_mlp_colsum": (I32, [I32, I32, P, P, P]),
+    "fvx_mlp_adam": (I32, [I32, P, P, P, P, P, F, F, F, F, I32, P]),
     "fvx_tc_gemm_probe": (I32, [P, P, I32, I32, P, I32, P]),
     "fvx_uvlm_kinematics": (I32, [I64, P, D, D, D, D, D, P, P]),
     "fvx_uvlm_lattice": (I32, [P, I32, I32, P, P, P, P, P, P, P, P, P, P, P]),

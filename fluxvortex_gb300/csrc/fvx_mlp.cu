@@ -1,15 +1,22 @@
 // fvx_mlp.cu -- BF16 tensor-core MLP of the learned far-field operator.
 //
 // Network: 48 inputs (35 features, zero padded) -> 3 x 128 hidden (SiLU) ->
-// 16 outputs (12 used), weights [out][in] in BF16 with FP32 master copies,
-// FP32 biases.  Inference and training run on tcgen05 (fvx_tc.cuh): one CTA
-// of 128 threads takes 128-row tiles (persistent over the tiles), keeps all
-// weights in shared memory in the K-major canonical layout, and chains the
-// four layers through tensor memory: MMA into TMEM -> tcgen05.ld -> bias +
-// SiLU in registers -> BF16 back into the shared activation tile -> next MMA.
-// The backward pass uses the same machinery for dX = dZ W (weights staged
-// transposed) and dW = dZ^T X (operands staged transposed, one MMA chain per
-// 128-row tile, partial dW accumulated across CTAs with FP32 atomics).
+// 32 outputs (30 used), weights [out][in] in BF16 with FP32 master copies,
+// FP32 biases.  Inference and training run on tcgen05 (fvx_tc.cuh):
+//   * forward: one CTA of 128 threads per 128-row tile (persistent over the
+//     tiles) keeps all weights in shared memory in the K-major canonical
+//     layout and chains the four layers through tensor memory: MMA into TMEM
+//     -> tcgen05.ld -> bias + SiLU in registers -> BF16 back into the shared
+//     activation tile -> next MMA.  Two input/output policies: plain rows
+//     (X -> Y, with the hidden pre-activations / activations kept for
+//     training), and the treecode's learned far field (features computed
+//     in-kernel from the (target leaf, source cell) pair list, outputs scaled
+//     back to physical local-expansion coefficients and added to the leaf's
+//     local expansion);
+//   * training: a generic tile GEMM C = op(A) op(B)^T on tcgen05 (operands
+//     staged transposed as needed by the threads, split over K with FP32
+//     atomics) for dW = dZ^T H and dH = dZ W, plus element-wise kernels for
+//     the loss gradient, the SiLU backward with bias gradients, and Adam.
 #include <cuda_bf16.h>
 
 #include "fvx_common.cuh"
@@ -18,13 +25,14 @@
 namespace fvx {
 namespace mlp {
 
-constexpr int IN = 48, H = 128, OUT = 16;
+constexpr int IN = 48, H = 128, OUT = 32, NFEAT = 35, NOUT = 30;
 constexpr int kThreads = 128;
 // packed BF16 weight offsets (elements)
 constexpr int W1o = 0, W2o = W1o + H * IN, W3o = W2o + H * H, W4o = W3o + H * H,
               WN = W4o + OUT * H;
 // packed bias offsets
 constexpr int B1o = 0, B2o = H, B3o = 2 * H, B4o = 3 * H, BN = 3 * H + OUT;
+constexpr int kRecFloats = 40;  // treecode cell record (fvx_tree.cu)
 
 struct FwdSmem {
   __nv_bfloat16 w1[H * IN];
@@ -38,6 +46,10 @@ struct FwdSmem {
 };
 
 __device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float silu_grad(float z) {
+  const float s = 1.f / (1.f + __expf(-z));
+  return s * (1.f + z * (1.f - s));
+}
 
 // Copies a row-major [R][K] BF16 matrix into the K-major canonical layout.
 __device__ void stage_kmajor(__nv_bfloat16* dst, const __nv_bfloat16* src, int R, int K) {
@@ -49,9 +61,85 @@ __device__ void stage_kmajor(__nv_bfloat16* dst, const __nv_bfloat16* src, int R
   }
 }
 
-// this thread's row of a 128 x H accumulator -> bias + SiLU -> BF16 act tile;
-// optionally keeps the pre-activation (FP32) and activation (BF16) rows
-__device__ void epilogue_hidden(uint32_t tmem, const float* bias, __nv_bfloat16* act, int row,
+// ---- features of a (target leaf, source cell) pair -----------------------------
+// R = c_T - c_S, d = |R|; m = |M0| + |M1| / h_S + |M2| / h_S^2 (Frobenius);
+// f = [R/d, h_S/d, h_T/d, M0/m, M1/(m h_S), M2/(m h_S^2) (6 unique per row)];
+// the network's outputs are u d^2/m, J d^3/m, H d^4/m (local expansion at c_T).
+struct PairScale {
+  float s2, s3, s4;  // m/d^2, m/d^3, m/d^4
+};
+
+__device__ __forceinline__ PairScale pair_features(const float* rec, float cTx, float cTy,
+                                                   float cTz, float hT, float* f) {
+  const float Rx = cTx - rec[0], Ry = cTy - rec[1], Rz = cTz - rec[2];
+  const float d2 = Rx * Rx + Ry * Ry + Rz * Rz;
+  const float id = rsqrtf(d2);
+  const float hS = rec[3];
+  float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+  for (int q = 0; q < 3; ++q) n0 += rec[4 + q] * rec[4 + q];
+  for (int q = 0; q < 9; ++q) n1 += rec[10 + q] * rec[10 + q];
+  for (int m = 0; m < 3; ++m) {
+    const float* Q = rec + 19 + 6 * m;
+    n2 += Q[0] * Q[0] + Q[3] * Q[3] + Q[5] * Q[5] + 2.f * (Q[1] * Q[1] + Q[2] * Q[2] + Q[4] * Q[4]);
+  }
+  const float ih = 1.f / hS;
+  const float m = sqrtf(n0) + sqrtf(n1) * ih + sqrtf(n2) * ih * ih + 1e-30f;
+  const float im = 1.f / m;
+  f[0] = Rx * id;
+  f[1] = Ry * id;
+  f[2] = Rz * id;
+  f[3] = hS * id;
+  f[4] = hT * id;
+  for (int q = 0; q < 3; ++q) f[5 + q] = rec[4 + q] * im;
+  for (int q = 0; q < 9; ++q) f[8 + q] = rec[10 + q] * im * ih;
+  for (int q = 0; q < 18; ++q) f[17 + q] = rec[19 + q] * im * ih * ih;
+  for (int q = NFEAT; q < IN; ++q) f[q] = 0.f;
+  PairScale s;
+  s.s2 = m * id * id;
+  s.s3 = s.s2 * id;
+  s.s4 = s.s3 * id;
+  return s;
+}
+
+__device__ __forceinline__ float3 leaf_center(uint32_t key, float h) {
+  auto compact = [](uint32_t v) {
+    v &= 0x09249249u;
+    v = (v | (v >> 2)) & 0x030C30C3u;
+    v = (v | (v >> 4)) & 0x0300F00Fu;
+    v = (v | (v >> 8)) & 0x030000FFu;
+    v = (v | (v >> 16)) & 0x000003FFu;
+    return v;
+  };
+  return make_float3((static_cast<float>(compact(key)) + 0.5f) * h,
+                     (static_cast<float>(compact(key >> 1)) + 0.5f) * h,
+                     (static_cast<float>(compact(key >> 2)) + 0.5f) * h);
+}
+
+// ---- forward policies --------------------------------------------------------------
+struct RowsIO {
+  const __nv_bfloat16* X;
+  float* Y;
+  float* z_store;
+  __nv_bfloat16* h_store;
+};
+
+struct FarIO {
+  const int* pair_leaf;    // leaf id of each learned pair
+  const int* pair_cell;    // global cell id of each learned pair
+  const uint32_t* leaf_key;
+  const float* rec;        // cell records
+  float h;                 // leaf size
+  float* leaf_local;       // [n_leaves][32] local expansions (accumulated)
+};
+
+template <bool FAR>
+struct FwdArgs {
+  RowsIO r;
+  FarIO f;
+};
+
+// this thread's row of a 128 x H accumulator -> bias + SiLU -> BF16 act tile
+__device__ void epilogue_hidden(uint32_t tmem, const float* bias, __nv_bfloat16* act,
                                 float* z_out, __nv_bfloat16* h_out) {
   const int warp = threadIdx.x >> 5;
   const uint32_t lane_base = static_cast<uint32_t>(32 * (warp & 3)) << 16;
@@ -75,10 +163,8 @@ __device__ void epilogue_hidden(uint32_t tmem, const float* bias, __nv_bfloat16*
       *reinterpret_cast<uint4*>(h_out + c0 + 8) = *reinterpret_cast<uint4*>(&b[8]);
     }
   }
-  (void)row;
 }
 
-// Waits for the MMA chain committed to `bar` (phase `ph`), bounded.
 __device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& ph) {
   const bool ok = mbar_wait(bar, ph);
   ph ^= 1u;
@@ -86,11 +172,10 @@ __device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& ph) {
   return ok;
 }
 
-// Y[rows][16] = MLP(X[rows][48]); with z/h stores for training.
-__global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(
-    const __nv_bfloat16* __restrict__ X, int rows, const __nv_bfloat16* __restrict__ W,
-    const float* __restrict__ bias, float* __restrict__ Y, float* __restrict__ z_store,
-    __nv_bfloat16* __restrict__ h_store, int stride_mode) {
+template <bool FAR>
+__global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int rows,
+                                                           const __nv_bfloat16* __restrict__ W,
+                                                           const float* __restrict__ bias) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   FwdSmem& S = *reinterpret_cast<FwdSmem*>(smem_raw);
   if (threadIdx.x < 32) tc::tmem_alloc(&S.tmem, 128);
@@ -108,20 +193,41 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = S.tmem;
+  const uint32_t lane_base = static_cast<uint32_t>(32 * ((threadIdx.x >> 5) & 3)) << 16;
   uint32_t ph = 0;
   bool ok = true;
   const int ntiles = (rows + 127) / 128;
   for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int row = tile * 128 + threadIdx.x;
     const bool act_row = row < rows;
+    PairScale sc{0.f, 0.f, 0.f};
+    int leaf = 0;
     // input tile (K = 48)
     {
       char* base = reinterpret_cast<char*>(S.act);
-      for (int k8 = 0; k8 < IN / 8; ++k8) {
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (act_row)
-          v = *reinterpret_cast<const uint4*>(X + static_cast<int64_t>(row) * IN + 8 * k8);
-        *reinterpret_cast<uint4*>(base + tc::kmajor_offset(threadIdx.x, 8 * k8, IN)) = v;
+      if constexpr (FAR) {
+        float f[IN];
+        if (act_row) {
+          leaf = A.f.pair_leaf[row];
+          const float3 cT = leaf_center(A.f.leaf_key[leaf], A.f.h);
+          sc = pair_features(A.f.rec + static_cast<int64_t>(A.f.pair_cell[row]) * kRecFloats,
+                             cT.x, cT.y, cT.z, A.f.h, f);
+        } else {
+          for (int q = 0; q < IN; ++q) f[q] = 0.f;
+        }
+        for (int k8 = 0; k8 < IN / 8; ++k8) {
+          __align__(16) __nv_bfloat16 b[8];
+          for (int q = 0; q < 8; ++q) b[q] = __float2bfloat16(f[8 * k8 + q]);
+          *reinterpret_cast<uint4*>(base + tc::kmajor_offset(threadIdx.x, 8 * k8, IN)) =
+              *reinterpret_cast<uint4*>(b);
+        }
+      } else {
+        for (int k8 = 0; k8 < IN / 8; ++k8) {
+          uint4 v = make_uint4(0, 0, 0, 0);
+          if (act_row)
+            v = *reinterpret_cast<const uint4*>(A.r.X + static_cast<int64_t>(row) * IN + 8 * k8);
+          *reinterpret_cast<uint4*>(base + tc::kmajor_offset(threadIdx.x, 8 * k8, IN)) = v;
+        }
       }
     }
     const __nv_bfloat16* wl[3] = {S.w1, S.w2, S.w3};
@@ -132,38 +238,69 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(
       tc::fence_after_sync();
       if (threadIdx.x == 0)
         tc::gemm_issue(tmem, S.act, wl[l], l == 0 ? IN : H, tc::idesc_bf16(128, H), false,
-                       &S.bar, stride_mode);
+                       &S.bar, 0);
       if (!__syncthreads_and(wait_mma(&S.bar, ph))) {
         ok = false;
         break;
       }
-      epilogue_hidden(tmem, S.bias + l * H, S.act, row,
-                      (z_store && act_row) ? z_store + (static_cast<int64_t>(l) * rows + row) * H
-                                           : nullptr,
-                      (h_store && act_row) ? h_store + (static_cast<int64_t>(l) * rows + row) * H
-                                           : nullptr);
+      float* zo = nullptr;
+      __nv_bfloat16* ho = nullptr;
+      if constexpr (!FAR) {
+        if (A.r.z_store && act_row) zo = A.r.z_store + (static_cast<int64_t>(l) * rows + row) * H;
+        if (A.r.h_store && act_row) ho = A.r.h_store + (static_cast<int64_t>(l) * rows + row) * H;
+      }
+      epilogue_hidden(tmem, S.bias + l * H, S.act, zo, ho);
     }
     if (!ok) break;
-    // output layer (N = 16)
     tc::fence_smem_to_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     if (threadIdx.x == 0)
-      tc::gemm_issue(tmem, S.act, S.w4, H, tc::idesc_bf16(128, OUT), false, &S.bar, stride_mode);
+      tc::gemm_issue(tmem, S.act, S.w4, H, tc::idesc_bf16(128, OUT), false, &S.bar, 0);
     if (!__syncthreads_and(wait_mma(&S.bar, ph))) {
       ok = false;
       break;
     }
-    float v[16];
-    tc::tmem_ld16(tmem + (static_cast<uint32_t>(32 * ((threadIdx.x >> 5) & 3)) << 16), v);
-    if (act_row) {
-      float4* y = reinterpret_cast<float4*>(Y + static_cast<int64_t>(row) * OUT);
+    for (int c0 = 0; c0 < OUT; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(tmem + lane_base + c0, v);
+      if constexpr (FAR) {
+        // pairs are ordered by leaf: reduce each run of equal leaves inside
+        // the warp to its first lane, which adds it to the leaf's expansion
+        const int lane = threadIdx.x & 31;
+        const int my = act_row ? leaf : -1 - lane;
+        const int up = __shfl_up_sync(0xffffffffu, my, 1);
+        const bool head = act_row && (lane == 0 || up != my);
+        float* L = act_row ? A.f.leaf_local + static_cast<int64_t>(leaf) * OUT : nullptr;
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
-        y[q] = make_float4(v[4 * q] + S.bias[B4o + 4 * q], v[4 * q + 1] + S.bias[B4o + 4 * q + 1],
-                           v[4 * q + 2] + S.bias[B4o + 4 * q + 2],
-                           v[4 * q + 3] + S.bias[B4o + 4 * q + 3]);
+        for (int i = 0; i < 16; ++i) {
+          const int c = c0 + i;
+          float x = 0.f;
+          if (act_row && c < NOUT) {
+            const float s = c < 3 ? sc.s2 : (c < 12 ? sc.s3 : sc.s4);
+            x = (v[i] + S.bias[B4o + c]) * s;
+          }
+#pragma unroll
+          for (int off = 1; off < 32; off <<= 1) {
+            const float o = __shfl_down_sync(0xffffffffu, x, off);
+            const int ol = __shfl_down_sync(0xffffffffu, my, off);
+            if (lane + off < 32 && ol == my) x += o;
+          }
+          if (head && c < NOUT) atomicAdd(L + c, x);
+        }
+        continue;
+      }
+      if (!act_row) continue;
+      {
+        float4* y = reinterpret_cast<float4*>(A.r.Y + static_cast<int64_t>(row) * OUT + c0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          y[q] = make_float4(v[4 * q] + S.bias[B4o + c0 + 4 * q],
+                             v[4 * q + 1] + S.bias[B4o + c0 + 4 * q + 1],
+                             v[4 * q + 2] + S.bias[B4o + c0 + 4 * q + 2],
+                             v[4 * q + 3] + S.bias[B4o + c0 + 4 * q + 3]);
+      }
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -173,6 +310,222 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(
   tc::fence_before_sync();
   __syncthreads();
   if (threadIdx.x < 32) tc::tmem_dealloc(tmem, 128);
+}
+
+// ---- training data: features + exact local expansions of sampled pairs ----------
+// One warp per pair: FP64 direct sums over the source cell's particles of the
+// singular Biot-Savart field and its first two derivatives at c_T.
+__global__ void pair_targets_kernel(int npairs, int stride, const int* __restrict__ pair_leaf,
+                                    const int* __restrict__ pair_cell,
+                                    const uint32_t* __restrict__ leaf_key,
+                                    const float* __restrict__ rec, const int* __restrict__ cell_start,
+                                    const int* __restrict__ cell_count,
+                                    const float4* __restrict__ sp, const float4* __restrict__ sa,
+                                    const int* __restrict__ leaf_of_particle, float h,
+                                    __nv_bfloat16* __restrict__ X, float* __restrict__ T) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= npairs) return;
+  const int t = pair_leaf[static_cast<int64_t>(warp) * stride],
+            g = pair_cell[static_cast<int64_t>(warp) * stride];
+  const float3 cT = leaf_center(leaf_key[t], h);
+  double acc[NOUT];
+#pragma unroll
+  for (int q = 0; q < NOUT; ++q) acc[q] = 0.0;
+  const int s0 = cell_start[g], n = cell_count[g];
+  for (int i = s0 + lane; i < s0 + n; i += 32) {
+    const float3 cs = leaf_center(leaf_key[leaf_of_particle[i] - 1], h);
+    const float4 p = sp[i];
+    const float4 a = sa[i];
+    const double d[3] = {static_cast<double>(cT.x - cs.x) - p.x,
+                         static_cast<double>(cT.y - cs.y) - p.y,
+                         static_cast<double>(cT.z - cs.z) - p.z};
+    const double al[3] = {a.x, a.y, a.z};
+    const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const double ir = rsqrt(r2), ir2 = ir * ir;
+    const double f = ir2 * ir, fpr = -3.0 * f * ir2, fpp = 15.0 * f * ir2 * ir2;
+    const double c[3] = {d[1] * al[2] - d[2] * al[1], d[2] * al[0] - d[0] * al[2],
+                         d[0] * al[1] - d[1] * al[0]};
+    // eps_inm a_m as a matrix E[i][n]
+    const double E[3][3] = {{0.0, al[2], -al[1]}, {-al[2], 0.0, al[0]}, {al[1], -al[0], 0.0}};
+    for (int i2 = 0; i2 < 3; ++i2) {
+      acc[i2] += f * c[i2];
+      for (int n2 = 0; n2 < 3; ++n2) acc[3 + 3 * i2 + n2] += fpr * d[n2] * c[i2] + f * E[i2][n2];
+      int u = 0;
+      for (int k = 0; k < 3; ++k)
+        for (int m = k; m < 3; ++m, ++u) {
+          const double v = (fpp * d[k] * d[m] + (k == m ? fpr : 0.0)) * c[i2] +
+                           fpr * d[m] * E[i2][k] + fpr * d[k] * E[i2][m];
+          acc[12 + 6 * i2 + u] += v;
+        }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NOUT; ++q)
+    for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+  if (lane == 0) {
+    float f[IN];
+    const PairScale sc =
+        pair_features(rec + static_cast<int64_t>(g) * kRecFloats, cT.x, cT.y, cT.z, h, f);
+    for (int q = 0; q < IN; ++q) X[static_cast<int64_t>(warp) * IN + q] = __float2bfloat16(f[q]);
+    for (int q = 0; q < OUT; ++q) {
+      float v = 0.f;
+      if (q < NOUT) {
+        const double s = q < 3 ? sc.s2 : (q < 12 ? sc.s3 : sc.s4);
+        v = static_cast<float>(acc[q] / s);
+      }
+      T[static_cast<int64_t>(warp) * OUT + q] = v;
+    }
+  }
+}
+
+// ---- generic tile GEMM for training: C[M][N] (+)= sum_k opA[m][k] opB[n][k] -------
+// opA[m][k] = tA ? A[k*lda + m] : A[m*lda + k]; same for B.  Grid (M/128, N/128,
+// splitK); each CTA runs its K range in chunks of 128 through TMEM and adds its
+// partial into C with FP32 atomics (C must be zeroed when accumulating).
+struct GemmSmem {
+  __nv_bfloat16 a[128 * 128];
+  __nv_bfloat16 b[128 * 128];
+  uint64_t bar;
+  uint32_t tmem;
+};
+
+__global__ void __launch_bounds__(128) gemm_tn_kernel(const __nv_bfloat16* __restrict__ A, int lda,
+                                                      int tA, const __nv_bfloat16* __restrict__ B,
+                                                      int ldb, int tB, float* __restrict__ C,
+                                                      int ldc, int M, int N, int K, int kchunk,
+                                                      int atomic) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  GemmSmem& S = *reinterpret_cast<GemmSmem*>(smem_raw);
+  if (threadIdx.x < 32) tc::tmem_alloc(&S.tmem, 128);
+  if (threadIdx.x == 0) {
+    mbar_init(&S.bar, 1);
+    fence_mbar_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = S.tmem;
+  const int m0 = blockIdx.x * 128, n0 = blockIdx.y * 128;
+  const int nt = min(128, N - n0);
+  const int nt16 = (nt + 15) & ~15;
+  const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+  uint32_t ph = 0;
+  bool ok = true, any = false;
+  for (int k0 = kb; k0 < ke; k0 += 128) {
+    const int kc = min(128, ke - k0);
+    const int kc16 = (kc + 15) & ~15;
+    // stage op(A)[m0 .. m0+128][k0 .. k0+kc16] and op(B)[n0 .. n0+nt16][...]
+    for (int e = threadIdx.x; e < 128 * kc16; e += blockDim.x) {
+      const int r = tA ? e % 128 : e / kc16, k = tA ? e / 128 : e % kc16;
+      const int gm = m0 + r, gk = k0 + k;
+      __nv_bfloat16 v = __float2bfloat16(0.f);
+      if (gm < M && k < kc) v = tA ? A[static_cast<int64_t>(gk) * lda + gm] : A[static_cast<int64_t>(gm) * lda + gk];
+      *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(S.a) + tc::kmajor_offset(r, k, kc16)) = v;
+    }
+    for (int e = threadIdx.x; e < nt16 * kc16; e += blockDim.x) {
+      const int r = tB ? e % nt16 : e / kc16, k = tB ? e / nt16 : e % kc16;
+      const int gn = n0 + r, gk = k0 + k;
+      __nv_bfloat16 v = __float2bfloat16(0.f);
+      if (r < nt && k < kc) v = tB ? B[static_cast<int64_t>(gk) * ldb + gn] : B[static_cast<int64_t>(gn) * ldb + gk];
+      *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<char*>(S.b) + tc::kmajor_offset(r, k, kc16)) = v;
+    }
+    tc::fence_smem_to_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (threadIdx.x == 0)
+      tc::gemm_issue(tmem, S.a, S.b, kc16, tc::idesc_bf16(128, nt16), any, &S.bar, 0);
+    any = true;
+    if (!__syncthreads_and(wait_mma(&S.bar, ph))) {
+      ok = false;
+      break;
+    }
+  }
+  if (ok && any) {
+    const uint32_t lb = static_cast<uint32_t>(32 * ((threadIdx.x >> 5) & 3)) << 16;
+    const int gm = m0 + threadIdx.x;
+    for (int c0 = 0; c0 < nt16; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(tmem + lb + c0, v);
+      if (gm >= M) continue;
+      for (int i = 0; i < 16; ++i) {
+        const int gn = n0 + c0 + i;
+        if (c0 + i >= nt) break;
+        float* p = C + static_cast<int64_t>(gm) * ldc + gn;
+        if (atomic)
+          atomicAdd(p, v[i]);
+        else
+          *p = v[i];
+      }
+    }
+  }
+  if (!ok && threadIdx.x == 0) flag_status(kStatusTimeout);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32) tc::tmem_dealloc(tmem, 128);
+}
+
+// ---- element-wise training kernels ---------------------------------------------------
+// dY = 2 (Y - T) / (rows * NOUT) on the used outputs; loss partial sums.
+__global__ void loss_grad_kernel(int rows, const float* __restrict__ Y, const float* __restrict__ T,
+                                 __nv_bfloat16* __restrict__ dY, float* __restrict__ dY32,
+                                 float* __restrict__ loss) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t n = static_cast<int64_t>(rows) * OUT;
+  float l = 0.f;
+  if (i < n) {
+    const int c = static_cast<int>(i % OUT);
+    float g = 0.f;
+    if (c < NOUT) {
+      const float e = Y[i] - T[i];
+      l = e * e;
+      g = 2.f * e / (static_cast<float>(rows) * NOUT);
+    }
+    dY[i] = __float2bfloat16(g);
+    dY32[i] = g;
+  }
+  for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+  if ((threadIdx.x & 31) == 0 && l != 0.f) atomicAdd(loss, l);
+}
+
+// dZ = dH * SiLU'(Z) (BF16 out), db += column sums of dZ.
+__global__ void silu_back_kernel(int rows, int cols, const float* __restrict__ dH,
+                                 const float* __restrict__ Z, __nv_bfloat16* __restrict__ dZ,
+                                 float* __restrict__ db) {
+  const int c = threadIdx.x;  // blockDim.x == cols
+  float acc = 0.f;
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int64_t i = static_cast<int64_t>(r) * cols + c;
+    const float g = dH[i] * silu_grad(Z[i]);
+    dZ[i] = __float2bfloat16(g);
+    acc += g;
+  }
+  atomicAdd(db + c, acc);
+}
+
+__global__ void colsum_kernel(int rows, int cols, const float* __restrict__ G, float* __restrict__ db) {
+  const int c = threadIdx.x;
+  float acc = 0.f;
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) acc += G[static_cast<int64_t>(r) * cols + c];
+  atomicAdd(db + c, acc);
+}
+
+// Adam on FP32 master weights; refreshes the BF16 copy.
+__global__ void adam_kernel(int n, float* __restrict__ w, const float* __restrict__ g,
+                            float* __restrict__ m, float* __restrict__ v,
+                            __nv_bfloat16* __restrict__ wb, float lr, float b1, float b2,
+                            float eps, float bc1, float bc2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+  w[i] = wi;
+  if (wb) wb[i] = __float2bfloat16(wi);
 }
 
 // ---- probe: C[128][N] = A[128][K] B[N][K]^T (validates layouts / descriptors) ----
@@ -196,7 +549,8 @@ __global__ void __launch_bounds__(128) gemm_probe_kernel(const __nv_bfloat16* __
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tslot;
-  if (threadIdx.x == 0) tc::gemm_issue(tmem, sA, sB, K, tc::idesc_bf16(128, N), false, &bar, stride_mode);
+  if (threadIdx.x == 0)
+    tc::gemm_issue(tmem, sA, sB, K, tc::idesc_bf16(128, N), false, &bar, stride_mode);
   uint32_t ph = 0;
   const bool ok = __syncthreads_and(wait_mma(&bar, ph));
   if (ok) {
@@ -214,7 +568,52 @@ __global__ void __launch_bounds__(128) gemm_probe_kernel(const __nv_bfloat16* __
   if (threadIdx.x < 32) tc::tmem_dealloc(tmem, 128);
 }
 
+template <typename K>
+int set_smem(K kernel, size_t bytes) {
+  FVX_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(bytes)));
+  return FVX_OK;
+}
+
 }  // namespace mlp
+
+// Fused learned far field for the treecode: local expansions of the learned
+// (leaf, cell) pairs added into leaf_local[n_leaves][32] (zeroed by the caller).
+int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
+                        const uint32_t* leaf_key, const float* rec, float h, const void* W,
+                        const float* bias, float* leaf_local, cudaStream_t s) {
+  using namespace mlp;
+  if (npairs <= 0) return FVX_OK;
+  static int done = 0;
+  if (!done) {
+    int rc = set_smem(mlp_fwd_kernel<true>, sizeof(FwdSmem));
+    if (rc) return rc;
+    done = 1;
+  }
+  FwdArgs<true> A;
+  A.r = RowsIO{nullptr, nullptr, nullptr, nullptr};
+  A.f = FarIO{pair_leaf, pair_cell, leaf_key, rec, h, leaf_local};
+  const int ntiles = (npairs + 127) / 128;
+  const int grid = ntiles < device_sm_count() ? ntiles : device_sm_count();
+  mlp_fwd_kernel<true><<<grid, kThreads, sizeof(FwdSmem), s>>>(
+      A, npairs, static_cast<const __nv_bfloat16*>(W), bias);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const int* pair_cell,
+                            const uint32_t* leaf_key, const float* rec, const int* cell_start,
+                            const int* cell_count, const float4* sp, const float4* sa,
+                            const int* leaf_of_particle, float h, void* X, float* T,
+                            cudaStream_t s) {
+  if (npairs <= 0) return FVX_OK;
+  mlp::pair_targets_kernel<<<(npairs * 32 + 255) / 256, 256, 0, s>>>(
+      npairs, stride, pair_leaf, pair_cell, leaf_key, rec, cell_start, cell_count, sp, sa,
+      leaf_of_particle, h, static_cast<__nv_bfloat16*>(X), T);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
 }  // namespace fvx
 
 extern "C" {
@@ -233,22 +632,87 @@ int fvx_tc_gemm_probe(const void* A, const void* B, int N, int K, float* C, int 
 }
 
 int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, float* Y,
-                    float* z_store, void* h_store, int stride_mode, void* stream) {
+                    float* z_store, void* h_store, void* stream) {
   using namespace fvx::mlp;
   FVX_ARG_CHECK(rows >= 0 && X && W && bias && Y, "null argument");
   if (rows == 0) return FVX_OK;
-  const size_t smem = sizeof(FwdSmem);
-  static bool attr_set = false;
-  if (!attr_set) {
-    FVX_CUDA_TRY(cudaFuncSetAttribute(mlp_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(smem)));
-    attr_set = true;
+  static int done = 0;
+  if (!done) {
+    int rc = set_smem(mlp_fwd_kernel<false>, sizeof(FwdSmem));
+    if (rc) return rc;
+    done = 1;
   }
+  FwdArgs<false> A;
+  A.r = RowsIO{static_cast<const __nv_bfloat16*>(X), Y, z_store,
+               static_cast<__nv_bfloat16*>(h_store)};
+  A.f = FarIO{nullptr, nullptr, nullptr, nullptr, 0.f, nullptr};
   const int ntiles = (rows + 127) / 128;
   const int grid = ntiles < fvx::device_sm_count() ? ntiles : fvx::device_sm_count();
-  mlp_fwd_kernel<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(
-      static_cast<const __nv_bfloat16*>(X), rows, static_cast<const __nv_bfloat16*>(W), bias, Y,
-      z_store, static_cast<__nv_bfloat16*>(h_store), stride_mode);
+  mlp_fwd_kernel<false><<<grid, kThreads, sizeof(FwdSmem), static_cast<cudaStream_t>(stream)>>>(
+      A, rows, static_cast<const __nv_bfloat16*>(W), bias);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_mlp_gemm(const void* A, int lda, int tA, const void* B, int ldb, int tB, float* C,
+                 int ldc, int M, int N, int K, int split_k, int accumulate, void* stream) {
+  using namespace fvx::mlp;
+  FVX_ARG_CHECK(A && B && C && M > 0 && N > 0 && K > 0 && split_k >= 1, "bad gemm arguments");
+  FVX_ARG_CHECK(split_k == 1 || accumulate, "split-K needs accumulation into C");
+  static int done = 0;
+  if (!done) {
+    int rc = set_smem(gemm_tn_kernel, sizeof(GemmSmem));
+    if (rc) return rc;
+    done = 1;
+  }
+  int kchunk = (K + split_k - 1) / split_k;
+  kchunk = (kchunk + 127) & ~127;
+  const int sk = (K + kchunk - 1) / kchunk;
+  dim3 grid((M + 127) / 128, (N + 127) / 128, sk);
+  gemm_tn_kernel<<<grid, 128, sizeof(GemmSmem), static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const __nv_bfloat16*>(A), lda, tA, static_cast<const __nv_bfloat16*>(B), ldb,
+      tB, C, ldc, M, N, K, kchunk, accumulate);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_mlp_loss_grad(int rows, const float* Y, const float* T, void* dY, float* dY32,
+                      float* loss, void* stream) {
+  FVX_ARG_CHECK(rows >= 0 && Y && T && dY && dY32 && loss, "null argument");
+  const int64_t n = static_cast<int64_t>(rows) * fvx::mlp::OUT;
+  if (n == 0) return FVX_OK;
+  fvx::mlp::loss_grad_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0,
+                               static_cast<cudaStream_t>(stream)>>>(
+      rows, Y, T, static_cast<__nv_bfloat16*>(dY), dY32, loss);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_mlp_silu_back(int rows, int cols, const float* dH, const float* Z, void* dZ, float* db,
+                      void* stream) {
+  FVX_ARG_CHECK(rows > 0 && cols > 0 && cols <= 1024 && dH && Z && dZ && db, "bad arguments");
+  const int grid = rows < 1024 ? rows : 1024;
+  fvx::mlp::silu_back_kernel<<<grid, cols, 0, static_cast<cudaStream_t>(stream)>>>(
+      rows, cols, dH, Z, static_cast<__nv_bfloat16*>(dZ), db);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_mlp_colsum(int rows, int cols, const float* G, float* db, void* stream) {
+  FVX_ARG_CHECK(rows > 0 && cols > 0 && cols <= 1024 && G && db, "bad arguments");
+  const int grid = rows < 1024 ? rows : 1024;
+  fvx::mlp::colsum_kernel<<<grid, cols, 0, static_cast<cudaStream_t>(stream)>>>(rows, cols, G, db);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_mlp_adam(int n, float* w, const float* g, float* m, float* v, void* wb, float lr,
+                 float b1, float b2, float eps, int step, void* stream) {
+  FVX_ARG_CHECK(n > 0 && w && g && m && v && step >= 1, "bad arguments");
+  const float bc1 = 1.f - powf(b1, static_cast<float>(step));
+  const float bc2 = 1.f - powf(b2, static_cast<float>(step));
+  fvx::mlp::adam_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      n, w, g, m, v, static_cast<__nv_bfloat16*>(wb), lr, b1, b2, eps, bc1, bc2);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }

@@ -457,6 +457,17 @@ struct TreeView {
   const uint32_t* key;
   const int* child_lo;  // level-local ids of the children (level l+1)
   const int* child_hi;
+  double mac_kl;        // learned far field: 3/4 / theta_L^2 (0: off)
+  int learned_only;     // learned pairs leave the analytic list (weights loaded)
+};
+
+// (target leaf, source cell) pairs handed to the learned far-field operator
+struct LearnedLists {
+  int* cnt;
+  const int* off;
+  int* leaf;
+  int* cell;
+  int cap;
 };
 
 template <bool FILL>
@@ -464,7 +475,7 @@ __global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
                                 const int* __restrict__ far_off, int* __restrict__ near_cnt,
                                 int* __restrict__ far_cnt, int* __restrict__ near_idx,
                                 int* __restrict__ far_idx, int near_cap, int far_cap,
-                                unsigned* __restrict__ overflow) {
+                                unsigned* __restrict__ overflow, LearnedLists LL) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nleaf = T.ncell[T.L];
   if (t >= nleaf) return;
@@ -476,7 +487,8 @@ __global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
   int stack[96];
   int sp = 0;
   for (int c = T.ncell[0] - 1; c >= 0; --c) stack[sp++] = T.base[0] + c;
-  int nn = 0, nf = 0;
+  int nn = 0, nf = 0, nl = 0;
+  const int lo0 = (FILL && LL.off) ? LL.off[t] : 0;
   long long near_pairs = 0;
   const int cT_count = T.count[gT];
   int no = FILL ? near_off[t] : 0, fo = FILL ? far_off[t] : 0;
@@ -494,8 +506,18 @@ __global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
     const double d2 = dx * dx + dy * dy + dz * dz;
     const double hs = T.h + static_cast<double>(sc) * T.h;
     if (d2 > T.mac_k * (hs * hs)) {
-      if (FILL && fo + nf < far_cap) far_idx[fo + nf] = g;
-      ++nf;
+      const bool lrn = T.mac_kl > 0.0 && d2 > T.mac_kl * (hs * hs);
+      if (lrn) {
+        if (FILL && LL.leaf && lo0 + nl < LL.cap) {
+          LL.leaf[lo0 + nl] = t;
+          LL.cell[lo0 + nl] = g;
+        }
+        ++nl;
+      }
+      if (!lrn || !T.learned_only) {
+        if (FILL && fo + nf < far_cap) far_idx[fo + nf] = g;
+        ++nf;
+      }
     } else if (l == T.L) {
       if (FILL && no + nn < near_cap) near_idx[no + nn] = g - T.base[T.L];
       near_pairs += static_cast<long long>(cT_count) * T.count[g];
@@ -514,6 +536,7 @@ __global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
   if (!FILL) {
     near_cnt[t] = nn;
     far_cnt[t] = nf;
+    if (LL.cnt) LL.cnt[t] = nl;
   } else {
     if (no + nn > near_cap || fo + nf > far_cap) atomicOr(overflow, 2u);
     // work counters: near particle pairs, far (target particle, cell) pairs
@@ -542,7 +565,42 @@ struct EvalArgs {
   const int* perm;
   double* out_a;
   double* out_b;
+  const float* leaf_local;  // [leaves][32] learned local expansions, or null
 };
+
+// Learned local expansion of the leaf at offset d = x - c_T (u, J = du/dx,
+// H_i,kn = d2 u_i / dx_k dx_n with 6 unique (k, n) per component).
+template <int MODE>
+__device__ __forceinline__ void l2p(float* acc, const float* L, float dx, float dy, float dz,
+                                    float gx, float gy, float gz) {
+  const float d[3] = {dx, dy, dz};
+  float J[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float* Hi = L + 12 + 6 * i;  // xx xy xz yy yz zz
+    const float Hm[3][3] = {{Hi[0], Hi[1], Hi[2]}, {Hi[1], Hi[3], Hi[4]}, {Hi[2], Hi[4], Hi[5]}};
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      J[i][n] = L[3 + 3 * i + n] + Hm[n][0] * d[0] + Hm[n][1] * d[1] + Hm[n][2] * d[2];
+    if (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_VELOCITY_STRETCH) {
+      // u_i = L_i + J0_in d_n + 1/2 d H_i d = L_i + 1/2 (J0_in + J_in) d_n
+      float u = L[i];
+#pragma unroll
+      for (int n = 0; n < 3; ++n) u += 0.5f * (L[3 + 3 * i + n] + J[i][n]) * d[n];
+      acc[i] += u;
+    }
+  }
+  if (MODE == FVX_PAIR_STRETCH || MODE == FVX_PAIR_VELOCITY_STRETCH) {
+    constexpr int o = MODE == FVX_PAIR_STRETCH ? 0 : 3;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) acc[o + i] += J[i][0] * gx + J[i][1] * gy + J[i][2] * gz;
+  }
+  if (MODE == FVX_PAIR_VORTICITY) {
+    acc[0] += J[2][1] - J[1][2];
+    acc[1] += J[0][2] - J[2][0];
+    acc[2] += J[1][0] - J[0][1];
+  }
+}
 
 template <typename T>
 __device__ __forceinline__ void fold(T& hi, T& lo, T p) {
@@ -742,6 +800,21 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
 #pragma unroll
         for (int c = 0; c < NC; ++c) fold(hi[j][c], lo[j][c], part[j][c]);
     }
+    if (A.leaf_local) {
+      const float* L = A.leaf_local + static_cast<int64_t>(t) * 32;
+      float Ls[30];
+#pragma unroll
+      for (int c = 0; c < 30; ++c) Ls[c] = L[c];
+#pragma unroll
+      for (int j = 0; j < TPT; ++j) {
+        float part[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) part[c] = 0.f;
+        l2p<MODE>(part, Ls, ox[j], oy[j], oz[j], gx[j], gy[j], gz[j]);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) fold(hi[j][c], lo[j][c], part[c]);
+      }
+    }
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
       if (!act[j]) continue;
@@ -816,6 +889,15 @@ void grid_params(const double lo[3], const double hi[3], int64_t n, int leaf_tar
 
 }  // namespace
 
+int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
+                        const uint32_t* leaf_key, const float* rec, float h, const void* W,
+                        const float* bias, float* leaf_local, cudaStream_t s);
+int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const int* pair_cell,
+                            const uint32_t* leaf_key, const float* rec, const int* cell_start,
+                            const int* cell_count, const float4* sp, const float4* sa,
+                            const int* leaf_of_particle, float h, void* X, float* T,
+                            cudaStream_t s);
+
 }  // namespace fvx
 
 struct fvx_tree {
@@ -824,6 +906,19 @@ struct fvx_tree {
       sg, lists_meta, near_list, far_list, bbox;
   int64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the last evaluation launch
+  // learned far field
+  const void* mlp_W = nullptr;
+  const float* mlp_b = nullptr;
+  double theta_l = 0.0;
+  fvx::DevBuf lrn_meta, lrn_leaf, lrn_cell, leaf_local;
+  int n_learned = 0;
+  // the last sweep's tree, for sampling training pairs
+  int last_L = 0, last_nleaf = 0;
+  double last_h = 0.0;
+  const uint32_t* last_leaf_key = nullptr;
+  const int* last_cell_start = nullptr;
+  const int* last_cell_count = nullptr;
+  const int* last_cid = nullptr;
 };
 
 namespace fvx {
@@ -1013,7 +1108,16 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   V.key = reinterpret_cast<const uint32_t*>(lvb + 2 * total_cells);
   V.child_lo = lvb + 3 * total_cells;
   V.child_hi = lvb + 4 * total_cells;
+  const bool learned = T->theta_l > 0.0;
+  V.mac_kl = learned ? 0.75 / (T->theta_l * T->theta_l) : 0.0;
+  V.learned_only = learned && T->mlp_W != nullptr;
   if ((rc = grow(T->lists_meta, 4 * size_t(nleaf) * 4 + 64))) return rc;
+  if (learned && (rc = grow(T->lrn_meta, 4 * size_t(nleaf) * 2 + 64))) return rc;
+  LearnedLists LL{nullptr, nullptr, nullptr, nullptr, 0};
+  if (learned) {
+    LL.cnt = P<int>(T->lrn_meta);
+    LL.off = P<int>(T->lrn_meta) + nleaf;
+  }
   int* near_cnt = P<int>(T->lists_meta);
   int* far_cnt = near_cnt + nleaf;
   int* near_off = far_cnt + nleaf;
@@ -1021,10 +1125,17 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   unsigned* ovf = reinterpret_cast<unsigned*>(far_off + nleaf);  // + 2 x u64 work counters
   FVX_CUDA_TRY(cudaMemsetAsync(ovf, 0, 24, s));
   traverse_kernel<false><<<(nleaf + 127) / 128, 128, 0, s>>>(
-      V, nullptr, nullptr, near_cnt, far_cnt, nullptr, nullptr, 0, 0, ovf);
+      V, nullptr, nullptr, near_cnt, far_cnt, nullptr, nullptr, 0, 0, ovf, LL);
   FVX_LAUNCH_CHECK();
   if ((rc = scan_ints(near_cnt, nleaf, near_off, 0, P<int>(T->scan_tmp), s))) return rc;
   if ((rc = scan_ints(far_cnt, nleaf, far_off, 0, P<int>(T->scan_tmp), s))) return rc;
+  int ltail[2] = {0, 0};
+  if (learned) {
+    if ((rc = scan_ints(LL.cnt, nleaf, P<int>(T->lrn_meta) + nleaf, 0, P<int>(T->scan_tmp), s)))
+      return rc;
+    FVX_CUDA_TRY(cudaMemcpyAsync(&ltail[0], LL.cnt + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
+    FVX_CUDA_TRY(cudaMemcpyAsync(&ltail[1], LL.off + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
+  }
   int tail[4];
   FVX_CUDA_TRY(cudaMemcpyAsync(&tail[0], near_cnt + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
   FVX_CUDA_TRY(cudaMemcpyAsync(&tail[1], near_off + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
@@ -1038,9 +1149,20 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   if ((rc = grow(T->near_list, 4 * size_t(near_total + 1))) ||
       (rc = grow(T->far_list, 4 * size_t(far_total + 1))))
     return rc;
+  const int64_t lrn_total = int64_t(ltail[0]) + ltail[1];
+  FVX_ARG_CHECK(lrn_total < (int64_t(1) << 31), "learned pair list too long");
+  if (learned) {
+    if ((rc = grow(T->lrn_leaf, 4 * size_t(lrn_total + 1))) ||
+        (rc = grow(T->lrn_cell, 4 * size_t(lrn_total + 1))))
+      return rc;
+    LL.leaf = P<int>(T->lrn_leaf);
+    LL.cell = P<int>(T->lrn_cell);
+    LL.cap = static_cast<int>(lrn_total);
+  }
+  T->n_learned = static_cast<int>(lrn_total);
   traverse_kernel<true><<<(nleaf + 127) / 128, 128, 0, s>>>(
       V, near_off, far_off, nullptr, nullptr, P<int>(T->near_list), P<int>(T->far_list),
-      static_cast<int>(near_total), static_cast<int>(far_total), ovf);
+      static_cast<int>(near_total), static_cast<int>(far_total), ovf, LL);
   FVX_LAUNCH_CHECK();
   // 7. evaluation
   EvalArgs A;
@@ -1061,6 +1183,23 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   A.perm = perm;
   A.out_a = out_a;
   A.out_b = out_b;
+  A.leaf_local = nullptr;
+  if (learned && T->mlp_W && lrn_total > 0) {
+    if ((rc = grow(T->leaf_local, sizeof(float) * 32 * size_t(nleaf)))) return rc;
+    FVX_CUDA_TRY(cudaMemsetAsync(T->leaf_local.p, 0, sizeof(float) * 32 * size_t(nleaf), s));
+    if ((rc = mlp_farfield_launch(static_cast<int>(lrn_total), P<int>(T->lrn_leaf),
+                                  P<int>(T->lrn_cell), leaves.key, rec, static_cast<float>(h),
+                                  T->mlp_W, T->mlp_b, P<float>(T->leaf_local), s)))
+      return rc;
+    A.leaf_local = P<float>(T->leaf_local);
+  }
+  T->last_L = L;
+  T->last_nleaf = nleaf;
+  T->last_h = h;
+  T->last_leaf_key = leaves.key;
+  T->last_cell_start = lvb;
+  T->last_cell_count = lvb + total_cells;
+  T->last_cid = cid;
   if (!T->ev0) {
     FVX_CUDA_TRY(cudaEventCreate(&T->ev0));
     FVX_CUDA_TRY(cudaEventCreate(&T->ev1));
@@ -1078,7 +1217,7 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   T->stats[1] = nleaf;
   T->stats[2] = near_total;
   T->stats[3] = far_total;
-  T->stats[4] = total_cells;
+  T->stats[4] = lrn_total;
   if (stats) {
     FVX_CUDA_TRY(cudaStreamSynchronize(s));
     unsigned long long work[2];
@@ -1107,10 +1246,11 @@ void fvx_tree_destroy(fvx_tree* T) {
   if (!T) return;
   if (T->ev0) cudaEventDestroy(T->ev0);
   if (T->ev1) cudaEventDestroy(T->ev1);
-  fvx::DevBuf* bufs[] = {&T->keys0, &T->keys1,      &T->idx0,      &T->idx1,      &T->table,
-                         &T->scan_tmp, &T->flags,   &T->cid,       &T->levels,    &T->counts,
-                         &T->rec,   &T->sp,         &T->sa,        &T->sg,        &T->lists_meta,
-                         &T->near_list, &T->far_list, &T->bbox};
+  fvx::DevBuf* bufs[] = {&T->keys0,   &T->keys1,     &T->idx0,     &T->idx1,     &T->table,
+                         &T->scan_tmp, &T->flags,   &T->cid,      &T->levels,   &T->counts,
+                         &T->rec,     &T->sp,       &T->sa,       &T->sg,       &T->lists_meta,
+                         &T->near_list, &T->far_list, &T->bbox,   &T->lrn_meta, &T->lrn_leaf,
+                         &T->lrn_cell, &T->leaf_local};
   for (auto* b : bufs)
     if (b->p) cudaFree(b->p);
   delete T;
@@ -1121,6 +1261,35 @@ int fvx_tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const d
                    int leaf_target, double* out_a, double* out_b, int64_t* stats, void* stream) {
   return fvx::tree_sweep(T, mode, kernel, pos, alpha, sigma, tgt_gamma, n, theta, leaf_target,
                          out_a, out_b, stats, static_cast<cudaStream_t>(stream));
+}
+
+int fvx_tree_set_learned(fvx_tree* T, const void* W, const float* b, double theta_learned) {
+  FVX_ARG_CHECK(T != nullptr, "null tree handle");
+  FVX_ARG_CHECK(theta_learned >= 0.0 && theta_learned < 1.0, "bad theta_learned");
+  FVX_ARG_CHECK((W == nullptr) == (b == nullptr), "weights and biases go together");
+  T->mlp_W = W;
+  T->mlp_b = b;
+  T->theta_l = theta_learned;
+  return FVX_OK;
+}
+
+int fvx_tree_sample_pairs(fvx_tree* T, int max_pairs, void* X, float* Tgt, int* n_out,
+                          void* stream) {
+  FVX_ARG_CHECK(T && X && Tgt && n_out && max_pairs > 0, "bad arguments");
+  *n_out = 0;
+  FVX_ARG_CHECK(T->theta_l > 0.0, "sampling needs theta_learned > 0 on the last sweep");
+  const int n = T->n_learned;
+  if (n <= 0) return FVX_OK;
+  const int stride = n > max_pairs ? n / max_pairs : 1;
+  const int np = n / stride < max_pairs ? n / stride : max_pairs;
+  int rc = fvx::mlp_pair_targets_launch(
+      np, stride, fvx::P<int>(T->lrn_leaf), fvx::P<int>(T->lrn_cell), T->last_leaf_key,
+      fvx::P<float>(T->rec), T->last_cell_start, T->last_cell_count, fvx::P<float4>(T->sp),
+      fvx::P<float4>(T->sa), T->last_cid, static_cast<float>(T->last_h), X, Tgt,
+      static_cast<cudaStream_t>(stream));
+  if (rc) return rc;
+  *n_out = np;
+  return FVX_OK;
 }
 
 int fvx_tree_last_eval_ms(fvx_tree* T, float* ms) {

@@ -28,6 +28,8 @@ class TreeSweeper:
         _capi.check(self.lib.fvx_tree_create(ctypes.byref(h)))
         self.handle = h.value
         self.stats = np.zeros(8, dtype=np.int64)
+        self._mlp = None
+        self.theta_learned = 0.0
 
     def __del__(self):
         try:
@@ -53,3 +55,29 @@ class TreeSweeper:
         ms = ctypes.c_float(0.0)
         _capi.check(self.lib.fvx_tree_last_eval_ms(self.handle, ctypes.byref(ms)))
         return float(ms.value)
+
+    # ---- learned far field ------------------------------------------------------
+    def set_learned(self, mlp=None, theta_learned=None):
+        """Routes the accepted cells with |dc|^2 > 3/4 (h_T + h_S)^2 / theta_learned^2
+        through ``mlp`` (a learned.FarFieldMLP; its device weights must outlive
+        the sweeps).  mlp=None with theta_learned > 0 only lists those pairs
+        (they stay on the quadrupole path) so that they can be sampled;
+        theta_learned=None or 0 turns the split off."""
+        th = 0.0 if not theta_learned else float(theta_learned)
+        self._mlp = mlp if th > 0.0 else None
+        W = None if self._mlp is None else self._mlp.wb.data_ptr()
+        b = None if self._mlp is None else self._mlp.b.data_ptr()
+        _capi.check(self.lib.fvx_tree_set_learned(self.handle, W, b, th))
+        self.theta_learned = th
+
+    def sample_pairs(self, max_pairs, stream=None, device="cuda"):
+        """Features X (k, 48) BF16 and exact normalised targets T (k, 32) FP32 of up
+        to max_pairs learned pairs of the last sweep (evenly strided over its
+        learned list)."""
+        X = torch.empty((max_pairs, 48), dtype=torch.bfloat16, device=device)
+        T = torch.empty((max_pairs, 32), dtype=torch.float32, device=device)
+        st = stream if stream is not None else torch.cuda.current_stream(X.device).cuda_stream
+        k = ctypes.c_int(0)
+        _capi.check(self.lib.fvx_tree_sample_pairs(self.handle, int(max_pairs), X.data_ptr(),
+                                                    T.data_ptr(), ctypes.byref(k), st))
+        return X[: k.value], T[: k.value]

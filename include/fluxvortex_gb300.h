@@ -202,6 +202,19 @@ int fvx_tree_sweep(fvx_tree* tree, int mode, int kernel, const double* pos, cons
 /* Device time of the last sweep's evaluation kernel (waits for it).  stats
  * of the same sweep: [6] near particle pairs, [7] far (target, cell) pairs. */
 int fvx_tree_last_eval_ms(fvx_tree* tree, float* ms);
+/* Learned far field (new; no reference counterpart).  theta_learned > 0
+ * splits the accepted cells: those with |dc|^2 > 3/4 (h_T + h_S)^2 /
+ * theta_learned^2 form the learned list (stats[4] = its length).  With W and
+ * b set (device pointers in the fvx_mlp_forward packing, kept by the handle)
+ * the learned pairs are evaluated by the tensor-core MLP into per-leaf local
+ * expansions applied to each target; with W = b = NULL they stay on the
+ * quadrupole path and are only listed (for sampling).  theta_learned = 0
+ * turns the split off.  fvx_tree_sample_pairs: features X[k][48] (BF16) and
+ * exact FP64-summed normalised targets T[k][32] (FP32) of k <= max_pairs
+ * learned pairs of the last sweep, strided evenly over the list (*n_out = k). */
+int fvx_tree_set_learned(fvx_tree* tree, const void* W, const float* b, double theta_learned);
+int fvx_tree_sample_pairs(fvx_tree* tree, int max_pairs, void* X, float* T, int* n_out,
+                          void* stream);
 
 /* ---- panel side of the hybrid panel-particle step (FP64) ------------------------
  * Replaces the PteraSoftware solver stages that HybridSolver runs around the
@@ -263,16 +276,41 @@ int fvx_uvlm_convert(int R, int n_keep, int ns, const double* W, const double* g
                      double* pos, double* alpha, double* sigma, double* age, void* stream);
 
 /* ---- learned far-field operator: BF16 tensor-core MLP (tcgen05) ---------------
- * 48 inputs -> 3 x 128 SiLU -> 16 outputs; W packed [out][in] BF16 (W1 128x48,
- * W2 128x128, W3 128x128, W4 16x128), bias packed FP32 (3 x 128 + 16).
- * fvx_mlp_forward: Y[rows][16] FP32 from X[rows][48] BF16; z_store
- * (3 x rows x 128 FP32) and h_store (3 x rows x 128 BF16), if not NULL,
- * receive the hidden pre-activations and activations for training.
- * stride_mode selects the descriptor stride convention (0 in production).
- * fvx_tc_gemm_probe: C[128][N] = A[128][K] B[N][K]^T on one CTA (layout check).
- * No reference counterpart (the operator is new). */
+ * No reference counterpart: the reference's notes plan a learned far field in
+ * a treecode (docs/phase0A_findings.md:33-35); the operator is new.
+ * Network: 48 inputs (35 used) -> 3 x 128 SiLU -> 32 outputs (30 used); W
+ * packed [out][in] BF16 (W1 128x48, W2 128x128, W3 128x128, W4 32x128 = 45056
+ * elements), bias packed FP32 (3 x 128 + 32 = 416).  For a (target leaf T,
+ * source cell S) pair with R = c_T - c_S, d = |R| and m = |M0| + |M1|/h_S +
+ * |M2|/h_S^2 (Frobenius norms of the cell's moments), the inputs are R/d,
+ * h_S/d, h_T/d, M0/m, M1/(m h_S), M2/(m h_S^2) and the outputs the local
+ * expansion of S's singular Biot-Savart field at c_T: u d^2/m (3), du/dx d^3/m
+ * (9, [i][n] = du_i/dx_n), d2u/dx2 d^4/m (18, per component xx xy xz yy yz zz).
+ * fvx_mlp_forward: Y[rows][32] FP32 from X[rows][48] BF16; z_store
+ *   (3 x rows x 128 FP32) and h_store (3 x rows x 128 BF16), if not NULL,
+ *   receive the hidden pre-activations and activations for training.
+ * fvx_mlp_gemm: C[M][N] (+)= sum_k opA[m][k] opB[n][k], opA[m][k] = tA ?
+ *   A[k*lda + m] : A[m*lda + k] (same for B), BF16 in, FP32 out, split over K
+ *   into split_k slices added with atomics (accumulate != 0 adds into C).
+ * fvx_mlp_loss_grad: mean-square loss over the 30 used outputs: loss += sum
+ *   (Y - T)^2 (device scalar), dY = 2 (Y - T) / (30 rows) in BF16 and FP32.
+ * fvx_mlp_silu_back: dZ = dH SiLU'(Z) (BF16 out), db[c] += sum_r dZ[r][c].
+ * fvx_mlp_colsum: db[c] += sum_r G[r][c].
+ * fvx_mlp_adam: Adam step `step` (1-based) on FP32 master weights w with
+ *   moments m, v; writes the BF16 copy wb when not NULL.
+ * fvx_tc_gemm_probe: C[128][N] = A[128][K] B[N][K]^T on one CTA (layout check;
+ *   stride_mode 0 is the convention every kernel uses). */
 int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, float* Y,
-                    float* z_store, void* h_store, int stride_mode, void* stream);
+                    float* z_store, void* h_store, void* stream);
+int fvx_mlp_gemm(const void* A, int lda, int tA, const void* B, int ldb, int tB, float* C,
+                 int ldc, int M, int N, int K, int split_k, int accumulate, void* stream);
+int fvx_mlp_loss_grad(int rows, const float* Y, const float* T, void* dY, float* dY32,
+                      float* loss, void* stream);
+int fvx_mlp_silu_back(int rows, int cols, const float* dH, const float* Z, void* dZ, float* db,
+                      void* stream);
+int fvx_mlp_colsum(int rows, int cols, const float* G, float* db, void* stream);
+int fvx_mlp_adam(int n, float* w, const float* g, float* m, float* v, void* wb, float lr,
+                 float b1, float b2, float eps, int step, void* stream);
 int fvx_tc_gemm_probe(const void* A, const void* B, int N, int K, float* C, int stride_mode,
                       void* stream);
 

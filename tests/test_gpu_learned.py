@@ -1,0 +1,160 @@
+"""Learned far-field operator on the GPU: the tcgen05 training GEMM, the MLP
+forward and backward against the CPU oracle (gradient check), the sampled
+training pairs against exact FP64 local expansions, and training."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import learned as OL
+from oracle import treecode as TC
+
+pytestmark = pytest.mark.gpu
+
+
+def _lib():
+    from fluxvortex_gb300 import _capi
+    return _capi
+
+
+@pytest.mark.parametrize("tA,tB,M,N,K,split", [(0, 0, 128, 128, 128, 1), (1, 1, 32, 128, 1000, 3),
+                                              (0, 1, 300, 128, 32, 1), (1, 1, 128, 48, 4096, 4),
+                                              (1, 0, 200, 80, 130, 2)])
+def test_tc_gemm_matches_fp32(cuda, tA, tB, M, N, K, split):
+    capi = _lib()
+    lib = capi.load()
+    g = torch.Generator().manual_seed(M * 7 + N + K)
+    a = torch.randn((K, M) if tA else (M, K), generator=g).to(torch.bfloat16)
+    b = torch.randn((K, N) if tB else (N, K), generator=g).to(torch.bfloat16)
+    A, B = a.cuda(), b.cuda()
+    C = torch.zeros((M, N), dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    capi.check(lib.fvx_mlp_gemm(A.data_ptr(), A.shape[1], tA, B.data_ptr(), B.shape[1], tB,
+                                C.data_ptr(), N, M, N, K, split, 1 if split > 1 else 0, st))
+    opA = a.float().T if tA else a.float()
+    opB = b.float() if tB else b.float().T
+    ref = (opA.double() @ opB.double())
+    err = (C.cpu().double() - ref).abs().max() / ref.abs().max()
+    assert err < 1e-5, err
+    assert capi.status_read_and_clear() == 0
+
+
+def _net(seed):
+    from fluxvortex_gb300 import learned as L
+    w, b = L.init_weights(seed)
+    rng = np.random.default_rng(seed)
+    b = (rng.standard_normal(b.size) * 0.1).astype(np.float32)
+    return L.FarFieldMLP(w, b)
+
+
+def test_mlp_forward_matches_oracle(cuda):
+    from fluxvortex_gb300 import learned as L
+    m = _net(11)
+    rng = np.random.default_rng(12)
+    rows = 1000                      # 8 tiles, the last one partial
+    X = np.zeros((rows, L.IN), np.float32)
+    X[:, :L.NFEAT] = rng.standard_normal((rows, L.NFEAT))
+    Xd = torch.tensor(X).to(torch.bfloat16).cuda()
+    Y, Z, Hs = m.forward(Xd, store=True)
+    w, b = m.weights_numpy()
+    Yo, (Zo, Ho) = OL.forward(w, b, Xd.float().cpu().numpy())
+    Y = Y.cpu().numpy()
+    err = np.abs(Y[:, :L.NOUT] - Yo[:, :L.NOUT]).max() / np.abs(Yo[:, :L.NOUT]).max()
+    assert err < 1e-2, err
+    zerr = np.abs(Z.cpu().numpy()[0] - Zo[0]).max() / np.abs(Zo[0]).max()
+    assert zerr < 1e-5, zerr          # first layer: same BF16 operands, FP32 accumulation
+    assert torch.isfinite(Hs.float()).all()
+    assert _lib().status_read_and_clear() == 0
+
+
+def test_mlp_gradients_match_oracle(cuda):
+    """Gradient check: tensor-core backward against the FP64 oracle with the same
+    BF16 rounding points."""
+    from fluxvortex_gb300 import learned as L
+    m = _net(21)
+    rng = np.random.default_rng(22)
+    rows = 2048
+    X = np.zeros((rows, L.IN), np.float32)
+    X[:, :L.NFEAT] = rng.standard_normal((rows, L.NFEAT))
+    T = np.zeros((rows, L.OUT), np.float32)
+    T[:, :L.NOUT] = rng.standard_normal((rows, L.NOUT))
+    Xd = torch.tensor(X).to(torch.bfloat16).cuda()
+    Td = torch.tensor(T).cuda()
+    loss, _ = m.gradients(Xd, Td)
+    w, b = m.weights_numpy()
+    lo, gwo, gbo = OL.gradients(w, b, Xd.float().cpu().numpy(), T)
+    assert abs(float(loss.item()) - lo) <= 1e-3 * lo
+    gw, gb = m.gw.cpu().numpy(), m.gb.cpu().numpy()
+    for li, ((r, c), o) in enumerate(zip(L.LAYERS, L.W_OFFSETS)):
+        a, e = gw[o:o + r * c], gwo[o:o + r * c]
+        rel = np.abs(a - e).max() / np.abs(e).max()
+        assert rel < 2e-2, (li, rel)
+        cos = float(a @ e / (np.linalg.norm(a) * np.linalg.norm(e)))
+        assert cos > 0.9995, (li, cos)
+    for li, ((r, _), o) in enumerate(zip(L.LAYERS, L.B_OFFSETS)):
+        a, e = gb[o:o + r], gbo[o:o + r]
+        rel = np.abs(a - e).max() / np.abs(e).max()
+        assert rel < 2e-2, (li, rel)
+    assert _lib().status_read_and_clear() == 0
+
+
+def _slab(n, seed):
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform([0, 0, 0], [4.0, 2.0, 0.4], (n, 3))
+    alpha = rng.standard_normal((n, 3)) * 1e-3
+    sigma = np.full(n, 0.02)
+    return pos, alpha, sigma
+
+
+def test_sampled_pairs_match_exact_local_expansions(cuda):
+    from fluxvortex_gb300.tree import TreeSweeper
+    from fluxvortex_gb300 import _capi
+    n, leaf = 6000, 16
+    pos, alpha, sigma = _slab(n, 31)
+    ts = TreeSweeper(theta=0.5, leaf_target=leaf)
+    ts.set_learned(None, 0.4)
+    d = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")  # noqa: E731
+    out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    stats = ts.sweep(_capi.PAIR_VELOCITY, "winckelmans", d(pos), d(alpha), d(sigma), n, out,
+                     check=True)
+    tree = TC.build(pos, theta=0.5, leaf_target=leaf)
+    pairs = OL.learned_pairs(tree, 0.4)
+    assert int(stats[4]) == len(pairs) > 0
+    max_pairs = 97
+    Xg, Tg = ts.sample_pairs(max_pairs)
+    stride = len(pairs) // max_pairs if len(pairs) > max_pairs else 1
+    k = min(len(pairs) // stride, max_pairs)
+    assert Xg.shape[0] == k
+    Xo, To = OL.pair_samples(tree, pos, alpha, [pairs[i * stride] for i in range(k)])
+    Xg = Xg.float().cpu().numpy()
+    Tg = Tg.cpu().numpy()
+    # features: the device's BF16 rounding of FP32 values, one BF16 step at most
+    assert np.all(np.abs(Xg - Xo) <= 2.0 ** -7 * np.abs(Xo) + 1e-6)
+    # targets: FP64 sums of FP32 particle offsets
+    rel = np.abs(Tg - To).max(axis=1) / np.abs(To).max(axis=1)
+    assert rel.max() < 1e-4, rel.max()
+    # the analytic path still evaluates the learned pairs (no weights set)
+    ts.set_learned(None, 0.0)
+    out2 = torch.empty_like(out)
+    ts.sweep(_capi.PAIR_VELOCITY, "winckelmans", d(pos), d(alpha), d(sigma), n, out2)
+    assert torch.equal(out, out2)
+    assert _capi.status_read_and_clear() == 0
+
+
+def test_training_reduces_loss(cuda):
+    from fluxvortex_gb300 import learned as L
+    from fluxvortex_gb300.tree import TreeSweeper
+    n = 60000
+    pos, alpha, sigma = _slab(n, 41)
+    d = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")  # noqa: E731
+    ts = TreeSweeper(theta=0.5, leaf_target=32)
+    X, T = L.harvest(ts, d(pos), d(alpha), d(sigma), n, 40000)
+    assert X.shape[0] > 10000
+    m = L.FarFieldMLP(seed=3)
+    e0 = float(m.errors(X, T).median())
+    hist = m.fit(X, T, steps=400, batch=4096, lr=2e-3, log_every=100)
+    e1 = float(m.errors(X, T).median())
+    assert hist[-1][1] < 0.2 * hist[0][1], hist
+    assert e1 < 0.5 * e0, (e0, e1)
+    assert _lib().status_read_and_clear() == 0

@@ -1,0 +1,102 @@
+"""Pins of the learned far-field oracle (CPU): network gradients against central
+differences, exact local expansions against the quadrupole far field and a
+Taylor step, BF16 rounding against torch's conversion."""
+import numpy as np
+import torch
+
+from oracle import learned as OL
+from oracle import treecode as TC
+
+
+def _rand_net(seed, scale=0.3):
+    rng = np.random.default_rng(seed)
+    nw = sum(r * c for r, c in OL.LAYERS)
+    nb = sum(r for r, _ in OL.LAYERS)
+    return rng.standard_normal(nw) * scale, rng.standard_normal(nb) * 0.1
+
+
+def test_bf16_rounding_matches_torch():
+    rng = np.random.default_rng(1)
+    x = np.concatenate([rng.standard_normal(4096) * 10.0 ** rng.integers(-6, 6, 4096),
+                        [1.0 + 2.0 ** -8, 1.0 + 3 * 2.0 ** -8, -1.0 - 2.0 ** -8, 0.0]])
+    ref = torch.tensor(x, dtype=torch.float32).to(torch.bfloat16).double().numpy()
+    np.testing.assert_array_equal(OL.bf16(x), ref)
+
+
+def test_gradients_match_central_differences():
+    w, b = _rand_net(2)
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((5, OL.IN))
+    T = rng.standard_normal((5, OL.OUT))
+    loss, gw, gb = OL.gradients(w, b, X, T, rounding=False)
+    scale = 1.0 / (X.shape[0] * OL.NOUT)
+    eps = 1e-6
+    for idx in list(rng.integers(0, w.size, 24)) + [OL.W_OFFSETS[3] + 5, OL.W_OFFSETS[0] + 3]:
+        wp, wm = w.copy(), w.copy()
+        wp[idx] += eps
+        wm[idx] -= eps
+        fd = (OL.gradients(wp, b, X, T, False)[0] - OL.gradients(wm, b, X, T, False)[0]) / (2 * eps)
+        assert abs(fd * scale - gw[idx]) <= 1e-6 * max(1.0, abs(gw[idx])) + 1e-9, idx
+    for idx in list(rng.integers(0, b.size, 12)) + [b.size - 1]:
+        bp, bm = b.copy(), b.copy()
+        bp[idx] += eps
+        bm[idx] -= eps
+        fd = (OL.gradients(w, bp, X, T, False)[0] - OL.gradients(w, bm, X, T, False)[0]) / (2 * eps)
+        assert abs(fd * scale - gb[idx]) <= 1e-6 * max(1.0, abs(gb[idx])) + 1e-9, idx
+    # padded output columns carry no gradient
+    assert np.all(gb[OL.B_OFFSETS[3] + OL.NOUT:] == 0.0)
+
+
+def test_local_expansion_matches_quadrupole_far_field():
+    rng = np.random.default_rng(4)
+    c = np.array([0.3, -0.2, 0.1])
+    pos = c + rng.uniform(-0.05, 0.05, (40, 3))
+    alpha = rng.standard_normal((40, 3))
+    x0 = c + np.array([1.5, 0.7, -0.9])
+    u, J, H = OL.local_expansion(x0, pos, alpha)
+    d = pos - c
+    M0 = alpha.sum(0)
+    M1 = np.einsum("pm,pj->mj", alpha, d)
+    M2 = np.einsum("pm,pj,pk->mjk", alpha, d, d)
+    uq, Jq = TC.far_field(x0 - c, M0, M1, M2)
+    # the quadrupole truncation error is O((r_S / d)^3) ~ 1e-4 here
+    assert np.abs(u - uq).max() <= 2e-4 * np.abs(u).max()
+    assert np.abs(J - Jq).max() <= 2e-4 * np.abs(J).max()
+    assert np.allclose(H, np.swapaxes(H, 1, 2), rtol=0, atol=1e-14 * np.abs(H).max())
+
+
+def test_local_expansion_taylor_step():
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(-0.1, 0.1, (30, 3))
+    alpha = rng.standard_normal((30, 3))
+    x0 = np.array([1.2, 0.4, -0.5])
+    u, J, H = OL.local_expansion(x0, pos, alpha)
+    for k in range(3):
+        e = np.zeros(3)
+        e[k] = 1e-5
+        up, Jp, _ = OL.local_expansion(x0 + e, pos, alpha)
+        um, Jm, _ = OL.local_expansion(x0 - e, pos, alpha)
+        np.testing.assert_allclose((up - um) / 2e-5, J[:, k], rtol=1e-6, atol=1e-8)
+        np.testing.assert_allclose((Jp - Jm) / 2e-5, H[:, :, k], rtol=1e-6, atol=1e-8)
+    # the divergence of a curl vanishes
+    assert abs(np.trace(J)) <= 1e-12 * np.abs(J).max()
+
+
+def test_pair_samples_consistent_with_tree():
+    rng = np.random.default_rng(6)
+    n = 3000
+    pos = rng.uniform([0, 0, 0], [4.0, 2.0, 0.4], (n, 3))
+    alpha = rng.standard_normal((n, 3)) * 1e-3
+    tree = TC.build(pos, theta=0.5, leaf_target=16)
+    pairs = OL.learned_pairs(tree, 0.5)
+    far_total = sum(len(f) for _, f in TC.lists(tree))
+    assert 0 < len(pairs) == far_total     # theta_learned = theta: every accepted cell
+    fewer = OL.learned_pairs(tree, 0.35)
+    assert 0 < len(fewer) < len(pairs)
+    X, T = OL.pair_samples(tree, pos, alpha, pairs[::max(1, len(pairs) // 50)])
+    np.testing.assert_allclose(np.linalg.norm(X[:, 0:3], axis=1), 1.0, rtol=1e-12)
+    m = (np.linalg.norm(X[:, 5:8], axis=1) + np.linalg.norm(X[:, 8:17], axis=1)
+         + np.sqrt((X[:, 17:35] ** 2 * np.tile([1, 2, 2, 1, 2, 1], 3)).sum(1)))
+    np.testing.assert_allclose(m, 1.0, rtol=1e-12)
+    assert np.all(X[:, OL.NFEAT:] == 0.0) and np.all(T[:, OL.NOUT:] == 0.0)
+    assert np.all(np.isfinite(T)) and np.abs(T).max() < 1e3
