@@ -26,6 +26,7 @@ KERNELS = {"gaussianerf": KERNEL_GAUSSIANERF, "winckelmans": KERNEL_WINCKELMANS}
 PREC_F64, PREC_F32C = 0, 1
 PRECISIONS = {"f64": PREC_F64, "fp64": PREC_F64, "f32c": PREC_F32C, "fp32c": PREC_F32C}
 PAIR_VELOCITY, PAIR_STRETCH, PAIR_VELOCITY_STRETCH, PAIR_JACOBIAN, PAIR_VORTICITY = range(5)
+FAR_M2P, FAR_M2L, FAR_LEARNED = range(3)
 
 # name -> (restype, argtypes); mirrors include/fluxvortex_gb300.h
 SIGNATURES = {
@@ -53,11 +54,12 @@ SIGNATURES = {
     "fvx_tree_destroy": (None, [P]),
     "fvx_tree_sweep": (I32, [P, I32, I32, P, P, P, P, I64, D, I32, P, P, P, P]),
     "fvx_tree_last_eval_ms": (I32, [P, P]),
-    "fvx_tree_set_learned": (I32, [P, P, P, D]),
-    "fvx_tree_sample_pairs": (I32, [P, I32, P, P, P, P]),
+    "fvx_tree_set_far_field": (I32, [P, I32, P, P, D]),
+    "fvx_tree_last_local_ms": (I32, [P, P]),
+    "fvx_tree_sample_pairs": (I32, [P, I32, P, P, P, P, P]),
     "fvx_mlp_forward": (I32, [P, I32, P, P, P, P, P, P]),
     "fvx_mlp_gemm": (I32, [P, I32, I32, P, I32, I32, P, I32, I32, I32, I32, I32, I32, P]),
-    "fvx_mlp_loss_grad": (I32, [I32, P, P, P, P, P, P]),
+    "fvx_mlp_loss_grad": (I32, [I32, P, P, P, P, P, P, P]),
     "fvx_mlp_silu_back": (I32, [I32, I32, P, P, P, P, P]),
     "fvx_mlp_colsum": (I32, [I32, I32, P, P, P]),
     "fvx_mlp_adam": (I32, [I32, P, P, P, P, P, F, F, F, F, I32, P]),

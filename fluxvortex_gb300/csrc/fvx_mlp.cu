@@ -3,11 +3,12 @@
 // Network: 48 inputs (35 features, zero padded) -> 3 x 128 hidden (SiLU) ->
 // 32 outputs (30 used), weights [out][in] in BF16 with FP32 master copies,
 // FP32 biases.  Inference and training run on tcgen05 (fvx_tc.cuh):
-//   * forward: one CTA of 128 threads per 128-row tile (persistent over the
-//     tiles) keeps all weights in shared memory in the K-major canonical
-//     layout and chains the four layers through tensor memory: MMA into TMEM
-//     -> tcgen05.ld -> bias + SiLU in registers -> BF16 back into the shared
-//     activation tile -> next MMA.  Two input/output policies: plain rows
+//   * forward: a persistent CTA per SM keeps all weights in shared memory in
+//     the K-major canonical layout; each of its two warpgroups owns a 128-row
+//     tile at a time and chains the four layers through its half of the
+//     tensor memory: MMA into TMEM -> tcgen05.ld -> bias + SiLU in registers
+//     -> BF16 back into the group's shared activation tile -> next MMA, so
+//     one group's epilogue overlaps the other's MMAs.  Two input/output policies: plain rows
 //     (X -> Y, with the hidden pre-activations / activations kept for
 //     training), and the treecode's learned far field (features computed
 //     in-kernel from the (target leaf, source cell) pair list, outputs scaled
@@ -26,7 +27,7 @@ namespace fvx {
 namespace mlp {
 
 constexpr int IN = 48, H = 128, OUT = 32, NFEAT = 35, NOUT = 30;
-constexpr int kThreads = 128;
+constexpr int kThreads = 256;  // forward: two warpgroups
 // packed BF16 weight offsets (elements)
 constexpr int W1o = 0, W2o = W1o + H * IN, W3o = W2o + H * H, W4o = W3o + H * H,
               WN = W4o + OUT * H;
@@ -34,21 +35,52 @@ constexpr int W1o = 0, W2o = W1o + H * IN, W3o = W2o + H * H, W4o = W3o + H * H,
 constexpr int B1o = 0, B2o = H, B3o = 2 * H, B4o = 3 * H, BN = 3 * H + OUT;
 constexpr int kRecFloats = 40;  // treecode cell record (fvx_tree.cu)
 
+// Two 128-row tiles are in flight per CTA (one per warpgroup): while one
+// group runs its epilogue on the CUDA cores, the other's MMA runs.
+constexpr int kGroups = 2;
+
 struct FwdSmem {
   __nv_bfloat16 w1[H * IN];
   __nv_bfloat16 w2[H * H];
   __nv_bfloat16 w3[H * H];
   __nv_bfloat16 w4[OUT * H];
-  __nv_bfloat16 act[128 * H];
+  __nv_bfloat16 act[kGroups][128 * H];
+  float aux[kGroups][128][33];  // far field: analytic M2L (30) and the output scales (3)
   float bias[BN];
-  uint64_t bar;
+  uint64_t bar[kGroups];
   uint32_t tmem;
 };
 
-__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// SiLU z sigmoid(z) = z/2 (1 + tanh(z/2)): one MUFU operation per element
+__device__ __forceinline__ float silu(float z) {
+  const float h = 0.5f * z;
+  return fmaf(h, tanh_approx(h), h);
+}
 __device__ __forceinline__ float silu_grad(float z) {
   const float s = 1.f / (1.f + __expf(-z));
   return s * (1.f + z * (1.f - s));
+}
+
+// Barrier over the 128 threads of warpgroup g (named barrier 1 + g).
+__device__ __forceinline__ void group_sync(int g) {
+  asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory");
+}
+__device__ __forceinline__ bool group_sync_and(int g, bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred q, d;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.and.pred d, %2, 128, q;\n\t"
+      "selp.u32 %0, 1, 0, d;\n\t}"
+      : "=r"(r)
+      : "r"(static_cast<uint32_t>(p)), "r"(1 + g)
+      : "memory");
+  return r != 0;
 }
 
 // Copies a row-major [R][K] BF16 matrix into the K-major canonical layout.
@@ -101,6 +133,76 @@ __device__ __forceinline__ PairScale pair_features(const float* rec, float cTx, 
   return s;
 }
 
+// Multipole to local, analytic: the local expansion at the target centre of
+// the source cell's quadrupole expansion, in the network's normalised output
+// units (unit distance along n = R/d; f = the pair's FP32 features).  With
+// C-scaled moments the vector potential is Psi_m = -(M0_m phi - M1_ma d_a phi
+// + 1/2 M2_mab d_ab phi), phi = 1/|r|, and u_i = eps_ijm d_j Psi_m; the
+// derivatives of phi at |r| = 1 are contracted with the moments in closed
+// form (d^p phi = sum over index pairings of (-1)^(p-k) (2p-2k-1)!! n..n d..d).
+__device__ void m2l_quadrupole(const float* f, float* out) {
+  const float nv[3] = {f[0], f[1], f[2]};
+  const float hs = f[3];
+#pragma unroll
+  for (int q = 0; q < NOUT; ++q) out[q] = 0.f;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const float c = f[5 + m];
+    const float v[3] = {f[8 + 3 * m] * hs, f[9 + 3 * m] * hs, f[10 + 3 * m] * hs};
+    const float* q6 = f + 17 + 6 * m;
+    const float h2 = hs * hs;
+    const float Q[3][3] = {{q6[0] * h2, q6[1] * h2, q6[2] * h2},
+                           {q6[1] * h2, q6[3] * h2, q6[4] * h2},
+                           {q6[2] * h2, q6[4] * h2, q6[5] * h2}};
+    const float vn = v[0] * nv[0] + v[1] * nv[1] + v[2] * nv[2];
+    float qn[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) qn[j] = Q[j][0] * nv[0] + Q[j][1] * nv[1] + Q[j][2] * nv[2];
+    const float nqn = qn[0] * nv[0] + qn[1] * nv[1] + qn[2] * nv[2];
+    const float tr = Q[0][0] + Q[1][1] + Q[2][2];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      if (j == m) continue;
+      const int i = 3 - m - j;
+      const float sg = ((j - i + 3) % 3 == 1) ? 1.f : -1.f;  // eps_ijm
+      const float nj = nv[j];
+      // u: c phi_j - v_a phi_aj + 1/2 Q_ab phi_abj
+      const float p1 = -nj * c - (3.f * vn * nj - v[j]) + 0.5f * (-15.f * nqn * nj + 3.f * tr * nj + 6.f * qn[j]);
+      out[i] -= sg * p1;
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        const float dl = j == n ? 1.f : 0.f;
+        const float nn = nv[n];
+        const float phi2 = 3.f * nj * nn - dl;
+        const float vphi3 = -15.f * vn * nj * nn + 3.f * (v[j] * nn + v[n] * nj + vn * dl);
+        const float qphi4 = 105.f * nqn * nj * nn -
+                            15.f * (tr * nj * nn + 2.f * qn[j] * nn + 2.f * qn[n] * nj + nqn * dl) +
+                            3.f * tr * dl + 6.f * Q[j][n];
+        out[3 + 3 * i + n] -= sg * (c * phi2 - vphi3 + 0.5f * qphi4);
+      }
+#pragma unroll
+      for (int u = 0; u < 6; ++u) {
+        const int k = u < 3 ? 0 : (u < 5 ? 1 : 2);
+        const int n = u < 3 ? u : (u < 5 ? u - 2 : 2);
+        const float nk = nv[k], nn = nv[n];
+        const float djk = j == k ? 1.f : 0.f, djn = j == n ? 1.f : 0.f, dkn = k == n ? 1.f : 0.f;
+        const float nnn = nj * nk * nn;
+        const float dsum = djk * nn + djn * nk + dkn * nj;
+        const float phi3 = -15.f * nnn + 3.f * dsum;
+        const float vphi4 = 105.f * vn * nnn -
+                            15.f * (v[j] * nk * nn + v[k] * nj * nn + v[n] * nj * nk + vn * dsum) +
+                            3.f * (v[j] * dkn + v[k] * djn + v[n] * djk);
+        const float qphi5 =
+            -945.f * nqn * nnn +
+            105.f * (tr * nnn + 2.f * (qn[j] * nk * nn + qn[k] * nj * nn + qn[n] * nj * nk) + nqn * dsum) -
+            15.f * (2.f * (qn[j] * dkn + qn[k] * djn + qn[n] * djk) + nj * (tr * dkn + 2.f * Q[k][n]) +
+                    nk * (tr * djn + 2.f * Q[j][n]) + nn * (tr * djk + 2.f * Q[j][k]));
+        out[12 + 6 * i + u] -= sg * (c * phi3 - vphi4 + 0.5f * qphi5);
+      }
+    }
+  }
+}
+
 __device__ __forceinline__ float3 leaf_center(uint32_t key, float h) {
   auto compact = [](uint32_t v) {
     v &= 0x09249249u;
@@ -138,29 +240,31 @@ struct FwdArgs {
   FarIO f;
 };
 
-// this thread's row of a 128 x H accumulator -> bias + SiLU -> BF16 act tile
-__device__ void epilogue_hidden(uint32_t tmem, const float* bias, __nv_bfloat16* act,
+// row `row` of a 128 x H accumulator -> bias + SiLU -> BF16 activation tile
+__device__ void epilogue_hidden(uint32_t tmem, int row, const float* bias, __nv_bfloat16* act,
                                 float* z_out, __nv_bfloat16* h_out) {
-  const int warp = threadIdx.x >> 5;
-  const uint32_t lane_base = static_cast<uint32_t>(32 * (warp & 3)) << 16;
+  const uint32_t lane_base = static_cast<uint32_t>(32 * ((threadIdx.x >> 5) & 3)) << 16;
+  char* base = reinterpret_cast<char*>(act);
   for (int c0 = 0; c0 < H; c0 += 16) {
     float v[16];
     tc::tmem_ld16(tmem + lane_base + c0, v);
-    __align__(16) __nv_bfloat16 b[16];
+    __align__(16) __nv_bfloat162 b[8];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const float z = v[i] + bias[c0 + i];
-      if (z_out) z_out[c0 + i] = z;
-      b[i] = __float2bfloat16(silu(z));
+    for (int i = 0; i < 8; ++i) {
+      const float z0 = v[2 * i] + bias[c0 + 2 * i], z1 = v[2 * i + 1] + bias[c0 + 2 * i + 1];
+      if (z_out) {
+        z_out[c0 + 2 * i] = z0;
+        z_out[c0 + 2 * i + 1] = z1;
+      }
+      b[i] = __floats2bfloat162_rn(silu(z0), silu(z1));
     }
-    char* base = reinterpret_cast<char*>(act);
-    *reinterpret_cast<uint4*>(base + tc::kmajor_offset(threadIdx.x, c0, H)) =
+    *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, c0, H)) =
         *reinterpret_cast<uint4*>(&b[0]);
-    *reinterpret_cast<uint4*>(base + tc::kmajor_offset(threadIdx.x, c0 + 8, H)) =
-        *reinterpret_cast<uint4*>(&b[8]);
+    *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, c0 + 8, H)) =
+        *reinterpret_cast<uint4*>(&b[4]);
     if (h_out) {
       *reinterpret_cast<uint4*>(h_out + c0) = *reinterpret_cast<uint4*>(&b[0]);
-      *reinterpret_cast<uint4*>(h_out + c0 + 8) = *reinterpret_cast<uint4*>(&b[8]);
+      *reinterpret_cast<uint4*>(h_out + c0 + 8) = *reinterpret_cast<uint4*>(&b[4]);
     }
   }
 }
@@ -172,15 +276,23 @@ __device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& ph) {
   return ok;
 }
 
+// group-local fence + barrier: smem writes -> async proxy, TMEM reads done
+__device__ __forceinline__ void group_handoff(int g) {
+  tc::fence_smem_to_async();
+  tc::fence_before_sync();
+  group_sync(g);
+  tc::fence_after_sync();
+}
+
 template <bool FAR>
 __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int rows,
                                                            const __nv_bfloat16* __restrict__ W,
                                                            const float* __restrict__ bias) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   FwdSmem& S = *reinterpret_cast<FwdSmem*>(smem_raw);
-  if (threadIdx.x < 32) tc::tmem_alloc(&S.tmem, 128);
+  if (threadIdx.x < 32) tc::tmem_alloc(&S.tmem, 128 * kGroups);
   if (threadIdx.x == 0) {
-    mbar_init(&S.bar, 1);
+    for (int g = 0; g < kGroups; ++g) mbar_init(&S.bar[g], 1);
     fence_mbar_init();
   }
   stage_kmajor(S.w1, W + W1o, H, IN);
@@ -192,33 +304,42 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  const uint32_t tmem = S.tmem;
+  const int grp = threadIdx.x >> 7;   // warpgroup
+  const int lt = threadIdx.x & 127;   // row of the group's tile
+  const uint32_t tmem = S.tmem + static_cast<uint32_t>(128 * grp);
   const uint32_t lane_base = static_cast<uint32_t>(32 * ((threadIdx.x >> 5) & 3)) << 16;
+  __nv_bfloat16* act = S.act[grp];
+  uint64_t* bar = &S.bar[grp];
   uint32_t ph = 0;
   bool ok = true;
   const int ntiles = (rows + 127) / 128;
-  for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-    const int row = tile * 128 + threadIdx.x;
+  for (int tile = kGroups * blockIdx.x + grp; tile < ntiles && ok; tile += kGroups * gridDim.x) {
+    const int row = tile * 128 + lt;
     const bool act_row = row < rows;
-    PairScale sc{0.f, 0.f, 0.f};
     int leaf = 0;
     // input tile (K = 48)
     {
-      char* base = reinterpret_cast<char*>(S.act);
+      char* base = reinterpret_cast<char*>(act);
       if constexpr (FAR) {
         float f[IN];
+        float* ax = S.aux[grp][lt];
         if (act_row) {
           leaf = A.f.pair_leaf[row];
           const float3 cT = leaf_center(A.f.leaf_key[leaf], A.f.h);
-          sc = pair_features(A.f.rec + static_cast<int64_t>(A.f.pair_cell[row]) * kRecFloats,
-                             cT.x, cT.y, cT.z, A.f.h, f);
+          const PairScale sc = pair_features(
+              A.f.rec + static_cast<int64_t>(A.f.pair_cell[row]) * kRecFloats, cT.x, cT.y, cT.z,
+              A.f.h, f);
+          m2l_quadrupole(f, ax);
+          ax[30] = sc.s2;
+          ax[31] = sc.s3;
+          ax[32] = sc.s4;
         } else {
           for (int q = 0; q < IN; ++q) f[q] = 0.f;
         }
         for (int k8 = 0; k8 < IN / 8; ++k8) {
-          __align__(16) __nv_bfloat16 b[8];
-          for (int q = 0; q < 8; ++q) b[q] = __float2bfloat16(f[8 * k8 + q]);
-          *reinterpret_cast<uint4*>(base + tc::kmajor_offset(threadIdx.x, 8 * k8, IN)) =
+          __align__(16) __nv_bfloat162 b[4];
+          for (int q = 0; q < 4; ++q) b[q] = __floats2bfloat162_rn(f[8 * k8 + 2 * q], f[8 * k8 + 2 * q + 1]);
+          *reinterpret_cast<uint4*>(base + tc::kmajor_offset(lt, 8 * k8, IN)) =
               *reinterpret_cast<uint4*>(b);
         }
       } else {
@@ -226,20 +347,16 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
           uint4 v = make_uint4(0, 0, 0, 0);
           if (act_row)
             v = *reinterpret_cast<const uint4*>(A.r.X + static_cast<int64_t>(row) * IN + 8 * k8);
-          *reinterpret_cast<uint4*>(base + tc::kmajor_offset(threadIdx.x, 8 * k8, IN)) = v;
+          *reinterpret_cast<uint4*>(base + tc::kmajor_offset(lt, 8 * k8, IN)) = v;
         }
       }
     }
     const __nv_bfloat16* wl[3] = {S.w1, S.w2, S.w3};
     for (int l = 0; l < 3 && ok; ++l) {
-      tc::fence_smem_to_async();
-      tc::fence_before_sync();
-      __syncthreads();
-      tc::fence_after_sync();
-      if (threadIdx.x == 0)
-        tc::gemm_issue(tmem, S.act, wl[l], l == 0 ? IN : H, tc::idesc_bf16(128, H), false,
-                       &S.bar, 0);
-      if (!__syncthreads_and(wait_mma(&S.bar, ph))) {
+      group_handoff(grp);
+      if (lt == 0)
+        tc::gemm_issue(tmem, act, wl[l], l == 0 ? IN : H, tc::idesc_bf16(128, H), false, bar, 0);
+      if (!group_sync_and(grp, wait_mma(bar, ph))) {
         ok = false;
         break;
       }
@@ -249,16 +366,12 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
         if (A.r.z_store && act_row) zo = A.r.z_store + (static_cast<int64_t>(l) * rows + row) * H;
         if (A.r.h_store && act_row) ho = A.r.h_store + (static_cast<int64_t>(l) * rows + row) * H;
       }
-      epilogue_hidden(tmem, S.bias + l * H, S.act, zo, ho);
+      epilogue_hidden(tmem, lt, S.bias + l * H, act, zo, ho);
     }
     if (!ok) break;
-    tc::fence_smem_to_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (threadIdx.x == 0)
-      tc::gemm_issue(tmem, S.act, S.w4, H, tc::idesc_bf16(128, OUT), false, &S.bar, 0);
-    if (!__syncthreads_and(wait_mma(&S.bar, ph))) {
+    group_handoff(grp);
+    if (lt == 0) tc::gemm_issue(tmem, act, S.w4, H, tc::idesc_bf16(128, OUT), false, bar, 0);
+    if (!group_sync_and(grp, wait_mma(bar, ph))) {
       ok = false;
       break;
     }
@@ -278,8 +391,10 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
           const int c = c0 + i;
           float x = 0.f;
           if (act_row && c < NOUT) {
-            const float s = c < 3 ? sc.s2 : (c < 12 ? sc.s3 : sc.s4);
-            x = (v[i] + S.bias[B4o + c]) * s;
+            // analytic M2L + learned residual, back to physical units
+            const float* ax = S.aux[grp][lt];
+            const float s = c < 3 ? ax[30] : (c < 12 ? ax[31] : ax[32]);
+            x = (ax[c] + v[i] + S.bias[B4o + c]) * s;
           }
 #pragma unroll
           for (int off = 1; off < 32; off <<= 1) {
@@ -303,13 +418,13 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
       }
     }
     tc::fence_before_sync();
-    __syncthreads();
+    group_sync(grp);
     tc::fence_after_sync();
   }
-  if (!ok && threadIdx.x == 0) flag_status(kStatusTimeout);
+  if (!ok && lt == 0) flag_status(kStatusTimeout);
   tc::fence_before_sync();
   __syncthreads();
-  if (threadIdx.x < 32) tc::tmem_dealloc(tmem, 128);
+  if (threadIdx.x < 32) tc::tmem_dealloc(S.tmem, 128 * kGroups);
 }
 
 // ---- training data: features + exact local expansions of sampled pairs ----------
@@ -322,7 +437,8 @@ __global__ void pair_targets_kernel(int npairs, int stride, const int* __restric
                                     const int* __restrict__ cell_count,
                                     const float4* __restrict__ sp, const float4* __restrict__ sa,
                                     const int* __restrict__ leaf_of_particle, float h,
-                                    __nv_bfloat16* __restrict__ X, float* __restrict__ T) {
+                                    __nv_bfloat16* __restrict__ X, float* __restrict__ T,
+                                    float* __restrict__ Aout) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= npairs) return;
@@ -368,6 +484,11 @@ __global__ void pair_targets_kernel(int npairs, int stride, const int* __restric
     const PairScale sc =
         pair_features(rec + static_cast<int64_t>(g) * kRecFloats, cT.x, cT.y, cT.z, h, f);
     for (int q = 0; q < IN; ++q) X[static_cast<int64_t>(warp) * IN + q] = __float2bfloat16(f[q]);
+    if (Aout) {
+      float a[NOUT];
+      m2l_quadrupole(f, a);
+      for (int q = 0; q < OUT; ++q) Aout[static_cast<int64_t>(warp) * OUT + q] = q < NOUT ? a[q] : 0.f;
+    }
     for (int q = 0; q < OUT; ++q) {
       float v = 0.f;
       if (q < NOUT) {
@@ -376,6 +497,47 @@ __global__ void pair_targets_kernel(int npairs, int stride, const int* __restric
       }
       T[static_cast<int64_t>(warp) * OUT + q] = v;
     }
+  }
+}
+
+// ---- analytic far field of the local-expansion path (no network) ---------------------
+// One thread per (leaf, cell) pair: features -> M2L -> physical units -> sum
+// over the warp's runs of equal leaves -> atomics into the leaf's expansion.
+__global__ void __launch_bounds__(256) m2l_pairs_kernel(int npairs, const int* __restrict__ pair_leaf,
+                                                        const int* __restrict__ pair_cell,
+                                                        const uint32_t* __restrict__ leaf_key,
+                                                        const float* __restrict__ rec, float h,
+                                                        float* __restrict__ leaf_local) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool act_row = row < npairs;
+  float a[NOUT];
+  PairScale sc{0.f, 0.f, 0.f};
+  int leaf = 0;
+  if (act_row) {
+    float f[IN];
+    leaf = pair_leaf[row];
+    const float3 cT = leaf_center(leaf_key[leaf], h);
+    sc = pair_features(rec + static_cast<int64_t>(pair_cell[row]) * kRecFloats, cT.x, cT.y, cT.z,
+                       h, f);
+    m2l_quadrupole(f, a);
+  } else {
+#pragma unroll
+    for (int q = 0; q < NOUT; ++q) a[q] = 0.f;
+  }
+  const int my = act_row ? leaf : -1 - lane;
+  const int up = __shfl_up_sync(0xffffffffu, my, 1);
+  const bool head = act_row && (lane == 0 || up != my);
+#pragma unroll
+  for (int c = 0; c < NOUT; ++c) {
+    float x = a[c] * (c < 3 ? sc.s2 : (c < 12 ? sc.s3 : sc.s4));
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const float o = __shfl_down_sync(0xffffffffu, x, off);
+      const int ol = __shfl_down_sync(0xffffffffu, my, off);
+      if (lane + off < 32 && ol == my) x += o;
+    }
+    if (head) atomicAdd(leaf_local + static_cast<int64_t>(leaf) * OUT + c, x);
   }
 }
 
@@ -467,10 +629,11 @@ __global__ void __launch_bounds__(128) gemm_tn_kernel(const __nv_bfloat16* __res
 }
 
 // ---- element-wise training kernels ---------------------------------------------------
-// dY = 2 (Y - T) / (rows * NOUT) on the used outputs; loss partial sums.
+// dY = 2 w_r (Y - T) / (rows * NOUT) on the used outputs (w_r = 1 without
+// row weights); loss partial sums of w_r (Y - T)^2.
 __global__ void loss_grad_kernel(int rows, const float* __restrict__ Y, const float* __restrict__ T,
-                                 __nv_bfloat16* __restrict__ dY, float* __restrict__ dY32,
-                                 float* __restrict__ loss) {
+                                 const float* __restrict__ wrow, __nv_bfloat16* __restrict__ dY,
+                                 float* __restrict__ dY32, float* __restrict__ loss) {
   const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   const int64_t n = static_cast<int64_t>(rows) * OUT;
   float l = 0.f;
@@ -478,9 +641,10 @@ __global__ void loss_grad_kernel(int rows, const float* __restrict__ Y, const fl
     const int c = static_cast<int>(i % OUT);
     float g = 0.f;
     if (c < NOUT) {
+      const float w = wrow ? wrow[i / OUT] : 1.f;
       const float e = Y[i] - T[i];
-      l = e * e;
-      g = 2.f * e / (static_cast<float>(rows) * NOUT);
+      l = w * e * e;
+      g = 2.f * w * e / (static_cast<float>(rows) * NOUT);
     }
     dY[i] = __float2bfloat16(g);
     dY32[i] = g;
@@ -593,10 +757,20 @@ int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
   FwdArgs<true> A;
   A.r = RowsIO{nullptr, nullptr, nullptr, nullptr};
   A.f = FarIO{pair_leaf, pair_cell, leaf_key, rec, h, leaf_local};
-  const int ntiles = (npairs + 127) / 128;
-  const int grid = ntiles < device_sm_count() ? ntiles : device_sm_count();
+  const int nctas = ((npairs + 127) / 128 + kGroups - 1) / kGroups;
+  const int grid = nctas < device_sm_count() ? nctas : device_sm_count();
   mlp_fwd_kernel<true><<<grid, kThreads, sizeof(FwdSmem), s>>>(
       A, npairs, static_cast<const __nv_bfloat16*>(W), bias);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int m2l_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
+                        const uint32_t* leaf_key, const float* rec, float h, float* leaf_local,
+                        cudaStream_t s) {
+  if (npairs <= 0) return FVX_OK;
+  mlp::m2l_pairs_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(npairs, pair_leaf, pair_cell,
+                                                             leaf_key, rec, h, leaf_local);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
@@ -605,11 +779,11 @@ int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const 
                             const uint32_t* leaf_key, const float* rec, const int* cell_start,
                             const int* cell_count, const float4* sp, const float4* sa,
                             const int* leaf_of_particle, float h, void* X, float* T,
-                            cudaStream_t s) {
+                            float* A, cudaStream_t s) {
   if (npairs <= 0) return FVX_OK;
   mlp::pair_targets_kernel<<<(npairs * 32 + 255) / 256, 256, 0, s>>>(
       npairs, stride, pair_leaf, pair_cell, leaf_key, rec, cell_start, cell_count, sp, sa,
-      leaf_of_particle, h, static_cast<__nv_bfloat16*>(X), T);
+      leaf_of_particle, h, static_cast<__nv_bfloat16*>(X), T, A);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
@@ -646,8 +820,8 @@ int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, f
   A.r = RowsIO{static_cast<const __nv_bfloat16*>(X), Y, z_store,
                static_cast<__nv_bfloat16*>(h_store)};
   A.f = FarIO{nullptr, nullptr, nullptr, nullptr, 0.f, nullptr};
-  const int ntiles = (rows + 127) / 128;
-  const int grid = ntiles < fvx::device_sm_count() ? ntiles : fvx::device_sm_count();
+  const int nctas = ((rows + 127) / 128 + kGroups - 1) / kGroups;
+  const int grid = nctas < fvx::device_sm_count() ? nctas : fvx::device_sm_count();
   mlp_fwd_kernel<false><<<grid, kThreads, sizeof(FwdSmem), static_cast<cudaStream_t>(stream)>>>(
       A, rows, static_cast<const __nv_bfloat16*>(W), bias);
   FVX_LAUNCH_CHECK();
@@ -676,14 +850,14 @@ int fvx_mlp_gemm(const void* A, int lda, int tA, const void* B, int ldb, int tB,
   return FVX_OK;
 }
 
-int fvx_mlp_loss_grad(int rows, const float* Y, const float* T, void* dY, float* dY32,
-                      float* loss, void* stream) {
+int fvx_mlp_loss_grad(int rows, const float* Y, const float* T, const float* row_weight, void* dY,
+                      float* dY32, float* loss, void* stream) {
   FVX_ARG_CHECK(rows >= 0 && Y && T && dY && dY32 && loss, "null argument");
   const int64_t n = static_cast<int64_t>(rows) * fvx::mlp::OUT;
   if (n == 0) return FVX_OK;
   fvx::mlp::loss_grad_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0,
                                static_cast<cudaStream_t>(stream)>>>(
-      rows, Y, T, static_cast<__nv_bfloat16*>(dY), dY32, loss);
+      rows, Y, T, row_weight, static_cast<__nv_bfloat16*>(dY), dY32, loss);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }

@@ -896,7 +896,10 @@ int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const 
                             const uint32_t* leaf_key, const float* rec, const int* cell_start,
                             const int* cell_count, const float4* sp, const float4* sa,
                             const int* leaf_of_particle, float h, void* X, float* T,
-                            cudaStream_t s);
+                            float* A, cudaStream_t s);
+int m2l_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
+                        const uint32_t* leaf_key, const float* rec, float h, float* leaf_local,
+                        cudaStream_t s);
 
 }  // namespace fvx
 
@@ -906,10 +909,12 @@ struct fvx_tree {
       sg, lists_meta, near_list, far_list, bbox;
   int64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the last evaluation launch
-  // learned far field
+  // far-field method of the pairs beyond theta_l (FVX_FAR_*)
+  int far_method = FVX_FAR_M2P;
   const void* mlp_W = nullptr;
   const float* mlp_b = nullptr;
   double theta_l = 0.0;
+  cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // around the local-expansion stage
   fvx::DevBuf lrn_meta, lrn_leaf, lrn_cell, leaf_local;
   int n_learned = 0;
   // the last sweep's tree, for sampling training pairs
@@ -1108,9 +1113,9 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   V.key = reinterpret_cast<const uint32_t*>(lvb + 2 * total_cells);
   V.child_lo = lvb + 3 * total_cells;
   V.child_hi = lvb + 4 * total_cells;
-  const bool learned = T->theta_l > 0.0;
+  const bool learned = T->far_method != FVX_FAR_M2P && T->theta_l > 0.0;
   V.mac_kl = learned ? 0.75 / (T->theta_l * T->theta_l) : 0.0;
-  V.learned_only = learned && T->mlp_W != nullptr;
+  V.learned_only = learned ? 1 : 0;
   if ((rc = grow(T->lists_meta, 4 * size_t(nleaf) * 4 + 64))) return rc;
   if (learned && (rc = grow(T->lrn_meta, 4 * size_t(nleaf) * 2 + 64))) return rc;
   LearnedLists LL{nullptr, nullptr, nullptr, nullptr, 0};
@@ -1184,13 +1189,24 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   A.out_a = out_a;
   A.out_b = out_b;
   A.leaf_local = nullptr;
-  if (learned && T->mlp_W && lrn_total > 0) {
+  if (learned && lrn_total > 0) {
     if ((rc = grow(T->leaf_local, sizeof(float) * 32 * size_t(nleaf)))) return rc;
     FVX_CUDA_TRY(cudaMemsetAsync(T->leaf_local.p, 0, sizeof(float) * 32 * size_t(nleaf), s));
-    if ((rc = mlp_farfield_launch(static_cast<int>(lrn_total), P<int>(T->lrn_leaf),
-                                  P<int>(T->lrn_cell), leaves.key, rec, static_cast<float>(h),
-                                  T->mlp_W, T->mlp_b, P<float>(T->leaf_local), s)))
-      return rc;
+    if (!T->ev2) {
+      FVX_CUDA_TRY(cudaEventCreate(&T->ev2));
+      FVX_CUDA_TRY(cudaEventCreate(&T->ev3));
+    }
+    FVX_CUDA_TRY(cudaEventRecord(T->ev2, s));
+    if (T->far_method == FVX_FAR_LEARNED)
+      rc = mlp_farfield_launch(static_cast<int>(lrn_total), P<int>(T->lrn_leaf),
+                               P<int>(T->lrn_cell), leaves.key, rec, static_cast<float>(h),
+                               T->mlp_W, T->mlp_b, P<float>(T->leaf_local), s);
+    else
+      rc = m2l_farfield_launch(static_cast<int>(lrn_total), P<int>(T->lrn_leaf),
+                               P<int>(T->lrn_cell), leaves.key, rec, static_cast<float>(h),
+                               P<float>(T->leaf_local), s);
+    if (rc) return rc;
+    FVX_CUDA_TRY(cudaEventRecord(T->ev3, s));
     A.leaf_local = P<float>(T->leaf_local);
   }
   T->last_L = L;
@@ -1246,6 +1262,8 @@ void fvx_tree_destroy(fvx_tree* T) {
   if (!T) return;
   if (T->ev0) cudaEventDestroy(T->ev0);
   if (T->ev1) cudaEventDestroy(T->ev1);
+  if (T->ev2) cudaEventDestroy(T->ev2);
+  if (T->ev3) cudaEventDestroy(T->ev3);
   fvx::DevBuf* bufs[] = {&T->keys0,   &T->keys1,     &T->idx0,     &T->idx1,     &T->table,
                          &T->scan_tmp, &T->flags,   &T->cid,      &T->levels,   &T->counts,
                          &T->rec,     &T->sp,       &T->sa,       &T->sg,       &T->lists_meta,
@@ -1263,21 +1281,36 @@ int fvx_tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const d
                          out_a, out_b, stats, static_cast<cudaStream_t>(stream));
 }
 
-int fvx_tree_set_learned(fvx_tree* T, const void* W, const float* b, double theta_learned) {
+int fvx_tree_set_far_field(fvx_tree* T, int method, const void* W, const float* b,
+                           double theta_local) {
   FVX_ARG_CHECK(T != nullptr, "null tree handle");
-  FVX_ARG_CHECK(theta_learned >= 0.0 && theta_learned < 1.0, "bad theta_learned");
-  FVX_ARG_CHECK((W == nullptr) == (b == nullptr), "weights and biases go together");
-  T->mlp_W = W;
-  T->mlp_b = b;
-  T->theta_l = theta_learned;
+  FVX_ARG_CHECK(method == FVX_FAR_M2P || method == FVX_FAR_M2L || method == FVX_FAR_LEARNED,
+                "unknown far-field method %d", method);
+  FVX_ARG_CHECK(method == FVX_FAR_M2P || (theta_local > 0.0 && theta_local < 1.0),
+                "bad theta_local");
+  FVX_ARG_CHECK(method != FVX_FAR_LEARNED || (W != nullptr && b != nullptr),
+                "the learned far field needs weights and biases");
+  T->far_method = method;
+  T->mlp_W = method == FVX_FAR_LEARNED ? W : nullptr;
+  T->mlp_b = method == FVX_FAR_LEARNED ? b : nullptr;
+  T->theta_l = method == FVX_FAR_M2P ? 0.0 : theta_local;
   return FVX_OK;
 }
 
-int fvx_tree_sample_pairs(fvx_tree* T, int max_pairs, void* X, float* Tgt, int* n_out,
+int fvx_tree_last_local_ms(fvx_tree* T, float* ms) {
+  FVX_ARG_CHECK(T && ms, "null argument");
+  *ms = 0.f;
+  if (!T->ev2 || T->n_learned <= 0) return FVX_OK;
+  FVX_CUDA_TRY(cudaEventSynchronize(T->ev3));
+  FVX_CUDA_TRY(cudaEventElapsedTime(ms, T->ev2, T->ev3));
+  return FVX_OK;
+}
+
+int fvx_tree_sample_pairs(fvx_tree* T, int max_pairs, void* X, float* Tgt, float* A, int* n_out,
                           void* stream) {
   FVX_ARG_CHECK(T && X && Tgt && n_out && max_pairs > 0, "bad arguments");
   *n_out = 0;
-  FVX_ARG_CHECK(T->theta_l > 0.0, "sampling needs theta_learned > 0 on the last sweep");
+  FVX_ARG_CHECK(T->theta_l > 0.0, "sampling needs the local-expansion path on the last sweep");
   const int n = T->n_learned;
   if (n <= 0) return FVX_OK;
   const int stride = n > max_pairs ? n / max_pairs : 1;
@@ -1285,7 +1318,7 @@ int fvx_tree_sample_pairs(fvx_tree* T, int max_pairs, void* X, float* Tgt, int* 
   int rc = fvx::mlp_pair_targets_launch(
       np, stride, fvx::P<int>(T->lrn_leaf), fvx::P<int>(T->lrn_cell), T->last_leaf_key,
       fvx::P<float>(T->rec), T->last_cell_start, T->last_cell_count, fvx::P<float4>(T->sp),
-      fvx::P<float4>(T->sa), T->last_cid, static_cast<float>(T->last_h), X, Tgt,
+      fvx::P<float4>(T->sa), T->last_cid, static_cast<float>(T->last_h), X, Tgt, A,
       static_cast<cudaStream_t>(stream));
   if (rc) return rc;
   *n_out = np;

@@ -1,23 +1,30 @@
 """Learned far-field operator of the treecode (new: the reference has no tree).
 
 A (target leaf T, source cell S) pair accepted by the opening test is mapped
-by a small MLP to the local expansion of S's singular Biot-Savart field about
-T's centre: velocity, velocity gradient and second derivatives (30 numbers),
-which the evaluation kernel applies once per target particle.  The inputs are
-scale free -- R/d, h_S/d, h_T/d and the cell's moments M0, M1/h_S, M2/h_S^2
-divided by m = |M0| + |M1|/h_S + |M2|/h_S^2 -- and so are the outputs
-(u d^2/m, J d^3/m, H d^4/m); the kernels undo the scaling.
+to the local expansion of S's singular Biot-Savart field about T's centre:
+velocity, velocity gradient and second derivatives (30 numbers), which the
+evaluation kernel applies once per target particle.  The expansion is the
+analytic multipole-to-local translation of S's quadrupole plus a learned
+residual: a small MLP trained on exact FP64 local expansions, i.e. on what
+the truncated quadrupole misses (the part of the higher moments that the
+known moments and the cell geometry predict).  The inputs are scale free --
+R/d, h_S/d, h_T/d and the cell's moments M0, M1/h_S, M2/h_S^2 divided by
+m = |M0| + |M1|/h_S + |M2|/h_S^2 -- and so are the outputs (u d^2/m, J d^3/m,
+H d^4/m); the kernels undo the scaling.
 
 Everything runs on the tensor cores through the C ABI:
-  * inference inside the sweep (fvx_tree_set_learned: the MLP kernel computes
-    the features from the pair list and accumulates the expansions);
+  * inference inside the sweep (TreeSweeper.set_far_field("learned"): one
+    kernel computes the features from the pair list, the analytic translation
+    on the CUDA cores and the residual on the tensor cores, and accumulates the
+    expansions per leaf);
   * training (``FarFieldMLP.fit``): forward with stored activations, then per
     layer the weight gradient dW = dZ^T H and the input gradient dH = dZ W as
     BF16 tcgen05 GEMMs with FP32 accumulation, SiLU backward, Adam on FP32
     master weights with a BF16 copy for the kernels;
-  * training data (``harvest``): pairs sampled from the learned lists of the
-    solver's own particle fields, with targets summed directly in FP64 over
-    the source cell's particles.
+  * training data (``harvest``): pairs sampled from the local-expansion lists
+    of the solver's own particle fields, with targets summed directly in FP64
+    over the source cell's particles; the network fits T - A (exact minus
+    analytic).
 
 Weight packing (fvx_mlp_forward): W1 128x48, W2 128x128, W3 128x128, W4 32x128
 as [out][in] BF16 back to back; biases 128, 128, 128, 32 in FP32.
@@ -47,7 +54,8 @@ def init_weights(seed=0):
     rng = np.random.default_rng(seed)
     w = np.zeros(NW, dtype=np.float32)
     for li, ((o, i), off) in enumerate(zip(LAYERS, W_OFFSETS)):
-        std = math.sqrt(1.0 / i) if li == 3 else math.sqrt(2.0 / i)
+        # the output layer starts near zero: an untrained network adds no residual
+        std = 0.01 * math.sqrt(1.0 / i) if li == 3 else math.sqrt(2.0 / i)
         fan_in = NFEAT if li == 0 else i
         blk = rng.standard_normal((o, i)) * std * math.sqrt(i / fan_in)
         if li == 0:
@@ -133,9 +141,10 @@ class FarFieldMLP:
             self._bufs = {rows: bufs}
         return bufs
 
-    def gradients(self, X, T):
-        """Loss sum((Y - T)^2) over the 30 used outputs (device scalar) and the
-        gradients of the mean loss into self.gw / self.gb."""
+    def gradients(self, X, T, weights=None):
+        """Loss sum(w_r (Y - T)^2) over the 30 used outputs (device scalar; w_r = 1
+        without row weights) and the gradients of the mean loss into self.gw /
+        self.gb."""
         rows = X.shape[0]
         Y, Z, Hs = self.forward(X, store=True)
         bf = self._buffers(rows)
@@ -144,8 +153,10 @@ class FarFieldMLP:
         bf["loss"].zero_()
         st = self._stream()
         lib = self.lib
-        _capi.check(lib.fvx_mlp_loss_grad(rows, Y.data_ptr(), T.data_ptr(), bf["dY"].data_ptr(),
-                                          bf["dY32"].data_ptr(), bf["loss"].data_ptr(), st))
+        _capi.check(lib.fvx_mlp_loss_grad(rows, Y.data_ptr(), T.data_ptr(),
+                                          None if weights is None else weights.data_ptr(),
+                                          bf["dY"].data_ptr(), bf["dY32"].data_ptr(),
+                                          bf["loss"].data_ptr(), st))
         split = max(1, rows // 1024)
         gw, wb = self.gw.data_ptr(), self.wb.data_ptr()
         es_w, es_b = self.gw.element_size(), self.wb.element_size()
@@ -181,9 +192,11 @@ class FarFieldMLP:
                                           self.mb.data_ptr(), self.vb.data_ptr(), None, lr, b1,
                                           b2, eps, self.step_count, st))
 
-    def fit(self, X, T, steps=2000, batch=8192, lr=2e-3, lr_final=2e-5, seed=0, log_every=0):
-        """Adam over random minibatches of (X, T); cosine learning-rate decay.
-        Returns the mean-square losses at the logging points."""
+    def fit(self, X, T, steps=2000, batch=8192, lr=2e-3, lr_final=2e-5, seed=0, log_every=0,
+            weights=None):
+        """Adam over random minibatches of (X, T) (optional per-row loss weights);
+        cosine learning-rate decay.  Returns the mean-square losses at the
+        logging points."""
         n = X.shape[0]
         g = torch.Generator(device=self.device)
         g.manual_seed(seed)
@@ -191,30 +204,45 @@ class FarFieldMLP:
         hist = []
         for it in range(steps):
             idx = torch.randint(0, n, (batch,), device=self.device, generator=g)
-            loss, _ = self.gradients(X[idx].contiguous(), T[idx].contiguous())
+            loss, _ = self.gradients(X[idx].contiguous(), T[idx].contiguous(),
+                                     None if weights is None else weights[idx].contiguous())
             c = 0.5 * (1.0 + math.cos(math.pi * it / max(1, steps - 1)))
             self.adam(lr_final + (lr - lr_final) * c)
             if log_every and (it % log_every == 0 or it == steps - 1):
                 hist.append((it, float(loss.item()) / (batch * NOUT)))
         return hist
 
-    def errors(self, X, T):
-        """Per-row relative error |Y - T| / |T| over the 30 used outputs."""
+    def errors(self, X, T, A):
+        """Per-row relative error |A + Y - T| / |T| over the 30 used outputs
+        (A: the analytic translation, T: the exact expansion)."""
         Y = self.forward(X)
-        d = (Y[:, :NOUT] - T[:, :NOUT]).norm(dim=1)
+        d = (A[:, :NOUT] + Y[:, :NOUT] - T[:, :NOUT]).norm(dim=1)
         return d / T[:, :NOUT].norm(dim=1).clamp_min(1e-30)
 
 
-def harvest(sweeper, field_pos, field_gamma, field_sigma, n, max_pairs, theta_learned=None,
+def relative_weights(T):
+    """Per-row loss weights mean(|T|^2) / |T_r|^2: the fit then minimises the
+    relative error of each pair's expansion rather than the absolute one."""
+    n2 = T[:, :NOUT].pow(2).sum(dim=1).clamp_min(1e-30)
+    return (n2.mean() / n2).float().contiguous()
+
+
+def analytic_errors(T, A):
+    """Per-row relative error |A - T| / |T| of the analytic translation alone."""
+    d = (A[:, :NOUT] - T[:, :NOUT]).norm(dim=1)
+    return d / T[:, :NOUT].norm(dim=1).clamp_min(1e-30)
+
+
+def harvest(sweeper, field_pos, field_gamma, field_sigma, n, max_pairs, theta_local=None,
             kernel="winckelmans"):
-    """Training pairs from one particle field: a velocity sweep lists the learned
-    pairs (theta_learned defaults to the sweeper's theta, i.e. every accepted
-    cell), then up to max_pairs of them are sampled with FP64 targets."""
-    th = theta_learned or sweeper.theta
-    prev = (sweeper._mlp, sweeper.theta_learned)
-    sweeper.set_learned(None, th)
+    """Training pairs from one particle field: a velocity sweep on the analytic
+    local-expansion path lists the pairs (theta_local defaults to the sweeper's
+    theta, i.e. every accepted cell), then up to max_pairs of them are sampled
+    with FP64 targets T and the analytic translation A.  Returns (X, T, A)."""
+    prev = (sweeper.far_method, sweeper._mlp, sweeper.theta_local)
+    sweeper.set_far_field("m2l", theta_local=theta_local)
     out = torch.empty((n, 3), dtype=torch.float64, device=field_pos.device)
     sweeper.sweep(_capi.PAIR_VELOCITY, kernel, field_pos, field_gamma, field_sigma, n, out)
-    X, T = sweeper.sample_pairs(max_pairs, device=field_pos.device)
-    sweeper.set_learned(*prev)
-    return X, T
+    X, T, A = sweeper.sample_pairs(max_pairs, device=field_pos.device)
+    sweeper.set_far_field(prev[0], prev[1], prev[2] or None)
+    return X, T, A

@@ -3,8 +3,11 @@
 ``TreeSweeper.sweep`` evaluates a self-sweep -- every particle as a target
 of every particle -- with direct FP32 pairs between near leaves and a
 quadrupole multipole expansion for cells accepted by the opening test
-|c_T - c_S| > (r_T + r_S) / theta (r = cell half diagonal).  theta = 0.5 and
-the leaf size are the defaults of the synthetic 2^20-particle sweep case.
+|c_T - c_S| > (r_T + r_S) / theta (r = cell half diagonal).  The accepted
+cells are evaluated either at every target particle ("m2p") or once per
+target leaf as a local expansion ("m2l": analytic translation; "learned":
+plus a tensor-core MLP residual), see ``set_far_field``.  theta = 0.5 and the
+leaf size are the defaults of the synthetic 2^20-particle sweep case.
 """
 from __future__ import annotations
 
@@ -29,7 +32,8 @@ class TreeSweeper:
         self.handle = h.value
         self.stats = np.zeros(8, dtype=np.int64)
         self._mlp = None
-        self.theta_learned = 0.0
+        self.far_method = "m2p"
+        self.theta_local = 0.0
 
     def __del__(self):
         try:
@@ -56,28 +60,40 @@ class TreeSweeper:
         _capi.check(self.lib.fvx_tree_last_eval_ms(self.handle, ctypes.byref(ms)))
         return float(ms.value)
 
-    # ---- learned far field ------------------------------------------------------
-    def set_learned(self, mlp=None, theta_learned=None):
-        """Routes the accepted cells with |dc|^2 > 3/4 (h_T + h_S)^2 / theta_learned^2
-        through ``mlp`` (a learned.FarFieldMLP; its device weights must outlive
-        the sweeps).  mlp=None with theta_learned > 0 only lists those pairs
-        (they stay on the quadrupole path) so that they can be sampled;
-        theta_learned=None or 0 turns the split off."""
-        th = 0.0 if not theta_learned else float(theta_learned)
-        self._mlp = mlp if th > 0.0 else None
+    # ---- far-field method ---------------------------------------------------------
+    def set_far_field(self, method="m2p", mlp=None, theta_local=None):
+        """"m2p": quadrupole at every target particle (default).  "m2l": the
+        accepted cells with |dc|^2 > 3/4 (h_T + h_S)^2 / theta_local^2 (all of
+        them for theta_local = theta, the default) go through per-leaf local
+        expansions from the analytic multipole-to-local translation.
+        "learned": the same plus the residual of ``mlp`` (a learned.FarFieldMLP
+        whose device weights must outlive the sweeps)."""
+        mid = {"m2p": _capi.FAR_M2P, "m2l": _capi.FAR_M2L, "learned": _capi.FAR_LEARNED}[method]
+        th = 0.0 if mid == _capi.FAR_M2P else float(theta_local or self.theta)
+        if mid == _capi.FAR_LEARNED and mlp is None:
+            raise ValueError("the learned far field needs a FarFieldMLP")
+        self._mlp = mlp if mid == _capi.FAR_LEARNED else None
         W = None if self._mlp is None else self._mlp.wb.data_ptr()
         b = None if self._mlp is None else self._mlp.b.data_ptr()
-        _capi.check(self.lib.fvx_tree_set_learned(self.handle, W, b, th))
-        self.theta_learned = th
+        _capi.check(self.lib.fvx_tree_set_far_field(self.handle, mid, W, b, th))
+        self.far_method = method
+        self.theta_local = th
+
+    def last_local_ms(self):
+        ms = ctypes.c_float(0.0)
+        _capi.check(self.lib.fvx_tree_last_local_ms(self.handle, ctypes.byref(ms)))
+        return float(ms.value)
 
     def sample_pairs(self, max_pairs, stream=None, device="cuda"):
-        """Features X (k, 48) BF16 and exact normalised targets T (k, 32) FP32 of up
-        to max_pairs learned pairs of the last sweep (evenly strided over its
-        learned list)."""
+        """Features X (k, 48) BF16, exact normalised targets T (k, 32) and the
+        analytic translation A (k, 32) of up to max_pairs local-path pairs of the
+        last sweep (evenly strided over its list)."""
         X = torch.empty((max_pairs, 48), dtype=torch.bfloat16, device=device)
         T = torch.empty((max_pairs, 32), dtype=torch.float32, device=device)
+        A = torch.empty((max_pairs, 32), dtype=torch.float32, device=device)
         st = stream if stream is not None else torch.cuda.current_stream(X.device).cuda_stream
         k = ctypes.c_int(0)
         _capi.check(self.lib.fvx_tree_sample_pairs(self.handle, int(max_pairs), X.data_ptr(),
-                                                    T.data_ptr(), ctypes.byref(k), st))
-        return X[: k.value], T[: k.value]
+                                                    T.data_ptr(), A.data_ptr(), ctypes.byref(k),
+                                                    st))
+        return X[: k.value], T[: k.value], A[: k.value]

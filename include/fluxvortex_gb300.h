@@ -202,18 +202,31 @@ int fvx_tree_sweep(fvx_tree* tree, int mode, int kernel, const double* pos, cons
 /* Device time of the last sweep's evaluation kernel (waits for it).  stats
  * of the same sweep: [6] near particle pairs, [7] far (target, cell) pairs. */
 int fvx_tree_last_eval_ms(fvx_tree* tree, float* ms);
-/* Learned far field (new; no reference counterpart).  theta_learned > 0
- * splits the accepted cells: those with |dc|^2 > 3/4 (h_T + h_S)^2 /
- * theta_learned^2 form the learned list (stats[4] = its length).  With W and
- * b set (device pointers in the fvx_mlp_forward packing, kept by the handle)
- * the learned pairs are evaluated by the tensor-core MLP into per-leaf local
- * expansions applied to each target; with W = b = NULL they stay on the
- * quadrupole path and are only listed (for sampling).  theta_learned = 0
- * turns the split off.  fvx_tree_sample_pairs: features X[k][48] (BF16) and
- * exact FP64-summed normalised targets T[k][32] (FP32) of k <= max_pairs
- * learned pairs of the last sweep, strided evenly over the list (*n_out = k). */
-int fvx_tree_set_learned(fvx_tree* tree, const void* W, const float* b, double theta_learned);
-int fvx_tree_sample_pairs(fvx_tree* tree, int max_pairs, void* X, float* T, int* n_out,
+/* Far-field method of the pairs beyond theta_local (new; no reference
+ * counterpart).  FVX_FAR_M2P (default): every accepted cell is evaluated at
+ * every target particle of the leaf from its quadrupole expansion.  The other
+ * two move the accepted cells with |dc|^2 > 3/4 (h_T + h_S)^2 / theta_local^2
+ * (all of them when theta_local = theta; stats[4] = their number) to a
+ * local-expansion path: one evaluation per (target leaf, source cell) pair
+ * gives the second-order local expansion (u, grad u, grad grad u) at the leaf
+ * centre, summed per leaf and applied to each target particle.
+ * FVX_FAR_M2L: the expansion is the analytic multipole-to-local translation
+ * of the quadrupole.  FVX_FAR_LEARNED: the analytic translation plus the
+ * tensor-core MLP's learned residual (W, b in the fvx_mlp_forward packing;
+ * device pointers kept by the handle).
+ * fvx_tree_last_local_ms: device time of the last sweep's local-expansion
+ * stage (waits for it).
+ * fvx_tree_sample_pairs: features X[k][48] (BF16), exact FP64-summed
+ * normalised targets T[k][32] (FP32) and, if A is not NULL, the analytic
+ * translation A[k][32] of k <= max_pairs local-path pairs of the last sweep,
+ * strided evenly over the list (*n_out = k). */
+#define FVX_FAR_M2P 0
+#define FVX_FAR_M2L 1
+#define FVX_FAR_LEARNED 2
+int fvx_tree_set_far_field(fvx_tree* tree, int method, const void* W, const float* b,
+                           double theta_local);
+int fvx_tree_last_local_ms(fvx_tree* tree, float* ms);
+int fvx_tree_sample_pairs(fvx_tree* tree, int max_pairs, void* X, float* T, float* A, int* n_out,
                           void* stream);
 
 /* ---- panel side of the hybrid panel-particle step (FP64) ------------------------
@@ -292,8 +305,9 @@ int fvx_uvlm_convert(int R, int n_keep, int ns, const double* W, const double* g
  * fvx_mlp_gemm: C[M][N] (+)= sum_k opA[m][k] opB[n][k], opA[m][k] = tA ?
  *   A[k*lda + m] : A[m*lda + k] (same for B), BF16 in, FP32 out, split over K
  *   into split_k slices added with atomics (accumulate != 0 adds into C).
- * fvx_mlp_loss_grad: mean-square loss over the 30 used outputs: loss += sum
- *   (Y - T)^2 (device scalar), dY = 2 (Y - T) / (30 rows) in BF16 and FP32.
+ * fvx_mlp_loss_grad: weighted mean-square loss over the 30 used outputs:
+ *   loss += sum w_r (Y - T)^2 (device scalar), dY = 2 w_r (Y - T) / (30 rows)
+ *   in BF16 and FP32; row_weight (w_r, FP32 [rows]) may be NULL (w_r = 1).
  * fvx_mlp_silu_back: dZ = dH SiLU'(Z) (BF16 out), db[c] += sum_r dZ[r][c].
  * fvx_mlp_colsum: db[c] += sum_r G[r][c].
  * fvx_mlp_adam: Adam step `step` (1-based) on FP32 master weights w with
@@ -304,8 +318,8 @@ int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, f
                     float* z_store, void* h_store, void* stream);
 int fvx_mlp_gemm(const void* A, int lda, int tA, const void* B, int ldb, int tB, float* C,
                  int ldc, int M, int N, int K, int split_k, int accumulate, void* stream);
-int fvx_mlp_loss_grad(int rows, const float* Y, const float* T, void* dY, float* dY32,
-                      float* loss, void* stream);
+int fvx_mlp_loss_grad(int rows, const float* Y, const float* T, const float* row_weight, void* dY,
+                      float* dY32, float* loss, void* stream);
 int fvx_mlp_silu_back(int rows, int cols, const float* dH, const float* Z, void* dZ, float* db,
                       void* stream);
 int fvx_mlp_colsum(int rows, int cols, const float* G, float* db, void* stream);

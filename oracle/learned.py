@@ -9,6 +9,9 @@ reference's to pin it to.  Its pins are mathematical:
     vector potential Psi_m = (1/4pi) sum a_m / |x - x_p| (u = curl Psi) with
     the derivative tensors of oracle/treecode.py; tested against the
     quadrupole far field and against a Taylor step;
+  * ``m2l``: the quadrupole expansion's local expansion (multipole to local,
+    second order), with the derivative tensors of 1/r from their closed form;
+    tested against ``local_expansion`` of compact clusters;
   * ``forward`` / ``gradients``: the network in FP64 with the same BF16
     rounding points as the tensor-core kernels (inputs, weights, hidden
     activations; dY and dZ for the backward GEMMs), tested against central
@@ -47,6 +50,75 @@ def local_expansion(x0, pos, alpha):
     J = np.einsum("ijm,pm,pjn->in", TC.EPS, a, D2)
     H = np.einsum("ijm,pm,pjkn->ikn", TC.EPS, a, D3)
     return u, J, H
+
+
+def _pairings(idx):
+    """Every way to pick disjoint pairs from the positions idx: (pairs, unpaired)."""
+    if not idx:
+        yield [], []
+        return
+    first, rest = idx[0], idx[1:]
+    for pr, rs in _pairings(rest):
+        yield pr, [first] + rs
+    for i, o in enumerate(rest):
+        for pr, rs in _pairings(rest[:i] + rest[i + 1:]):
+            yield [(first, o)] + pr, rs
+
+
+def _dfact(n):
+    return 1 if n <= 0 else n * _dfact(n - 2)
+
+
+def dtensor(r, p):
+    """p-th derivative tensor of 1/|r| at r (3,), from the closed form
+    d^p (1/r) = sum_k (-1)^(p-k) (2p-2k-1)!! r^-(2p-2k+1) sum over the ways to
+    pair 2k of the p indices (Kronecker deltas) times x for the others."""
+    R = np.sqrt(r @ r)
+    out = np.zeros((3,) * p)
+    pl = list(_pairings(list(range(p))))
+    for ii in np.ndindex(*((3,) * p)):
+        s = 0.0
+        for prs, rest in pl:
+            if any(ii[a] != ii[b] for a, b in prs):
+                continue
+            k = len(prs)
+            term = (-1) ** (p - k) * _dfact(2 * p - 2 * k - 1) * R ** (-(2 * p - 2 * k + 1))
+            for q in rest:
+                term *= r[ii[q]]
+            s += term
+        out[ii] = s
+    return out
+
+
+def m2l(R, M0, M1, M2):
+    """Local expansion (u, J, H) at offset R from a cell centre of the cell's
+    quadrupole expansion; moments of C-scaled strengths a' = -a/4pi, so that the
+    vector potential is Psi_m = -(M0_m phi - M1_ma d_a phi + 1/2 M2_mab d_ab phi),
+    phi = 1/|r|.  M1 (3,3) [m][a], M2 (3,3,3) [m][a][b]."""
+    D = [None] + [dtensor(np.asarray(R, np.float64), p) for p in range(1, 6)]
+    P1 = -(np.einsum("m,j->mj", M0, D[1]) - np.einsum("ma,aj->mj", M1, D[2])
+           + 0.5 * np.einsum("mab,abj->mj", M2, D[3]))
+    P2 = -(np.einsum("m,jn->mjn", M0, D[2]) - np.einsum("ma,ajn->mjn", M1, D[3])
+           + 0.5 * np.einsum("mab,abjn->mjn", M2, D[4]))
+    P3 = -(np.einsum("m,jkn->mjkn", M0, D[3]) - np.einsum("ma,ajkn->mjkn", M1, D[4])
+           + 0.5 * np.einsum("mab,abjkn->mjkn", M2, D[5]))
+    u = np.einsum("ijm,mj->i", TC.EPS, P1)
+    J = np.einsum("ijm,mjn->in", TC.EPS, P2)
+    H = np.einsum("ijm,mjkn->ikn", TC.EPS, P3)
+    return u, J, H
+
+
+def m2l_from_features(f):
+    """Normalised (u d^2/m, J d^3/m, H d^4/m) of the quadrupole expansion from
+    one pair's features (unit distance along R/d)."""
+    f = np.asarray(f, np.float64)
+    hs = f[3]
+    M1 = f[8:17].reshape(3, 3) * hs
+    M2 = np.zeros((3, 3, 3))
+    for m in range(3):
+        for q, (j, k) in enumerate(UNIQUE):
+            M2[m, j, k] = M2[m, k, j] = f[17 + 6 * m + q] * hs * hs
+    return pack_expansion(*m2l(f[0:3], f[5:8], M1, M2))
 
 
 def pack_expansion(u, J, H):

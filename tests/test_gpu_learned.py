@@ -113,7 +113,7 @@ def test_sampled_pairs_match_exact_local_expansions(cuda):
     n, leaf = 6000, 16
     pos, alpha, sigma = _slab(n, 31)
     ts = TreeSweeper(theta=0.5, leaf_target=leaf)
-    ts.set_learned(None, 0.4)
+    ts.set_far_field("m2l", theta_local=0.4)
     d = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")  # noqa: E731
     out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
     stats = ts.sweep(_capi.PAIR_VELOCITY, "winckelmans", d(pos), d(alpha), d(sigma), n, out,
@@ -122,23 +122,25 @@ def test_sampled_pairs_match_exact_local_expansions(cuda):
     pairs = OL.learned_pairs(tree, 0.4)
     assert int(stats[4]) == len(pairs) > 0
     max_pairs = 97
-    Xg, Tg = ts.sample_pairs(max_pairs)
+    Xg, Tg, Ag = ts.sample_pairs(max_pairs)
     stride = len(pairs) // max_pairs if len(pairs) > max_pairs else 1
     k = min(len(pairs) // stride, max_pairs)
     assert Xg.shape[0] == k
     Xo, To = OL.pair_samples(tree, pos, alpha, [pairs[i * stride] for i in range(k)])
     Xg = Xg.float().cpu().numpy()
     Tg = Tg.cpu().numpy()
+    Ag = Ag.cpu().numpy()
     # features: the device's BF16 rounding of FP32 values, one BF16 step at most
     assert np.all(np.abs(Xg - Xo) <= 2.0 ** -7 * np.abs(Xo) + 1e-6)
     # targets: FP64 sums of FP32 particle offsets
     rel = np.abs(Tg - To).max(axis=1) / np.abs(To).max(axis=1)
     assert rel.max() < 1e-4, rel.max()
-    # the analytic path still evaluates the learned pairs (no weights set)
-    ts.set_learned(None, 0.0)
-    out2 = torch.empty_like(out)
-    ts.sweep(_capi.PAIR_VELOCITY, "winckelmans", d(pos), d(alpha), d(sigma), n, out2)
-    assert torch.equal(out, out2)
+    # analytic multipole-to-local translation: FP32 device vs FP64 closed form
+    Ao = np.stack([OL.m2l_from_features(x) for x in Xo])
+    rel = np.abs(Ag - Ao).max(axis=1) / np.abs(Ao).max(axis=1)
+    assert rel.max() < 1e-4, rel.max()
+    # and it approximates the exact expansion to the quadrupole's truncation
+    assert np.median(np.linalg.norm(Ao - To, axis=1) / np.linalg.norm(To, axis=1)) < 0.05
     assert _capi.status_read_and_clear() == 0
 
 
@@ -149,12 +151,19 @@ def test_training_reduces_loss(cuda):
     pos, alpha, sigma = _slab(n, 41)
     d = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")  # noqa: E731
     ts = TreeSweeper(theta=0.5, leaf_target=32)
-    X, T = L.harvest(ts, d(pos), d(alpha), d(sigma), n, 40000)
+    X, T, A = L.harvest(ts, d(pos), d(alpha), d(sigma), n, 40000)
     assert X.shape[0] > 10000
+    # a network fitting the exact expansion itself learns fast from scratch
     m = L.FarFieldMLP(seed=3)
-    e0 = float(m.errors(X, T).median())
+    Z = torch.zeros_like(A)
+    e0 = float(m.errors(X, T, Z).median())
     hist = m.fit(X, T, steps=400, batch=4096, lr=2e-3, log_every=100)
-    e1 = float(m.errors(X, T).median())
+    e1 = float(m.errors(X, T, Z).median())
     assert hist[-1][1] < 0.2 * hist[0][1], hist
     assert e1 < 0.5 * e0, (e0, e1)
+    # the residual network starts at the analytic translation's accuracy
+    r = L.FarFieldMLP(seed=4)
+    ea = float(L.analytic_errors(T, A).median())
+    er = float(r.errors(X, T, A).median())
+    assert abs(er - ea) < 0.05 * ea, (er, ea)
     assert _lib().status_read_and_clear() == 0

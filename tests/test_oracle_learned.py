@@ -100,3 +100,55 @@ def test_pair_samples_consistent_with_tree():
     np.testing.assert_allclose(m, 1.0, rtol=1e-12)
     assert np.all(X[:, OL.NFEAT:] == 0.0) and np.all(T[:, OL.NOUT:] == 0.0)
     assert np.all(np.isfinite(T)) and np.abs(T).max() < 1e3
+
+
+def test_dtensor_closed_form_matches_explicit_tensors():
+    r = np.array([0.7, -1.1, 0.4])
+    D1, D2, D3, D4 = TC.phi_derivs(r)
+    for p, D in ((1, D1), (2, D2), (3, D3), (4, D4)):
+        np.testing.assert_allclose(OL.dtensor(r, p), D, rtol=1e-12, atol=1e-14)
+    # the fifth derivative by central differences of the fourth
+    D5 = OL.dtensor(r, 5)
+    for k in range(3):
+        e = np.zeros(3)
+        e[k] = 1e-5
+        fd = (OL.dtensor(r + e, 4) - OL.dtensor(r - e, 4)) / 2e-5
+        np.testing.assert_allclose(D5[..., k], fd, rtol=1e-6, atol=1e-6 * np.abs(D5).max())
+
+
+def test_m2l_converges_to_exact_local_expansion():
+    rng = np.random.default_rng(7)
+    c = np.array([0.2, 0.1, -0.3])
+    pos = c + rng.uniform(-0.05, 0.05, (25, 3))
+    alpha = rng.standard_normal((25, 3))
+    errs = []
+    for dist in (1.0, 2.0, 4.0):
+        x0 = c + dist * np.array([0.6, -0.48, 0.64])
+        exact = OL.pack_expansion(*OL.local_expansion(x0, pos, alpha))
+        a = alpha * OL.KC
+        d = pos - c
+        M1 = np.einsum("pm,pj->mj", a, d)
+        M2 = np.einsum("pm,pj,pk->mjk", a, d, d)
+        approx = OL.pack_expansion(*OL.m2l(x0 - c, a.sum(0), M1, M2))
+        errs.append(np.abs(approx - exact).max() / np.abs(exact).max())
+    # octupole truncation: error ~ (r_S / d)^3, so x8 less per doubling
+    assert errs[0] < 3e-3 and errs[1] < errs[0] / 5 and errs[2] < errs[1] / 5, errs
+
+
+def test_m2l_from_features_matches_moments():
+    rng = np.random.default_rng(8)
+    pos = rng.uniform(-0.5, 0.5, (30, 3)) + np.array([0.0, 0.0, 0.0])
+    alpha = rng.standard_normal((30, 3))
+    cS, hS, cT, hT = np.zeros(3), 1.0, np.array([3.0, -2.0, 1.5]), 0.5
+    M0, M1, M2 = OL.cell_moments(cS, pos, alpha)
+    f, (s2, s3, s4) = OL.features(cT, hT, cS, hS, M0, M1, M2)
+    got = OL.m2l_from_features(f)
+    M1m = M1.reshape(3, 3)
+    M2m = np.zeros((3, 3, 3))
+    for m in range(3):
+        for q, (j, k) in enumerate(OL.UNIQUE):
+            M2m[m, j, k] = M2m[m, k, j] = M2[6 * m + q]
+    ref = OL.pack_expansion(*OL.m2l(cT - cS, M0, M1m, M2m))
+    np.testing.assert_allclose(got[0:3] * s2, ref[0:3], rtol=1e-10, atol=1e-14)
+    np.testing.assert_allclose(got[3:12] * s3, ref[3:12], rtol=1e-10, atol=1e-14)
+    np.testing.assert_allclose(got[12:30] * s4, ref[12:30], rtol=1e-10, atol=1e-14)
