@@ -54,6 +54,7 @@ SIGNATURES = {
     "fvx_tree_destroy": (None, [P]),
     "fvx_tree_sweep": (I32, [P, I32, I32, P, P, P, P, I64, D, I32, P, P, P, P]),
     "fvx_tree_last_eval_ms": (I32, [P, P]),
+    "fvx_flutter_sweep": (I32, [P, P, I32, I32, I32, P]),
     "fvx_tree_set_far_field": (I32, [P, I32, P, P, D]),
     "fvx_tree_last_local_ms": (I32, [P, P]),
     "fvx_tree_sample_pairs": (I32, [P, I32, P, P, P, P, P]),

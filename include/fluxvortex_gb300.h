@@ -288,6 +288,59 @@ int fvx_uvlm_convert(int R, int n_keep, int ns, const double* W, const double* g
                      int sigma_rule, double sigma_vdt, int64_t capacity, int64_t* count,
                      double* pos, double* alpha, double* sigma, double* age, void* stream);
 
+/* ---- batched aeroelastic flutter sweep ------------------------------------------
+ * Replaces the reference's per-airspeed AeroelasticSolver runs
+ * (src/fluxvortex/aeroelastic_solver.py:68-221 with beam_fe.py:231-351, driven
+ * by tests/benchmark_goland.py:100-248) by one persistent launch: CTA e runs
+ * environment e (airspeed u_inf[e]) from its stored step to
+ * min(step_end, n_steps[e]) and stores its state back, so a sweep can be
+ * advanced in one launch or in chunks (a CUDA graph may capture them).  The
+ * coupled model per step: beam-deformed ring lattice, AIC, wake rings and
+ * particles at collocation points and bound legs (particles in FP64, or FP32
+ * with compensated sums for precision FVX_PREC_F32C), FP64 LU solve,
+ * Kutta-Joukowski loads, station lift/torque about the elastic axis
+ * distributed to the nodes, Newmark average-acceleration beam step with the
+ * precomputed inverse effective stiffness, tip history, wake convection,
+ * shedding and conversion of the ring row past n_keep into particles
+ * (FIFO store of max_particles per environment).  threads: a multiple of
+ * 2 x nc x ns and of 32, at most 512.  Limits: nc x ns <= 64, ns <= 16,
+ * n_keep <= 15, 3 x nnodes <= 48.  A zero pivot sets status bit 2.
+ * Layouts (env-major, FP64 unless noted): base_verts[(nc+1)(ns+1)][3];
+ * vert_node/vert_xi: the span interpolation of each vertex; station_node/
+ * station_xi: of each spanwise column's load station; kinv, mr, cr:
+ * [nf][nf] (nf = 3 nnodes - 3, root clamped); u_inf[E][3]; n_steps[E] (int).
+ * State: d, v, a [E][3 nnodes]; W[E][n_keep+2][ns+1][3], wgam[E][n_keep+1][ns],
+ * wage[E][n_keep+1], nrows[E] (int); ppos, palp [E][max_particles][3],
+ * psig[E][max_particles], phead, pcount [E] (int); gprev[E][nc ns],
+ * has_prev[E] (int); hist_w, hist_th [E][max_steps]; step[E] (int). */
+typedef struct FlutterParams {
+  int n_env, nc, ns, nnodes, n_keep, max_particles, max_steps, pad0;
+  double x_ea, rc0, nu, rho, dt, beta, gamma, pad1;
+  const double* base_verts;
+  const int* vert_node;
+  const double* vert_xi;
+  const int* station_node;
+  const double* station_xi;
+  const double* kinv;
+  const double* mr;
+  const double* cr;
+  const double* u_inf;
+  const int* n_steps;
+} FlutterParams;
+typedef struct FlutterState {
+  double *d, *v, *a;
+  double *W, *wgam, *wage;
+  int* nrows;
+  double *ppos, *palp, *psig;
+  int *phead, *pcount;
+  double* gprev;
+  int* has_prev;
+  double *hist_w, *hist_th;
+  int* step;
+} FlutterState;
+int fvx_flutter_sweep(const FlutterParams* params, const FlutterState* state, int step_end,
+                      int precision, int threads, void* stream);
+
 /* ---- learned far-field operator: BF16 tensor-core MLP (tcgen05) ---------------
  * No reference counterpart: the reference's notes plan a learned far field in
  * a treecode (docs/phase0A_findings.md:33-35); the operator is new.

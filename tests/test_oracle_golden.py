@@ -139,3 +139,19 @@ def test_beam_frequencies(golden):
     z = golden("beam_goland.npz")
     f = z["freqs"]
     assert abs(f[0] - 7.695) < 5e-3 and abs(f[1] - 21.14) < 5e-3
+
+
+def test_beam_oracle_matches_reference_model(golden):
+    """The restated beam (matrices, Newmark history) against the reference's BeamFE."""
+    from oracle.beam import Beam
+    z = golden("beam_goland.npz")
+    b = Beam(length=6.096, n_elements=8, EI=9.773e6, GJ=0.988e6, m_per_length=35.72, Ip=4.98,
+             x_ea_cg=0.183)
+    np.testing.assert_allclose(b.K, z["K"], rtol=1e-14, atol=1e-14 * np.abs(z["K"]).max())
+    np.testing.assert_allclose(b.M, z["M"], rtol=1e-14, atol=1e-14 * np.abs(z["M"]).max())
+    np.testing.assert_allclose(b.frequencies(), z["freqs"], rtol=1e-10)
+    for k in range(z["history"].shape[0]):
+        b.step(z["force"], float(z["dt"]))
+        got = np.concatenate([b.d, b.v, b.a])
+        ref = z["history"][k]
+        assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
