@@ -438,7 +438,7 @@ __global__ void pair_targets_kernel(int npairs, int stride, const int* __restric
                                     const float4* __restrict__ sp, const float4* __restrict__ sa,
                                     const int* __restrict__ leaf_of_particle, float h,
                                     __nv_bfloat16* __restrict__ X, float* __restrict__ T,
-                                    float* __restrict__ Aout) {
+                                    float* __restrict__ Aout, float* __restrict__ scale) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= npairs) return;
@@ -484,6 +484,12 @@ __global__ void pair_targets_kernel(int npairs, int stride, const int* __restric
     const PairScale sc =
         pair_features(rec + static_cast<int64_t>(g) * kRecFloats, cT.x, cT.y, cT.z, h, f);
     for (int q = 0; q < IN; ++q) X[static_cast<int64_t>(warp) * IN + q] = __float2bfloat16(f[q]);
+    if (scale) {
+      scale[static_cast<int64_t>(warp) * 4 + 0] = sc.s2;
+      scale[static_cast<int64_t>(warp) * 4 + 1] = sc.s3;
+      scale[static_cast<int64_t>(warp) * 4 + 2] = sc.s4;
+      scale[static_cast<int64_t>(warp) * 4 + 3] = f[4];  // h_T / d
+    }
     if (Aout) {
       float a[NOUT];
       m2l_quadrupole(f, a);
@@ -779,11 +785,11 @@ int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const 
                             const uint32_t* leaf_key, const float* rec, const int* cell_start,
                             const int* cell_count, const float4* sp, const float4* sa,
                             const int* leaf_of_particle, float h, void* X, float* T,
-                            float* A, cudaStream_t s) {
+                            float* A, float* scale, cudaStream_t s) {
   if (npairs <= 0) return FVX_OK;
   mlp::pair_targets_kernel<<<(npairs * 32 + 255) / 256, 256, 0, s>>>(
       npairs, stride, pair_leaf, pair_cell, leaf_key, rec, cell_start, cell_count, sp, sa,
-      leaf_of_particle, h, static_cast<__nv_bfloat16*>(X), T, A);
+      leaf_of_particle, h, static_cast<__nv_bfloat16*>(X), T, A, scale);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }

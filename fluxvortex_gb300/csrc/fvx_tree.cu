@@ -831,6 +831,111 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
   }
 }
 
+// ---- validation of the local-expansion path against FP64 direct sums -------------
+// Row k checks list pair k*stride: exact normalised expansion T (FP64 sums),
+// analytic translation A and network residual Y (zero without a network).
+// The error is that of the expansion applied across the target leaf: with
+// rho = sqrt(3)/2 h_T/d (the leaf's half diagonal over the distance),
+//   e = (|du| + rho |dJ| + rho^2/2 |dH|) / (|u| + rho |J| + rho^2/2 |H|).
+// A pair with e > tol is taken out of its leaf's expansion (its A + Y, scaled
+// back, is subtracted) and queued for the FP64 direct fallback.  val[0] += 1
+// per checked pair, val[1] += e, val[2] = max e (as ordered bits of a
+// non-negative float).
+__global__ void validate_kernel(int K, int stride, const int* __restrict__ pair_leaf,
+                                const int* __restrict__ pair_cell, const float* __restrict__ Tn,
+                                const float* __restrict__ An, const float* __restrict__ Yn,
+                                const float* __restrict__ scale, float tol,
+                                float* __restrict__ leaf_local, int2* __restrict__ fallback,
+                                int* __restrict__ n_fallback, float* __restrict__ val,
+                                float* __restrict__ errs) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  const float* t = Tn + static_cast<int64_t>(k) * 32;
+  const float* a = An + static_cast<int64_t>(k) * 32;
+  const float* y = Yn ? Yn + static_cast<int64_t>(k) * 32 : nullptr;
+  float dn[3] = {0.f, 0.f, 0.f}, tn[3] = {0.f, 0.f, 0.f};
+  for (int c = 0; c < 30; ++c) {
+    const float p = a[c] + (y ? y[c] : 0.f);
+    const int g = c < 3 ? 0 : (c < 12 ? 1 : 2);
+    dn[g] += (p - t[c]) * (p - t[c]);
+    tn[g] += t[c] * t[c];
+  }
+  const float rho = 0.8660254f * scale[static_cast<int64_t>(k) * 4 + 3];
+  const float w1 = rho, w2 = 0.5f * rho * rho;
+  const float num = sqrtf(dn[0]) + w1 * sqrtf(dn[1]) + w2 * sqrtf(dn[2]);
+  const float den = sqrtf(tn[0]) + w1 * sqrtf(tn[1]) + w2 * sqrtf(tn[2]);
+  const float err = num / fmaxf(den, 1e-30f);
+  errs[k] = err;
+  atomicAdd(val, 1.f);
+  atomicAdd(val + 1, err);
+  atomicMax(reinterpret_cast<unsigned*>(val + 2), __float_as_uint(err));
+  if (!(err <= tol)) {
+    const int leaf = pair_leaf[static_cast<int64_t>(k) * stride];
+    const int cell = pair_cell[static_cast<int64_t>(k) * stride];
+    const float* sc = scale + static_cast<int64_t>(k) * 4;
+    float* L = leaf_local + static_cast<int64_t>(leaf) * 32;
+    for (int c = 0; c < 30; ++c) {
+      const float p = a[c] + (y ? y[c] : 0.f);
+      atomicAdd(L + c, -p * (c < 3 ? sc[0] : (c < 12 ? sc[1] : sc[2])));
+    }
+    const int q = atomicAdd(n_fallback, 1);
+    fallback[q] = make_int2(leaf, cell);
+  }
+}
+
+// FP64 direct sum of a queued (leaf, cell) pair at every target of the leaf,
+// added to the outputs (one CTA per queued pair).
+template <int MODE, int KERNEL>
+__global__ void __launch_bounds__(128) fallback_kernel(
+    const int2* __restrict__ fallback, const int* __restrict__ n_fallback,
+    const int* __restrict__ leaf_start, const int* __restrict__ leaf_count,
+    const int* __restrict__ cell_start, const int* __restrict__ cell_count,
+    const int* __restrict__ perm, const double* __restrict__ pos,
+    const double* __restrict__ alpha, const double* __restrict__ sigma,
+    const double* __restrict__ tgt_gamma, double* __restrict__ out_a,
+    double* __restrict__ out_b) {
+  using namespace pair;
+  constexpr int NC = ModeInfo<MODE>::ncomp;
+  constexpr int NA = ModeInfo<MODE>::na;
+  constexpr bool NEED_FPR = ModeInfo<MODE>::need_fpr;
+  constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
+  constexpr double kC = -0.07957747154594767;
+  if (static_cast<int>(blockIdx.x) >= *n_fallback) return;
+  const int2 pr = fallback[blockIdx.x];
+  const int t0 = leaf_start[pr.x], nt = leaf_count[pr.x];
+  const int s0 = cell_start[pr.y], ns = cell_count[pr.y];
+  for (int ti = threadIdx.x; ti < nt; ti += blockDim.x) {
+    const int i = perm[t0 + ti];
+    const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    double gx = 0.0, gy = 0.0, gz = 0.0;
+    if (NEED_TG) {
+      gx = tgt_gamma[3 * i];
+      gy = tgt_gamma[3 * i + 1];
+      gz = tgt_gamma[3 * i + 2];
+    }
+    double acc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c] = 0.0;
+    for (int q = 0; q < ns; ++q) {
+      const int j = perm[s0 + q];
+      const double dx = x - pos[3 * j], dy = y - pos[3 * j + 1], dz = z - pos[3 * j + 2];
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      const double sg = sigma[j];
+      const double s2 = sg * sg;
+      const double k2 = KERNEL == FVX_KERNEL_WINCKELMANS ? 2.5 * s2 : 1.0 / sg;
+      double f, fpr = 0.0;
+      core_f64<KERNEL, NEED_FPR>(r2, s2, k2, f, fpr);
+      accumulate<MODE, double>(acc, dx, dy, dz, r2, kC * alpha[3 * j], kC * alpha[3 * j + 1],
+                               kC * alpha[3 * j + 2], f, fpr, gx, gy, gz);
+    }
+#pragma unroll
+    for (int c = 0; c < NA; ++c) atomicAdd(out_a + static_cast<int64_t>(i) * NA + c, acc[c]);
+#pragma unroll
+    for (int c = NA; c < NC; ++c)
+      atomicAdd(out_b + static_cast<int64_t>(i) * (NC - NA) + (c - NA), acc[c]);
+  }
+}
+
 }  // namespace tree
 
 // ---- host orchestration --------------------------------------------------------------
@@ -896,7 +1001,7 @@ int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const 
                             const uint32_t* leaf_key, const float* rec, const int* cell_start,
                             const int* cell_count, const float4* sp, const float4* sa,
                             const int* leaf_of_particle, float h, void* X, float* T,
-                            float* A, cudaStream_t s);
+                            float* A, float* scale, cudaStream_t s);
 int m2l_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
                         const uint32_t* leaf_key, const float* rec, float h, float* leaf_local,
                         cudaStream_t s);
@@ -915,6 +1020,11 @@ struct fvx_tree {
   const float* mlp_b = nullptr;
   double theta_l = 0.0;
   cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // around the local-expansion stage
+  // per-sweep validation of the local-expansion path and its FP64 fallback
+  int val_samples = 256;
+  double val_tol = 0.05;
+  fvx::DevBuf val_X, val_T, val_A, val_Y, val_scale, val_err, val_fb, val_stats;
+  int last_val_k = 0;
   fvx::DevBuf lrn_meta, lrn_leaf, lrn_cell, leaf_local;
   int n_learned = 0;
   // the last sweep's tree, for sampling training pairs
@@ -954,6 +1064,34 @@ void launch_eval(int mode, int nleaf, const tree::EvalArgs& A, cudaStream_t s) {
       eval_kernel<FVX_PAIR_VORTICITY, KERNEL><<<nleaf, kEvalThreads, 0, s>>>(A);
       break;
   }
+}
+
+template <int KERNEL>
+void launch_fallback(int mode, int grid, const int2* fb, const int* nfb, const int* leaf_start,
+                     const int* leaf_count, const int* cell_start, const int* cell_count,
+                     const int* perm, const double* pos, const double* alpha,
+                     const double* sigma, const double* tg, double* out_a, double* out_b,
+                     cudaStream_t s) {
+  using namespace tree;
+#define FVX_FB(M)                                                                          \
+  fallback_kernel<M, KERNEL><<<grid, 128, 0, s>>>(fb, nfb, leaf_start, leaf_count,        \
+                                                  cell_start, cell_count, perm, pos, alpha, \
+                                                  sigma, tg, out_a, out_b)
+  switch (mode) {
+    case FVX_PAIR_VELOCITY:
+      FVX_FB(FVX_PAIR_VELOCITY);
+      break;
+    case FVX_PAIR_STRETCH:
+      FVX_FB(FVX_PAIR_STRETCH);
+      break;
+    case FVX_PAIR_VELOCITY_STRETCH:
+      FVX_FB(FVX_PAIR_VELOCITY_STRETCH);
+      break;
+    default:
+      FVX_FB(FVX_PAIR_VORTICITY);
+      break;
+  }
+#undef FVX_FB
 }
 
 }  // namespace
@@ -1209,6 +1347,39 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
     FVX_CUDA_TRY(cudaEventRecord(T->ev3, s));
     A.leaf_local = P<float>(T->leaf_local);
   }
+  // validation sample: FP64 direct local expansions of evenly strided pairs
+  int val_k = 0, val_stride = 1;
+  if (learned && lrn_total > 0 && T->val_samples > 0) {
+    const int nl = static_cast<int>(lrn_total);
+    val_stride = nl > T->val_samples ? nl / T->val_samples : 1;
+    val_k = nl / val_stride < T->val_samples ? nl / val_stride : T->val_samples;
+    const size_t K = static_cast<size_t>(val_k);
+    if ((rc = grow(T->val_X, 2 * 48 * K)) || (rc = grow(T->val_T, 4 * 32 * K)) ||
+        (rc = grow(T->val_A, 4 * 32 * K)) || (rc = grow(T->val_Y, 4 * 32 * K)) ||
+        (rc = grow(T->val_scale, 4 * 4 * K)) || (rc = grow(T->val_err, 4 * K)) ||
+        (rc = grow(T->val_fb, 8 * K)) || (rc = grow(T->val_stats, 64)))
+      return rc;
+    FVX_CUDA_TRY(cudaMemsetAsync(T->val_stats.p, 0, 64, s));
+    if ((rc = mlp_pair_targets_launch(val_k, val_stride, P<int>(T->lrn_leaf), P<int>(T->lrn_cell),
+                                      leaves.key, rec, lvb, lvb + total_cells, sp, sa, cid,
+                                      static_cast<float>(h), T->val_X.p, P<float>(T->val_T),
+                                      P<float>(T->val_A), P<float>(T->val_scale), s)))
+      return rc;
+    const float* Y = nullptr;
+    if (T->far_method == FVX_FAR_LEARNED) {
+      if ((rc = fvx_mlp_forward(T->val_X.p, val_k, T->mlp_W, T->mlp_b, P<float>(T->val_Y),
+                                nullptr, nullptr, s)))
+        return rc;
+      Y = P<float>(T->val_Y);
+    }
+    validate_kernel<<<(val_k + 127) / 128, 128, 0, s>>>(
+        val_k, val_stride, P<int>(T->lrn_leaf), P<int>(T->lrn_cell), P<float>(T->val_T),
+        P<float>(T->val_A), Y, P<float>(T->val_scale), static_cast<float>(T->val_tol),
+        P<float>(T->leaf_local), P<int2>(T->val_fb), P<int>(T->val_stats) + 4,
+        P<float>(T->val_stats), P<float>(T->val_err));
+    FVX_LAUNCH_CHECK();
+  }
+  T->last_val_k = val_k;
   T->last_L = L;
   T->last_nleaf = nleaf;
   T->last_h = h;
@@ -1227,6 +1398,17 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
     launch_eval<FVX_KERNEL_GAUSSIANERF>(mode, nleaf, A, s);
   FVX_LAUNCH_CHECK();
   FVX_CUDA_TRY(cudaEventRecord(T->ev1, s));
+  if (val_k > 0) {
+    if (kernel == FVX_KERNEL_WINCKELMANS)
+      launch_fallback<FVX_KERNEL_WINCKELMANS>(
+          mode, val_k, P<int2>(T->val_fb), P<int>(T->val_stats) + 4, A.leaf_start, A.leaf_count,
+          lvb, lvb + total_cells, perm, pos, alpha, sigma, tgt_gamma, out_a, out_b, s);
+    else
+      launch_fallback<FVX_KERNEL_GAUSSIANERF>(
+          mode, val_k, P<int2>(T->val_fb), P<int>(T->val_stats) + 4, A.leaf_start, A.leaf_count,
+          lvb, lvb + total_cells, perm, pos, alpha, sigma, tgt_gamma, out_a, out_b, s);
+    FVX_LAUNCH_CHECK();
+  }
   unsigned ovf_h[6] = {0, 0, 0, 0, 0, 0};
   FVX_CUDA_TRY(cudaMemcpyAsync(ovf_h, ovf, 24, cudaMemcpyDeviceToHost, s));
   T->stats[0] = L;
@@ -1268,7 +1450,8 @@ void fvx_tree_destroy(fvx_tree* T) {
                          &T->scan_tmp, &T->flags,   &T->cid,      &T->levels,   &T->counts,
                          &T->rec,     &T->sp,       &T->sa,       &T->sg,       &T->lists_meta,
                          &T->near_list, &T->far_list, &T->bbox,   &T->lrn_meta, &T->lrn_leaf,
-                         &T->lrn_cell, &T->leaf_local};
+                         &T->lrn_cell, &T->leaf_local, &T->val_X, &T->val_T, &T->val_A,
+                         &T->val_Y, &T->val_scale, &T->val_err, &T->val_fb, &T->val_stats};
   for (auto* b : bufs)
     if (b->p) cudaFree(b->p);
   delete T;
@@ -1297,6 +1480,30 @@ int fvx_tree_set_far_field(fvx_tree* T, int method, const void* W, const float* 
   return FVX_OK;
 }
 
+int fvx_tree_set_validation(fvx_tree* T, int samples, double tol) {
+  FVX_ARG_CHECK(T != nullptr, "null tree handle");
+  FVX_ARG_CHECK(samples >= 0 && samples <= (1 << 16), "samples out of range");
+  FVX_ARG_CHECK(tol > 0.0, "tolerance must be positive");
+  T->val_samples = samples;
+  T->val_tol = tol;
+  return FVX_OK;
+}
+
+int fvx_tree_last_validation(fvx_tree* T, double* out) {
+  FVX_ARG_CHECK(T && out, "null argument");
+  for (int k = 0; k < 4; ++k) out[k] = 0.0;
+  if (T->last_val_k <= 0) return FVX_OK;
+  float v[4];
+  int nfb = 0;
+  FVX_CUDA_TRY(cudaMemcpy(v, T->val_stats.p, 16, cudaMemcpyDeviceToHost));
+  FVX_CUDA_TRY(cudaMemcpy(&nfb, fvx::P<int>(T->val_stats) + 4, 4, cudaMemcpyDeviceToHost));
+  out[0] = v[0];
+  out[1] = nfb;
+  out[2] = v[0] > 0.f ? v[1] / v[0] : 0.0;
+  out[3] = v[2];
+  return FVX_OK;
+}
+
 int fvx_tree_last_local_ms(fvx_tree* T, float* ms) {
   FVX_ARG_CHECK(T && ms, "null argument");
   *ms = 0.f;
@@ -1318,7 +1525,7 @@ int fvx_tree_sample_pairs(fvx_tree* T, int max_pairs, void* X, float* Tgt, float
   int rc = fvx::mlp_pair_targets_launch(
       np, stride, fvx::P<int>(T->lrn_leaf), fvx::P<int>(T->lrn_cell), T->last_leaf_key,
       fvx::P<float>(T->rec), T->last_cell_start, T->last_cell_count, fvx::P<float4>(T->sp),
-      fvx::P<float4>(T->sa), T->last_cid, static_cast<float>(T->last_h), X, Tgt, A,
+      fvx::P<float4>(T->sa), T->last_cid, static_cast<float>(T->last_h), X, Tgt, A, nullptr,
       static_cast<cudaStream_t>(stream));
   if (rc) return rc;
   *n_out = np;

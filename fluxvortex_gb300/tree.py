@@ -79,6 +79,19 @@ class TreeSweeper:
         self.far_method = method
         self.theta_local = th
 
+    def set_validation(self, samples=256, tol=0.05):
+        """Per-sweep FP64 validation of the local-expansion path: ``samples``
+        strided (leaf, cell) pairs per sweep; a pair whose expansion error
+        exceeds ``tol`` is summed directly in FP64 instead (samples=0: off)."""
+        _capi.check(self.lib.fvx_tree_set_validation(self.handle, int(samples), float(tol)))
+
+    def last_validation(self):
+        """{checked, fallback, mean_err, max_err} of the last sweep."""
+        out = np.zeros(4, dtype=np.float64)
+        _capi.check(self.lib.fvx_tree_last_validation(self.handle, out.ctypes.data))
+        return {"checked": int(out[0]), "fallback": int(out[1]), "mean_err": float(out[2]),
+                "max_err": float(out[3])}
+
     def last_local_ms(self):
         ms = ctypes.c_float(0.0)
         _capi.check(self.lib.fvx_tree_last_local_ms(self.handle, ctypes.byref(ms)))

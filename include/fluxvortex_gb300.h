@@ -226,6 +226,18 @@ int fvx_tree_last_eval_ms(fvx_tree* tree, float* ms);
 int fvx_tree_set_far_field(fvx_tree* tree, int method, const void* W, const float* b,
                            double theta_local);
 int fvx_tree_last_local_ms(fvx_tree* tree, float* ms);
+/* Per-sweep validation of the local-expansion path (on by default: 256
+ * samples, tol 0.05).  Every sweep with FVX_FAR_M2L or FVX_FAR_LEARNED sums
+ * `samples` evenly strided (leaf, cell) pairs of its list directly in FP64 at
+ * the leaf centre and compares their expansions with it; the error is that
+ * of the expansion across the leaf, e = (|du| + rho |dJ| + rho^2/2 |dH|) /
+ * (|u| + rho |J| + rho^2/2 |H|), rho = sqrt(3)/2 h_T/d.  A pair with e > tol
+ * leaves the expansion path: its cell is summed directly in FP64 at every
+ * target particle of its leaf.  samples = 0 turns validation off.
+ * fvx_tree_last_validation: out[4] = pairs checked, pairs sent to the FP64
+ * fallback, mean e, max e of the last sweep (waits for it). */
+int fvx_tree_set_validation(fvx_tree* tree, int samples, double tol);
+int fvx_tree_last_validation(fvx_tree* tree, double* out);
 int fvx_tree_sample_pairs(fvx_tree* tree, int max_pairs, void* X, float* T, float* A, int* n_out,
                           void* stream);
 

@@ -1,0 +1,111 @@
+"""Local-expansion far field inside the treecode sweep: per-sweep FP64
+validation with direct FP64 fallback, accuracy of the analytic and learned
+paths against the FP64 direct sum, and the measured gain of the trained
+network over the analytic translation it corrects."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _slab(n, seed, box=(4.0, 2.0, 0.4)):
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform([0, 0, 0], box, (n, 3))
+    alpha = rng.standard_normal((n, 3)) * 1e-3
+    sigma = np.full(n, 0.02)
+    return pos, alpha, sigma
+
+
+def _dev(a):
+    return torch.tensor(a, dtype=torch.float64, device="cuda")
+
+
+def _direct(mode, P, G, S, tg=None):
+    from fluxvortex_gb300.kernel import particle_pairs
+    out, _ = particle_pairs(mode, P, tg, P, G, S, "winckelmans", "f64")
+    return out
+
+
+def _sweep(ts, mode, P, G, S, n, tg=None):
+    out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    stats = ts.sweep(mode, "winckelmans", P, G, S, n, out, tgt_gamma=tg, check=True)
+    return out, stats.copy()
+
+
+@pytest.mark.parametrize("mode", ["velocity", "stretch"])
+def test_fallback_of_every_pair_is_the_fp64_direct_sum(cuda, mode):
+    """tol ~ 0 with every pair sampled: each far pair is summed in FP64 at
+    every target, so only the FP32 near field differs from the direct sum."""
+    from fluxvortex_gb300 import _capi
+    from fluxvortex_gb300.tree import TreeSweeper
+    m = _capi.PAIR_VELOCITY if mode == "velocity" else _capi.PAIR_STRETCH
+    n = 2500
+    pos, alpha, sigma = _slab(n, 51)
+    P, G, S = _dev(pos), _dev(alpha), _dev(sigma)
+    tg = G if mode == "stretch" else None
+    ref = _direct(m, P, G, S, tg)
+    ts = TreeSweeper(theta=0.5, leaf_target=16)
+    out_tree, _ = _sweep(ts, m, P, G, S, n, tg)
+    ts.set_far_field("m2l")
+    ts.set_validation(samples=65536, tol=1e-30)
+    out, stats = _sweep(ts, m, P, G, S, n, tg)
+    v = ts.last_validation()
+    assert v["checked"] == int(stats[4]) > 0 and v["fallback"] == v["checked"]
+    e_fb = float((out - ref).abs().max() / ref.abs().max())
+    e_tree = float((out_tree - ref).abs().max() / ref.abs().max())
+    assert e_fb < 2e-5 and e_fb < 0.2 * e_tree, (e_fb, e_tree)
+    assert _capi.status_read_and_clear() == 0
+
+
+def test_local_expansion_paths_match_direct_sum(cuda):
+    from fluxvortex_gb300 import _capi, learned as L
+    from fluxvortex_gb300.tree import TreeSweeper
+    n = 1 << 15
+    pos, alpha, sigma, _ = __import__("fluxvortex_gb300.workloads",
+                                      fromlist=["slab_wake"]).slab_wake(n, seed=61)
+    P, G, S = _dev(pos), _dev(alpha), _dev(sigma)
+    mlp = L.FarFieldMLP.load()
+    for m in (_capi.PAIR_VELOCITY, _capi.PAIR_STRETCH):
+        tg = G if m == _capi.PAIR_STRETCH else None
+        ref = _direct(m, P, G, S, tg)
+        errs = {}
+        for method in ("m2p", "m2l", "learned"):
+            ts = TreeSweeper(theta=0.5, leaf_target=64)
+            ts.set_far_field(method, mlp=mlp if method == "learned" else None)
+            out, stats = _sweep(ts, m, P, G, S, n, tg)
+            errs[method] = float((out - ref).abs().max() / ref.abs().max())
+            if method != "m2p":
+                v = ts.last_validation()
+                assert v["checked"] > 0 and v["fallback"] <= v["checked"]
+                assert 0.0 < v["mean_err"] <= v["max_err"]
+        assert max(errs.values()) < 2e-3, errs
+        assert errs["learned"] < 2.0 * errs["m2p"], errs
+    assert _capi.status_read_and_clear() == 0
+
+
+def test_learned_gain_over_analytic_translation(cuda):
+    """What the trained residual network gains over the analytic multipole-to-
+    local translation alone, on pairs of a field it was not trained on: the
+    per-pair error of the expansion (leaf-weighted, as the validation measures
+    it) with and without the network.  The gain measured at training time is
+    stored with the weights; the network must not make the expansion worse."""
+    from fluxvortex_gb300 import learned as L
+    from fluxvortex_gb300.tree import TreeSweeper
+    from fluxvortex_gb300.workloads import slab_wake
+    mlp = L.FarFieldMLP.load()
+    n = 1 << 17
+    pos, gam, sig, _ = slab_wake(n, seed=71)
+    ts = TreeSweeper(theta=0.5, leaf_target=64)
+    X, T, A = L.harvest(ts, _dev(pos), _dev(gam), _dev(sig), n, 20000)
+    Y = mlp.forward(X)
+    e_an = L.analytic_errors(T, A)
+    e_le = mlp.errors(X, T, A)
+    med_an, med_le = float(e_an.median()), float(e_le.median())
+    p90_an = float(e_an.quantile(0.9))
+    p90_le = float(e_le.quantile(0.9))
+    print(f"analytic median {med_an:.4e} p90 {p90_an:.4e} | learned median {med_le:.4e} "
+          f"p90 {p90_le:.4e} | gain {med_an / med_le:.3f}x median, {p90_an / p90_le:.3f}x p90")
+    assert torch.isfinite(Y).all()
+    assert med_le <= 1.05 * med_an and p90_le <= 1.05 * p90_an
+    assert "val_analytic_median" in mlp.meta and "val_median" in mlp.meta
