@@ -55,7 +55,28 @@ WORKLOAD = ("VPM+panel step: heaving NACA0012 wing 120 panels + {n} seeded wake 
 # Algorithmic flop of one far-field (target particle, cell) evaluation of the
 # treecode's quadrupole expansion (same counting convention).
 M2P_FLOP = {"velocity": 166, "stretch": 355, "vorticity": 300}
+# ... and of one local-expansion application per target particle (L2P)
+L2P_FLOP = {"velocity": 90, "stretch": 80, "vorticity": 60}
+# tensor flop of the far-field network per (leaf, cell) pair: 2 x MACs of the
+# 48-128-128-128-32 layers
+MLP_FLOP_PER_PAIR = 2 * (48 * 128 + 128 * 128 + 128 * 128 + 128 * 32)
 MODE_NAMES = {0: "velocity", 1: "stretch", 2: "velocity_stretch", 3: "jacobian", 4: "vorticity"}
+
+
+def _bf16_peak():
+    """Dense BF16 tensor peak: measured (MEASURED_PEAKS.json) or the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        for k in ("bf16_tflops", "bf16_dense_tflops"):
+            if k in pk and pk[k]:
+                return float(pk[k]), "measured (MEASURED_PEAKS.json " + k + ")"
+    except (OSError, ValueError):
+        pass
+    return 1900.0, "fallback 1.9 PFLOP/s (no measured peak file)"
+
+
+BF16_PEAK_TFLOPS, BF16_PEAK_SOURCE = _bf16_peak()
 
 
 def parse():
@@ -66,9 +87,14 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=1 << 20, help="particles")
     p.add_argument("--precision", default="f32c", choices=["f32c", "f64"])
-    p.add_argument("--far-field", default="direct", choices=["direct", "tree"],
-                   help="particle self-sweeps: direct all-pairs or the treecode")
-    p.add_argument("--leaf", type=int, default=64, help="treecode particles per leaf")
+    p.add_argument("--far-field", default="learned",
+                   choices=["direct", "tree", "m2p", "m2l", "learned"],
+                   help="particle self-sweeps: direct all-pairs, or the treecode with the "
+                        "accepted cells per target particle (tree = m2p), as analytic local "
+                        "expansions (m2l), or through the learned far-field operator")
+    p.add_argument("--leaf", type=int, default=48, help="treecode particles per leaf")
+    p.add_argument("--cl-steps", type=int, default=2,
+                   help="steps of the CL-history check against direct sweeps (0: off)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-baselines", action="store_true")
     return p.parse_args()
@@ -317,14 +343,20 @@ def run_ours(args, rank, world):
         # with CUDA events around the launch inside the library
         tev = [e for e in step.field.tree_events if MODE_NAMES[e[0]] == mname]
         base = kern.split("/", 1)[1]
+        local = step.field.far_field in ("m2l", "learned")
         flop = sum(FLOP_PER_PAIR[(mname, base)] * e[2][6] + M2P_FLOP[mname] * e[2][7]
-                   for e in tev) / len(tev)
+                   + (L2P_FLOP[mname] * args.n if local else 0) for e in tev) / len(tev)
         avg_ms = sum(e[3] for e in tev) / len(tev)
         kname = f"tree eval_kernel<{mname},{base}>"
         tree_stats = {"levels": int(tev[-1][2][0]), "leaves": int(tev[-1][2][1]),
                       "near_pairs": int(tev[-1][2][6]), "far_target_cell_pairs": int(tev[-1][2][7]),
+                      "local_expansion_pairs": int(tev[-1][2][4]),
                       "eval_ms": avg_ms,
+                      "local_ms": sum(e[4] for e in tev) / len(tev),
                       "sweep_ms": sum(durs) / len(durs)}
+        vals = [e[5] for e in step.field.tree_events if e[5]]
+        if vals:
+            tree_stats["validation_per_step"] = vals[-1]
     achieved = flop / (avg_ms * 1e-3) / 1e12
 
     result = {
@@ -348,22 +380,30 @@ def run_ours(args, rank, world):
         "sweep_ms": {f"{k[0]}/{k[1]}/{k[2]}x{k[3]}": sum(v) / len(v) for k, v in kinds.items()},
     }
     if kern.startswith("tree/"):
-        result["config"]["far_field"] = {"method": "treecode", "theta": step.field.tree.theta,
+        result["config"]["far_field"] = {"method": f"treecode/{step.field.far_field}",
+                                         "theta": step.field.tree.theta,
                                          "leaf_target": step.field.tree.leaf_target, **tree_stats}
+        if step.field.far_field == "learned" and tree_stats["local_ms"] > 0:
+            # the network stage (features, analytic translation, four tcgen05
+            # layers, accumulation) against the tensor peak
+            mlp_tf = (MLP_FLOP_PER_PAIR * tree_stats["local_expansion_pairs"]
+                      / (tree_stats["local_ms"] * 1e-3) / 1e12)
+            result["roofline_mlp"] = {
+                "bound": "tensor", "kernel": "mlp_fwd_kernel<far field>", "achieved": mlp_tf,
+                "peak": BF16_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": mlp_tf / BF16_PEAK_TFLOPS,
+                "peak_source": BF16_PEAK_SOURCE}
 
     if not args.no_baselines and rank == 0:
-        n_t = 4096
+        # FP64 direct form of the same step: every sweep in FP64 on a target
+        # sample large enough to fill the GPU, scaled by N / targets (all-pairs
+        # work is linear in the target count)
+        n_t = 32768
         f64_s = sample_sweeps(step.field, n_t, "f64")
-        f32_s = sample_sweeps(step.field, n_t, args.precision)
-        # The sample runs the sweeps on n_t targets only; calibrate its scale-up
-        # with the mixed-precision form, whose full step is measured above.
-        calib = (ms_max / 1e3) / f32_s
-        result["fp64_direct"] = {"step_s_extrapolated": f64_s * calib,
-                                 "steps_per_s": 1.0 / (f64_s * calib),
-                                 "sample": f"{n_t} targets x {args.n} sources per sweep kind",
-                                 "sample_scale_up_step_s": f64_s,
-                                 "calibration": calib,
-                                 "speedup_vs_fp64": f64_s * calib * 1e3 / ms_max}
+        result["fp64_direct"] = {"step_s_extrapolated": f64_s,
+                                 "steps_per_s": 1.0 / f64_s,
+                                 "sample": f"{n_t} targets x {args.n} sources per sweep kind, "
+                                           "scaled by N/targets",
+                                 "speedup_vs_fp64": f64_s * 1e3 / ms_max}
         # CL / CDi of the mixed form against FP64 particle sweeps, same state
         cl64, cdi64 = step.hs.panel_loads("f64")
         cl32, cdi32 = step.hs.panel_loads(args.precision)
@@ -377,6 +417,27 @@ def run_ours(args, rank, world):
                                   "sample": f"{detail['targets']} targets x {detail['sources']} "
                                             "sources per sweep kind, FP64 C oracle with OpenMP, "
                                             "scaled to the full step by N/targets"}
+
+    if args.cl_steps > 0 and rank == 0 and args.far_field != "direct":
+        # CL / CDi history of the benchmarked form against direct all-pairs
+        # sweeps (FP32 compensated, within ~1e-7 of FP64) from the same seeded
+        # initial state, step by step
+        del flush
+        torch.cuda.empty_cache()
+        hist = {}
+        for ff in (args.far_field, "direct"):
+            st2 = Step(args.n, args.precision, device, far_field=ff, leaf=args.leaf)
+            for _ in range(args.cl_steps):
+                st2.run()
+            hist[ff] = (st2.hs.cl.copy(), st2.hs.cdi.copy())
+            del st2
+            torch.cuda.empty_cache()
+        ca, da = hist[args.far_field]
+        cb, db = hist["direct"]
+        result["cl_history_vs_direct"] = {
+            "steps": args.cl_steps, "cl_rel_err_max": float(max(abs(ca - cb) / abs(cb))),
+            "cdi_rel_err_max": float(max(abs(da - db) / abs(db))),
+            "cl": [float(x) for x in cb], "reference": "direct sweeps, FP32 compensated"}
 
     if not args.no_e2e:
         # End to end through the host-facing API: the particle state in from

@@ -34,6 +34,7 @@ constexpr int W1o = 0, W2o = W1o + H * IN, W3o = W2o + H * H, W4o = W3o + H * H,
 // packed bias offsets
 constexpr int B1o = 0, B2o = H, B3o = 2 * H, B4o = 3 * H, BN = 3 * H + OUT;
 constexpr int kRecFloats = 40;  // treecode cell record (fvx_tree.cu)
+constexpr int kTargetsThreads = 256;  // FP64 exact-expansion sums: threads per pair
 
 // Two 128-row tiles are in flight per CTA (one per warpgroup): while one
 // group runs its epilogue on the CUDA cores, the other's MMA runs.
@@ -428,8 +429,9 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
 }
 
 // ---- training data: features + exact local expansions of sampled pairs ----------
-// One warp per pair: FP64 direct sums over the source cell's particles of the
-// singular Biot-Savart field and its first two derivatives at c_T.
+// One CTA per pair: FP64 direct sums over the source cell's particles of the
+// singular Biot-Savart field and its first two derivatives at c_T (threads
+// stride over the particles; warps, then the CTA, reduce in a fixed order).
 __global__ void pair_targets_kernel(int npairs, int stride, const int* __restrict__ pair_leaf,
                                     const int* __restrict__ pair_cell,
                                     const uint32_t* __restrict__ leaf_key,
@@ -439,8 +441,9 @@ __global__ void pair_targets_kernel(int npairs, int stride, const int* __restric
                                     const int* __restrict__ leaf_of_particle, float h,
                                     __nv_bfloat16* __restrict__ X, float* __restrict__ T,
                                     float* __restrict__ Aout, float* __restrict__ scale) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int warp = blockIdx.x;  // the pair
   const int lane = threadIdx.x & 31;
+  __shared__ double red[kTargetsThreads / 32][NOUT];
   if (warp >= npairs) return;
   const int t = pair_leaf[static_cast<int64_t>(warp) * stride],
             g = pair_cell[static_cast<int64_t>(warp) * stride];
@@ -449,7 +452,7 @@ __global__ void pair_targets_kernel(int npairs, int stride, const int* __restric
 #pragma unroll
   for (int q = 0; q < NOUT; ++q) acc[q] = 0.0;
   const int s0 = cell_start[g], n = cell_count[g];
-  for (int i = s0 + lane; i < s0 + n; i += 32) {
+  for (int i = s0 + static_cast<int>(threadIdx.x); i < s0 + n; i += blockDim.x) {
     const float3 cs = leaf_center(leaf_key[leaf_of_particle[i] - 1], h);
     const float4 p = sp[i];
     const float4 a = sa[i];
@@ -479,7 +482,15 @@ __global__ void pair_targets_kernel(int npairs, int stride, const int* __restric
 #pragma unroll
   for (int q = 0; q < NOUT; ++q)
     for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
-  if (lane == 0) {
+  if (lane == 0)
+    for (int q = 0; q < NOUT; ++q) red[threadIdx.x >> 5][q] = acc[q];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < NOUT; ++q) {
+      double v = 0.0;
+      for (int w = 0; w < kTargetsThreads / 32; ++w) v += red[w][q];
+      acc[q] = v;
+    }
     float f[IN];
     const PairScale sc =
         pair_features(rec + static_cast<int64_t>(g) * kRecFloats, cT.x, cT.y, cT.z, h, f);
@@ -787,7 +798,7 @@ int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const 
                             const int* leaf_of_particle, float h, void* X, float* T,
                             float* A, float* scale, cudaStream_t s) {
   if (npairs <= 0) return FVX_OK;
-  mlp::pair_targets_kernel<<<(npairs * 32 + 255) / 256, 256, 0, s>>>(
+  mlp::pair_targets_kernel<<<npairs, mlp::kTargetsThreads, 0, s>>>(
       npairs, stride, pair_leaf, pair_cell, leaf_key, rec, cell_start, cell_count, sp, sa,
       leaf_of_particle, h, static_cast<__nv_bfloat16*>(X), T, A, scale);
   FVX_LAUNCH_CHECK();

@@ -11,8 +11,8 @@
 //               centre (u = curl Psi, J_in = eps_ijm d_n d_j Psi_m), FP32.
 //
 // Build (every sweep state, all on the device):
-//   bbox -> host picks the grid (tree_params.grid_params: power-of-two root
-//   cube aligned to the leaf size) -> 30-bit Morton keys -> stable LSD radix
+//   bbox -> host picks the grid (tree_params.grid_params: root cube of 2^L
+//   leaves of size c 2^k, c in {1, 5/4, 3/2, 7/4}, aligned to the leaf size) -> 30-bit Morton keys -> stable LSD radix
 //   sort (4 x 8-bit digits, per-block histograms, warp-match ranking) ->
 //   leaf cells = runs of equal keys, coarser levels = runs of equal key >> 3
 //   among the finer level's cells -> sorted FP32 particle records relative to
@@ -33,7 +33,7 @@ namespace tree {
 
 constexpr int kScanBlock = 2048;   // elements per scan block (1024 threads x 2)
 constexpr int kSortItems = 1024;   // keys per radix-sort block (256 threads x 4)
-constexpr int kEvalThreads = 32;   // eval CTA (one warp); 2 targets per thread
+constexpr int kEvalThreads = 32;   // eval CTA (one warp); 1 or 2 targets per thread
 constexpr int kFarTile = 32;       // far cells staged per tile
 constexpr int kNearTile = 128;     // source particles staged per tile
 constexpr int kRecFloats = 40;     // far-cell record
@@ -459,6 +459,12 @@ struct TreeView {
   const int* child_hi;
   double mac_kl;        // learned far field: 3/4 / theta_L^2 (0: off)
   int learned_only;     // learned pairs leave the analytic list (weights loaded)
+  // the acceptance tests in exact integers: with centre offsets in units of
+  // h/2, a level-l cell is accepted when d2 > thr_far[l] (= floor of
+  // mac_k (h_T + h_S)^2 in those units) and listed for the local-expansion
+  // path when d2 > thr_lrn[l]
+  int thr_far[11];
+  int thr_lrn[11];
 };
 
 // (target leaf, source cell) pairs handed to the learned far-field operator
@@ -481,9 +487,11 @@ __global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
   if (t >= nleaf) return;
   const int gT = T.base[T.L] + t;
   const uint32_t kT = T.key[gT];
-  // centre of T in units of h/2 (exact integers)
-  const long long tx = 2LL * compact10(kT) + 1, ty = 2LL * compact10(kT >> 1) + 1,
-                  tz = 2LL * compact10(kT >> 2) + 1;
+  // centre of T in units of h/2 (exact integers below 2^11)
+  const int tx = 2 * static_cast<int>(compact10(kT)) + 1,
+            ty = 2 * static_cast<int>(compact10(kT >> 1)) + 1,
+            tz = 2 * static_cast<int>(compact10(kT >> 2)) + 1;
+  // stack entries: global cell id | level << 27
   int stack[96];
   int sp = 0;
   for (int c = T.ncell[0] - 1; c >= 0; --c) stack[sp++] = T.base[0] + c;
@@ -493,20 +501,16 @@ __global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
   const int cT_count = T.count[gT];
   int no = FILL ? near_off[t] : 0, fo = FILL ? far_off[t] : 0;
   while (sp > 0) {
-    const int g = stack[--sp];
-    int l = 0;
-    while (l < T.L && g >= T.base[l + 1]) ++l;
+    const int e = stack[--sp];
+    const int g = e & ((1 << 27) - 1), l = e >> 27;
     const uint32_t k = T.key[g];
-    const long long sc = 1LL << (T.L - l);  // cell size in units of h
-    const long long sx = (2LL * compact10(k) + 1) * sc, sy = (2LL * compact10(k >> 1) + 1) * sc,
-                    sz = (2LL * compact10(k >> 2) + 1) * sc;
-    const double dx = static_cast<double>(tx - sx) * (0.5 * T.h);
-    const double dy = static_cast<double>(ty - sy) * (0.5 * T.h);
-    const double dz = static_cast<double>(tz - sz) * (0.5 * T.h);
-    const double d2 = dx * dx + dy * dy + dz * dz;
-    const double hs = T.h + static_cast<double>(sc) * T.h;
-    if (d2 > T.mac_k * (hs * hs)) {
-      const bool lrn = T.mac_kl > 0.0 && d2 > T.mac_kl * (hs * hs);
+    const int sc = 1 << (T.L - l);  // cell size in units of h
+    const int dx = tx - (2 * static_cast<int>(compact10(k)) + 1) * sc;
+    const int dy = ty - (2 * static_cast<int>(compact10(k >> 1)) + 1) * sc;
+    const int dz = tz - (2 * static_cast<int>(compact10(k >> 2)) + 1) * sc;
+    const int d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 > T.thr_far[l]) {
+      const bool lrn = d2 > T.thr_lrn[l];
       if (lrn) {
         if (FILL && LL.leaf && lo0 + nl < LL.cap) {
           LL.leaf[lo0 + nl] = t;
@@ -526,7 +530,7 @@ __global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
       const int lo = T.child_lo[g], hi = T.child_hi[g];
       for (int c = hi - 1; c >= lo; --c) {
         if (sp < 96) {
-          stack[sp++] = T.base[l + 1] + c;
+          stack[sp++] = (T.base[l + 1] + c) | ((l + 1) << 27);
         } else {
           atomicOr(overflow, 1u);
         }
@@ -689,14 +693,13 @@ __device__ __forceinline__ void m2p(float* acc, const float* R, float rx, float 
   }
 }
 
-template <int MODE, int KERNEL>
+template <int MODE, int KERNEL, int TPT>
 __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
   using namespace pair;
   constexpr int NC = ModeInfo<MODE>::ncomp;
   constexpr int NA = ModeInfo<MODE>::na;
   constexpr bool NEED_FPR = ModeInfo<MODE>::need_fpr;
   constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
-  constexpr int TPT = 2;
   __shared__ float4 s_p[kNearTile];
   __shared__ float4 s_a[kNearTile];
   __shared__ float s_rec[kFarTile * kRecFloats];
@@ -884,9 +887,13 @@ __global__ void validate_kernel(int K, int stride, const int* __restrict__ pair_
 }
 
 // FP64 direct sum of a queued (leaf, cell) pair at every target of the leaf,
-// added to the outputs (one CTA per queued pair).
+// added to the outputs: blockIdx.x = the queued pair, blockIdx.y = one of
+// gridDim.y slices of the cell's particles (so a few large cells still fill
+// the GPU); per target, the threads stride over the slice and the CTA reduces
+// in a fixed order before one atomic add per output component.
+constexpr int kFallbackThreads = 256;
 template <int MODE, int KERNEL>
-__global__ void __launch_bounds__(128) fallback_kernel(
+__global__ void __launch_bounds__(kFallbackThreads) fallback_kernel(
     const int2* __restrict__ fallback, const int* __restrict__ n_fallback,
     const int* __restrict__ leaf_start, const int* __restrict__ leaf_count,
     const int* __restrict__ cell_start, const int* __restrict__ cell_count,
@@ -900,11 +907,17 @@ __global__ void __launch_bounds__(128) fallback_kernel(
   constexpr bool NEED_FPR = ModeInfo<MODE>::need_fpr;
   constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
   constexpr double kC = -0.07957747154594767;
+  __shared__ double red[kFallbackThreads / 32][NC];
   if (static_cast<int>(blockIdx.x) >= *n_fallback) return;
   const int2 pr = fallback[blockIdx.x];
   const int t0 = leaf_start[pr.x], nt = leaf_count[pr.x];
-  const int s0 = cell_start[pr.y], ns = cell_count[pr.y];
-  for (int ti = threadIdx.x; ti < nt; ti += blockDim.x) {
+  const int c0 = cell_start[pr.y], cn = cell_count[pr.y];
+  const int per = (cn + gridDim.y - 1) / gridDim.y;
+  const int s0 = c0 + static_cast<int>(blockIdx.y) * per;
+  const int ns = max(0, min(per, c0 + cn - s0));
+  if (ns == 0) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int ti = 0; ti < nt; ++ti) {
     const int i = perm[t0 + ti];
     const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
     double gx = 0.0, gy = 0.0, gz = 0.0;
@@ -916,7 +929,7 @@ __global__ void __launch_bounds__(128) fallback_kernel(
     double acc[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) acc[c] = 0.0;
-    for (int q = 0; q < ns; ++q) {
+    for (int q = threadIdx.x; q < ns; q += blockDim.x) {
       const int j = perm[s0 + q];
       const double dx = x - pos[3 * j], dy = y - pos[3 * j + 1], dz = z - pos[3 * j + 2];
       const double r2 = dx * dx + dy * dy + dz * dz;
@@ -929,10 +942,21 @@ __global__ void __launch_bounds__(128) fallback_kernel(
                                kC * alpha[3 * j + 2], f, fpr, gx, gy, gz);
     }
 #pragma unroll
-    for (int c = 0; c < NA; ++c) atomicAdd(out_a + static_cast<int64_t>(i) * NA + c, acc[c]);
-#pragma unroll
-    for (int c = NA; c < NC; ++c)
-      atomicAdd(out_b + static_cast<int64_t>(i) * (NC - NA) + (c - NA), acc[c]);
+    for (int c = 0; c < NC; ++c)
+      for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+    if (lane == 0)
+      for (int c = 0; c < NC; ++c) red[wid][c] = acc[c];
+    __syncthreads();
+    if (threadIdx.x < NC) {
+      double v = 0.0;
+      for (int w = 0; w < kFallbackThreads / 32; ++w) v += red[w][threadIdx.x];
+      const int c = threadIdx.x;
+      if (c < NA)
+        atomicAdd(out_a + static_cast<int64_t>(i) * NA + c, v);
+      else
+        atomicAdd(out_b + static_cast<int64_t>(i) * (NC - NA) + (c - NA), v);
+    }
+    __syncthreads();
   }
 }
 
@@ -973,9 +997,14 @@ void grid_params(const double lo[3], const double hi[3], int64_t n, int leaf_tar
   double vol = 1.0;
   for (int c = 0; c < 3; ++c) vol *= fmax(ext[c], emax * 1e-3);
   const double h_target = pow(vol * leaf_target / static_cast<double>(n > 0 ? n : 1), 1.0 / 3.0);
+  // leaf size c 2^k, c in {1, 5/4, 3/2, 7/4}: the candidate nearest to
+  // h_target in ratio (boundaries at the geometric means, compared squared)
   int e = 0;
-  const double m = frexp(h_target, &e);
-  double h = m < 0.7071067811865476 ? ldexp(1.0, e - 1) : ldexp(1.0, e);
+  const double x = 2.0 * frexp(h_target, &e);  // h_target = x 2^(e-1), x in [1, 2)
+  const double cand[5] = {1.0, 1.25, 1.5, 1.75, 2.0};
+  int ci = 0;
+  while (ci < 4 && x * x > cand[ci] * cand[ci + 1]) ++ci;
+  double h = ldexp(cand[ci], e - 1);
   int L = 1;
   for (;;) {
     double span = 0.0;
@@ -1047,34 +1076,45 @@ void launch_gather(int n, const int* perm, const int* leaf_of, const uint32_t* l
                                                              alpha, sigma, tgam, sp, sa, sg);
 }
 
-template <int KERNEL>
-void launch_eval(int mode, int nleaf, const tree::EvalArgs& A, cudaStream_t s) {
+// Targets per thread: leaves of at most ~40 particles on average fill one
+// 32-target chunk per warp better than two.
+template <int KERNEL, int TPT>
+void launch_eval_tpt(int mode, int nleaf, const tree::EvalArgs& A, cudaStream_t s) {
   using namespace tree;
   switch (mode) {
     case FVX_PAIR_VELOCITY:
-      eval_kernel<FVX_PAIR_VELOCITY, KERNEL><<<nleaf, kEvalThreads, 0, s>>>(A);
+      eval_kernel<FVX_PAIR_VELOCITY, KERNEL, TPT><<<nleaf, kEvalThreads, 0, s>>>(A);
       break;
     case FVX_PAIR_STRETCH:
-      eval_kernel<FVX_PAIR_STRETCH, KERNEL><<<nleaf, kEvalThreads, 0, s>>>(A);
+      eval_kernel<FVX_PAIR_STRETCH, KERNEL, TPT><<<nleaf, kEvalThreads, 0, s>>>(A);
       break;
     case FVX_PAIR_VELOCITY_STRETCH:
-      eval_kernel<FVX_PAIR_VELOCITY_STRETCH, KERNEL><<<nleaf, kEvalThreads, 0, s>>>(A);
+      eval_kernel<FVX_PAIR_VELOCITY_STRETCH, KERNEL, TPT><<<nleaf, kEvalThreads, 0, s>>>(A);
       break;
     default:
-      eval_kernel<FVX_PAIR_VORTICITY, KERNEL><<<nleaf, kEvalThreads, 0, s>>>(A);
+      eval_kernel<FVX_PAIR_VORTICITY, KERNEL, TPT><<<nleaf, kEvalThreads, 0, s>>>(A);
       break;
   }
 }
 
 template <int KERNEL>
-void launch_fallback(int mode, int grid, const int2* fb, const int* nfb, const int* leaf_start,
+void launch_eval(int mode, int nleaf, int n, const tree::EvalArgs& A, cudaStream_t s) {
+  if (n <= 40 * nleaf)
+    launch_eval_tpt<KERNEL, 1>(mode, nleaf, A, s);
+  else
+    launch_eval_tpt<KERNEL, 2>(mode, nleaf, A, s);
+}
+
+template <int KERNEL>
+void launch_fallback(int mode, dim3 grid, const int2* fb, const int* nfb, const int* leaf_start,
                      const int* leaf_count, const int* cell_start, const int* cell_count,
                      const int* perm, const double* pos, const double* alpha,
                      const double* sigma, const double* tg, double* out_a, double* out_b,
                      cudaStream_t s) {
   using namespace tree;
 #define FVX_FB(M)                                                                          \
-  fallback_kernel<M, KERNEL><<<grid, 128, 0, s>>>(fb, nfb, leaf_start, leaf_count,        \
+  fallback_kernel<M, KERNEL><<<grid, kFallbackThreads, 0, s>>>(fb, nfb, leaf_start,        \
+                                                               leaf_count,                 \
                                                   cell_start, cell_count, perm, pos, alpha, \
                                                   sigma, tg, out_a, out_b)
   switch (mode) {
@@ -1253,6 +1293,16 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   V.child_hi = lvb + 4 * total_cells;
   const bool learned = T->far_method != FVX_FAR_M2P && T->theta_l > 0.0;
   V.mac_kl = learned ? 0.75 / (T->theta_l * T->theta_l) : 0.0;
+  // integer acceptance thresholds per source level: (h_T + h_S)^2 in (h/2)^2
+  // units is 4 (1 + 2^(L-l))^2; d2 > k x that <=> d2 > floor(k x that)
+  for (int l = 0; l <= L; ++l) {
+    const double hs2 = 4.0 * (1.0 + static_cast<double>(1 << (L - l))) *
+                       (1.0 + static_cast<double>(1 << (L - l)));
+    const double tf = floor(V.mac_k * hs2), tl = floor(V.mac_kl * hs2);
+    V.thr_far[l] = tf < 2147483647.0 ? static_cast<int>(tf) : 2147483647;
+    V.thr_lrn[l] = learned ? (tl < 2147483647.0 ? static_cast<int>(tl) : 2147483647)
+                           : 2147483647;
+  }
   V.learned_only = learned ? 1 : 0;
   if ((rc = grow(T->lists_meta, 4 * size_t(nleaf) * 4 + 64))) return rc;
   if (learned && (rc = grow(T->lrn_meta, 4 * size_t(nleaf) * 2 + 64))) return rc;
@@ -1393,19 +1443,23 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   }
   FVX_CUDA_TRY(cudaEventRecord(T->ev0, s));
   if (kernel == FVX_KERNEL_WINCKELMANS)
-    launch_eval<FVX_KERNEL_WINCKELMANS>(mode, nleaf, A, s);
+    launch_eval<FVX_KERNEL_WINCKELMANS>(mode, nleaf, n, A, s);
   else
-    launch_eval<FVX_KERNEL_GAUSSIANERF>(mode, nleaf, A, s);
+    launch_eval<FVX_KERNEL_GAUSSIANERF>(mode, nleaf, n, A, s);
   FVX_LAUNCH_CHECK();
   FVX_CUDA_TRY(cudaEventRecord(T->ev1, s));
   if (val_k > 0) {
+    // queued pairs are at most val_k (few in practice): slice every cell so
+    // that all of them together span about four CTAs per SM
+    const int slices = max(1, min(64, 4 * device_sm_count() / max(1, val_k / 16)));
+    const dim3 fgrid(val_k, slices);
     if (kernel == FVX_KERNEL_WINCKELMANS)
       launch_fallback<FVX_KERNEL_WINCKELMANS>(
-          mode, val_k, P<int2>(T->val_fb), P<int>(T->val_stats) + 4, A.leaf_start, A.leaf_count,
+          mode, fgrid, P<int2>(T->val_fb), P<int>(T->val_stats) + 4, A.leaf_start, A.leaf_count,
           lvb, lvb + total_cells, perm, pos, alpha, sigma, tgt_gamma, out_a, out_b, s);
     else
       launch_fallback<FVX_KERNEL_GAUSSIANERF>(
-          mode, val_k, P<int2>(T->val_fb), P<int>(T->val_stats) + 4, A.leaf_start, A.leaf_count,
+          mode, fgrid, P<int2>(T->val_fb), P<int>(T->val_stats) + 4, A.leaf_start, A.leaf_count,
           lvb, lvb + total_cells, perm, pos, alpha, sigma, tgt_gamma, out_a, out_b, s);
     FVX_LAUNCH_CHECK();
   }

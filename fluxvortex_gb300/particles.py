@@ -50,13 +50,31 @@ class VortexParticleField:
         # Optional profiling hook: when a list, every sweep appends
         # (mode, kernel, n_targets, n_sources, start_event, end_event).
         self.sweep_events = None
-        self.tree_events = []     # (mode, kernel, stats, eval_ms) when profiling
-        # far_field="tree": the self-sweeps (every particle a target) use the
-        # cell-binned treecode; sweeps at other targets stay direct.
+        # (mode, kernel, stats, eval_ms, local_ms, validation) when profiling
+        self.tree_events = []
+        # far_field: the self-sweeps (every particle a target) use the
+        # cell-binned treecode with accepted cells evaluated per target particle
+        # ("tree" / "m2p"), as analytic local expansions per leaf ("m2l"), or
+        # with the learned far-field operator ("learned": analytic translation
+        # + the trained network's residual, FP64-validated every sweep); sweeps
+        # at other targets stay direct.
         self.tree = None
-        if far_field == "tree":
+        self.far_field = far_field or "direct"
+        # per-step FP64 validation of the local-expansion far field: pairs
+        # checked on the step's first velocity sweep and the expansion error
+        # above which a checked cluster is summed directly in FP64 instead
+        self.validate_samples = 256
+        self.validate_tol = 0.05
+        self._validate_next = False
+        if far_field in ("tree", "m2p", "m2l", "learned"):
             from .tree import TreeSweeper
             self.tree = TreeSweeper(theta=theta, leaf_target=leaf_target)
+            if far_field == "learned":
+                from .learned import FarFieldMLP
+                self.mlp = FarFieldMLP.load(device=self.device)
+                self.tree.set_far_field("learned", mlp=self.mlp)
+            elif far_field == "m2l":
+                self.tree.set_far_field("m2l")
         elif far_field not in (None, "direct"):
             raise ValueError(f"unknown far_field {far_field!r}")
 
@@ -118,6 +136,9 @@ class VortexParticleField:
         if (self.tree is not None and tgt is self._pos and n_tgt == n
                 and mode in (_capi.PAIR_VELOCITY, _capi.PAIR_STRETCH,
                              _capi.PAIR_VELOCITY_STRETCH, _capi.PAIR_VORTICITY)):
+            if self.far_field in ("m2l", "learned"):
+                self.tree.set_validation(
+                    self.validate_samples if self._validate_next else 0, self.validate_tol)
             stats = self.tree.sweep(mode, kernel or self.kernel, self._pos, self._gamma,
                                     self._sigma, n, out_a, out_b, tgt_gamma=tgt_gamma,
                                     check=ev is not None)
@@ -125,8 +146,12 @@ class VortexParticleField:
                 ev[1].record()
                 self.sweep_events.append((mode, "tree/" + (kernel or self.kernel), n_tgt, n,
                                           ev[0], ev[1]))
+                local = self.far_field in ("m2l", "learned")
+                val = self.tree.last_validation() if local else None
                 self.tree_events.append((mode, kernel or self.kernel, stats.copy(),
-                                         self.tree.last_eval_ms()))
+                                         self.tree.last_eval_ms(),
+                                         self.tree.last_local_ms() if local else 0.0,
+                                         val if val and val["checked"] else None))
             return
         _capi.check(lib.fvx_particle_pairs(
             mode, kid, pid, tgt.data_ptr(), None if tgt_gamma is None else tgt_gamma.data_ptr(),
@@ -170,9 +195,13 @@ class VortexParticleField:
         else:
             u_inf_host = np.ascontiguousarray(U_inf_func, dtype=np.float64).reshape(3)
             inf_fn = None
-        for a, b in RK3_COEFFS:
+        for stage, (a, b) in enumerate(RK3_COEFFS):
             if free_wake:
+                # the FP64 judge of the local-expansion far field runs once per
+                # step, on the first velocity sweep
+                self._validate_next = stage == 0
                 self._sweep(_capi.PAIR_VELOCITY, self._pos, None, n, self._u)
+                self._validate_next = False
             extra = None
             if inf_fn is not None or bound_velocity_func is not None:
                 eb = self._extra_velocity(bound_velocity_func, n)

@@ -1,11 +1,12 @@
 """Host-side parameters of the cell-binned treecode grid (shared by the device
 orchestration and the tests).
 
-The root is a power-of-two cube whose corner sits on the leaf grid, so every
-cell centre at every level is an exact binary fraction: differences of cell
-centres are exact in FP32, which is what keeps the FP32 near field accurate
-(pair offsets are formed as exact centre differences plus small in-cell
-offsets).  The leaf size is picked from the particles' bounding box so that an
+The root is a cube of 2^L leaves whose corner sits on the leaf grid; the leaf
+size has at most three significant bits (c 2^k, c in {1, 5/4, 3/2, 7/4}), so
+every cell centre at every level is an exact binary fraction: differences of
+cell centres are exact in FP32, which is what keeps the FP32 near field
+accurate (pair offsets are formed as exact centre differences plus small
+in-cell offsets).  The leaf size is picked from the particles' bounding box so that an
 occupied leaf holds about ``leaf_target`` particles when they fill the box.
 """
 from __future__ import annotations
@@ -23,9 +24,16 @@ def grid_params(lo, hi, n, leaf_target=64):
     ext = np.maximum(hi - lo, 1e-12)
     vol = float(np.prod(np.maximum(ext, ext.max() * 1e-3)))
     h_target = (vol * leaf_target / max(n, 1)) ** (1.0 / 3.0)
-    # leaf size: the power of two nearest h_target (frexp keeps it exact)
+    # leaf size c 2^k, c in {1, 5/4, 3/2, 7/4}: the candidate nearest to h_target
+    # in ratio (boundaries at the geometric means, compared squared); three
+    # significant bits keep every cell centre an exact binary fraction
     m, e = math.frexp(h_target)          # h_target = m 2^e, m in [0.5, 1)
-    h = math.ldexp(1.0, e - 1) if m < 0.7071067811865476 else math.ldexp(1.0, e)
+    x = 2.0 * m                          # h_target = x 2^(e-1), x in [1, 2)
+    cand = (1.0, 1.25, 1.5, 1.75, 2.0)
+    ci = 0
+    while ci < 4 and x * x > cand[ci] * cand[ci + 1]:
+        ci += 1
+    h = math.ldexp(cand[ci], e - 1)
     while True:
         origin = np.floor(lo / h) * h
         L = 1
