@@ -693,6 +693,89 @@ __device__ __forceinline__ void m2p(float* acc, const float* R, float rx, float 
   }
 }
 
+// ---- paired FP32 (f32x2) arithmetic: two targets per instruction -------------
+namespace x2 {
+__device__ __forceinline__ uint64_t pack(float a, float b) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void unpack(uint64_t v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t add(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t sub(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t mul(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t fma(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+}  // namespace x2
+
+// One source per row of the packed near tile, every value duplicated into
+// both halves of a 64-bit pair: {-x, -y}, {-z, s2}, {k2, ax}, {ay, az},
+// {10.5 s2, -}.
+struct NearX2 {
+  ulonglong2 q[5];
+};
+
+// Near pairs of one staged tile for the thread's two targets (Winckelmans
+// core, velocity or stretching) with paired FP32 instructions; same formulas
+// as core_f32 + accumulate.
+template <int MODE>
+__device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, int nt, uint64_t TX,
+                                             uint64_t TY, uint64_t TZ, uint64_t GX, uint64_t GY,
+                                             uint64_t GZ, uint64_t* acc) {
+  const uint64_t C3 = x2::pack(3.f, 3.f);
+  for (int k = 0; k < nt; ++k) {
+    const ulonglong2 q0 = tile[k].q[0], q1 = tile[k].q[1], q2 = tile[k].q[2],
+                     q3 = tile[k].q[3];
+    const uint64_t DX = x2::add(TX, q0.x), DY = x2::add(TY, q0.y), DZ = x2::add(TZ, q1.x);
+    uint64_t R2 = x2::mul(DX, DX);
+    R2 = x2::fma(DY, DY, R2);
+    R2 = x2::fma(DZ, DZ, R2);
+    float qa, qb;
+    x2::unpack(x2::add(R2, q1.y), qa, qb);
+    const uint64_t T = x2::pack(rsqrtf(qa), rsqrtf(qb));
+    const uint64_t T2 = x2::mul(T, T);
+    const uint64_t T5 = x2::mul(x2::mul(T2, T2), T);
+    const uint64_t F = x2::mul(x2::add(R2, q2.x), T5);
+    const uint64_t AX = q2.y, AY = q3.x, AZ = q3.y;
+    if (MODE == FVX_PAIR_VELOCITY) {
+      const uint64_t EX = x2::mul(F, DX), EY = x2::mul(F, DY), EZ = x2::mul(F, DZ);
+      acc[0] = x2::sub(x2::fma(EY, AZ, acc[0]), x2::mul(EZ, AY));
+      acc[1] = x2::sub(x2::fma(EZ, AX, acc[1]), x2::mul(EX, AZ));
+      acc[2] = x2::sub(x2::fma(EX, AY, acc[2]), x2::mul(EY, AX));
+    } else {
+      // S += (f G + fpr (d . G) d) x a, fpr = -(3 r2 + 10.5 s2) t^7
+      const ulonglong2 q4 = tile[k].q[4];
+      uint64_t DG = x2::mul(DX, GX);
+      DG = x2::fma(DY, GY, DG);
+      DG = x2::fma(DZ, GZ, DG);
+      const uint64_t W = x2::mul(x2::mul(x2::fma(R2, C3, q4.x), x2::mul(T5, T2)), DG);
+      const uint64_t VX = x2::sub(x2::mul(F, GX), x2::mul(W, DX));
+      const uint64_t VY = x2::sub(x2::mul(F, GY), x2::mul(W, DY));
+      const uint64_t VZ = x2::sub(x2::mul(F, GZ), x2::mul(W, DZ));
+      acc[0] = x2::sub(x2::fma(VY, AZ, acc[0]), x2::mul(VZ, AY));
+      acc[1] = x2::sub(x2::fma(VZ, AX, acc[1]), x2::mul(VX, AZ));
+      acc[2] = x2::sub(x2::fma(VX, AY, acc[2]), x2::mul(VY, AX));
+    }
+  }
+}
+
 template <int MODE, int KERNEL, int TPT>
 __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
   using namespace pair;
@@ -700,9 +783,18 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
   constexpr int NA = ModeInfo<MODE>::na;
   constexpr bool NEED_FPR = ModeInfo<MODE>::need_fpr;
   constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
-  __shared__ float4 s_p[kNearTile];
-  __shared__ float4 s_a[kNearTile];
-  __shared__ float s_rec[kFarTile * kRecFloats];
+  // paired path: Winckelmans velocity / stretching with two targets per thread
+  constexpr bool PACKED = TPT == 2 && KERNEL == FVX_KERNEL_WINCKELMANS &&
+                          (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_STRETCH);
+  // near tile (plain or paired layout) and far-cell records share the storage
+  constexpr int kNearBytes = PACKED ? kNearTile * static_cast<int>(sizeof(NearX2))
+                                    : kNearTile * 2 * static_cast<int>(sizeof(float4));
+  constexpr int kFarBytes = kFarTile * kRecFloats * 4;
+  __shared__ __align__(16) unsigned char s_raw[kNearBytes > kFarBytes ? kNearBytes : kFarBytes];
+  float4* s_p = reinterpret_cast<float4*>(s_raw);
+  float4* s_a = s_p + kNearTile;
+  NearX2* s_x2 = reinterpret_cast<NearX2*>(s_raw);
+  float* s_rec = reinterpret_cast<float*>(s_raw);
 
   const int t = blockIdx.x;
   const int tstart = A.leaf_start[t], tcount = A.leaf_count[t];
@@ -744,6 +836,37 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
         tx[j] = ox[j] + dcx;
         ty[j] = oy[j] + dcy;
         tz[j] = oz[j] + dcz;
+      }
+      if constexpr (PACKED) {
+        const uint64_t TX = x2::pack(tx[0], tx[TPT - 1]), TY = x2::pack(ty[0], ty[TPT - 1]),
+                       TZ = x2::pack(tz[0], tz[TPT - 1]);
+        const uint64_t GX = x2::pack(gx[0], gx[TPT - 1]), GY = x2::pack(gy[0], gy[TPT - 1]),
+                       GZ = x2::pack(gz[0], gz[TPT - 1]);
+        for (int k0 = 0; k0 < sn; k0 += kNearTile) {
+          const int nt = min(kNearTile, sn - k0);
+          __syncthreads();
+          for (int k = threadIdx.x; k < nt; k += kEvalThreads) {
+            const float4 pv = A.sp[ss + k0 + k], av = A.sa[ss + k0 + k];
+            NearX2 e;
+            e.q[0] = make_ulonglong2(x2::pack(-pv.x, -pv.x), x2::pack(-pv.y, -pv.y));
+            e.q[1] = make_ulonglong2(x2::pack(-pv.z, -pv.z), x2::pack(pv.w, pv.w));
+            e.q[2] = make_ulonglong2(x2::pack(av.w, av.w), x2::pack(av.x, av.x));
+            e.q[3] = make_ulonglong2(x2::pack(av.y, av.y), x2::pack(av.z, av.z));
+            e.q[4] = make_ulonglong2(x2::pack(10.5f * pv.w, 10.5f * pv.w), 0ull);
+            s_x2[k] = e;
+          }
+          __syncthreads();
+          uint64_t acc2[3] = {0ull, 0ull, 0ull};
+          near_tile_x2<MODE>(s_x2, nt, TX, TY, TZ, GX, GY, GZ, acc2);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            float a0, a1;
+            x2::unpack(acc2[c], a0, a1);
+            fold(hi[0][c], lo[0][c], a0);
+            fold(hi[TPT - 1][c], lo[TPT - 1][c], a1);
+          }
+        }
+        continue;
       }
       for (int k0 = 0; k0 < sn; k0 += kNearTile) {
         const int nt = min(kNearTile, sn - k0);
@@ -1099,7 +1222,12 @@ void launch_eval_tpt(int mode, int nleaf, const tree::EvalArgs& A, cudaStream_t 
 
 template <int KERNEL>
 void launch_eval(int mode, int nleaf, int n, const tree::EvalArgs& A, cudaStream_t s) {
-  if (n <= 40 * nleaf)
+  // Two targets per thread (paired f32x2 arithmetic for Winckelmans velocity
+  // and stretching) once leaves average more than one warp of targets; at
+  // fewer, one target per thread wastes fewer lanes.
+  const bool paired = KERNEL == FVX_KERNEL_WINCKELMANS &&
+                      (mode == FVX_PAIR_VELOCITY || mode == FVX_PAIR_STRETCH);
+  if (n <= (paired ? 32 : 40) * nleaf)
     launch_eval_tpt<KERNEL, 1>(mode, nleaf, A, s);
   else
     launch_eval_tpt<KERNEL, 2>(mode, nleaf, A, s);
