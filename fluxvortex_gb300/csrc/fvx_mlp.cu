@@ -27,7 +27,7 @@ namespace fvx {
 namespace mlp {
 
 constexpr int IN = 48, H = 128, OUT = 32, NFEAT = 35, NOUT = 30;
-constexpr int kThreads = 256;  // forward: two warpgroups
+constexpr int kThreads = 512;  // forward: four warpgroups
 // packed BF16 weight offsets (elements)
 constexpr int W1o = 0, W2o = W1o + H * IN, W3o = W2o + H * H, W4o = W3o + H * H,
               WN = W4o + OUT * H;
@@ -36,9 +36,10 @@ constexpr int B1o = 0, B2o = H, B3o = 2 * H, B4o = 3 * H, BN = 3 * H + OUT;
 constexpr int kRecFloats = 40;  // treecode cell record (fvx_tree.cu)
 constexpr int kTargetsThreads = 256;  // FP64 exact-expansion sums: threads per pair
 
-// Two 128-row tiles are in flight per CTA (one per warpgroup): while one
-// group runs its epilogue on the CUDA cores, the other's MMA runs.
-constexpr int kGroups = 2;
+// Four 128-row tiles are in flight per CTA (one per warpgroup, each with a
+// quarter of the tensor memory): while some groups run their epilogues on the
+// CUDA cores, the others' MMAs run.
+constexpr int kGroups = 4;
 
 struct FwdSmem {
   __nv_bfloat16 w1[H * IN];
@@ -46,7 +47,7 @@ struct FwdSmem {
   __nv_bfloat16 w3[H * H];
   __nv_bfloat16 w4[OUT * H];
   __nv_bfloat16 act[kGroups][128 * H];
-  float aux[kGroups][128][33];  // far field: analytic M2L (30) and the output scales (3)
+  float aux[kGroups][128][4];  // far field: the output scales m/d^2, m/d^3, m/d^4 of each row
   float bias[BN];
   uint64_t bar[kGroups];
   uint32_t tmem;
@@ -102,12 +103,20 @@ struct PairScale {
   float s2, s3, s4;  // m/d^2, m/d^3, m/d^4
 };
 
-__device__ __forceinline__ PairScale pair_features(const float* rec, float cTx, float cTy,
-                                                   float cTz, float hT, float* f) {
-  const float Rx = cTx - rec[0], Ry = cTy - rec[1], Rz = cTz - rec[2];
-  const float d2 = Rx * Rx + Ry * Ry + Rz * Rz;
-  const float id = rsqrtf(d2);
-  const float hS = rec[3];
+// Geometry and moment normalisation of a pair (shared by the features, the
+// analytic translation and the output scaling).
+struct PairGeom {
+  float Rx, Ry, Rz, id, hS, ih, m, im;
+};
+
+__device__ __forceinline__ PairGeom pair_geom(const float* rec, float cTx, float cTy, float cTz) {
+  PairGeom g;
+  g.Rx = cTx - rec[0];
+  g.Ry = cTy - rec[1];
+  g.Rz = cTz - rec[2];
+  const float d2 = g.Rx * g.Rx + g.Ry * g.Ry + g.Rz * g.Rz;
+  g.id = rsqrtf(d2);
+  g.hS = rec[3];
   float n0 = 0.f, n1 = 0.f, n2 = 0.f;
   for (int q = 0; q < 3; ++q) n0 += rec[4 + q] * rec[4 + q];
   for (int q = 0; q < 9; ++q) n1 += rec[10 + q] * rec[10 + q];
@@ -115,23 +124,33 @@ __device__ __forceinline__ PairScale pair_features(const float* rec, float cTx, 
     const float* Q = rec + 19 + 6 * m;
     n2 += Q[0] * Q[0] + Q[3] * Q[3] + Q[5] * Q[5] + 2.f * (Q[1] * Q[1] + Q[2] * Q[2] + Q[4] * Q[4]);
   }
-  const float ih = 1.f / hS;
-  const float m = sqrtf(n0) + sqrtf(n1) * ih + sqrtf(n2) * ih * ih + 1e-30f;
-  const float im = 1.f / m;
-  f[0] = Rx * id;
-  f[1] = Ry * id;
-  f[2] = Rz * id;
-  f[3] = hS * id;
-  f[4] = hT * id;
-  for (int q = 0; q < 3; ++q) f[5 + q] = rec[4 + q] * im;
-  for (int q = 0; q < 9; ++q) f[8 + q] = rec[10 + q] * im * ih;
-  for (int q = 0; q < 18; ++q) f[17 + q] = rec[19 + q] * im * ih * ih;
-  for (int q = NFEAT; q < IN; ++q) f[q] = 0.f;
+  g.ih = 1.f / g.hS;
+  g.m = sqrtf(n0) + sqrtf(n1) * g.ih + sqrtf(n2) * g.ih * g.ih + 1e-30f;
+  g.im = 1.f / g.m;
+  return g;
+}
+
+__device__ __forceinline__ PairScale pair_scale(const PairGeom& g) {
   PairScale s;
-  s.s2 = m * id * id;
-  s.s3 = s.s2 * id;
-  s.s4 = s.s3 * id;
+  s.s2 = g.m * g.id * g.id;
+  s.s3 = s.s2 * g.id;
+  s.s4 = s.s3 * g.id;
   return s;
+}
+
+__device__ __forceinline__ PairScale pair_features(const float* rec, float cTx, float cTy,
+                                                   float cTz, float hT, float* f) {
+  const PairGeom g = pair_geom(rec, cTx, cTy, cTz);
+  f[0] = g.Rx * g.id;
+  f[1] = g.Ry * g.id;
+  f[2] = g.Rz * g.id;
+  f[3] = g.hS * g.id;
+  f[4] = hT * g.id;
+  for (int q = 0; q < 3; ++q) f[5 + q] = rec[4 + q] * g.im;
+  for (int q = 0; q < 9; ++q) f[8 + q] = rec[10 + q] * g.im * g.ih;
+  for (int q = 0; q < 18; ++q) f[17 + q] = rec[19 + q] * g.im * g.ih * g.ih;
+  for (int q = NFEAT; q < IN; ++q) f[q] = 0.f;
+  return pair_scale(g);
 }
 
 // Multipole to local, analytic: the local expansion at the target centre of
@@ -141,17 +160,48 @@ __device__ __forceinline__ PairScale pair_features(const float* rec, float cTx, 
 // + 1/2 M2_mab d_ab phi), phi = 1/|r|, and u_i = eps_ijm d_j Psi_m; the
 // derivatives of phi at |r| = 1 are contracted with the moments in closed
 // form (d^p phi = sum over index pairings of (-1)^(p-k) (2p-2k-1)!! n..n d..d).
-__device__ void m2l_quadrupole(const float* f, float* out) {
-  const float nv[3] = {f[0], f[1], f[2]};
-  const float hs = f[3];
+// Normalised moments of one pair, read from the 48 features...
+struct FeatureMoments {
+  const float* f;
+  __device__ float n(int i) const { return f[i]; }
+  __device__ float hs() const { return f[3]; }
+  __device__ float c(int m) const { return f[5 + m]; }
+  __device__ float m1(int q) const { return f[8 + q]; }    // M1 / (m h_S)
+  __device__ float m2(int q) const { return f[17 + q]; }   // M2 / (m h_S^2)
+};
+// ... or straight from the cell record (same roundings as pair_features), so
+// that the analytic kernel keeps only one component's moments live
+struct RecordMoments {
+  const float* rec;
+  float nx, ny, nz, hs_d, im, ih;
+  __device__ float n(int i) const { return i == 0 ? nx : (i == 1 ? ny : nz); }
+  __device__ float hs() const { return hs_d; }
+  __device__ float c(int m) const { return rec[4 + m] * im; }
+  __device__ float m1(int q) const { return rec[10 + q] * im * ih; }
+  __device__ float m2(int q) const { return rec[19 + q] * im * ih * ih; }
+};
+
+// Multipole to local, analytic: the local expansion at the target centre of
+// the source cell's quadrupole expansion, in the network's normalised output
+// units (unit distance along n = R/d).  With C-scaled moments the vector
+// potential is Psi_m = -(M0_m phi - M1_ma d_a phi + 1/2 M2_mab d_ab phi),
+// phi = 1/|r|, and u_i = eps_ijm d_j Psi_m; the derivatives of phi at |r| = 1
+// are contracted with the moments in closed form (d^p phi = sum over index
+// pairings of (-1)^(p-k) (2p-2k-1)!! n..n d..d).
+template <class Src>
+__device__ __forceinline__ void m2l_core(const Src& src, float* out) {
+  const float nv[3] = {src.n(0), src.n(1), src.n(2)};
+  const float hs = src.hs();
 #pragma unroll
   for (int q = 0; q < NOUT; ++q) out[q] = 0.f;
-#pragma unroll
+#pragma unroll 1
   for (int m = 0; m < 3; ++m) {
-    const float c = f[5 + m];
-    const float v[3] = {f[8 + 3 * m] * hs, f[9 + 3 * m] * hs, f[10 + 3 * m] * hs};
-    const float* q6 = f + 17 + 6 * m;
+    const float c = src.c(m);
+    const float v[3] = {src.m1(3 * m) * hs, src.m1(3 * m + 1) * hs, src.m1(3 * m + 2) * hs};
     const float h2 = hs * hs;
+    float q6[6];
+#pragma unroll
+    for (int u = 0; u < 6; ++u) q6[u] = src.m2(6 * m + u);
     const float Q[3][3] = {{q6[0] * h2, q6[1] * h2, q6[2] * h2},
                            {q6[1] * h2, q6[3] * h2, q6[4] * h2},
                            {q6[2] * h2, q6[4] * h2, q6[5] * h2}};
@@ -162,8 +212,8 @@ __device__ void m2l_quadrupole(const float* f, float* out) {
     const float nqn = qn[0] * nv[0] + qn[1] * nv[1] + qn[2] * nv[2];
     const float tr = Q[0][0] + Q[1][1] + Q[2][2];
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      if (j == m) continue;
+    for (int jj = 0; jj < 2; ++jj) {
+      const int j = (m + 1 + jj) % 3;      // the two j != m
       const int i = 3 - m - j;
       const float sg = ((j - i + 3) % 3 == 1) ? 1.f : -1.f;  // eps_ijm
       const float nj = nv[j];
@@ -202,6 +252,10 @@ __device__ void m2l_quadrupole(const float* f, float* out) {
       }
     }
   }
+}
+
+__device__ __forceinline__ void m2l_quadrupole(const float* f, float* out) {
+  m2l_core(FeatureMoments{f}, out);
 }
 
 __device__ __forceinline__ float3 leaf_center(uint32_t key, float h) {
@@ -330,10 +384,9 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
           const PairScale sc = pair_features(
               A.f.rec + static_cast<int64_t>(A.f.pair_cell[row]) * kRecFloats, cT.x, cT.y, cT.z,
               A.f.h, f);
-          m2l_quadrupole(f, ax);
-          ax[30] = sc.s2;
-          ax[31] = sc.s3;
-          ax[32] = sc.s4;
+          ax[0] = sc.s2;
+          ax[1] = sc.s3;
+          ax[2] = sc.s4;
         } else {
           for (int q = 0; q < IN; ++q) f[q] = 0.f;
         }
@@ -392,10 +445,11 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
           const int c = c0 + i;
           float x = 0.f;
           if (act_row && c < NOUT) {
-            // analytic M2L + learned residual, back to physical units
+            // the learned residual, back to physical units (the analytic
+            // translation is added by its own kernel)
             const float* ax = S.aux[grp][lt];
-            const float s = c < 3 ? ax[30] : (c < 12 ? ax[31] : ax[32]);
-            x = (ax[c] + v[i] + S.bias[B4o + c]) * s;
+            const float s = c < 3 ? ax[0] : (c < 12 ? ax[1] : ax[2]);
+            x = (v[i] + S.bias[B4o + c]) * s;
           }
 #pragma unroll
           for (int off = 1; off < 32; off <<= 1) {
@@ -532,12 +586,13 @@ __global__ void __launch_bounds__(256) m2l_pairs_kernel(int npairs, const int* _
   PairScale sc{0.f, 0.f, 0.f};
   int leaf = 0;
   if (act_row) {
-    float f[IN];
     leaf = pair_leaf[row];
     const float3 cT = leaf_center(leaf_key[leaf], h);
-    sc = pair_features(rec + static_cast<int64_t>(pair_cell[row]) * kRecFloats, cT.x, cT.y, cT.z,
-                       h, f);
-    m2l_quadrupole(f, a);
+    const float* r = rec + static_cast<int64_t>(pair_cell[row]) * kRecFloats;
+    const PairGeom g = pair_geom(r, cT.x, cT.y, cT.z);
+    const RecordMoments src{r, g.Rx * g.id, g.Ry * g.id, g.Rz * g.id, g.hS * g.id, g.im, g.ih};
+    m2l_core(src, a);
+    sc = pair_scale(g);
   } else {
 #pragma unroll
     for (int q = 0; q < NOUT; ++q) a[q] = 0.f;

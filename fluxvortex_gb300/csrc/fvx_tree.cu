@@ -1513,14 +1513,15 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
       FVX_CUDA_TRY(cudaEventCreate(&T->ev3));
     }
     FVX_CUDA_TRY(cudaEventRecord(T->ev2, s));
+    // the analytic translation, then (learned) the network's residual
+    rc = m2l_farfield_launch(static_cast<int>(lrn_total), P<int>(T->lrn_leaf),
+                             P<int>(T->lrn_cell), leaves.key, rec, static_cast<float>(h),
+                             P<float>(T->leaf_local), s);
+    if (rc) return rc;
     if (T->far_method == FVX_FAR_LEARNED)
       rc = mlp_farfield_launch(static_cast<int>(lrn_total), P<int>(T->lrn_leaf),
                                P<int>(T->lrn_cell), leaves.key, rec, static_cast<float>(h),
                                T->mlp_W, T->mlp_b, P<float>(T->leaf_local), s);
-    else
-      rc = m2l_farfield_launch(static_cast<int>(lrn_total), P<int>(T->lrn_leaf),
-                               P<int>(T->lrn_cell), leaves.key, rec, static_cast<float>(h),
-                               P<float>(T->leaf_local), s);
     if (rc) return rc;
     FVX_CUDA_TRY(cudaEventRecord(T->ev3, s));
     A.leaf_local = P<float>(T->leaf_local);
