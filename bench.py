@@ -93,6 +93,8 @@ def parse():
                         "accepted cells per target particle (tree = m2p), as analytic local "
                         "expansions (m2l), or through the learned far-field operator")
     p.add_argument("--leaf", type=int, default=48, help="treecode particles per leaf")
+    p.add_argument("--no-flutter", dest="flutter", action="store_false",
+                   help="skip the batched flutter-sweep measurement")
     p.add_argument("--cl-steps", type=int, default=2,
                    help="steps of the CL-history check against direct sweeps (0: off)")
     p.add_argument("--no-e2e", action="store_true")
@@ -237,6 +239,57 @@ def cpu_oracle_step_seconds(host, n_t, threads=None):
 
 
 # ---------------------------------------------------------------------------
+def flutter_sweep_measure(args):
+    """The batched flutter sweep (Goland wing, 64 airspeeds over 80-180 m/s,
+    100 chords of travel each: 339..762 steps, particle wakes of uneven
+    length): one persistent launch per sweep replayed from a CUDA graph, with
+    the aerodynamic particle sums in FP32 (compensated) and in FP64; flutter
+    speeds of both, and the FP64 CPU oracle's time for one environment step
+    scaled to the sweep."""
+    import numpy as np
+    import torch
+    from fluxvortex_gb300.flutter import FlutterSweep, goland
+    cfg = goland()
+    V = cfg.velocities(64)
+    out = {"workload": "Goland wing 8x4 panels, beam 8 elements, 64 airspeeds 80-180 m/s, "
+                       f"{cfg.num_chords:g} chords, n_keep {cfg.n_keep}, "
+                       f"<= {cfg.max_particles} particles per environment",
+           "steps_per_env": [int(min(cfg.n_steps(v) for v in V)), int(max(cfg.n_steps(v) for v in V))]}
+    for prec in ("f32c", "f64"):
+        sw = FlutterSweep(cfg, V, precision=prec, threads="auto")
+        sw.run(graph=True)                    # capture + first replay
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(3):
+            sw.reset()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            sw.run(graph=True)
+            e.record()
+            torch.cuda.synchronize()
+            ms.append(s.elapsed_time(e))
+        total_steps = int(sw.steps.sum())
+        out[prec] = {"sweep_ms": min(ms), "env_steps_per_s": total_steps / (min(ms) * 1e-3),
+                     "threads_per_env": sw.threads, "flutter_speed_mps": sw.flutter_speed()}
+    a, b = out["f32c"]["flutter_speed_mps"], out["f64"]["flutter_speed_mps"]
+    out["flutter_speed_diff_mps"] = None if a is None or b is None else abs(a - b)
+    if not args.no_baselines:
+        import time as _t
+        from oracle.flutter import FlutterOracle
+        o = FlutterOracle(cfg, float(V[0]))
+        for _ in range(30):                   # wake rows start converting after n_keep
+            o.step()
+        t0 = _t.perf_counter()
+        for _ in range(10):
+            o.step()
+        per_step = (_t.perf_counter() - t0) / 10
+        out["cpu_oracle"] = {"s_per_env_step": per_step,
+                             "sweep_s_extrapolated": per_step * int(sw.steps.sum()),
+                             "kind": "port", "cores": 1,
+                             "sample": "10 steps of the 80 m/s environment after 30 warm-up steps"}
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -417,6 +470,9 @@ def run_ours(args, rank, world):
                                   "sample": f"{detail['targets']} targets x {detail['sources']} "
                                             "sources per sweep kind, FP64 C oracle with OpenMP, "
                                             "scaled to the full step by N/targets"}
+
+    if args.flutter and rank == 0:
+        result["flutter_sweep"] = flutter_sweep_measure(args)
 
     if args.cl_steps > 0 and rank == 0 and args.far_field != "direct":
         # CL / CDi history of the benchmarked form against direct all-pairs

@@ -183,7 +183,7 @@ class FlutterSweep:
         E = len(self.V)
         nc, ns = cfg.nc, cfg.ns
         P = nc * ns
-        self.threads = threads or min(512, 4 * 2 * P)
+        self.threads = None if threads in (None, "auto") else int(threads)
         beam = cfg.beam_model()
         self.beam = beam
         self.steps = np.array([cfg.n_steps(v) for v in self.V], dtype=np.int32)
@@ -229,6 +229,28 @@ class FlutterSweep:
         self.state = _State(**{n: t.data_ptr() for n, t in self.st.items()})
         self._graph = None
         self.reset()
+        if self.threads is None:
+            self.threads = self.autotune()
+
+    def autotune(self, steps=40):
+        """Threads per environment CTA (the number of slices the wake sums are
+        split into) from timing the first ``steps`` steps of this sweep with
+        each candidate; cached per device and problem."""
+        from . import autotune
+        P = self.cfg.nc * self.cfg.ns
+        cands = [t for t in (64, 128, 256, 512) if t >= 2 * P and t % (2 * P) == 0]
+        st = self.torch.cuda.current_stream(self.device).cuda_stream
+
+        def run(t):
+            self.reset()
+            self.threads = t
+            self._launch(min(steps, self.max_steps), st)
+
+        key = (f"flutter_sweep/nc{self.cfg.nc}ns{self.cfg.ns}/E{len(self.V)}"
+               f"/particles{self.cfg.max_particles}/prec{self.precision}/steps{steps}")
+        best = autotune.best(key, cands, run)
+        self.reset()
+        return best
 
     def reset(self):
         torch = self.torch
