@@ -483,29 +483,35 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
 }
 
 // ---- training data: features + exact local expansions of sampled pairs ----------
-// One CTA per pair: FP64 direct sums over the source cell's particles of the
-// singular Biot-Savart field and its first two derivatives at c_T (threads
-// stride over the particles; warps, then the CTA, reduce in a fixed order).
-__global__ void pair_targets_kernel(int npairs, int stride, const int* __restrict__ pair_leaf,
-                                    const int* __restrict__ pair_cell,
-                                    const uint32_t* __restrict__ leaf_key,
-                                    const float* __restrict__ rec, const int* __restrict__ cell_start,
-                                    const int* __restrict__ cell_count,
-                                    const float4* __restrict__ sp, const float4* __restrict__ sa,
-                                    const int* __restrict__ leaf_of_particle, float h,
-                                    __nv_bfloat16* __restrict__ X, float* __restrict__ T,
-                                    float* __restrict__ Aout, float* __restrict__ scale) {
-  const int warp = blockIdx.x;  // the pair
+// FP64 direct sums over the source cell's particles of the singular
+// Biot-Savart field and its first two derivatives at c_T.  blockIdx.x = the
+// pair, blockIdx.y = one of gridDim.y slices of the cell's particles (so that
+// a few very large cells still spread over the GPU); threads stride over the
+// slice, warps then the CTA reduce in a fixed order, and each slice writes its
+// own partial sums (no atomics: the result does not depend on timing).
+__global__ void pair_sums_kernel(int npairs, int stride, const int* __restrict__ pair_leaf,
+                                 const int* __restrict__ pair_cell,
+                                 const uint32_t* __restrict__ tgt_key, float h_tgt,
+                                 const uint32_t* __restrict__ leaf_key,
+                                 const int* __restrict__ cell_start,
+                                 const int* __restrict__ cell_count,
+                                 const float4* __restrict__ sp, const float4* __restrict__ sa,
+                                 const int* __restrict__ leaf_of_particle, float h,
+                                 double* __restrict__ partial) {
+  const int pr = blockIdx.x;
   const int lane = threadIdx.x & 31;
   __shared__ double red[kTargetsThreads / 32][NOUT];
-  if (warp >= npairs) return;
-  const int t = pair_leaf[static_cast<int64_t>(warp) * stride],
-            g = pair_cell[static_cast<int64_t>(warp) * stride];
-  const float3 cT = leaf_center(leaf_key[t], h);
+  if (pr >= npairs) return;
+  const int t = pair_leaf[static_cast<int64_t>(pr) * stride],
+            g = pair_cell[static_cast<int64_t>(pr) * stride];
+  const float3 cT = leaf_center(tgt_key[t], h_tgt);
   double acc[NOUT];
 #pragma unroll
   for (int q = 0; q < NOUT; ++q) acc[q] = 0.0;
-  const int s0 = cell_start[g], n = cell_count[g];
+  const int c0 = cell_start[g], cn = cell_count[g];
+  const int per = (cn + gridDim.y - 1) / gridDim.y;
+  const int s0 = c0 + static_cast<int>(blockIdx.y) * per;
+  const int n = max(0, min(per, c0 + cn - s0));
   for (int i = s0 + static_cast<int>(threadIdx.x); i < s0 + n; i += blockDim.x) {
     const float3 cs = leaf_center(leaf_key[leaf_of_particle[i] - 1], h);
     const float4 p = sp[i];
@@ -539,35 +545,53 @@ __global__ void pair_targets_kernel(int npairs, int stride, const int* __restric
   if (lane == 0)
     for (int q = 0; q < NOUT; ++q) red[threadIdx.x >> 5][q] = acc[q];
   __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int q = 0; q < NOUT; ++q) {
-      double v = 0.0;
-      for (int w = 0; w < kTargetsThreads / 32; ++w) v += red[w][q];
-      acc[q] = v;
+  if (threadIdx.x < NOUT) {
+    double v = 0.0;
+    for (int w = 0; w < kTargetsThreads / 32; ++w) v += red[w][threadIdx.x];
+    partial[(static_cast<int64_t>(pr) * gridDim.y + blockIdx.y) * NOUT + threadIdx.x] = v;
+  }
+}
+
+// Per pair: the slices' sums in order, the features (BF16), the output scales,
+// the analytic translation and the normalised exact targets.
+__global__ void pair_targets_kernel(int npairs, int stride, int slices,
+                                    const int* __restrict__ pair_leaf,
+                                    const int* __restrict__ pair_cell,
+                                    const uint32_t* __restrict__ tgt_key, float h_tgt,
+                                    const float* __restrict__ rec,
+                                    const double* __restrict__ partial,
+                                    __nv_bfloat16* __restrict__ X, float* __restrict__ T,
+                                    float* __restrict__ Aout, float* __restrict__ scale) {
+  const int pr = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pr >= npairs) return;
+  const int t = pair_leaf[static_cast<int64_t>(pr) * stride],
+            g = pair_cell[static_cast<int64_t>(pr) * stride];
+  const float3 cT = leaf_center(tgt_key[t], h_tgt);
+  float f[IN];
+  const PairScale sc =
+      pair_features(rec + static_cast<int64_t>(g) * kRecFloats, cT.x, cT.y, cT.z, h_tgt, f);
+  for (int q = 0; q < IN; ++q) X[static_cast<int64_t>(pr) * IN + q] = __float2bfloat16(f[q]);
+  if (scale) {
+    scale[static_cast<int64_t>(pr) * 4 + 0] = sc.s2;
+    scale[static_cast<int64_t>(pr) * 4 + 1] = sc.s3;
+    scale[static_cast<int64_t>(pr) * 4 + 2] = sc.s4;
+    scale[static_cast<int64_t>(pr) * 4 + 3] = f[4];  // h_T / d
+  }
+  if (Aout) {
+    float a[NOUT];
+    m2l_quadrupole(f, a);
+    for (int q = 0; q < OUT; ++q) Aout[static_cast<int64_t>(pr) * OUT + q] = q < NOUT ? a[q] : 0.f;
+  }
+  const double* ps = partial + static_cast<int64_t>(pr) * slices * NOUT;
+  for (int q = 0; q < OUT; ++q) {
+    float v = 0.f;
+    if (q < NOUT) {
+      double acc = 0.0;
+      for (int k = 0; k < slices; ++k) acc += ps[k * NOUT + q];
+      const double s = q < 3 ? sc.s2 : (q < 12 ? sc.s3 : sc.s4);
+      v = static_cast<float>(acc / s);
     }
-    float f[IN];
-    const PairScale sc =
-        pair_features(rec + static_cast<int64_t>(g) * kRecFloats, cT.x, cT.y, cT.z, h, f);
-    for (int q = 0; q < IN; ++q) X[static_cast<int64_t>(warp) * IN + q] = __float2bfloat16(f[q]);
-    if (scale) {
-      scale[static_cast<int64_t>(warp) * 4 + 0] = sc.s2;
-      scale[static_cast<int64_t>(warp) * 4 + 1] = sc.s3;
-      scale[static_cast<int64_t>(warp) * 4 + 2] = sc.s4;
-      scale[static_cast<int64_t>(warp) * 4 + 3] = f[4];  // h_T / d
-    }
-    if (Aout) {
-      float a[NOUT];
-      m2l_quadrupole(f, a);
-      for (int q = 0; q < OUT; ++q) Aout[static_cast<int64_t>(warp) * OUT + q] = q < NOUT ? a[q] : 0.f;
-    }
-    for (int q = 0; q < OUT; ++q) {
-      float v = 0.f;
-      if (q < NOUT) {
-        const double s = q < 3 ? sc.s2 : (q < 12 ? sc.s3 : sc.s4);
-        v = static_cast<float>(acc[q] / s);
-      }
-      T[static_cast<int64_t>(warp) * OUT + q] = v;
-    }
+    T[static_cast<int64_t>(pr) * OUT + q] = v;
   }
 }
 
@@ -847,15 +871,22 @@ int m2l_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
   return FVX_OK;
 }
 
+// partial: scratch of npairs x slices x 30 doubles
 int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const int* pair_cell,
-                            const uint32_t* leaf_key, const float* rec, const int* cell_start,
+                            const uint32_t* tgt_key, float h_tgt, const uint32_t* leaf_key,
+                            const float* rec, const int* cell_start,
                             const int* cell_count, const float4* sp, const float4* sa,
                             const int* leaf_of_particle, float h, void* X, float* T,
-                            float* A, float* scale, cudaStream_t s) {
+                            float* A, float* scale, double* partial, int slices,
+                            cudaStream_t s) {
   if (npairs <= 0) return FVX_OK;
-  mlp::pair_targets_kernel<<<npairs, mlp::kTargetsThreads, 0, s>>>(
-      npairs, stride, pair_leaf, pair_cell, leaf_key, rec, cell_start, cell_count, sp, sa,
-      leaf_of_particle, h, static_cast<__nv_bfloat16*>(X), T, A, scale);
+  mlp::pair_sums_kernel<<<dim3(npairs, slices), mlp::kTargetsThreads, 0, s>>>(
+      npairs, stride, pair_leaf, pair_cell, tgt_key, h_tgt, leaf_key, cell_start, cell_count, sp,
+      sa, leaf_of_particle, h, partial);
+  FVX_LAUNCH_CHECK();
+  mlp::pair_targets_kernel<<<(npairs + 127) / 128, 128, 0, s>>>(
+      npairs, stride, slices, pair_leaf, pair_cell, tgt_key, h_tgt, rec, partial,
+      static_cast<__nv_bfloat16*>(X), T, A, scale);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }

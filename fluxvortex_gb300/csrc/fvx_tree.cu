@@ -465,6 +465,7 @@ struct TreeView {
   // path when d2 > thr_lrn[l]
   int thr_far[11];
   int thr_lrn[11];
+  int thr_par[11];  // the same test for a parent of leaves (size 2h) as the target
 };
 
 // (target leaf, source cell) pairs handed to the learned far-field operator
@@ -550,6 +551,150 @@ __global__ void traverse_kernel(TreeView T, const int* __restrict__ near_off,
   }
 }
 
+// ---- two-level (dual) traversal for the local-expansion far field -------------------
+// The source cells A are tested against the parent P of each leaf T (level
+// L-1) first: A is accepted for the whole parent when the test passes for P
+// (one local expansion about c_P, shared by P's leaves); a failing A larger
+// than P is accepted by T itself when it passes for every possible child of P
+// (the nearest octant), and opened otherwise; a failing A of P's size or a
+// leaf is then tested against T, which accepts A (local pair), or -- A being a
+// leaf -- keeps it as a near leaf, or accepts / keeps near each of A's children.  This is the dual-tree
+// rule "split the larger cell" on (P, A) then (T, A): every source particle
+// reaches every leaf exactly once, through P's expansion, T's own expansions
+// or T's near list.  One thread per leaf (the parent-level decisions depend on
+// P only, so siblings take them identically); the first child of each parent
+// writes the parent's pairs.
+struct DualLists {
+  int* near_cnt;     // per leaf
+  int* lrn_cnt;      // per leaf: (leaf, cell) local pairs
+  int* par_cnt;      // per parent: (parent, cell) local pairs
+  const int* near_off;
+  const int* lrn_off;
+  const int* par_off;
+  int* near_idx;
+  int* lrn_leaf;
+  int* lrn_cell;
+  int* par_par;
+  int* par_cell;
+  int* leaf_parent;  // per leaf: its parent's level-local index
+  int near_cap, lrn_cap, par_cap;
+};
+
+template <bool FILL>
+__global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restrict__ overflow) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = T.L;
+  const int nleaf = T.ncell[L];
+  if (t >= nleaf) return;
+  const int gT = T.base[L] + t;
+  const uint32_t kT = T.key[gT];
+  // the parent: binary search of key >> 3 among the level L-1 keys
+  const uint32_t kP = kT >> 3;
+  int lo = 0, hi = T.ncell[L - 1] - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (T.key[T.base[L - 1] + mid] < kP)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  const int p = lo;
+  const int gP = T.base[L - 1] + p;
+  const bool first = T.child_lo[gP] == t;
+  // centres in units of h/2: a parent (size 2h) at (2 k + 1) 2, a leaf at 2 k + 1
+  const int px = 2 * (2 * static_cast<int>(compact10(kP)) + 1),
+            py = 2 * (2 * static_cast<int>(compact10(kP >> 1)) + 1),
+            pz = 2 * (2 * static_cast<int>(compact10(kP >> 2)) + 1);
+  const int tx = 2 * static_cast<int>(compact10(kT)) + 1,
+            ty = 2 * static_cast<int>(compact10(kT >> 1)) + 1,
+            tz = 2 * static_cast<int>(compact10(kT >> 2)) + 1;
+  const int tcount = T.count[gT];
+  if (FILL) D.leaf_parent[t] = p;
+  int nn = 0, nl = 0, np = 0;
+  const int no = FILL ? D.near_off[t] : 0, lo_ = FILL ? D.lrn_off[t] : 0;
+  const int po = (FILL && first) ? D.par_off[p] : 0;
+  long long near_pairs = 0;
+  // T against source cell g at level l; false: an inner cell that fails
+  auto leaf_visit = [&](int g, int l) {
+    const uint32_t k = T.key[g];
+    const int sc = 1 << (L - l);
+    const int dx = tx - (2 * static_cast<int>(compact10(k)) + 1) * sc;
+    const int dy = ty - (2 * static_cast<int>(compact10(k >> 1)) + 1) * sc;
+    const int dz = tz - (2 * static_cast<int>(compact10(k >> 2)) + 1) * sc;
+    const int d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 > T.thr_far[l]) {
+      if (FILL && lo_ + nl < D.lrn_cap) {
+        D.lrn_leaf[lo_ + nl] = t;
+        D.lrn_cell[lo_ + nl] = g;
+      }
+      ++nl;
+      return true;
+    }
+    if (l == L) {
+      if (FILL && no + nn < D.near_cap) D.near_idx[no + nn] = g - T.base[L];
+      near_pairs += static_cast<long long>(tcount) * T.count[g];
+      ++nn;
+      return true;
+    }
+    return false;
+  };
+  int stack[96];
+  int sp = 0;
+  for (int c = T.ncell[0] - 1; c >= 0; --c) stack[sp++] = T.base[0] + c;
+  while (sp > 0) {
+    const int e = stack[--sp];
+    const int g = e & ((1 << 27) - 1), l = e >> 27;
+    const uint32_t k = T.key[g];
+    const int sc = 1 << (L - l);
+    const int dx = px - (2 * static_cast<int>(compact10(k)) + 1) * sc;
+    const int dy = py - (2 * static_cast<int>(compact10(k >> 1)) + 1) * sc;
+    const int dz = pz - (2 * static_cast<int>(compact10(k >> 2)) + 1) * sc;
+    const int d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 > T.thr_par[l]) {
+      if (first) {
+        if (FILL && po + np < D.par_cap) {
+          D.par_par[po + np] = p;
+          D.par_cell[po + np] = g;
+        }
+        ++np;
+      }
+      continue;
+    }
+    if (l < L - 1) {
+      // accepted by every child of P (the octant of P nearest to A passes the
+      // leaf test; the decision depends on P and A only): a pair of T's own,
+      // as the per-leaf traversal would make it; otherwise A is opened
+      const int ax = abs(dx) - 1, ay = abs(dy) - 1, az = abs(dz) - 1;
+      if (ax * ax + ay * ay + az * az > T.thr_far[l]) {
+        leaf_visit(g, l);
+        continue;
+      }
+      const int clo = T.child_lo[g], chi = T.child_hi[g];
+      for (int c = chi - 1; c >= clo; --c) {
+        if (sp < 96)
+          stack[sp++] = (T.base[l + 1] + c) | ((l + 1) << 27);
+        else
+          atomicOr(overflow, 1u);
+      }
+      continue;
+    }
+    // A of P's size (level L-1) or a leaf: against T itself
+    if (leaf_visit(g, l)) continue;
+    const int clo = T.child_lo[g], chi = T.child_hi[g];  // A at level L-1: leaves below
+    for (int q = clo; q < chi; ++q) leaf_visit(T.base[L] + q, L);
+  }
+  if (!FILL) {
+    D.near_cnt[t] = nn;
+    D.lrn_cnt[t] = nl;
+    if (first) D.par_cnt[p] = np;
+  } else {
+    if (no + nn > D.near_cap || lo_ + nl > D.lrn_cap || (first && po + np > D.par_cap))
+      atomicOr(overflow, 2u);
+    unsigned long long* work = reinterpret_cast<unsigned long long*>(overflow + 2);
+    atomicAdd(work, static_cast<unsigned long long>(near_pairs));
+  }
+}
+
 // ---- evaluation -----------------------------------------------------------------------
 struct EvalArgs {
   float h;  // leaf size
@@ -570,6 +715,8 @@ struct EvalArgs {
   double* out_a;
   double* out_b;
   const float* leaf_local;  // [leaves][32] learned local expansions, or null
+  const float* parent_local;  // [parents][32] expansions shared by a parent's leaves, or null
+  const int* leaf_parent;     // parent index of each leaf (with parent_local)
 };
 
 // Learned local expansion of the leaf at offset d = x - c_T (u, J = du/dx,
@@ -727,9 +874,10 @@ __device__ __forceinline__ uint64_t fma(uint64_t a, uint64_t b, uint64_t c) {
 
 // One source per row of the packed near tile, every value duplicated into
 // both halves of a 64-bit pair: {-x, -y}, {-z, s2}, {k2, ax}, {ay, az},
-// {10.5 s2, -}.
+// {-ax, -ay}, {-az, 10.5 s2} (the negated strengths turn each cross-product
+// component into two fused multiply-adds).
 struct NearX2 {
-  ulonglong2 q[5];
+  ulonglong2 q[6];
 };
 
 // Near pairs of one staged tile for the thread's two targets (Winckelmans
@@ -753,25 +901,25 @@ __device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, in
     const uint64_t T2 = x2::mul(T, T);
     const uint64_t T5 = x2::mul(x2::mul(T2, T2), T);
     const uint64_t F = x2::mul(x2::add(R2, q2.x), T5);
-    const uint64_t AX = q2.y, AY = q3.x, AZ = q3.y;
+    const ulonglong2 q4 = tile[k].q[4], q5 = tile[k].q[5];
+    const uint64_t AX = q2.y, AY = q3.x, AZ = q3.y, NAX = q4.x, NAY = q4.y, NAZ = q5.x;
     if (MODE == FVX_PAIR_VELOCITY) {
       const uint64_t EX = x2::mul(F, DX), EY = x2::mul(F, DY), EZ = x2::mul(F, DZ);
-      acc[0] = x2::sub(x2::fma(EY, AZ, acc[0]), x2::mul(EZ, AY));
-      acc[1] = x2::sub(x2::fma(EZ, AX, acc[1]), x2::mul(EX, AZ));
-      acc[2] = x2::sub(x2::fma(EX, AY, acc[2]), x2::mul(EY, AX));
+      acc[0] = x2::fma(EZ, NAY, x2::fma(EY, AZ, acc[0]));
+      acc[1] = x2::fma(EX, NAZ, x2::fma(EZ, AX, acc[1]));
+      acc[2] = x2::fma(EY, NAX, x2::fma(EX, AY, acc[2]));
     } else {
       // S += (f G + fpr (d . G) d) x a, fpr = -(3 r2 + 10.5 s2) t^7
-      const ulonglong2 q4 = tile[k].q[4];
       uint64_t DG = x2::mul(DX, GX);
       DG = x2::fma(DY, GY, DG);
       DG = x2::fma(DZ, GZ, DG);
-      const uint64_t W = x2::mul(x2::mul(x2::fma(R2, C3, q4.x), x2::mul(T5, T2)), DG);
+      const uint64_t W = x2::mul(x2::mul(x2::fma(R2, C3, q5.y), x2::mul(T5, T2)), DG);
       const uint64_t VX = x2::sub(x2::mul(F, GX), x2::mul(W, DX));
       const uint64_t VY = x2::sub(x2::mul(F, GY), x2::mul(W, DY));
       const uint64_t VZ = x2::sub(x2::mul(F, GZ), x2::mul(W, DZ));
-      acc[0] = x2::sub(x2::fma(VY, AZ, acc[0]), x2::mul(VZ, AY));
-      acc[1] = x2::sub(x2::fma(VZ, AX, acc[1]), x2::mul(VX, AZ));
-      acc[2] = x2::sub(x2::fma(VX, AY, acc[2]), x2::mul(VY, AX));
+      acc[0] = x2::fma(VZ, NAY, x2::fma(VY, AZ, acc[0]));
+      acc[1] = x2::fma(VX, NAZ, x2::fma(VZ, AX, acc[1]));
+      acc[2] = x2::fma(VY, NAX, x2::fma(VX, AY, acc[2]));
     }
   }
 }
@@ -852,7 +1000,8 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
             e.q[1] = make_ulonglong2(x2::pack(-pv.z, -pv.z), x2::pack(pv.w, pv.w));
             e.q[2] = make_ulonglong2(x2::pack(av.w, av.w), x2::pack(av.x, av.x));
             e.q[3] = make_ulonglong2(x2::pack(av.y, av.y), x2::pack(av.z, av.z));
-            e.q[4] = make_ulonglong2(x2::pack(10.5f * pv.w, 10.5f * pv.w), 0ull);
+            e.q[4] = make_ulonglong2(x2::pack(-av.x, -av.x), x2::pack(-av.y, -av.y));
+            e.q[5] = make_ulonglong2(x2::pack(-av.z, -av.z), x2::pack(10.5f * pv.w, 10.5f * pv.w));
             s_x2[k] = e;
           }
           __syncthreads();
@@ -925,6 +1074,24 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
       for (int j = 0; j < TPT; ++j)
 #pragma unroll
         for (int c = 0; c < NC; ++c) fold(hi[j][c], lo[j][c], part[j][c]);
+    }
+    if (A.parent_local) {
+      // the parent's expansion about its own centre (parent key = leaf key >> 3)
+      const float3 cP = cell_center_rel(A.leaf_key[t] >> 3, 2.f * A.h);
+      const float qx = cT.x - cP.x, qy = cT.y - cP.y, qz = cT.z - cP.z;
+      const float* L = A.parent_local + static_cast<int64_t>(A.leaf_parent[t]) * 32;
+      float Ls[30];
+#pragma unroll
+      for (int c = 0; c < 30; ++c) Ls[c] = L[c];
+#pragma unroll
+      for (int j = 0; j < TPT; ++j) {
+        float part[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) part[c] = 0.f;
+        l2p<MODE>(part, Ls, ox[j] + qx, oy[j] + qy, oz[j] + qz, gx[j], gy[j], gz[j]);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) fold(hi[j][c], lo[j][c], part[c]);
+      }
     }
     if (A.leaf_local) {
       const float* L = A.leaf_local + static_cast<int64_t>(t) * 32;
@@ -1150,10 +1317,12 @@ int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
                         const uint32_t* leaf_key, const float* rec, float h, const void* W,
                         const float* bias, float* leaf_local, cudaStream_t s);
 int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const int* pair_cell,
-                            const uint32_t* leaf_key, const float* rec, const int* cell_start,
+                            const uint32_t* tgt_key, float h_tgt, const uint32_t* leaf_key,
+                            const float* rec, const int* cell_start,
                             const int* cell_count, const float4* sp, const float4* sa,
                             const int* leaf_of_particle, float h, void* X, float* T,
-                            float* A, float* scale, cudaStream_t s);
+                            float* A, float* scale, double* partial, int slices,
+                            cudaStream_t s);
 int m2l_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
                         const uint32_t* leaf_key, const float* rec, float h, float* leaf_local,
                         cudaStream_t s);
@@ -1177,6 +1346,10 @@ struct fvx_tree {
   double val_tol = 0.05;
   fvx::DevBuf val_X, val_T, val_A, val_Y, val_scale, val_err, val_fb, val_stats;
   int last_val_k = 0;
+  // two-level traversal: per-parent lists and expansions
+  fvx::DevBuf dual_meta, par_par, par_cell, parent_local;
+  fvx::DevBuf pair_partial;  // slices of the FP64 exact-expansion sums
+  int n_parent_pairs = 0;
   fvx::DevBuf lrn_meta, lrn_leaf, lrn_cell, leaf_local;
   int n_learned = 0;
   // the last sweep's tree, for sampling training pairs
@@ -1432,8 +1605,20 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
                            : 2147483647;
   }
   V.learned_only = learned ? 1 : 0;
+  // two-level traversal when every accepted cell takes the local expansion
+  bool dual = learned && L >= 1;
+  for (int l = 0; l <= L; ++l) {
+    if (V.thr_lrn[l] != V.thr_far[l]) dual = false;
+    // (h_P + h_S)^2 in (h/2)^2 units for a parent of leaves (size 2h)
+    const double hp2 = 4.0 * (2.0 + static_cast<double>(1 << (L - l))) *
+                       (2.0 + static_cast<double>(1 << (L - l)));
+    const double tp = floor(V.mac_k * hp2);
+    V.thr_par[l] = tp < 2147483647.0 ? static_cast<int>(tp) : 2147483647;
+  }
+  const int npar = dual ? ncells[L - 1] : 0;
   if ((rc = grow(T->lists_meta, 4 * size_t(nleaf) * 4 + 64))) return rc;
   if (learned && (rc = grow(T->lrn_meta, 4 * size_t(nleaf) * 2 + 64))) return rc;
+  if (dual && (rc = grow(T->dual_meta, 4 * (2 * size_t(npar) + size_t(nleaf)) + 64))) return rc;
   LearnedLists LL{nullptr, nullptr, nullptr, nullptr, 0};
   if (learned) {
     LL.cnt = P<int>(T->lrn_meta);
@@ -1444,18 +1629,40 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   int* near_off = far_cnt + nleaf;
   int* far_off = near_off + nleaf;
   unsigned* ovf = reinterpret_cast<unsigned*>(far_off + nleaf);  // + 2 x u64 work counters
+  int* par_cnt = dual ? P<int>(T->dual_meta) : nullptr;
+  int* par_off = dual ? par_cnt + npar : nullptr;
+  int* leaf_parent = dual ? par_off + npar : nullptr;
   FVX_CUDA_TRY(cudaMemsetAsync(ovf, 0, 24, s));
-  traverse_kernel<false><<<(nleaf + 127) / 128, 128, 0, s>>>(
-      V, nullptr, nullptr, near_cnt, far_cnt, nullptr, nullptr, 0, 0, ovf, LL);
+  DualLists D{};
+  if (dual) {
+    // no per-target far cells on this path
+    FVX_CUDA_TRY(cudaMemsetAsync(far_cnt, 0, sizeof(int) * size_t(nleaf), s));
+    D.near_cnt = near_cnt;
+    D.lrn_cnt = LL.cnt;
+    D.par_cnt = par_cnt;
+    D.near_off = near_off;
+    D.lrn_off = LL.off;
+    D.par_off = par_off;
+    D.leaf_parent = leaf_parent;
+    traverse_dual_kernel<false><<<(nleaf + 127) / 128, 128, 0, s>>>(V, D, ovf);
+  } else {
+    traverse_kernel<false><<<(nleaf + 127) / 128, 128, 0, s>>>(
+        V, nullptr, nullptr, near_cnt, far_cnt, nullptr, nullptr, 0, 0, ovf, LL);
+  }
   FVX_LAUNCH_CHECK();
   if ((rc = scan_ints(near_cnt, nleaf, near_off, 0, P<int>(T->scan_tmp), s))) return rc;
   if ((rc = scan_ints(far_cnt, nleaf, far_off, 0, P<int>(T->scan_tmp), s))) return rc;
-  int ltail[2] = {0, 0};
+  int ltail[4] = {0, 0, 0, 0};
   if (learned) {
     if ((rc = scan_ints(LL.cnt, nleaf, P<int>(T->lrn_meta) + nleaf, 0, P<int>(T->scan_tmp), s)))
       return rc;
     FVX_CUDA_TRY(cudaMemcpyAsync(&ltail[0], LL.cnt + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
     FVX_CUDA_TRY(cudaMemcpyAsync(&ltail[1], LL.off + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
+  }
+  if (dual) {
+    if ((rc = scan_ints(par_cnt, npar, par_off, 0, P<int>(T->scan_tmp), s))) return rc;
+    FVX_CUDA_TRY(cudaMemcpyAsync(&ltail[2], par_cnt + npar - 1, 4, cudaMemcpyDeviceToHost, s));
+    FVX_CUDA_TRY(cudaMemcpyAsync(&ltail[3], par_off + npar - 1, 4, cudaMemcpyDeviceToHost, s));
   }
   int tail[4];
   FVX_CUDA_TRY(cudaMemcpyAsync(&tail[0], near_cnt + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
@@ -1471,7 +1678,9 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
       (rc = grow(T->far_list, 4 * size_t(far_total + 1))))
     return rc;
   const int64_t lrn_total = int64_t(ltail[0]) + ltail[1];
-  FVX_ARG_CHECK(lrn_total < (int64_t(1) << 31), "learned pair list too long");
+  const int64_t par_total = int64_t(ltail[2]) + ltail[3];
+  FVX_ARG_CHECK(lrn_total < (int64_t(1) << 31) && par_total < (int64_t(1) << 31),
+                "local-expansion pair list too long");
   if (learned) {
     if ((rc = grow(T->lrn_leaf, 4 * size_t(lrn_total + 1))) ||
         (rc = grow(T->lrn_cell, 4 * size_t(lrn_total + 1))))
@@ -1480,10 +1689,28 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
     LL.cell = P<int>(T->lrn_cell);
     LL.cap = static_cast<int>(lrn_total);
   }
+  if (dual) {
+    if ((rc = grow(T->par_par, 4 * size_t(par_total + 1))) ||
+        (rc = grow(T->par_cell, 4 * size_t(par_total + 1))))
+      return rc;
+  }
   T->n_learned = static_cast<int>(lrn_total);
-  traverse_kernel<true><<<(nleaf + 127) / 128, 128, 0, s>>>(
-      V, near_off, far_off, nullptr, nullptr, P<int>(T->near_list), P<int>(T->far_list),
-      static_cast<int>(near_total), static_cast<int>(far_total), ovf, LL);
+  T->n_parent_pairs = static_cast<int>(par_total);
+  if (dual) {
+    D.near_idx = P<int>(T->near_list);
+    D.lrn_leaf = LL.leaf;
+    D.lrn_cell = LL.cell;
+    D.par_par = P<int>(T->par_par);
+    D.par_cell = P<int>(T->par_cell);
+    D.near_cap = static_cast<int>(near_total);
+    D.lrn_cap = static_cast<int>(lrn_total);
+    D.par_cap = static_cast<int>(par_total);
+    traverse_dual_kernel<true><<<(nleaf + 127) / 128, 128, 0, s>>>(V, D, ovf);
+  } else {
+    traverse_kernel<true><<<(nleaf + 127) / 128, 128, 0, s>>>(
+        V, near_off, far_off, nullptr, nullptr, P<int>(T->near_list), P<int>(T->far_list),
+        static_cast<int>(near_total), static_cast<int>(far_total), ovf, LL);
+  }
   FVX_LAUNCH_CHECK();
   // 7. evaluation
   EvalArgs A;
@@ -1505,60 +1732,99 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   A.out_a = out_a;
   A.out_b = out_b;
   A.leaf_local = nullptr;
-  if (learned && lrn_total > 0) {
-    if ((rc = grow(T->leaf_local, sizeof(float) * 32 * size_t(nleaf)))) return rc;
-    FVX_CUDA_TRY(cudaMemsetAsync(T->leaf_local.p, 0, sizeof(float) * 32 * size_t(nleaf), s));
+  A.parent_local = nullptr;
+  A.leaf_parent = leaf_parent;
+  const uint32_t* par_key = dual ? V.key + base[L - 1] : nullptr;
+  if (learned && lrn_total + par_total > 0) {
     if (!T->ev2) {
       FVX_CUDA_TRY(cudaEventCreate(&T->ev2));
       FVX_CUDA_TRY(cudaEventCreate(&T->ev3));
     }
     FVX_CUDA_TRY(cudaEventRecord(T->ev2, s));
-    // the analytic translation, then (learned) the network's residual
-    rc = m2l_farfield_launch(static_cast<int>(lrn_total), P<int>(T->lrn_leaf),
-                             P<int>(T->lrn_cell), leaves.key, rec, static_cast<float>(h),
-                             P<float>(T->leaf_local), s);
-    if (rc) return rc;
-    if (T->far_method == FVX_FAR_LEARNED)
-      rc = mlp_farfield_launch(static_cast<int>(lrn_total), P<int>(T->lrn_leaf),
-                               P<int>(T->lrn_cell), leaves.key, rec, static_cast<float>(h),
-                               T->mlp_W, T->mlp_b, P<float>(T->leaf_local), s);
-    if (rc) return rc;
-    FVX_CUDA_TRY(cudaEventRecord(T->ev3, s));
+    // the analytic translation, then (learned) the network's residual, for the
+    // leaves' own pairs and for the pairs shared through their parents
+    auto local_stage = [&](int npairs, const int* tgt, const int* cell, const uint32_t* tkey,
+                           float th, int ntgt, DevBuf& buf) -> int {
+      int r = grow(buf, sizeof(float) * 32 * size_t(ntgt));
+      if (r) return r;
+      FVX_CUDA_TRY(cudaMemsetAsync(buf.p, 0, sizeof(float) * 32 * size_t(ntgt), s));
+      if (npairs == 0) return FVX_OK;
+      r = m2l_farfield_launch(npairs, tgt, cell, tkey, rec, th, P<float>(buf), s);
+      if (r) return r;
+      if (T->far_method == FVX_FAR_LEARNED)
+        r = mlp_farfield_launch(npairs, tgt, cell, tkey, rec, th, T->mlp_W, T->mlp_b,
+                                P<float>(buf), s);
+      return r;
+    };
+    if ((rc = local_stage(static_cast<int>(lrn_total), P<int>(T->lrn_leaf), P<int>(T->lrn_cell),
+                          leaves.key, static_cast<float>(h), nleaf, T->leaf_local)))
+      return rc;
     A.leaf_local = P<float>(T->leaf_local);
+    if (dual) {
+      if ((rc = local_stage(static_cast<int>(par_total), P<int>(T->par_par), P<int>(T->par_cell),
+                            par_key, static_cast<float>(2.0 * h), npar, T->parent_local)))
+        return rc;
+      A.parent_local = P<float>(T->parent_local);
+    }
+    FVX_CUDA_TRY(cudaEventRecord(T->ev3, s));
   }
-  // validation sample: FP64 direct local expansions of evenly strided pairs
-  int val_k = 0, val_stride = 1;
-  if (learned && lrn_total > 0 && T->val_samples > 0) {
-    const int nl = static_cast<int>(lrn_total);
-    val_stride = nl > T->val_samples ? nl / T->val_samples : 1;
-    val_k = nl / val_stride < T->val_samples ? nl / val_stride : T->val_samples;
-    const size_t K = static_cast<size_t>(val_k);
+  // validation sample: FP64 direct local expansions of evenly strided pairs of
+  // each list (leaves' own pairs; parents' pairs), half of the samples each
+  int val_k = 0, val_k_par = 0;
+  const int64_t val_cap = T->val_samples;
+  if (learned && lrn_total + par_total > 0 && T->val_samples > 0) {
+    const size_t K = static_cast<size_t>(T->val_samples);
     if ((rc = grow(T->val_X, 2 * 48 * K)) || (rc = grow(T->val_T, 4 * 32 * K)) ||
         (rc = grow(T->val_A, 4 * 32 * K)) || (rc = grow(T->val_Y, 4 * 32 * K)) ||
         (rc = grow(T->val_scale, 4 * 4 * K)) || (rc = grow(T->val_err, 4 * K)) ||
-        (rc = grow(T->val_fb, 8 * K)) || (rc = grow(T->val_stats, 64)))
+        (rc = grow(T->val_fb, 8 * 2 * K)) || (rc = grow(T->val_stats, 64)))
       return rc;
     FVX_CUDA_TRY(cudaMemsetAsync(T->val_stats.p, 0, 64, s));
-    if ((rc = mlp_pair_targets_launch(val_k, val_stride, P<int>(T->lrn_leaf), P<int>(T->lrn_cell),
-                                      leaves.key, rec, lvb, lvb + total_cells, sp, sa, cid,
-                                      static_cast<float>(h), T->val_X.p, P<float>(T->val_T),
-                                      P<float>(T->val_A), P<float>(T->val_scale), s)))
+    auto validate = [&](int nlist, int samples, const int* tgt, const int* cell,
+                        const uint32_t* tkey, float th, float* local, int2* fb, int* nfb,
+                        int* k_out) -> int {
+      *k_out = 0;
+      if (nlist <= 0 || samples <= 0) return FVX_OK;
+      const int stride = nlist > samples ? nlist / samples : 1;
+      const int k = nlist / stride < samples ? nlist / stride : samples;
+      // slices: about eight CTAs per SM over the k sums
+      const int slices = max(1, min(64, 8 * device_sm_count() / k));
+      int r = grow(T->pair_partial, sizeof(double) * 30 * size_t(k) * slices);
+      if (r) return r;
+      r = mlp_pair_targets_launch(k, stride, tgt, cell, tkey, th, leaves.key, rec, lvb,
+                                  lvb + total_cells, sp, sa, cid, static_cast<float>(h),
+                                  T->val_X.p, P<float>(T->val_T), P<float>(T->val_A),
+                                  P<float>(T->val_scale), P<double>(T->pair_partial), slices, s);
+      if (r) return r;
+      const float* Y = nullptr;
+      if (T->far_method == FVX_FAR_LEARNED) {
+        if ((r = fvx_mlp_forward(T->val_X.p, k, T->mlp_W, T->mlp_b, P<float>(T->val_Y),
+                                 nullptr, nullptr, s)))
+          return r;
+        Y = P<float>(T->val_Y);
+      }
+      validate_kernel<<<(k + 127) / 128, 128, 0, s>>>(
+          k, stride, tgt, cell, P<float>(T->val_T), P<float>(T->val_A), Y,
+          P<float>(T->val_scale), static_cast<float>(T->val_tol), local, fb, nfb,
+          P<float>(T->val_stats), P<float>(T->val_err));
+      FVX_LAUNCH_CHECK();
+      *k_out = k;
+      return FVX_OK;
+    };
+    const int k_leaf = dual && par_total > 0 ? (T->val_samples + 1) / 2 : T->val_samples;
+    if ((rc = validate(static_cast<int>(lrn_total), k_leaf, P<int>(T->lrn_leaf),
+                       P<int>(T->lrn_cell), leaves.key, static_cast<float>(h),
+                       P<float>(T->leaf_local), P<int2>(T->val_fb), P<int>(T->val_stats) + 4,
+                       &val_k)))
       return rc;
-    const float* Y = nullptr;
-    if (T->far_method == FVX_FAR_LEARNED) {
-      if ((rc = fvx_mlp_forward(T->val_X.p, val_k, T->mlp_W, T->mlp_b, P<float>(T->val_Y),
-                                nullptr, nullptr, s)))
-        return rc;
-      Y = P<float>(T->val_Y);
-    }
-    validate_kernel<<<(val_k + 127) / 128, 128, 0, s>>>(
-        val_k, val_stride, P<int>(T->lrn_leaf), P<int>(T->lrn_cell), P<float>(T->val_T),
-        P<float>(T->val_A), Y, P<float>(T->val_scale), static_cast<float>(T->val_tol),
-        P<float>(T->leaf_local), P<int2>(T->val_fb), P<int>(T->val_stats) + 4,
-        P<float>(T->val_stats), P<float>(T->val_err));
-    FVX_LAUNCH_CHECK();
+    if (dual &&
+        (rc = validate(static_cast<int>(par_total), T->val_samples - k_leaf, P<int>(T->par_par),
+                       P<int>(T->par_cell), par_key, static_cast<float>(2.0 * h),
+                       P<float>(T->parent_local), P<int2>(T->val_fb) + val_cap,
+                       P<int>(T->val_stats) + 5, &val_k_par)))
+      return rc;
   }
-  T->last_val_k = val_k;
+  T->last_val_k = val_k + val_k_par;
   T->last_L = L;
   T->last_nleaf = nleaf;
   T->last_h = h;
@@ -1577,28 +1843,35 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
     launch_eval<FVX_KERNEL_GAUSSIANERF>(mode, nleaf, n, A, s);
   FVX_LAUNCH_CHECK();
   FVX_CUDA_TRY(cudaEventRecord(T->ev1, s));
-  if (val_k > 0) {
-    // queued pairs are at most val_k (few in practice): slice every cell so
-    // that all of them together span about four CTAs per SM
-    const int slices = max(1, min(64, 4 * device_sm_count() / max(1, val_k / 16)));
-    const dim3 fgrid(val_k, slices);
+  // FP64 direct sums of the queued clusters at every target of their leaf / parent
+  auto fallback = [&](int k, const int2* fb, const int* nfb, const int* tstart,
+                      const int* tcount) {
+    if (k <= 0) return;
+    // queued pairs are at most k (few in practice): slice every cell so that
+    // all of them together span about four CTAs per SM
+    const int slices = max(1, min(64, 4 * device_sm_count() / max(1, k / 16)));
+    const dim3 fgrid(k, slices);
     if (kernel == FVX_KERNEL_WINCKELMANS)
-      launch_fallback<FVX_KERNEL_WINCKELMANS>(
-          mode, fgrid, P<int2>(T->val_fb), P<int>(T->val_stats) + 4, A.leaf_start, A.leaf_count,
-          lvb, lvb + total_cells, perm, pos, alpha, sigma, tgt_gamma, out_a, out_b, s);
+      launch_fallback<FVX_KERNEL_WINCKELMANS>(mode, fgrid, fb, nfb, tstart, tcount, lvb,
+                                              lvb + total_cells, perm, pos, alpha, sigma,
+                                              tgt_gamma, out_a, out_b, s);
     else
-      launch_fallback<FVX_KERNEL_GAUSSIANERF>(
-          mode, fgrid, P<int2>(T->val_fb), P<int>(T->val_stats) + 4, A.leaf_start, A.leaf_count,
-          lvb, lvb + total_cells, perm, pos, alpha, sigma, tgt_gamma, out_a, out_b, s);
-    FVX_LAUNCH_CHECK();
-  }
+      launch_fallback<FVX_KERNEL_GAUSSIANERF>(mode, fgrid, fb, nfb, tstart, tcount, lvb,
+                                              lvb + total_cells, perm, pos, alpha, sigma,
+                                              tgt_gamma, out_a, out_b, s);
+  };
+  fallback(val_k, P<int2>(T->val_fb), P<int>(T->val_stats) + 4, A.leaf_start, A.leaf_count);
+  if (dual)
+    fallback(val_k_par, P<int2>(T->val_fb) + val_cap, P<int>(T->val_stats) + 5,
+             V.start + base[L - 1], V.count + base[L - 1]);
+  FVX_LAUNCH_CHECK();
   unsigned ovf_h[6] = {0, 0, 0, 0, 0, 0};
   FVX_CUDA_TRY(cudaMemcpyAsync(ovf_h, ovf, 24, cudaMemcpyDeviceToHost, s));
   T->stats[0] = L;
   T->stats[1] = nleaf;
   T->stats[2] = near_total;
   T->stats[3] = far_total;
-  T->stats[4] = lrn_total;
+  T->stats[4] = lrn_total + par_total;
   if (stats) {
     FVX_CUDA_TRY(cudaStreamSynchronize(s));
     unsigned long long work[2];
@@ -1634,7 +1907,9 @@ void fvx_tree_destroy(fvx_tree* T) {
                          &T->rec,     &T->sp,       &T->sa,       &T->sg,       &T->lists_meta,
                          &T->near_list, &T->far_list, &T->bbox,   &T->lrn_meta, &T->lrn_leaf,
                          &T->lrn_cell, &T->leaf_local, &T->val_X, &T->val_T, &T->val_A,
-                         &T->val_Y, &T->val_scale, &T->val_err, &T->val_fb, &T->val_stats};
+                         &T->val_Y, &T->val_scale, &T->val_err, &T->val_fb, &T->val_stats,
+                         &T->dual_meta, &T->par_par, &T->par_cell, &T->parent_local,
+                         &T->pair_partial};
   for (auto* b : bufs)
     if (b->p) cudaFree(b->p);
   delete T;
@@ -1677,11 +1952,11 @@ int fvx_tree_last_validation(fvx_tree* T, double* out) {
   for (int k = 0; k < 4; ++k) out[k] = 0.0;
   if (T->last_val_k <= 0) return FVX_OK;
   float v[4];
-  int nfb = 0;
+  int nfb[2] = {0, 0};
   FVX_CUDA_TRY(cudaMemcpy(v, T->val_stats.p, 16, cudaMemcpyDeviceToHost));
-  FVX_CUDA_TRY(cudaMemcpy(&nfb, fvx::P<int>(T->val_stats) + 4, 4, cudaMemcpyDeviceToHost));
+  FVX_CUDA_TRY(cudaMemcpy(nfb, fvx::P<int>(T->val_stats) + 4, 8, cudaMemcpyDeviceToHost));
   out[0] = v[0];
-  out[1] = nfb;
+  out[1] = nfb[0] + nfb[1];
   out[2] = v[0] > 0.f ? v[1] / v[0] : 0.0;
   out[3] = v[2];
   return FVX_OK;
@@ -1705,11 +1980,14 @@ int fvx_tree_sample_pairs(fvx_tree* T, int max_pairs, void* X, float* Tgt, float
   if (n <= 0) return FVX_OK;
   const int stride = n > max_pairs ? n / max_pairs : 1;
   const int np = n / stride < max_pairs ? n / stride : max_pairs;
-  int rc = fvx::mlp_pair_targets_launch(
+  const int slices = np < 4096 ? 8 : (np < 32768 ? 4 : 2);
+  int rc = fvx::grow(T->pair_partial, sizeof(double) * 30 * size_t(np) * slices);
+  if (rc) return rc;
+  rc = fvx::mlp_pair_targets_launch(
       np, stride, fvx::P<int>(T->lrn_leaf), fvx::P<int>(T->lrn_cell), T->last_leaf_key,
-      fvx::P<float>(T->rec), T->last_cell_start, T->last_cell_count, fvx::P<float4>(T->sp),
+      static_cast<float>(T->last_h), T->last_leaf_key, fvx::P<float>(T->rec), T->last_cell_start, T->last_cell_count, fvx::P<float4>(T->sp),
       fvx::P<float4>(T->sa), T->last_cid, static_cast<float>(T->last_h), X, Tgt, A, nullptr,
-      static_cast<cudaStream_t>(stream));
+      fvx::P<double>(T->pair_partial), slices, static_cast<cudaStream_t>(stream));
   if (rc) return rc;
   *n_out = np;
   return FVX_OK;
