@@ -429,38 +429,61 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
       ok = false;
       break;
     }
-    for (int c0 = 0; c0 < OUT; c0 += 16) {
-      float v[16];
-      tc::tmem_ld16(tmem + lane_base + c0, v);
-      if constexpr (FAR) {
-        // pairs are ordered by leaf: reduce each run of equal leaves inside
-        // the warp to its first lane, which adds it to the leaf's expansion
-        const int lane = threadIdx.x & 31;
-        const int my = act_row ? leaf : -1 - lane;
+    if constexpr (FAR) {
+      // the learned residual of this row, back to physical units (the analytic
+      // translation is added by its own kernel)
+      float x[OUT];
+      for (int c0 = 0; c0 < OUT; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tmem + lane_base + c0, v);
+        const float* ax = S.aux[grp][lt];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int c = c0 + i;
+          const float sc = c < 3 ? ax[0] : (c < 12 ? ax[1] : ax[2]);
+          x[c] = (act_row && c < NOUT) ? (v[i] + S.bias[B4o + c]) * sc : 0.f;
+        }
+      }
+      const int lane = threadIdx.x & 31;
+      const int my = act_row ? leaf : -1 - lane;
+      if (__all_sync(0xffffffffu, my == __shfl_sync(0xffffffffu, my, 0))) {
+        // one target for the whole warp (pairs are ordered by target, runs are
+        // long): reduce-scatter by recursive halving, 31 shuffles for the 32
+        // columns; lane c ends with the warp's sum of column c
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+          const bool upper = (lane & off) != 0;
+#pragma unroll
+          for (int j = 0; j < off; ++j) {
+            const float send = upper ? x[j] : x[j + off];
+            const float keep = upper ? x[j + off] : x[j];
+            x[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+          }
+        }
+        if (lane < NOUT) atomicAdd(A.f.leaf_local + static_cast<int64_t>(leaf) * OUT + lane, x[0]);
+      } else {
+        // runs of equal targets inside the warp: segmented sums to each run's
+        // first lane, which adds them to the target's expansion
         const int up = __shfl_up_sync(0xffffffffu, my, 1);
         const bool head = act_row && (lane == 0 || up != my);
         float* L = act_row ? A.f.leaf_local + static_cast<int64_t>(leaf) * OUT : nullptr;
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int c = c0 + i;
-          float x = 0.f;
-          if (act_row && c < NOUT) {
-            // the learned residual, back to physical units (the analytic
-            // translation is added by its own kernel)
-            const float* ax = S.aux[grp][lt];
-            const float s = c < 3 ? ax[0] : (c < 12 ? ax[1] : ax[2]);
-            x = (v[i] + S.bias[B4o + c]) * s;
-          }
+        for (int c = 0; c < NOUT; ++c) {
+          float y = x[c];
 #pragma unroll
           for (int off = 1; off < 32; off <<= 1) {
-            const float o = __shfl_down_sync(0xffffffffu, x, off);
+            const float o = __shfl_down_sync(0xffffffffu, y, off);
             const int ol = __shfl_down_sync(0xffffffffu, my, off);
-            if (lane + off < 32 && ol == my) x += o;
+            if (lane + off < 32 && ol == my) y += o;
           }
-          if (head && c < NOUT) atomicAdd(L + c, x);
+          if (head) atomicAdd(L + c, y);
         }
-        continue;
       }
+    }
+    for (int c0 = 0; c0 < OUT && !FAR; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(tmem + lane_base + c0, v);
+      if constexpr (FAR) continue;
       if (!act_row) continue;
       {
         float4* y = reinterpret_cast<float4*>(A.r.Y + static_cast<int64_t>(row) * OUT + c0);

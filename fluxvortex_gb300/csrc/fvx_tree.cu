@@ -874,8 +874,8 @@ __device__ __forceinline__ uint64_t fma(uint64_t a, uint64_t b, uint64_t c) {
 
 // One source per row of the packed near tile, every value duplicated into
 // both halves of a 64-bit pair: {-x, -y}, {-z, s2}, {k2, ax}, {ay, az},
-// {-ax, -ay}, {-az, 10.5 s2} (the negated strengths turn each cross-product
-// component into two fused multiply-adds).
+// {-ax, -ay}, {-az, -10.5 s2} (the negated values turn each cross-product
+// and stretching component into two fused multiply-adds).
 struct NearX2 {
   ulonglong2 q[6];
 };
@@ -887,7 +887,7 @@ template <int MODE>
 __device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, int nt, uint64_t TX,
                                              uint64_t TY, uint64_t TZ, uint64_t GX, uint64_t GY,
                                              uint64_t GZ, uint64_t* acc) {
-  const uint64_t C3 = x2::pack(3.f, 3.f);
+  const uint64_t CM3 = x2::pack(-3.f, -3.f);
   for (int k = 0; k < nt; ++k) {
     const ulonglong2 q0 = tile[k].q[0], q1 = tile[k].q[1], q2 = tile[k].q[2],
                      q3 = tile[k].q[3];
@@ -909,14 +909,14 @@ __device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, in
       acc[1] = x2::fma(EX, NAZ, x2::fma(EZ, AX, acc[1]));
       acc[2] = x2::fma(EY, NAX, x2::fma(EX, AY, acc[2]));
     } else {
-      // S += (f G + fpr (d . G) d) x a, fpr = -(3 r2 + 10.5 s2) t^7
+      // S += (f G + w d) x a, w = fpr (d . G), fpr = -(3 r2 + 10.5 s2) t^7
       uint64_t DG = x2::mul(DX, GX);
       DG = x2::fma(DY, GY, DG);
       DG = x2::fma(DZ, GZ, DG);
-      const uint64_t W = x2::mul(x2::mul(x2::fma(R2, C3, q5.y), x2::mul(T5, T2)), DG);
-      const uint64_t VX = x2::sub(x2::mul(F, GX), x2::mul(W, DX));
-      const uint64_t VY = x2::sub(x2::mul(F, GY), x2::mul(W, DY));
-      const uint64_t VZ = x2::sub(x2::mul(F, GZ), x2::mul(W, DZ));
+      const uint64_t W = x2::mul(x2::mul(x2::fma(R2, CM3, q5.y), x2::mul(T5, T2)), DG);
+      const uint64_t VX = x2::fma(W, DX, x2::mul(F, GX));
+      const uint64_t VY = x2::fma(W, DY, x2::mul(F, GY));
+      const uint64_t VZ = x2::fma(W, DZ, x2::mul(F, GZ));
       acc[0] = x2::fma(VZ, NAY, x2::fma(VY, AZ, acc[0]));
       acc[1] = x2::fma(VX, NAZ, x2::fma(VZ, AX, acc[1]));
       acc[2] = x2::fma(VY, NAX, x2::fma(VX, AY, acc[2]));
@@ -1001,7 +1001,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
             e.q[2] = make_ulonglong2(x2::pack(av.w, av.w), x2::pack(av.x, av.x));
             e.q[3] = make_ulonglong2(x2::pack(av.y, av.y), x2::pack(av.z, av.z));
             e.q[4] = make_ulonglong2(x2::pack(-av.x, -av.x), x2::pack(-av.y, -av.y));
-            e.q[5] = make_ulonglong2(x2::pack(-av.z, -av.z), x2::pack(10.5f * pv.w, 10.5f * pv.w));
+            e.q[5] = make_ulonglong2(x2::pack(-av.z, -av.z), x2::pack(-10.5f * pv.w, -10.5f * pv.w));
             s_x2[k] = e;
           }
           __syncthreads();
