@@ -26,6 +26,10 @@ Algorithm (shared with the device code through fluxvortex_gb300.tree_params):
      quadrupole expansion of the vector potential Psi_m = (1/4pi) sum a_m / |x - x_s|
      (singular kernel; the cores are negligible beyond the acceptance
      distance): u = curl Psi, J_in = eps_ijm d_n d_j Psi_m.
+  7. ``dual_lists``: the two-level lists of the local-expansion far field
+     (cells shared by a parent's leaves, each leaf's own cells, near leaves),
+     whose partition of the sources is tested here and whose counts pin the
+     device traversal.
 """
 from __future__ import annotations
 
@@ -176,3 +180,68 @@ def evaluate(tree, pos, alpha, sigma, tgt_gamma=None, kernel="winckelmans"):
             u[perm[s:e]] += du
             J[perm[s:e]] += dJ
     return u, J
+
+
+def dual_lists(tree):
+    """Two-level interaction lists of the local-expansion far field.
+
+    For each leaf T with parent P (level L-1): source cells A are visited depth
+    first from the roots; A passing the acceptance test against P goes to P's
+    list (recorded by P's first child only); a failing A larger than P is
+    accepted by T when it passes against the octant of P nearest to it (so all
+    of P's children decide alike), else opened; a failing A of P's size or a
+    leaf is tested against T: accepted (T's list), or near if a leaf, or its
+    children (leaves) are each accepted or near.  The test on a pair of cells
+    of sizes h_1, h_2 is |dc|^2 > 3/4 (h_1 + h_2)^2 / theta^2.
+    Returns (near, leaf_far, parent_far): per leaf lists of leaf ids and of
+    (level, cell), and per parent a list of (level, cell)."""
+    L, theta = tree["L"], tree["theta"]
+    k = 0.75 / (theta * theta)
+    levels = tree["levels"]
+    leaves, parents = levels[L], levels[L - 1]
+    h = leaves["h"]
+    near, leaf_far = [], []
+    parent_far = [[] for _ in range(len(parents["start"]))]
+    pkeys = parents["key"]
+    for t in range(len(leaves["start"])):
+        kT = leaves["key"][t]
+        p = int(np.searchsorted(pkeys, kT >> 3))
+        first = parents["child_lo"][p] == t
+        cT, cP = leaves["center"][t], parents["center"][p]
+        nr, lf = [], []
+
+        def accept_t(l, c):
+            lev = levels[l]
+            d2 = ((cT - lev["center"][c]) ** 2).sum()
+            if d2 > k * (h + lev["h"]) ** 2:
+                lf.append((l, c))
+                return True
+            if l == L:
+                nr.append(c)
+                return True
+            return False
+
+        stack = [(0, c) for c in range(len(levels[0]["start"]) - 1, -1, -1)]
+        while stack:
+            l, c = stack.pop()
+            lev = levels[l]
+            dc = cP - lev["center"][c]
+            if (dc ** 2).sum() > k * (2 * h + lev["h"]) ** 2:
+                if first:
+                    parent_far[p].append((l, c))
+                continue
+            if l < L - 1:
+                near_oct = np.maximum(np.abs(dc) - 0.5 * h, 0.0)
+                if (near_oct ** 2).sum() > k * (h + lev["h"]) ** 2:
+                    accept_t(l, c)
+                    continue
+                for ch in range(lev["child_hi"][c] - 1, lev["child_lo"][c] - 1, -1):
+                    stack.append((l + 1, ch))
+                continue
+            if accept_t(l, c):
+                continue
+            for q in range(lev["child_lo"][c], lev["child_hi"][c]):
+                accept_t(L, q)
+        near.append(nr)
+        leaf_far.append(lf)
+    return near, leaf_far, parent_far

@@ -111,3 +111,24 @@ def test_learned_gain_over_analytic_translation(cuda):
     assert torch.isfinite(Y).all()
     assert med_le <= 1.05 * med_an and p90_le <= 1.05 * p90_an
     assert "val_analytic_median" in mlp.meta and "val_median" in mlp.meta
+
+
+def test_two_level_lists_match_oracle(cuda):
+    """The device's two-level traversal makes the oracle's lists (counts of near
+    leaves and of leaf- and parent-level local-expansion pairs)."""
+    from fluxvortex_gb300 import _capi
+    from fluxvortex_gb300.tree import TreeSweeper
+    from oracle import treecode as TC
+    n = 4000
+    pos, alpha, sigma = _slab(n, 81, box=(6.0, 3.0, 0.5))
+    P, G, S = _dev(pos), _dev(alpha), _dev(sigma)
+    ts = TreeSweeper(theta=0.5, leaf_target=16)
+    ts.set_far_field("m2l")
+    ts.set_validation(0, 0.05)
+    _, stats = _sweep(ts, _capi.PAIR_VELOCITY, P, G, S, n)
+    tree = TC.build(pos, theta=0.5, leaf_target=16)
+    near, leaf_far, parent_far = TC.dual_lists(tree)
+    assert int(stats[2]) == sum(len(x) for x in near)
+    assert int(stats[3]) == 0
+    assert int(stats[4]) == sum(len(x) for x in leaf_far) + sum(len(x) for x in parent_far)
+    assert _capi.status_read_and_clear() == 0

@@ -152,3 +152,25 @@ def test_m2l_from_features_matches_moments():
     np.testing.assert_allclose(got[0:3] * s2, ref[0:3], rtol=1e-10, atol=1e-14)
     np.testing.assert_allclose(got[3:12] * s3, ref[3:12], rtol=1e-10, atol=1e-14)
     np.testing.assert_allclose(got[12:30] * s4, ref[12:30], rtol=1e-10, atol=1e-14)
+
+
+def test_dual_lists_partition_every_source_once():
+    """The two-level lists reach every source particle from every target leaf
+    exactly once (parent expansion, own expansion or near list)."""
+    rng = np.random.default_rng(9)
+    n = 4000
+    pos = rng.uniform([0, 0, 0], [6.0, 3.0, 0.5], (n, 3))
+    tree = TC.build(pos, theta=0.5, leaf_target=16)
+    L = tree["L"]
+    near, leaf_far, parent_far = TC.dual_lists(tree)
+    levels = tree["levels"]
+    leaves, parents = levels[L], levels[L - 1]
+    assert sum(len(x) for x in parent_far) > 0 and sum(len(x) for x in leaf_far) > 0
+    for t in range(len(leaves["start"])):
+        p = int(np.searchsorted(parents["key"], leaves["key"][t] >> 3))
+        cover = np.zeros(n, dtype=np.int64)
+        for c in near[t]:
+            cover[leaves["start"][c]:leaves["end"][c]] += 1
+        for (l, c) in leaf_far[t] + parent_far[p]:
+            cover[levels[l]["start"][c]:levels[l]["end"][c]] += 1
+        assert np.all(cover == 1), t
