@@ -1343,7 +1343,7 @@ struct fvx_tree {
   cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // around the local-expansion stage
   // per-sweep validation of the local-expansion path and its FP64 fallback
   int val_samples = 256;
-  double val_tol = 0.05;
+  double val_tol = 0.1;
   fvx::DevBuf val_X, val_T, val_A, val_Y, val_scale, val_err, val_fb, val_stats;
   int last_val_k = 0;
   // two-level traversal: per-parent lists and expansions

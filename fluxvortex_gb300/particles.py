@@ -64,7 +64,7 @@ class VortexParticleField:
         # checked on the step's first velocity sweep and the expansion error
         # above which a checked cluster is summed directly in FP64 instead
         self.validate_samples = 256
-        self.validate_tol = 0.05
+        self.validate_tol = 0.1
         self._validate_next = False
         if far_field in ("tree", "m2p", "m2l", "learned"):
             from .tree import TreeSweeper

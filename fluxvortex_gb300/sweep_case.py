@@ -34,7 +34,7 @@ def main(argv=None):
         from .learned import FarFieldMLP
         mlp = FarFieldMLP.load()
     ts.set_far_field(a.far_field, mlp=mlp)
-    ts.set_validation(0, 0.05)
+    ts.set_validation(0, 0.1)
     out = torch.empty((a.n, 3), dtype=torch.float64, device="cuda")
     ts.sweep(_capi.PAIR_VELOCITY, "winckelmans", P, G, S, a.n, out)
     ts.sweep(_capi.PAIR_STRETCH, "winckelmans", P, G, S, a.n, out, tgt_gamma=G)

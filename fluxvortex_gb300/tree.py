@@ -79,7 +79,7 @@ class TreeSweeper:
         self.far_method = method
         self.theta_local = th
 
-    def set_validation(self, samples=256, tol=0.05):
+    def set_validation(self, samples=256, tol=0.1):
         """Per-sweep FP64 validation of the local-expansion path: ``samples``
         strided (leaf, cell) pairs per sweep; a pair whose expansion error
         exceeds ``tol`` is summed directly in FP64 instead (samples=0: off)."""

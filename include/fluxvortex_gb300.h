@@ -227,7 +227,7 @@ int fvx_tree_set_far_field(fvx_tree* tree, int method, const void* W, const floa
                            double theta_local);
 int fvx_tree_last_local_ms(fvx_tree* tree, float* ms);
 /* Per-sweep validation of the local-expansion path (on by default: 256
- * samples, tol 0.05).  Every sweep with FVX_FAR_M2L or FVX_FAR_LEARNED sums
+ * samples, tol 0.1).  Every sweep with FVX_FAR_M2L or FVX_FAR_LEARNED sums
  * `samples` evenly strided (leaf, cell) pairs of its list directly in FP64 at
  * the leaf centre and compares their expansions with it; the error is that
  * of the expansion across the leaf, e = (|du| + rho |dJ| + rho^2/2 |dH|) /
