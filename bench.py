@@ -85,7 +85,9 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--n", type=int, default=1 << 20, help="particles")
+    p.add_argument("--particles", "--n", dest="n", type=int, default=1 << 20,
+                   help="particles (spell it --particles under torchrun, whose own options "
+                        "share the --n prefix)")
     p.add_argument("--precision", default="f32c", choices=["f32c", "f64"])
     p.add_argument("--far-field", default="learned",
                    choices=["direct", "tree", "m2p", "m2l", "learned"],
@@ -290,6 +292,16 @@ def flutter_sweep_measure(args):
     return out
 
 
+def max_over_ranks(value, world, device=None):
+    """The largest of every rank's value (the job's time is its slowest rank's)."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -374,10 +386,7 @@ def run_ours(args, rank, world):
     events = step.field.sweep_events
     step.field.sweep_events = None
     ms = sum(step_ms) / len(step_ms)
-    t = torch.tensor([ms], dtype=torch.float64, device=device)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = max_over_ranks(ms, world, device)
     value = world * 1e3 / ms_max
 
     # per-kind sweep durations inside the timed steps
@@ -526,13 +535,10 @@ def run_ours(args, rank, world):
             hc[1:2].copy_(step.hs._cdi[kk:kk + 1], non_blocking=True)
         e.record()
         torch.cuda.synchronize()
-        e2e_ms = s.elapsed_time(e) / e2e_steps
-        t = torch.tensor([e2e_ms], dtype=torch.float64, device=device)
-        if world > 1:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = max_over_ranks(s.elapsed_time(e) / e2e_steps, world, device)
         h2d = n * (3 + 3 + 1) * 8
         d2h = n * (3 + 3 + 1) * 8 + 2 * 8
-        result["e2e"] = {"value": world * 1e3 / float(t.item()), "unit": UNIT,
+        result["e2e"] = {"value": world * 1e3 / e2e_ms, "unit": UNIT,
                          "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     if rank == 0:
