@@ -8,8 +8,9 @@
 //   chord rings, 3/4-chord collocation points, normals, areas, bound legs);
 //   AIC[i][j] = (unit ring j at collocation i) . n_i; wake ring rows and the
 //   particle wake induced at the 2P points (collocation + bound-leg centres),
-//   particles in FP64 or FP32 with compensated sums (staged through shared
-//   memory, split over thread slices, slices reduced in fixed order); the
+//   in FP64 or -- mixed precision -- in FP32 on FP64 offsets with compensated
+//   particle sums (particles staged through shared memory, split over thread
+//   slices, slices reduced in fixed order); the
 //   right-hand side; an in-place LU solve with partial pivoting (first
 //   largest pivot, as LAPACK's getrf); Kutta-Joukowski forces on the bound
 //   legs with the full induced velocity and the unsteady term; station lift
@@ -140,6 +141,41 @@ __device__ void build_lattice(Smem& S, const FlutterParams& p) {
   }
 }
 
+// One wake ring at point p in FP32 on offsets taken in FP64 (the ring-vortex
+// formula and skip tests of seg::vortex_velocity, ring leg set).
+__device__ __forceinline__ void ring_velocity_f32(const seg::VortexRec& R, double px, double py,
+                                                  double pz, float& vx, float& vy, float& vz) {
+  float dx[4], dy[4], dz[4], len[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    dx[c] = static_cast<float>(R.c[c][0] - px);
+    dy[c] = static_cast<float>(R.c[c][1] - py);
+    dz[c] = static_cast<float>(R.c[c][2] - pz);
+    len[c] = sqrtf(dx[c] * dx[c] + dy[c] * dy[c] + dz[c] * dz[c]);
+  }
+  const float c1 = static_cast<float>(R.c1);
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    const int a = l, b = (l + 1) & 3;
+    if (!((R.valid >> l) & 1)) continue;
+    const float tol = static_cast<float>(R.tol[l]);
+    if (len[a] < tol || len[b] < tol) continue;
+    const float r3x = dy[a] * dz[b] - dz[a] * dy[b];
+    const float r3y = dz[a] * dx[b] - dx[a] * dz[b];
+    const float r3z = dx[a] * dy[b] - dy[a] * dx[b];
+    const float r3_sq = r3x * r3x + r3y * r3y + r3z * r3z;
+    const float r1r2 = len[a] * len[b];
+    const float thr = 1.0e-10f * r1r2;
+    if (r3_sq < 2.f * thr * thr && sqrtf(r3_sq) < thr) continue;
+    const float c3 = dx[a] * dx[b] + dy[a] * dy[b] + dz[a] * dz[b];
+    const float c4 = c1 * (len[a] + len[b]) * (r1r2 - c3) /
+                     (r1r2 * (r3_sq + static_cast<float>(R.c2[l])));
+    vx += c4 * r3x;
+    vy += c4 * r3y;
+    vz += c4 * r3z;
+  }
+}
+
 // Induced velocity of the wake rings and particles at the 2P points
 // (collocation points, then bound-leg centres) into S.Vind.
 template <bool F32>
@@ -159,9 +195,19 @@ __device__ void wake_induction(Smem& S, const FlutterParams& p, const FlutterSta
   // wake rings: slice sl takes rings sl, sl + slices, ...
   double vx = 0.0, vy = 0.0, vz = 0.0;
   int cnt[4] = {0, 0, 0, 0};
-  if (active)
-    for (int r = sl; r < R * p.ns; r += slices)
-      seg::vortex_velocity<FVX_LEGS_RING>(S.wake[r], px, py, pz, vx, vy, vz, cnt);
+  if (active) {
+    if constexpr (F32) {
+      float fx = 0.f, fy = 0.f, fz = 0.f;
+      for (int r = sl; r < R * p.ns; r += slices)
+        ring_velocity_f32(S.wake[r], px, py, pz, fx, fy, fz);
+      vx = fx;
+      vy = fy;
+      vz = fz;
+    } else {
+      for (int r = sl; r < R * p.ns; r += slices)
+        seg::vortex_velocity<FVX_LEGS_RING>(S.wake[r], px, py, pz, vx, vy, vz, cnt);
+    }
+  }
   // particles, staged in tiles, oldest first
   const int Pm = p.max_particles;
   const double* pp = st.ppos + static_cast<int64_t>(env) * Pm * 3;
