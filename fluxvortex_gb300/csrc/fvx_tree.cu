@@ -1356,6 +1356,7 @@ struct fvx_tree {
   int last_L = 0, last_nleaf = 0;
   double last_h = 0.0;
   const uint32_t* last_leaf_key = nullptr;
+  const uint32_t* last_par_key = nullptr;  // level L-1 keys (two-level lists)
   const int* last_cell_start = nullptr;
   const int* last_cell_count = nullptr;
   const int* last_cid = nullptr;
@@ -1829,6 +1830,7 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   T->last_nleaf = nleaf;
   T->last_h = h;
   T->last_leaf_key = leaves.key;
+  T->last_par_key = par_key;
   T->last_cell_start = lvb;
   T->last_cell_count = lvb + total_cells;
   T->last_cid = cid;
@@ -1971,22 +1973,27 @@ int fvx_tree_last_local_ms(fvx_tree* T, float* ms) {
   return FVX_OK;
 }
 
-int fvx_tree_sample_pairs(fvx_tree* T, int max_pairs, void* X, float* Tgt, float* A, int* n_out,
-                          void* stream) {
+int fvx_tree_sample_pairs(fvx_tree* T, int list, int max_pairs, void* X, float* Tgt, float* A,
+                          int* n_out, void* stream) {
   FVX_ARG_CHECK(T && X && Tgt && n_out && max_pairs > 0, "bad arguments");
+  FVX_ARG_CHECK(list == 0 || list == 1, "list is 0 (leaf pairs) or 1 (parent pairs)");
   *n_out = 0;
   FVX_ARG_CHECK(T->theta_l > 0.0, "sampling needs the local-expansion path on the last sweep");
-  const int n = T->n_learned;
+  const int n = list == 0 ? T->n_learned : T->n_parent_pairs;
   if (n <= 0) return FVX_OK;
   const int stride = n > max_pairs ? n / max_pairs : 1;
   const int np = n / stride < max_pairs ? n / stride : max_pairs;
   const int slices = np < 4096 ? 8 : (np < 32768 ? 4 : 2);
   int rc = fvx::grow(T->pair_partial, sizeof(double) * 30 * size_t(np) * slices);
   if (rc) return rc;
+  const int* tgt = list == 0 ? fvx::P<int>(T->lrn_leaf) : fvx::P<int>(T->par_par);
+  const int* cell = list == 0 ? fvx::P<int>(T->lrn_cell) : fvx::P<int>(T->par_cell);
+  const uint32_t* tkey = list == 0 ? T->last_leaf_key : T->last_par_key;
+  const float th = static_cast<float>(list == 0 ? T->last_h : 2.0 * T->last_h);
   rc = fvx::mlp_pair_targets_launch(
-      np, stride, fvx::P<int>(T->lrn_leaf), fvx::P<int>(T->lrn_cell), T->last_leaf_key,
-      static_cast<float>(T->last_h), T->last_leaf_key, fvx::P<float>(T->rec), T->last_cell_start, T->last_cell_count, fvx::P<float4>(T->sp),
-      fvx::P<float4>(T->sa), T->last_cid, static_cast<float>(T->last_h), X, Tgt, A, nullptr,
+      np, stride, tgt, cell, tkey, th, T->last_leaf_key, fvx::P<float>(T->rec),
+      T->last_cell_start, T->last_cell_count, fvx::P<float4>(T->sp), fvx::P<float4>(T->sa),
+      T->last_cid, static_cast<float>(T->last_h), X, Tgt, A, nullptr,
       fvx::P<double>(T->pair_partial), slices, static_cast<cudaStream_t>(stream));
   if (rc) return rc;
   *n_out = np;

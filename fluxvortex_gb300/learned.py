@@ -234,7 +234,7 @@ def analytic_errors(T, A):
 
 
 def harvest(sweeper, field_pos, field_gamma, field_sigma, n, max_pairs, theta_local=None,
-            kernel="winckelmans"):
+            kernel="winckelmans", parent_share=0.5):
     """Training pairs from one particle field: a velocity sweep on the analytic
     local-expansion path lists the pairs (theta_local defaults to the sweeper's
     theta, i.e. every accepted cell), then up to max_pairs of them are sampled
@@ -244,5 +244,11 @@ def harvest(sweeper, field_pos, field_gamma, field_sigma, n, max_pairs, theta_lo
     out = torch.empty((n, 3), dtype=torch.float64, device=field_pos.device)
     sweeper.sweep(_capi.PAIR_VELOCITY, kernel, field_pos, field_gamma, field_sigma, n, out)
     X, T, A = sweeper.sample_pairs(max_pairs, device=field_pos.device)
+    if parent_share > 0:
+        # the pairs shared through parents of leaves (two-level lists), which
+        # the network evaluates too
+        Xp, Tp, Ap = sweeper.sample_pairs(int(max_pairs * parent_share),
+                                          device=field_pos.device, parents=True)
+        X, T, A = torch.cat([X, Xp]), torch.cat([T, Tp]), torch.cat([A, Ap])
     sweeper.set_far_field(prev[0], prev[1], prev[2] or None)
     return X, T, A

@@ -97,16 +97,18 @@ class TreeSweeper:
         _capi.check(self.lib.fvx_tree_last_local_ms(self.handle, ctypes.byref(ms)))
         return float(ms.value)
 
-    def sample_pairs(self, max_pairs, stream=None, device="cuda"):
+    def sample_pairs(self, max_pairs, stream=None, device="cuda", parents=False):
         """Features X (k, 48) BF16, exact normalised targets T (k, 32) and the
         analytic translation A (k, 32) of up to max_pairs local-path pairs of the
-        last sweep (evenly strided over its list)."""
+        last sweep (evenly strided over its list): the leaves' own pairs, or with
+        parents=True the pairs shared through parents of leaves."""
         X = torch.empty((max_pairs, 48), dtype=torch.bfloat16, device=device)
         T = torch.empty((max_pairs, 32), dtype=torch.float32, device=device)
         A = torch.empty((max_pairs, 32), dtype=torch.float32, device=device)
         st = stream if stream is not None else torch.cuda.current_stream(X.device).cuda_stream
         k = ctypes.c_int(0)
-        _capi.check(self.lib.fvx_tree_sample_pairs(self.handle, int(max_pairs), X.data_ptr(),
+        _capi.check(self.lib.fvx_tree_sample_pairs(self.handle, 1 if parents else 0,
+                                                    int(max_pairs), X.data_ptr(),
                                                     T.data_ptr(), A.data_ptr(), ctypes.byref(k),
                                                     st))
         return X[: k.value], T[: k.value], A[: k.value]

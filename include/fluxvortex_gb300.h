@@ -219,7 +219,9 @@ int fvx_tree_last_eval_ms(fvx_tree* tree, float* ms);
  * fvx_tree_sample_pairs: features X[k][48] (BF16), exact FP64-summed
  * normalised targets T[k][32] (FP32) and, if A is not NULL, the analytic
  * translation A[k][32] of k <= max_pairs local-path pairs of the last sweep,
- * strided evenly over the list (*n_out = k). */
+ * strided evenly over the list (*n_out = k): list 0 = the leaves' own pairs,
+ * 1 = the pairs shared through a parent of leaves (two-level lists, used when
+ * theta_local = theta). */
 #define FVX_FAR_M2P 0
 #define FVX_FAR_M2L 1
 #define FVX_FAR_LEARNED 2
@@ -238,8 +240,8 @@ int fvx_tree_last_local_ms(fvx_tree* tree, float* ms);
  * fallback, mean e, max e of the last sweep (waits for it). */
 int fvx_tree_set_validation(fvx_tree* tree, int samples, double tol);
 int fvx_tree_last_validation(fvx_tree* tree, double* out);
-int fvx_tree_sample_pairs(fvx_tree* tree, int max_pairs, void* X, float* T, float* A, int* n_out,
-                          void* stream);
+int fvx_tree_sample_pairs(fvx_tree* tree, int list, int max_pairs, void* X, float* T, float* A,
+                          int* n_out, void* stream);
 
 /* ---- panel side of the hybrid panel-particle step (FP64) ------------------------
  * Replaces the PteraSoftware solver stages that HybridSolver runs around the

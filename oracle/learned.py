@@ -177,11 +177,12 @@ def learned_pairs(tree, theta_learned):
     return out
 
 
-def pair_samples(tree, pos, alpha, pairs):
-    """Features X (k, 48) and normalised exact targets T (k, 32) of the pairs."""
+def pair_samples(tree, pos, alpha, pairs, target_level=None):
+    """Features X (k, 48) and normalised exact targets T (k, 32) of the pairs
+    (target cells at the leaf level, or at ``target_level``)."""
     perm = tree["perm"]
     sp, sa = pos[perm], alpha[perm]
-    leaves = tree["levels"][tree["L"]]
+    leaves = tree["levels"][tree["L"] if target_level is None else target_level]
     X = np.zeros((len(pairs), IN))
     T = np.zeros((len(pairs), OUT))
     for r, (t, l, c) in enumerate(pairs):

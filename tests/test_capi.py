@@ -58,3 +58,35 @@ def test_scratch_query_is_host_only():
     lib = _capi.load()
     assert lib.fvx_segments_collapsed_scratch_bytes(0, 10, 0) == 0
     assert lib.fvx_particle_pairs_scratch_bytes(0, 0, 0, 10) == 0
+
+
+def test_flutter_structs_match_the_header_layout(tmp_path):
+    """The ctypes mirrors of FlutterParams / FlutterState have the C layout
+    (sizes and field offsets from a C program compiled against the header)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    from fluxvortex_gb300.flutter import _Params, _State
+    fields = {"FlutterParams": _Params, "FlutterState": _State}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fluxvortex_gb300.h"',
+             'int main(void) {']
+    for cname, cls in fields.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    got = {}
+    for line in out.splitlines():
+        cname, what, val = line.split()
+        got[(cname, what)] = int(val)
+    for cname, cls in fields.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)

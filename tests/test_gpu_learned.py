@@ -167,3 +167,34 @@ def test_training_reduces_loss(cuda):
     er = float(r.errors(X, T, A).median())
     assert abs(er - ea) < 0.05 * ea, (er, ea)
     assert _lib().status_read_and_clear() == 0
+
+
+def test_sampled_parent_pairs_match_exact_local_expansions(cuda):
+    """Pairs shared through parents of leaves (two-level lists): features and
+    FP64 targets about the parent's centre against the oracle."""
+    from fluxvortex_gb300.tree import TreeSweeper
+    from fluxvortex_gb300 import _capi
+    n, leaf = 6000, 16
+    pos, alpha, sigma = _slab(n, 33)
+    ts = TreeSweeper(theta=0.5, leaf_target=leaf)
+    ts.set_far_field("m2l")
+    ts.set_validation(0, 0.1)
+    d = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")  # noqa: E731
+    out = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+    ts.sweep(_capi.PAIR_VELOCITY, "winckelmans", d(pos), d(alpha), d(sigma), n, out)
+    tree = TC.build(pos, theta=0.5, leaf_target=leaf)
+    _, _, parent_far = TC.dual_lists(tree)
+    pairs = [(p, l, c) for p, lst in enumerate(parent_far) for (l, c) in lst]
+    assert len(pairs) > 0
+    max_pairs = 61
+    Xg, Tg, Ag = ts.sample_pairs(max_pairs, parents=True)
+    stride = len(pairs) // max_pairs if len(pairs) > max_pairs else 1
+    k = min(len(pairs) // stride, max_pairs)
+    assert Xg.shape[0] == k
+    Xo, To = OL.pair_samples(tree, pos, alpha, [pairs[i * stride] for i in range(k)],
+                             target_level=tree["L"] - 1)
+    Xg, Tg = Xg.float().cpu().numpy(), Tg.cpu().numpy()
+    assert np.all(np.abs(Xg - Xo) <= 2.0 ** -7 * np.abs(Xo) + 1e-6)
+    rel = np.abs(Tg - To).max(axis=1) / np.abs(To).max(axis=1)
+    assert rel.max() < 1e-4, rel.max()
+    assert _capi.status_read_and_clear() == 0
