@@ -132,3 +132,57 @@ def test_two_level_lists_match_oracle(cuda):
     assert int(stats[3]) == 0
     assert int(stats[4]) == sum(len(x) for x in leaf_far) + sum(len(x) for x in parent_far)
     assert _capi.status_read_and_clear() == 0
+
+
+@pytest.mark.parametrize("case", ["empty", "one", "two", "coincident", "line", "sheet",
+                                  "clustered"])
+@pytest.mark.parametrize("method", ["m2l", "learned"])
+def test_local_expansion_degenerate_inputs(cuda, case, method):
+    """Empty, tiny, coincident, collinear, planar and strongly clustered fields
+    through the local-expansion far field (two-level lists, validation on):
+    finite outputs, and the direct sum's accuracy where there is a field."""
+    from fluxvortex_gb300 import _capi, learned as L
+    from fluxvortex_gb300.tree import TreeSweeper
+    rng = np.random.default_rng(11)
+    if case == "empty":
+        pos = np.zeros((0, 3))
+    elif case == "one":
+        pos = np.array([[0.3, -0.2, 0.1]])
+    elif case == "two":
+        pos = np.array([[0.0, 0.0, 0.0], [0.05, 0.0, 0.0]])
+    elif case == "coincident":
+        pos = np.tile([[0.5, 0.5, 0.5]], (40, 1)) + rng.normal(0, 1e-9, (40, 3))
+    elif case == "line":
+        pos = np.c_[np.linspace(0, 8, 3000), np.zeros(3000), np.zeros(3000)]
+    elif case == "sheet":
+        pos = np.c_[rng.uniform(0, 4, (4000, 2)), np.full(4000, 0.25)]
+    else:
+        centres = rng.uniform(0, 6, (12, 3))
+        pos = (centres[rng.integers(0, 12, 5000)] + rng.normal(0, 0.05, (5000, 3)))
+    n = pos.shape[0]
+    gam = rng.normal(0, 1e-3, (n, 3))
+    sig = np.full(n, 0.02)
+    ts = TreeSweeper(theta=0.5, leaf_target=16)
+    ts.set_far_field(method, mlp=L.FarFieldMLP.load() if method == "learned" else None)
+    ts.set_validation(64, 0.1)
+    if n == 0:
+        out = torch.zeros((1, 3), dtype=torch.float64, device="cuda")
+        P = torch.zeros((1, 3), dtype=torch.float64, device="cuda")
+        ts.sweep(_capi.PAIR_VELOCITY, "winckelmans", P, P, P[:, 0], 0, out)
+        assert _capi.status_read_and_clear() == 0
+        return
+    P, G, S = _dev(pos), _dev(gam), _dev(sig)
+    out, stats = _sweep(ts, _capi.PAIR_VELOCITY, P, G, S, n)
+    u = out.cpu().numpy()
+    assert np.all(np.isfinite(u))
+    ref = _direct(_capi.PAIR_VELOCITY, P, G, S).cpu().numpy()
+    if np.abs(ref).max() > 0:
+        err = np.abs(u - ref).max() / np.abs(ref).max()
+        # Where a particle's field is one or a few far pairs (two isolated
+        # particles; a line) it carries their full truncation error at the
+        # acceptance boundary (second-order expansions at theta = 0.5: a few
+        # per cent for one pair); a planar sheet lines those errors up; fields of
+        # many particles average them.
+        tol = {"two": 5e-2, "line": 2e-2, "sheet": 5e-3}.get(case, 2e-3)
+        assert err < tol, err
+    assert _capi.status_read_and_clear() == 0
