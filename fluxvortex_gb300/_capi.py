@@ -67,17 +67,25 @@ SIGNATURES = {
     "fvx_mlp_colsum": (I32, [I32, I32, P, P, P]),
     "fvx_mlp_adam": (I32, [I32, P, P, P, P, P, F, F, F, F, I32, P]),
     "fvx_tc_gemm_probe": (I32, [P, P, I32, I32, P, I32, P]),
-    "fvx_uvlm_kinematics": (I32, [I64, P, D, D, D, D, D, P, P]),
-    "fvx_uvlm_lattice": (I32, [P, I32, I32, P, P, P, P, P, P, P, P, P, P, P]),
+    "fvx_uvlm_kinematics": (I32, [I32, P, P, D, P, P]),
+    "fvx_uvlm_lattice": (I32, [P, I32, P, P, P, P, P, P, P, P, P, P, P, P]),
     "fvx_uvlm_aic": (I32, [I32, I32, P, P, P, P, P, P, D, D, P, P]),
-    "fvx_uvlm_rhs": (I32, [I32, P, P, P, P, P, D, D, D, D, D, P, P]),
+    "fvx_uvlm_rhs": (I32, [I32, P, P, P, P, P, P, D, P, P]),
     "fvx_lu_solve_batched": (I32, [I32, I32, P, P, P]),
-    "fvx_uvlm_loads": (I32, [I32, I32, P, P, P, P, P, P, P, P, P, P, D, D, D, D, D, D, D, P, P,
-                             P, P]),
-    "fvx_uvlm_wake_rings": (I32, [I32, I32, P, P, P, D, P, P, P, P, P, P, P, P]),
-    "fvx_uvlm_shed": (I32, [I32, I32, I32, P, P, P, P, P, P, D, P, P, P, P]),
-    "fvx_uvlm_convert": (I32, [I32, I32, I32, P, P, I32, D, I64, P, P, P, P, P, P]),
+    "fvx_uvlm_loads": (I32, [I32, P, P, P, P, P, P, P, P, P, P, P, D, D, D, D, P, P, P, P]),
+    "fvx_uvlm_wake_rings": (I32, [I32, P, P, P, P, D, P, P, P, P, P, P, P, P]),
+    "fvx_uvlm_shed": (I32, [I32, I32, P, P, P, P, P, P, P, D, P, P, P, P]),
+    "fvx_uvlm_convert": (I32, [I32, I32, P, P, P, I32, D, I64, P, P, P, P, P, P]),
 }
+
+
+
+class Surfaces(ctypes.Structure):
+    """FvxSurfaces: the surface layout of a panel grid (the arrays are device
+    pointers; the struct itself is passed by host pointer)."""
+    _fields_ = [("ns", ctypes.c_int32), ("w", ctypes.c_int32), ("col", P), ("surf", P),
+                ("motion", P)]
+
 
 _lock = threading.Lock()
 _lib = None

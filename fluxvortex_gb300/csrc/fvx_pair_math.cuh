@@ -129,7 +129,10 @@ __device__ __forceinline__ void core_f32(float r2, float s2, float k2, float& f,
     float t2 = t * t;
     float t5 = t2 * t2 * t;
     f = (r2 + k2) * t5;
-    if (NEED_FPR) fpr = -(3.0f * r2 + 10.5f * s2) * (t5 * t2);
+    // (3 r2 + 10.5 s2) t^2 <= 10.5 first: t^7 alone overflows FP32 once
+    // r^2 + s^2 < ~1e-11 (cores near the integrator's 1e-6 floor), and the
+    // self pair's 0 x inf would then be NaN where the FP64 sum gives 0
+    if (NEED_FPR) fpr = -((3.0f * r2 + 10.5f * s2) * t2) * t5;
   } else {
     const float inv_s = k2;
     const float x = r2 * inv_s * inv_s;

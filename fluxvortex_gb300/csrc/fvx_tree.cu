@@ -101,17 +101,25 @@ int scan_ints(const int* in, int n, int* out, int inclusive, int* tmp, cudaStrea
 namespace tree {
 
 // ---- bounding box -------------------------------------------------------------
+// Bounding box of the finite positions; particles with a non-finite
+// coordinate are counted into *nonfinite (the sweep refuses them).
 __global__ void bbox_partial_kernel(int64_t n, const double* __restrict__ pos,
-                                    double* __restrict__ partial) {
+                                    double* __restrict__ partial,
+                                    unsigned* __restrict__ nonfinite) {
   double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  unsigned bad = 0;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    bool fin = true;
     for (int c = 0; c < 3; ++c) {
       const double v = pos[3 * i + c];
+      fin = fin && isfinite(v);
       lo[c] = fmin(lo[c], v);
       hi[c] = fmax(hi[c], v);
     }
+    bad += fin ? 0u : 1u;
   }
+  if (bad) atomicAdd(nonfinite, bad);
   __shared__ double s[6][256];
   for (int c = 0; c < 3; ++c) {
     s[c][threadIdx.x] = lo[c];
@@ -909,11 +917,13 @@ __device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, in
       acc[1] = x2::fma(EX, NAZ, x2::fma(EZ, AX, acc[1]));
       acc[2] = x2::fma(EY, NAX, x2::fma(EX, AY, acc[2]));
     } else {
-      // S += (f G + w d) x a, w = fpr (d . G), fpr = -(3 r2 + 10.5 s2) t^7
+      // S += (f G + w d) x a, w = fpr (d . G), fpr = -(3 r2 + 10.5 s2) t^7,
+      // formed as ((-3 r2 - 10.5 s2) t^2) t^5 so that no factor overflows
+      // FP32 for cores down to the integrator's 1e-6 floor
       uint64_t DG = x2::mul(DX, GX);
       DG = x2::fma(DY, GY, DG);
       DG = x2::fma(DZ, GZ, DG);
-      const uint64_t W = x2::mul(x2::mul(x2::fma(R2, CM3, q5.y), x2::mul(T5, T2)), DG);
+      const uint64_t W = x2::mul(x2::mul(x2::mul(x2::fma(R2, CM3, q5.y), T2), T5), DG);
       const uint64_t VX = x2::fma(W, DX, x2::mul(F, GX));
       const uint64_t VY = x2::fma(W, DY, x2::mul(F, GY));
       const uint64_t VZ = x2::fma(W, DZ, x2::mul(F, GZ));
@@ -1459,15 +1469,22 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   int rc;
   // 1. bounding box -> grid
   const int nbb = 256;
-  if ((rc = grow(T->bbox, sizeof(double) * (6 * nbb + 6)))) return rc;
-  bbox_partial_kernel<<<nbb, 256, 0, s>>>(n, pos, P<double>(T->bbox));
+  if ((rc = grow(T->bbox, sizeof(double) * (6 * nbb + 7)))) return rc;
+  unsigned* nonfinite = reinterpret_cast<unsigned*>(P<double>(T->bbox) + 6 * nbb + 6);
+  FVX_CUDA_TRY(cudaMemsetAsync(nonfinite, 0, sizeof(unsigned), s));
+  bbox_partial_kernel<<<nbb, 256, 0, s>>>(n, pos, P<double>(T->bbox), nonfinite);
   FVX_LAUNCH_CHECK();
   bbox_final_kernel<<<1, 32, 0, s>>>(nbb, P<double>(T->bbox), P<double>(T->bbox) + 6 * nbb);
   FVX_LAUNCH_CHECK();
   double lohi[6];
+  unsigned nbad = 0;
   FVX_CUDA_TRY(cudaMemcpyAsync(lohi, P<double>(T->bbox) + 6 * nbb, sizeof(lohi),
                                cudaMemcpyDeviceToHost, s));
+  FVX_CUDA_TRY(cudaMemcpyAsync(&nbad, nonfinite, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   FVX_CUDA_TRY(cudaStreamSynchronize(s));
+  // a non-finite position would otherwise collapse the grid (all keys in one
+  // cell) and turn the sweep into an all-pairs sum on a few CTAs
+  FVX_ARG_CHECK(nbad == 0, "treecode: %u particles with non-finite positions", nbad);
   int L;
   double h, origin[3];
   grid_params(lohi, lohi + 3, n, leaf_target, &L, &h, origin);

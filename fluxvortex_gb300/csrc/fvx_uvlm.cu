@@ -3,7 +3,8 @@
 // Kernels for one step of a ring-vortex UVLM with a hybrid ring/particle
 // wake, in the order the reference's solver runs it (PteraSoftware's step,
 // overridden by tests/experiment_hybrid_panel_particle.py:114-204):
-//   kinematics      base vertex grid -> vertices at time t (heave + flapping)
+//   kinematics      base vertex grid -> vertices at time t (heave + flapping,
+//                   per surface)
 //   lattice         quarter-chord ring corners, 3/4-chord collocation points,
 //                   normals, areas, bound-leg centres/vectors, TE back edge
 //   aic             AIC[i,j] = (unit ring j at collocation i) . n_i, the
@@ -18,7 +19,10 @@
 //   convert         HybridSolver._convert_old_wake_to_particles (:145-204):
 //                   rows >= N_keep -> 4 particles per ring, appended on the
 //                   device with a block-wide compaction
-// All per-step inputs are device arrays; the host only sequences launches.
+// Several lifting surfaces share one vertex grid (FvxSurfaces): ring strip j
+// spans vertex columns col[j], col[j]+1 and vertex column c moves with
+// surface surf[c]; ring k = i ns + j.  All per-step inputs are device arrays;
+// the host only sequences launches.
 #include "fvx_common.cuh"
 #include "fvx_segment_math.cuh"
 
@@ -42,33 +46,45 @@ struct Motion {
   double heave_amp, flap_amp, omega, y0, t;
 };
 
+__device__ __forceinline__ int strip_col(const FvxSurfaces& s, int j) {
+  return s.col ? s.col[j] : j;
+}
+
+// Motion of vertex column c at time t: the surface's row of the table
+// (heave_amp, flap_amp, omega, y0).
+__device__ __forceinline__ Motion column_motion(const FvxSurfaces& s, int c, double t) {
+  const double* m = s.motion + 4 * (s.surf ? s.surf[c] : 0);
+  return Motion{m[0], m[1], m[2], m[3], t};
+}
+
 // Body-point velocity at current position p: heave rate on z, flapping about
-// the x axis through y0 mirrored per half wing.
+// the x axis through the hinge line y = +-y0 of the point's half wing,
+// mirrored per half.
 __device__ __forceinline__ void body_velocity(const Motion& m, const double p[3], double v[3]) {
   const double h = m.heave_amp * sin(m.omega * m.t);
   const double hdot = m.heave_amp * m.omega * cos(m.omega * m.t);
   const double thdot = m.flap_amp * m.omega * cos(m.omega * m.t);
-  const double dy = p[1] - m.y0;
-  const double s = dy >= 0.0 ? 1.0 : -1.0;
+  const double s = p[1] >= 0.0 ? 1.0 : -1.0;
+  const double dy = p[1] - s * m.y0;
   const double Z = p[2] - h;
   v[0] = 0.0;
   v[1] = -s * thdot * Z;
   v[2] = s * thdot * dy + hdot;
 }
 
-__global__ void kinematics_kernel(int64_t nv, const double* __restrict__ base, Motion m,
-                                  double* __restrict__ out) {
+__global__ void kinematics_kernel(int64_t nv, const double* __restrict__ base, FvxSurfaces sf,
+                                  double t, double* __restrict__ out) {
   int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= nv) return;
+  const Motion m = column_motion(sf, static_cast<int>(i % sf.w), t);
   double v[3];
   load3(base, i, v);
   if (m.flap_amp != 0.0) {
     const double th = m.flap_amp * sin(m.omega * m.t);
-    const double dy = v[1] - m.y0;
-    const double s = dy > 0.0 ? 1.0 : (dy < 0.0 ? -1.0 : 0.0);
-    const double y = fabs(dy), z = v[2];
+    const double s = v[1] > 0.0 ? 1.0 : (v[1] < 0.0 ? -1.0 : 0.0);
+    const double y = fabs(v[1]) - m.y0, z = v[2];
     const double c = cos(th), sn = sin(th);
-    v[1] = m.y0 + s * (y * c - z * sn);
+    v[1] = s * (m.y0 + (y * c - z * sn));
     v[2] = y * sn + z * c;
   }
   if (m.heave_amp != 0.0) v[2] += m.heave_amp * sin(m.omega * m.t);
@@ -79,9 +95,8 @@ struct LatticeOut {
   double *br, *fr, *fl, *bl, *colloc, *normal, *area, *leg_center, *leg_vec, *te_back;
 };
 
-// quarter-chord lattice point of vertex (i, j)
-__device__ __forceinline__ void vq(const double* v, int nc, int ns, int i, int j, double o[3]) {
-  const int w = ns + 1;
+// quarter-chord lattice point of vertex (i, j) of a grid w columns wide
+__device__ __forceinline__ void vq(const double* v, int nc, int w, int i, int j, double o[3]) {
   double a[3], b[3];
   if (i < nc) {
     load3(v, static_cast<int64_t>(i) * w + j, a);
@@ -94,22 +109,23 @@ __device__ __forceinline__ void vq(const double* v, int nc, int ns, int i, int j
   }
 }
 
-__global__ void lattice_kernel(const double* __restrict__ v, int nc, int ns, LatticeOut o) {
+__global__ void lattice_kernel(const double* __restrict__ v, int nc, FvxSurfaces sf,
+                               LatticeOut o) {
+  const int ns = sf.ns, w = sf.w;
   const int P = nc * ns;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int w = ns + 1;
-  if (k <= ns && k < w) {  // trailing-edge back edge
+  if (k < w) {  // trailing-edge back edge, every vertex column
     double tb[3];
-    vq(v, nc, ns, nc, k, tb);
+    vq(v, nc, w, nc, k, tb);
     store3(o.te_back, k, tb);
   }
   if (k >= P) return;
-  const int i = k / ns, j = k % ns;
+  const int i = k / ns, j = strip_col(sf, k % ns);
   double fl[3], fr[3], br[3], bl[3];
-  vq(v, nc, ns, i, j, fl);
-  vq(v, nc, ns, i, j + 1, fr);
-  vq(v, nc, ns, i + 1, j + 1, br);
-  vq(v, nc, ns, i + 1, j, bl);
+  vq(v, nc, w, i, j, fl);
+  vq(v, nc, w, i, j + 1, fr);
+  vq(v, nc, w, i + 1, j + 1, br);
+  vq(v, nc, w, i + 1, j, bl);
   store3(o.fl, k, fl);
   store3(o.fr, k, fr);
   store3(o.br, k, br);
@@ -163,12 +179,13 @@ __global__ void aic_kernel(int P, const double* __restrict__ colloc,
 }
 
 // rhs_i = -((U_inf - v_body) + (v1 + v2)) . n   (v1, v2 may be null)
-__global__ void rhs_kernel(int P, const double* __restrict__ colloc,
+__global__ void rhs_kernel(int P, FvxSurfaces sf, const double* __restrict__ colloc,
                            const double* __restrict__ normal, const double* __restrict__ v1,
                            const double* __restrict__ v2, double ux, double uy, double uz,
-                           Motion m, double* __restrict__ rhs) {
+                           double t, double* __restrict__ rhs) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P) return;
+  const Motion m = column_motion(sf, strip_col(sf, i % sf.ns), t);
   double p[3], vb[3], n[3];
   load3(colloc, i, p);
   load3(normal, i, n);
@@ -266,7 +283,8 @@ __global__ void __launch_bounds__(256) lu_solve_kernel(int P, double* __restrict
 }
 
 struct LoadsArgs {
-  int nc, ns;
+  int nc;
+  FvxSurfaces sf;
   const double* gamma;
   const double* gamma_prev;  // null: no unsteady term (first step)
   const double* leg_center;
@@ -276,25 +294,26 @@ struct LoadsArgs {
   const double* v1;  // induced velocities at the leg centres (summed, any may be null)
   const double* v2;
   const double* v3;
-  double ux, uy, uz, rho, dt;
-  Motion m;
+  double ux, uy, uz, rho, dt, t;
+  double s_ref;     // <= 0: the sum of the panel areas
   double* cl_out;   // cl_out[0], cdi_out[0] written
   double* cdi_out;
   double* force;    // optional (P,3) per-panel force
 };
 
 __global__ void __launch_bounds__(256) loads_kernel(LoadsArgs a) {
-  const int P = a.nc * a.ns;
+  const int ns = a.sf.ns;
+  const int P = a.nc * ns;
   double F[3] = {0.0, 0.0, 0.0}, S = 0.0;
   for (int k = threadIdx.x; k < P; k += blockDim.x) {
-    const int i = k / a.ns;
+    const int i = k / ns;
     const double g = a.gamma[k];
-    const double geff = i > 0 ? g - a.gamma[k - a.ns] : g;
+    const double geff = i > 0 ? g - a.gamma[k - ns] : g;
     double p[3], vb[3], l[3], n[3];
     load3(a.leg_center, k, p);
     load3(a.leg_vec, k, l);
     load3(a.normal, k, n);
-    body_velocity(a.m, p, vb);
+    body_velocity(column_motion(a.sf, strip_col(a.sf, k % ns), a.t), p, vb);
     double w[3] = {0.0, 0.0, 0.0};
     if (a.v1) load3(a.v1, k, w);
     if (a.v2) {
@@ -341,20 +360,21 @@ __global__ void __launch_bounds__(256) loads_kernel(LoadsArgs a) {
     const double V = sqrt(a.ux * a.ux + a.uy * a.uy + a.uz * a.uz);
     const double eD[3] = {a.ux / V, a.uy / V, a.uz / V};
     const double eL[3] = {-eD[2], 0.0, eD[0]};
-    const double qS = 0.5 * a.rho * V * V * red[3][0];
+    const double qS = 0.5 * a.rho * V * V * (a.s_ref > 0.0 ? a.s_ref : red[3][0]);
     a.cl_out[0] = (red[0][0] * eL[0] + red[1][0] * eL[1] + red[2][0] * eL[2]) / qS;
     a.cdi_out[0] = (red[0][0] * eD[0] + red[1][0] * eD[1] + red[2][0] * eD[2]) / qS;
   }
 }
 
-// Ring wake (R rows x ns rings) from the vertex lattice W ((R+1) x (ns+1)).
-__global__ void wake_rings_kernel(int R, int ns, const double* __restrict__ W,
+// Ring wake (R rows x ns rings) from the vertex lattice W ((R+1) x w).
+__global__ void wake_rings_kernel(int R, FvxSurfaces sf, const double* __restrict__ W,
                                   const double* __restrict__ gam, const double* __restrict__ age,
                                   double rc0, double* br, double* fr, double* fl, double* bl,
                                   double* strength, double* rc0s, double* ages) {
+  const int ns = sf.ns, w = sf.w;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= R * ns) return;
-  const int r = k / ns, j = k % ns, w = ns + 1;
+  const int r = k / ns, j = strip_col(sf, k % ns);
   double p[3];
   load3(W, static_cast<int64_t>(r) * w + j, p);
   store3(fl, k, p);
@@ -372,13 +392,12 @@ __global__ void wake_rings_kernel(int R, int ns, const double* __restrict__ W,
 // New wake from the old one: row 0 = trailing edge of the next step, rows
 // m >= 1 = old rows convected by U_inf dt; strengths shift by one row and take
 // the trailing-edge ring strengths; ages shift and grow by dt.
-__global__ void shed_kernel(int R_old, int nc, int ns, const double* __restrict__ W_old,
+__global__ void shed_kernel(int R_old, int nc, int ns, int w, const double* __restrict__ W_old,
                             const double* __restrict__ gam_old,
                             const double* __restrict__ age_old,
                             const double* __restrict__ te_next, const double* __restrict__ gamma,
                             double dx, double dy, double dz, double dt, double* __restrict__ W_new,
                             double* __restrict__ gam_new, double* __restrict__ age_new) {
-  const int w = ns + 1;
   const int nverts = (R_old + 2) * w;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < nverts) {
@@ -402,7 +421,7 @@ __global__ void shed_kernel(int R_old, int nc, int ns, const double* __restrict_
 }
 
 // Rows r >= n_keep of the wake lattice -> particles appended at *count.
-__global__ void __launch_bounds__(256) convert_kernel(int R, int n_keep, int ns,
+__global__ void __launch_bounds__(256) convert_kernel(int R, int n_keep, FvxSurfaces sf,
                                                       const double* __restrict__ W,
                                                       const double* __restrict__ gam,
                                                       int sigma_rule, double sigma_vdt,
@@ -413,16 +432,16 @@ __global__ void __launch_bounds__(256) convert_kernel(int R, int n_keep, int ns,
   __shared__ int64_t s_base;
   if (threadIdx.x == 0) s_base = *count;
   __syncthreads();
+  const int ns = sf.ns, w = sf.w;
   const int nrings = (R - n_keep) * ns;
-  const int w = ns + 1;
   for (int c0 = 0; c0 < nrings; c0 += blockDim.x) {
     const int k = c0 + threadIdx.x;
     double q[4][3], al[4][3];
     int emit = 0, mask = 0;
     double sg = sigma_vdt;
     if (k < nrings) {
-      const int r = n_keep + k / ns, j = k % ns;
-      const double g = gam[r * ns + j];
+      const int r = n_keep + k / ns, j = strip_col(sf, k % ns);
+      const double g = gam[r * ns + k % ns];
       double fl[3], fr[3], bl[3], br[3];
       load3(W, static_cast<int64_t>(r) * w + j, fl);
       load3(W, static_cast<int64_t>(r) * w + j + 1, fr);
@@ -489,29 +508,33 @@ unsigned nblk(int64_t n, int t = kT) { return static_cast<unsigned>((n + t - 1) 
 }  // namespace
 }  // namespace fvx
 
-using fvx::Motion;
+
+// A layout is usable when its sizes are positive, the motion table is given
+// and, without a strip map, the grid is one surface (w = ns + 1).
+static bool layout_ok(const FvxSurfaces* s) {
+  return s && s->ns >= 1 && s->w >= 2 && s->motion && (s->col || s->w == s->ns + 1);
+}
 
 extern "C" {
 
-int fvx_uvlm_kinematics(int64_t n_verts, const double* base, double heave_amp, double flap_amp,
-                        double omega, double y0, double t, double* out, void* stream) {
-  FVX_ARG_CHECK(n_verts >= 0 && base && out, "bad kinematics arguments");
-  if (n_verts == 0) return FVX_OK;
-  Motion m{heave_amp, flap_amp, omega, y0, t};
-  fvx::kinematics_kernel<<<fvx::nblk(n_verts), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(
-      n_verts, base, m, out);
+int fvx_uvlm_kinematics(int nc, const FvxSurfaces* s, const double* base, double t, double* out,
+                        void* stream) {
+  FVX_ARG_CHECK(nc >= 1 && layout_ok(s) && base && out, "bad kinematics arguments");
+  const int64_t nv = static_cast<int64_t>(nc + 1) * s->w;
+  fvx::kinematics_kernel<<<fvx::nblk(nv), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(
+      nv, base, *s, t, out);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
 
-int fvx_uvlm_lattice(const double* verts, int nc, int ns, double* br, double* fr, double* fl,
-                     double* bl, double* colloc, double* normal, double* area,
+int fvx_uvlm_lattice(const double* verts, int nc, const FvxSurfaces* s, double* br, double* fr,
+                     double* fl, double* bl, double* colloc, double* normal, double* area,
                      double* leg_center, double* leg_vec, double* te_back, void* stream) {
-  FVX_ARG_CHECK(nc >= 2 && ns >= 1 && verts, "lattice needs nc >= 2, ns >= 1");
+  FVX_ARG_CHECK(nc >= 2 && layout_ok(s) && verts, "lattice needs nc >= 2 and a layout");
   fvx::LatticeOut o{br, fr, fl, bl, colloc, normal, area, leg_center, leg_vec, te_back};
-  const int n = nc * ns > ns + 1 ? nc * ns : ns + 1;
+  const int n = nc * s->ns > s->w ? nc * s->ns : s->w;
   fvx::lattice_kernel<<<fvx::nblk(n), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(verts, nc,
-                                                                                      ns, o);
+                                                                                      *s, o);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
@@ -528,13 +551,14 @@ int fvx_uvlm_aic(int n_systems, int P, const double* colloc, const double* norma
   return FVX_OK;
 }
 
-int fvx_uvlm_rhs(int P, const double* colloc, const double* normal, const double* v1,
-                 const double* v2, const double* u_inf, double heave_amp, double flap_amp,
-                 double omega, double y0, double t, double* rhs, void* stream) {
-  FVX_ARG_CHECK(P >= 1 && colloc && normal && u_inf && rhs, "bad rhs arguments");
-  Motion m{heave_amp, flap_amp, omega, y0, t};
+int fvx_uvlm_rhs(int nc, const FvxSurfaces* s, const double* colloc, const double* normal,
+                 const double* v1, const double* v2, const double* u_inf, double t, double* rhs,
+                 void* stream) {
+  FVX_ARG_CHECK(nc >= 1 && layout_ok(s) && colloc && normal && u_inf && rhs,
+                "bad rhs arguments");
+  const int P = nc * s->ns;
   fvx::rhs_kernel<<<fvx::nblk(P), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(
-      P, colloc, normal, v1, v2, u_inf[0], u_inf[1], u_inf[2], m, rhs);
+      P, *s, colloc, normal, v1, v2, u_inf[0], u_inf[1], u_inf[2], t, rhs);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
@@ -546,52 +570,54 @@ int fvx_lu_solve_batched(int n_systems, int P, double* A, double* b, void* strea
   return FVX_OK;
 }
 
-int fvx_uvlm_loads(int nc, int ns, const double* gamma, const double* gamma_prev,
+int fvx_uvlm_loads(int nc, const FvxSurfaces* s, const double* gamma, const double* gamma_prev,
                    const double* leg_center, const double* leg_vec, const double* area,
                    const double* normal, const double* v1, const double* v2, const double* v3,
-                   const double* u_inf, double rho, double dt, double heave_amp, double flap_amp,
-                   double omega, double y0, double t, double* cl, double* cdi, double* force,
-                   void* stream) {
-  FVX_ARG_CHECK(nc >= 1 && ns >= 1 && gamma && u_inf && cl && cdi, "bad loads arguments");
-  fvx::LoadsArgs a{nc,        ns,   gamma, gamma_prev, leg_center, leg_vec, area, normal, v1,
-                   v2,        v3,   u_inf[0], u_inf[1], u_inf[2],  rho,     dt,
-                   Motion{heave_amp, flap_amp, omega, y0, t}, cl, cdi, force};
+                   const double* u_inf, double rho, double dt, double t, double s_ref,
+                   double* cl, double* cdi, double* force, void* stream) {
+  FVX_ARG_CHECK(nc >= 1 && layout_ok(s) && gamma && u_inf && cl && cdi, "bad loads arguments");
+  fvx::LoadsArgs a{nc,       *s,       gamma,    gamma_prev, leg_center, leg_vec, area,
+                   normal,   v1,       v2,       v3,         u_inf[0],   u_inf[1], u_inf[2],
+                   rho,      dt,       t,        s_ref,      cl,         cdi,     force};
   fvx::loads_kernel<<<1, 256, 0, static_cast<cudaStream_t>(stream)>>>(a);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
 
-int fvx_uvlm_wake_rings(int R, int ns, const double* W, const double* gam, const double* age,
-                        double rc0, double* br, double* fr, double* fl, double* bl,
-                        double* strength, double* rc0s, double* ages, void* stream) {
-  FVX_ARG_CHECK(R >= 0 && ns >= 1, "bad wake sizes");
+int fvx_uvlm_wake_rings(int R, const FvxSurfaces* s, const double* W, const double* gam,
+                        const double* age, double rc0, double* br, double* fr, double* fl,
+                        double* bl, double* strength, double* rc0s, double* ages, void* stream) {
+  FVX_ARG_CHECK(R >= 0 && layout_ok(s), "bad wake sizes");
   if (R == 0) return FVX_OK;
-  fvx::wake_rings_kernel<<<fvx::nblk(R * ns), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(
-      R, ns, W, gam, age, rc0, br, fr, fl, bl, strength, rc0s, ages);
+  fvx::wake_rings_kernel<<<fvx::nblk(R * s->ns), fvx::kT, 0,
+                           static_cast<cudaStream_t>(stream)>>>(R, *s, W, gam, age, rc0, br, fr,
+                                                                fl, bl, strength, rc0s, ages);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
 
-int fvx_uvlm_shed(int R_old, int nc, int ns, const double* W_old, const double* gam_old,
-                  const double* age_old, const double* te_next, const double* gamma,
-                  const double* u_inf, double dt, double* W_new, double* gam_new,
-                  double* age_new, void* stream) {
-  FVX_ARG_CHECK(R_old >= 0 && nc >= 1 && ns >= 1 && u_inf, "bad shed arguments");
-  const int n = (R_old + 2) * (ns + 1);
+int fvx_uvlm_shed(int R_old, int nc, const FvxSurfaces* s, const double* W_old,
+                  const double* gam_old, const double* age_old, const double* te_next,
+                  const double* gamma, const double* u_inf, double dt, double* W_new,
+                  double* gam_new, double* age_new, void* stream) {
+  FVX_ARG_CHECK(R_old >= 0 && nc >= 1 && layout_ok(s) && u_inf, "bad shed arguments");
+  const int n = (R_old + 2) * s->w;
   fvx::shed_kernel<<<fvx::nblk(n), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(
-      R_old, nc, ns, W_old, gam_old, age_old, te_next, gamma, u_inf[0] * dt, u_inf[1] * dt,
+      R_old, nc, s->ns, s->w, W_old, gam_old, age_old, te_next, gamma, u_inf[0] * dt,
+      u_inf[1] * dt,
       u_inf[2] * dt, dt, W_new, gam_new, age_new);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
 
-int fvx_uvlm_convert(int R, int n_keep, int ns, const double* W, const double* gam,
-                     int sigma_rule, double sigma_vdt, int64_t capacity, int64_t* count,
-                     double* pos, double* alpha, double* sigma, double* age, void* stream) {
-  FVX_ARG_CHECK(R >= 0 && n_keep >= 0 && ns >= 1 && count, "bad convert arguments");
+int fvx_uvlm_convert(int R, int n_keep, const FvxSurfaces* s, const double* W,
+                     const double* gam, int sigma_rule, double sigma_vdt, int64_t capacity,
+                     int64_t* count, double* pos, double* alpha, double* sigma, double* age,
+                     void* stream) {
+  FVX_ARG_CHECK(R >= 0 && n_keep >= 0 && layout_ok(s) && count, "bad convert arguments");
   if (R <= n_keep) return FVX_OK;
   fvx::convert_kernel<<<1, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      R, n_keep, ns, W, gam, sigma_rule, sigma_vdt, capacity, count, pos, alpha, sigma, age);
+      R, n_keep, *s, W, gam, sigma_rule, sigma_vdt, capacity, count, pos, alpha, sigma, age);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }

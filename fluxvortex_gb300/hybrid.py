@@ -16,6 +16,8 @@ solve and the time integration stay FP64.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import torch
 
@@ -30,10 +32,20 @@ class HybridStep:
         self.precision = precision
         self.device = torch.device(device)
         self.lib = _capi.load()
-        nc, ns = cfg.verts.shape[0] - 1, cfg.verts.shape[1] - 1
-        self.nc, self.ns, self.P = nc, ns, nc * ns
+        col, surf, kins = cfg.layout()
+        nc, ns, w = cfg.verts.shape[0] - 1, int(col.size), cfg.verts.shape[1]
+        self.nc, self.ns, self.w, self.P = nc, ns, w, nc * ns
         d = dict(dtype=torch.float64, device=self.device)
         P = self.P
+        # surface layout: strip -> vertex column, column -> surface, motions
+        i32 = dict(dtype=torch.int32, device=self.device)
+        self._col = torch.as_tensor(np.asarray(col, dtype=np.int32), **i32)
+        self._surf = torch.as_tensor(np.asarray(surf, dtype=np.int32), **i32)
+        self._motion = torch.tensor([[k.heave_amp, k.flap_amp, 2.0 * np.pi / k.period, k.y0]
+                                     for k in kins], **d).reshape(-1).contiguous()
+        self._sf = _capi.Surfaces(ns, w, self._col.data_ptr(), self._surf.data_ptr(),
+                                  self._motion.data_ptr())
+        self.sf = ctypes.addressof(self._sf)
         self.base = torch.as_tensor(cfg.verts.reshape(-1, 3), **d).contiguous()
         self.verts = torch.empty_like(self.base)
         self.verts_next = torch.empty_like(self.base)
@@ -41,8 +53,8 @@ class HybridStep:
         self.L = {k: z3(P) for k in ("br", "fr", "fl", "bl", "colloc", "normal", "leg_center",
                                      "leg_vec")}
         self.L["area"] = torch.zeros(P, **d)
-        self.te = z3(ns + 1)
-        self.te_next = z3(ns + 1)
+        self.te = z3(w)
+        self.te_next = z3(w)
         self.Ln = {k: z3(P) for k in self.L if k != "area"}
         self.Ln["area"] = torch.zeros(P, **d)
         self.aic = torch.zeros((P, P), **d)
@@ -52,7 +64,7 @@ class HybridStep:
         self.force = z3(P)
         # ring wake: vertex lattice (R+1 rows) ping-pong, row strengths, ages
         rows = cfg.n_keep + 2
-        self.W = [z3(rows * (ns + 1)), z3(rows * (ns + 1))]
+        self.W = [z3(rows * w), z3(rows * w)]
         self.wg = [torch.zeros(rows * ns, **d), torch.zeros(rows * ns, **d)]
         self.wa = [torch.zeros(rows, **d), torch.zeros(rows, **d)]
         self.cur = 0
@@ -70,7 +82,7 @@ class HybridStep:
                                          far_field=cfg.far_field)
         self.count = torch.zeros(1, dtype=torch.int64, device=self.device)
         self.u_inf = np.ascontiguousarray(cfg.u_inf, dtype=np.float64)
-        self.omega = 2.0 * np.pi / cfg.kin.period
+        self.s_ref = -1.0 if cfg.s_ref is None else float(cfg.s_ref)
         self.cl_hist = torch.zeros(0, **d)
         self._cl = torch.zeros(4096, **d)
         self._cdi = torch.zeros(4096, **d)
@@ -78,21 +90,19 @@ class HybridStep:
         # initial wake lattice: the trailing edge at t = 0
         self._kin(0.0, self.verts)
         self._lattice(self.verts, self.L, self.te)
-        self.W[0][: ns + 1].copy_(self.te)
+        self.W[0][:w].copy_(self.te)
 
     # ---- helpers ------------------------------------------------------------
     def _st(self):
         return torch.cuda.current_stream(self.device).cuda_stream
 
     def _kin(self, t, out):
-        k = self.cfg.kin
-        _capi.check(self.lib.fvx_uvlm_kinematics(self.base.shape[0], self.base.data_ptr(),
-                                                 k.heave_amp, k.flap_amp, self.omega, k.y0, t,
+        _capi.check(self.lib.fvx_uvlm_kinematics(self.nc, self.sf, self.base.data_ptr(), t,
                                                  out.data_ptr(), self._st()))
 
     def _lattice(self, verts, L, te):
         _capi.check(self.lib.fvx_uvlm_lattice(
-            verts.data_ptr(), self.nc, self.ns, L["br"].data_ptr(), L["fr"].data_ptr(),
+            verts.data_ptr(), self.nc, self.sf, L["br"].data_ptr(), L["fr"].data_ptr(),
             L["fl"].data_ptr(), L["bl"].data_ptr(),
             L["colloc"].data_ptr() if "colloc" in L else None,
             L["normal"].data_ptr(), L["area"].data_ptr(), L["leg_center"].data_ptr(),
@@ -141,10 +151,8 @@ class HybridStep:
 
     def _panel(self, out2):
         cfg, lib, st = self.cfg, self.lib, self._st()
-        kin = cfg.kin
         P, ns = self.P, self.ns
         t = self.k * cfg.dt
-        mot = (kin.heave_amp, kin.flap_amp, self.omega, kin.y0, t)
         self._kin(t, self.verts)
         self._lattice(self.verts, self.L, self.te)
         L = self.L
@@ -157,7 +165,8 @@ class HybridStep:
         Wc, gc, ac = self.W[self.cur], self.wg[self.cur], self.wa[self.cur]
         nr = R * ns
         if R:
-            _capi.check(lib.fvx_uvlm_wake_rings(R, ns, Wc.data_ptr(), gc.data_ptr(), ac.data_ptr(),
+            _capi.check(lib.fvx_uvlm_wake_rings(R, self.sf, Wc.data_ptr(), gc.data_ptr(),
+                                                ac.data_ptr(),
                                                 cfg.rc0, self.wr["br"].data_ptr(),
                                                 self.wr["fr"].data_ptr(), self.wr["fl"].data_ptr(),
                                                 self.wr["bl"].data_ptr(), self.wr_s.data_ptr(),
@@ -167,10 +176,11 @@ class HybridStep:
         npart = self.field.np
         if npart:
             self.field._sweep(_capi.PAIR_VELOCITY, L["colloc"], None, P, self.v_part_c)
-        _capi.check(lib.fvx_uvlm_rhs(P, L["colloc"].data_ptr(), L["normal"].data_ptr(),
+        _capi.check(lib.fvx_uvlm_rhs(self.nc, self.sf, L["colloc"].data_ptr(),
+                                     L["normal"].data_ptr(),
                                      self.v_ring_c.data_ptr() if R else None,
                                      self.v_part_c.data_ptr() if npart else None,
-                                     self.u_inf.ctypes.data, *mot, self.rhs.data_ptr(), st))
+                                     self.u_inf.ctypes.data, t, self.rhs.data_ptr(), st))
         # 4. strengths (in place: rhs -> Gamma)
         self.gamma.copy_(self.rhs)
         _capi.check(lib.fvx_lu_solve_batched(1, P, self.aic.data_ptr(), self.gamma.data_ptr(), st))
@@ -186,16 +196,15 @@ class HybridStep:
         cl_p = self._cl[k:].data_ptr() if out2 is None else out2[0:].data_ptr()
         cdi_p = self._cdi[k:].data_ptr() if out2 is None else out2[1:].data_ptr()
         _capi.check(lib.fvx_uvlm_loads(
-            self.nc, ns, self.gamma.data_ptr(), self.gamma_prev.data_ptr() if k else None,
+            self.nc, self.sf, self.gamma.data_ptr(), self.gamma_prev.data_ptr() if k else None,
             L["leg_center"].data_ptr(), L["leg_vec"].data_ptr(), L["area"].data_ptr(),
             L["normal"].data_ptr(), self.v_ring_l.data_ptr() if R else None,
             self.v_part_l.data_ptr() if npart else None, self.v_bound_l.data_ptr(),
-            self.u_inf.ctypes.data, cfg.rho, cfg.dt, *mot, cl_p, cdi_p, self.force.data_ptr(),
-            st))
+            self.u_inf.ctypes.data, cfg.rho, cfg.dt, t, self.s_ref, cl_p, cdi_p,
+            self.force.data_ptr(), st))
 
     def _advance(self):
         cfg, lib, st = self.cfg, self.lib, self._st()
-        ns = self.ns
         t = self.k * cfg.dt
         R = self.R
         Wc, gc, ac = self.W[self.cur], self.wg[self.cur], self.wa[self.cur]
@@ -203,7 +212,8 @@ class HybridStep:
         self._kin(t + cfg.dt, self.verts_next)
         self._lattice(self.verts_next, self.Ln, self.te_next)
         nxt = 1 - self.cur
-        _capi.check(lib.fvx_uvlm_shed(R, self.nc, ns, Wc.data_ptr(), gc.data_ptr(), ac.data_ptr(),
+        _capi.check(lib.fvx_uvlm_shed(R, self.nc, self.sf, Wc.data_ptr(), gc.data_ptr(),
+                                      ac.data_ptr(),
                                       self.te_next.data_ptr(), self.gamma.data_ptr(),
                                       self.u_inf.ctypes.data, cfg.dt, self.W[nxt].data_ptr(),
                                       self.wg[nxt].data_ptr(), self.wa[nxt].data_ptr(), st))
@@ -214,7 +224,7 @@ class HybridStep:
             f = self.field
             self.count.fill_(f.np)
             _capi.check(lib.fvx_uvlm_convert(
-                R, cfg.n_keep, ns, self.W[nxt].data_ptr(), self.wg[nxt].data_ptr(),
+                R, cfg.n_keep, self.sf, self.W[nxt].data_ptr(), self.wg[nxt].data_ptr(),
                 1 if cfg.sigma_rule == "edge" else 0, cfg.speed * cfg.dt, f.max_particles,
                 self.count.data_ptr(), f._pos.data_ptr(), f._gamma.data_ptr(),
                 f._sigma.data_ptr(), f._age.data_ptr(), st))
@@ -227,6 +237,41 @@ class HybridStep:
                                   free_wake=cfg.free_vpm)
         self.gamma_prev.copy_(self.gamma)
         self.k += 1
+
+    # ---- snapshot / restore ------------------------------------------------------
+    def snapshot(self, host=False):
+        """Everything a later step reads: the ring wake (vertex rows, strengths,
+        ages), the last strengths, the step count and CL / CDi history, and the
+        particle field.  Device copies, or NumPy arrays with ``host`` (e.g. for
+        ``numpy.savez``); ``restore`` resumes bitwise."""
+        cur = self.cur
+        st = {"W": self.W[cur].clone(), "wg": self.wg[cur].clone(), "wa": self.wa[cur].clone(),
+              "gamma": self.gamma.clone(), "gamma_prev": self.gamma_prev.clone(),
+              "cl": self._cl[: self.k].clone(), "cdi": self._cdi[: self.k].clone()}
+        if host:
+            st = {k: v.cpu().numpy() for k, v in st.items()}
+        st["R"], st["k"] = self.R, self.k
+        st["field"] = self.field.snapshot(host)
+        return st
+
+    def restore(self, st):
+        """Resumes from a ``snapshot`` (device or host arrays)."""
+        cur = self.cur
+        self.W[cur].copy_(torch.as_tensor(st["W"]))
+        self.wg[cur].copy_(torch.as_tensor(st["wg"]))
+        self.wa[cur].copy_(torch.as_tensor(st["wa"]))
+        self.gamma.copy_(torch.as_tensor(st["gamma"]))
+        self.gamma_prev.copy_(torch.as_tensor(st["gamma_prev"]))
+        self.R, self.k = int(st["R"]), int(st["k"])
+        if self._cl.numel() < self.k:
+            grow = self.k - self._cl.numel() + 4096
+            self._cl = torch.cat([self._cl, torch.zeros(grow, dtype=self._cl.dtype,
+                                                        device=self.device)])
+            self._cdi = torch.cat([self._cdi, torch.zeros(grow, dtype=self._cdi.dtype,
+                                                          device=self.device)])
+        self._cl[: self.k].copy_(torch.as_tensor(st["cl"]))
+        self._cdi[: self.k].copy_(torch.as_tensor(st["cdi"]))
+        self.field.restore(st["field"])
 
     def _rc0_bound(self):
         if not hasattr(self, "_rcb"):

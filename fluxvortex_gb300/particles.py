@@ -113,6 +113,26 @@ class VortexParticleField:
     def ages(self):
         return self._age[: self.np].cpu().numpy().copy()
 
+    # ---- snapshot / restore ------------------------------------------------------
+    def snapshot(self, host=False):
+        """The particle state (positions, strengths, cores, ages of the live
+        particles): device copies, or NumPy arrays with ``host``."""
+        n = self.np
+        st = {k: getattr(self, "_" + k)[:n].clone() for k in ("pos", "gamma", "sigma", "age")}
+        if host:
+            st = {k: v.cpu().numpy() for k, v in st.items()}
+        st["np"] = n
+        return st
+
+    def restore(self, st):
+        """Puts back a state taken by ``snapshot`` (device or host arrays)."""
+        n = int(st["np"])
+        if n > self.max_particles:
+            raise ValueError(f"snapshot of {n} particles exceeds the capacity {self.max_particles}")
+        for k in ("pos", "gamma", "sigma", "age"):
+            getattr(self, "_" + k)[:n].copy_(torch.as_tensor(st[k]), non_blocking=False)
+        self.np = n
+
     # ---- sweeps ----------------------------------------------------------------
     def _stream(self):
         return torch.cuda.current_stream(self.device).cuda_stream

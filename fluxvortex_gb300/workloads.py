@@ -6,19 +6,27 @@ y in [-5, 5], z in [-1, 1]), vector strengths i.i.d. N(0, (1e-3 m^3/s)^2)
 per component, core radius 0.02c, plus 4096 collocation targets on a planar
 64 x 64 grid over the wing (x in [0, 1], y in [-5, 5], z = 0).  The
 reference measures nothing at this scale; these inputs stand in for its wake
-runs with its stated shapes and value distributions.
+runs with its stated shapes and value distributions.  ``x0`` moves the slab's
+upstream face (default: one chord behind the leading edge), e.g. behind the
+ring rows of a larger configuration.
+
+``AIRCRAFT_SLAB_X0``: the slab's upstream face behind the large flapping
+configuration -- past the V-tail's trailing edge (x = 6.5) and its N_keep = 10
+ring rows (10 dt V = 2.3 m), so that the seeded particles fill the far wake
+and not the surfaces.
 """
 from __future__ import annotations
 
 import numpy as np
 
 SEED = 20261203
+AIRCRAFT_SLAB_X0 = 9.0
 
 
-def slab_wake(n: int, seed: int = SEED, chord: float = 1.0):
+def slab_wake(n: int, seed: int = SEED, chord: float = 1.0, x0: float = 1.0):
     rng = np.random.default_rng(seed)
-    lo = np.array([1.0, -5.0, -1.0]) * chord
-    hi = np.array([21.0, 5.0, 1.0]) * chord
+    lo = np.array([x0, -5.0, -1.0]) * chord
+    hi = np.array([x0 + 20.0, 5.0, 1.0]) * chord
     pos = rng.uniform(lo, hi, size=(n, 3))
     gamma = rng.normal(0.0, 1e-3, size=(n, 3))
     sigma = np.full(n, 0.02 * chord)

@@ -247,14 +247,23 @@ int fvx_tree_sample_pairs(fvx_tree* tree, int list, int max_pairs, void* X, floa
  * Replaces the PteraSoftware solver stages that HybridSolver runs around the
  * Biot-Savart calls (tests/experiment_hybrid_panel_particle.py:114-204 and the
  * PS step order of idea-stage/architecture_analysis.md:7-27).  A wing is a
- * vertex grid verts[(nc+1)*(ns+1)][3] (chordwise rows LE->TE, spanwise columns
- * left->right); P = nc*ns panels.  Motion: heave h(t) = heave_amp sin(omega t)
- * and flapping theta(t) = flap_amp sin(omega t) about the x axis through y0.
+ * vertex grid verts[(nc+1)*w][3] (chordwise rows LE->TE, spanwise columns
+ * left->right).  Several lifting surfaces with the same nc (PS airplanes with
+ * several wings, e.g. tests/benchmark_flapping.py:28-141) share one grid, their
+ * columns side by side, described by an FvxSurfaces layout: ring strip j spans
+ * vertex columns col[j] and col[j]+1, ring k = i ns + j, P = nc*ns panels, and
+ * vertex column c moves with surface surf[c], whose row of the motion table is
+ * (heave_amp, flap_amp, omega, y0): heave h(t) = heave_amp sin(omega t) and
+ * flapping theta(t) = flap_amp sin(omega t) about the x axis through the hinge
+ * line y = +-y0 of each half wing (mirrored).  col NULL: one surface, strip j
+ * spans columns j, j+1 (w = ns + 1); surf NULL: every column is surface 0.
+ * The layout struct is read on the host at each call; its arrays are device
+ * memory.
  *
  * kinematics: vertices at time t.
  * lattice: quarter-chord ring corners (br, fr, fl, bl: (P,3)), 3/4-chord
  *   collocation points, unit normals, areas, bound-leg centres and FR->FL
- *   vectors (P,3), trailing-edge back edge te_back (ns+1,3).
+ *   vectors (P,3), trailing-edge back edge te_back (w,3).
  * aic: AIC[b][i][j] = (unit ring j at collocation i) . n_i for n_systems
  *   systems stored back to back (expanded ring Biot-Savart fused with n).
  * rhs: rhs_i = -((u_inf - v_body) + v1 + v2) . n_i (v1, v2 may be NULL).
@@ -262,9 +271,10 @@ int fvx_tree_sample_pairs(fvx_tree* tree, int list, int max_pairs, void* X, floa
  *   systems, partial pivoting; a zero pivot sets status bit 2.
  * loads: Kutta-Joukowski force on each bound leg, rho (G_ij - G_i-1,j) (V x l),
  *   V = u_inf - v_body + v1 + v2 + v3, minus rho dG/dt A n (gamma_prev NULL:
- *   no unsteady term); writes CL and CDi (device scalars) and optionally the
+ *   no unsteady term); writes CL and CDi (device scalars) on the reference
+ *   area s_ref (<= 0: the sum of the panel areas) and optionally the
  *   per-panel forces.
- * wake_rings: ring-wake vertex lattice W[(R+1)*(ns+1)][3] with row strengths
+ * wake_rings: ring-wake vertex lattice W[(R+1)*w][3] with row strengths
  *   gam[R*ns] and row ages age[R] -> the ring layout of the Biot-Savart entries.
  * shed: W_new = [te_next; W_old + u_inf dt], gam_new = [TE ring strengths;
  *   gam_old], age_new = [0; age_old + dt].
@@ -273,34 +283,42 @@ int fvx_tree_sample_pairs(fvx_tree* tree, int list, int max_pairs, void* X, floa
  *   (experiment_hybrid_panel_particle.py:173-200); sigma = sigma_vdt
  *   (sigma_rule 0) or 1.3 x the ring's mean edge (sigma_rule 1); appended at
  *   *count (device int64), clipped at capacity (status bit 4). */
-int fvx_uvlm_kinematics(int64_t n_verts, const double* base, double heave_amp, double flap_amp,
-                        double omega, double y0, double t, double* out, void* stream);
-int fvx_uvlm_lattice(const double* verts, int nc, int ns, double* br, double* fr, double* fl,
-                     double* bl, double* colloc, double* normal, double* area,
+typedef struct FvxSurfaces {
+  int32_t ns;           /* ring strips per chordwise row */
+  int32_t w;            /* vertex columns */
+  const int32_t* col;   /* device (ns) or NULL */
+  const int32_t* surf;  /* device (w) or NULL */
+  const double* motion; /* device (4 per surface) */
+} FvxSurfaces;
+
+int fvx_uvlm_kinematics(int nc, const FvxSurfaces* s, const double* base, double t, double* out,
+                        void* stream);
+int fvx_uvlm_lattice(const double* verts, int nc, const FvxSurfaces* s, double* br, double* fr,
+                     double* fl, double* bl, double* colloc, double* normal, double* area,
                      double* leg_center, double* leg_vec, double* te_back, void* stream);
 int fvx_uvlm_aic(int n_systems, int P, const double* colloc, const double* normal,
                  const double* br, const double* fr, const double* fl, const double* bl,
                  double rc0, double nu, double* aic, void* stream);
-int fvx_uvlm_rhs(int P, const double* colloc, const double* normal, const double* v1,
-                 const double* v2, const double* u_inf, double heave_amp, double flap_amp,
-                 double omega, double y0, double t, double* rhs, void* stream);
+int fvx_uvlm_rhs(int nc, const FvxSurfaces* s, const double* colloc, const double* normal,
+                 const double* v1, const double* v2, const double* u_inf, double t, double* rhs,
+                 void* stream);
 int fvx_lu_solve_batched(int n_systems, int P, double* A, double* b, void* stream);
-int fvx_uvlm_loads(int nc, int ns, const double* gamma, const double* gamma_prev,
+int fvx_uvlm_loads(int nc, const FvxSurfaces* s, const double* gamma, const double* gamma_prev,
                    const double* leg_center, const double* leg_vec, const double* area,
                    const double* normal, const double* v1, const double* v2, const double* v3,
-                   const double* u_inf, double rho, double dt, double heave_amp, double flap_amp,
-                   double omega, double y0, double t, double* cl, double* cdi, double* force,
-                   void* stream);
-int fvx_uvlm_wake_rings(int R, int ns, const double* W, const double* gam, const double* age,
-                        double rc0, double* br, double* fr, double* fl, double* bl,
-                        double* strength, double* rc0s, double* ages, void* stream);
-int fvx_uvlm_shed(int R_old, int nc, int ns, const double* W_old, const double* gam_old,
-                  const double* age_old, const double* te_next, const double* gamma,
-                  const double* u_inf, double dt, double* W_new, double* gam_new,
-                  double* age_new, void* stream);
-int fvx_uvlm_convert(int R, int n_keep, int ns, const double* W, const double* gam,
-                     int sigma_rule, double sigma_vdt, int64_t capacity, int64_t* count,
-                     double* pos, double* alpha, double* sigma, double* age, void* stream);
+                   const double* u_inf, double rho, double dt, double t, double s_ref,
+                   double* cl, double* cdi, double* force, void* stream);
+int fvx_uvlm_wake_rings(int R, const FvxSurfaces* s, const double* W, const double* gam,
+                        const double* age, double rc0, double* br, double* fr, double* fl,
+                        double* bl, double* strength, double* rc0s, double* ages, void* stream);
+int fvx_uvlm_shed(int R_old, int nc, const FvxSurfaces* s, const double* W_old,
+                  const double* gam_old, const double* age_old, const double* te_next,
+                  const double* gamma, const double* u_inf, double dt, double* W_new,
+                  double* gam_new, double* age_new, void* stream);
+int fvx_uvlm_convert(int R, int n_keep, const FvxSurfaces* s, const double* W,
+                     const double* gam, int sigma_rule, double sigma_vdt, int64_t capacity,
+                     int64_t* count, double* pos, double* alpha, double* sigma, double* age,
+                     void* stream);
 
 /* ---- batched aeroelastic flutter sweep ------------------------------------------
  * Replaces the reference's per-airspeed AeroelasticSolver runs

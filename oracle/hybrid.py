@@ -29,6 +29,11 @@ overrides it, is followed:
   8. particle convection: VortexParticleField.advect_rk3 (particles.py:85)
      with U_inf and free-wake self-induction (:125-143), then relaxation.
 
+Several lifting surfaces (PteraSoftware's multi-wing airplanes, e.g.
+tests/benchmark_flapping.py:28-141) share one vertex grid: strip j spans
+vertex columns col[j], col[j]+1, each surface sheds its own wake strips from
+its own trailing-edge vertices, and each moves with its own kinematics.
+
 Every Biot-Savart evaluation goes through ``oracle.oracle`` (the C
 restatement pinned to the reference's golden vectors).
 """
@@ -44,9 +49,10 @@ class HybridOracle:
     def __init__(self, cfg: HybridConfig):
         self.cfg = cfg
         self.k = 0
-        ns = cfg.verts.shape[1] - 1
+        self.col = cfg.layout()[0]
+        ns = self.col.size
         self.ns = ns
-        L0 = lattice(cfg.kin.vertices(cfg.verts, 0.0))
+        L0 = lattice(cfg.vertices(0.0), self.col)
         self.W = L0.te_back[None].copy()        # wake vertex rows, newest first
         self.wgam = np.zeros((0, ns))
         self.wage = np.zeros(0)
@@ -64,10 +70,11 @@ class HybridOracle:
         if R == 0:
             e = np.zeros((0, 3))
             return e, e, e, e, np.zeros(0), np.zeros(0), np.zeros(0)
-        fl = W[:R, :-1].reshape(-1, 3)
-        fr = W[:R, 1:].reshape(-1, 3)
-        br = W[1:R + 1, 1:].reshape(-1, 3)
-        bl = W[1:R + 1, :-1].reshape(-1, 3)
+        a, b = self.col, self.col + 1
+        fl = W[:R, a].reshape(-1, 3)
+        fr = W[:R, b].reshape(-1, 3)
+        br = W[1:R + 1, b].reshape(-1, 3)
+        bl = W[1:R + 1, a].reshape(-1, 3)
         g = self.wgam.reshape(-1)
         rc = np.full(R * ns, self.cfg.rc0)
         ages = np.repeat(self.wage, ns)
@@ -86,8 +93,8 @@ class HybridOracle:
     def step(self):
         cfg = self.cfg
         t = self.k * cfg.dt
-        verts = cfg.kin.vertices(cfg.verts, t)
-        L = lattice(verts)
+        verts = cfg.vertices(t)
+        L = lattice(verts, self.col)
         P = L.colloc.shape[0]
         ones = np.ones(P)
         rc_b = np.full(P, cfg.rc0)
@@ -98,7 +105,7 @@ class HybridOracle:
         # 2-3. freestream, body motion, wake
         rings = self.wake_rings()
         Vw = self._induced(L.colloc, rings)
-        vb = cfg.kin.point_velocity(L.colloc, t)
+        vb = cfg.point_velocity(L.colloc, t)
         rhs = -np.einsum("ic,ic->i", (cfg.u_inf[None, :] - vb) + Vw, L.normal)
         # 4. strengths
         gam = np.linalg.solve(A, rhs)
@@ -106,7 +113,7 @@ class HybridOracle:
         Vl = self._induced(L.leg_center, rings)
         Vb = O.collapsed_velocities_from_ring_vortices(L.leg_center, L.br, L.fr, L.fl, L.bl, gam,
                                                        rc_b, None, None, cfg.nu)
-        vbl = cfg.kin.point_velocity(L.leg_center, t)
+        vbl = cfg.point_velocity(L.leg_center, t)
         V = (cfg.u_inf[None, :] - vbl) + (Vl + Vb)
         g2 = gam.reshape(L.nc, L.ns)
         geff = g2.copy()
@@ -119,11 +126,11 @@ class HybridOracle:
         V0 = cfg.speed
         eD = cfg.u_inf / V0
         eL = np.array([-eD[2], 0.0, eD[0]])
-        qS = 0.5 * cfg.rho * V0 ** 2 * L.area.sum()
+        qS = 0.5 * cfg.rho * V0 ** 2 * (L.area.sum() if cfg.s_ref is None else cfg.s_ref)
         self.cl.append(float(Ft @ eL / qS))
         self.cdi.append(float(Ft @ eD / qS))
         # 6. next wake
-        Ln = lattice(cfg.kin.vertices(cfg.verts, t + cfg.dt))
+        Ln = lattice(cfg.vertices(t + cfg.dt), self.col)
         Wc = self.W + cfg.u_inf * cfg.dt
         self.W = np.concatenate([Ln.te_back[None], Wc], axis=0)
         self.wgam = np.concatenate([g2[-1][None], self.wgam], axis=0)
@@ -137,8 +144,9 @@ class HybridOracle:
                     g = self.wgam[r, j]
                     if abs(g) < 1e-15:
                         continue
-                    fl, fr = self.W[r, j], self.W[r, j + 1]
-                    bl, br = self.W[r + 1, j], self.W[r + 1, j + 1]
+                    c = self.col[j]
+                    fl, fr = self.W[r, c], self.W[r, c + 1]
+                    bl, br = self.W[r + 1, c], self.W[r + 1, c + 1]
                     if cfg.sigma_rule == "edge":
                         s = 1.3 * 0.25 * (np.linalg.norm(fl - fr) + np.linalg.norm(bl - fl)
                                           + np.linalg.norm(br - bl) + np.linalg.norm(fr - br))

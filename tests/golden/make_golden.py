@@ -6,7 +6,8 @@ Run once, in a container that holds the FLUXVortex reference tree:
 
 The reference's particle code (``src/fluxvortex/kernel.py``,
 ``src/fluxvortex/particles.py``) and beam model (``src/fluxvortex/beam_fe.py``)
-import with NumPy/SciPy only and are called directly.  The reference's
+import with NumPy/SciPy only and are called directly; its recorded flapping
+histories (``figures/flapping_results.npz``) are copied as they are.  The reference's
 line-vortex code (``src/fluxvortex/warp_kernels.py``) needs NVIDIA Warp, which
 is not installed; this script registers a small pure-Python stand-in for the
 ``warp`` runtime (kernels run as Python functions, one call per thread id,
@@ -278,8 +279,22 @@ def make_beam(ref_root):
     print("  beam done", freqs[:4])
 
 
+def make_flapping(ref_root):
+    """The reference's recorded CL / CDi histories of its flapping benchmark
+    (figures/flapping_results.npz, written by tests/benchmark_flapping.py:251):
+    PteraSoftware's ring wake and the hybrid N_keep = 10 run, 129 steps.  These
+    are outputs of PteraSoftware geometry, so they pin the restated geometry
+    qualitatively (correlation, mean, amplitude), not to round-off."""
+    d = np.load(os.path.join(ref_root, "figures", "flapping_results.npz"), allow_pickle=False)
+    np.savez_compressed(os.path.join(HERE, "flapping_history.npz"),
+                        **{k: np.asarray(d[k], dtype=np.float64)
+                           for k in ("t_ps", "cl_ps", "cdi_ps", "t_h10", "cl_h10", "cdi_h10")})
+    print("  flapping done", d["cl_h10"].shape)
+
+
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     make_segments(root)
     make_particles(root)
     make_beam(root)
+    make_flapping(root)

@@ -60,15 +60,16 @@ def test_scratch_query_is_host_only():
     assert lib.fvx_particle_pairs_scratch_bytes(0, 0, 0, 10) == 0
 
 
-def test_flutter_structs_match_the_header_layout(tmp_path):
-    """The ctypes mirrors of FlutterParams / FlutterState have the C layout
+def test_structs_match_the_header_layout(tmp_path):
+    """The ctypes mirrors of FlutterParams / FlutterState / FvxSurfaces have the C layout
     (sizes and field offsets from a C program compiled against the header)."""
     import shutil
     import subprocess
     if shutil.which("gcc") is None:
         pytest.skip("no C compiler")
+    from fluxvortex_gb300._capi import Surfaces
     from fluxvortex_gb300.flutter import _Params, _State
-    fields = {"FlutterParams": _Params, "FlutterState": _State}
+    fields = {"FlutterParams": _Params, "FlutterState": _State, "FvxSurfaces": Surfaces}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fluxvortex_gb300.h"',
              'int main(void) {']
     for cname, cls in fields.items():

@@ -6,7 +6,7 @@ compensated particle sweeps: CL within 1e-4."""
 import numpy as np
 import pytest
 
-from fluxvortex_gb300.geometry import heaving_wing, static_wing
+from fluxvortex_gb300.geometry import flapping_aircraft, heaving_wing, static_wing
 from fluxvortex_gb300.hybrid import HybridStep
 from oracle.hybrid import HybridOracle
 from tests.conftest import rel_err
@@ -59,3 +59,57 @@ def test_heaving_wing_f32c_cl_within_1e4(cuda):
         g32.step()
     assert _hist_err(g32.cl, g64.cl) < 1e-4
     assert _hist_err(g32.cdi, g64.cdi) < 1e-3
+
+
+@pytest.mark.parametrize("flapping,free,stretch,steps", [("right", False, False, 12),
+                                                         ("both", True, False, 12),
+                                                         ("both", True, True, 8)])
+def test_flapping_aircraft_fp64(cuda, flapping, free, stretch, steps):
+    """Three surfaces (two main-wing halves with a gap between their roots, a
+    V-tail of 16 strips) in one grid: per-surface kinematics, per-surface
+    trailing edges and wake strips, conversion with the strip map.  With free
+    wake and stretching the converted particles (|alpha| up to ~80, sigma
+    ~0.2) amplify round-off by 10-30x per step once they act on each other
+    (1e-15 at step 5, 1e-8 at step 11), so that case stops at step 8."""
+    cfg = flapping_aircraft(n_keep=4, flapping=flapping, free_vpm=free, stretch=stretch)
+    g, o = _run(cfg, steps)
+    assert g.P == 192
+    assert g.field.np == o.p_pos.shape[0] == (steps - 4) * 32 * 4
+    assert _hist_err(g.cl, o.cl) < 1e-10
+    assert _hist_err(g.cdi, o.cdi) < 1e-10
+    assert rel_err(g.gamma.cpu().numpy(), o.gamma) < 1e-10
+    assert rel_err(g.field.positions, o.p_pos) < 1e-10
+    assert rel_err(g.field.gammas, o.p_gam) < 1e-10
+
+
+def test_snapshot_restore_resumes_bitwise(cuda, tmp_path):
+    """A device snapshot, and a host snapshot written with numpy.savez and read
+    back, both resume the step bitwise (FP64 direct sweeps and the panel side
+    reduce in a fixed order)."""
+    cfg = flapping_aircraft(n_keep=3, flapping="both", free_vpm=True, stretch=True)
+    g = HybridStep(cfg, precision="f64")
+    for _ in range(5):
+        g.step()
+    dev = g.snapshot()
+    host = g.snapshot(host=True)
+    flat = {k: v for k, v in host.items() if k != "field"}
+    flat.update({"field_" + k: v for k, v in host["field"].items()})
+    np.savez(tmp_path / "state.npz", **flat)
+    for _ in range(4):
+        g.step()
+    ref = (g.cl.copy(), g.cdi.copy(), g.field.positions, g.field.gammas, g.field.sigmas)
+    assert g.field.np > host["field"]["np"] > 0
+
+    def again(state):
+        g.restore(state)
+        for _ in range(4):
+            g.step()
+        got = (g.cl, g.cdi, g.field.positions, g.field.gammas, g.field.sigmas)
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b)
+
+    again(dev)
+    z = np.load(tmp_path / "state.npz")
+    st = {k: z[k] for k in z.files if not k.startswith("field_")}
+    st["field"] = {k[6:]: z[k] for k in z.files if k.startswith("field_")}
+    again(st)
