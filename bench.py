@@ -95,7 +95,7 @@ def parse():
                    help="particle self-sweeps: direct all-pairs, or the treecode with the "
                         "accepted cells per target particle (tree = m2p), as analytic local "
                         "expansions (m2l), or through the learned far-field operator")
-    p.add_argument("--leaf", type=int, default=48, help="treecode particles per leaf")
+    p.add_argument("--leaf", type=int, default=32, help="treecode particles per leaf")
     p.add_argument("--no-flutter", dest="flutter", action="store_false",
                    help="skip the batched flutter-sweep measurement")
     p.add_argument("--cl-steps", type=int, default=2,

@@ -880,10 +880,11 @@ __device__ __forceinline__ uint64_t fma(uint64_t a, uint64_t b, uint64_t c) {
 }
 }  // namespace x2
 
-// One source per row of the packed near tile, every value duplicated into
-// both halves of a 64-bit pair: {-x, -y}, {-z, s2}, {k2, ax}, {ay, az},
+// One row of the packed near tile: {-x, -y}, {-z, s2}, {k2, ax}, {ay, az},
 // {-ax, -ay}, {-az, -10.5 s2} (the negated values turn each cross-product
-// and stretching component into two fused multiply-adds).
+// and stretching component into two fused multiply-adds), each a 64-bit pair
+// whose halves hold either one source twice (two targets per lane) or two
+// consecutive sources (one target per lane, two source phases).
 struct NearX2 {
   ulonglong2 q[6];
 };
@@ -892,11 +893,12 @@ struct NearX2 {
 // core, velocity or stretching) with paired FP32 instructions; same formulas
 // as core_f32 + accumulate.
 template <int MODE>
-__device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, int nt, uint64_t TX,
-                                             uint64_t TY, uint64_t TZ, uint64_t GX, uint64_t GY,
-                                             uint64_t GZ, uint64_t* acc) {
+__device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, int nt, int stride,
+                                             uint64_t TX, uint64_t TY, uint64_t TZ, uint64_t GX,
+                                             uint64_t GY, uint64_t GZ, uint64_t* acc) {
   const uint64_t CM3 = x2::pack(-3.f, -3.f);
-  for (int k = 0; k < nt; ++k) {
+  for (int i = 0; i < nt; ++i) {
+    const int k = i * stride;
     const ulonglong2 q0 = tile[k].q[0], q1 = tile[k].q[1], q2 = tile[k].q[2],
                      q3 = tile[k].q[3];
     const uint64_t DX = x2::add(TX, q0.x), DY = x2::add(TY, q0.y), DZ = x2::add(TZ, q1.x);
@@ -959,17 +961,29 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
   const float3 cT = cell_center_rel(A.leaf_key[t], A.h);
   const int nno = A.near_off[t], nnc = A.near_cnt[t];
   const int fno = A.far_off[t], fnc = A.far_cnt[t];
+  // Source phases (paired path): a leaf of more than 32 targets takes two per
+  // lane, one in each half of the paired registers; a smaller one takes one
+  // per lane and gives each target G = 2, 4 or 8 workers -- the two halves
+  // times G/2 groups of lanes -- each summing every G-th source, so that the
+  // 64 paired slots stay busy for leaves of 32, 16 or 8 particles.
+  int G = 1;
+  if constexpr (PACKED) G = tcount > 32 ? 1 : (tcount > 16 ? 2 : (tcount > 8 ? 4 : 8));
+  const int gl = G == 1 ? kEvalThreads : 2 * kEvalThreads / G;  // lanes per group
+  const int grp = threadIdx.x / gl, tl = threadIdx.x - grp * gl;
 
   for (int chunk = 0; chunk < tcount; chunk += kEvalThreads * TPT) {
     float ox[TPT], oy[TPT], oz[TPT], gx[TPT], gy[TPT], gz[TPT];
     float hi[TPT][NC], lo[TPT][NC];
     bool act[TPT];
+    int kk[TPT];
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      const int k = chunk + threadIdx.x + j * kEvalThreads;
-      act[j] = k < tcount;
+      // G > 1: both slots hold the lane's one target; only group 0 writes it
+      const int k = G == 1 ? chunk + threadIdx.x + j * kEvalThreads : tl;
+      kk[j] = k;
+      act[j] = k < tcount && (G == 1 || (j == 0 && grp == 0));
       float4 p = make_float4(0.f, 0.f, 0.f, 0.f), g = p;
-      if (act[j]) {
+      if (k < tcount) {
         p = A.sp[tstart + k];
         if (NEED_TG) g = A.sg[tstart + k];
       }
@@ -983,7 +997,108 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
       for (int c = 0; c < NC; ++c) hi[j][c] = lo[j][c] = 0.f;
     }
     // near field: direct pairs with every near leaf
-    for (int q = 0; q < nnc; ++q) {
+    if constexpr (PACKED) {
+      // Tiles of up to kNearTile sources filled from up to 32 near leaves at
+      // a time: lane l holds near leaf l's start, count and exact centre
+      // difference c_T - c_S, a warp prefix sum places the leaves' sources
+      // one after another, and each staged source is stored relative to the
+      // target leaf's centre (the centre difference folded in while staging,
+      // the same two roundings as forming the target relative to the source
+      // leaf), so one tile mixes leaves and its barriers, loads and fold are
+      // paid per 128 sources instead of per near leaf.
+      const unsigned full = 0xffffffffu;
+      const int lane = threadIdx.x;
+      const uint64_t TX = x2::pack(ox[0], ox[TPT - 1]), TY = x2::pack(oy[0], oy[TPT - 1]),
+                     TZ = x2::pack(oz[0], oz[TPT - 1]);
+      const uint64_t GX = x2::pack(gx[0], gx[TPT - 1]), GY = x2::pack(gy[0], gy[TPT - 1]),
+                     GZ = x2::pack(gz[0], gz[TPT - 1]);
+      const int ng = G == 1 ? 1 : G / 2;
+      for (int q0 = 0; q0 < nnc; q0 += kEvalThreads) {
+        int mss = 0, msn = 0;
+        float mdx = 0.f, mdy = 0.f, mdz = 0.f;
+        if (q0 + lane < nnc) {
+          const int S = A.near_idx[nno + q0 + lane];
+          mss = A.leaf_start[S];
+          msn = A.leaf_count[S];
+          const float3 cS = cell_center_rel(A.leaf_key[S], A.h);
+          mdx = cT.x - cS.x;
+          mdy = cT.y - cS.y;
+          mdz = cT.z - cS.z;
+        }
+        int incl = msn;
+#pragma unroll
+        for (int o = 1; o < kEvalThreads; o <<= 1) {
+          const int v = __shfl_up_sync(full, incl, o);
+          if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(full, incl, kEvalThreads - 1);
+        const int excl = incl - msn;
+        for (int b0 = 0; b0 < total; b0 += kNearTile) {
+          const int nt = min(kNearTile, total - b0);
+          // rows: nt sources (G = 1), or ceil(nt/2) source pairs padded with
+          // zero-strength sources to a multiple of the G/2 lane groups
+          const int rows = G == 1 ? nt : ((nt + 1) / 2 + ng - 1) / ng * ng;
+          __syncthreads();
+          for (int r0 = 0; r0 < rows; r0 += kEvalThreads) {
+            const int k = r0 + lane;
+            float4 p[2], a[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int sk = G == 1 ? k : 2 * k + h;  // source of this half
+              const int g = b0 + (sk < nt ? sk : 0);
+              // near leaf of source g: the lanes whose inclusive prefix is <= g
+              int li = 0;
+#pragma unroll
+              for (int step = 16; step >= 1; step >>= 1) {
+                const int v = __shfl_sync(full, incl, li + step - 1);
+                if (v <= g) li += step;
+              }
+              const int lss = __shfl_sync(full, mss, li), lex = __shfl_sync(full, excl, li);
+              const float ldx = __shfl_sync(full, mdx, li), ldy = __shfl_sync(full, mdy, li),
+                          ldz = __shfl_sync(full, mdz, li);
+              p[h] = make_float4(0.f, 0.f, 0.f, 1.f);
+              a[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+              if (k < rows && sk < nt) {
+                const float4 pv = A.sp[lss + g - lex];
+                p[h] = make_float4(pv.x - ldx, pv.y - ldy, pv.z - ldz, pv.w);
+                a[h] = A.sa[lss + g - lex];
+              }
+            }
+            if (k < rows) {
+              NearX2 e;
+              e.q[0] = make_ulonglong2(x2::pack(-p[0].x, -p[1].x), x2::pack(-p[0].y, -p[1].y));
+              e.q[1] = make_ulonglong2(x2::pack(-p[0].z, -p[1].z), x2::pack(p[0].w, p[1].w));
+              e.q[2] = make_ulonglong2(x2::pack(a[0].w, a[1].w), x2::pack(a[0].x, a[1].x));
+              e.q[3] = make_ulonglong2(x2::pack(a[0].y, a[1].y), x2::pack(a[0].z, a[1].z));
+              e.q[4] = make_ulonglong2(x2::pack(-a[0].x, -a[1].x), x2::pack(-a[0].y, -a[1].y));
+              e.q[5] = make_ulonglong2(x2::pack(-a[0].z, -a[1].z),
+                                       x2::pack(-10.5f * p[0].w, -10.5f * p[1].w));
+              s_x2[k] = e;
+            }
+          }
+          __syncthreads();
+          uint64_t acc2[3] = {0ull, 0ull, 0ull};
+          near_tile_x2<MODE>(s_x2 + (G == 1 ? 0 : grp), rows / ng, ng, TX, TY, TZ, GX, GY, GZ,
+                             acc2);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            float a0, a1;
+            x2::unpack(acc2[c], a0, a1);
+            if (G == 1) {
+              fold(hi[0][c], lo[0][c], a0);
+              fold(hi[TPT - 1][c], lo[TPT - 1][c], a1);
+            } else {
+              // the target's G partial sums: the two halves, then the groups
+              float v = a0 + a1;
+              if (G == 8) v += __shfl_xor_sync(full, v, 8);
+              if (G >= 4) v += __shfl_xor_sync(full, v, 16);
+              fold(hi[0][c], lo[0][c], v);
+            }
+          }
+        }
+      }
+    }
+    for (int q = 0; q < (PACKED ? 0 : nnc); ++q) {
       const int S = A.near_idx[nno + q];
       const int ss = A.leaf_start[S], sn = A.leaf_count[S];
       const float3 cS = cell_center_rel(A.leaf_key[S], A.h);
@@ -994,38 +1109,6 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
         tx[j] = ox[j] + dcx;
         ty[j] = oy[j] + dcy;
         tz[j] = oz[j] + dcz;
-      }
-      if constexpr (PACKED) {
-        const uint64_t TX = x2::pack(tx[0], tx[TPT - 1]), TY = x2::pack(ty[0], ty[TPT - 1]),
-                       TZ = x2::pack(tz[0], tz[TPT - 1]);
-        const uint64_t GX = x2::pack(gx[0], gx[TPT - 1]), GY = x2::pack(gy[0], gy[TPT - 1]),
-                       GZ = x2::pack(gz[0], gz[TPT - 1]);
-        for (int k0 = 0; k0 < sn; k0 += kNearTile) {
-          const int nt = min(kNearTile, sn - k0);
-          __syncthreads();
-          for (int k = threadIdx.x; k < nt; k += kEvalThreads) {
-            const float4 pv = A.sp[ss + k0 + k], av = A.sa[ss + k0 + k];
-            NearX2 e;
-            e.q[0] = make_ulonglong2(x2::pack(-pv.x, -pv.x), x2::pack(-pv.y, -pv.y));
-            e.q[1] = make_ulonglong2(x2::pack(-pv.z, -pv.z), x2::pack(pv.w, pv.w));
-            e.q[2] = make_ulonglong2(x2::pack(av.w, av.w), x2::pack(av.x, av.x));
-            e.q[3] = make_ulonglong2(x2::pack(av.y, av.y), x2::pack(av.z, av.z));
-            e.q[4] = make_ulonglong2(x2::pack(-av.x, -av.x), x2::pack(-av.y, -av.y));
-            e.q[5] = make_ulonglong2(x2::pack(-av.z, -av.z), x2::pack(-10.5f * pv.w, -10.5f * pv.w));
-            s_x2[k] = e;
-          }
-          __syncthreads();
-          uint64_t acc2[3] = {0ull, 0ull, 0ull};
-          near_tile_x2<MODE>(s_x2, nt, TX, TY, TZ, GX, GY, GZ, acc2);
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            float a0, a1;
-            x2::unpack(acc2[c], a0, a1);
-            fold(hi[0][c], lo[0][c], a0);
-            fold(hi[TPT - 1][c], lo[TPT - 1][c], a1);
-          }
-        }
-        continue;
       }
       for (int k0 = 0; k0 < sn; k0 += kNearTile) {
         const int nt = min(kNearTile, sn - k0);
@@ -1121,7 +1204,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
       if (!act[j]) continue;
-      const int i = A.perm[tstart + chunk + threadIdx.x + j * kEvalThreads];
+      const int i = A.perm[tstart + kk[j]];
 #pragma unroll
       for (int c = 0; c < NA; ++c)
         A.out_a[static_cast<int64_t>(i) * NA + c] =
@@ -1406,12 +1489,13 @@ void launch_eval_tpt(int mode, int nleaf, const tree::EvalArgs& A, cudaStream_t 
 
 template <int KERNEL>
 void launch_eval(int mode, int nleaf, int n, const tree::EvalArgs& A, cudaStream_t s) {
-  // Two targets per thread (paired f32x2 arithmetic for Winckelmans velocity
-  // and stretching) once leaves average more than one warp of targets; at
-  // fewer, one target per thread wastes fewer lanes.
+  // Winckelmans velocity and stretching: the paired f32x2 kernel, whose
+  // source phases keep small leaves' slots busy.  Otherwise two targets per
+  // thread once leaves average more than ~40 particles; at fewer, one target
+  // per thread wastes fewer lanes.
   const bool paired = KERNEL == FVX_KERNEL_WINCKELMANS &&
                       (mode == FVX_PAIR_VELOCITY || mode == FVX_PAIR_STRETCH);
-  if (n <= (paired ? 32 : 40) * nleaf)
+  if (!paired && n <= 40 * nleaf)
     launch_eval_tpt<KERNEL, 1>(mode, nleaf, A, s);
   else
     launch_eval_tpt<KERNEL, 2>(mode, nleaf, A, s);
