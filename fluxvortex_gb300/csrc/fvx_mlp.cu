@@ -645,18 +645,41 @@ __global__ void __launch_bounds__(256) m2l_pairs_kernel(int npairs, const int* _
     for (int q = 0; q < NOUT; ++q) a[q] = 0.f;
   }
   const int my = act_row ? leaf : -1 - lane;
-  const int up = __shfl_up_sync(0xffffffffu, my, 1);
-  const bool head = act_row && (lane == 0 || up != my);
+  float x[32];
 #pragma unroll
-  for (int c = 0; c < NOUT; ++c) {
-    float x = a[c] * (c < 3 ? sc.s2 : (c < 12 ? sc.s3 : sc.s4));
+  for (int c = 0; c < 32; ++c)
+    x[c] = c < NOUT ? a[c] * (c < 3 ? sc.s2 : (c < 12 ? sc.s3 : sc.s4)) : 0.f;
+  if (__all_sync(0xffffffffu, my == __shfl_sync(0xffffffffu, my, 0))) {
+    // one target for the whole warp (pairs are ordered by target, runs are
+    // long): reduce-scatter by recursive halving, 31 shuffles for the 32
+    // columns; lane c ends with the warp's sum of column c
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const float o = __shfl_down_sync(0xffffffffu, x, off);
-      const int ol = __shfl_down_sync(0xffffffffu, my, off);
-      if (lane + off < 32 && ol == my) x += o;
+    for (int off = 16; off >= 1; off >>= 1) {
+      const bool upper = (lane & off) != 0;
+#pragma unroll
+      for (int j = 0; j < off; ++j) {
+        const float send = upper ? x[j] : x[j + off];
+        const float keep = upper ? x[j + off] : x[j];
+        x[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+      }
     }
-    if (head) atomicAdd(leaf_local + static_cast<int64_t>(leaf) * OUT + c, x);
+    if (lane < NOUT) atomicAdd(leaf_local + static_cast<int64_t>(leaf) * OUT + lane, x[0]);
+  } else {
+    // runs of equal targets inside the warp: segmented sums to each run's
+    // first lane
+    const int up = __shfl_up_sync(0xffffffffu, my, 1);
+    const bool head = act_row && (lane == 0 || up != my);
+#pragma unroll
+    for (int c = 0; c < NOUT; ++c) {
+      float y = x[c];
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const float o = __shfl_down_sync(0xffffffffu, y, off);
+        const int ol = __shfl_down_sync(0xffffffffu, my, off);
+        if (lane + off < 32 && ol == my) y += o;
+      }
+      if (head) atomicAdd(leaf_local + static_cast<int64_t>(leaf) * OUT + c, y);
+    }
   }
 }
 

@@ -203,83 +203,116 @@ __global__ void rhs_kernel(int P, FvxSurfaces sf, const double* __restrict__ col
 
 // In-place solve of A x = b for B systems (A: B x P x P row-major, b: B x P);
 // Gaussian elimination with partial pivoting (first maximum wins).  x -> b.
-__global__ void __launch_bounds__(256) lu_solve_kernel(int P, double* __restrict__ A,
-                                                       double* __restrict__ b) {
+// One CTA of kLuThreads per system: warp-shuffle pivot search, the pivot row
+// and the multipliers cached in shared memory, the trailing update over 32
+// warps of rows with the lanes along the columns, then a column-oriented back
+// substitution with one barrier per column.
+constexpr int kLuThreads = 1024;
+constexpr int kLuMaxP = 2048;
+
+__global__ void __launch_bounds__(kLuThreads) lu_solve_kernel(int P, double* __restrict__ A,
+                                                              double* __restrict__ b) {
   const int64_t PP = static_cast<int64_t>(P) * P;
   double* a = A + blockIdx.x * PP;
   double* x = b + static_cast<int64_t>(blockIdx.x) * P;
-  __shared__ double s_val[256];
-  __shared__ int s_idx[256];
+  __shared__ double s_row[kLuMaxP];
+  __shared__ double s_l[kLuMaxP];
+  __shared__ double s_wv[kLuThreads / 32];
+  __shared__ int s_wi[kLuThreads / 32];
   __shared__ int s_piv;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int k = 0; k < P; ++k) {
-    // pivot search in column k, rows k..P-1
+    // pivot search in column k, rows k..P-1: max |a|, the first row on ties
     double best = -1.0;
     int bi = P;
-    for (int r = k + threadIdx.x; r < P; r += blockDim.x) {
+    for (int r = k + tid; r < P; r += kLuThreads) {
       const double v = fabs(a[static_cast<int64_t>(r) * P + k]);
       if (v > best) {
         best = v;
         bi = r;
       }
     }
-    s_val[threadIdx.x] = best;
-    s_idx[threadIdx.x] = bi;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double v2 = __shfl_down_sync(0xffffffffu, best, o);
+      const int i2 = __shfl_down_sync(0xffffffffu, bi, o);
+      if (v2 > best || (v2 == best && i2 < bi)) {
+        best = v2;
+        bi = i2;
+      }
+    }
+    if (lane == 0) {
+      s_wv[warp] = best;
+      s_wi[warp] = bi;
+    }
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) {
-        const double v2 = s_val[threadIdx.x + s];
-        const int i2 = s_idx[threadIdx.x + s];
-        if (v2 > s_val[threadIdx.x] || (v2 == s_val[threadIdx.x] && i2 < s_idx[threadIdx.x])) {
-          s_val[threadIdx.x] = v2;
-          s_idx[threadIdx.x] = i2;
+    if (warp == 0) {
+      best = s_wv[lane];
+      bi = s_wi[lane];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double v2 = __shfl_down_sync(0xffffffffu, best, o);
+        const int i2 = __shfl_down_sync(0xffffffffu, bi, o);
+        if (v2 > best || (v2 == best && i2 < bi)) {
+          best = v2;
+          bi = i2;
         }
       }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      s_piv = s_idx[0];
-      if (!(s_val[0] > 0.0)) flag_status(kStatusNonFinite);
+      if (lane == 0) {
+        s_piv = bi;
+        if (!(best > 0.0)) flag_status(kStatusNonFinite);
+      }
     }
     __syncthreads();
     const int piv = s_piv;
-    if (piv != k && piv < P) {
-      for (int c = threadIdx.x; c < P; c += blockDim.x) {
-        const double t = a[static_cast<int64_t>(k) * P + c];
-        a[static_cast<int64_t>(k) * P + c] = a[static_cast<int64_t>(piv) * P + c];
-        a[static_cast<int64_t>(piv) * P + c] = t;
+    // swap rows k and piv (columns k.. only change from here on, but the
+    // whole row is swapped as the unblocked form does) and cache row k
+    for (int c = tid; c < P; c += kLuThreads) {
+      double rk = a[static_cast<int64_t>(k) * P + c];
+      if (piv != k && piv < P) {
+        const double rp = a[static_cast<int64_t>(piv) * P + c];
+        a[static_cast<int64_t>(piv) * P + c] = rk;
+        a[static_cast<int64_t>(k) * P + c] = rp;
+        rk = rp;
       }
-      if (threadIdx.x == 0) {
-        const double t = x[k];
-        x[k] = x[piv];
-        x[piv] = t;
-      }
+      s_row[c] = rk;
+    }
+    if (tid == 0 && piv != k && piv < P) {
+      const double t = x[k];
+      x[k] = x[piv];
+      x[piv] = t;
     }
     __syncthreads();
-    const double akk = a[static_cast<int64_t>(k) * P + k];
-    // eliminate below: one warp per row, lanes over columns
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int r = k + 1 + warp; r < P; r += nw) {
+    const double akk = s_row[k];
+    const double xk = x[k];
+    // multipliers of the rows below
+    for (int r = k + 1 + tid; r < P; r += kLuThreads) {
       const double l = a[static_cast<int64_t>(r) * P + k] / akk;
-      for (int c = k + 1 + lane; c < P; c += 32)
-        a[static_cast<int64_t>(r) * P + c] -= l * a[static_cast<int64_t>(k) * P + c];
-      if (lane == 0) x[r] -= l * x[k];
+      s_l[r] = l;
+      x[r] -= l * xk;
+    }
+    __syncthreads();
+    // trailing update a_rc -= l_r a_kc over rows r > k (warps), columns c > k
+    // (lanes, coalesced); the rows of a warp are independent, so their loads
+    // overlap
+    for (int r = k + 1 + warp; r < P; r += kLuThreads / 32) {
+      const double l = s_l[r];
+      double* ar = a + static_cast<int64_t>(r) * P;
+      for (int c = k + 1 + lane; c < P; c += 32) ar[c] -= l * s_row[c];
     }
     __syncthreads();
   }
-  // back substitution, one row at a time with a block reduction
+  // back substitution by columns: x_k /= a_kk, then x_r -= a_rk x_k for r < k
+  for (int r = tid; r < P; r += kLuThreads) s_l[r] = x[r];
+  __syncthreads();
   for (int k = P - 1; k >= 0; --k) {
-    double s = 0.0;
-    for (int c = k + 1 + threadIdx.x; c < P; c += blockDim.x)
-      s += a[static_cast<int64_t>(k) * P + c] * x[c];
-    s_val[threadIdx.x] = s;
+    const double xk = s_l[k] / a[static_cast<int64_t>(k) * P + k];
+    for (int r = tid; r < k; r += kLuThreads) s_l[r] -= a[static_cast<int64_t>(r) * P + k] * xk;
     __syncthreads();
-    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
-      if (threadIdx.x < st) s_val[threadIdx.x] += s_val[threadIdx.x + st];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) x[k] = (x[k] - s_val[0]) / a[static_cast<int64_t>(k) * P + k];
+    if (tid == 0) s_l[k] = xk;
     __syncthreads();
   }
+  for (int r = tid; r < P; r += kLuThreads) x[r] = s_l[r];
 }
 
 struct LoadsArgs {
@@ -564,8 +597,10 @@ int fvx_uvlm_rhs(int nc, const FvxSurfaces* s, const double* colloc, const doubl
 }
 
 int fvx_lu_solve_batched(int n_systems, int P, double* A, double* b, void* stream) {
-  FVX_ARG_CHECK(n_systems >= 1 && P >= 1 && A && b, "bad solve arguments");
-  fvx::lu_solve_kernel<<<n_systems, 256, 0, static_cast<cudaStream_t>(stream)>>>(P, A, b);
+  FVX_ARG_CHECK(n_systems >= 1 && P >= 1 && P <= fvx::kLuMaxP && A && b,
+                "bad solve arguments (P must be 1..%d)", fvx::kLuMaxP);
+  fvx::lu_solve_kernel<<<n_systems, fvx::kLuThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      P, A, b);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }

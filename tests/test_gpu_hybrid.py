@@ -113,3 +113,37 @@ def test_snapshot_restore_resumes_bitwise(cuda, tmp_path):
     st = {k: z[k] for k in z.files if not k.startswith("field_")}
     st["field"] = {k[6:]: z[k] for k in z.files if k.startswith("field_")}
     again(st)
+
+
+@pytest.mark.parametrize("P,nsys", [(1, 1), (7, 3), (120, 2), (192, 3), (600, 1)])
+def test_lu_solve_batched_matches_numpy(cuda, P, nsys):
+    """The batched FP64 solve (partial pivoting) against numpy.linalg.solve on
+    diagonally weak random systems whose first pivot needs a row swap."""
+    import torch
+    from fluxvortex_gb300 import _capi
+    rng = np.random.default_rng(P)
+    A = rng.standard_normal((nsys, P, P)) + 0.5 * np.eye(P)
+    if P > 1:
+        A[:, 0, 0] = 0.0                           # forces a swap at k = 0
+    b = rng.standard_normal((nsys, P))
+    x = np.stack([np.linalg.solve(A[i], b[i]) for i in range(nsys)])
+    dA = torch.as_tensor(A, device="cuda").contiguous()
+    db = torch.as_tensor(b, device="cuda").contiguous()
+    _capi.check(_capi.load().fvx_lu_solve_batched(nsys, P, dA.data_ptr(), db.data_ptr(), None))
+    got = db.cpu().numpy()
+    assert _capi.status_read_and_clear() == 0
+    assert np.abs(got - x).max() <= 1e-9 * np.abs(x).max()
+
+
+def test_lu_solve_flags_a_singular_system_and_refuses_oversize(cuda):
+    import torch
+    from fluxvortex_gb300 import _capi
+    lib = _capi.load()
+    A = torch.zeros((1, 4, 4), dtype=torch.float64, device="cuda")
+    b = torch.ones((1, 4), dtype=torch.float64, device="cuda")
+    _capi.check(lib.fvx_lu_solve_batched(1, 4, A.data_ptr(), b.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert _capi.status_read_and_clear() != 0
+    big = torch.zeros(1, dtype=torch.float64, device="cuda")
+    with pytest.raises(_capi.FvxError):
+        _capi.check(lib.fvx_lu_solve_batched(1, 4096, big.data_ptr(), big.data_ptr(), None))
