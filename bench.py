@@ -554,6 +554,7 @@ def run_ours(args, rank, world):
             f._pos[:n].copy_(hp, non_blocking=True)
             f._gamma[:n].copy_(hg, non_blocking=True)
             f._sigma[:n].copy_(hs, non_blocking=True)
+            f.positions_changed()
             step.run()
             m = f.np
             kk = step.hs.k - 1

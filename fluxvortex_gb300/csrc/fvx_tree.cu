@@ -1445,6 +1445,20 @@ struct fvx_tree {
   int n_parent_pairs = 0;
   fvx::DevBuf lrn_meta, lrn_leaf, lrn_cell, leaf_local;
   int n_learned = 0;
+  // the structure of the last full build (grid, sort, cells, interaction
+  // lists), reused by a sweep hinted to have the same positions
+  bool reuse_next = false;
+  struct Structure {
+    bool valid = false;
+    const double* pos = nullptr;
+    int n = 0, leaf_target = 0, far_method = 0;
+    double theta = 0.0, theta_l = 0.0;
+    int L = 0, total_cells = 0, nleaf = 0;
+    double h = 0.0, origin[3] = {0.0, 0.0, 0.0};
+    int cap[11] = {}, base[12] = {}, ncells[11] = {};
+    const int* perm = nullptr;
+    int64_t near_total = 0, far_total = 0, lrn_total = 0, par_total = 0;
+  } st;
   // the last sweep's tree, for sampling training pairs
   int last_L = 0, last_nleaf = 0;
   double last_h = 0.0;
@@ -1551,6 +1565,44 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
                     (mode != FVX_PAIR_VELOCITY_STRETCH || out_b),
                 "null array");
   int rc;
+  // A sweep hinted to have the last full build's positions (same array,
+  // count, opening angles, leaf size and far-field method) reuses its grid,
+  // sort, cells and interaction lists; strengths, cores and target strengths
+  // are gathered anew and the moments, expansions and evaluation recomputed.
+  auto& ST = T->st;
+  const bool reuse = T->reuse_next && ST.valid && ST.pos == pos && ST.n == n &&
+                     ST.theta == theta && ST.leaf_target == leaf_target &&
+                     ST.far_method == T->far_method && ST.theta_l == T->theta_l;
+  T->reuse_next = false;
+  int L = 0, total_cells = 0, nleaf = 0;
+  double h = 0.0, origin[3] = {0.0, 0.0, 0.0};
+  int cap[11] = {}, base[12] = {}, ncells[11] = {};
+  const int* perm = nullptr;
+  int* lvb = nullptr;
+  auto level = [&](int l) {
+    Level v;
+    v.start = lvb + base[l];
+    v.count = lvb + total_cells + base[l];
+    v.key = reinterpret_cast<uint32_t*>(lvb + 2 * total_cells + base[l]);
+    v.child_lo = lvb + 3 * total_cells + base[l];
+    v.child_hi = lvb + 4 * total_cells + base[l];
+    return v;
+  };
+  if (reuse) {
+    L = ST.L;
+    total_cells = ST.total_cells;
+    nleaf = ST.nleaf;
+    h = ST.h;
+    for (int c = 0; c < 3; ++c) origin[c] = ST.origin[c];
+    for (int l = 0; l < 11; ++l) {
+      cap[l] = ST.cap[l];
+      ncells[l] = ST.ncells[l];
+    }
+    for (int l = 0; l < 12; ++l) base[l] = ST.base[l];
+    perm = ST.perm;
+    lvb = P<int>(T->levels);
+  } else {
+  ST.valid = false;
   // 1. bounding box -> grid
   const int nbb = 256;
   if ((rc = grow(T->bbox, sizeof(double) * (6 * nbb + 7)))) return rc;
@@ -1569,11 +1621,8 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   // a non-finite position would otherwise collapse the grid (all keys in one
   // cell) and turn the sweep into an all-pairs sum on a few CTAs
   FVX_ARG_CHECK(nbad == 0, "treecode: %u particles with non-finite positions", nbad);
-  int L;
-  double h, origin[3];
   grid_params(lohi, lohi + 3, n, leaf_target, &L, &h, origin);
   // level capacities and bases
-  int cap[11], base[12];
   cap[L] = n;
   for (int l = L - 1; l >= 0; --l) {
     const int64_t full = int64_t(1) << (3 * l);
@@ -1581,7 +1630,7 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   }
   base[0] = 0;
   for (int l = 0; l <= L; ++l) base[l + 1] = base[l] + cap[l];
-  const int total_cells = base[L + 1];
+  total_cells = base[L + 1];
   const int nblk = (n + kSortItems - 1) / kSortItems;
   if ((rc = grow(T->keys0, 4 * size_t(n))) || (rc = grow(T->keys1, 4 * size_t(n))) ||
       (rc = grow(T->idx0, 4 * size_t(n))) || (rc = grow(T->idx1, 4 * size_t(n))) ||
@@ -1617,18 +1666,9 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
     ib = ti;
   }
   const uint32_t* keys = ka;  // sorted
-  const int* perm = ia;
+  perm = ia;
   // 3. cells: leaves from particles, parents from children
-  int* lvb = P<int>(T->levels);
-  auto level = [&](int l) {
-    Level v;
-    v.start = lvb + base[l];
-    v.count = lvb + total_cells + base[l];
-    v.key = reinterpret_cast<uint32_t*>(lvb + 2 * total_cells + base[l]);
-    v.child_lo = lvb + 3 * total_cells + base[l];
-    v.child_hi = lvb + 4 * total_cells + base[l];
-    return v;
-  };
+  lvb = P<int>(T->levels);
   int* ncells_d = P<int>(T->counts);
   int* flag = P<int>(T->flags);
   int* cid = P<int>(T->cid);
@@ -1656,10 +1696,13 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
     parent_counts_kernel<<<(cap[l] + 255) / 256, 256, 0, s>>>(ch, par, ncells_d + l);
     FVX_LAUNCH_CHECK();
   }
-  int ncells[11];
   FVX_CUDA_TRY(cudaMemcpyAsync(ncells, ncells_d, sizeof(int) * (L + 1), cudaMemcpyDeviceToHost, s));
   FVX_CUDA_TRY(cudaStreamSynchronize(s));
-  const int nleaf = ncells[L];
+  nleaf = ncells[L];
+  }
+  int* ncells_d = P<int>(T->counts);
+  int* cid = P<int>(T->cid);
+  Level leaves = level(L);
   // 4. sorted FP32 records
   Grid g{origin[0], origin[1], origin[2], h, L};
   float4 *sp = P<float4>(T->sp), *sa = P<float4>(T->sa), *sg = P<float4>(T->sg);
@@ -1734,6 +1777,13 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   int* par_cnt = dual ? P<int>(T->dual_meta) : nullptr;
   int* par_off = dual ? par_cnt + npar : nullptr;
   int* leaf_parent = dual ? par_off + npar : nullptr;
+  int64_t near_total = 0, far_total = 0, lrn_total = 0, par_total = 0;
+  if (reuse) {
+    near_total = ST.near_total;
+    far_total = ST.far_total;
+    lrn_total = ST.lrn_total;
+    par_total = ST.par_total;
+  } else {
   FVX_CUDA_TRY(cudaMemsetAsync(ovf, 0, 24, s));
   DualLists D{};
   if (dual) {
@@ -1772,15 +1822,15 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   FVX_CUDA_TRY(cudaMemcpyAsync(&tail[2], far_cnt + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
   FVX_CUDA_TRY(cudaMemcpyAsync(&tail[3], far_off + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
   FVX_CUDA_TRY(cudaStreamSynchronize(s));
-  const int64_t near_total = int64_t(tail[0]) + tail[1];
-  const int64_t far_total = int64_t(tail[2]) + tail[3];
+  near_total = int64_t(tail[0]) + tail[1];
+  far_total = int64_t(tail[2]) + tail[3];
   FVX_ARG_CHECK(near_total < (int64_t(1) << 31) && far_total < (int64_t(1) << 31),
                 "interaction lists too long");
   if ((rc = grow(T->near_list, 4 * size_t(near_total + 1))) ||
       (rc = grow(T->far_list, 4 * size_t(far_total + 1))))
     return rc;
-  const int64_t lrn_total = int64_t(ltail[0]) + ltail[1];
-  const int64_t par_total = int64_t(ltail[2]) + ltail[3];
+  lrn_total = int64_t(ltail[0]) + ltail[1];
+  par_total = int64_t(ltail[2]) + ltail[3];
   FVX_ARG_CHECK(lrn_total < (int64_t(1) << 31) && par_total < (int64_t(1) << 31),
                 "local-expansion pair list too long");
   if (learned) {
@@ -1814,6 +1864,29 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
         static_cast<int>(near_total), static_cast<int>(far_total), ovf, LL);
   }
   FVX_LAUNCH_CHECK();
+  ST.pos = pos;
+  ST.n = n;
+  ST.leaf_target = leaf_target;
+  ST.far_method = T->far_method;
+  ST.theta = theta;
+  ST.theta_l = T->theta_l;
+  ST.L = L;
+  ST.total_cells = total_cells;
+  ST.nleaf = nleaf;
+  ST.h = h;
+  for (int c = 0; c < 3; ++c) ST.origin[c] = origin[c];
+  for (int l = 0; l < 11; ++l) {
+    ST.cap[l] = cap[l];
+    ST.ncells[l] = ncells[l];
+  }
+  for (int l = 0; l < 12; ++l) ST.base[l] = base[l];
+  ST.perm = perm;
+  ST.near_total = near_total;
+  ST.far_total = far_total;
+  ST.lrn_total = lrn_total;
+  ST.par_total = par_total;
+  ST.valid = true;
+  }
   // 7. evaluation
   EvalArgs A;
   A.h = static_cast<float>(h);
@@ -1991,6 +2064,12 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
 }  // namespace fvx
 
 extern "C" {
+
+int fvx_tree_hint_same_positions(fvx_tree* T) {
+  FVX_ARG_CHECK(T != nullptr, "null tree handle");
+  T->reuse_next = true;
+  return FVX_OK;
+}
 
 int fvx_tree_create(fvx_tree** out) {
   FVX_ARG_CHECK(out != nullptr, "null handle pointer");

@@ -229,6 +229,7 @@ class HybridStep:
                 self.count.data_ptr(), f._pos.data_ptr(), f._gamma.data_ptr(),
                 f._sigma.data_ptr(), f._age.data_ptr(), st))
             f.np = int(self.count.item())
+            f.positions_changed()
             R = cfg.n_keep
         self.R = R
         # 8. particles

@@ -46,6 +46,10 @@ class VortexParticleField:
         self._u, self._S, self._w = z3(), z3(), z3()
         self._scratch = torch.empty(1, dtype=torch.uint8, device=self.device)
         self.np = 0
+        # bumped whenever positions (or the count) change: a tree sweep at
+        # the positions of the tree's last build reuses its structure
+        self._pos_version = 0
+        self._tree_version = -1
         self._lib = _capi.load()
         # Optional profiling hook: when a list, every sweep appends
         # (mode, kernel, n_targets, n_sources, start_event, end_event).
@@ -96,6 +100,7 @@ class VortexParticleField:
         self._sigma[sl] = t(sigmas).reshape(n)
         self._age[sl] = 0.0
         self.np += n
+        self._pos_version += 1
 
     @property
     def positions(self):
@@ -132,6 +137,11 @@ class VortexParticleField:
         for k in ("pos", "gamma", "sigma", "age"):
             getattr(self, "_" + k)[:n].copy_(torch.as_tensor(st[k]), non_blocking=False)
         self.np = n
+        self._pos_version += 1
+
+    def positions_changed(self):
+        """Call after writing the position buffer directly (``_pos``)."""
+        self._pos_version += 1
 
     # ---- sweeps ----------------------------------------------------------------
     def _stream(self):
@@ -161,7 +171,9 @@ class VortexParticleField:
                     self.validate_samples if self._validate_next else 0, self.validate_tol)
             stats = self.tree.sweep(mode, kernel or self.kernel, self._pos, self._gamma,
                                     self._sigma, n, out_a, out_b, tgt_gamma=tgt_gamma,
-                                    check=ev is not None)
+                                    check=ev is not None,
+                                    same_positions=self._tree_version == self._pos_version)
+            self._tree_version = self._pos_version
             if ev is not None:
                 ev[1].record()
                 self.sweep_events.append((mode, "tree/" + (kernel or self.kernel), n_tgt, n,
@@ -231,6 +243,7 @@ class VortexParticleField:
                 n, a, b, dt, u_inf_host.ctypes.data, self._u.data_ptr() if free_wake else None,
                 None if extra is None else extra.data_ptr(), self._pos.data_ptr(),
                 self._rk_X.data_ptr(), st))
+            self._pos_version += 1
             if stretch:
                 self._sweep(_capi.PAIR_STRETCH, self._pos, self._gamma, n, self._S)
                 _capi.check(lib.fvx_vpm_stage_strength(

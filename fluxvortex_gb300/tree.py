@@ -44,10 +44,14 @@ class TreeSweeper:
             pass
 
     def sweep(self, mode, kernel, pos, alpha, sigma, n, out_a, out_b=None, tgt_gamma=None,
-              stream=None, check=False):
-        """Device tensors (FP64 AoS) in, FP64 outputs written in place."""
+              stream=None, check=False, same_positions=False):
+        """Device tensors (FP64 AoS) in, FP64 outputs written in place.
+        ``same_positions``: the positions are those of the last full build
+        (the tree structure is reused; see fvx_tree_hint_same_positions)."""
         st = stream if stream is not None else torch.cuda.current_stream(pos.device).cuda_stream
         stats = self.stats.ctypes.data if check else None
+        if same_positions:
+            _capi.check(self.lib.fvx_tree_hint_same_positions(self.handle))
         _capi.check(self.lib.fvx_tree_sweep(
             self.handle, mode, _capi.KERNELS[kernel], pos.data_ptr(), alpha.data_ptr(),
             sigma.data_ptr(), None if tgt_gamma is None else tgt_gamma.data_ptr(), int(n),

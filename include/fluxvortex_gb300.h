@@ -239,6 +239,13 @@ int fvx_tree_last_local_ms(fvx_tree* tree, float* ms);
  * fvx_tree_last_validation: out[4] = pairs checked, pairs sent to the FP64
  * fallback, mean e, max e of the last sweep (waits for it). */
 int fvx_tree_set_validation(fvx_tree* tree, int samples, double tol);
+/* fvx_tree_hint_same_positions: the next sweep's particle positions are those
+ * of the last full build (the caller has not moved them): the grid, sort,
+ * cells and interaction lists are reused, while strengths, cores and target
+ * strengths are gathered anew and the moments, expansions, validation and
+ * evaluation recomputed.  A sweep with another position array, count, opening
+ * angle, leaf size or far-field method builds anew whatever the hint. */
+int fvx_tree_hint_same_positions(fvx_tree* tree);
 int fvx_tree_last_validation(fvx_tree* tree, double* out);
 int fvx_tree_sample_pairs(fvx_tree* tree, int list, int max_pairs, void* X, float* T, float* A,
                           int* n_out, void* stream);

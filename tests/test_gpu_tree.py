@@ -89,3 +89,50 @@ def test_tree_degenerate_inputs(cuda, case):
     if np.abs(ud).max() > 0:
         # a planar sheet puts every far cell's quadrupole error in one plane
         assert rel_err(gu, ud) < (3e-3 if case == "sheet" else 1e-3)
+
+
+@pytest.mark.parametrize("far", ["m2p", "learned"])
+def test_reused_structure_matches_a_full_build(cuda, far):
+    """A sweep hinted to have the last build's positions (new strengths and
+    cores) equals a fresh full build: bitwise with the per-particle far field,
+    within FP32 atomic-order noise with local expansions (their sums use
+    atomics).  A hint with another particle count builds anew."""
+    from fluxvortex_gb300.learned import FarFieldMLP
+    pos, gam, sig, _ = slab_wake(1 << 15)
+    rng = np.random.default_rng(3)
+    gam2, sig2 = gam * rng.uniform(0.5, 1.5, gam.shape), sig * rng.uniform(0.8, 1.2, sig.shape)
+    n = pos.shape[0]
+    P, G, S = _dev(pos, cuda), _dev(gam, cuda), _dev(sig, cuda)
+    G2, S2 = _dev(gam2, cuda), _dev(sig2, cuda)
+    mlp = FarFieldMLP.load() if far == "learned" else None
+
+    def sweeper():
+        ts = TreeSweeper(theta=0.5, leaf_target=32)
+        if far == "learned":
+            ts.set_far_field("learned", mlp=mlp)
+            ts.set_validation(0)
+        return ts
+
+    out = lambda: torch.empty((n, 3), dtype=torch.float64, device=cuda)  # noqa: E731
+    ts = sweeper()
+    first, reused = out(), out()
+    ts.sweep(_capi.PAIR_STRETCH, "winckelmans", P, G, S, n, first, tgt_gamma=G)
+    ts.sweep(_capi.PAIR_STRETCH, "winckelmans", P, G2, S2, n, reused, tgt_gamma=G2,
+             same_positions=True)
+    fresh = out()
+    sweeper().sweep(_capi.PAIR_STRETCH, "winckelmans", P, G2, S2, n, fresh, tgt_gamma=G2)
+    a, b = reused.cpu().numpy(), fresh.cpu().numpy()
+    if far == "m2p":
+        assert np.array_equal(a, b)
+    else:
+        assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max()
+    # the hint is ignored when the count changes
+    m = n - 1000
+    part, part_fresh = out(), out()
+    ts.sweep(_capi.PAIR_STRETCH, "winckelmans", P, G2, S2, m, part, tgt_gamma=G2,
+             same_positions=True)
+    sweeper().sweep(_capi.PAIR_STRETCH, "winckelmans", P, G2, S2, m, part_fresh, tgt_gamma=G2)
+    a, b = part[:m].cpu().numpy(), part_fresh[:m].cpu().numpy()
+    tol = 0.0 if far == "m2p" else 1e-5 * np.abs(b).max()
+    assert np.abs(a - b).max() <= tol
+    assert _capi.status_read_and_clear() == 0
