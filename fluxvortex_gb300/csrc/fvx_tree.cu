@@ -880,37 +880,43 @@ __device__ __forceinline__ uint64_t fma(uint64_t a, uint64_t b, uint64_t c) {
 }
 }  // namespace x2
 
-// One row of the packed near tile: {-x, -y}, {-z, s2}, {k2, ax}, {ay, az},
-// {-ax, -ay}, {-az, -10.5 s2} (the negated values turn each cross-product
-// and stretching component into two fused multiply-adds), each a 64-bit pair
-// whose halves hold either one source twice (two targets per lane) or two
-// consecutive sources (one target per lane, two source phases).
+// One row of the packed near tile: {-x, -y}, {-z, s2}, {c1, ax}, {ay, az},
+// {-ax, -ay}, {-az, c2} with c1 = 1.5 s2, c2 = -7.5 s2 (the negated values
+// turn each cross-product and stretching component into two fused
+// multiply-adds), each a 64-bit pair whose halves hold either one source
+// twice (two targets per lane) or two consecutive sources (one target per
+// lane, two source phases).
 struct NearX2 {
   ulonglong2 q[6];
 };
 
-// Near pairs of one staged tile for the thread's two targets (Winckelmans
-// core, velocity or stretching) with paired FP32 instructions; same formulas
-// as core_f32 + accumulate.
+// Near pairs of one staged tile for the thread's two target slots (Winckelmans
+// core, velocity or stretching) with paired FP32 instructions.  With
+// q = r^2 + s^2 and t = q^-1/2 the core terms are written in q alone,
+//   f   = (r^2 + 2.5 s^2) t^5  = t^3 (1 + 1.5 s^2 t^2),
+//   fpr = -(3 r^2 + 10.5 s^2) t^7 = t^5 (-3 - 7.5 s^2 t^2),
+// so q comes from three fused multiply-adds seeded with s^2, r^2 is never
+// formed, and every factor stays bounded (no FP32 overflow for cores down to
+// the integrator's 1e-6 floor).
 template <int MODE>
 __device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, int nt, int stride,
                                              uint64_t TX, uint64_t TY, uint64_t TZ, uint64_t GX,
                                              uint64_t GY, uint64_t GZ, uint64_t* acc) {
-  const uint64_t CM3 = x2::pack(-3.f, -3.f);
+  const uint64_t ONE = x2::pack(1.f, 1.f), CM3 = x2::pack(-3.f, -3.f);
   for (int i = 0; i < nt; ++i) {
     const int k = i * stride;
     const ulonglong2 q0 = tile[k].q[0], q1 = tile[k].q[1], q2 = tile[k].q[2],
                      q3 = tile[k].q[3];
     const uint64_t DX = x2::add(TX, q0.x), DY = x2::add(TY, q0.y), DZ = x2::add(TZ, q1.x);
-    uint64_t R2 = x2::mul(DX, DX);
-    R2 = x2::fma(DY, DY, R2);
-    R2 = x2::fma(DZ, DZ, R2);
+    uint64_t Q = x2::fma(DX, DX, q1.y);
+    Q = x2::fma(DY, DY, Q);
+    Q = x2::fma(DZ, DZ, Q);
     float qa, qb;
-    x2::unpack(x2::add(R2, q1.y), qa, qb);
+    x2::unpack(Q, qa, qb);
     const uint64_t T = x2::pack(rsqrtf(qa), rsqrtf(qb));
     const uint64_t T2 = x2::mul(T, T);
-    const uint64_t T5 = x2::mul(x2::mul(T2, T2), T);
-    const uint64_t F = x2::mul(x2::add(R2, q2.x), T5);
+    const uint64_t T3 = x2::mul(T2, T);
+    const uint64_t F = x2::mul(T3, x2::fma(q2.x, T2, ONE));
     const ulonglong2 q4 = tile[k].q[4], q5 = tile[k].q[5];
     const uint64_t AX = q2.y, AY = q3.x, AZ = q3.y, NAX = q4.x, NAY = q4.y, NAZ = q5.x;
     if (MODE == FVX_PAIR_VELOCITY) {
@@ -919,13 +925,12 @@ __device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, in
       acc[1] = x2::fma(EX, NAZ, x2::fma(EZ, AX, acc[1]));
       acc[2] = x2::fma(EY, NAX, x2::fma(EX, AY, acc[2]));
     } else {
-      // S += (f G + w d) x a, w = fpr (d . G), fpr = -(3 r2 + 10.5 s2) t^7,
-      // formed as ((-3 r2 - 10.5 s2) t^2) t^5 so that no factor overflows
-      // FP32 for cores down to the integrator's 1e-6 floor
+      // S += (f G + w d) x a, w = fpr (d . G)
       uint64_t DG = x2::mul(DX, GX);
       DG = x2::fma(DY, GY, DG);
       DG = x2::fma(DZ, GZ, DG);
-      const uint64_t W = x2::mul(x2::mul(x2::mul(x2::fma(R2, CM3, q5.y), T2), T5), DG);
+      const uint64_t T5 = x2::mul(T3, T2);
+      const uint64_t W = x2::mul(x2::mul(x2::fma(q5.y, T2, CM3), T5), DG);
       const uint64_t VX = x2::fma(W, DX, x2::mul(F, GX));
       const uint64_t VY = x2::fma(W, DY, x2::mul(F, GY));
       const uint64_t VZ = x2::fma(W, DZ, x2::mul(F, GZ));
@@ -1068,11 +1073,12 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
               NearX2 e;
               e.q[0] = make_ulonglong2(x2::pack(-p[0].x, -p[1].x), x2::pack(-p[0].y, -p[1].y));
               e.q[1] = make_ulonglong2(x2::pack(-p[0].z, -p[1].z), x2::pack(p[0].w, p[1].w));
-              e.q[2] = make_ulonglong2(x2::pack(a[0].w, a[1].w), x2::pack(a[0].x, a[1].x));
+              e.q[2] = make_ulonglong2(x2::pack(1.5f * p[0].w, 1.5f * p[1].w),
+                                       x2::pack(a[0].x, a[1].x));
               e.q[3] = make_ulonglong2(x2::pack(a[0].y, a[1].y), x2::pack(a[0].z, a[1].z));
               e.q[4] = make_ulonglong2(x2::pack(-a[0].x, -a[1].x), x2::pack(-a[0].y, -a[1].y));
               e.q[5] = make_ulonglong2(x2::pack(-a[0].z, -a[1].z),
-                                       x2::pack(-10.5f * p[0].w, -10.5f * p[1].w));
+                                       x2::pack(-7.5f * p[0].w, -7.5f * p[1].w));
               s_x2[k] = e;
             }
           }

@@ -50,8 +50,11 @@ class HybridStep:
         self.verts = torch.empty_like(self.base)
         self.verts_next = torch.empty_like(self.base)
         z3 = lambda n: torch.zeros((n, 3), **d)  # noqa: E731
-        self.L = {k: z3(P) for k in ("br", "fr", "fl", "bl", "colloc", "normal", "leg_center",
-                                     "leg_vec")}
+        self.L = {k: z3(P) for k in ("br", "fr", "fl", "bl", "normal", "leg_vec")}
+        # collocation points and bound-leg centres side by side, so that the
+        # wake rings and the particles are swept at both in one call
+        self._pts = z3(2 * P)
+        self.L["colloc"], self.L["leg_center"] = self._pts[:P], self._pts[P:]
         self.L["area"] = torch.zeros(P, **d)
         self.te = z3(w)
         self.te_next = z3(w)
@@ -74,8 +77,10 @@ class HybridStep:
         self.wr_s = torch.zeros(nr, **d)
         self.wr_rc = torch.zeros(nr, **d)
         self.wr_age = torch.zeros(nr, **d)
-        self.v_ring_c, self.v_part_c = z3(P), z3(P)
-        self.v_ring_l, self.v_part_l, self.v_bound_l = z3(P), z3(P), z3(P)
+        self._v_ring, self._v_part = z3(2 * P), z3(2 * P)
+        self.v_ring_c, self.v_ring_l = self._v_ring[:P], self._v_ring[P:]
+        self.v_part_c, self.v_part_l = self._v_part[:P], self._v_part[P:]
+        self.v_bound_l = z3(P)
         self.seg_scratch = torch.empty(1, dtype=torch.uint8, device=self.device)
         self.field = VortexParticleField(cfg.max_particles, nu=cfg.nu, rlxf=cfg.rlxf,
                                          kernel=cfg.kernel, precision=precision, device=device,
@@ -171,11 +176,14 @@ class HybridStep:
                                                 self.wr["fr"].data_ptr(), self.wr["fl"].data_ptr(),
                                                 self.wr["bl"].data_ptr(), self.wr_s.data_ptr(),
                                                 self.wr_rc.data_ptr(), self.wr_age.data_ptr(), st))
-            self._rings_at(L["colloc"], P, self.v_ring_c, self.wr_s, nr, self.wr, self.wr_rc,
+            # wake rings at the collocation points and the bound-leg centres
+            self._rings_at(self._pts, 2 * P, self._v_ring, self.wr_s, nr, self.wr, self.wr_rc,
                            self.wr_age)
         npart = self.field.np
         if npart:
-            self.field._sweep(_capi.PAIR_VELOCITY, L["colloc"], None, P, self.v_part_c)
+            # the particles at both point sets (the state does not change
+            # until the step's convection)
+            self.field._sweep(_capi.PAIR_VELOCITY, self._pts, None, 2 * P, self._v_part)
         _capi.check(lib.fvx_uvlm_rhs(self.nc, self.sf, L["colloc"].data_ptr(),
                                      L["normal"].data_ptr(),
                                      self.v_ring_c.data_ptr() if R else None,
@@ -184,12 +192,7 @@ class HybridStep:
         # 4. strengths (in place: rhs -> Gamma)
         self.gamma.copy_(self.rhs)
         _capi.check(lib.fvx_lu_solve_batched(1, P, self.aic.data_ptr(), self.gamma.data_ptr(), st))
-        # 5. loads at the bound-leg centres
-        if R:
-            self._rings_at(L["leg_center"], P, self.v_ring_l, self.wr_s, nr, self.wr, self.wr_rc,
-                           self.wr_age)
-        if npart:
-            self.field._sweep(_capi.PAIR_VELOCITY, L["leg_center"], None, P, self.v_part_l)
+        # 5. loads at the bound-leg centres (wake and particles swept above)
         self._rings_at(L["leg_center"], P, self.v_bound_l, self.gamma, P, L,
                        self._rc0_bound(), None)
         k = self.k
