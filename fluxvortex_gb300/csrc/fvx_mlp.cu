@@ -188,8 +188,23 @@ struct RecordMoments {
 // phi = 1/|r|, and u_i = eps_ijm d_j Psi_m; the derivatives of phi at |r| = 1
 // are contracted with the moments in closed form (d^p phi = sum over index
 // pairings of (-1)^(p-k) (2p-2k-1)!! n..n d..d).
-template <class Src>
-__device__ __forceinline__ void m2l_core(const Src& src, float* out) {
+// Output accumulators of m2l_core: a register array, or a thread's column of
+// a shared-memory block (stride = the block size), whose dynamic indexing
+// (the output row depends on the loop's component) stays out of local memory.
+struct SharedColumn {
+  float* base;
+  int stride;
+  __device__ float& operator[](int q) const { return base[q * stride]; }
+};
+
+// x[i] of a 3-vector held in registers, for a run-time i (selects, not a
+// local-memory array)
+__device__ __forceinline__ float sel3(float x0, float x1, float x2, int i) {
+  return i == 0 ? x0 : (i == 1 ? x1 : x2);
+}
+
+template <class Src, class Out>
+__device__ __forceinline__ void m2l_core(const Src& src, Out&& out) {
   const float nv[3] = {src.n(0), src.n(1), src.n(2)};
   const float hs = src.hs();
 #pragma unroll
@@ -216,19 +231,22 @@ __device__ __forceinline__ void m2l_core(const Src& src, float* out) {
       const int j = (m + 1 + jj) % 3;      // the two j != m
       const int i = 3 - m - j;
       const float sg = ((j - i + 3) % 3 == 1) ? 1.f : -1.f;  // eps_ijm
-      const float nj = nv[j];
+      const float nj = sel3(nv[0], nv[1], nv[2], j);
+      const float vj = sel3(v[0], v[1], v[2], j);
+      const float qnj = sel3(qn[0], qn[1], qn[2], j);
       // u: c phi_j - v_a phi_aj + 1/2 Q_ab phi_abj
-      const float p1 = -nj * c - (3.f * vn * nj - v[j]) + 0.5f * (-15.f * nqn * nj + 3.f * tr * nj + 6.f * qn[j]);
+      const float p1 = -nj * c - (3.f * vn * nj - vj) + 0.5f * (-15.f * nqn * nj + 3.f * tr * nj + 6.f * qnj);
       out[i] -= sg * p1;
 #pragma unroll
       for (int n = 0; n < 3; ++n) {
         const float dl = j == n ? 1.f : 0.f;
         const float nn = nv[n];
         const float phi2 = 3.f * nj * nn - dl;
-        const float vphi3 = -15.f * vn * nj * nn + 3.f * (v[j] * nn + v[n] * nj + vn * dl);
+        const float vphi3 = -15.f * vn * nj * nn + 3.f * (vj * nn + v[n] * nj + vn * dl);
+        const float qjn = sel3(Q[0][n], Q[1][n], Q[2][n], j);
         const float qphi4 = 105.f * nqn * nj * nn -
-                            15.f * (tr * nj * nn + 2.f * qn[j] * nn + 2.f * qn[n] * nj + nqn * dl) +
-                            3.f * tr * dl + 6.f * Q[j][n];
+                            15.f * (tr * nj * nn + 2.f * qnj * nn + 2.f * qn[n] * nj + nqn * dl) +
+                            3.f * tr * dl + 6.f * qjn;
         out[3 + 3 * i + n] -= sg * (c * phi2 - vphi3 + 0.5f * qphi4);
       }
 #pragma unroll
@@ -241,13 +259,15 @@ __device__ __forceinline__ void m2l_core(const Src& src, float* out) {
         const float dsum = djk * nn + djn * nk + dkn * nj;
         const float phi3 = -15.f * nnn + 3.f * dsum;
         const float vphi4 = 105.f * vn * nnn -
-                            15.f * (v[j] * nk * nn + v[k] * nj * nn + v[n] * nj * nk + vn * dsum) +
-                            3.f * (v[j] * dkn + v[k] * djn + v[n] * djk);
+                            15.f * (vj * nk * nn + v[k] * nj * nn + v[n] * nj * nk + vn * dsum) +
+                            3.f * (vj * dkn + v[k] * djn + v[n] * djk);
+        const float qjn = sel3(Q[0][n], Q[1][n], Q[2][n], j);
+        const float qjk = sel3(Q[0][k], Q[1][k], Q[2][k], j);
         const float qphi5 =
             -945.f * nqn * nnn +
-            105.f * (tr * nnn + 2.f * (qn[j] * nk * nn + qn[k] * nj * nn + qn[n] * nj * nk) + nqn * dsum) -
-            15.f * (2.f * (qn[j] * dkn + qn[k] * djn + qn[n] * djk) + nj * (tr * dkn + 2.f * Q[k][n]) +
-                    nk * (tr * djn + 2.f * Q[j][n]) + nn * (tr * djk + 2.f * Q[j][k]));
+            105.f * (tr * nnn + 2.f * (qnj * nk * nn + qn[k] * nj * nn + qn[n] * nj * nk) + nqn * dsum) -
+            15.f * (2.f * (qnj * dkn + qn[k] * djn + qn[n] * djk) + nj * (tr * dkn + 2.f * Q[k][n]) +
+                    nk * (tr * djn + 2.f * qjn) + nn * (tr * djk + 2.f * qjk));
         out[12 + 6 * i + u] -= sg * (c * phi3 - vphi4 + 0.5f * qphi5);
       }
     }
@@ -621,7 +641,9 @@ __global__ void pair_targets_kernel(int npairs, int stride, int slices,
 // ---- analytic far field of the local-expansion path (no network) ---------------------
 // One thread per (leaf, cell) pair: features -> M2L -> physical units -> sum
 // over the warp's runs of equal leaves -> atomics into the leaf's expansion.
-__global__ void __launch_bounds__(256) m2l_pairs_kernel(int npairs, const int* __restrict__ pair_leaf,
+constexpr int kM2lThreads = 256;
+
+__global__ void __launch_bounds__(kM2lThreads) m2l_pairs_kernel(int npairs, const int* __restrict__ pair_leaf,
                                                         const int* __restrict__ pair_cell,
                                                         const uint32_t* __restrict__ leaf_key,
                                                         const float* __restrict__ rec, float h,
@@ -629,7 +651,8 @@ __global__ void __launch_bounds__(256) m2l_pairs_kernel(int npairs, const int* _
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool act_row = row < npairs;
-  float a[NOUT];
+  __shared__ float s_acc[NOUT * kM2lThreads];
+  const SharedColumn acc{s_acc + threadIdx.x, kM2lThreads};
   PairScale sc{0.f, 0.f, 0.f};
   int leaf = 0;
   if (act_row) {
@@ -638,12 +661,12 @@ __global__ void __launch_bounds__(256) m2l_pairs_kernel(int npairs, const int* _
     const float* r = rec + static_cast<int64_t>(pair_cell[row]) * kRecFloats;
     const PairGeom g = pair_geom(r, cT.x, cT.y, cT.z);
     const RecordMoments src{r, g.Rx * g.id, g.Ry * g.id, g.Rz * g.id, g.hS * g.id, g.im, g.ih};
-    m2l_core(src, a);
+    m2l_core(src, acc);
     sc = pair_scale(g);
-  } else {
-#pragma unroll
-    for (int q = 0; q < NOUT; ++q) a[q] = 0.f;
   }
+  float a[NOUT];
+#pragma unroll
+  for (int q = 0; q < NOUT; ++q) a[q] = act_row ? acc[q] : 0.f;
   const int my = act_row ? leaf : -1 - lane;
   float x[32];
 #pragma unroll
