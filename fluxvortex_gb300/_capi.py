@@ -68,6 +68,9 @@ SIGNATURES = {
     "fvx_mlp_colsum": (I32, [I32, I32, P, P, P]),
     "fvx_mlp_adam": (I32, [I32, P, P, P, P, P, F, F, F, F, I32, P]),
     "fvx_tc_gemm_probe": (I32, [P, P, I32, I32, P, I32, P]),
+    "fvx_vpm_population_scratch_bytes": (SZ, [I64]),
+    "fvx_vpm_drop_oldest": (I32, [I64, I64, P, P, P, P, P, P, SZ, P]),
+    "fvx_vpm_merge_pass": (I32, [I64, P, P, P, P, P, I32, P, D, D, I64, D, P, P, P, SZ, P]),
     "fvx_uvlm_kinematics": (I32, [I32, P, P, D, P, P]),
     "fvx_uvlm_lattice": (I32, [P, I32, P, P, P, P, P, P, P, P, P, P, P, P]),
     "fvx_uvlm_aic": (I32, [I32, I32, P, P, P, P, P, P, D, D, P, P]),

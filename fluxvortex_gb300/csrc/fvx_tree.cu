@@ -236,6 +236,40 @@ __global__ void __launch_bounds__(256) radix_scatter_kernel(
   }
 }
 
+}  // namespace tree
+
+// Stable LSD radix sort of (key, index) pairs by 32-bit keys, four 8-bit
+// passes: the pairs are read from (keys, idx) and returned there, (keys_tmp,
+// idx_tmp) hold n each, table sort_table_ints(n) ints, scan_tmp 2 x 2048 ints.
+int sort_table_ints(int n) { return 256 * ((n + tree::kSortItems - 1) / tree::kSortItems) * 2; }
+
+int sort_pairs_u32(uint32_t* keys, int* idx, uint32_t* keys_tmp, int* idx_tmp, int n, int* table,
+                   int* scan_tmp, cudaStream_t s) {
+  using namespace tree;
+  if (n <= 0) return FVX_OK;
+  const int nblk = (n + kSortItems - 1) / kSortItems;
+  int* table_ex = table + 256 * nblk;
+  uint32_t *ka = keys, *kb = keys_tmp;
+  int *ia = idx, *ib = idx_tmp;
+  for (int pass = 0; pass < 4; ++pass) {
+    radix_hist_kernel<<<nblk, 256, 0, s>>>(ka, n, 8 * pass, nblk, table);
+    FVX_LAUNCH_CHECK();
+    int rc = scan_ints(table, 256 * nblk, table_ex, 0, scan_tmp, s);
+    if (rc) return rc;
+    radix_scatter_kernel<<<nblk, 256, 0, s>>>(ka, ia, n, 8 * pass, nblk, table_ex, kb, ib);
+    FVX_LAUNCH_CHECK();
+    uint32_t* tk = ka;
+    ka = kb;
+    kb = tk;
+    int* ti = ia;
+    ia = ib;
+    ib = ti;
+  }
+  return FVX_OK;  // four passes: the result is back in (keys, idx)
+}
+
+namespace tree {
+
 // ---- cells ----------------------------------------------------------------------
 // flag[i] = 1 where the level key (key >> shift) changes
 __global__ void flags_kernel(const uint32_t* __restrict__ keys, const int* __restrict__ n_ptr,

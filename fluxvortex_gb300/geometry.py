@@ -238,6 +238,22 @@ class HybridConfig:
     surf: np.ndarray = None
     kins: list = None
     s_ref: float = None            # CL / CDi reference area (None: sum of panel areas)
+    # particle population control after each step's convection
+    # (newton_pc/adapters/flap.py:264-279, 466-563): "none", "drop" (keep the
+    # newest pop_max) or "merge" (one moment-conserving merge pass judged at 9
+    # collocation points against merge_eps |V_inf|, the newest merge_protect
+    # particles or those within merge_protect_dist of the wing excluded)
+    population: str = "none"
+    pop_max: int = 60000
+    merge_eps: float = 1e-3
+    merge_protect: int = 64
+    merge_protect_dist: float = None
+
+    def ref_points(self, colloc):
+        """The 9 wing reference points of the merge test: every (P // 9)-th
+        collocation point (flap.py:426)."""
+        P = colloc.shape[0]
+        return colloc[:: max(1, P // 9)][:9]
 
     @property
     def speed(self):

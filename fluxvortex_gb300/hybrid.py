@@ -92,6 +92,10 @@ class HybridStep:
         self._cl = torch.zeros(4096, **d)
         self._cdi = torch.zeros(4096, **d)
         self.k = 0
+        self.n_merged = 0
+        self.n_dropped = 0
+        if cfg.population not in ("none", "drop", "merge"):
+            raise ValueError(f"population must be none, drop or merge, not {cfg.population!r}")
         # initial wake lattice: the trailing edge at t = 0
         self._kin(0.0, self.verts)
         self._lattice(self.verts, self.L, self.te)
@@ -239,6 +243,13 @@ class HybridStep:
         if self.field.np:
             self.field.advect_rk3(cfg.dt, self.u_inf, stretch=cfg.stretch,
                                   free_wake=cfg.free_vpm)
+        # 9. population control (flap.py:469-475)
+        if cfg.population == "drop" and self.field.np > cfg.pop_max:
+            self.n_dropped += self.field.drop_oldest(cfg.pop_max)
+        elif cfg.population == "merge" and self.field.np:
+            ref = cfg.ref_points(self.L["colloc"]).cpu().numpy()
+            self.n_merged += self.field.merge_pass(ref, cfg.speed, cfg.merge_eps,
+                                                   cfg.merge_protect, cfg.merge_protect_dist)
         self.gamma_prev.copy_(self.gamma)
         self.k += 1
 

@@ -17,6 +17,8 @@ positions, strengths and the time integration stay FP64.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import torch
 
@@ -142,6 +144,48 @@ class VortexParticleField:
     def positions_changed(self):
         """Call after writing the position buffer directly (``_pos``)."""
         self._pos_version += 1
+
+    # ---- population control (newton_pc/adapters/flap.py:466-563) -----------------
+    def _pop_scratch_for(self, n):
+        nb = self._lib.fvx_vpm_population_scratch_bytes(n)
+        if getattr(self, "_pop_scratch", None) is None or self._pop_scratch.numel() < nb:
+            self._pop_scratch = torch.empty(int(nb), dtype=torch.uint8, device=self.device)
+        return self._pop_scratch
+
+    def drop_oldest(self, keep):
+        """Keeps the newest ``keep`` particles; returns how many were dropped."""
+        n = self.np
+        if n <= keep:
+            return 0
+        sc = self._pop_scratch_for(n)
+        out = ctypes.c_int64(n)
+        _capi.check(self._lib.fvx_vpm_drop_oldest(
+            n, int(keep), self._pos.data_ptr(), self._gamma.data_ptr(), self._sigma.data_ptr(),
+            self._age.data_ptr(), ctypes.byref(out), sc.data_ptr(), sc.numel(), self._stream()))
+        self.np = int(out.value)
+        self._pos_version += 1
+        return n - self.np
+
+    def merge_pass(self, ref_pts, speed, eps=1e-3, protect_newest=64, protect_dist=None):
+        """One pass of pairwise moment-conserving merging judged at the wing
+        reference points ``ref_pts`` ((R,3), R <= 64) against eps x ``speed``;
+        returns the number of merges."""
+        ref = np.ascontiguousarray(ref_pts, dtype=np.float64).reshape(-1, 3)
+        wing_c = np.ascontiguousarray(ref.mean(axis=0))
+        dref = torch.as_tensor(ref, device=self.device)
+        n = self.np
+        sc = self._pop_scratch_for(max(n, 1))
+        out, merged = ctypes.c_int64(n), ctypes.c_int64(0)
+        _capi.check(self._lib.fvx_vpm_merge_pass(
+            n, self._pos.data_ptr(), self._gamma.data_ptr(), self._sigma.data_ptr(),
+            self._age.data_ptr(), dref.data_ptr(), ref.shape[0], wing_c.ctypes.data,
+            float(speed), float(eps), int(protect_newest),
+            float(protect_dist) if protect_dist else 0.0, ctypes.byref(out),
+            ctypes.byref(merged), sc.data_ptr(), sc.numel(), self._stream()))
+        if merged.value:
+            self.np = int(out.value)
+            self._pos_version += 1
+        return int(merged.value)
 
     # ---- sweeps ----------------------------------------------------------------
     def _stream(self):

@@ -327,6 +327,32 @@ int fvx_uvlm_convert(int R, int n_keep, const FvxSurfaces* s, const double* W,
                      int64_t* count, double* pos, double* alpha, double* sigma, double* age,
                      void* stream);
 
+/* ---- particle population control (FP64) -------------------------------------------
+ * The population control of the reference's flapping adapter
+ * (newton_pc/adapters/flap.py:466-563), which keeps a long run's particle count
+ * bounded.  Both entries work in place on the first n particles (pos, alpha:
+ * (n,3); sigma, age: (n); device), keep the survivors in their order, return
+ * the new count in *n_out (host) and synchronise the stream; n <= 2^22.
+ * drop_oldest: keeps the newest `keep` particles (the oldest are at the front).
+ * merge_pass: one pass of pairwise moment-conserving merging.  Candidates are
+ *   the particles but the newest protect_newest, or, with protect_dist > 0, the
+ *   particles farther than protect_dist from wing_c (nothing merges while
+ *   n < 2 protect_newest).  Each is hashed to a cell of size 0.1 + 0.15 |x -
+ *   wing_c|; consecutive candidates of a cell in the stable lexicographic order
+ *   of the cell keys pair greedily when their strengths are aligned; a pair
+ *   becomes alpha = a1 + a2 at the |a|-weighted centroid with the larger core,
+ *   accepted when the velocity it induces at the n_ref (1..64) wing reference
+ *   points ref_pts (device, (n_ref,3)) changes by less than eps x speed.
+ *   wing_c (host, 3) = the mean of ref_pts; *n_merged (host) = merges accepted. */
+size_t fvx_vpm_population_scratch_bytes(int64_t n);
+int fvx_vpm_drop_oldest(int64_t n, int64_t keep, double* pos, double* alpha, double* sigma,
+                        double* age, int64_t* n_out, void* scratch, size_t scratch_bytes,
+                        void* stream);
+int fvx_vpm_merge_pass(int64_t n, double* pos, double* alpha, double* sigma, double* age,
+                       const double* ref_pts, int n_ref, const double* wing_c, double speed,
+                       double eps, int64_t protect_newest, double protect_dist, int64_t* n_out,
+                       int64_t* n_merged, void* scratch, size_t scratch_bytes, void* stream);
+
 /* ---- batched aeroelastic flutter sweep ------------------------------------------
  * Replaces the reference's per-airspeed AeroelasticSolver runs
  * (src/fluxvortex/aeroelastic_solver.py:68-221 with beam_fe.py:231-351, driven

@@ -43,6 +43,7 @@ import numpy as np
 
 from fluxvortex_gb300.geometry import HybridConfig, lattice
 from oracle import oracle as O
+from oracle import population as POP
 
 
 class HybridOracle:
@@ -63,6 +64,7 @@ class HybridOracle:
         self.gamma_prev = None
         self.cl, self.cdi = [], []
         self.gamma = None
+        self.n_merged = 0
 
     # ring wake in the five-function layout
     def wake_rings(self):
@@ -171,6 +173,16 @@ class HybridOracle:
             self.p_pos, self.p_gam, self.p_sig, self.p_age = O.advect_rk3(
                 self.p_pos, self.p_gam, self.p_sig, self.p_age, cfg.dt, cfg.u_inf, cfg.kernel,
                 cfg.nu, cfg.rlxf, cfg.stretch, cfg.free_vpm)
+        # 9. population control (newton_pc/adapters/flap.py:469-475)
+        state = (self.p_pos, self.p_gam, self.p_sig, self.p_age)
+        if cfg.population == "drop":
+            state = POP.drop_oldest(*state, cfg.pop_max)
+        elif cfg.population == "merge" and self.p_pos.shape[0]:
+            *state, merged = POP.merge_pass(*state, cfg.ref_points(L.colloc), cfg.speed,
+                                            cfg.merge_eps, cfg.merge_protect,
+                                            cfg.merge_protect_dist)
+            self.n_merged += merged
+        self.p_pos, self.p_gam, self.p_sig, self.p_age = state
         self.gamma_prev = gam
         self.gamma = gam
         self.k += 1

@@ -292,9 +292,54 @@ def make_flapping(ref_root):
     print("  flapping done", d["cl_h10"].shape)
 
 
+def _population_inputs(seed=11, n=3000):
+    """A seeded wake-like cloud behind a unit wing: particles 0.2-12 chords
+    downstream, strengths mostly along +y with noise (so that many cells hold
+    aligned pairs), cores 0.05-0.25; 9 reference points on the wing."""
+    rng = np.random.default_rng(seed)
+    pos = np.column_stack([rng.uniform(0.2, 12.0, n), rng.uniform(-3.0, 3.0, n),
+                           rng.normal(0.0, 0.3, n)])
+    alpha = np.column_stack([rng.normal(0.0, 0.2, n), rng.normal(1.0, 0.5, n),
+                             rng.normal(0.0, 0.2, n)]) * 1e-3
+    sigma = rng.uniform(0.05, 0.25, n)
+    ref = np.column_stack([np.full(9, 0.75), np.linspace(-2.5, 2.5, 9), np.zeros(9)])
+    return pos, alpha, sigma, ref
+
+
+def make_population(ref_root):
+    """The reference's own merge pass (newton_pc/adapters/flap.py:478-563),
+    called on a stand-in provider holding only the attributes it reads."""
+    sys.path.insert(0, os.path.join(ref_root, "src"))
+    sys.path.insert(0, ref_root)
+    from newton_pc.adapters.flap import FlapUVLMProvider  # noqa: E402  (reference module)
+    out = {}
+    cases = {"count": dict(eps=1e-3, protect=64, dist=None),
+             "dist": dict(eps=1e-3, protect=64, dist=3.0),
+             "tight": dict(eps=1e-6, protect=200, dist=None)}
+    for name, c in cases.items():
+        pos, alpha, sigma, ref = _population_inputs()
+        prov = types.SimpleNamespace(p_pos=pos.copy(), p_alpha=alpha.copy(), p_sigma=sigma.copy(),
+                                     merge_protect=c["protect"], merge_eps=c["eps"],
+                                     V_inf=np.array([10.0, 0.0, 0.0]),
+                                     stats=dict(n_merged=0))
+        if c["dist"]:
+            prov.merge_protect_dist = c["dist"]
+        FlapUVLMProvider._merge_pass(prov, ref)
+        out.update({f"{name}_pos": prov.p_pos, f"{name}_alpha": prov.p_alpha,
+                    f"{name}_sigma": prov.p_sigma,
+                    f"{name}_merged": np.int64(prov.stats["n_merged"]),
+                    f"{name}_eps": np.float64(c["eps"]), f"{name}_protect": np.int64(c["protect"]),
+                    f"{name}_dist": np.float64(c["dist"] or 0.0)})
+        print(f"  population {name}: {prov.stats['n_merged']} merges")
+    pos, alpha, sigma, ref = _population_inputs()
+    np.savez_compressed(os.path.join(HERE, "population_merge.npz"), pos=pos, alpha=alpha,
+                        sigma=sigma, ref=ref, speed=np.float64(10.0), **out)
+
+
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     make_segments(root)
     make_particles(root)
     make_beam(root)
     make_flapping(root)
+    make_population(root)

@@ -155,3 +155,31 @@ def test_beam_oracle_matches_reference_model(golden):
         got = np.concatenate([b.d, b.v, b.a])
         ref = z["history"][k]
         assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("case", ["count", "dist", "tight"])
+def test_population_merge_matches_reference(golden, case):
+    """The oracle's merge pass against the reference's own (flap.py:478-563)
+    on a seeded wake-like cloud: same merges, bitwise the same particles."""
+    from oracle import population as POP
+    z = golden("population_merge.npz")
+    n = z["sigma"].shape[0]
+    p, a, s, _, m = POP.merge_pass(z["pos"], z["alpha"], z["sigma"], np.arange(n, dtype=float),
+                                   z["ref"], float(z["speed"]), float(z[case + "_eps"]),
+                                   int(z[case + "_protect"]), float(z[case + "_dist"]) or None)
+    assert m == int(z[case + "_merged"]) > 0
+    assert np.array_equal(p, z[case + "_pos"])
+    assert np.array_equal(a, z[case + "_alpha"])
+    assert np.array_equal(s, z[case + "_sigma"])
+    # moment conservation: the total strength is unchanged up to rounding
+    assert np.abs(a.sum(0) - z["alpha"].sum(0)).max() < 1e-15 * n
+
+
+def test_population_drop_keeps_the_newest():
+    from oracle import population as POP
+    n = 10
+    pos = np.arange(3 * n, dtype=float).reshape(n, 3)
+    out = POP.drop_oldest(pos, pos, np.arange(n, dtype=float), np.arange(n, dtype=float), 4)
+    assert np.array_equal(out[2], [6.0, 7.0, 8.0, 9.0])
+    same = POP.drop_oldest(pos, pos, np.arange(n, dtype=float), np.arange(n, dtype=float), 20)
+    assert same[0].shape[0] == n
