@@ -78,7 +78,9 @@ SIGNATURES = {
     "fvx_lu_solve_batched": (I32, [I32, I32, P, P, P]),
     "fvx_uvlm_loads": (I32, [I32, P, P, P, P, P, P, P, P, P, P, P, D, D, D, D, P, P, P, P]),
     "fvx_uvlm_wake_rings": (I32, [I32, P, P, P, P, D, P, P, P, P, P, P, P, P]),
-    "fvx_uvlm_shed": (I32, [I32, I32, P, P, P, P, P, P, P, D, P, P, P, P]),
+    "fvx_uvlm_shed": (I32, [I32, I32, P, P, P, P, P, P, P, D, P, P, P, P, P, P, P]),
+    "fvx_uvlm_loads_bernoulli": (I32, [I32, P, P, P, P, P, P, P, P, P, P, D, D, D, D, P, P, P,
+                                       P]),
     "fvx_uvlm_convert": (I32, [I32, I32, P, P, P, I32, D, I64, P, P, P, P, P, P]),
 }
 

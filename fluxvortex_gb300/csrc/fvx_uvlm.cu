@@ -399,6 +399,102 @@ __global__ void __launch_bounds__(256) loads_kernel(LoadsArgs a) {
   }
 }
 
+// Unsteady Bernoulli loads (newton_pc/adapters/flap.py:357-377): per panel
+// the chordwise and spanwise tangents between the midpoints of its vertex
+// edges, the circulation gradients along them (first row / first strip of a
+// surface: the panel's own strength), and the pressure jump
+// dp = rho (V . t_c dG/dc + V . t_s dG/ds + dG/dt) acting along the normal
+// over the panel area, V = u_inf - v_body + v1 + v2 at the collocation point
+// (the wake rings and particles; no bound self-induction).
+struct BernoulliArgs {
+  int nc;
+  FvxSurfaces sf;
+  const double* verts;
+  const double* gamma;
+  const double* gamma_prev;  // null: no unsteady term
+  const double* colloc;
+  const double* area;
+  const double* normal;
+  const double* v1;
+  const double* v2;
+  double ux, uy, uz, rho, dt, t, s_ref;
+  double* cl_out;
+  double* cdi_out;
+  double* force;
+};
+
+__global__ void __launch_bounds__(256) bernoulli_loads_kernel(BernoulliArgs a) {
+  const int ns = a.sf.ns, w = a.sf.w;
+  const int P = a.nc * ns;
+  double F[3] = {0.0, 0.0, 0.0}, S = 0.0;
+  for (int k = threadIdx.x; k < P; k += blockDim.x) {
+    const int i = k / ns, jj = k % ns, c = strip_col(a.sf, jj);
+    double a0[3], a1[3], b0[3], b1[3];
+    load3(a.verts, static_cast<int64_t>(i) * w + c, a0);
+    load3(a.verts, static_cast<int64_t>(i) * w + c + 1, a1);
+    load3(a.verts, static_cast<int64_t>(i + 1) * w + c, b0);
+    load3(a.verts, static_cast<int64_t>(i + 1) * w + c + 1, b1);
+    double tc[3], ts[3];
+    for (int q = 0; q < 3; ++q) {
+      tc[q] = 0.5 * (b1[q] + b0[q]) - 0.5 * (a1[q] + a0[q]);
+      ts[q] = 0.5 * (b1[q] + a1[q]) - 0.5 * (b0[q] + a0[q]);
+    }
+    const double dc = sqrt(tc[0] * tc[0] + tc[1] * tc[1] + tc[2] * tc[2]);
+    const double ds = sqrt(ts[0] * ts[0] + ts[1] * ts[1] + ts[2] * ts[2]);
+    const double g = a.gamma[k];
+    const bool first_strip = jj == 0 || strip_col(a.sf, jj - 1) + 1 != c;
+    const double dgc = (i > 0 ? g - a.gamma[k - ns] : g) / dc;
+    const double dgs = (first_strip ? g : g - a.gamma[k - 1]) / ds;
+    double p[3], vb[3], n[3];
+    load3(a.colloc, k, p);
+    load3(a.normal, k, n);
+    body_velocity(column_motion(a.sf, c, a.t), p, vb);
+    double wv[3] = {0.0, 0.0, 0.0};
+    if (a.v1) load3(a.v1, k, wv);
+    if (a.v2)
+      for (int q = 0; q < 3; ++q) wv[q] += a.v2[3 * k + q];
+    const double V0 = (a.ux - vb[0]) + wv[0], V1 = (a.uy - vb[1]) + wv[1],
+                 V2 = (a.uz - vb[2]) + wv[2];
+    const double vtc = (V0 * tc[0] + V1 * tc[1] + V2 * tc[2]) / dc;
+    const double vts = (V0 * ts[0] + V1 * ts[1] + V2 * ts[2]) / ds;
+    const double dgdt = a.gamma_prev ? (g - a.gamma_prev[k]) / a.dt : 0.0;
+    // the reference's rings circulate front-left -> front-right -> back-right
+    // -> back-left (flap.py:330-332), against PteraSoftware's (these
+    // strengths): the same flow has the opposite strengths, so dp changes sign
+    const double dp = -a.rho * (vtc * dgc + vts * dgs + dgdt);
+    const double f0 = dp * a.area[k] * n[0], f1 = dp * a.area[k] * n[1],
+                 f2 = dp * a.area[k] * n[2];
+    if (a.force) {
+      a.force[3 * k] = f0;
+      a.force[3 * k + 1] = f1;
+      a.force[3 * k + 2] = f2;
+    }
+    F[0] += f0;
+    F[1] += f1;
+    F[2] += f2;
+    S += a.area[k];
+  }
+  __shared__ double red[4][256];
+  red[0][threadIdx.x] = F[0];
+  red[1][threadIdx.x] = F[1];
+  red[2][threadIdx.x] = F[2];
+  red[3][threadIdx.x] = S;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int c = 0; c < 4; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double V = sqrt(a.ux * a.ux + a.uy * a.uy + a.uz * a.uz);
+    const double eD[3] = {a.ux / V, a.uy / V, a.uz / V};
+    const double eL[3] = {-eD[2], 0.0, eD[0]};
+    const double qS = 0.5 * a.rho * V * V * (a.s_ref > 0.0 ? a.s_ref : red[3][0]);
+    a.cl_out[0] = (red[0][0] * eL[0] + red[1][0] * eL[1] + red[2][0] * eL[2]) / qS;
+    a.cdi_out[0] = (red[0][0] * eD[0] + red[1][0] * eD[1] + red[2][0] * eD[2]) / qS;
+  }
+}
+
 // Ring wake (R rows x ns rings) from the vertex lattice W ((R+1) x w).
 __global__ void wake_rings_kernel(int R, FvxSurfaces sf, const double* __restrict__ W,
                                   const double* __restrict__ gam, const double* __restrict__ age,
@@ -425,11 +521,16 @@ __global__ void wake_rings_kernel(int R, FvxSurfaces sf, const double* __restric
 // New wake from the old one: row 0 = trailing edge of the next step, rows
 // m >= 1 = old rows convected by U_inf dt; strengths shift by one row and take
 // the trailing-edge ring strengths; ages shift and grow by dt.
+// Free ring wake: v1..v3 (any null) are velocities induced at the old
+// vertices, which then move by (u_inf + v1 + v2 + v3) dt; all null: the
+// prescribed wake (u_inf dt).
 __global__ void shed_kernel(int R_old, int nc, int ns, int w, const double* __restrict__ W_old,
                             const double* __restrict__ gam_old,
                             const double* __restrict__ age_old,
                             const double* __restrict__ te_next, const double* __restrict__ gamma,
-                            double dx, double dy, double dz, double dt, double* __restrict__ W_new,
+                            double ux, double uy, double uz, double dt,
+                            const double* __restrict__ v1, const double* __restrict__ v2,
+                            const double* __restrict__ v3, double* __restrict__ W_new,
                             double* __restrict__ gam_new, double* __restrict__ age_new) {
   const int nverts = (R_old + 2) * w;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -439,10 +540,21 @@ __global__ void shed_kernel(int R_old, int nc, int ns, int w, const double* __re
     if (r == 0) {
       load3(te_next, j, p);
     } else {
-      load3(W_old, static_cast<int64_t>(r - 1) * w + j, p);
-      p[0] += dx;
-      p[1] += dy;
-      p[2] += dz;
+      const int64_t o = static_cast<int64_t>(r - 1) * w + j;
+      load3(W_old, o, p);
+      if (v1 || v2 || v3) {
+        double v[3] = {ux, uy, uz};
+        const double* vs[3] = {v1, v2, v3};
+        for (int q = 0; q < 3; ++q)
+          if (vs[q])
+            for (int c = 0; c < 3; ++c) v[c] += vs[q][3 * o + c];
+        for (int c = 0; c < 3; ++c) p[c] = __dadd_rn(p[c], __dmul_rn(v[c], dt));
+      } else {
+        // u dt rounded, then added (no fused multiply-add)
+        p[0] = __dadd_rn(p[0], __dmul_rn(ux, dt));
+        p[1] = __dadd_rn(p[1], __dmul_rn(uy, dt));
+        p[2] = __dadd_rn(p[2], __dmul_rn(uz, dt));
+      }
     }
     store3(W_new, k, p);
   }
@@ -619,6 +731,23 @@ int fvx_uvlm_loads(int nc, const FvxSurfaces* s, const double* gamma, const doub
   return FVX_OK;
 }
 
+int fvx_uvlm_loads_bernoulli(int nc, const FvxSurfaces* s, const double* verts,
+                             const double* gamma, const double* gamma_prev, const double* colloc,
+                             const double* area, const double* normal, const double* v1,
+                             const double* v2, const double* u_inf, double rho, double dt,
+                             double t, double s_ref, double* cl, double* cdi, double* force,
+                             void* stream) {
+  FVX_ARG_CHECK(nc >= 1 && layout_ok(s) && verts && gamma && colloc && area && normal && u_inf &&
+                    cl && cdi,
+                "bad loads arguments");
+  fvx::BernoulliArgs a{nc,    *s,     verts,    gamma,    gamma_prev, colloc, area,
+                       normal, v1,    v2,       u_inf[0], u_inf[1],   u_inf[2], rho,
+                       dt,     t,     s_ref,    cl,       cdi,        force};
+  fvx::bernoulli_loads_kernel<<<1, 256, 0, static_cast<cudaStream_t>(stream)>>>(a);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
 int fvx_uvlm_wake_rings(int R, const FvxSurfaces* s, const double* W, const double* gam,
                         const double* age, double rc0, double* br, double* fr, double* fl,
                         double* bl, double* strength, double* rc0s, double* ages, void* stream) {
@@ -633,14 +762,14 @@ int fvx_uvlm_wake_rings(int R, const FvxSurfaces* s, const double* W, const doub
 
 int fvx_uvlm_shed(int R_old, int nc, const FvxSurfaces* s, const double* W_old,
                   const double* gam_old, const double* age_old, const double* te_next,
-                  const double* gamma, const double* u_inf, double dt, double* W_new,
-                  double* gam_new, double* age_new, void* stream) {
+                  const double* gamma, const double* u_inf, double dt, const double* v1,
+                  const double* v2, const double* v3, double* W_new, double* gam_new,
+                  double* age_new, void* stream) {
   FVX_ARG_CHECK(R_old >= 0 && nc >= 1 && layout_ok(s) && u_inf, "bad shed arguments");
   const int n = (R_old + 2) * s->w;
   fvx::shed_kernel<<<fvx::nblk(n), fvx::kT, 0, static_cast<cudaStream_t>(stream)>>>(
-      R_old, nc, s->ns, s->w, W_old, gam_old, age_old, te_next, gamma, u_inf[0] * dt,
-      u_inf[1] * dt,
-      u_inf[2] * dt, dt, W_new, gam_new, age_new);
+      R_old, nc, s->ns, s->w, W_old, gam_old, age_old, te_next, gamma, u_inf[0], u_inf[1],
+      u_inf[2], dt, v1, v2, v3, W_new, gam_new, age_new);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }

@@ -243,6 +243,14 @@ class HybridConfig:
     # newest pop_max) or "merge" (one moment-conserving merge pass judged at 9
     # collocation points against merge_eps |V_inf|, the newest merge_protect
     # particles or those within merge_protect_dist of the wing excluded)
+    # free ring wake: the kept ring rows move with the local velocity (bound
+    # rings, wake rings, particles, freestream; PteraSoftware's free wake, cf.
+    # newton_pc/adapters/flap.py:379-401) instead of the freestream alone
+    free_ring_wake: bool = False
+    # loads: "kj" (Kutta-Joukowski on the bound legs + unsteady term, the
+    # PteraSoftware form) or "bernoulli" (unsteady Bernoulli pressure,
+    # newton_pc/adapters/flap.py:357-377)
+    loads: str = "kj"
     population: str = "none"
     pop_max: int = 60000
     merge_eps: float = 1e-3

@@ -70,6 +70,8 @@ class HybridStep:
         self.W = [z3(rows * w), z3(rows * w)]
         self.wg = [torch.zeros(rows * ns, **d), torch.zeros(rows * ns, **d)]
         self.wa = [torch.zeros(rows, **d), torch.zeros(rows, **d)]
+        # velocities induced at the wake vertices (free ring wake)
+        self._wv = [z3(rows * w) for _ in range(3)] if cfg.free_ring_wake else None
         self.cur = 0
         self.R = 0
         nr = (cfg.n_keep + 1) * ns
@@ -94,6 +96,8 @@ class HybridStep:
         self.k = 0
         self.n_merged = 0
         self.n_dropped = 0
+        if cfg.loads not in ("kj", "bernoulli"):
+            raise ValueError(f"loads must be kj or bernoulli, not {cfg.loads!r}")
         if cfg.population not in ("none", "drop", "merge"):
             raise ValueError(f"population must be none, drop or merge, not {cfg.population!r}")
         # initial wake lattice: the trailing edge at t = 0
@@ -197,11 +201,22 @@ class HybridStep:
         self.gamma.copy_(self.rhs)
         _capi.check(lib.fvx_lu_solve_batched(1, P, self.aic.data_ptr(), self.gamma.data_ptr(), st))
         # 5. loads at the bound-leg centres (wake and particles swept above)
-        self._rings_at(L["leg_center"], P, self.v_bound_l, self.gamma, P, L,
-                       self._rc0_bound(), None)
         k = self.k
         cl_p = self._cl[k:].data_ptr() if out2 is None else out2[0:].data_ptr()
         cdi_p = self._cdi[k:].data_ptr() if out2 is None else out2[1:].data_ptr()
+        if cfg.loads == "bernoulli":
+            # unsteady Bernoulli pressure (flap.py:357-377) from the collocation
+            # velocities already swept for the right-hand side
+            _capi.check(lib.fvx_uvlm_loads_bernoulli(
+                self.nc, self.sf, self.verts.data_ptr(), self.gamma.data_ptr(),
+                self.gamma_prev.data_ptr() if k else None, L["colloc"].data_ptr(),
+                L["area"].data_ptr(), L["normal"].data_ptr(),
+                self.v_ring_c.data_ptr() if R else None,
+                self.v_part_c.data_ptr() if npart else None, self.u_inf.ctypes.data, cfg.rho,
+                cfg.dt, t, self.s_ref, cl_p, cdi_p, self.force.data_ptr(), st))
+            return
+        self._rings_at(L["leg_center"], P, self.v_bound_l, self.gamma, P, L,
+                       self._rc0_bound(), None)
         _capi.check(lib.fvx_uvlm_loads(
             self.nc, self.sf, self.gamma.data_ptr(), self.gamma_prev.data_ptr() if k else None,
             L["leg_center"].data_ptr(), L["leg_vec"].data_ptr(), L["area"].data_ptr(),
@@ -219,10 +234,25 @@ class HybridStep:
         self._kin(t + cfg.dt, self.verts_next)
         self._lattice(self.verts_next, self.Ln, self.te_next)
         nxt = 1 - self.cur
+        vel = (None, None, None)
+        if cfg.free_ring_wake:
+            # free ring wake: every old vertex moves with the velocity the bound
+            # rings, the wake rings and the particles induce there (PS core law)
+            nv = (R + 1) * self.w
+            vb, vw, vp = (t_[:nv] for t_ in self._wv)
+            self._rings_at(Wc, nv, vb, self.gamma, self.P, self.L, self._rc0_bound(), None)
+            if R:
+                self._rings_at(Wc, nv, vw, self.wr_s, R * self.ns, self.wr, self.wr_rc,
+                               self.wr_age)
+            if self.field.np:
+                self.field._sweep(_capi.PAIR_VELOCITY, Wc, None, nv, vp)
+            vel = (vb.data_ptr(), vw.data_ptr() if R else None,
+                   vp.data_ptr() if self.field.np else None)
         _capi.check(lib.fvx_uvlm_shed(R, self.nc, self.sf, Wc.data_ptr(), gc.data_ptr(),
                                       ac.data_ptr(),
                                       self.te_next.data_ptr(), self.gamma.data_ptr(),
-                                      self.u_inf.ctypes.data, cfg.dt, self.W[nxt].data_ptr(),
+                                      self.u_inf.ctypes.data, cfg.dt, *vel,
+                                      self.W[nxt].data_ptr(),
                                       self.wg[nxt].data_ptr(), self.wa[nxt].data_ptr(), st))
         self.cur = nxt
         R += 1

@@ -283,8 +283,19 @@ int fvx_tree_sample_pairs(fvx_tree* tree, int list, int max_pairs, void* X, floa
  *   per-panel forces.
  * wake_rings: ring-wake vertex lattice W[(R+1)*w][3] with row strengths
  *   gam[R*ns] and row ages age[R] -> the ring layout of the Biot-Savart entries.
- * shed: W_new = [te_next; W_old + u_inf dt], gam_new = [TE ring strengths;
- *   gam_old], age_new = [0; age_old + dt].
+ * loads_bernoulli: the unsteady Bernoulli form of the loads
+ *   (newton_pc/adapters/flap.py:357-377): per panel dp = rho (V . t_c dG/dc +
+ *   V . t_s dG/ds + dG/dt) over the panel area along the normal (negated: the
+ *   reference's rings circulate opposite to these), with t_c, t_s
+ *   between the midpoints of the panel's vertex edges (verts = the grid of the
+ *   step), the gradients restarting at the first row and at each surface's
+ *   first strip, V = u_inf - v_body + v1 + v2 at the collocation points (no
+ *   bound self-induction); CL, CDi and per-panel forces as for loads.
+ * shed: W_new = [te_next; W_old + V dt], gam_new = [TE ring strengths;
+ *   gam_old], age_new = [0; age_old + dt]; V = u_inf (prescribed wake) or, for
+ *   a free ring wake, u_inf + v1 + v2 + v3 with v1..v3 ((R_old+1) w, 3) the
+ *   velocities induced at the old vertices (any may be NULL; all NULL: the
+ *   prescribed wake).
  * convert: rows r >= n_keep of W -> 4 particles per ring at leg midpoints
  *   with alpha = Gamma (b - a), skipping |Gamma| < 1e-15 and |alpha|^2 <= 1e-30
  *   (experiment_hybrid_panel_particle.py:173-200); sigma = sigma_vdt
@@ -318,10 +329,17 @@ int fvx_uvlm_loads(int nc, const FvxSurfaces* s, const double* gamma, const doub
 int fvx_uvlm_wake_rings(int R, const FvxSurfaces* s, const double* W, const double* gam,
                         const double* age, double rc0, double* br, double* fr, double* fl,
                         double* bl, double* strength, double* rc0s, double* ages, void* stream);
+int fvx_uvlm_loads_bernoulli(int nc, const FvxSurfaces* s, const double* verts,
+                             const double* gamma, const double* gamma_prev, const double* colloc,
+                             const double* area, const double* normal, const double* v1,
+                             const double* v2, const double* u_inf, double rho, double dt,
+                             double t, double s_ref, double* cl, double* cdi, double* force,
+                             void* stream);
 int fvx_uvlm_shed(int R_old, int nc, const FvxSurfaces* s, const double* W_old,
                   const double* gam_old, const double* age_old, const double* te_next,
-                  const double* gamma, const double* u_inf, double dt, double* W_new,
-                  double* gam_new, double* age_new, void* stream);
+                  const double* gamma, const double* u_inf, double dt, const double* v1,
+                  const double* v2, const double* v3, double* W_new, double* gam_new,
+                  double* age_new, void* stream);
 int fvx_uvlm_convert(int R, int n_keep, const FvxSurfaces* s, const double* W,
                      const double* gam, int sigma_rule, double sigma_vdt, int64_t capacity,
                      int64_t* count, double* pos, double* alpha, double* sigma, double* age,

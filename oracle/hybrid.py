@@ -14,15 +14,19 @@ overrides it, is followed:
      plus the vortex particles -> velocity_from_particles
      (experiment_hybrid_panel_particle.py:114-123)
   4. strengths: AIC Gamma = -(U_inf - v_body + V_wake) . n (FP64 solve)
-  5. loads: Kutta-Joukowski on each ring's bound (front) leg, F = rho
+  5. loads (``loads="bernoulli"``: the unsteady Bernoulli pressure of
+     newton_pc/adapters/flap.py:357-377 instead): Kutta-Joukowski on each
+     ring's bound (front) leg, F = rho
      (Gamma_ij - Gamma_i-1,j) (V x l), with V the freestream minus the body
      motion plus the velocity induced by every bound ring, the wake rings and
      the particles (segments collinear with the leg are skipped by the
      kernel's own tests, warp_kernels.py:81), plus the unsteady term
      -rho dGamma/dt A n
   6. populate the next wake: convect the ring-wake lattice with the
-     freestream (prescribed wake), attach a new row whose strength is the
-     trailing-edge ring's, ages += dt
+     freestream (prescribed wake) or, with ``free_ring_wake``, each vertex with
+     the freestream plus the velocity the bound rings, wake rings and particles
+     induce at it (PteraSoftware's free wake), attach a new row whose strength
+     is the trailing-edge ring's, ages += dt
   7. HybridSolver._convert_old_wake_to_particles (:145-204): rows >= N_keep
      become 4 particles per ring (leg midpoints, alpha = Gamma (b - a)),
      rings with |Gamma| < 1e-15 and legs with |alpha|^2 <= 1e-30 skipped
@@ -92,6 +96,42 @@ class HybridOracle:
                                               self.cfg.kernel)
         return v
 
+    def _bernoulli(self, verts, L, gam, Vext, t):
+        """Unsteady Bernoulli loads (newton_pc/adapters/flap.py:357-377) on this
+        lattice: tangents between vertex-edge midpoints, circulation gradients
+        restarting at the first row and each surface's first strip,
+        dp = rho (V . t_c dG/dc + V . t_s dG/ds + dG/dt), F = sum dp A n."""
+        cfg = self.cfg
+        nc, ns = L.nc, L.ns
+        a, b = self.col, self.col + 1
+        v0, v1 = verts[:-1], verts[1:]
+        tau_c = (0.5 * (v1[:, b] + v1[:, a]) - 0.5 * (v0[:, b] + v0[:, a])).reshape(-1, 3)
+        tau_s = (0.5 * (v1[:, b] + v0[:, b]) - 0.5 * (v1[:, a] + v0[:, a])).reshape(-1, 3)
+        dc = np.linalg.norm(tau_c, axis=1)
+        ds = np.linalg.norm(tau_s, axis=1)
+        g2 = gam.reshape(nc, ns)
+        gc = g2.copy()
+        gc[1:] -= g2[:-1]
+        first = np.r_[True, self.col[1:] != self.col[:-1] + 1]
+        gs = g2.copy()
+        gs[:, ~first] -= g2[:, np.flatnonzero(~first) - 1]
+        vb = cfg.point_velocity(L.colloc, t)
+        V = (cfg.u_inf[None, :] - vb) + Vext
+        gprev = gam if self.gamma_prev is None else self.gamma_prev
+        # flap.py's rings circulate opposite to PteraSoftware's (these
+        # strengths, flap.py:330-332): the same flow gives -dp here
+        dp = -cfg.rho * (np.einsum("ic,ic->i", V, tau_c) / dc * (gc.reshape(-1) / dc)
+                         + np.einsum("ic,ic->i", V, tau_s) / ds * (gs.reshape(-1) / ds)
+                         + (gam - gprev) / cfg.dt)
+        Ft = (dp * L.area)[:, None] * L.normal
+        Ft = Ft.sum(axis=0)
+        V0 = cfg.speed
+        eD = cfg.u_inf / V0
+        eL = np.array([-eD[2], 0.0, eD[0]])
+        qS = 0.5 * cfg.rho * V0 ** 2 * (L.area.sum() if cfg.s_ref is None else cfg.s_ref)
+        self.cl.append(float(Ft @ eL / qS))
+        self.cdi.append(float(Ft @ eD / qS))
+
     def step(self):
         cfg = self.cfg
         t = self.k * cfg.dt
@@ -112,28 +152,50 @@ class HybridOracle:
         # 4. strengths
         gam = np.linalg.solve(A, rhs)
         # 5. loads
-        Vl = self._induced(L.leg_center, rings)
-        Vb = O.collapsed_velocities_from_ring_vortices(L.leg_center, L.br, L.fr, L.fl, L.bl, gam,
-                                                       rc_b, None, None, cfg.nu)
-        vbl = cfg.point_velocity(L.leg_center, t)
-        V = (cfg.u_inf[None, :] - vbl) + (Vl + Vb)
-        g2 = gam.reshape(L.nc, L.ns)
-        geff = g2.copy()
-        geff[1:] -= g2[:-1]
-        gprev = gam if self.gamma_prev is None else self.gamma_prev
-        dgdt = (gam - gprev) / cfg.dt
-        F = (cfg.rho * geff.reshape(-1)[:, None] * np.cross(V, L.leg_vec)
-             - (cfg.rho * dgdt * L.area)[:, None] * L.normal)
-        Ft = F.sum(axis=0)
-        V0 = cfg.speed
-        eD = cfg.u_inf / V0
-        eL = np.array([-eD[2], 0.0, eD[0]])
-        qS = 0.5 * cfg.rho * V0 ** 2 * (L.area.sum() if cfg.s_ref is None else cfg.s_ref)
-        self.cl.append(float(Ft @ eL / qS))
-        self.cdi.append(float(Ft @ eD / qS))
+        if cfg.loads == "bernoulli":
+            self._bernoulli(verts, L, gam, Vw, t)
+            Vl = None
+        else:
+            Vl = self._induced(L.leg_center, rings)
+        if Vl is not None:
+            Vb = O.collapsed_velocities_from_ring_vortices(L.leg_center, L.br, L.fr, L.fl, L.bl, gam,
+                                                           rc_b, None, None, cfg.nu)
+            vbl = cfg.point_velocity(L.leg_center, t)
+            V = (cfg.u_inf[None, :] - vbl) + (Vl + Vb)
+            g2 = gam.reshape(L.nc, L.ns)
+            geff = g2.copy()
+            geff[1:] -= g2[:-1]
+            gprev = gam if self.gamma_prev is None else self.gamma_prev
+            dgdt = (gam - gprev) / cfg.dt
+            F = (cfg.rho * geff.reshape(-1)[:, None] * np.cross(V, L.leg_vec)
+                 - (cfg.rho * dgdt * L.area)[:, None] * L.normal)
+            Ft = F.sum(axis=0)
+            V0 = cfg.speed
+            eD = cfg.u_inf / V0
+            eL = np.array([-eD[2], 0.0, eD[0]])
+            qS = 0.5 * cfg.rho * V0 ** 2 * (L.area.sum() if cfg.s_ref is None else cfg.s_ref)
+            self.cl.append(float(Ft @ eL / qS))
+            self.cdi.append(float(Ft @ eD / qS))
         # 6. next wake
+        g2 = gam.reshape(L.nc, L.ns)
         Ln = lattice(cfg.vertices(t + cfg.dt), self.col)
-        Wc = self.W + cfg.u_inf * cfg.dt
+        if cfg.free_ring_wake:
+            # free ring wake: each old vertex moves with u_inf + bound rings +
+            # wake rings + particles at it
+            pts = self.W.reshape(-1, 3)
+            rc_b = np.full(L.colloc.shape[0], cfg.rc0)
+            V = cfg.u_inf[None, :] + O.collapsed_velocities_from_ring_vortices(
+                pts, L.br, L.fr, L.fl, L.bl, gam, rc_b, None, None, cfg.nu)
+            if rings[4].size:
+                br, fr, fl, bl, g, rc, ages = rings
+                V = V + O.collapsed_velocities_from_ring_vortices(pts, br, fr, fl, bl, g, rc, None,
+                                                                  ages, cfg.nu)
+            if self.p_pos.shape[0]:
+                V = V + O.velocity_from_particles(pts, self.p_pos, self.p_gam, self.p_sig,
+                                                  cfg.kernel)
+            Wc = self.W + V.reshape(self.W.shape) * cfg.dt
+        else:
+            Wc = self.W + cfg.u_inf * cfg.dt
         self.W = np.concatenate([Ln.te_back[None], Wc], axis=0)
         self.wgam = np.concatenate([g2[-1][None], self.wgam], axis=0)
         self.wage = np.concatenate([[0.0], self.wage + cfg.dt])

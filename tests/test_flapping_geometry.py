@@ -88,3 +88,17 @@ def test_oracle_tracks_the_reference_flapping_history(golden):
     amp = lambda x: 0.5 * (x.max() - x.min())  # noqa: E731
     assert abs(amp(last) / amp(rlast) - 1.0) < 0.08
     assert abs(cdi[-43:].mean() / rcdi[-43:].mean() - 1.0) < 0.1
+
+
+def test_bernoulli_lift_matches_kutta_joukowski_on_the_static_wing():
+    """The two load paths of the oracle integrate the same circulation: the
+    lift agrees (the drag differs: normal pressure carries no suction)."""
+    from fluxvortex_gb300.geometry import static_wing
+    from oracle.hybrid import HybridOracle
+    cl = {}
+    for loads in ("kj", "bernoulli"):
+        o = HybridOracle(static_wing(free_vpm=False, loads=loads))
+        for _ in range(12):
+            o.step()
+        cl[loads] = np.array(o.cl)
+    assert np.abs(cl["bernoulli"][3:] / cl["kj"][3:] - 1.0).max() < 2e-3

@@ -147,3 +147,22 @@ def test_lu_solve_flags_a_singular_system_and_refuses_oversize(cuda):
     big = torch.zeros(1, dtype=torch.float64, device="cuda")
     with pytest.raises(_capi.FvxError):
         _capi.check(lib.fvx_lu_solve_batched(1, 4096, big.data_ptr(), big.data_ptr(), None))
+
+
+@pytest.mark.parametrize("free,loads", [(True, "kj"), (False, "bernoulli"), (True, "bernoulli")])
+def test_free_ring_wake_and_bernoulli_loads(cuda, free, loads):
+    """Free ring wake (every kept vertex moves with the induced velocity) and
+    the unsteady Bernoulli loads of newton_pc/adapters/flap.py:357-401 on the
+    three-surface configuration, against the oracle (prescribed particles)."""
+    cfg = flapping_aircraft(n_keep=4, flapping="both", free_vpm=False, free_ring_wake=free,
+                            loads=loads)
+    g, o = _run(cfg, 10)
+    assert _hist_err(g.cl, o.cl) < 1e-10
+    if loads == "kj":
+        assert _hist_err(g.cdi, o.cdi) < 1e-10
+    else:
+        assert np.abs(np.array(g.cdi) - np.array(o.cdi)).max() < 1e-10 * np.abs(o.cl).max()
+    nv = o.W.shape[0] * o.W.shape[1]
+    W = g.W[g.cur][:nv].cpu().numpy()
+    assert np.abs(W - o.W.reshape(-1, 3)).max() < 1e-10
+    assert rel_err(g.field.positions, o.p_pos) < 1e-10
