@@ -620,6 +620,11 @@ struct DualLists {
   int* par_cell;
   int* leaf_parent;  // per leaf: its parent's level-local index
   int near_cap, lrn_cap, par_cap;
+  // slot mode (fill pass with these > 0): leaf t's near leaves at
+  // near_idx[t slot_near ..], its local cells at lrn_cell[t slot_lrn ..],
+  // parent p's cells at par_cell[p slot_par ..]; the counts are written and
+  // an overflow of a slot sets overflow bit 4 (lrn_leaf, par_par unused)
+  int slot_near, slot_lrn, slot_par;
 };
 
 template <bool FILL>
@@ -653,8 +658,13 @@ __global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restri
   const int tcount = T.count[gT];
   if (FILL) D.leaf_parent[t] = p;
   int nn = 0, nl = 0, np = 0;
-  const int no = FILL ? D.near_off[t] : 0, lo_ = FILL ? D.lrn_off[t] : 0;
-  const int po = (FILL && first) ? D.par_off[p] : 0;
+  const bool slot = FILL && D.slot_near > 0;
+  const int no = FILL ? (slot ? t * D.slot_near : D.near_off[t]) : 0;
+  const int lo_ = FILL ? (slot ? t * D.slot_lrn : D.lrn_off[t]) : 0;
+  const int po = (FILL && first) ? (slot ? p * D.slot_par : D.par_off[p]) : 0;
+  const int near_end = slot ? no + D.slot_near : D.near_cap;
+  const int lrn_end = slot ? lo_ + D.slot_lrn : D.lrn_cap;
+  const int par_end = slot ? po + D.slot_par : D.par_cap;
   long long near_pairs = 0;
   // T against source cell g at level l; false: an inner cell that fails
   auto leaf_visit = [&](int g, int l) {
@@ -665,15 +675,15 @@ __global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restri
     const int dz = tz - (2 * static_cast<int>(compact10(k >> 2)) + 1) * sc;
     const int d2 = dx * dx + dy * dy + dz * dz;
     if (d2 > T.thr_far[l]) {
-      if (FILL && lo_ + nl < D.lrn_cap) {
-        D.lrn_leaf[lo_ + nl] = t;
+      if (FILL && lo_ + nl < lrn_end) {
+        if (!slot) D.lrn_leaf[lo_ + nl] = t;
         D.lrn_cell[lo_ + nl] = g;
       }
       ++nl;
       return true;
     }
     if (l == L) {
-      if (FILL && no + nn < D.near_cap) D.near_idx[no + nn] = g - T.base[L];
+      if (FILL && no + nn < near_end) D.near_idx[no + nn] = g - T.base[L];
       near_pairs += static_cast<long long>(tcount) * T.count[g];
       ++nn;
       return true;
@@ -694,8 +704,8 @@ __global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restri
     const int d2 = dx * dx + dy * dy + dz * dz;
     if (d2 > T.thr_par[l]) {
       if (first) {
-        if (FILL && po + np < D.par_cap) {
-          D.par_par[po + np] = p;
+        if (FILL && po + np < par_end) {
+          if (!slot) D.par_par[po + np] = p;
           D.par_cell[po + np] = g;
         }
         ++np;
@@ -725,16 +735,36 @@ __global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restri
     const int clo = T.child_lo[g], chi = T.child_hi[g];  // A at level L-1: leaves below
     for (int q = clo; q < chi; ++q) leaf_visit(T.base[L] + q, L);
   }
-  if (!FILL) {
+  if (!FILL || slot) {
     D.near_cnt[t] = nn;
     D.lrn_cnt[t] = nl;
     if (first) D.par_cnt[p] = np;
-  } else {
-    if (no + nn > D.near_cap || lo_ + nl > D.lrn_cap || (first && po + np > D.par_cap))
-      atomicOr(overflow, 2u);
+  }
+  if (FILL) {
+    if (no + nn > near_end || lo_ + nl > lrn_end || (first && po + np > par_end))
+      atomicOr(overflow, slot ? 4u : 2u);
     unsigned long long* work = reinterpret_cast<unsigned long long*>(overflow + 2);
     atomicAdd(work, static_cast<unsigned long long>(near_pairs));
   }
+}
+
+// slot-mode lists -> flat (target, cell) pair lists ordered by target: warp
+// per target, lanes over its slot; off = the exclusive scan of the counts
+__global__ void compact_slots_kernel(int ntgt, int cap, const int* __restrict__ cnt,
+                                     const int* __restrict__ off, const int* __restrict__ slots,
+                                     int* __restrict__ tgt, int* __restrict__ cell) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= ntgt) return;
+  const int c = cnt[w], o = off[w];
+  for (int q = lane; q < c; q += 32) {
+    tgt[o + q] = w;
+    cell[o + q] = slots[static_cast<int64_t>(w) * cap + q];
+  }
+}
+
+__global__ void iota_scaled_kernel(int n, int step, int* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = i * step;
 }
 
 // ---- evaluation -----------------------------------------------------------------------
@@ -1484,6 +1514,8 @@ struct fvx_tree {
   fvx::DevBuf pair_partial;  // slices of the FP64 exact-expansion sums
   int n_parent_pairs = 0;
   fvx::DevBuf lrn_meta, lrn_leaf, lrn_cell, leaf_local;
+  fvx::DevBuf lrn_slot, par_slot;  // one-pass (slot) form of the two-level lists
+  int slot_near = 512, slot_lrn = 1024, slot_par = 1024;  // 0: counting pass always
   int n_learned = 0;
   // the structure of the last full build (grid, sort, cells, interaction
   // lists), reused by a sweep hinted to have the same positions
@@ -1824,6 +1856,73 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
     lrn_total = ST.lrn_total;
     par_total = ST.par_total;
   } else {
+  // Two-level lists in one pass: each leaf's near leaves and local cells and
+  // each parent's cells go to fixed-capacity slots (no counting pass); the
+  // local-expansion pairs are then compacted into flat lists ordered by
+  // target.  A slot overflow falls back to the counting pass and exact lists.
+  bool slotted = false;
+  if (dual && T->slot_near > 0 && T->slot_lrn > 0 && T->slot_par > 0) {
+    const int kSlotNear = T->slot_near, kSlotLrn = T->slot_lrn, kSlotPar = T->slot_par;
+    if ((rc = grow(T->near_list, 4 * size_t(nleaf) * kSlotNear)) ||
+        (rc = grow(T->lrn_slot, 4 * size_t(nleaf) * kSlotLrn)) ||
+        (rc = grow(T->par_slot, 4 * size_t(npar) * kSlotPar)))
+      return rc;
+    FVX_CUDA_TRY(cudaMemsetAsync(ovf, 0, 24, s));
+    FVX_CUDA_TRY(cudaMemsetAsync(far_cnt, 0, sizeof(int) * size_t(nleaf), s));
+    DualLists D{};
+    D.near_cnt = near_cnt;
+    D.lrn_cnt = LL.cnt;
+    D.par_cnt = par_cnt;
+    D.near_idx = P<int>(T->near_list);
+    D.lrn_cell = P<int>(T->lrn_slot);
+    D.par_cell = P<int>(T->par_slot);
+    D.leaf_parent = leaf_parent;
+    D.slot_near = kSlotNear;
+    D.slot_lrn = kSlotLrn;
+    D.slot_par = kSlotPar;
+    traverse_dual_kernel<true><<<(nleaf + 127) / 128, 128, 0, s>>>(V, D, ovf);
+    FVX_LAUNCH_CHECK();
+    iota_scaled_kernel<<<(nleaf + 255) / 256, 256, 0, s>>>(nleaf, kSlotNear, near_off);
+    FVX_LAUNCH_CHECK();
+    if ((rc = scan_ints(LL.cnt, nleaf, P<int>(T->lrn_meta) + nleaf, 0, P<int>(T->scan_tmp), s)))
+      return rc;
+    if ((rc = scan_ints(par_cnt, npar, par_off, 0, P<int>(T->scan_tmp), s))) return rc;
+    // the near total through a scan into far_off (no far cells on this path)
+    if ((rc = scan_ints(near_cnt, nleaf, far_off, 0, P<int>(T->scan_tmp), s))) return rc;
+    int tl[6] = {0, 0, 0, 0, 0, 0};
+    unsigned flags = 0;
+    FVX_CUDA_TRY(cudaMemcpyAsync(&tl[0], LL.cnt + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
+    FVX_CUDA_TRY(cudaMemcpyAsync(&tl[1], LL.off + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
+    FVX_CUDA_TRY(cudaMemcpyAsync(&tl[2], par_cnt + npar - 1, 4, cudaMemcpyDeviceToHost, s));
+    FVX_CUDA_TRY(cudaMemcpyAsync(&tl[3], par_off + npar - 1, 4, cudaMemcpyDeviceToHost, s));
+    FVX_CUDA_TRY(cudaMemcpyAsync(&tl[4], near_cnt + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
+    FVX_CUDA_TRY(cudaMemcpyAsync(&tl[5], far_off + nleaf - 1, 4, cudaMemcpyDeviceToHost, s));
+    FVX_CUDA_TRY(cudaMemcpyAsync(&flags, ovf, 4, cudaMemcpyDeviceToHost, s));
+    FVX_CUDA_TRY(cudaStreamSynchronize(s));
+    if (!(flags & 4u)) {
+      near_total = int64_t(tl[4]) + tl[5];
+      far_total = 0;
+      lrn_total = int64_t(tl[0]) + tl[1];
+      par_total = int64_t(tl[2]) + tl[3];
+      if ((rc = grow(T->lrn_leaf, 4 * size_t(lrn_total + 1))) ||
+          (rc = grow(T->lrn_cell, 4 * size_t(lrn_total + 1))) ||
+          (rc = grow(T->par_par, 4 * size_t(par_total + 1))) ||
+          (rc = grow(T->par_cell, 4 * size_t(par_total + 1))))
+        return rc;
+      compact_slots_kernel<<<(nleaf * 32 + 255) / 256, 256, 0, s>>>(
+          nleaf, kSlotLrn, LL.cnt, LL.off, P<int>(T->lrn_slot), P<int>(T->lrn_leaf),
+          P<int>(T->lrn_cell));
+      FVX_LAUNCH_CHECK();
+      compact_slots_kernel<<<(npar * 32 + 255) / 256, 256, 0, s>>>(
+          npar, kSlotPar, par_cnt, par_off, P<int>(T->par_slot), P<int>(T->par_par),
+          P<int>(T->par_cell));
+      FVX_LAUNCH_CHECK();
+      T->n_learned = static_cast<int>(lrn_total);
+      T->n_parent_pairs = static_cast<int>(par_total);
+      slotted = true;
+    }
+  }
+  if (!slotted) {
   FVX_CUDA_TRY(cudaMemsetAsync(ovf, 0, 24, s));
   DualLists D{};
   if (dual) {
@@ -1904,6 +2003,8 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
         static_cast<int>(near_total), static_cast<int>(far_total), ovf, LL);
   }
   FVX_LAUNCH_CHECK();
+
+  }
   ST.pos = pos;
   ST.n = n;
   ST.leaf_target = leaf_target;
@@ -2105,6 +2206,15 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
 
 extern "C" {
 
+int fvx_tree_set_list_slots(fvx_tree* T, int near, int lrn, int par) {
+  FVX_ARG_CHECK(T != nullptr && near >= 0 && lrn >= 0 && par >= 0, "bad slot capacities");
+  T->slot_near = near;
+  T->slot_lrn = lrn;
+  T->slot_par = par;
+  T->st.valid = false;
+  return FVX_OK;
+}
+
 int fvx_tree_hint_same_positions(fvx_tree* T) {
   FVX_ARG_CHECK(T != nullptr, "null tree handle");
   T->reuse_next = true;
@@ -2131,6 +2241,7 @@ void fvx_tree_destroy(fvx_tree* T) {
                          &T->lrn_cell, &T->leaf_local, &T->val_X, &T->val_T, &T->val_A,
                          &T->val_Y, &T->val_scale, &T->val_err, &T->val_fb, &T->val_stats,
                          &T->dual_meta, &T->par_par, &T->par_cell, &T->parent_local,
+                         &T->lrn_slot, &T->par_slot,
                          &T->pair_partial};
   for (auto* b : bufs)
     if (b->p) cudaFree(b->p);

@@ -83,6 +83,10 @@ class TreeSweeper:
         self.far_method = method
         self.theta_local = th
 
+    def set_list_slots(self, near=512, lrn=1024, par=1024):
+        """Slot capacities of the one-pass two-level lists (0: always count)."""
+        _capi.check(self.lib.fvx_tree_set_list_slots(self.handle, int(near), int(lrn), int(par)))
+
     def set_validation(self, samples=256, tol=0.1):
         """Per-sweep FP64 validation of the local-expansion path: ``samples``
         strided (leaf, cell) pairs per sweep; a pair whose expansion error

@@ -246,6 +246,11 @@ int fvx_tree_set_validation(fvx_tree* tree, int samples, double tol);
  * evaluation recomputed.  A sweep with another position array, count, opening
  * angle, leaf size or far-field method builds anew whatever the hint. */
 int fvx_tree_hint_same_positions(fvx_tree* tree);
+/* fvx_tree_set_list_slots: capacities of the one-pass form of the two-level
+ * lists (near leaves and local cells per leaf, cells per parent; defaults 512,
+ * 1024, 1024): the lists are written into fixed slots without a counting pass,
+ * a slot overflow falls back to counting; any 0 = always count. */
+int fvx_tree_set_list_slots(fvx_tree* tree, int near, int lrn, int par);
 int fvx_tree_last_validation(fvx_tree* tree, double* out);
 int fvx_tree_sample_pairs(fvx_tree* tree, int list, int max_pairs, void* X, float* T, float* A,
                           int* n_out, void* stream);

@@ -136,3 +136,25 @@ def test_reused_structure_matches_a_full_build(cuda, far):
     tol = 0.0 if far == "m2p" else 1e-5 * np.abs(b).max()
     assert np.abs(a - b).max() <= tol
     assert _capi.status_read_and_clear() == 0
+
+
+def test_one_pass_lists_and_their_overflow_fallback(cuda):
+    """The two-level lists written in one pass into slots, with slots so small
+    that they overflow (counting fallback), and with the counting pass only,
+    give the same sweep."""
+    pos, gam, sig, _ = slab_wake(1 << 15)
+    n = pos.shape[0]
+    P, G, S = _dev(pos, cuda), _dev(gam, cuda), _dev(sig, cuda)
+    outs = []
+    for slots in ((512, 1024, 1024), (4, 4, 4), (0, 0, 0)):
+        ts = TreeSweeper(theta=0.5, leaf_target=32)
+        ts.set_far_field("m2l")
+        ts.set_validation(0)
+        ts.set_list_slots(*slots)
+        out = torch.empty((n, 3), dtype=torch.float64, device=cuda)
+        stats = ts.sweep(_capi.PAIR_VELOCITY, "winckelmans", P, G, S, n, out, check=True).copy()
+        outs.append((out.cpu().numpy(), stats))
+    ref = outs[2][0]
+    for o, st in outs[:2]:
+        assert np.abs(o - ref).max() <= 1e-5 * np.abs(ref).max()
+        assert np.array_equal(st[:5], outs[2][1][:5])
