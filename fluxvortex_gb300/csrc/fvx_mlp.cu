@@ -19,15 +19,16 @@
 //     atomics) for dW = dZ^T H and dH = dZ W, plus element-wise kernels for
 //     the loss gradient, the SiLU backward with bias gradients, and Adam.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "fvx_common.cuh"
+#include "fvx_m2l_tensor.cuh"
 #include "fvx_tc.cuh"
 
 namespace fvx {
 namespace mlp {
 
 constexpr int IN = 48, H = 128, OUT = 32, NFEAT = 35, NOUT = 30;
-constexpr int kThreads = 512;  // forward: four warpgroups
 // packed BF16 weight offsets (elements)
 constexpr int W1o = 0, W2o = W1o + H * IN, W3o = W2o + H * H, W4o = W3o + H * H,
               WN = W4o + OUT * H;
@@ -49,6 +50,7 @@ struct FwdSmem {
   __nv_bfloat16 act[kGroups][128 * H];
   float aux[kGroups][128][4];  // far field: the output scales m/d^2, m/d^3, m/d^4 of each row
   float bias[BN];
+  uint32_t hbias[3 * H / 2];  // F16 form: half the hidden layers' biases, packed F16 pairs
   uint64_t bar[kGroups];
   uint32_t tmem;
 };
@@ -63,24 +65,39 @@ __device__ __forceinline__ float silu(float z) {
   const float h = 0.5f * z;
   return fmaf(h, tanh_approx(h), h);
 }
+// Two SiLUs in packed F16 from two accumulator columns of the halved weights
+// (acc = W x / 2) and the packed halved biases hb: h = z/2 = acc + b/2, then
+// one MUFU operation (tanh.approx.f16x2) and one packed FMA, h + h tanh(h) =
+// z sigmoid(z); the F16 result is the next layer's operand as it stands.
+// Element 0 goes to the low half (the lower address in shared memory).
+__device__ __forceinline__ uint32_t silu_half2(float a0, float a1, uint32_t hb) {
+  uint32_t h, t, s;
+  asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(a1), "f"(a0));
+  asm("add.rn.f16x2 %0, %1, %2;" : "=r"(h) : "r"(h), "r"(hb));
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(h));
+  asm("fma.rn.f16x2 %0, %1, %2, %1;" : "=r"(s) : "r"(h), "r"(t));
+  return s;
+}
 __device__ __forceinline__ float silu_grad(float z) {
   const float s = 1.f / (1.f + __expf(-z));
   return s * (1.f + z * (1.f - s));
 }
 
-// Barrier over the 128 threads of warpgroup g (named barrier 1 + g).
+// Barrier over the N threads of group g (named barrier 1 + g).
+template <int N = 128>
 __device__ __forceinline__ void group_sync(int g) {
-  asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory");
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "n"(N) : "memory");
 }
+template <int N = 128>
 __device__ __forceinline__ bool group_sync_and(int g, bool p) {
   uint32_t r;
   asm volatile(
       "{\n\t.reg .pred q, d;\n\t"
       "setp.ne.u32 q, %1, 0;\n\t"
-      "bar.red.and.pred d, %2, 128, q;\n\t"
+      "bar.red.and.pred d, %2, %3, q;\n\t"
       "selp.u32 %0, 1, 0, d;\n\t}"
       : "=r"(r)
-      : "r"(static_cast<uint32_t>(p)), "r"(1 + g)
+      : "r"(static_cast<uint32_t>(p)), "r"(1 + g), "n"(N)
       : "memory");
   return r != 0;
 }
@@ -92,6 +109,34 @@ __device__ void stage_kmajor(__nv_bfloat16* dst, const __nv_bfloat16* src, int R
     const int r = c / (K / 8), k8 = c % (K / 8);
     const uint4 v = *reinterpret_cast<const uint4*>(src + static_cast<int64_t>(r) * K + 8 * k8);
     *reinterpret_cast<uint4*>(reinterpret_cast<char*>(dst) + tc::kmajor_offset(r, 8 * k8, K)) = v;
+  }
+}
+
+// Eight BF16 values -> eight F16 values (round to nearest; every BF16 weight
+// of magnitude 6.1e-5 to 65504 is exact in F16, smaller ones keep an absolute
+// error below 3e-8).
+__device__ __forceinline__ uint4 bf16x8_to_f16x8(uint4 v, float scale = 1.f) {
+  const __nv_bfloat162* p = reinterpret_cast<const __nv_bfloat162*>(&v);
+  uint4 o;
+  __half2* q = reinterpret_cast<__half2*>(&o);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float2 f = __bfloat1622float2(p[i]);
+    q[i] = __floats2half2_rn(f.x * scale, f.y * scale);
+  }
+  return o;
+}
+
+// As stage_kmajor, converting the BF16 matrix to F16 times `scale` (a power
+// of two: exact unless the product is an F16 subnormal) on the way.
+__device__ void stage_kmajor_f16(__nv_bfloat16* dst, const __nv_bfloat16* src, int R, int K,
+                                 float scale) {
+  const int chunks = R * (K / 8);
+  for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
+    const int r = c / (K / 8), k8 = c % (K / 8);
+    const uint4 v = *reinterpret_cast<const uint4*>(src + static_cast<int64_t>(r) * K + 8 * k8);
+    *reinterpret_cast<uint4*>(reinterpret_cast<char*>(dst) + tc::kmajor_offset(r, 8 * k8, K)) =
+        bf16x8_to_f16x8(v, scale);
   }
 }
 
@@ -130,6 +175,26 @@ __device__ __forceinline__ PairGeom pair_geom(const float* rec, float cTx, float
   return g;
 }
 
+// A cell record into registers with ten 16-byte loads (records are 160 bytes
+// apart from a 256-byte aligned base); read with constant indices only, so
+// that the array stays in registers.
+struct RecRegs {
+  float v[kRecFloats];
+};
+__device__ __forceinline__ RecRegs load_record(const float* rec) {
+  RecRegs r;
+  const float4* r4 = reinterpret_cast<const float4*>(rec);
+#pragma unroll
+  for (int q = 0; q < kRecFloats / 4; ++q) {
+    const float4 x = __ldg(r4 + q);
+    r.v[4 * q] = x.x;
+    r.v[4 * q + 1] = x.y;
+    r.v[4 * q + 2] = x.z;
+    r.v[4 * q + 3] = x.w;
+  }
+  return r;
+}
+
 __device__ __forceinline__ PairScale pair_scale(const PairGeom& g) {
   PairScale s;
   s.s2 = g.m * g.id * g.id;
@@ -153,13 +218,11 @@ __device__ __forceinline__ PairScale pair_features(const float* rec, float cTx, 
   return pair_scale(g);
 }
 
-// Multipole to local, analytic: the local expansion at the target centre of
-// the source cell's quadrupole expansion, in the network's normalised output
-// units (unit distance along n = R/d; f = the pair's FP32 features).  With
-// C-scaled moments the vector potential is Psi_m = -(M0_m phi - M1_ma d_a phi
-// + 1/2 M2_mab d_ab phi), phi = 1/|r|, and u_i = eps_ijm d_j Psi_m; the
-// derivatives of phi at |r| = 1 are contracted with the moments in closed
-// form (d^p phi = sum over index pairings of (-1)^(p-k) (2p-2k-1)!! n..n d..d).
+// Multipole to local, analytic (m2l_tensor, fvx_m2l_tensor.cuh): the local
+// expansion at the target centre of the source cell's quadrupole expansion,
+// in the network's normalised output units (unit distance along n = R/d).
+// With C-scaled moments the vector potential is Psi_m = -(M0_m phi - M1_ma
+// d_a phi + 1/2 M2_mab d_ab phi), phi = 1/|r|, and u_i = eps_ijm d_j Psi_m.
 // Normalised moments of one pair, read from the 48 features...
 struct FeatureMoments {
   const float* f;
@@ -170,7 +233,7 @@ struct FeatureMoments {
   __device__ float m2(int q) const { return f[17 + q]; }   // M2 / (m h_S^2)
 };
 // ... or straight from the cell record (same roundings as pair_features), so
-// that the analytic kernel keeps only one component's moments live
+// that the analytic kernel reads each moment when it is first used
 struct RecordMoments {
   const float* rec;
   float nx, ny, nz, hs_d, im, ih;
@@ -181,101 +244,8 @@ struct RecordMoments {
   __device__ float m2(int q) const { return rec[19 + q] * im * ih * ih; }
 };
 
-// Multipole to local, analytic: the local expansion at the target centre of
-// the source cell's quadrupole expansion, in the network's normalised output
-// units (unit distance along n = R/d).  With C-scaled moments the vector
-// potential is Psi_m = -(M0_m phi - M1_ma d_a phi + 1/2 M2_mab d_ab phi),
-// phi = 1/|r|, and u_i = eps_ijm d_j Psi_m; the derivatives of phi at |r| = 1
-// are contracted with the moments in closed form (d^p phi = sum over index
-// pairings of (-1)^(p-k) (2p-2k-1)!! n..n d..d).
-// Output accumulators of m2l_core: a register array, or a thread's column of
-// a shared-memory block (stride = the block size), whose dynamic indexing
-// (the output row depends on the loop's component) stays out of local memory.
-struct SharedColumn {
-  float* base;
-  int stride;
-  __device__ float& operator[](int q) const { return base[q * stride]; }
-};
-
-// x[i] of a 3-vector held in registers, for a run-time i (selects, not a
-// local-memory array)
-__device__ __forceinline__ float sel3(float x0, float x1, float x2, int i) {
-  return i == 0 ? x0 : (i == 1 ? x1 : x2);
-}
-
-template <class Src, class Out>
-__device__ __forceinline__ void m2l_core(const Src& src, Out&& out) {
-  const float nv[3] = {src.n(0), src.n(1), src.n(2)};
-  const float hs = src.hs();
-#pragma unroll
-  for (int q = 0; q < NOUT; ++q) out[q] = 0.f;
-#pragma unroll 1
-  for (int m = 0; m < 3; ++m) {
-    const float c = src.c(m);
-    const float v[3] = {src.m1(3 * m) * hs, src.m1(3 * m + 1) * hs, src.m1(3 * m + 2) * hs};
-    const float h2 = hs * hs;
-    float q6[6];
-#pragma unroll
-    for (int u = 0; u < 6; ++u) q6[u] = src.m2(6 * m + u);
-    const float Q[3][3] = {{q6[0] * h2, q6[1] * h2, q6[2] * h2},
-                           {q6[1] * h2, q6[3] * h2, q6[4] * h2},
-                           {q6[2] * h2, q6[4] * h2, q6[5] * h2}};
-    const float vn = v[0] * nv[0] + v[1] * nv[1] + v[2] * nv[2];
-    float qn[3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) qn[j] = Q[j][0] * nv[0] + Q[j][1] * nv[1] + Q[j][2] * nv[2];
-    const float nqn = qn[0] * nv[0] + qn[1] * nv[1] + qn[2] * nv[2];
-    const float tr = Q[0][0] + Q[1][1] + Q[2][2];
-#pragma unroll
-    for (int jj = 0; jj < 2; ++jj) {
-      const int j = (m + 1 + jj) % 3;      // the two j != m
-      const int i = 3 - m - j;
-      const float sg = ((j - i + 3) % 3 == 1) ? 1.f : -1.f;  // eps_ijm
-      const float nj = sel3(nv[0], nv[1], nv[2], j);
-      const float vj = sel3(v[0], v[1], v[2], j);
-      const float qnj = sel3(qn[0], qn[1], qn[2], j);
-      // u: c phi_j - v_a phi_aj + 1/2 Q_ab phi_abj
-      const float p1 = -nj * c - (3.f * vn * nj - vj) + 0.5f * (-15.f * nqn * nj + 3.f * tr * nj + 6.f * qnj);
-      out[i] -= sg * p1;
-#pragma unroll
-      for (int n = 0; n < 3; ++n) {
-        const float dl = j == n ? 1.f : 0.f;
-        const float nn = nv[n];
-        const float phi2 = 3.f * nj * nn - dl;
-        const float vphi3 = -15.f * vn * nj * nn + 3.f * (vj * nn + v[n] * nj + vn * dl);
-        const float qjn = sel3(Q[0][n], Q[1][n], Q[2][n], j);
-        const float qphi4 = 105.f * nqn * nj * nn -
-                            15.f * (tr * nj * nn + 2.f * qnj * nn + 2.f * qn[n] * nj + nqn * dl) +
-                            3.f * tr * dl + 6.f * qjn;
-        out[3 + 3 * i + n] -= sg * (c * phi2 - vphi3 + 0.5f * qphi4);
-      }
-#pragma unroll
-      for (int u = 0; u < 6; ++u) {
-        const int k = u < 3 ? 0 : (u < 5 ? 1 : 2);
-        const int n = u < 3 ? u : (u < 5 ? u - 2 : 2);
-        const float nk = nv[k], nn = nv[n];
-        const float djk = j == k ? 1.f : 0.f, djn = j == n ? 1.f : 0.f, dkn = k == n ? 1.f : 0.f;
-        const float nnn = nj * nk * nn;
-        const float dsum = djk * nn + djn * nk + dkn * nj;
-        const float phi3 = -15.f * nnn + 3.f * dsum;
-        const float vphi4 = 105.f * vn * nnn -
-                            15.f * (vj * nk * nn + v[k] * nj * nn + v[n] * nj * nk + vn * dsum) +
-                            3.f * (vj * dkn + v[k] * djn + v[n] * djk);
-        const float qjn = sel3(Q[0][n], Q[1][n], Q[2][n], j);
-        const float qjk = sel3(Q[0][k], Q[1][k], Q[2][k], j);
-        const float qphi5 =
-            -945.f * nqn * nnn +
-            105.f * (tr * nnn + 2.f * (qnj * nk * nn + qn[k] * nj * nn + qn[n] * nj * nk) + nqn * dsum) -
-            15.f * (2.f * (qnj * dkn + qn[k] * djn + qn[n] * djk) + nj * (tr * dkn + 2.f * Q[k][n]) +
-                    nk * (tr * djn + 2.f * qjn) + nn * (tr * djk + 2.f * qjk));
-        out[12 + 6 * i + u] -= sg * (c * phi3 - vphi4 + 0.5f * qphi5);
-      }
-    }
-  }
-}
-
 __device__ __forceinline__ void m2l_quadrupole(const float* f, float* out) {
-  m2l_core(FeatureMoments{f}, out);
+  m2l_tensor(FeatureMoments{f}, out);
 }
 
 __device__ __forceinline__ float3 leaf_center(uint32_t key, float h) {
@@ -344,6 +314,45 @@ __device__ void epilogue_hidden(uint32_t tmem, int row, const float* bias, __nv_
   }
 }
 
+// Inference form of epilogue_hidden: F16 activations.  The layer's weights
+// are halved (acc = z/2 - b/2) and hbias holds its halved biases as packed F16
+// pairs, so each pair of columns is one silu_half2.
+// The TMEM loads are double-buffered: the next 16 columns load while the
+// current ones are processed.
+__device__ __forceinline__ void silu_chunk_f16(const uint32_t (&r)[16], const uint32_t* hbias,
+                                               char* base, int row, int c0) {
+  __align__(16) uint32_t b[8];
+  const uint4 h0 = *reinterpret_cast<const uint4*>(hbias + c0 / 2);
+  const uint4 h1 = *reinterpret_cast<const uint4*>(hbias + c0 / 2 + 4);
+  const uint32_t hb[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    b[i] = silu_half2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]), hb[i]);
+  *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, c0, H)) =
+      *reinterpret_cast<uint4*>(&b[0]);
+  *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, c0 + 8, H)) =
+      *reinterpret_cast<uint4*>(&b[4]);
+}
+// Columns [cb, cb + NC) of the row (NC a multiple of 32).
+template <int NC>
+__device__ void epilogue_hidden_f16(uint32_t tmem, int row, int cb, const uint32_t* hbias,
+                                    void* act) {
+  const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * ((threadIdx.x >> 5) & 3)) << 16);
+  char* base = reinterpret_cast<char*>(act);
+  uint32_t ra[16], rb[16];
+  tc::tmem_ld16_issue(taddr + cb, ra);
+  tc::tmem_ld_wait(ra);
+#pragma unroll
+  for (int c0 = cb; c0 < cb + NC; c0 += 32) {
+    tc::tmem_ld16_issue(taddr + c0 + 16, rb);
+    silu_chunk_f16(ra, hbias, base, row, c0);
+    tc::tmem_ld_wait(rb);
+    if (c0 + 32 < cb + NC) tc::tmem_ld16_issue(taddr + c0 + 32, ra);
+    silu_chunk_f16(rb, hbias, base, row, c0 + 16);
+    if (c0 + 32 < cb + NC) tc::tmem_ld_wait(ra);
+  }
+}
+
 __device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& ph) {
   const bool ok = mbar_wait(bar, ph);
   ph ^= 1u;
@@ -352,15 +361,24 @@ __device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& ph) {
 }
 
 // group-local fence + barrier: smem writes -> async proxy, TMEM reads done
+template <int N = 128>
 __device__ __forceinline__ void group_handoff(int g) {
   tc::fence_smem_to_async();
   tc::fence_before_sync();
-  group_sync(g);
+  group_sync<N>(g);
   tc::fence_after_sync();
 }
 
-template <bool FAR>
-__global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int rows,
+// HALF: F16 operands and activations (weights converted while staged, the
+// packed SiLU of epilogue_hidden_f16) -- the inference form, always taken by
+// the treecode far field; the training forward (with stored pre-activations
+// and activations) keeps BF16, the type its backward GEMMs read.
+// TPG: threads per group and 128-row tile, 128 or (F16 form) 256; with 256 the
+// two halves of a group split each row's features and hidden columns, which
+// doubles the warps that hide the epilogues' latencies (1024 threads, at most
+// 64 registers each).
+template <bool FAR, bool HALF, int TPG>
+__global__ void __launch_bounds__(kGroups * TPG, 1) mlp_fwd_kernel(FwdArgs<FAR> A, int rows,
                                                            const __nv_bfloat16* __restrict__ W,
                                                            const float* __restrict__ bias) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -370,17 +388,32 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
     for (int g = 0; g < kGroups; ++g) mbar_init(&S.bar[g], 1);
     fence_mbar_init();
   }
-  stage_kmajor(S.w1, W + W1o, H, IN);
-  stage_kmajor(S.w2, W + W2o, H, H);
-  stage_kmajor(S.w3, W + W3o, H, H);
-  stage_kmajor(S.w4, W + W4o, OUT, H);
+  static_assert(HALF || !FAR, "the far field runs the F16 form");
+  static_assert(TPG == 128 || (TPG == 256 && HALF), "128 threads per group, or 256 in F16");
+  if constexpr (HALF) {
+    // hidden layers halved: their accumulators are z/2, the tanh argument
+    stage_kmajor_f16(S.w1, W + W1o, H, IN, 0.5f);
+    stage_kmajor_f16(S.w2, W + W2o, H, H, 0.5f);
+    stage_kmajor_f16(S.w3, W + W3o, H, H, 0.5f);
+    stage_kmajor_f16(S.w4, W + W4o, OUT, H, 1.f);
+    for (int i = threadIdx.x; i < 3 * H / 2; i += blockDim.x) {
+      const __half2 hb = __floats2half2_rn(0.5f * bias[2 * i], 0.5f * bias[2 * i + 1]);
+      S.hbias[i] = *reinterpret_cast<const uint32_t*>(&hb);
+    }
+  } else {
+    stage_kmajor(S.w1, W + W1o, H, IN);
+    stage_kmajor(S.w2, W + W2o, H, H);
+    stage_kmajor(S.w3, W + W3o, H, H);
+    stage_kmajor(S.w4, W + W4o, OUT, H);
+  }
   for (int i = threadIdx.x; i < BN; i += blockDim.x) S.bias[i] = bias[i];
   tc::fence_smem_to_async();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  const int grp = threadIdx.x >> 7;   // warpgroup
+  const int grp = threadIdx.x / TPG;  // group
   const int lt = threadIdx.x & 127;   // row of the group's tile
+  const int half = (threadIdx.x & (TPG - 1)) >> 7;  // which half of the row (TPG 256)
   const uint32_t tmem = S.tmem + static_cast<uint32_t>(128 * grp);
   const uint32_t lane_base = static_cast<uint32_t>(32 * ((threadIdx.x >> 5) & 3)) << 16;
   __nv_bfloat16* act = S.act[grp];
@@ -401,36 +434,51 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
         if (act_row) {
           leaf = A.f.pair_leaf[row];
           const float3 cT = leaf_center(A.f.leaf_key[leaf], A.f.h);
-          const PairScale sc = pair_features(
-              A.f.rec + static_cast<int64_t>(A.f.pair_cell[row]) * kRecFloats, cT.x, cT.y, cT.z,
-              A.f.h, f);
-          ax[0] = sc.s2;
-          ax[1] = sc.s3;
-          ax[2] = sc.s4;
+          const RecRegs rr =
+              load_record(A.f.rec + static_cast<int64_t>(A.f.pair_cell[row]) * kRecFloats);
+          const PairScale sc = pair_features(rr.v, cT.x, cT.y, cT.z, A.f.h, f);
+          if (half == 0) {
+            ax[0] = sc.s2;
+            ax[1] = sc.s3;
+            ax[2] = sc.s4;
+          }
         } else {
           for (int q = 0; q < IN; ++q) f[q] = 0.f;
         }
-        for (int k8 = 0; k8 < IN / 8; ++k8) {
-          __align__(16) __nv_bfloat162 b[4];
-          for (int q = 0; q < 4; ++q) b[q] = __floats2bfloat162_rn(f[8 * k8 + 2 * q], f[8 * k8 + 2 * q + 1]);
+        // 16-byte chunks k8 of the row (constant indices into f after unrolling)
+        auto put = [&](int k8) {
+          __align__(16) __half2 b[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) b[q] = __floats2half2_rn(f[8 * k8 + 2 * q], f[8 * k8 + 2 * q + 1]);
           *reinterpret_cast<uint4*>(base + tc::kmajor_offset(lt, 8 * k8, IN)) =
               *reinterpret_cast<uint4*>(b);
+        };
+        if (TPG == 128) {
+#pragma unroll
+          for (int k8 = 0; k8 < IN / 8; ++k8) put(k8);
+        } else if (half == 0) {
+#pragma unroll
+          for (int k8 = 0; k8 < IN / 16; ++k8) put(k8);
+        } else {
+#pragma unroll
+          for (int k8 = IN / 16; k8 < IN / 8; ++k8) put(k8);
         }
       } else {
         for (int k8 = 0; k8 < IN / 8; ++k8) {
           uint4 v = make_uint4(0, 0, 0, 0);
           if (act_row)
             v = *reinterpret_cast<const uint4*>(A.r.X + static_cast<int64_t>(row) * IN + 8 * k8);
+          if constexpr (HALF) v = bf16x8_to_f16x8(v);
           *reinterpret_cast<uint4*>(base + tc::kmajor_offset(lt, 8 * k8, IN)) = v;
         }
       }
     }
-    const __nv_bfloat16* wl[3] = {S.w1, S.w2, S.w3};
     for (int l = 0; l < 3 && ok; ++l) {
-      group_handoff(grp);
-      if (lt == 0)
-        tc::gemm_issue(tmem, act, wl[l], l == 0 ? IN : H, tc::idesc_bf16(128, H), false, bar, 0);
-      if (!group_sync_and(grp, wait_mma(bar, ph))) {
+      group_handoff<TPG>(grp);
+      if (lt == 0 && half == 0)
+        tc::gemm_issue(tmem, act, l == 0 ? S.w1 : (l == 1 ? S.w2 : S.w3), l == 0 ? IN : H,
+                       HALF ? tc::idesc_f16(128, H) : tc::idesc_bf16(128, H), false, bar, 0);
+      if (!group_sync_and<TPG>(grp, wait_mma(bar, ph))) {
         ok = false;
         break;
       }
@@ -440,16 +488,23 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
         if (A.r.z_store && act_row) zo = A.r.z_store + (static_cast<int64_t>(l) * rows + row) * H;
         if (A.r.h_store && act_row) ho = A.r.h_store + (static_cast<int64_t>(l) * rows + row) * H;
       }
-      epilogue_hidden(tmem, lt, S.bias + l * H, act, zo, ho);
+      if constexpr (HALF)
+        epilogue_hidden_f16<H * 128 / TPG>(tmem, lt, half * (H * 128 / TPG), S.hbias + l * H / 2,
+                                           act);
+      else
+        epilogue_hidden(tmem, lt, S.bias + l * H, act, zo, ho);
     }
     if (!ok) break;
-    group_handoff(grp);
-    if (lt == 0) tc::gemm_issue(tmem, act, S.w4, H, tc::idesc_bf16(128, OUT), false, bar, 0);
-    if (!group_sync_and(grp, wait_mma(bar, ph))) {
+    group_handoff<TPG>(grp);
+    if (lt == 0 && half == 0)
+      tc::gemm_issue(tmem, act, S.w4, H, HALF ? tc::idesc_f16(128, OUT) : tc::idesc_bf16(128, OUT),
+                     false, bar, 0);
+    if (!group_sync_and<TPG>(grp, wait_mma(bar, ph))) {
       ok = false;
       break;
     }
-    if constexpr (FAR) {
+    // the output stage runs on the first half of the group
+    if (FAR && half == 0) {
       // the learned residual of this row, back to physical units (the analytic
       // translation is added by its own kernel)
       float x[OUT];
@@ -500,7 +555,7 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
         }
       }
     }
-    for (int c0 = 0; c0 < OUT && !FAR; c0 += 16) {
+    for (int c0 = 0; c0 < OUT && !FAR && half == 0; c0 += 16) {
       float v[16];
       tc::tmem_ld16(tmem + lane_base + c0, v);
       if constexpr (FAR) continue;
@@ -516,10 +571,10 @@ __global__ void __launch_bounds__(kThreads) mlp_fwd_kernel(FwdArgs<FAR> A, int r
       }
     }
     tc::fence_before_sync();
-    group_sync(grp);
+    group_sync<TPG>(grp);
     tc::fence_after_sync();
   }
-  if (!ok && lt == 0) flag_status(kStatusTimeout);
+  if (!ok && lt == 0 && half == 0) flag_status(kStatusTimeout);
   tc::fence_before_sync();
   __syncthreads();
   if (threadIdx.x < 32) tc::tmem_dealloc(S.tmem, 128 * kGroups);
@@ -651,22 +706,20 @@ __global__ void __launch_bounds__(kM2lThreads) m2l_pairs_kernel(int npairs, cons
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool act_row = row < npairs;
-  __shared__ float s_acc[NOUT * kM2lThreads];
-  const SharedColumn acc{s_acc + threadIdx.x, kM2lThreads};
+  float a[NOUT];
+#pragma unroll
+  for (int q = 0; q < NOUT; ++q) a[q] = 0.f;
   PairScale sc{0.f, 0.f, 0.f};
   int leaf = 0;
   if (act_row) {
     leaf = pair_leaf[row];
     const float3 cT = leaf_center(leaf_key[leaf], h);
-    const float* r = rec + static_cast<int64_t>(pair_cell[row]) * kRecFloats;
-    const PairGeom g = pair_geom(r, cT.x, cT.y, cT.z);
-    const RecordMoments src{r, g.Rx * g.id, g.Ry * g.id, g.Rz * g.id, g.hS * g.id, g.im, g.ih};
-    m2l_core(src, acc);
+    const RecRegs rr = load_record(rec + static_cast<int64_t>(pair_cell[row]) * kRecFloats);
+    const PairGeom g = pair_geom(rr.v, cT.x, cT.y, cT.z);
+    const RecordMoments src{rr.v, g.Rx * g.id, g.Ry * g.id, g.Rz * g.id, g.hS * g.id, g.im, g.ih};
+    m2l_tensor(src, a);
     sc = pair_scale(g);
   }
-  float a[NOUT];
-#pragma unroll
-  for (int q = 0; q < NOUT; ++q) a[q] = act_row ? acc[q] : 0.f;
   const int my = act_row ? leaf : -1 - lane;
   float x[32];
 #pragma unroll
@@ -908,14 +961,16 @@ int set_smem(K kernel, size_t bytes) {
 
 // Fused learned far field for the treecode: local expansions of the learned
 // (leaf, cell) pairs added into leaf_local[n_leaves][32] (zeroed by the caller).
+// tpg: threads per 128-row tile, 128 or 256 (mlp_fwd_kernel's TPG).
 int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
                         const uint32_t* leaf_key, const float* rec, float h, const void* W,
-                        const float* bias, float* leaf_local, cudaStream_t s) {
+                        const float* bias, float* leaf_local, int tpg, cudaStream_t s) {
   using namespace mlp;
   if (npairs <= 0) return FVX_OK;
   static int done = 0;
   if (!done) {
-    int rc = set_smem(mlp_fwd_kernel<true>, sizeof(FwdSmem));
+    int rc = set_smem(mlp_fwd_kernel<true, true, 128>, sizeof(FwdSmem));
+    if (!rc) rc = set_smem(mlp_fwd_kernel<true, true, 256>, sizeof(FwdSmem));
     if (rc) return rc;
     done = 1;
   }
@@ -924,8 +979,12 @@ int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
   A.f = FarIO{pair_leaf, pair_cell, leaf_key, rec, h, leaf_local};
   const int nctas = ((npairs + 127) / 128 + kGroups - 1) / kGroups;
   const int grid = nctas < device_sm_count() ? nctas : device_sm_count();
-  mlp_fwd_kernel<true><<<grid, kThreads, sizeof(FwdSmem), s>>>(
-      A, npairs, static_cast<const __nv_bfloat16*>(W), bias);
+  if (tpg == 256)
+    mlp_fwd_kernel<true, true, 256><<<grid, kGroups * 256, sizeof(FwdSmem), s>>>(
+        A, npairs, static_cast<const __nv_bfloat16*>(W), bias);
+  else
+    mlp_fwd_kernel<true, true, 128><<<grid, kGroups * 128, sizeof(FwdSmem), s>>>(
+        A, npairs, static_cast<const __nv_bfloat16*>(W), bias);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
@@ -984,7 +1043,8 @@ int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, f
   if (rows == 0) return FVX_OK;
   static int done = 0;
   if (!done) {
-    int rc = set_smem(mlp_fwd_kernel<false>, sizeof(FwdSmem));
+    int rc = set_smem(mlp_fwd_kernel<false, false, 128>, sizeof(FwdSmem));
+    if (!rc) rc = set_smem(mlp_fwd_kernel<false, true, 128>, sizeof(FwdSmem));
     if (rc) return rc;
     done = 1;
   }
@@ -994,7 +1054,10 @@ int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, f
   A.f = FarIO{nullptr, nullptr, nullptr, nullptr, 0.f, nullptr};
   const int nctas = ((rows + 127) / 128 + kGroups - 1) / kGroups;
   const int grid = nctas < fvx::device_sm_count() ? nctas : fvx::device_sm_count();
-  mlp_fwd_kernel<false><<<grid, kThreads, sizeof(FwdSmem), static_cast<cudaStream_t>(stream)>>>(
+  // without stores it is inference: the F16 form the treecode far field runs
+  auto kern = (z_store || h_store) ? mlp_fwd_kernel<false, false, 128>
+                                   : mlp_fwd_kernel<false, true, 128>;
+  kern<<<grid, kGroups * 128, sizeof(FwdSmem), static_cast<cudaStream_t>(stream)>>>(
       A, rows, static_cast<const __nv_bfloat16*>(W), bias);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
