@@ -106,6 +106,16 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 
 __device__ __forceinline__ void flag_status(unsigned bits) { atomicOr(&g_status, bits); }
 
+// 1/sqrt(x) as the single approximate hardware instruction with subnormal
+// inputs and results flushed to zero: for arguments that are normal floats
+// (r^2 + sigma^2 with sigma >= 1e-6), the same value as rsqrtf without its
+// subnormal handling.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __host__ __device__ __forceinline__ int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
 
 __host__ __device__ __forceinline__ bool aligned16(const void* p) {

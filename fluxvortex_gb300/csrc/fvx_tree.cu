@@ -962,13 +962,17 @@ struct NearX2 {
 // so q comes from three fused multiply-adds seeded with s^2, r^2 is never
 // formed, and every factor stays bounded (no FP32 overflow for cores down to
 // the integrator's 1e-6 floor).
-template <int MODE>
-__device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, int nt, int stride,
+// NG: rows between a lane group's consecutive rows (the G/2 lane groups of
+// small leaves interleave), a compile-time constant so that the unrolled loop
+// addresses its rows by immediate offsets.
+template <int MODE, int NG>
+__device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, int nt,
                                              uint64_t TX, uint64_t TY, uint64_t TZ, uint64_t GX,
                                              uint64_t GY, uint64_t GZ, uint64_t* acc) {
   const uint64_t ONE = x2::pack(1.f, 1.f), CM3 = x2::pack(-3.f, -3.f);
+#pragma unroll 8
   for (int i = 0; i < nt; ++i) {
-    const int k = i * stride;
+    const int k = i * NG;
     const ulonglong2 q0 = tile[k].q[0], q1 = tile[k].q[1], q2 = tile[k].q[2],
                      q3 = tile[k].q[3];
     const uint64_t DX = x2::add(TX, q0.x), DY = x2::add(TY, q0.y), DZ = x2::add(TZ, q1.x);
@@ -977,7 +981,7 @@ __device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, in
     Q = x2::fma(DZ, DZ, Q);
     float qa, qb;
     x2::unpack(Q, qa, qb);
-    const uint64_t T = x2::pack(rsqrtf(qa), rsqrtf(qb));
+    const uint64_t T = x2::pack(rsqrt_ftz(qa), rsqrt_ftz(qb));
     const uint64_t T2 = x2::mul(T, T);
     const uint64_t T3 = x2::mul(T2, T);
     const uint64_t F = x2::mul(T3, x2::fma(q2.x, T2, ONE));
@@ -1148,8 +1152,13 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
           }
           __syncthreads();
           uint64_t acc2[3] = {0ull, 0ull, 0ull};
-          near_tile_x2<MODE>(s_x2 + (G == 1 ? 0 : grp), rows / ng, ng, TX, TY, TZ, GX, GY, GZ,
-                             acc2);
+          const NearX2* tile = s_x2 + (G == 1 ? 0 : grp);
+          if (ng == 1)
+            near_tile_x2<MODE, 1>(tile, rows, TX, TY, TZ, GX, GY, GZ, acc2);
+          else if (ng == 2)
+            near_tile_x2<MODE, 2>(tile, rows / 2, TX, TY, TZ, GX, GY, GZ, acc2);
+          else
+            near_tile_x2<MODE, 4>(tile, rows / 4, TX, TY, TZ, GX, GY, GZ, acc2);
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             float a0, a1;
