@@ -696,6 +696,7 @@ __global__ void pair_targets_kernel(int npairs, int stride, int slices,
 // ---- analytic far field of the local-expansion path (no network) ---------------------
 // One thread per (leaf, cell) pair: features -> M2L -> physical units -> sum
 // over the warp's runs of equal leaves -> atomics into the leaf's expansion.
+// Resident CTAs (two per SM at 128 registers) stride over blocks of pairs.
 constexpr int kM2lThreads = 256;
 
 __global__ void __launch_bounds__(kM2lThreads) m2l_pairs_kernel(int npairs, const int* __restrict__ pair_leaf,
@@ -703,60 +704,62 @@ __global__ void __launch_bounds__(kM2lThreads) m2l_pairs_kernel(int npairs, cons
                                                         const uint32_t* __restrict__ leaf_key,
                                                         const float* __restrict__ rec, float h,
                                                         float* __restrict__ leaf_local) {
-  const int row = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  const bool act_row = row < npairs;
-  float a[NOUT];
+  for (int base = blockIdx.x * kM2lThreads; base < npairs; base += gridDim.x * kM2lThreads) {
+    const int row = base + threadIdx.x;
+    const bool act_row = row < npairs;
+    float a[NOUT];
 #pragma unroll
-  for (int q = 0; q < NOUT; ++q) a[q] = 0.f;
-  PairScale sc{0.f, 0.f, 0.f};
-  int leaf = 0;
-  if (act_row) {
-    leaf = pair_leaf[row];
-    const float3 cT = leaf_center(leaf_key[leaf], h);
-    const RecRegs rr = load_record(rec + static_cast<int64_t>(pair_cell[row]) * kRecFloats);
-    const PairGeom g = pair_geom(rr.v, cT.x, cT.y, cT.z);
-    const RecordMoments src{rr.v, g.Rx * g.id, g.Ry * g.id, g.Rz * g.id, g.hS * g.id, g.im, g.ih};
-    m2l_tensor(src, a);
-    sc = pair_scale(g);
-  }
-  const int my = act_row ? leaf : -1 - lane;
-  float x[32];
+    for (int q = 0; q < NOUT; ++q) a[q] = 0.f;
+    PairScale sc{0.f, 0.f, 0.f};
+    int leaf = 0;
+    if (act_row) {
+      leaf = pair_leaf[row];
+      const float3 cT = leaf_center(leaf_key[leaf], h);
+      const RecRegs rr = load_record(rec + static_cast<int64_t>(pair_cell[row]) * kRecFloats);
+      const PairGeom g = pair_geom(rr.v, cT.x, cT.y, cT.z);
+      const RecordMoments src{rr.v, g.Rx * g.id, g.Ry * g.id, g.Rz * g.id, g.hS * g.id, g.im, g.ih};
+      m2l_tensor(src, a);
+      sc = pair_scale(g);
+    }
+    const int my = act_row ? leaf : -1 - lane;
+    float x[32];
 #pragma unroll
-  for (int c = 0; c < 32; ++c)
-    x[c] = c < NOUT ? a[c] * (c < 3 ? sc.s2 : (c < 12 ? sc.s3 : sc.s4)) : 0.f;
-  if (__all_sync(0xffffffffu, my == __shfl_sync(0xffffffffu, my, 0))) {
-    // one target for the whole warp (pairs are ordered by target, runs are
-    // long): reduce-scatter by recursive halving, 31 shuffles for the 32
-    // columns; lane c ends with the warp's sum of column c
+    for (int c = 0; c < 32; ++c)
+      x[c] = c < NOUT ? a[c] * (c < 3 ? sc.s2 : (c < 12 ? sc.s3 : sc.s4)) : 0.f;
+    if (__all_sync(0xffffffffu, my == __shfl_sync(0xffffffffu, my, 0))) {
+      // one target for the whole warp (pairs are ordered by target, runs are
+      // long): reduce-scatter by recursive halving, 31 shuffles for the 32
+      // columns; lane c ends with the warp's sum of column c
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) {
-      const bool upper = (lane & off) != 0;
+      for (int off = 16; off >= 1; off >>= 1) {
+        const bool upper = (lane & off) != 0;
 #pragma unroll
-      for (int j = 0; j < off; ++j) {
-        const float send = upper ? x[j] : x[j + off];
-        const float keep = upper ? x[j + off] : x[j];
-        x[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        for (int j = 0; j < off; ++j) {
+          const float send = upper ? x[j] : x[j + off];
+          const float keep = upper ? x[j + off] : x[j];
+          x[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+      }
+      if (lane < NOUT) atomicAdd(leaf_local + static_cast<int64_t>(leaf) * OUT + lane, x[0]);
+    } else {
+      // runs of equal targets inside the warp: segmented sums to each run's
+      // first lane
+      const int up = __shfl_up_sync(0xffffffffu, my, 1);
+      const bool head = act_row && (lane == 0 || up != my);
+#pragma unroll
+      for (int c = 0; c < NOUT; ++c) {
+        float y = x[c];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const float o = __shfl_down_sync(0xffffffffu, y, off);
+          const int ol = __shfl_down_sync(0xffffffffu, my, off);
+          if (lane + off < 32 && ol == my) y += o;
+        }
+        if (head) atomicAdd(leaf_local + static_cast<int64_t>(leaf) * OUT + c, y);
       }
     }
-    if (lane < NOUT) atomicAdd(leaf_local + static_cast<int64_t>(leaf) * OUT + lane, x[0]);
-  } else {
-    // runs of equal targets inside the warp: segmented sums to each run's
-    // first lane
-    const int up = __shfl_up_sync(0xffffffffu, my, 1);
-    const bool head = act_row && (lane == 0 || up != my);
-#pragma unroll
-    for (int c = 0; c < NOUT; ++c) {
-      float y = x[c];
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const float o = __shfl_down_sync(0xffffffffu, y, off);
-        const int ol = __shfl_down_sync(0xffffffffu, my, off);
-        if (lane + off < 32 && ol == my) y += o;
-      }
-      if (head) atomicAdd(leaf_local + static_cast<int64_t>(leaf) * OUT + c, y);
-    }
-  }
+  }  // pair blocks
 }
 
 // ---- generic tile GEMM for training: C[M][N] (+)= sum_k opA[m][k] opB[n][k] -------
@@ -993,8 +996,10 @@ int m2l_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
                         const uint32_t* leaf_key, const float* rec, float h, float* leaf_local,
                         cudaStream_t s) {
   if (npairs <= 0) return FVX_OK;
-  mlp::m2l_pairs_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(npairs, pair_leaf, pair_cell,
-                                                             leaf_key, rec, h, leaf_local);
+  const int blocks = (npairs + mlp::kM2lThreads - 1) / mlp::kM2lThreads;
+  const int grid = blocks < 2 * device_sm_count() ? blocks : 2 * device_sm_count();
+  mlp::m2l_pairs_kernel<<<grid, mlp::kM2lThreads, 0, s>>>(npairs, pair_leaf, pair_cell, leaf_key,
+                                                         rec, h, leaf_local);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
