@@ -4,11 +4,13 @@
 // 32 outputs (30 used), weights [out][in] in BF16 with FP32 master copies,
 // FP32 biases.  Inference and training run on tcgen05 (fvx_tc.cuh):
 //   * forward: a persistent CTA per SM keeps all weights in shared memory in
-//     the K-major canonical layout; each of its two warpgroups owns a 128-row
-//     tile at a time and chains the four layers through its half of the
+//     the K-major canonical layout; each of its four warpgroups owns a 128-row
+//     tile at a time and chains the four layers through its quarter of the
 //     tensor memory: MMA into TMEM -> tcgen05.ld -> bias + SiLU in registers
-//     -> BF16 back into the group's shared activation tile -> next MMA, so
-//     one group's epilogue overlaps the other's MMAs.  Two input/output policies: plain rows
+//     -> the group's shared activation tile -> next MMA, so one group's
+//     epilogue overlaps the others' MMAs.  Inference runs on F16 operands
+//     (weights converted while staged), training on BF16 (the type its
+//     backward GEMMs read).  Two input/output policies: plain rows
 //     (X -> Y, with the hidden pre-activations / activations kept for
 //     training), and the treecode's learned far field (features computed
 //     in-kernel from the (target leaf, source cell) pair list, outputs scaled
@@ -83,21 +85,19 @@ __device__ __forceinline__ float silu_grad(float z) {
   return s * (1.f + z * (1.f - s));
 }
 
-// Barrier over the N threads of group g (named barrier 1 + g).
-template <int N = 128>
+// Barrier over the 128 threads of warpgroup g (named barrier 1 + g).
 __device__ __forceinline__ void group_sync(int g) {
-  asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "n"(N) : "memory");
+  asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory");
 }
-template <int N = 128>
 __device__ __forceinline__ bool group_sync_and(int g, bool p) {
   uint32_t r;
   asm volatile(
       "{\n\t.reg .pred q, d;\n\t"
       "setp.ne.u32 q, %1, 0;\n\t"
-      "bar.red.and.pred d, %2, %3, q;\n\t"
+      "bar.red.and.pred d, %2, 128, q;\n\t"
       "selp.u32 %0, 1, 0, d;\n\t}"
       : "=r"(r)
-      : "r"(static_cast<uint32_t>(p)), "r"(1 + g), "n"(N)
+      : "r"(static_cast<uint32_t>(p)), "r"(1 + g)
       : "memory");
   return r != 0;
 }
@@ -333,23 +333,20 @@ __device__ __forceinline__ void silu_chunk_f16(const uint32_t (&r)[16], const ui
   *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, c0 + 8, H)) =
       *reinterpret_cast<uint4*>(&b[4]);
 }
-// Columns [cb, cb + NC) of the row (NC a multiple of 32).
-template <int NC>
-__device__ void epilogue_hidden_f16(uint32_t tmem, int row, int cb, const uint32_t* hbias,
-                                    void* act) {
+__device__ void epilogue_hidden_f16(uint32_t tmem, int row, const uint32_t* hbias, void* act) {
   const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * ((threadIdx.x >> 5) & 3)) << 16);
   char* base = reinterpret_cast<char*>(act);
   uint32_t ra[16], rb[16];
-  tc::tmem_ld16_issue(taddr + cb, ra);
+  tc::tmem_ld16_issue(taddr, ra);
   tc::tmem_ld_wait(ra);
 #pragma unroll
-  for (int c0 = cb; c0 < cb + NC; c0 += 32) {
+  for (int c0 = 0; c0 < H; c0 += 32) {
     tc::tmem_ld16_issue(taddr + c0 + 16, rb);
     silu_chunk_f16(ra, hbias, base, row, c0);
     tc::tmem_ld_wait(rb);
-    if (c0 + 32 < cb + NC) tc::tmem_ld16_issue(taddr + c0 + 32, ra);
+    if (c0 + 32 < H) tc::tmem_ld16_issue(taddr + c0 + 32, ra);
     silu_chunk_f16(rb, hbias, base, row, c0 + 16);
-    if (c0 + 32 < cb + NC) tc::tmem_ld_wait(ra);
+    if (c0 + 32 < H) tc::tmem_ld_wait(ra);
   }
 }
 
@@ -361,11 +358,10 @@ __device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& ph) {
 }
 
 // group-local fence + barrier: smem writes -> async proxy, TMEM reads done
-template <int N = 128>
 __device__ __forceinline__ void group_handoff(int g) {
   tc::fence_smem_to_async();
   tc::fence_before_sync();
-  group_sync<N>(g);
+  group_sync(g);
   tc::fence_after_sync();
 }
 
@@ -373,12 +369,8 @@ __device__ __forceinline__ void group_handoff(int g) {
 // packed SiLU of epilogue_hidden_f16) -- the inference form, always taken by
 // the treecode far field; the training forward (with stored pre-activations
 // and activations) keeps BF16, the type its backward GEMMs read.
-// TPG: threads per group and 128-row tile, 128 or (F16 form) 256; with 256 the
-// two halves of a group split each row's features and hidden columns, which
-// doubles the warps that hide the epilogues' latencies (1024 threads, at most
-// 64 registers each).
-template <bool FAR, bool HALF, int TPG>
-__global__ void __launch_bounds__(kGroups * TPG, 1) mlp_fwd_kernel(FwdArgs<FAR> A, int rows,
+template <bool FAR, bool HALF>
+__global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> A, int rows,
                                                            const __nv_bfloat16* __restrict__ W,
                                                            const float* __restrict__ bias) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -389,7 +381,6 @@ __global__ void __launch_bounds__(kGroups * TPG, 1) mlp_fwd_kernel(FwdArgs<FAR> 
     fence_mbar_init();
   }
   static_assert(HALF || !FAR, "the far field runs the F16 form");
-  static_assert(TPG == 128 || (TPG == 256 && HALF), "128 threads per group, or 256 in F16");
   if constexpr (HALF) {
     // hidden layers halved: their accumulators are z/2, the tanh argument
     stage_kmajor_f16(S.w1, W + W1o, H, IN, 0.5f);
@@ -411,9 +402,8 @@ __global__ void __launch_bounds__(kGroups * TPG, 1) mlp_fwd_kernel(FwdArgs<FAR> 
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  const int grp = threadIdx.x / TPG;  // group
+  const int grp = threadIdx.x >> 7;   // warpgroup
   const int lt = threadIdx.x & 127;   // row of the group's tile
-  const int half = (threadIdx.x & (TPG - 1)) >> 7;  // which half of the row (TPG 256)
   const uint32_t tmem = S.tmem + static_cast<uint32_t>(128 * grp);
   const uint32_t lane_base = static_cast<uint32_t>(32 * ((threadIdx.x >> 5) & 3)) << 16;
   __nv_bfloat16* act = S.act[grp];
@@ -421,7 +411,33 @@ __global__ void __launch_bounds__(kGroups * TPG, 1) mlp_fwd_kernel(FwdArgs<FAR> 
   uint32_t ph = 0;
   bool ok = true;
   const int ntiles = (rows + 127) / 128;
-  for (int tile = kGroups * blockIdx.x + grp; tile < ntiles && ok; tile += kGroups * gridDim.x) {
+  const int tile_step = kGroups * gridDim.x;
+  // Far field: the pair inputs of a row are loaded one tile ahead, in two
+  // dependent levels (the pair's leaf and cell indices while the next tile's
+  // first MMA runs, the leaf key and the cell record while its third MMA
+  // runs), so that the loads' latency leaves the tile's serial chain.
+  int pf_leaf = 0, pf_cell = 0;
+  uint32_t pf_key = 0;
+  RecRegs pf_rec;
+  auto fetch_index = [&](int t) {
+    const int r = t * 128 + lt;
+    if (t < ntiles && r < rows) {
+      pf_leaf = A.f.pair_leaf[r];
+      pf_cell = A.f.pair_cell[r];
+    }
+  };
+  auto fetch_record = [&](int t) {
+    const int r = t * 128 + lt;
+    if (t < ntiles && r < rows) {
+      pf_key = A.f.leaf_key[pf_leaf];
+      pf_rec = load_record(A.f.rec + static_cast<int64_t>(pf_cell) * kRecFloats);
+    }
+  };
+  if constexpr (FAR) {
+    fetch_index(kGroups * blockIdx.x + grp);
+    fetch_record(kGroups * blockIdx.x + grp);
+  }
+  for (int tile = kGroups * blockIdx.x + grp; tile < ntiles && ok; tile += tile_step) {
     const int row = tile * 128 + lt;
     const bool act_row = row < rows;
     int leaf = 0;
@@ -432,36 +448,22 @@ __global__ void __launch_bounds__(kGroups * TPG, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         float f[IN];
         float* ax = S.aux[grp][lt];
         if (act_row) {
-          leaf = A.f.pair_leaf[row];
-          const float3 cT = leaf_center(A.f.leaf_key[leaf], A.f.h);
-          const RecRegs rr =
-              load_record(A.f.rec + static_cast<int64_t>(A.f.pair_cell[row]) * kRecFloats);
-          const PairScale sc = pair_features(rr.v, cT.x, cT.y, cT.z, A.f.h, f);
-          if (half == 0) {
-            ax[0] = sc.s2;
-            ax[1] = sc.s3;
-            ax[2] = sc.s4;
-          }
+          leaf = pf_leaf;
+          const float3 cT = leaf_center(pf_key, A.f.h);
+          const PairScale sc = pair_features(pf_rec.v, cT.x, cT.y, cT.z, A.f.h, f);
+          ax[0] = sc.s2;
+          ax[1] = sc.s3;
+          ax[2] = sc.s4;
         } else {
           for (int q = 0; q < IN; ++q) f[q] = 0.f;
         }
-        // 16-byte chunks k8 of the row (constant indices into f after unrolling)
-        auto put = [&](int k8) {
+#pragma unroll
+        for (int k8 = 0; k8 < IN / 8; ++k8) {
           __align__(16) __half2 b[4];
 #pragma unroll
           for (int q = 0; q < 4; ++q) b[q] = __floats2half2_rn(f[8 * k8 + 2 * q], f[8 * k8 + 2 * q + 1]);
           *reinterpret_cast<uint4*>(base + tc::kmajor_offset(lt, 8 * k8, IN)) =
               *reinterpret_cast<uint4*>(b);
-        };
-        if (TPG == 128) {
-#pragma unroll
-          for (int k8 = 0; k8 < IN / 8; ++k8) put(k8);
-        } else if (half == 0) {
-#pragma unroll
-          for (int k8 = 0; k8 < IN / 16; ++k8) put(k8);
-        } else {
-#pragma unroll
-          for (int k8 = IN / 16; k8 < IN / 8; ++k8) put(k8);
         }
       } else {
         for (int k8 = 0; k8 < IN / 8; ++k8) {
@@ -474,11 +476,15 @@ __global__ void __launch_bounds__(kGroups * TPG, 1) mlp_fwd_kernel(FwdArgs<FAR> 
       }
     }
     for (int l = 0; l < 3 && ok; ++l) {
-      group_handoff<TPG>(grp);
-      if (lt == 0 && half == 0)
+      group_handoff(grp);
+      if (lt == 0)
         tc::gemm_issue(tmem, act, l == 0 ? S.w1 : (l == 1 ? S.w2 : S.w3), l == 0 ? IN : H,
                        HALF ? tc::idesc_f16(128, H) : tc::idesc_bf16(128, H), false, bar, 0);
-      if (!group_sync_and<TPG>(grp, wait_mma(bar, ph))) {
+      if constexpr (FAR) {
+        if (l == 0) fetch_index(tile + tile_step);
+        if (l == 2) fetch_record(tile + tile_step);
+      }
+      if (!group_sync_and(grp, wait_mma(bar, ph))) {
         ok = false;
         break;
       }
@@ -489,22 +495,20 @@ __global__ void __launch_bounds__(kGroups * TPG, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         if (A.r.h_store && act_row) ho = A.r.h_store + (static_cast<int64_t>(l) * rows + row) * H;
       }
       if constexpr (HALF)
-        epilogue_hidden_f16<H * 128 / TPG>(tmem, lt, half * (H * 128 / TPG), S.hbias + l * H / 2,
-                                           act);
+        epilogue_hidden_f16(tmem, lt, S.hbias + l * H / 2, act);
       else
         epilogue_hidden(tmem, lt, S.bias + l * H, act, zo, ho);
     }
     if (!ok) break;
-    group_handoff<TPG>(grp);
-    if (lt == 0 && half == 0)
+    group_handoff(grp);
+    if (lt == 0)
       tc::gemm_issue(tmem, act, S.w4, H, HALF ? tc::idesc_f16(128, OUT) : tc::idesc_bf16(128, OUT),
                      false, bar, 0);
-    if (!group_sync_and<TPG>(grp, wait_mma(bar, ph))) {
+    if (!group_sync_and(grp, wait_mma(bar, ph))) {
       ok = false;
       break;
     }
-    // the output stage runs on the first half of the group
-    if (FAR && half == 0) {
+    if constexpr (FAR) {
       // the learned residual of this row, back to physical units (the analytic
       // translation is added by its own kernel)
       float x[OUT];
@@ -555,7 +559,7 @@ __global__ void __launch_bounds__(kGroups * TPG, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         }
       }
     }
-    for (int c0 = 0; c0 < OUT && !FAR && half == 0; c0 += 16) {
+    for (int c0 = 0; c0 < OUT && !FAR; c0 += 16) {
       float v[16];
       tc::tmem_ld16(tmem + lane_base + c0, v);
       if constexpr (FAR) continue;
@@ -571,10 +575,10 @@ __global__ void __launch_bounds__(kGroups * TPG, 1) mlp_fwd_kernel(FwdArgs<FAR> 
       }
     }
     tc::fence_before_sync();
-    group_sync<TPG>(grp);
+    group_sync(grp);
     tc::fence_after_sync();
   }
-  if (!ok && lt == 0 && half == 0) flag_status(kStatusTimeout);
+  if (!ok && lt == 0) flag_status(kStatusTimeout);
   tc::fence_before_sync();
   __syncthreads();
   if (threadIdx.x < 32) tc::tmem_dealloc(S.tmem, 128 * kGroups);
@@ -964,16 +968,14 @@ int set_smem(K kernel, size_t bytes) {
 
 // Fused learned far field for the treecode: local expansions of the learned
 // (leaf, cell) pairs added into leaf_local[n_leaves][32] (zeroed by the caller).
-// tpg: threads per 128-row tile, 128 or 256 (mlp_fwd_kernel's TPG).
 int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
                         const uint32_t* leaf_key, const float* rec, float h, const void* W,
-                        const float* bias, float* leaf_local, int tpg, cudaStream_t s) {
+                        const float* bias, float* leaf_local, cudaStream_t s) {
   using namespace mlp;
   if (npairs <= 0) return FVX_OK;
   static int done = 0;
   if (!done) {
-    int rc = set_smem(mlp_fwd_kernel<true, true, 128>, sizeof(FwdSmem));
-    if (!rc) rc = set_smem(mlp_fwd_kernel<true, true, 256>, sizeof(FwdSmem));
+    int rc = set_smem(mlp_fwd_kernel<true, true>, sizeof(FwdSmem));
     if (rc) return rc;
     done = 1;
   }
@@ -982,12 +984,8 @@ int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
   A.f = FarIO{pair_leaf, pair_cell, leaf_key, rec, h, leaf_local};
   const int nctas = ((npairs + 127) / 128 + kGroups - 1) / kGroups;
   const int grid = nctas < device_sm_count() ? nctas : device_sm_count();
-  if (tpg == 256)
-    mlp_fwd_kernel<true, true, 256><<<grid, kGroups * 256, sizeof(FwdSmem), s>>>(
-        A, npairs, static_cast<const __nv_bfloat16*>(W), bias);
-  else
-    mlp_fwd_kernel<true, true, 128><<<grid, kGroups * 128, sizeof(FwdSmem), s>>>(
-        A, npairs, static_cast<const __nv_bfloat16*>(W), bias);
+  mlp_fwd_kernel<true, true><<<grid, kGroups * 128, sizeof(FwdSmem), s>>>(
+      A, npairs, static_cast<const __nv_bfloat16*>(W), bias);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
@@ -1048,8 +1046,8 @@ int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, f
   if (rows == 0) return FVX_OK;
   static int done = 0;
   if (!done) {
-    int rc = set_smem(mlp_fwd_kernel<false, false, 128>, sizeof(FwdSmem));
-    if (!rc) rc = set_smem(mlp_fwd_kernel<false, true, 128>, sizeof(FwdSmem));
+    int rc = set_smem(mlp_fwd_kernel<false, false>, sizeof(FwdSmem));
+    if (!rc) rc = set_smem(mlp_fwd_kernel<false, true>, sizeof(FwdSmem));
     if (rc) return rc;
     done = 1;
   }
@@ -1060,8 +1058,7 @@ int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, f
   const int nctas = ((rows + 127) / 128 + kGroups - 1) / kGroups;
   const int grid = nctas < fvx::device_sm_count() ? nctas : fvx::device_sm_count();
   // without stores it is inference: the F16 form the treecode far field runs
-  auto kern = (z_store || h_store) ? mlp_fwd_kernel<false, false, 128>
-                                   : mlp_fwd_kernel<false, true, 128>;
+  auto kern = (z_store || h_store) ? mlp_fwd_kernel<false, false> : mlp_fwd_kernel<false, true>;
   kern<<<grid, kGroups * 128, sizeof(FwdSmem), static_cast<cudaStream_t>(stream)>>>(
       A, rows, static_cast<const __nv_bfloat16*>(W), bias);
   FVX_LAUNCH_CHECK();

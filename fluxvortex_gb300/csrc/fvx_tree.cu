@@ -1487,7 +1487,7 @@ void grid_params(const double lo[3], const double hi[3], int64_t n, int leaf_tar
 
 int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
                         const uint32_t* leaf_key, const float* rec, float h, const void* W,
-                        const float* bias, float* leaf_local, int tpg, cudaStream_t s);
+                        const float* bias, float* leaf_local, cudaStream_t s);
 int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const int* pair_cell,
                             const uint32_t* tgt_key, float h_tgt, const uint32_t* leaf_key,
                             const float* rec, const int* cell_start,
@@ -1509,7 +1509,6 @@ struct fvx_tree {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the last evaluation launch
   // far-field method of the pairs beyond theta_l (FVX_FAR_*)
   int far_method = FVX_FAR_M2P;
-  int net_threads = 128;  // network far field: threads per 128-row tile
   const void* mlp_W = nullptr;
   const float* mlp_b = nullptr;
   double theta_l = 0.0;
@@ -2079,7 +2078,7 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
       if (r) return r;
       if (T->far_method == FVX_FAR_LEARNED)
         r = mlp_farfield_launch(npairs, tgt, cell, tkey, rec, th, T->mlp_W, T->mlp_b,
-                                P<float>(buf), T->net_threads, s);
+                                P<float>(buf), s);
       return r;
     };
     if ((rc = local_stage(static_cast<int>(lrn_total), P<int>(T->lrn_leaf), P<int>(T->lrn_cell),
@@ -2222,14 +2221,6 @@ int fvx_tree_set_list_slots(fvx_tree* T, int near, int lrn, int par) {
   T->slot_lrn = lrn;
   T->slot_par = par;
   T->st.valid = false;
-  return FVX_OK;
-}
-
-int fvx_tree_set_network_threads(fvx_tree* T, int threads_per_tile) {
-  FVX_ARG_CHECK(T != nullptr, "null tree handle");
-  FVX_ARG_CHECK(threads_per_tile == 128 || threads_per_tile == 256,
-                "network threads per tile must be 128 or 256 (got %d)", threads_per_tile);
-  T->net_threads = threads_per_tile;
   return FVX_OK;
 }
 

@@ -1,7 +1,7 @@
 """One treecode self-sweep pair (velocity, then stretching) of the seeded slab wake.
 
     python -m fluxvortex_gb300.sweep_case [--n 1048576] [--leaf 48] [--far-field learned]
-        [--net-threads 256] [--repeat 0]
+        [--repeat 0]
 
 The smallest complete invocation of the particle hot path: the slab wake of
 ``workloads.slab_wake`` (uniform in a 20c x 10c x 2c slab, sigma 0.02c),
@@ -27,8 +27,6 @@ def main(argv=None):
     p.add_argument("--n", type=int, default=1 << 20)
     p.add_argument("--leaf", type=int, default=48)
     p.add_argument("--far-field", default="learned", choices=["m2p", "m2l", "learned"])
-    p.add_argument("--net-threads", type=int, default=None,
-                   help="network threads per 128-row tile (128 or 256)")
     p.add_argument("--repeat", type=int, default=0)
     a = p.parse_args(argv)
     pos, gam, sig, _ = slab_wake(a.n)
@@ -40,8 +38,6 @@ def main(argv=None):
         from .learned import FarFieldMLP
         mlp = FarFieldMLP.load()
     ts.set_far_field(a.far_field, mlp=mlp)
-    if a.net_threads:
-        ts.set_network_threads(a.net_threads)
     ts.set_validation(0, 0.1)
     out = torch.empty((a.n, 3), dtype=torch.float64, device="cuda")
     ts.sweep(_capi.PAIR_VELOCITY, "winckelmans", P, G, S, a.n, out)

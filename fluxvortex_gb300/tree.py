@@ -87,11 +87,6 @@ class TreeSweeper:
         """Slot capacities of the one-pass two-level lists (0: always count)."""
         _capi.check(self.lib.fvx_tree_set_list_slots(self.handle, int(near), int(lrn), int(par)))
 
-    def set_network_threads(self, threads_per_tile=128):
-        """Threads per 128-row tile of the learned far field's network: 128
-        (one per row) or 256 (two per row)."""
-        _capi.check(self.lib.fvx_tree_set_network_threads(self.handle, int(threads_per_tile)))
-
     def set_validation(self, samples=256, tol=0.1):
         """Per-sweep FP64 validation of the local-expansion path: ``samples``
         strided (leaf, cell) pairs per sweep; a pair whose expansion error

@@ -251,11 +251,6 @@ int fvx_tree_hint_same_positions(fvx_tree* tree);
  * 1024, 1024): the lists are written into fixed slots without a counting pass,
  * a slot overflow falls back to counting; any 0 = always count. */
 int fvx_tree_set_list_slots(fvx_tree* tree, int near, int lrn, int par);
-/* fvx_tree_set_network_threads: threads that run each 128-row tile of the
- * learned far field's network, 128 (one per row; the default) or 256 (two per
- * row, each with half of the hidden columns).  No counterpart in the
- * reference (its far field is the direct sum). */
-int fvx_tree_set_network_threads(fvx_tree* tree, int threads_per_tile);
 int fvx_tree_last_validation(fvx_tree* tree, double* out);
 int fvx_tree_sample_pairs(fvx_tree* tree, int list, int max_pairs, void* X, float* T, float* A,
                           int* n_out, void* stream);
