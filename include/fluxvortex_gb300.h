@@ -442,7 +442,9 @@ int fvx_flutter_sweep(const FlutterParams* params, const FlutterState* state, in
  * (9, [i][n] = du_i/dx_n), d2u/dx2 d^4/m (18, per component xx xy xz yy yz zz).
  * fvx_mlp_forward: Y[rows][32] FP32 from X[rows][48] BF16; z_store
  *   (3 x rows x 128 FP32) and h_store (3 x rows x 128 BF16), if not NULL,
- *   receive the hidden pre-activations and activations for training.
+ *   receive the hidden pre-activations and activations for training.  With
+ *   both NULL (inference) the kernel runs the treecode far field's F16 form:
+ *   weights converted to F16 in shared memory, F16 hidden activations.
  * fvx_mlp_gemm: C[M][N] (+)= sum_k opA[m][k] opB[n][k], opA[m][k] = tA ?
  *   A[k*lda + m] : A[m*lda + k] (same for B), BF16 in, FP32 out, split over K
  *   into split_k slices added with atomics (accumulate != 0 adds into C).
