@@ -12,6 +12,8 @@ namespace fvx {
 
 // Number of SMs and other per-device facts, cached by the host layer.
 int device_sm_count();
+// Largest dynamic shared memory a block may opt in to (bytes).
+int device_smem_optin();
 
 // Thread-local error message of the last failing C-ABI call.
 void set_last_error(const char* fmt, ...);

@@ -85,7 +85,8 @@ __device__ __forceinline__ float silu_grad(float z) {
   return s * (1.f + z * (1.f - s));
 }
 
-// Barrier over the 128 threads of warpgroup g (named barrier 1 + g).
+// Barrier over the 128 threads of warpgroup g (named barrier 1 + g); the
+// second form returns the AND of every thread's p.
 __device__ __forceinline__ void group_sync(int g) {
   asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory");
 }
@@ -357,7 +358,21 @@ __device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& ph) {
   return ok;
 }
 
-// group-local fence + barrier: smem writes -> async proxy, TMEM reads done
+// Group-wide wait for the group's MMA: the group's first warp polls the
+// mbarrier while the other three wait at the group barrier (no instructions
+// issued), which then releases everyone with the AND of the outcome.
+__device__ __forceinline__ bool group_wait_mma(int g, uint64_t* bar, uint32_t& ph) {
+  bool w = true;
+  if ((threadIdx.x & 127) < 32) w = mbar_wait(bar, ph);
+  ph ^= 1u;
+  tc::fence_before_sync();
+  const bool ok = group_sync_and(g, w);
+  tc::fence_after_sync();
+  return ok;
+}
+
+// Group-local fence + barrier before an MMA: the group's shared-memory writes
+// made visible to the tensor core (async proxy) and its TMEM reads done.
 __device__ __forceinline__ void group_handoff(int g) {
   tc::fence_smem_to_async();
   tc::fence_before_sync();
@@ -475,7 +490,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         }
       }
     }
-    for (int l = 0; l < 3 && ok; ++l) {
+    for (int l = 0; l < 3; ++l) {
       group_handoff(grp);
       if (lt == 0)
         tc::gemm_issue(tmem, act, l == 0 ? S.w1 : (l == 1 ? S.w2 : S.w3), l == 0 ? IN : H,
@@ -484,7 +499,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         if (l == 0) fetch_index(tile + tile_step);
         if (l == 2) fetch_record(tile + tile_step);
       }
-      if (!group_sync_and(grp, wait_mma(bar, ph))) {
+      if (!group_wait_mma(grp, bar, ph)) {
         ok = false;
         break;
       }
@@ -504,7 +519,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
     if (lt == 0)
       tc::gemm_issue(tmem, act, S.w4, H, HALF ? tc::idesc_f16(128, OUT) : tc::idesc_bf16(128, OUT),
                      false, bar, 0);
-    if (!group_sync_and(grp, wait_mma(bar, ph))) {
+    if (!group_wait_mma(grp, bar, ph)) {
       ok = false;
       break;
     }
@@ -574,9 +589,8 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
                              v[4 * q + 3] + S.bias[B4o + c0 + 4 * q + 3]);
       }
     }
-    tc::fence_before_sync();
-    group_sync(grp);
-    tc::fence_after_sync();
+    // no barrier here: the next tile's first handoff orders this tile's TMEM
+    // reads before the MMA that overwrites them
   }
   if (!ok && lt == 0) flag_status(kStatusTimeout);
   tc::fence_before_sync();

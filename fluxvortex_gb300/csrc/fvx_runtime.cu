@@ -37,6 +37,7 @@ namespace {
 thread_local char t_err[512] = "";
 std::mutex g_dev_mu;
 std::vector<int> g_sm_count;
+std::vector<int> g_smem_optin;
 }  // namespace
 
 void set_last_error(const char* fmt, ...) {
@@ -58,6 +59,21 @@ int device_sm_count() {
     g_sm_count[dev] = n;
   }
   return g_sm_count[dev];
+}
+
+int device_smem_optin() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 48 * 1024;
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  if (dev >= static_cast<int>(g_smem_optin.size())) g_smem_optin.resize(dev + 1, 0);
+  if (g_smem_optin[dev] == 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        n <= 0)
+      n = 48 * 1024;
+    g_smem_optin[dev] = n;
+  }
+  return g_smem_optin[dev];
 }
 
 int segments_collapsed_launch(const double*, int64_t, const double*, const double*,

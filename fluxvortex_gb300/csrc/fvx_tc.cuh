@@ -110,7 +110,10 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 
 // Split form of tmem_ld16, so that a load can be in flight while the previous
 // chunk is processed: issue, then wait.  The wait names the registers as
-// read-write operands, which keeps every use of them after it.
+// read-write operands, which keeps every use of them after it.  Neither
+// clobbers memory (TMEM is not C++ memory; both stay ordered with the other
+// volatile tcgen05 statements), so shared-memory loads and stores of the
+// epilogue may be scheduled across them.
 __device__ __forceinline__ void tmem_ld16_issue(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15},"
@@ -118,16 +121,13 @@ __device__ __forceinline__ void tmem_ld16_issue(uint32_t taddr, uint32_t (&r)[16
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
         "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
         "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr)
-      : "memory");
+      : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;"
                : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
                  "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
-                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
-               :
-               : "memory");
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]));
 }
 
 // Issues the K/16 MMAs of D[128 x N] (+)= A[128 x K] B[N x K]^T from one

@@ -137,16 +137,34 @@ __global__ void bbox_partial_kernel(int64_t n, const double* __restrict__ pos,
   if (threadIdx.x < 6) partial[blockIdx.x * 6 + threadIdx.x] = s[threadIdx.x][0];
 }
 
-__global__ void bbox_final_kernel(int nb, const double* __restrict__ partial,
-                                  double* __restrict__ out) {
-  if (threadIdx.x != 0) return;
+// One CTA of kBboxFinalThreads: each thread folds a strided share of the
+// partial boxes (independent loads), then warps and the CTA reduce.
+constexpr int kBboxFinalThreads = 256;
+__global__ void __launch_bounds__(kBboxFinalThreads) bbox_final_kernel(
+    int nb, const double* __restrict__ partial, double* __restrict__ out) {
   double r[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
-  for (int b = 0; b < nb; ++b)
+  for (int b = threadIdx.x; b < nb; b += kBboxFinalThreads)
     for (int c = 0; c < 3; ++c) {
       r[c] = fmin(r[c], partial[b * 6 + c]);
       r[3 + c] = fmax(r[3 + c], partial[b * 6 + 3 + c]);
     }
-  for (int c = 0; c < 6; ++c) out[c] = r[c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    for (int c = 0; c < 3; ++c) {
+      r[c] = fmin(r[c], __shfl_xor_sync(0xffffffffu, r[c], o));
+      r[3 + c] = fmax(r[3 + c], __shfl_xor_sync(0xffffffffu, r[3 + c], o));
+    }
+  __shared__ double s[kBboxFinalThreads / 32][6];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+    for (int c = 0; c < 6; ++c) s[w][c] = r[c];
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    const int c = threadIdx.x;
+    double v = s[0][c];
+    for (int k = 1; k < kBboxFinalThreads / 32; ++k) v = c < 3 ? fmin(v, s[k][c]) : fmax(v, s[k][c]);
+    out[c] = v;
+  }
 }
 
 // ---- Morton keys ----------------------------------------------------------------
@@ -1691,7 +1709,8 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   FVX_CUDA_TRY(cudaMemsetAsync(nonfinite, 0, sizeof(unsigned), s));
   bbox_partial_kernel<<<nbb, 256, 0, s>>>(n, pos, P<double>(T->bbox), nonfinite);
   FVX_LAUNCH_CHECK();
-  bbox_final_kernel<<<1, 32, 0, s>>>(nbb, P<double>(T->bbox), P<double>(T->bbox) + 6 * nbb);
+  bbox_final_kernel<<<1, kBboxFinalThreads, 0, s>>>(nbb, P<double>(T->bbox),
+                                                    P<double>(T->bbox) + 6 * nbb);
   FVX_LAUNCH_CHECK();
   double lohi[6];
   unsigned nbad = 0;

@@ -203,35 +203,41 @@ __global__ void rhs_kernel(int P, FvxSurfaces sf, const double* __restrict__ col
 
 // In-place solve of A x = b for B systems (A: B x P x P row-major, b: B x P);
 // Gaussian elimination with partial pivoting (first maximum wins).  x -> b.
-// One CTA of kLuThreads per system: warp-shuffle pivot search, the pivot row
-// and the multipliers cached in shared memory, the trailing update over 32
-// warps of rows with the lanes along the columns, then a column-oriented back
-// substitution with one barrier per column.
+// One CTA of kLuThreads per system.  The right-hand side, the pivot row and
+// the multipliers live in shared memory.  The first k0 = P - T elimination
+// steps run on the matrix in global memory (L2): warp-shuffle pivot search,
+// trailing update over 32 warps of rows with the lanes along the columns.
+// The trailing T x T block, once it fits, moves into shared memory (row
+// stride T + 1) and the remaining T steps run there.  Back substitution:
+// the tail block's columns from shared memory, the head rows' share of them
+// as one pass over U12 (each row subtracting in the same column order as the
+// column-oriented form), then the head columns from U11.  Every element
+// sees the same sequence of operations as the all-global form, so the results
+// are the same.
 constexpr int kLuThreads = 1024;
 constexpr int kLuMaxP = 2048;
 
-__global__ void __launch_bounds__(kLuThreads) lu_solve_kernel(int P, double* __restrict__ A,
-                                                              double* __restrict__ b) {
-  const int64_t PP = static_cast<int64_t>(P) * P;
-  double* a = A + blockIdx.x * PP;
-  double* x = b + static_cast<int64_t>(blockIdx.x) * P;
-  __shared__ double s_row[kLuMaxP];
-  __shared__ double s_l[kLuMaxP];
-  __shared__ double s_wv[kLuThreads / 32];
-  __shared__ int s_wi[kLuThreads / 32];
-  __shared__ int s_piv;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int k = 0; k < P; ++k) {
-    // pivot search in column k, rows k..P-1: max |a|, the first row on ties
-    double best = -1.0;
-    int bi = P;
-    for (int r = k + tid; r < P; r += kLuThreads) {
-      const double v = fabs(a[static_cast<int64_t>(r) * P + k]);
-      if (v > best) {
-        best = v;
-        bi = r;
-      }
+// Pivot search over v (the candidates' |a|, index i): max |a|, first row on
+// ties; every thread returns the winner.
+__device__ __forceinline__ int lu_pivot(double best, int bi, double* s_wv, int* s_wi, int* s_piv) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v2 = __shfl_down_sync(0xffffffffu, best, o);
+    const int i2 = __shfl_down_sync(0xffffffffu, bi, o);
+    if (v2 > best || (v2 == best && i2 < bi)) {
+      best = v2;
+      bi = i2;
     }
+  }
+  if (lane == 0) {
+    s_wv[warp] = best;
+    s_wi[warp] = bi;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    best = s_wv[lane];
+    bi = s_wi[lane];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const double v2 = __shfl_down_sync(0xffffffffu, best, o);
@@ -242,31 +248,47 @@ __global__ void __launch_bounds__(kLuThreads) lu_solve_kernel(int P, double* __r
       }
     }
     if (lane == 0) {
-      s_wv[warp] = best;
-      s_wi[warp] = bi;
+      *s_piv = bi;
+      if (!(best > 0.0)) flag_status(kStatusNonFinite);
     }
-    __syncthreads();
-    if (warp == 0) {
-      best = s_wv[lane];
-      bi = s_wi[lane];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const double v2 = __shfl_down_sync(0xffffffffu, best, o);
-        const int i2 = __shfl_down_sync(0xffffffffu, bi, o);
-        if (v2 > best || (v2 == best && i2 < bi)) {
-          best = v2;
-          bi = i2;
-        }
-      }
-      if (lane == 0) {
-        s_piv = bi;
-        if (!(best > 0.0)) flag_status(kStatusNonFinite);
+  }
+  __syncthreads();
+  return *s_piv;
+}
+
+// Dynamic shared memory: s_x[P], s_row[P], s_l[P], then the tail block
+// (T rows of stride T + 1).
+__global__ void __launch_bounds__(kLuThreads) lu_solve_kernel(int P, int T, double* __restrict__ A,
+                                                              double* __restrict__ b) {
+  extern __shared__ double lu_smem[];
+  double* s_x = lu_smem;
+  double* s_row = s_x + P;
+  double* s_l = s_row + P;
+  double* S = s_l + P;
+  const int ld = T + 1;
+  __shared__ double s_wv[kLuThreads / 32];
+  __shared__ int s_wi[kLuThreads / 32];
+  __shared__ int s_piv;
+  const int64_t PP = static_cast<int64_t>(P) * P;
+  double* a = A + blockIdx.x * PP;
+  double* x = b + static_cast<int64_t>(blockIdx.x) * P;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int k0 = P - T;
+  for (int r = tid; r < P; r += kLuThreads) s_x[r] = x[r];
+  __syncthreads();
+  // ---- head steps on the matrix in global memory
+  for (int k = 0; k < k0; ++k) {
+    double best = -1.0;
+    int bi = P;
+    for (int r = k + tid; r < P; r += kLuThreads) {
+      const double v = fabs(a[static_cast<int64_t>(r) * P + k]);
+      if (v > best) {
+        best = v;
+        bi = r;
       }
     }
-    __syncthreads();
-    const int piv = s_piv;
-    // swap rows k and piv (columns k.. only change from here on, but the
-    // whole row is swapped as the unblocked form does) and cache row k
+    const int piv = lu_pivot(best, bi, s_wv, s_wi, &s_piv);
+    // swap rows k and piv (the whole rows) and cache row k
     for (int c = tid; c < P; c += kLuThreads) {
       double rk = a[static_cast<int64_t>(k) * P + c];
       if (piv != k && piv < P) {
@@ -278,23 +300,19 @@ __global__ void __launch_bounds__(kLuThreads) lu_solve_kernel(int P, double* __r
       s_row[c] = rk;
     }
     if (tid == 0 && piv != k && piv < P) {
-      const double t = x[k];
-      x[k] = x[piv];
-      x[piv] = t;
+      const double t = s_x[k];
+      s_x[k] = s_x[piv];
+      s_x[piv] = t;
     }
     __syncthreads();
     const double akk = s_row[k];
-    const double xk = x[k];
-    // multipliers of the rows below
+    const double xk = s_x[k];
     for (int r = k + 1 + tid; r < P; r += kLuThreads) {
       const double l = a[static_cast<int64_t>(r) * P + k] / akk;
       s_l[r] = l;
-      x[r] -= l * xk;
+      s_x[r] -= l * xk;
     }
     __syncthreads();
-    // trailing update a_rc -= l_r a_kc over rows r > k (warps), columns c > k
-    // (lanes, coalesced); the rows of a warp are independent, so their loads
-    // overlap
     for (int r = k + 1 + warp; r < P; r += kLuThreads / 32) {
       const double l = s_l[r];
       double* ar = a + static_cast<int64_t>(r) * P;
@@ -302,17 +320,90 @@ __global__ void __launch_bounds__(kLuThreads) lu_solve_kernel(int P, double* __r
     }
     __syncthreads();
   }
-  // back substitution by columns: x_k /= a_kk, then x_r -= a_rk x_k for r < k
-  for (int r = tid; r < P; r += kLuThreads) s_l[r] = x[r];
+  // ---- the trailing block into shared memory
+  for (int e = tid; e < T * T; e += kLuThreads) {
+    const int r = e / T, c = e - r * T;
+    S[r * ld + c] = a[static_cast<int64_t>(k0 + r) * P + k0 + c];
+  }
   __syncthreads();
-  for (int k = P - 1; k >= 0; --k) {
-    const double xk = s_l[k] / a[static_cast<int64_t>(k) * P + k];
-    for (int r = tid; r < k; r += kLuThreads) s_l[r] -= a[static_cast<int64_t>(r) * P + k] * xk;
+  for (int kk = 0; kk < T; ++kk) {
+    double best = -1.0;
+    int bi = T;
+    for (int r = kk + tid; r < T; r += kLuThreads) {
+      const double v = fabs(S[r * ld + kk]);
+      if (v > best) {
+        best = v;
+        bi = r;
+      }
+    }
+    const int piv = lu_pivot(best, bi, s_wv, s_wi, &s_piv);
+    // swap rows kk and piv of the block (columns kk.. are U's), cache row kk
+    for (int c = kk + tid; c < T; c += kLuThreads) {
+      double rk = S[kk * ld + c];
+      if (piv != kk && piv < T) {
+        const double rp = S[piv * ld + c];
+        S[piv * ld + c] = rk;
+        S[kk * ld + c] = rp;
+        rk = rp;
+      }
+      s_row[c] = rk;
+    }
+    if (tid == 0 && piv != kk && piv < T) {
+      const double t = s_x[k0 + kk];
+      s_x[k0 + kk] = s_x[k0 + piv];
+      s_x[k0 + piv] = t;
+    }
     __syncthreads();
-    if (tid == 0) s_l[k] = xk;
+    const double akk = s_row[kk];
+    const double xk = s_x[k0 + kk];
+    for (int r = kk + 1 + tid; r < T; r += kLuThreads) {
+      const double l = S[r * ld + kk] / akk;
+      s_l[r] = l;
+      s_x[k0 + r] -= l * xk;
+    }
+    __syncthreads();
+    for (int r = kk + 1 + warp; r < T; r += kLuThreads / 32) {
+      const double l = s_l[r];
+      double* sr = S + r * ld;
+      for (int c = kk + 1 + lane; c < T; c += 32) sr[c] -= l * s_row[c];
+    }
     __syncthreads();
   }
-  for (int r = tid; r < P; r += kLuThreads) x[r] = s_l[r];
+  // ---- back substitution: the tail columns
+  for (int kk = T - 1; kk >= 0; --kk) {
+    const double xk = s_x[k0 + kk] / S[kk * ld + kk];
+    for (int r = tid; r < kk; r += kLuThreads) s_x[k0 + r] -= S[r * ld + kk] * xk;
+    __syncthreads();
+    if (tid == 0) s_x[k0 + kk] = xk;
+    __syncthreads();
+  }
+  // the head rows' share of the tail columns (U12), columns in descending order
+  for (int r = tid; r < k0; r += kLuThreads) {
+    const double* ar = a + static_cast<int64_t>(r) * P + k0;
+    double v = s_x[r];
+    for (int c = T - 1; c >= 0; --c) v -= ar[c] * s_x[k0 + c];
+    s_x[r] = v;
+  }
+  __syncthreads();
+  // the head columns: U11 from shared memory when it fits in the block's room
+  const bool u11_smem = k0 <= T;
+  if (u11_smem) {
+    for (int e = tid; e < k0 * k0; e += kLuThreads) {
+      const int r = e / k0, c = e - r * k0;
+      S[r * ld + c] = a[static_cast<int64_t>(r) * P + c];
+    }
+    __syncthreads();
+  }
+  for (int k = k0 - 1; k >= 0; --k) {
+    const double ukk = u11_smem ? S[k * ld + k] : a[static_cast<int64_t>(k) * P + k];
+    const double xk = s_x[k] / ukk;
+    for (int r = tid; r < k; r += kLuThreads)
+      s_x[r] -= (u11_smem ? S[r * ld + k] : a[static_cast<int64_t>(r) * P + k]) * xk;
+    __syncthreads();
+    if (tid == 0) s_x[k] = xk;
+    __syncthreads();
+  }
+  for (int r = tid; r < P; r += kLuThreads) x[r] = s_x[r];
 }
 
 struct LoadsArgs {
@@ -711,8 +802,17 @@ int fvx_uvlm_rhs(int nc, const FvxSurfaces* s, const double* colloc, const doubl
 int fvx_lu_solve_batched(int n_systems, int P, double* A, double* b, void* stream) {
   FVX_ARG_CHECK(n_systems >= 1 && P >= 1 && P <= fvx::kLuMaxP && A && b,
                 "bad solve arguments (P must be 1..%d)", fvx::kLuMaxP);
-  fvx::lu_solve_kernel<<<n_systems, fvx::kLuThreads, 0, static_cast<cudaStream_t>(stream)>>>(
-      P, A, b);
+  // tail size T: the largest block (row stride T + 1) that fits next to the
+  // three P-vectors in the opt-in shared memory
+  const int budget = fvx::device_smem_optin() - 1024;  // static arrays of the kernel
+  int T = 0;
+  while (T < P && 8L * (3L * P + static_cast<long>(T + 1) * (T + 2)) <= budget) ++T;
+  const size_t smem = 8 * (3 * static_cast<size_t>(P) + static_cast<size_t>(T) * (T + 1));
+  FVX_CUDA_TRY(cudaFuncSetAttribute(fvx::lu_solve_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)));
+  fvx::lu_solve_kernel<<<n_systems, fvx::kLuThreads, smem, static_cast<cudaStream_t>(stream)>>>(
+      P, T, A, b);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }

@@ -115,7 +115,7 @@ def test_snapshot_restore_resumes_bitwise(cuda, tmp_path):
     again(st)
 
 
-@pytest.mark.parametrize("P,nsys", [(1, 1), (7, 3), (120, 2), (192, 3), (600, 1)])
+@pytest.mark.parametrize("P,nsys", [(1, 1), (7, 3), (120, 2), (164, 1), (192, 3), (300, 2), (600, 1)])
 def test_lu_solve_batched_matches_numpy(cuda, P, nsys):
     """The batched FP64 solve (partial pivoting) against numpy.linalg.solve on
     diagonally weak random systems whose first pivot needs a row swap."""
