@@ -517,6 +517,7 @@ struct TreeView {
   const uint32_t* key;
   const int* child_lo;  // level-local ids of the children (level l+1)
   const int* child_hi;
+  const int4* cen;      // cell centres in units of h/2 (dual traversal)
   double mac_kl;        // learned far field: 3/4 / theta_L^2 (0: off)
   int learned_only;     // learned pairs leave the analytic list (weights loaded)
   // the acceptance tests in exact integers: with centre offsets in units of
@@ -636,7 +637,7 @@ struct DualLists {
   int* lrn_cell;
   int* par_par;
   int* par_cell;
-  int* leaf_parent;  // per leaf: its parent's level-local index
+  const int* leaf_parent;  // per leaf: its parent's level-local index
   int near_cap, lrn_cap, par_cap;
   // slot mode (fill pass with these > 0): leaf t's near leaves at
   // near_idx[t slot_near ..], its local cells at lrn_cell[t slot_lrn ..],
@@ -645,6 +646,28 @@ struct DualLists {
   int slot_near, slot_lrn, slot_par;
 };
 
+// Cell centres (2 c + 1) 2^(L - l) in units of h/2, c the level-l cell's
+// integer coordinates: read by the dual traversal instead of decoding keys.
+__global__ void cell_centres_kernel(TreeView T, int total_cells, int4* __restrict__ cen) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total_cells) return;
+  int l = 0;
+  while (l < T.L && g >= T.base[l + 1]) ++l;
+  const uint32_t k = T.key[g];
+  const int sc = 1 << (T.L - l);
+  cen[g] = make_int4((2 * static_cast<int>(compact10(k)) + 1) * sc,
+                     (2 * static_cast<int>(compact10(k >> 1)) + 1) * sc,
+                     (2 * static_cast<int>(compact10(k >> 2)) + 1) * sc, l);
+}
+
+// leaf -> its parent's level-local index, from the parents' child ranges
+__global__ void leaf_parents_kernel(TreeView T, int* __restrict__ leaf_parent) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= T.ncell[T.L - 1]) return;
+  const int gP = T.base[T.L - 1] + p;
+  for (int c = T.child_lo[gP]; c < T.child_hi[gP]; ++c) leaf_parent[c] = p;
+}
+
 template <bool FILL>
 __global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restrict__ overflow) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -652,29 +675,14 @@ __global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restri
   const int nleaf = T.ncell[L];
   if (t >= nleaf) return;
   const int gT = T.base[L] + t;
-  const uint32_t kT = T.key[gT];
-  // the parent: binary search of key >> 3 among the level L-1 keys
-  const uint32_t kP = kT >> 3;
-  int lo = 0, hi = T.ncell[L - 1] - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (T.key[T.base[L - 1] + mid] < kP)
-      lo = mid + 1;
-    else
-      hi = mid;
-  }
-  const int p = lo;
+  const int p = D.leaf_parent[t];
   const int gP = T.base[L - 1] + p;
   const bool first = T.child_lo[gP] == t;
   // centres in units of h/2: a parent (size 2h) at (2 k + 1) 2, a leaf at 2 k + 1
-  const int px = 2 * (2 * static_cast<int>(compact10(kP)) + 1),
-            py = 2 * (2 * static_cast<int>(compact10(kP >> 1)) + 1),
-            pz = 2 * (2 * static_cast<int>(compact10(kP >> 2)) + 1);
-  const int tx = 2 * static_cast<int>(compact10(kT)) + 1,
-            ty = 2 * static_cast<int>(compact10(kT >> 1)) + 1,
-            tz = 2 * static_cast<int>(compact10(kT >> 2)) + 1;
+  const int4 cP = T.cen[gP], cT = T.cen[gT];
+  const int px = cP.x, py = cP.y, pz = cP.z;
+  const int tx = cT.x, ty = cT.y, tz = cT.z;
   const int tcount = T.count[gT];
-  if (FILL) D.leaf_parent[t] = p;
   int nn = 0, nl = 0, np = 0;
   const bool slot = FILL && D.slot_near > 0;
   const int no = FILL ? (slot ? t * D.slot_near : D.near_off[t]) : 0;
@@ -686,11 +694,8 @@ __global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restri
   long long near_pairs = 0;
   // T against source cell g at level l; false: an inner cell that fails
   auto leaf_visit = [&](int g, int l) {
-    const uint32_t k = T.key[g];
-    const int sc = 1 << (L - l);
-    const int dx = tx - (2 * static_cast<int>(compact10(k)) + 1) * sc;
-    const int dy = ty - (2 * static_cast<int>(compact10(k >> 1)) + 1) * sc;
-    const int dz = tz - (2 * static_cast<int>(compact10(k >> 2)) + 1) * sc;
+    const int4 c = T.cen[g];
+    const int dx = tx - c.x, dy = ty - c.y, dz = tz - c.z;
     const int d2 = dx * dx + dy * dy + dz * dz;
     if (d2 > T.thr_far[l]) {
       if (FILL && lo_ + nl < lrn_end) {
@@ -714,11 +719,8 @@ __global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restri
   while (sp > 0) {
     const int e = stack[--sp];
     const int g = e & ((1 << 27) - 1), l = e >> 27;
-    const uint32_t k = T.key[g];
-    const int sc = 1 << (L - l);
-    const int dx = px - (2 * static_cast<int>(compact10(k)) + 1) * sc;
-    const int dy = py - (2 * static_cast<int>(compact10(k >> 1)) + 1) * sc;
-    const int dz = pz - (2 * static_cast<int>(compact10(k >> 2)) + 1) * sc;
+    const int4 c = T.cen[g];
+    const int dx = px - c.x, dy = py - c.y, dz = pz - c.z;
     const int d2 = dx * dx + dy * dy + dz * dz;
     if (d2 > T.thr_par[l]) {
       if (first) {
@@ -1538,6 +1540,7 @@ struct fvx_tree {
   int last_val_k = 0;
   // two-level traversal: per-parent lists and expansions
   fvx::DevBuf dual_meta, par_par, par_cell, parent_local;
+  fvx::DevBuf cen;  // cell centres in units of h/2 (dual traversal)
   fvx::DevBuf pair_partial;  // slices of the FP64 exact-expansion sums
   int n_parent_pairs = 0;
   fvx::DevBuf lrn_meta, lrn_leaf, lrn_cell, leaf_local;
@@ -1837,6 +1840,7 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   V.key = reinterpret_cast<const uint32_t*>(lvb + 2 * total_cells);
   V.child_lo = lvb + 3 * total_cells;
   V.child_hi = lvb + 4 * total_cells;
+  V.cen = nullptr;
   const bool learned = T->far_method != FVX_FAR_M2P && T->theta_l > 0.0;
   V.mac_kl = learned ? 0.75 / (T->theta_l * T->theta_l) : 0.0;
   // integer acceptance thresholds per source level: (h_T + h_S)^2 in (h/2)^2
@@ -1888,6 +1892,15 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   // each parent's cells go to fixed-capacity slots (no counting pass); the
   // local-expansion pairs are then compacted into flat lists ordered by
   // target.  A slot overflow falls back to the counting pass and exact lists.
+  if (dual) {
+    // what every leaf's traversal reads: cell centres and its parent
+    if ((rc = grow(T->cen, 16 * size_t(total_cells)))) return rc;
+    V.cen = P<int4>(T->cen);
+    cell_centres_kernel<<<(total_cells + 255) / 256, 256, 0, s>>>(V, total_cells, P<int4>(T->cen));
+    FVX_LAUNCH_CHECK();
+    leaf_parents_kernel<<<(npar + 127) / 128, 128, 0, s>>>(V, leaf_parent);
+    FVX_LAUNCH_CHECK();
+  }
   bool slotted = false;
   if (dual && T->slot_near > 0 && T->slot_lrn > 0 && T->slot_par > 0) {
     const int kSlotNear = T->slot_near, kSlotLrn = T->slot_lrn, kSlotPar = T->slot_par;
@@ -2269,6 +2282,7 @@ void fvx_tree_destroy(fvx_tree* T) {
                          &T->lrn_cell, &T->leaf_local, &T->val_X, &T->val_T, &T->val_A,
                          &T->val_Y, &T->val_scale, &T->val_err, &T->val_fb, &T->val_stats,
                          &T->dual_meta, &T->par_par, &T->par_cell, &T->parent_local,
+                         &T->cen,
                          &T->lrn_slot, &T->par_slot,
                          &T->pair_partial};
   for (auto* b : bufs)
