@@ -310,7 +310,9 @@ int targets_per_cta(int mode, int precision) {
 int pair_splits(int mode, int precision, int64_t n_tgt, int64_t n_src, int64_t* chunk) {
   const int per_cta = targets_per_cta(mode, precision);
   const int64_t gx = (n_tgt + per_cta - 1) / per_cta;
-  const int64_t want = 2LL * device_sm_count();
+  // six resident CTAs per SM (80 registers x 128 threads): few targets
+  // (the panel points against every particle) split the sources that far
+  const int64_t want = 6LL * device_sm_count();
   int64_t s = gx >= want ? 1 : (want + gx - 1) / gx;
   // keep at least two source tiles per split
   int64_t maxs = (n_src + 2 * kSrcTile - 1) / (2 * kSrcTile);

@@ -647,17 +647,22 @@ struct DualLists {
 };
 
 // Cell centres (2 c + 1) 2^(L - l) in units of h/2, c the level-l cell's
-// integer coordinates: read by the dual traversal instead of decoding keys.
+// integer coordinates, and the children's level-local range packed as
+// (first << 4) | count (0 for leaves): what the dual traversal reads per
+// visited cell, in one 16-byte load instead of a key to decode and the
+// child bounds.
 __global__ void cell_centres_kernel(TreeView T, int total_cells, int4* __restrict__ cen) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= total_cells) return;
   int l = 0;
   while (l < T.L && g >= T.base[l + 1]) ++l;
+  if (g - T.base[l] >= T.ncell[l]) return;  // a level's unused capacity
   const uint32_t k = T.key[g];
   const int sc = 1 << (T.L - l);
+  const int kids = l < T.L ? (T.child_lo[g] << 4) | (T.child_hi[g] - T.child_lo[g]) : 0;
   cen[g] = make_int4((2 * static_cast<int>(compact10(k)) + 1) * sc,
                      (2 * static_cast<int>(compact10(k >> 1)) + 1) * sc,
-                     (2 * static_cast<int>(compact10(k >> 2)) + 1) * sc, l);
+                     (2 * static_cast<int>(compact10(k >> 2)) + 1) * sc, kids);
 }
 
 // leaf -> its parent's level-local index, from the parents' child ranges
@@ -741,10 +746,10 @@ __global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restri
         leaf_visit(g, l);
         continue;
       }
-      const int clo = T.child_lo[g], chi = T.child_hi[g];
-      for (int c = chi - 1; c >= clo; --c) {
+      const int clo = c.w >> 4, chi = clo + (c.w & 15);
+      for (int q = chi - 1; q >= clo; --q) {
         if (sp < 96)
-          stack[sp++] = (T.base[l + 1] + c) | ((l + 1) << 27);
+          stack[sp++] = (T.base[l + 1] + q) | ((l + 1) << 27);
         else
           atomicOr(overflow, 1u);
       }
@@ -752,7 +757,7 @@ __global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restri
     }
     // A of P's size (level L-1) or a leaf: against T itself
     if (leaf_visit(g, l)) continue;
-    const int clo = T.child_lo[g], chi = T.child_hi[g];  // A at level L-1: leaves below
+    const int clo = c.w >> 4, chi = clo + (c.w & 15);  // A at level L-1: leaves below
     for (int q = clo; q < chi; ++q) leaf_visit(T.base[L] + q, L);
   }
   if (!FILL || slot) {
