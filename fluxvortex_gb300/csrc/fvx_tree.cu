@@ -36,6 +36,7 @@ constexpr int kSortItems = 1024;   // keys per radix-sort block (256 threads x 4
 constexpr int kEvalThreads = 32;   // eval CTA (one warp); 1 or 2 targets per thread
 constexpr int kFarTile = 32;       // far cells staged per tile
 constexpr int kNearTile = 128;     // source particles staged per tile
+constexpr int kNearRows = 64;      // paired path: staged rows per tile (2 sources each, G > 1)
 constexpr int kRecFloats = 40;     // far-cell record
 constexpr double kC = -0.07957747154594767;  // -1/(4 pi)
 
@@ -1045,7 +1046,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
   constexpr bool PACKED = TPT == 2 && KERNEL == FVX_KERNEL_WINCKELMANS &&
                           (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_STRETCH);
   // near tile (plain or paired layout) and far-cell records share the storage
-  constexpr int kNearBytes = PACKED ? kNearTile * static_cast<int>(sizeof(NearX2))
+  constexpr int kNearBytes = PACKED ? kNearRows * static_cast<int>(sizeof(NearX2))
                                     : kNearTile * 2 * static_cast<int>(sizeof(float4));
   constexpr int kFarBytes = kFarTile * kRecFloats * 4;
   __shared__ __align__(16) unsigned char s_raw[kNearBytes > kFarBytes ? kNearBytes : kFarBytes];
@@ -1131,8 +1132,11 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
         }
         const int total = __shfl_sync(full, incl, kEvalThreads - 1);
         const int excl = incl - msn;
-        for (int b0 = 0; b0 < total; b0 += kNearTile) {
-          const int nt = min(kNearTile, total - b0);
+        // a tile is kNearRows staged rows: as many sources (G = 1), or twice
+        // as many (G > 1, two per row)
+        const int tile_src = G == 1 ? kNearRows : 2 * kNearRows;
+        for (int b0 = 0; b0 < total; b0 += tile_src) {
+          const int nt = min(tile_src, total - b0);
           // rows: nt sources (G = 1), or ceil(nt/2) source pairs padded with
           // zero-strength sources to a multiple of the G/2 lane groups
           const int rows = G == 1 ? nt : ((nt + 1) / 2 + ng - 1) / ng * ng;
