@@ -774,6 +774,220 @@ __global__ void traverse_dual_kernel(TreeView T, DualLists D, unsigned* __restri
   }
 }
 
+// ---- one-pass two-level lists in two phases --------------------------------------
+// The per-leaf traversal above tests every cell against the leaf's parent
+// first; the eight siblings repeat those tests.  Here the parent-level walk
+// runs once per parent, by a warp (phase 1), and leaves only the residual
+// cells to each child leaf (phase 2).  The lists are the same sets as the
+// per-leaf traversal's (the parent list of the parent, near leaves and local
+// cells of each leaf); their order within a leaf or parent differs.
+constexpr int kParWarps = 4;     // phase 1: warps (parents) per CTA
+constexpr int kParStack = 2048;  // phase 1: stack entries per warp (shared memory)
+
+// Phase 1: warp per parent of leaves P.  A shared stack is walked 32 entries
+// per round (lane 0 takes the top).  A cell that P accepts goes to P's list;
+// a cell accepted by every child of P (the octant test of the per-leaf
+// traversal), or a leaf- or parent-level cell that P does not accept, goes to
+// P's residual list; any other cell is opened.  Any capacity overflow sets
+// overflow bit 4 (the host then builds the lists with the counting passes).
+__global__ void __launch_bounds__(kParWarps * 32) traverse_parents_kernel(
+    TreeView T, int* __restrict__ par_cnt, int* __restrict__ par_cell, int slot_par,
+    int* __restrict__ res_cnt, int* __restrict__ res, int slot_res,
+    unsigned* __restrict__ overflow) {
+  __shared__ int s_stack[kParWarps][kParStack];
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int L = T.L;
+  const int p = blockIdx.x * kParWarps + w;
+  if (p >= T.ncell[L - 1]) return;  // whole warps
+  int* st = s_stack[w];
+  const int4 cP = T.cen[T.base[L - 1] + p];
+  const unsigned below = (1u << lane) - 1u;
+  const int nroot = T.ncell[0];
+  bool bad = nroot > kParStack;
+  int sp = 0;
+  if (!bad) {
+    for (int i = lane; i < nroot; i += 32) st[nroot - 1 - i] = T.base[0] + i;  // root 0 on top
+    sp = nroot;
+  }
+  __syncwarp();
+  int np = 0, nr = 0;
+  while (sp > 0 && !bad) {
+    const int n = sp < 32 ? sp : 32;
+    const int e = lane < n ? st[sp - 1 - lane] : -1;
+    sp -= n;
+    __syncwarp();
+    int cat = 0, kids = 0;  // 1: parent list, 2: residual, 3: open
+    if (e >= 0) {
+      const int g = e & ((1 << 27) - 1), l = e >> 27;
+      const int4 c = T.cen[g];
+      const int dx = cP.x - c.x, dy = cP.y - c.y, dz = cP.z - c.z;
+      const int d2 = dx * dx + dy * dy + dz * dz;
+      if (d2 > T.thr_par[l]) {
+        cat = 1;
+      } else if (l < L - 1) {
+        const int ax = abs(dx) - 1, ay = abs(dy) - 1, az = abs(dz) - 1;
+        if (ax * ax + ay * ay + az * az > T.thr_far[l]) {
+          cat = 2;
+        } else {
+          cat = 3;
+          kids = c.w;
+        }
+      } else {
+        cat = 2;
+      }
+    }
+    const unsigned m1 = __ballot_sync(full, cat == 1);
+    if (cat == 1) {
+      const int k = np + __popc(m1 & below);
+      if (k < slot_par) par_cell[static_cast<int64_t>(p) * slot_par + k] = e & ((1 << 27) - 1);
+    }
+    np += __popc(m1);
+    const unsigned m2 = __ballot_sync(full, cat == 2);
+    if (cat == 2) {
+      const int k = nr + __popc(m2 & below);
+      if (k < slot_res) res[static_cast<int64_t>(p) * slot_res + k] = e;
+    }
+    nr += __popc(m2);
+    // children: lower lanes' nearer the top, child 0 of a cell on top
+    const int cnt = cat == 3 ? (kids & 15) : 0;
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(full, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(full, incl, 31);
+    if (sp + total > kParStack) {
+      bad = true;
+    } else {
+      if (cnt > 0) {
+        const int l1 = (e >> 27) + 1, clo = kids >> 4;
+        const int top = sp + total - incl + cnt - 1;  // this lane's highest slot
+        for (int q = 0; q < cnt; ++q) st[top - q] = (T.base[l1] + clo + q) | (l1 << 27);
+      }
+      sp += total;
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    par_cnt[p] = np;
+    res_cnt[p] = nr;
+    if (bad || np > slot_par || nr > slot_res) atomicOr(overflow, 4u);
+  }
+}
+
+// Phase 2: warp per parent P: P's residual cells finished against each of its
+// child leaves.  Lanes take 32 residual cells at a time (their records, and
+// for a parent-level cell its leaves' records, loaded once for all children);
+// per child leaf, the accepted cells become local-expansion pairs and the
+// leaf-level ones near leaves, emitted in lane order (ballot prefixes).
+__global__ void __launch_bounds__(kParWarps * 32) traverse_residual_kernel(
+    TreeView T, DualLists D, const int* __restrict__ res_cnt, const int* __restrict__ res,
+    int slot_res, unsigned* __restrict__ overflow) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int L = T.L;
+  const int p = blockIdx.x * kParWarps + w;
+  if (p >= T.ncell[L - 1]) return;  // whole warps
+  const unsigned below = (1u << lane) - 1u;
+  const int kidsP = T.cen[T.base[L - 1] + p].w;
+  const int t0 = kidsP >> 4, nkP = kidsP & 15;  // the child leaves t0 .. t0 + nkP - 1
+  int4 cL[8];
+  int tc[8], nn[8], nl[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    nn[q] = nl[q] = 0;
+    tc[q] = 0;
+    cL[q] = make_int4(0, 0, 0, 0);
+    if (q < nkP) {
+      cL[q] = T.cen[T.base[L] + t0 + q];
+      tc[q] = T.count[T.base[L] + t0 + q];
+    }
+  }
+  long long near_pairs = 0;
+  const int nr = min(res_cnt[p], slot_res);
+  const int* rp = res + static_cast<int64_t>(p) * slot_res;
+  // emit the lanes' flagged cells g into child q's list (lrn or near)
+  auto emit = [&](int q, bool lrn, bool near, int g) {
+    const unsigned ml = __ballot_sync(full, lrn), mn = __ballot_sync(full, near);
+    const int t = t0 + q;
+    if (lrn) {
+      const int k = nl[q] + __popc(ml & below);
+      if (k < D.slot_lrn) D.lrn_cell[static_cast<int64_t>(t) * D.slot_lrn + k] = g;
+    }
+    if (near) {
+      const int k = nn[q] + __popc(mn & below);
+      if (k < D.slot_near) D.near_idx[static_cast<int64_t>(t) * D.slot_near + k] = g - T.base[L];
+      near_pairs += static_cast<long long>(tc[q]) * T.count[g];
+    }
+    nl[q] += __popc(ml);
+    nn[q] += __popc(mn);
+  };
+  for (int i0 = 0; i0 < nr; i0 += 32) {
+    const int e = i0 + lane < nr ? rp[i0 + lane] : -1;
+    const int g = e & ((1 << 27) - 1), l = e >> 27;
+    int4 c = make_int4(0, 0, 0, 0);
+    if (e >= 0) c = T.cen[g];
+    // a parent-level cell's leaves
+    const int nk = (e >= 0 && l == L - 1) ? (c.w & 15) : 0, clo = c.w >> 4;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (q >= nkP) break;  // uniform
+      bool acc = false, near = false, expand = false;
+      if (e >= 0) {
+        const int dx = cL[q].x - c.x, dy = cL[q].y - c.y, dz = cL[q].z - c.z;
+        const int d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 > T.thr_far[l])
+          acc = true;  // (for l < L - 1 always: accepted for every child of P)
+        else if (l == L)
+          near = true;
+        else if (l == L - 1)
+          expand = true;
+      }
+      emit(q, acc, near, g);
+      // parent-level cells that leaf q does not accept: their leaves, four
+      // cells per pass (eight lanes each), in lane order then child order
+      unsigned mexp = __ballot_sync(full, expand);
+      while (mexp) {
+        // this lane's cell: the (lane / 8)-th set bit of mexp
+        unsigned m = mexp;
+        for (int r = 0; r < (lane >> 3); ++r) m &= m - 1;
+        const int src = m ? __ffs(m) - 1 : 32;
+        const int sl = src < 32 ? src : 0, ch = lane & 7;
+        const int sclo = __shfl_sync(full, clo, sl), snk = __shfl_sync(full, nk, sl);
+        bool a2 = false, n2 = false;
+        int gl = 0;
+        if (src < 32 && ch < snk) {
+          gl = T.base[L] + sclo + ch;
+          const int4 c2 = T.cen[gl];
+          const int dx = cL[q].x - c2.x, dy = cL[q].y - c2.y, dz = cL[q].z - c2.z;
+          a2 = dx * dx + dy * dy + dz * dz > T.thr_far[L];
+          n2 = !a2;
+        }
+        emit(q, a2, n2, gl);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) mexp &= mexp - 1;  // the four cells done
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    if (q < nkP && lane == 0) {
+      const int t = t0 + q;
+      D.near_cnt[t] = nn[q];
+      D.lrn_cnt[t] = nl[q];
+      if (nn[q] > D.slot_near || nl[q] > D.slot_lrn) atomicOr(overflow, 4u);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) near_pairs += __shfl_xor_sync(full, near_pairs, o);
+  if (lane == 0) {
+    unsigned long long* work = reinterpret_cast<unsigned long long*>(overflow + 2);
+    atomicAdd(work, static_cast<unsigned long long>(near_pairs));
+  }
+}
+
 // slot-mode lists -> flat (target, cell) pair lists ordered by target: warp
 // per target, lanes over its slot; off = the exclusive scan of the counts
 __global__ void compact_slots_kernel(int ntgt, int cap, const int* __restrict__ cnt,
@@ -1554,6 +1768,7 @@ struct fvx_tree {
   int n_parent_pairs = 0;
   fvx::DevBuf lrn_meta, lrn_leaf, lrn_cell, leaf_local;
   fvx::DevBuf lrn_slot, par_slot;  // one-pass (slot) form of the two-level lists
+  fvx::DevBuf res_slot, res_cnt;   // per parent: residual cells for its leaves
   int slot_near = 512, slot_lrn = 1024, slot_par = 1024;  // 0: counting pass always
   int n_learned = 0;
   // the structure of the last full build (grid, sort, cells, interaction
@@ -1930,7 +2145,17 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
     D.slot_near = kSlotNear;
     D.slot_lrn = kSlotLrn;
     D.slot_par = kSlotPar;
-    traverse_dual_kernel<true><<<(nleaf + 127) / 128, 128, 0, s>>>(V, D, ovf);
+    // parent-level walk once per parent, then each leaf's residual cells
+    constexpr int kSlotRes = 1024;
+    if ((rc = grow(T->res_slot, 4 * size_t(npar) * kSlotRes)) ||
+        (rc = grow(T->res_cnt, 4 * size_t(npar))))
+      return rc;
+    traverse_parents_kernel<<<(npar + kParWarps - 1) / kParWarps, kParWarps * 32, 0, s>>>(
+        V, par_cnt, P<int>(T->par_slot), kSlotPar, P<int>(T->res_cnt), P<int>(T->res_slot),
+        kSlotRes, ovf);
+    FVX_LAUNCH_CHECK();
+    traverse_residual_kernel<<<(npar + kParWarps - 1) / kParWarps, kParWarps * 32, 0, s>>>(
+        V, D, P<int>(T->res_cnt), P<int>(T->res_slot), kSlotRes, ovf);
     FVX_LAUNCH_CHECK();
     iota_scaled_kernel<<<(nleaf + 255) / 256, 256, 0, s>>>(nleaf, kSlotNear, near_off);
     FVX_LAUNCH_CHECK();
@@ -2291,7 +2516,7 @@ void fvx_tree_destroy(fvx_tree* T) {
                          &T->lrn_cell, &T->leaf_local, &T->val_X, &T->val_T, &T->val_A,
                          &T->val_Y, &T->val_scale, &T->val_err, &T->val_fb, &T->val_stats,
                          &T->dual_meta, &T->par_par, &T->par_cell, &T->parent_local,
-                         &T->cen,
+                         &T->cen, &T->res_slot, &T->res_cnt,
                          &T->lrn_slot, &T->par_slot,
                          &T->pair_partial};
   for (auto* b : bufs)
