@@ -2378,7 +2378,8 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
       if (nlist <= 0 || samples <= 0) return FVX_OK;
       const int stride = nlist > samples ? nlist / samples : 1;
       const int k = nlist / stride < samples ? nlist / stride : samples;
-      // slices: about eight CTAs per SM over the k sums
+      // slices: about eight CTAs per SM over the k sums (more slices cost more
+      // in their FP64 reductions than they save on the few large cells)
       const int slices = max(1, min(64, 8 * device_sm_count() / k));
       int r = grow(T->pair_partial, sizeof(double) * 30 * size_t(k) * slices);
       if (r) return r;

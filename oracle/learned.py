@@ -177,6 +177,22 @@ def learned_pairs(tree, theta_learned):
     return out
 
 
+def pair_features(tree, pos, alpha, pairs, target_level=None):
+    """Features X (k, 48) alone of the pairs (as pair_samples, without the
+    exact local expansions)."""
+    perm = tree["perm"]
+    sp, sa = pos[perm], alpha[perm]
+    leaves = tree["levels"][tree["L"] if target_level is None else target_level]
+    X = np.zeros((len(pairs), IN))
+    for r, (t, l, c) in enumerate(pairs):
+        lev = tree["levels"][l]
+        s, e = lev["start"][c], lev["end"][c]
+        M0, M1, M2 = cell_moments(lev["center"][c], sp[s:e], sa[s:e])
+        X[r], _ = features(leaves["center"][t], leaves["h"], lev["center"][c], lev["h"], M0, M1,
+                           M2)
+    return X
+
+
 def pair_samples(tree, pos, alpha, pairs, target_level=None):
     """Features X (k, 48) and normalised exact targets T (k, 32) of the pairs
     (target cells at the leaf level, or at ``target_level``)."""

@@ -191,9 +191,20 @@ def test_sampled_parent_pairs_match_exact_local_expansions(cuda):
     stride = len(pairs) // max_pairs if len(pairs) > max_pairs else 1
     k = min(len(pairs) // stride, max_pairs)
     assert Xg.shape[0] == k
-    Xo, To = OL.pair_samples(tree, pos, alpha, [pairs[i * stride] for i in range(k)],
-                             target_level=tree["L"] - 1)
     Xg, Tg = Xg.float().cpu().numpy(), Tg.cpu().numpy()
+    # a parent's list is a set; its order on the device is the device's own.
+    # Each sampled device pair is matched to the oracle pair whose features it
+    # rounds (BF16), the matches must be distinct, and their FP64 targets agree
+    Xall = OL.pair_features(tree, pos, alpha, pairs, target_level=tree["L"] - 1)
+    idx = []
+    for x in Xg:
+        excess = (np.abs(Xall - x) - (2.0 ** -7 * np.abs(Xall) + 1e-6)).max(axis=1)
+        j = int(np.argmin(excess))
+        assert excess[j] <= 0.0, excess[j]
+        idx.append(j)
+    assert len(set(idx)) == len(idx)
+    Xo, To = OL.pair_samples(tree, pos, alpha, [pairs[j] for j in idx],
+                             target_level=tree["L"] - 1)
     assert np.all(np.abs(Xg - Xo) <= 2.0 ** -7 * np.abs(Xo) + 1e-6)
     rel = np.abs(Tg - To).max(axis=1) / np.abs(To).max(axis=1)
     assert rel.max() < 1e-4, rel.max()
