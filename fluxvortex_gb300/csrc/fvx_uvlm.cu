@@ -23,6 +23,8 @@
 // spans vertex columns col[j], col[j]+1 and vertex column c moves with
 // surface surf[c]; ring k = i ns + j.  All per-step inputs are device arrays;
 // the host only sequences launches.
+#include <cooperative_groups.h>
+
 #include "fvx_common.cuh"
 #include "fvx_segment_math.cuh"
 
@@ -404,6 +406,152 @@ __global__ void __launch_bounds__(kLuThreads) lu_solve_kernel(int P, int T, doub
     __syncthreads();
   }
   for (int r = tid; r < P; r += kLuThreads) x[r] = s_x[r];
+}
+
+// The same solve on a cluster of kLuCtas CTAs (systems with P <= kLuClusterMaxP):
+// one SM's FP64 pipe bounds the single-CTA form, so the columns are dealt out
+// cyclically (column j to CTA j mod kLuCtas, kept whole in its shared memory).
+// Step k: the owner of column k searches its pivot, swaps and forms the
+// multipliers in its own shared memory; after one cluster barrier every CTA
+// reads them (distributed shared memory), swaps rows k and piv in its
+// columns, updates its copy of the right-hand side and its trailing columns.
+// The multipliers alternate between two buffers, so one barrier per step
+// suffices (the owner of step k + 2 writes only after every CTA has passed
+// step k + 1's barrier, i.e. finished step k).  Every element sees the same
+// operations in the same order as the single-CTA form, so the factors and the
+// solution are the same.  The upper triangle is then gathered, packed, into
+// CTA 0, which back-substitutes.
+namespace cg = cooperative_groups;
+constexpr int kLuCtas = 8;
+constexpr int kLuClusterThreads = 256;
+constexpr int kLuClusterMaxP = 192;  // packed U, P (P + 1) / 2 doubles, in CTA 0
+
+// Dynamic shared memory per CTA: panel[ceil(P/kLuCtas)][P] (column-major),
+// s_l[2][P], s_x[P], packed U[P (P + 1) / 2] (used in CTA 0).
+__global__ void __cluster_dims__(kLuCtas, 1, 1) __launch_bounds__(kLuClusterThreads)
+    lu_solve_cluster_kernel(int P, double* __restrict__ A, double* __restrict__ b) {
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ double lc_smem[];
+  const int rank = static_cast<int>(cl.block_rank());
+  const int sys = blockIdx.x / kLuCtas;
+  double* a = A + static_cast<int64_t>(sys) * P * P;
+  double* xg = b + static_cast<int64_t>(sys) * P;
+  const int ncmax = (P + kLuCtas - 1) / kLuCtas;
+  const int ncol = rank < P ? (P - rank + kLuCtas - 1) / kLuCtas : 0;
+  double* panel = lc_smem;
+  double* s_l = panel + static_cast<size_t>(ncmax) * P;
+  double* s_x = s_l + 2 * P;
+  double* s_u = s_x + P;
+  __shared__ double s_wv[kLuClusterThreads / 32];
+  __shared__ int s_wi[kLuClusterThreads / 32];
+  __shared__ int s_piv[2];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NT = kLuClusterThreads;
+  for (int e = tid; e < ncol * P; e += NT) {
+    const int q = e / P, r = e - q * P;
+    panel[q * P + r] = a[static_cast<int64_t>(r) * P + rank + kLuCtas * q];
+  }
+  for (int r = tid; r < P; r += NT) s_x[r] = xg[r];
+  __syncthreads();
+  for (int k = 0; k < P; ++k) {
+    const int o = k % kLuCtas, par = k & 1;
+    double* l_own = s_l + par * P;
+    if (rank == o) {
+      double* col = panel + (k / kLuCtas) * P;
+      double best = -1.0;
+      int bi = P;
+      for (int r = k + tid; r < P; r += NT) {
+        const double v = fabs(col[r]);
+        if (v > best) {
+          best = v;
+          bi = r;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const double v2 = __shfl_down_sync(0xffffffffu, best, off);
+        const int i2 = __shfl_down_sync(0xffffffffu, bi, off);
+        if (v2 > best || (v2 == best && i2 < bi)) {
+          best = v2;
+          bi = i2;
+        }
+      }
+      if (lane == 0) {
+        s_wv[warp] = best;
+        s_wi[warp] = bi;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        best = s_wv[0];
+        bi = s_wi[0];
+        for (int w = 1; w < NT / 32; ++w)
+          if (s_wv[w] > best || (s_wv[w] == best && s_wi[w] < bi)) {
+            best = s_wv[w];
+            bi = s_wi[w];
+          }
+        if (!(best > 0.0)) flag_status(kStatusNonFinite);
+        s_piv[par] = bi;
+        if (bi != k && bi < P) {
+          const double t = col[k];
+          col[k] = col[bi];
+          col[bi] = t;
+        }
+      }
+      __syncthreads();
+      const double akk = col[k];
+      for (int r = k + 1 + tid; r < P; r += NT) l_own[r] = col[r] / akk;
+    }
+    cl.sync();
+    const double* l_src = cl.map_shared_rank(l_own, o);
+    const int piv = *cl.map_shared_rank(s_piv + par, o);
+    if (rank != o)
+      for (int r = k + 1 + tid; r < P; r += NT) l_own[r] = l_src[r];
+    // rows k and piv in this CTA's columns j > k (the owner's column k is done)
+    const int q0 = (k + 1 - rank + kLuCtas - 1) / kLuCtas > 0 ? (k + 1 - rank + kLuCtas - 1) / kLuCtas
+                                                             : 0;  // first q with j > k
+    if (piv != k && piv < P)
+      for (int q = q0 + tid; q < ncol; q += NT) {
+        double* c = panel + q * P;
+        const double t = c[k];
+        c[k] = c[piv];
+        c[piv] = t;
+      }
+    if (tid == 0 && piv != k && piv < P) {
+      const double t = s_x[k];
+      s_x[k] = s_x[piv];
+      s_x[piv] = t;
+    }
+    __syncthreads();
+    const double xk = s_x[k];
+    for (int r = k + 1 + tid; r < P; r += NT) s_x[r] -= l_own[r] * xk;
+    // trailing update of this CTA's columns j > k, rows r > k
+    const int nq = ncol - q0, nr = P - k - 1;
+    for (int e = tid; e < nq * nr; e += NT) {
+      const int qq = e / nr, r = k + 1 + (e - qq * nr);
+      double* c = panel + (q0 + qq) * P;
+      c[r] -= l_own[r] * c[k];
+    }
+    __syncthreads();
+  }
+  // gather the upper triangle, packed by columns, into CTA 0
+  double* u0 = cl.map_shared_rank(s_u, 0);
+  for (int q = 0; q < ncol; ++q) {
+    const int j = rank + kLuCtas * q;
+    const int base = j * (j + 1) / 2;
+    for (int r = tid; r <= j; r += NT) u0[base + r] = panel[q * P + r];
+  }
+  cl.sync();
+  if (rank == 0) {
+    for (int k = P - 1; k >= 0; --k) {
+      const int base = k * (k + 1) / 2;
+      const double xk = s_x[k] / s_u[base + k];
+      for (int r = tid; r < k; r += NT) s_x[r] -= s_u[base + r] * xk;
+      __syncthreads();
+      if (tid == 0) s_x[k] = xk;
+      __syncthreads();
+    }
+    for (int r = tid; r < P; r += NT) xg[r] = s_x[r];
+  }
 }
 
 struct LoadsArgs {
@@ -802,6 +950,18 @@ int fvx_uvlm_rhs(int nc, const FvxSurfaces* s, const double* colloc, const doubl
 int fvx_lu_solve_batched(int n_systems, int P, double* A, double* b, void* stream) {
   FVX_ARG_CHECK(n_systems >= 1 && P >= 1 && P <= fvx::kLuMaxP && A && b,
                 "bad solve arguments (P must be 1..%d)", fvx::kLuMaxP);
+  if (P <= fvx::kLuClusterMaxP) {
+    const int ncmax = (P + fvx::kLuCtas - 1) / fvx::kLuCtas;
+    const size_t smem =
+        8 * (static_cast<size_t>(ncmax) * P + 3 * static_cast<size_t>(P) + P * (P + 1) / 2);
+    FVX_CUDA_TRY(cudaFuncSetAttribute(fvx::lu_solve_cluster_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem)));
+    fvx::lu_solve_cluster_kernel<<<n_systems * fvx::kLuCtas, fvx::kLuClusterThreads, smem,
+                                   static_cast<cudaStream_t>(stream)>>>(P, A, b);
+    FVX_LAUNCH_CHECK();
+    return FVX_OK;
+  }
   // tail size T: the largest block (row stride T + 1) that fits next to the
   // three P-vectors in the opt-in shared memory
   const int budget = fvx::device_smem_optin() - 1024;  // static arrays of the kernel
