@@ -280,7 +280,10 @@ int fvx_tree_sample_pairs(fvx_tree* tree, int list, int max_pairs, void* X, floa
  *   systems stored back to back (expanded ring Biot-Savart fused with n).
  * rhs: rhs_i = -((u_inf - v_body) + v1 + v2) . n_i (v1, v2 may be NULL).
  * lu_solve_batched: solves A x = b in place (x -> b) for n_systems P x P
- *   systems, partial pivoting; a zero pivot sets status bit 2.
+ *   systems, partial pivoting; a zero pivot sets status bit 2.  P <= 192 runs
+ *   on a cluster of 8 CTAs per system (thread-block clusters), larger P on
+ *   one CTA per system; both give the same results.  A's contents afterwards
+ *   are unspecified (the one-CTA form works in it).
  * loads: Kutta-Joukowski force on each bound leg, rho (G_ij - G_i-1,j) (V x l),
  *   V = u_inf - v_body + v1 + v2 + v3, minus rho dG/dt A n (gamma_prev NULL:
  *   no unsteady term); writes CL and CDi (device scalars) on the reference
