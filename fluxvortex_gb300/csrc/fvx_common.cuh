@@ -15,6 +15,18 @@ int device_sm_count();
 // Largest dynamic shared memory a block may opt in to (bytes).
 int device_smem_optin();
 
+// One list of (target cell, source cell) local-expansion pairs of the
+// treecode: targets are leaves (or parents of leaves, size h = 2 x leaf size),
+// each pair's expansion added into local[target][32].
+struct FarPairs {
+  const int* pair_tgt;       // target id of each pair
+  const int* pair_cell;      // global source cell id of each pair
+  const uint32_t* tgt_key;   // Morton key of each target
+  float h;                   // target size
+  float* local;              // [targets][32] local expansions (accumulated)
+  int n;                     // pairs
+};
+
 // Thread-local error message of the last failing C-ABI call.
 void set_last_error(const char* fmt, ...);
 

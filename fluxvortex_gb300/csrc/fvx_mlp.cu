@@ -271,13 +271,11 @@ struct RowsIO {
   __nv_bfloat16* h_store;
 };
 
+// The far field's rows: list l0's pairs, then list l1's (the leaves' own
+// pairs and the pairs shared through parents of leaves, in one launch).
 struct FarIO {
-  const int* pair_leaf;    // leaf id of each learned pair
-  const int* pair_cell;    // global cell id of each learned pair
-  const uint32_t* leaf_key;
-  const float* rec;        // cell records
-  float h;                 // leaf size
-  float* leaf_local;       // [n_leaves][32] local expansions (accumulated)
+  FarPairs l0, l1;
+  const float* rec;  // cell records
 };
 
 template <bool FAR>
@@ -431,20 +429,22 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
   // dependent levels (the pair's leaf and cell indices while the next tile's
   // first MMA runs, the leaf key and the cell record while its third MMA
   // runs), so that the loads' latency leaves the tile's serial chain.
-  int pf_leaf = 0, pf_cell = 0;
+  int pf_leaf = 0, pf_cell = 0, pf_li = 0;
   uint32_t pf_key = 0;
   RecRegs pf_rec;
   auto fetch_index = [&](int t) {
     const int r = t * 128 + lt;
     if (t < ntiles && r < rows) {
-      pf_leaf = A.f.pair_leaf[r];
-      pf_cell = A.f.pair_cell[r];
+      pf_li = r >= A.f.l0.n ? 1 : 0;
+      const int rr = pf_li ? r - A.f.l0.n : r;
+      pf_leaf = (pf_li ? A.f.l1.pair_tgt : A.f.l0.pair_tgt)[rr];
+      pf_cell = (pf_li ? A.f.l1.pair_cell : A.f.l0.pair_cell)[rr];
     }
   };
   auto fetch_record = [&](int t) {
     const int r = t * 128 + lt;
     if (t < ntiles && r < rows) {
-      pf_key = A.f.leaf_key[pf_leaf];
+      pf_key = (pf_li ? A.f.l1.tgt_key : A.f.l0.tgt_key)[pf_leaf];
       pf_rec = load_record(A.f.rec + static_cast<int64_t>(pf_cell) * kRecFloats);
     }
   };
@@ -455,7 +455,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
   for (int tile = kGroups * blockIdx.x + grp; tile < ntiles && ok; tile += tile_step) {
     const int row = tile * 128 + lt;
     const bool act_row = row < rows;
-    int leaf = 0;
+    int leaf = 0, li = 0;
     // input tile (K = 48)
     {
       char* base = reinterpret_cast<char*>(act);
@@ -464,8 +464,10 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         float* ax = S.aux[grp][lt];
         if (act_row) {
           leaf = pf_leaf;
-          const float3 cT = leaf_center(pf_key, A.f.h);
-          const PairScale sc = pair_features(pf_rec.v, cT.x, cT.y, cT.z, A.f.h, f);
+          li = pf_li;
+          const float th = li ? A.f.l1.h : A.f.l0.h;
+          const float3 cT = leaf_center(pf_key, th);
+          const PairScale sc = pair_features(pf_rec.v, cT.x, cT.y, cT.z, th, f);
           ax[0] = sc.s2;
           ax[1] = sc.s3;
           ax[2] = sc.s4;
@@ -539,7 +541,10 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         }
       }
       const int lane = threadIdx.x & 31;
-      const int my = act_row ? leaf : -1 - lane;
+      // the target, unique across the two lists
+      const int my = act_row ? (leaf | (li << 30)) : -1 - lane;
+      float* L = act_row ? (li ? A.f.l1.local : A.f.l0.local) + static_cast<int64_t>(leaf) * OUT
+                         : nullptr;
       if (__all_sync(0xffffffffu, my == __shfl_sync(0xffffffffu, my, 0))) {
         // one target for the whole warp (pairs are ordered by target, runs are
         // long): reduce-scatter by recursive halving, 31 shuffles for the 32
@@ -554,13 +559,12 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
             x[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
           }
         }
-        if (lane < NOUT) atomicAdd(A.f.leaf_local + static_cast<int64_t>(leaf) * OUT + lane, x[0]);
+        if (lane < NOUT) atomicAdd(L + lane, x[0]);
       } else {
         // runs of equal targets inside the warp: segmented sums to each run's
         // first lane, which adds them to the target's expansion
         const int up = __shfl_up_sync(0xffffffffu, my, 1);
         const bool head = act_row && (lane == 0 || up != my);
-        float* L = act_row ? A.f.leaf_local + static_cast<int64_t>(leaf) * OUT : nullptr;
 #pragma unroll
         for (int c = 0; c < NOUT; ++c) {
           float y = x[c];
@@ -717,12 +721,9 @@ __global__ void pair_targets_kernel(int npairs, int stride, int slices,
 // Resident CTAs (two per SM at 128 registers) stride over blocks of pairs.
 constexpr int kM2lThreads = 256;
 
-__global__ void __launch_bounds__(kM2lThreads) m2l_pairs_kernel(int npairs, const int* __restrict__ pair_leaf,
-                                                        const int* __restrict__ pair_cell,
-                                                        const uint32_t* __restrict__ leaf_key,
-                                                        const float* __restrict__ rec, float h,
-                                                        float* __restrict__ leaf_local) {
+__global__ void __launch_bounds__(kM2lThreads) m2l_pairs_kernel(FarIO F) {
   const int lane = threadIdx.x & 31;
+  const int npairs = F.l0.n + F.l1.n;
   for (int base = blockIdx.x * kM2lThreads; base < npairs; base += gridDim.x * kM2lThreads) {
     const int row = base + threadIdx.x;
     const bool act_row = row < npairs;
@@ -730,17 +731,22 @@ __global__ void __launch_bounds__(kM2lThreads) m2l_pairs_kernel(int npairs, cons
 #pragma unroll
     for (int q = 0; q < NOUT; ++q) a[q] = 0.f;
     PairScale sc{0.f, 0.f, 0.f};
-    int leaf = 0;
+    int leaf = 0, li = 0;
+    float* L = nullptr;
     if (act_row) {
-      leaf = pair_leaf[row];
-      const float3 cT = leaf_center(leaf_key[leaf], h);
-      const RecRegs rr = load_record(rec + static_cast<int64_t>(pair_cell[row]) * kRecFloats);
+      li = row >= F.l0.n ? 1 : 0;
+      const int rr_ = li ? row - F.l0.n : row;
+      const FarPairs& fl = li ? F.l1 : F.l0;
+      leaf = fl.pair_tgt[rr_];
+      L = fl.local + static_cast<int64_t>(leaf) * OUT;
+      const float3 cT = leaf_center(fl.tgt_key[leaf], fl.h);
+      const RecRegs rr = load_record(F.rec + static_cast<int64_t>(fl.pair_cell[rr_]) * kRecFloats);
       const PairGeom g = pair_geom(rr.v, cT.x, cT.y, cT.z);
       const RecordMoments src{rr.v, g.Rx * g.id, g.Ry * g.id, g.Rz * g.id, g.hS * g.id, g.im, g.ih};
       m2l_tensor(src, a);
       sc = pair_scale(g);
     }
-    const int my = act_row ? leaf : -1 - lane;
+    const int my = act_row ? (leaf | (li << 30)) : -1 - lane;  // unique across the lists
     float x[32];
 #pragma unroll
     for (int c = 0; c < 32; ++c)
@@ -759,7 +765,7 @@ __global__ void __launch_bounds__(kM2lThreads) m2l_pairs_kernel(int npairs, cons
           x[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
         }
       }
-      if (lane < NOUT) atomicAdd(leaf_local + static_cast<int64_t>(leaf) * OUT + lane, x[0]);
+      if (lane < NOUT) atomicAdd(L + lane, x[0]);
     } else {
       // runs of equal targets inside the warp: segmented sums to each run's
       // first lane
@@ -774,7 +780,7 @@ __global__ void __launch_bounds__(kM2lThreads) m2l_pairs_kernel(int npairs, cons
           const int ol = __shfl_down_sync(0xffffffffu, my, off);
           if (lane + off < 32 && ol == my) y += o;
         }
-        if (head) atomicAdd(leaf_local + static_cast<int64_t>(leaf) * OUT + c, y);
+        if (head) atomicAdd(L + c, y);
       }
     }
   }  // pair blocks
@@ -982,10 +988,12 @@ int set_smem(K kernel, size_t bytes) {
 
 // Fused learned far field for the treecode: local expansions of the learned
 // (leaf, cell) pairs added into leaf_local[n_leaves][32] (zeroed by the caller).
-int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
-                        const uint32_t* leaf_key, const float* rec, float h, const void* W,
-                        const float* bias, float* leaf_local, cudaStream_t s) {
+// The learned far field of both lists in one launch: local expansions added
+// into a.local / b.local (zeroed by the caller).
+int mlp_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, const void* W,
+                        const float* bias, cudaStream_t s) {
   using namespace mlp;
+  const int npairs = a.n + b.n;
   if (npairs <= 0) return FVX_OK;
   static int done = 0;
   if (!done) {
@@ -995,7 +1003,7 @@ int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
   }
   FwdArgs<true> A;
   A.r = RowsIO{nullptr, nullptr, nullptr, nullptr};
-  A.f = FarIO{pair_leaf, pair_cell, leaf_key, rec, h, leaf_local};
+  A.f = FarIO{a, b, rec};
   const int nctas = ((npairs + 127) / 128 + kGroups - 1) / kGroups;
   const int grid = nctas < device_sm_count() ? nctas : device_sm_count();
   mlp_fwd_kernel<true, true><<<grid, kGroups * 128, sizeof(FwdSmem), s>>>(
@@ -1004,14 +1012,13 @@ int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
   return FVX_OK;
 }
 
-int m2l_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
-                        const uint32_t* leaf_key, const float* rec, float h, float* leaf_local,
-                        cudaStream_t s) {
+// The analytic multipole-to-local translation of both lists in one launch.
+int m2l_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, cudaStream_t s) {
+  const int npairs = a.n + b.n;
   if (npairs <= 0) return FVX_OK;
   const int blocks = (npairs + mlp::kM2lThreads - 1) / mlp::kM2lThreads;
   const int grid = blocks < 2 * device_sm_count() ? blocks : 2 * device_sm_count();
-  mlp::m2l_pairs_kernel<<<grid, mlp::kM2lThreads, 0, s>>>(npairs, pair_leaf, pair_cell, leaf_key,
-                                                         rec, h, leaf_local);
+  mlp::m2l_pairs_kernel<<<grid, mlp::kM2lThreads, 0, s>>>(mlp::FarIO{a, b, rec});
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
@@ -1068,7 +1075,7 @@ int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, f
   FwdArgs<false> A;
   A.r = RowsIO{static_cast<const __nv_bfloat16*>(X), Y, z_store,
                static_cast<__nv_bfloat16*>(h_store)};
-  A.f = FarIO{nullptr, nullptr, nullptr, nullptr, 0.f, nullptr};
+  A.f = FarIO{fvx::FarPairs{}, fvx::FarPairs{}, nullptr};
   const int nctas = ((rows + 127) / 128 + kGroups - 1) / kGroups;
   const int grid = nctas < fvx::device_sm_count() ? nctas : fvx::device_sm_count();
   // without stores it is inference: the F16 form the treecode far field runs

@@ -1728,9 +1728,8 @@ void grid_params(const double lo[3], const double hi[3], int64_t n, int leaf_tar
 
 }  // namespace
 
-int mlp_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
-                        const uint32_t* leaf_key, const float* rec, float h, const void* W,
-                        const float* bias, float* leaf_local, cudaStream_t s);
+int mlp_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, const void* W,
+                        const float* bias, cudaStream_t s);
 int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const int* pair_cell,
                             const uint32_t* tgt_key, float h_tgt, const uint32_t* leaf_key,
                             const float* rec, const int* cell_start,
@@ -1738,9 +1737,7 @@ int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const 
                             const int* leaf_of_particle, float h, void* X, float* T,
                             float* A, float* scale, double* partial, int slices,
                             cudaStream_t s);
-int m2l_farfield_launch(int npairs, const int* pair_leaf, const int* pair_cell,
-                        const uint32_t* leaf_key, const float* rec, float h, float* leaf_local,
-                        cudaStream_t s);
+int m2l_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, cudaStream_t s);
 
 }  // namespace fvx
 
@@ -2334,29 +2331,30 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
     FVX_CUDA_TRY(cudaEventRecord(T->ev2, s));
     // the analytic translation, then (learned) the network's residual, for the
     // leaves' own pairs and for the pairs shared through their parents
-    auto local_stage = [&](int npairs, const int* tgt, const int* cell, const uint32_t* tkey,
-                           float th, int ntgt, DevBuf& buf) -> int {
+    // zeroed expansions of the leaves (and parents), then the analytic
+    // translation and (learned) the network's residual of both lists, each in
+    // one launch
+    auto zeroed = [&](DevBuf& buf, int ntgt) -> int {
       int r = grow(buf, sizeof(float) * 32 * size_t(ntgt));
       if (r) return r;
       FVX_CUDA_TRY(cudaMemsetAsync(buf.p, 0, sizeof(float) * 32 * size_t(ntgt), s));
-      if (npairs == 0) return FVX_OK;
-      r = m2l_farfield_launch(npairs, tgt, cell, tkey, rec, th, P<float>(buf), s);
-      if (r) return r;
-      if (T->far_method == FVX_FAR_LEARNED)
-        r = mlp_farfield_launch(npairs, tgt, cell, tkey, rec, th, T->mlp_W, T->mlp_b,
-                                P<float>(buf), s);
-      return r;
+      return FVX_OK;
     };
-    if ((rc = local_stage(static_cast<int>(lrn_total), P<int>(T->lrn_leaf), P<int>(T->lrn_cell),
-                          leaves.key, static_cast<float>(h), nleaf, T->leaf_local)))
+    if ((rc = zeroed(T->leaf_local, nleaf))) return rc;
+    FarPairs la{P<int>(T->lrn_leaf), P<int>(T->lrn_cell), leaves.key, static_cast<float>(h),
+                P<float>(T->leaf_local), static_cast<int>(lrn_total)};
+    FarPairs lb{};
+    if (dual) {
+      if ((rc = zeroed(T->parent_local, npar))) return rc;
+      lb = FarPairs{P<int>(T->par_par), P<int>(T->par_cell), par_key, static_cast<float>(2.0 * h),
+                    P<float>(T->parent_local), static_cast<int>(par_total)};
+    }
+    if ((rc = m2l_farfield_launch(la, lb, rec, s))) return rc;
+    if (T->far_method == FVX_FAR_LEARNED &&
+        (rc = mlp_farfield_launch(la, lb, rec, T->mlp_W, T->mlp_b, s)))
       return rc;
     A.leaf_local = P<float>(T->leaf_local);
-    if (dual) {
-      if ((rc = local_stage(static_cast<int>(par_total), P<int>(T->par_par), P<int>(T->par_cell),
-                            par_key, static_cast<float>(2.0 * h), npar, T->parent_local)))
-        return rc;
-      A.parent_local = P<float>(T->parent_local);
-    }
+    if (dual) A.parent_local = P<float>(T->parent_local);
     FVX_CUDA_TRY(cudaEventRecord(T->ev3, s));
   }
   // validation sample: FP64 direct local expansions of evenly strided pairs of
