@@ -1056,6 +1056,8 @@ struct EvalArgs {
   const float* leaf_local;  // [leaves][32] learned local expansions, or null
   const float* parent_local;  // [parents][32] expansions shared by a parent's leaves, or null
   const int* leaf_parent;     // parent index of each leaf (with parent_local)
+  int nleaf;
+  int* leaf_next;             // leaf counter of the resident evaluation warps (zeroed)
 };
 
 // Learned local expansion of the leaf at offset d = x - c_T (u, J = du/dx,
@@ -1276,27 +1278,34 @@ __device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, in
   }
 }
 
+// Shared memory of an evaluation warp: the near tile (plain or paired layout)
+// and the far-cell records share the storage.
 template <int MODE, int KERNEL, int TPT>
-__global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
+struct EvalSmem {
+  // paired path: Winckelmans velocity / stretching with two targets per thread
+  static constexpr bool PACKED = TPT == 2 && KERNEL == FVX_KERNEL_WINCKELMANS &&
+                                 (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_STRETCH);
+  static constexpr int kNearBytes = PACKED ? kNearRows * static_cast<int>(sizeof(NearX2))
+                                           : kNearTile * 2 * static_cast<int>(sizeof(float4));
+  static constexpr int kFarBytes = kFarTile * kRecFloats * 4;
+  static constexpr int bytes = kNearBytes > kFarBytes ? kNearBytes : kFarBytes;
+};
+
+// Leaf t: its targets against its near leaves and far cells, plus the local
+// expansions (one warp).
+template <int MODE, int KERNEL, int TPT>
+__device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned char* s_raw) {
   using namespace pair;
   constexpr int NC = ModeInfo<MODE>::ncomp;
   constexpr int NA = ModeInfo<MODE>::na;
   constexpr bool NEED_FPR = ModeInfo<MODE>::need_fpr;
   constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
-  // paired path: Winckelmans velocity / stretching with two targets per thread
-  constexpr bool PACKED = TPT == 2 && KERNEL == FVX_KERNEL_WINCKELMANS &&
-                          (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_STRETCH);
-  // near tile (plain or paired layout) and far-cell records share the storage
-  constexpr int kNearBytes = PACKED ? kNearRows * static_cast<int>(sizeof(NearX2))
-                                    : kNearTile * 2 * static_cast<int>(sizeof(float4));
-  constexpr int kFarBytes = kFarTile * kRecFloats * 4;
-  __shared__ __align__(16) unsigned char s_raw[kNearBytes > kFarBytes ? kNearBytes : kFarBytes];
+  constexpr bool PACKED = EvalSmem<MODE, KERNEL, TPT>::PACKED;
   float4* s_p = reinterpret_cast<float4*>(s_raw);
   float4* s_a = s_p + kNearTile;
   NearX2* s_x2 = reinterpret_cast<NearX2*>(s_raw);
   float* s_rec = reinterpret_cast<float*>(s_raw);
 
-  const int t = blockIdx.x;
   const int tstart = A.leaf_start[t], tcount = A.leaf_count[t];
   const float3 cT = cell_center_rel(A.leaf_key[t], A.h);
   const int nno = A.near_off[t], nnc = A.near_cnt[t];
@@ -1566,6 +1575,22 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
   }
 }
 
+// Resident evaluation warps (one per CTA) take leaves from a shared counter
+// until none are left: the SMs stay at their occupancy limit to the end, and
+// no CTA is launched per leaf.
+template <int MODE, int KERNEL, int TPT>
+__global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
+  __shared__ __align__(16) unsigned char s_raw[EvalSmem<MODE, KERNEL, TPT>::bytes];
+  for (;;) {
+    int t = 0;
+    if (threadIdx.x == 0) t = atomicAdd(A.leaf_next, 1);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= A.nleaf) break;
+    eval_leaf<MODE, KERNEL, TPT>(A, t, s_raw);
+    __syncthreads();  // the next leaf restages the shared buffer
+  }
+}
+
 // ---- validation of the local-expansion path against FP64 direct sums -------------
 // Row k checks list pair k*stride: exact normalised expansion T (FP64 sums),
 // analytic translation A and network residual Y (zero without a network).
@@ -1788,6 +1813,7 @@ struct fvx_tree {
   // two-level traversal: per-parent lists and expansions
   fvx::DevBuf dual_meta, par_par, par_cell, parent_local;
   fvx::DevBuf cen;  // cell centres in units of h/2 (dual traversal)
+  fvx::DevBuf eval_next;  // leaf counter of the evaluation kernel
   fvx::DevBuf pair_partial;  // slices of the FP64 exact-expansion sums
   int n_parent_pairs = 0;
   fvx::DevBuf lrn_meta, lrn_leaf, lrn_cell, leaf_local;
@@ -1830,24 +1856,44 @@ void launch_gather(int n, const int* perm, const int* leaf_of, const uint32_t* l
                                                              alpha, sigma, tgam, sp, sa, sg);
 }
 
+// Resident CTAs: the occupancy limit per SM times the SMs (at most one per leaf).
+template <typename K>
+int resident_grid(K kernel, int nleaf) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, tree::kEvalThreads, 0) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const int64_t g = static_cast<int64_t>(per_sm) * device_sm_count();
+  return static_cast<int>(g < nleaf ? g : nleaf);
+}
+
 // Targets per thread: leaves of at most ~40 particles on average fill one
 // 32-target chunk per warp better than two.
 template <int KERNEL, int TPT>
 void launch_eval_tpt(int mode, int nleaf, const tree::EvalArgs& A, cudaStream_t s) {
   using namespace tree;
   switch (mode) {
-    case FVX_PAIR_VELOCITY:
-      eval_kernel<FVX_PAIR_VELOCITY, KERNEL, TPT><<<nleaf, kEvalThreads, 0, s>>>(A);
+    case FVX_PAIR_VELOCITY: {
+      auto k = eval_kernel<FVX_PAIR_VELOCITY, KERNEL, TPT>;
+      k<<<resident_grid(k, nleaf), kEvalThreads, 0, s>>>(A);
       break;
-    case FVX_PAIR_STRETCH:
-      eval_kernel<FVX_PAIR_STRETCH, KERNEL, TPT><<<nleaf, kEvalThreads, 0, s>>>(A);
+    }
+    case FVX_PAIR_STRETCH: {
+      auto k = eval_kernel<FVX_PAIR_STRETCH, KERNEL, TPT>;
+      k<<<resident_grid(k, nleaf), kEvalThreads, 0, s>>>(A);
       break;
-    case FVX_PAIR_VELOCITY_STRETCH:
-      eval_kernel<FVX_PAIR_VELOCITY_STRETCH, KERNEL, TPT><<<nleaf, kEvalThreads, 0, s>>>(A);
+    }
+    case FVX_PAIR_VELOCITY_STRETCH: {
+      auto k = eval_kernel<FVX_PAIR_VELOCITY_STRETCH, KERNEL, TPT>;
+      k<<<resident_grid(k, nleaf), kEvalThreads, 0, s>>>(A);
       break;
-    default:
-      eval_kernel<FVX_PAIR_VORTICITY, KERNEL, TPT><<<nleaf, kEvalThreads, 0, s>>>(A);
+    }
+    default: {
+      auto k = eval_kernel<FVX_PAIR_VORTICITY, KERNEL, TPT>;
+      k<<<resident_grid(k, nleaf), kEvalThreads, 0, s>>>(A);
       break;
+    }
   }
 }
 
@@ -2467,6 +2513,11 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
     FVX_CUDA_TRY(cudaEventCreate(&T->ev0));
     FVX_CUDA_TRY(cudaEventCreate(&T->ev1));
   }
+  // the resident evaluation warps' leaf counter
+  if ((rc = grow(T->eval_next, 16))) return rc;
+  FVX_CUDA_TRY(cudaMemsetAsync(T->eval_next.p, 0, sizeof(int), s));
+  A.nleaf = nleaf;
+  A.leaf_next = P<int>(T->eval_next);
   FVX_CUDA_TRY(cudaEventRecord(T->ev0, s));
   if (kernel == FVX_KERNEL_WINCKELMANS)
     launch_eval<FVX_KERNEL_WINCKELMANS>(mode, nleaf, n, A, s);
@@ -2555,7 +2606,7 @@ void fvx_tree_destroy(fvx_tree* T) {
                          &T->lrn_cell, &T->leaf_local, &T->val_X, &T->val_T, &T->val_A,
                          &T->val_Y, &T->val_scale, &T->val_err, &T->val_fb, &T->val_stats,
                          &T->dual_meta, &T->par_par, &T->par_cell, &T->parent_local,
-                         &T->cen, &T->res_slot, &T->res_cnt,
+                         &T->cen, &T->res_slot, &T->res_cnt, &T->eval_next,
                          &T->lrn_slot, &T->par_slot,
                          &T->pair_partial};
   for (auto* b : bufs)
