@@ -469,10 +469,10 @@ __global__ void leaf_moments_kernel(Level lv, const int* __restrict__ n_leaves, 
 }
 
 // parent moments from children (shift by s = c_child - c_parent, exact)
-// One parent cell's record from its children's records.
-__device__ __forceinline__ void m2m_cell(const Level& par, int p, float hl,
-                                         const float* __restrict__ child_rec,
-                                         float* __restrict__ par_rec) {
+__global__ void m2m_kernel(Level par, const int* __restrict__ n_par, float hl,
+                           const float* __restrict__ child_rec, float* __restrict__ par_rec) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= *n_par) return;
   const float3 cp = cell_center_rel(par.key[p], hl);
   float M0[3] = {0, 0, 0}, M1[9], M2[18];
   for (int q = 0; q < 9; ++q) M1[q] = 0.f;
@@ -504,33 +504,6 @@ __device__ __forceinline__ void m2m_cell(const Level& par, int p, float hl,
   for (int q = 0; q < 9; ++q) r[10 + q] = M1[q];
   for (int q = 0; q < 18; ++q) r[19 + q] = M2[q];
   r[37] = r[38] = r[39] = 0.f;
-}
-
-__global__ void m2m_kernel(Level par, const int* __restrict__ n_par, float hl,
-                           const float* __restrict__ child_rec, float* __restrict__ par_rec) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= *n_par) return;
-  m2m_cell(par, p, hl, child_rec, par_rec);
-}
-
-// The small upper levels top .. 0 in one CTA, bottom-up, a barrier between
-// levels (instead of a launch per level).
-constexpr int kM2mUpperThreads = 1024;
-constexpr int kM2mUpperCells = 4096;  // levels of at most this many cells go here
-struct M2mLevels {
-  Level lv[12];
-  float hl[12];
-  int64_t off[12];  // first record of each level (base[l] x kRecFloats)
-};
-__global__ void __launch_bounds__(kM2mUpperThreads) m2m_levels_kernel(M2mLevels M, int top,
-                                                                      const int* __restrict__ n_cells,
-                                                                      float* __restrict__ rec) {
-  for (int l = top; l >= 0; --l) {
-    const int n = n_cells[l];
-    for (int p = threadIdx.x; p < n; p += kM2mUpperThreads)
-      m2m_cell(M.lv[l], p, M.hl[l], rec + M.off[l + 1], rec + M.off[l]);
-    __syncthreads();
-  }
 }
 
 // ---- interaction lists --------------------------------------------------------------
@@ -2115,25 +2088,12 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   leaf_moments_kernel<<<(nleaf * 32 + 255) / 256, 256, 0, s>>>(
       leaves, ncells_d + L, static_cast<float>(h), sp, sa, rec + int64_t(base[L]) * kRecFloats);
   FVX_LAUNCH_CHECK();
-  {
-    int l = L - 1;
-    for (; l >= 0 && ncells[l] > kM2mUpperCells; --l) {
-      const float hl = static_cast<float>(h * static_cast<double>(1 << (L - l)));
-      m2m_kernel<<<(ncells[l] + 127) / 128, 128, 0, s>>>(
-          level(l), ncells_d + l, hl, rec + int64_t(base[l + 1]) * kRecFloats,
-          rec + int64_t(base[l]) * kRecFloats);
-      FVX_LAUNCH_CHECK();
-    }
-    if (l >= 0) {
-      M2mLevels M{};
-      for (int q = 0; q <= l + 1; ++q) {
-        M.lv[q] = level(q);
-        M.hl[q] = static_cast<float>(h * static_cast<double>(1 << (L - q)));
-        M.off[q] = int64_t(base[q]) * kRecFloats;
-      }
-      m2m_levels_kernel<<<1, kM2mUpperThreads, 0, s>>>(M, l, ncells_d, rec);
-      FVX_LAUNCH_CHECK();
-    }
+  for (int l = L - 1; l >= 0; --l) {
+    const float hl = static_cast<float>(h * static_cast<double>(1 << (L - l)));
+    m2m_kernel<<<(ncells[l] + 127) / 128, 128, 0, s>>>(
+        level(l), ncells_d + l, hl, rec + int64_t(base[l + 1]) * kRecFloats,
+        rec + int64_t(base[l]) * kRecFloats);
+    FVX_LAUNCH_CHECK();
   }
   // 6. interaction lists
   TreeView V;
