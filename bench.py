@@ -42,7 +42,8 @@ METRIC = "VPM+panel steps/s at 1e6 particles: learned/FP32 vs FP64 direct @CL er
 UNIT = "steps/s"
 
 # Algorithmic flop per (target, source) pair, counting + - * as 1, FMA as 2,
-# sqrt / rsqrt / div / exp / erf as 1 ("Work per unit").
+# sqrt / rsqrt / div / exp / erf as 1, with the per-source constants (sigma^2,
+# 2.5 sigma^2, the 1/4pi folded into the strengths) hoisted out of the pair.
 FLOP_PER_PAIR = {
     ("velocity", "winckelmans"): 30,
     ("stretch", "winckelmans"): 57,
