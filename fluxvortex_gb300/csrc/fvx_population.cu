@@ -27,7 +27,7 @@ namespace fvx {
 int scan_ints(const int* in, int n, int* out, int inclusive, int* tmp, cudaStream_t s);
 int sort_table_ints(int n);
 int sort_pairs_u32(uint32_t* keys, int* idx, uint32_t* keys_tmp, int* idx_tmp, int n, int* table,
-                   int* scan_tmp, cudaStream_t s);
+                   int* scan_tmp, cudaStream_t s, int passes = 4);
 
 namespace {
 

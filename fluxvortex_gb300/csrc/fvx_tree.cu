@@ -262,15 +262,18 @@ __global__ void __launch_bounds__(256) radix_scatter_kernel(
 // idx_tmp) hold n each, table sort_table_ints(n) ints, scan_tmp 2 x 2048 ints.
 int sort_table_ints(int n) { return 256 * ((n + tree::kSortItems - 1) / tree::kSortItems) * 2; }
 
+// passes: 8-bit digits sorted (an even number: the result is back in (keys, idx))
 int sort_pairs_u32(uint32_t* keys, int* idx, uint32_t* keys_tmp, int* idx_tmp, int n, int* table,
-                   int* scan_tmp, cudaStream_t s) {
+                   int* scan_tmp, cudaStream_t s, int passes = 4);
+int sort_pairs_u32(uint32_t* keys, int* idx, uint32_t* keys_tmp, int* idx_tmp, int n, int* table,
+                   int* scan_tmp, cudaStream_t s, int passes) {
   using namespace tree;
   if (n <= 0) return FVX_OK;
   const int nblk = (n + kSortItems - 1) / kSortItems;
   int* table_ex = table + 256 * nblk;
   uint32_t *ka = keys, *kb = keys_tmp;
   int *ia = idx, *ib = idx_tmp;
-  for (int pass = 0; pass < 4; ++pass) {
+  for (int pass = 0; pass < passes; ++pass) {
     radix_hist_kernel<<<nblk, 256, 0, s>>>(ka, n, 8 * pass, nblk, table);
     FVX_LAUNCH_CHECK();
     int rc = scan_ints(table, 256 * nblk, table_ex, 0, scan_tmp, s);
@@ -284,7 +287,7 @@ int sort_pairs_u32(uint32_t* keys, int* idx, uint32_t* keys_tmp, int* idx_tmp, i
     ia = ib;
     ib = ti;
   }
-  return FVX_OK;  // four passes: the result is back in (keys, idx)
+  return FVX_OK;  // an even number of passes: the result is back in (keys, idx)
 }
 
 namespace tree {
@@ -666,6 +669,18 @@ __global__ void cell_centres_kernel(TreeView T, int total_cells, int4* __restric
                      (2 * static_cast<int>(compact10(k >> 2)) + 1) * sc, kids);
 }
 
+// Sort keys of the evaluation order: leaves by decreasing near-field work
+// (near leaves x own particles, 16 bits), ties in leaf order.
+__global__ void order_keys_kernel(int nleaf, const int* __restrict__ near_cnt,
+                                  const int* __restrict__ leaf_count, uint32_t* __restrict__ keys,
+                                  int* __restrict__ idx) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nleaf) return;
+  const long long w = static_cast<long long>(near_cnt[t]) * leaf_count[t];
+  keys[t] = 0xFFFFu - static_cast<uint32_t>(w < 0xFFFF ? w : 0xFFFF);
+  idx[t] = t;
+}
+
 // leaf -> its parent's level-local index, from the parents' child ranges
 __global__ void leaf_parents_kernel(TreeView T, int* __restrict__ leaf_parent) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1031,6 +1046,7 @@ struct EvalArgs {
   const int* leaf_parent;     // parent index of each leaf (with parent_local)
   int nleaf;
   int* leaf_next;             // leaf counter of the resident evaluation warps (zeroed)
+  const int* leaf_order;      // the order the warps take the leaves in
 };
 
 // Learned local expansion of the leaf at offset d = x - c_T (u, J = du/dx,
@@ -1550,16 +1566,17 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
 
 // Resident evaluation warps (one per CTA) take leaves from a shared counter
 // until none are left: the SMs stay at their occupancy limit to the end, and
-// no CTA is launched per leaf.
+// no CTA is launched per leaf.  The leaves come in decreasing order of their
+// near-field work, so the last ones taken are the shortest.
 template <int MODE, int KERNEL, int TPT>
 __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
   __shared__ __align__(16) unsigned char s_raw[EvalSmem<MODE, KERNEL, TPT>::bytes];
   for (;;) {
-    int t = 0;
-    if (threadIdx.x == 0) t = atomicAdd(A.leaf_next, 1);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= A.nleaf) break;
-    eval_leaf<MODE, KERNEL, TPT>(A, t, s_raw);
+    int c = 0;
+    if (threadIdx.x == 0) c = atomicAdd(A.leaf_next, 1);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= A.nleaf) break;
+    eval_leaf<MODE, KERNEL, TPT>(A, A.leaf_order[c], s_raw);
     __syncthreads();  // the next leaf restages the shared buffer
   }
 }
@@ -1787,6 +1804,7 @@ struct fvx_tree {
   fvx::DevBuf dual_meta, par_par, par_cell, parent_local;
   fvx::DevBuf cen;  // cell centres in units of h/2 (dual traversal)
   fvx::DevBuf eval_next;  // leaf counter of the evaluation kernel
+  fvx::DevBuf leaf_order, order_table;  // evaluation order of the leaves (+ sort scratch)
   fvx::DevBuf pair_partial;  // slices of the FP64 exact-expansion sums
   int n_parent_pairs = 0;
   fvx::DevBuf lrn_meta, lrn_leaf, lrn_cell, leaf_local;
@@ -2344,6 +2362,20 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   ST.far_total = far_total;
   ST.lrn_total = lrn_total;
   ST.par_total = par_total;
+  // the evaluation order: leaves by decreasing near-field work
+  if ((rc = grow(T->leaf_order, 4 * 4 * size_t(nleaf))) ||
+      (rc = grow(T->order_table, 4 * size_t(sort_table_ints(nleaf)))))
+    return rc;
+  {
+    uint32_t* ok0 = P<uint32_t>(T->leaf_order) + 2 * size_t(nleaf);
+    int* oi0 = P<int>(T->leaf_order);
+    order_keys_kernel<<<(nleaf + 255) / 256, 256, 0, s>>>(
+        nleaf, near_cnt, lvb + total_cells + base[L], ok0, oi0);
+    FVX_LAUNCH_CHECK();
+    if ((rc = sort_pairs_u32(ok0, oi0, ok0 + nleaf, oi0 + nleaf, nleaf, P<int>(T->order_table),
+                             P<int>(T->scan_tmp), s, 2)))
+      return rc;
+  }
   ST.valid = true;
   }
   // 7. evaluation
@@ -2478,6 +2510,7 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   FVX_CUDA_TRY(cudaMemsetAsync(T->eval_next.p, 0, sizeof(int), s));
   A.nleaf = nleaf;
   A.leaf_next = P<int>(T->eval_next);
+  A.leaf_order = P<int>(T->leaf_order);
   FVX_CUDA_TRY(cudaEventRecord(T->ev0, s));
   if (kernel == FVX_KERNEL_WINCKELMANS)
     launch_eval<FVX_KERNEL_WINCKELMANS>(mode, nleaf, n, A, s);
@@ -2567,6 +2600,7 @@ void fvx_tree_destroy(fvx_tree* T) {
                          &T->val_Y, &T->val_scale, &T->val_err, &T->val_fb, &T->val_stats,
                          &T->dual_meta, &T->par_par, &T->par_cell, &T->parent_local,
                          &T->cen, &T->res_slot, &T->res_cnt, &T->eval_next,
+                         &T->leaf_order, &T->order_table,
                          &T->lrn_slot, &T->par_slot,
                          &T->pair_partial};
   for (auto* b : bufs)
