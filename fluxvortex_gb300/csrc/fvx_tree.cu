@@ -1299,17 +1299,24 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
   const float3 cT = cell_center_rel(A.leaf_key[t], A.h);
   const int nno = A.near_off[t], nnc = A.near_cnt[t];
   const int fno = A.far_off[t], fnc = A.far_cnt[t];
-  // Source phases (paired path): a leaf of more than 32 targets takes two per
-  // lane, one in each half of the paired registers; a smaller one takes one
-  // per lane and gives each target G = 2, 4 or 8 workers -- the two halves
+  // Source phases (paired path): the leaf's targets go in chunks of 32, one
+  // target per lane, and each target of a chunk of c gets G = 2, 4 or 8
+  // workers (c > 16, > 8, <= 8) -- the two halves of the paired registers
   // times G/2 groups of lanes -- each summing every G-th source, so that the
-  // 64 paired slots stay busy for leaves of 32, 16 or 8 particles.
-  int G = 1;
-  if constexpr (PACKED) G = tcount > 32 ? 1 : (tcount > 16 ? 2 : (tcount > 8 ? 4 : 8));
-  const int gl = G == 1 ? kEvalThreads : 2 * kEvalThreads / G;  // lanes per group
-  const int grp = threadIdx.x / gl, tl = threadIdx.x - grp * gl;
+  // 64 paired slots stay busy for chunks of 32, 16 or 8 targets.  (Two
+  // targets per lane over 64 slots would leave a leaf of 33..63 targets
+  // 48..2 % idle; a chunk of 32 plus a smaller one with more phases costs
+  // fewer rows.)  The other paths take TPT targets per lane, G = 1.
+  const int chunk_step = PACKED ? kEvalThreads : kEvalThreads * TPT;
 
-  for (int chunk = 0; chunk < tcount; chunk += kEvalThreads * TPT) {
+  for (int chunk = 0; chunk < tcount; chunk += chunk_step) {
+    int G = 1;
+    if constexpr (PACKED) {
+      const int cnt = min(kEvalThreads, tcount - chunk);
+      G = cnt > 16 ? 2 : (cnt > 8 ? 4 : 8);
+    }
+    const int gl = G == 1 ? kEvalThreads : 2 * kEvalThreads / G;  // lanes per group
+    const int grp = threadIdx.x / gl, tl = threadIdx.x - grp * gl;
     float ox[TPT], oy[TPT], oz[TPT], gx[TPT], gy[TPT], gz[TPT];
     float hi[TPT][NC], lo[TPT][NC];
     bool act[TPT];
@@ -1317,7 +1324,7 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
       // G > 1: both slots hold the lane's one target; only group 0 writes it
-      const int k = G == 1 ? chunk + threadIdx.x + j * kEvalThreads : tl;
+      const int k = G == 1 ? chunk + threadIdx.x + j * kEvalThreads : chunk + tl;
       kk[j] = k;
       act[j] = k < tcount && (G == 1 || (j == 0 && grp == 0));
       float4 p = make_float4(0.f, 0.f, 0.f, 0.f), g = p;
