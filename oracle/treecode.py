@@ -29,7 +29,9 @@ Algorithm (shared with the device code through fluxvortex_gb300.tree_params):
   7. ``dual_lists``: the two-level lists of the local-expansion far field
      (cells shared by a parent's leaves, each leaf's own cells, near leaves),
      whose partition of the sources is tested here and whose counts pin the
-     device traversal.
+     device traversal.  ``dual_lists_two_phase`` builds the same sets the way
+     the device does (a walk once per parent, then each parent's residual
+     cells against its leaves); a CPU test checks the two constructions agree.
 """
 from __future__ import annotations
 
@@ -240,6 +242,74 @@ def dual_lists(tree):
                 continue
             if accept_t(l, c):
                 continue
+            for q in range(lev["child_lo"][c], lev["child_hi"][c]):
+                accept_t(L, q)
+        near.append(nr)
+        leaf_far.append(lf)
+    return near, leaf_far, parent_far
+
+
+def dual_lists_two_phase(tree):
+    """The same lists built the way the device builds them: (1) once per parent
+    P, the walk against P alone -- a cell A passing against P goes to P's list;
+    A larger than P passing against the octant of P nearest to it, or A of P's
+    size or a leaf failing against P, goes to P's residual list; other cells are
+    opened -- and (2) per leaf T of P, the residual cells finished against T as
+    in dual_lists.  Returns (near, leaf_far, parent_far) like dual_lists (the
+    order within a list may differ; the sets are the same)."""
+    L, theta = tree["L"], tree["theta"]
+    k = 0.75 / (theta * theta)
+    levels = tree["levels"]
+    leaves, parents = levels[L], levels[L - 1]
+    h = leaves["h"]
+    parent_far, residual = [], []
+    for p in range(len(parents["start"])):
+        cP = parents["center"][p]
+        pf, res = [], []
+        stack = [(0, c) for c in range(len(levels[0]["start"]) - 1, -1, -1)]
+        while stack:
+            l, c = stack.pop()
+            lev = levels[l]
+            dc = cP - lev["center"][c]
+            if (dc ** 2).sum() > k * (2 * h + lev["h"]) ** 2:
+                pf.append((l, c))
+                continue
+            if l < L - 1:
+                near_oct = np.maximum(np.abs(dc) - 0.5 * h, 0.0)
+                if (near_oct ** 2).sum() > k * (h + lev["h"]) ** 2:
+                    res.append((l, c))
+                    continue
+                for ch in range(lev["child_hi"][c] - 1, lev["child_lo"][c] - 1, -1):
+                    stack.append((l + 1, ch))
+                continue
+            res.append((l, c))
+        parent_far.append(pf)
+        residual.append(res)
+    pkeys = parents["key"]
+    near, leaf_far = [], []
+    for t in range(len(leaves["start"])):
+        p = int(np.searchsorted(pkeys, leaves["key"][t] >> 3))
+        cT = leaves["center"][t]
+        nr, lf = [], []
+
+        def accept_t(l, c):
+            lev = levels[l]
+            d2 = ((cT - lev["center"][c]) ** 2).sum()
+            if d2 > k * (h + lev["h"]) ** 2:
+                lf.append((l, c))
+                return True
+            if l == L:
+                nr.append(c)
+                return True
+            return False
+
+        for (l, c) in residual[p]:
+            if l < L - 1:
+                accept_t(l, c)
+                continue
+            if accept_t(l, c):
+                continue
+            lev = levels[l]
             for q in range(lev["child_lo"][c], lev["child_hi"][c]):
                 accept_t(L, q)
         near.append(nr)

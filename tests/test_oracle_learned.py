@@ -176,6 +176,24 @@ def test_dual_lists_partition_every_source_once():
         assert np.all(cover == 1), t
 
 
+def test_two_phase_lists_equal_per_leaf_lists():
+    """The device's construction of the two-level lists (the walk once per
+    parent, then each parent's residual cells against its leaves) gives the
+    same sets as the per-leaf traversal, on a slab and on a clustered cloud."""
+    rng = np.random.default_rng(13)
+    clouds = [rng.uniform([0, 0, 0], [6.0, 3.0, 0.5], (3000, 3)),
+              np.concatenate([rng.normal(0.0, 0.3, (1500, 3)),
+                              rng.normal(2.0, 0.1, (1500, 3))])]
+    for pos in clouds:
+        tree = TC.build(pos, theta=0.5, leaf_target=16)
+        a = TC.dual_lists(tree)
+        b = TC.dual_lists_two_phase(tree)
+        for la, lb in zip(a, b):
+            assert len(la) == len(lb)
+            for x, y in zip(la, lb):
+                assert sorted(x) == sorted(y)
+
+
 def _gen_m2l():
     import importlib.util
     import os
