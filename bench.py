@@ -123,7 +123,12 @@ def start_clock_sampler():
     try:
         f = open(path, "w")
         proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                 "-lms", "200"], stdout=f, stderr=subprocess.DEVNULL)
+                                 "-lms", "50"], stdout=f, stderr=subprocess.DEVNULL)
+        # the timed steps start once the sampler has written its first line
+        # (nvidia-smi takes a few hundred ms to start)
+        t_end = time.perf_counter() + 3.0
+        while time.perf_counter() < t_end and os.path.getsize(path) == 0 and proc.poll() is None:
+            time.sleep(0.02)
         return proc, f, path
     except (OSError, FileNotFoundError):
         return None, None, path
@@ -442,6 +447,14 @@ def run_ours(args, rank, world):
         if vals:
             tree_stats["validation_per_step"] = vals[-1]
     achieved = flop / (avg_ms * 1e-3) / 1e12
+    # DRAM bytes per launch of the stretching evaluation from one ncu capture
+    # (dram__bytes_read.sum + dram__bytes_write.sum = 109.9 + 24.6 MB) of the
+    # same kernel on 2^20 slab particles, leaf target 32; reported only for the
+    # workload that capture matches
+    traffic = None
+    if (kname == "tree eval_kernel<stretch,winckelmans>" and args.n == 1 << 20
+            and args.leaf == 32 and args.precision == "f32c"):
+        traffic = 1.3454e8
 
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -460,7 +473,8 @@ def run_ours(args, rank, world):
         "clocks": clk,
         "roofline": {"bound": "fp32", "kernel": kname,
                      "achieved": achieved, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / (fp32_peak / 1e12), "traffic": None,
+                     "frac": achieved / (fp32_peak / 1e12), "traffic": traffic,
+                     "traffic_unit": "bytes per launch (ncu capture)",
                      "flop_per_launch": flop, "avg_launch_ms": avg_ms,
                      "peak_source": "measured FP32 FMA probe (fvx_probe_fp32_fma) on this GPU"},
         "sweep_ms": {f"{k[0]}/{k[1]}/{k[2]}x{k[3]}": sum(v) / len(v) for k, v in kinds.items()},
