@@ -1643,9 +1643,12 @@ __global__ void validate_kernel(int K, int stride, const int* __restrict__ pair_
 // FP64 direct sum of a queued (leaf, cell) pair at every target of the leaf,
 // added to the outputs: blockIdx.x = the queued pair, blockIdx.y = one of
 // gridDim.y slices of the cell's particles (so a few large cells still fill
-// the GPU); per target, the threads stride over the slice and the CTA reduces
-// in a fixed order before one atomic add per output component.
+// the GPU), each slice at least kFallbackMinSlice particles (the surplus
+// CTAs of a small cell return at once).  Each warp takes whole targets: its
+// lanes stride over the slice, reduce by shuffles and add one atomic per
+// output component, with no block-wide barrier per target.
 constexpr int kFallbackThreads = 256;
+constexpr int kFallbackMinSlice = 128;
 template <int MODE, int KERNEL>
 __global__ void __launch_bounds__(kFallbackThreads) fallback_kernel(
     const int2* __restrict__ fallback, const int* __restrict__ n_fallback,
@@ -1661,17 +1664,18 @@ __global__ void __launch_bounds__(kFallbackThreads) fallback_kernel(
   constexpr bool NEED_FPR = ModeInfo<MODE>::need_fpr;
   constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
   constexpr double kC = -0.07957747154594767;
-  __shared__ double red[kFallbackThreads / 32][NC];
   if (static_cast<int>(blockIdx.x) >= *n_fallback) return;
   const int2 pr = fallback[blockIdx.x];
   const int t0 = leaf_start[pr.x], nt = leaf_count[pr.x];
   const int c0 = cell_start[pr.y], cn = cell_count[pr.y];
-  const int per = (cn + gridDim.y - 1) / gridDim.y;
-  const int s0 = c0 + static_cast<int>(blockIdx.y) * per;
-  const int ns = max(0, min(per, c0 + cn - s0));
-  if (ns == 0) return;
+  const int per = max(kFallbackMinSlice, (cn + static_cast<int>(gridDim.y) - 1) /
+                                             static_cast<int>(gridDim.y));
+  const int64_t s0_64 = c0 + static_cast<int64_t>(blockIdx.y) * per;
+  if (s0_64 >= c0 + cn) return;
+  const int s0 = static_cast<int>(s0_64);
+  const int ns = min(per, c0 + cn - s0);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int ti = 0; ti < nt; ++ti) {
+  for (int ti = wid; ti < nt; ti += kFallbackThreads / 32) {
     const int i = perm[t0 + ti];
     const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
     double gx = 0.0, gy = 0.0, gz = 0.0;
@@ -1683,7 +1687,7 @@ __global__ void __launch_bounds__(kFallbackThreads) fallback_kernel(
     double acc[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) acc[c] = 0.0;
-    for (int q = threadIdx.x; q < ns; q += blockDim.x) {
+    for (int q = lane; q < ns; q += 32) {
       const int j = perm[s0 + q];
       const double dx = x - pos[3 * j], dy = y - pos[3 * j + 1], dz = z - pos[3 * j + 2];
       const double r2 = dx * dx + dy * dy + dz * dz;
@@ -1698,19 +1702,14 @@ __global__ void __launch_bounds__(kFallbackThreads) fallback_kernel(
 #pragma unroll
     for (int c = 0; c < NC; ++c)
       for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
-    if (lane == 0)
-      for (int c = 0; c < NC; ++c) red[wid][c] = acc[c];
-    __syncthreads();
-    if (threadIdx.x < NC) {
-      double v = 0.0;
-      for (int w = 0; w < kFallbackThreads / 32; ++w) v += red[w][threadIdx.x];
-      const int c = threadIdx.x;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      if (lane != c) continue;
       if (c < NA)
-        atomicAdd(out_a + static_cast<int64_t>(i) * NA + c, v);
+        atomicAdd(out_a + static_cast<int64_t>(i) * NA + c, acc[c]);
       else
-        atomicAdd(out_b + static_cast<int64_t>(i) * (NC - NA) + (c - NA), v);
+        atomicAdd(out_b + static_cast<int64_t>(i) * (NC - NA) + (c - NA), acc[c]);
     }
-    __syncthreads();
   }
 }
 
