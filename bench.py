@@ -62,6 +62,11 @@ L2P_FLOP = {"velocity": 90, "stretch": 80, "vorticity": 60}
 # tensor flop of the far-field network per (leaf, cell) pair: 2 x MACs of the
 # 48-128-128-128-32 layers
 MLP_FLOP_PER_PAIR = 2 * (48 * 128 + 128 * 128 + 128 * 128 + 128 * 32)
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the stretching
+# evaluation kernel on the 2^20-particle slab at this leaf target, from the ncu
+# capture summarised in ``source`` (which gives the command and the commit)
+EVAL_TRAFFIC = {"bytes": 1.3454e8, "leaf": 32,
+                "source": "profiles/eval_kernel_phased_tiles_slab_1e6_leaf32.md"}
 MODE_NAMES = {0: "velocity", 1: "stretch", 2: "velocity_stretch", 3: "jacobian", 4: "vorticity"}
 
 
@@ -103,6 +108,11 @@ def parse():
                    help="steps of the CL-history check against direct sweeps (0: off)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-baselines", action="store_true")
+    p.add_argument("--sweep-case", action="store_true",
+                   help="instead of the step: one treecode velocity + stretching sweep pair of "
+                        "the seeded slab (the profiling case of the evaluation and network "
+                        "kernels); --repeat R more pairs print median kernel times")
+    p.add_argument("--repeat", type=int, default=0)
     return p.parse_args()
 
 
@@ -115,11 +125,52 @@ def progress(msg):
 
 
 # ---------------------------------------------------------------------------
+CLOCK_QUERY = ("uuid,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def device_uuid(device):
+    """nvidia-smi's identifier ("GPU-<uuid>") of a CUDA device.  nvidia-smi
+    numbers GPUs in PCI order, whatever CUDA_VISIBLE_DEVICES says, so the
+    process-local CUDA ordinal cannot select the GPU's rows; its UUID can."""
+    import torch
+    u = getattr(torch.cuda.get_device_properties(device), "uuid", None)
+    if u is None:
+        return None
+    s = str(u)
+    return s if s.startswith("GPU-") else "GPU-" + s
+
+
+def parse_clock_samples(lines, gpu_uuid):
+    """Summary of nvidia-smi rows (``CLOCK_QUERY`` order, csv, no header, no
+    units) of the GPU whose UUID is ``gpu_uuid``: median SM clock under load,
+    the maximum clock, and every throttle reason seen active."""
+    sm, smax, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    want = (gpu_uuid or "").lower()
+    for line in lines:
+        parts = [x.strip() for x in line.split(",")]
+        if len(parts) < 10 or parts[0].lower() != want:
+            continue
+        try:
+            sm.append(float(parts[2]))
+            smax.append(float(parts[3]))
+        except ValueError:
+            continue
+        for nm, v in zip(names, parts[6:10]):
+            if v.lower() == "active":
+                reasons.add(nm)
+    if not sm:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+    loaded = [x for x in sm if x > 0.5 * max(sm)] or sm
+    return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax),
+            "reasons": sorted(reasons), "samples": len(sm), "gpu": gpu_uuid}
+
+
 def start_clock_sampler():
     path = tempfile.mktemp(prefix="clocks_", suffix=".csv")
-    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    q = CLOCK_QUERY
     try:
         f = open(path, "w")
         proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
@@ -134,7 +185,7 @@ def start_clock_sampler():
         return None, None, path
 
 
-def stop_clock_sampler(handle, gpu_index=0):
+def stop_clock_sampler(handle, gpu_uuid):
     proc, f, path = handle
     if proc is None:
         return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -144,26 +195,10 @@ def stop_clock_sampler(handle, gpu_index=0):
     except subprocess.TimeoutExpired:
         proc.kill()
     f.close()
-    sm, smax, reasons = [], [], set()
-    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-    for line in open(path):
-        parts = [x.strip() for x in line.split(",")]
-        if len(parts) < 9 or parts[0] != str(gpu_index):
-            continue
-        try:
-            sm.append(float(parts[1]))
-            smax.append(float(parts[2]))
-        except ValueError:
-            continue
-        for nm, v in zip(names, parts[5:9]):
-            if v.lower() == "active":
-                reasons.add(nm)
+    with open(path) as fh:
+        out = parse_clock_samples(fh.readlines(), gpu_uuid)
     os.unlink(path)
-    if not sm:
-        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-    loaded = [x for x in sm if x > 0.5 * max(sm)] or sm
-    return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax),
-            "reasons": sorted(reasons), "samples": len(sm)}
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -309,6 +344,54 @@ def flutter_sweep_measure(args):
     return out
 
 
+def run_sweep_case(args):
+    """One treecode self-sweep pair (velocity, then stretching) of the seeded
+    slab wake (``workloads.slab_wake``: uniform in a 20c x 10c x 2c slab,
+    sigma 0.02c) with the chosen far field and FP64 validation off: the
+    smallest complete invocation of the particle hot path, used as the
+    profiling case of the evaluation, translation and network kernels.
+    ``--repeat R`` runs R more sweep pairs at the same positions and prints the
+    median times of the evaluation kernel and of the local-expansion stage
+    (CUDA events inside the library)."""
+    import torch
+    from fluxvortex_gb300 import _capi
+    from fluxvortex_gb300.tree import TreeSweeper
+    from fluxvortex_gb300.workloads import slab_wake
+    ff = {"tree": "m2p", "direct": "m2p"}.get(args.far_field, args.far_field)
+    pos, gam, sig, _ = slab_wake(args.n)
+    d = lambda x: torch.as_tensor(x, dtype=torch.float64, device="cuda")  # noqa: E731
+    P, G, S = d(pos), d(gam), d(sig)
+    ts = TreeSweeper(theta=0.5, leaf_target=args.leaf)
+    mlp = None
+    if ff == "learned":
+        from fluxvortex_gb300.learned import FarFieldMLP
+        mlp = FarFieldMLP.load()
+    ts.set_far_field(ff, mlp=mlp)
+    ts.set_validation(0, 0.1)
+    out = torch.empty((args.n, 3), dtype=torch.float64, device="cuda")
+    ts.sweep(_capi.PAIR_VELOCITY, "winckelmans", P, G, S, args.n, out)
+    ts.sweep(_capi.PAIR_STRETCH, "winckelmans", P, G, S, args.n, out, tgt_gamma=G)
+    times = {"velocity": [], "stretch": []}
+    for _ in range(args.repeat):
+        for name, mode, tg in (("velocity", _capi.PAIR_VELOCITY, None),
+                               ("stretch", _capi.PAIR_STRETCH, G)):
+            ts.sweep(mode, "winckelmans", P, G, S, args.n, out, tgt_gamma=tg, check=True,
+                     same_positions=True)
+            loc = ts.last_local_ms() if ff != "m2p" else 0.0
+            times[name].append((ts.last_eval_ms(), loc))
+    torch.cuda.synchronize()
+    for name, t in times.items():
+        if t:
+            ev = sorted(x[0] for x in t)[len(t) // 2]
+            lo = sorted(x[1] for x in t)[len(t) // 2]
+            print(f"{name}: evaluation {ev:.3f} ms, local-expansion stage {lo:.3f} ms "
+                  f"(median of {len(t)})", file=sys.stderr)
+    st = _capi.status_read_and_clear()
+    print(f"sweep case ok: max |S| = {float(out.abs().max())}, status {st}", file=sys.stderr)
+    if st:
+        raise SystemExit(f"device status {st}")
+
+
 def max_over_ranks(value, world, device=None):
     """The largest of every rank's value (the job's time is its slowest rank's)."""
     import torch
@@ -409,7 +492,7 @@ def run_ours(args, rank, world):
         barrier()
         step_ms.append(s.elapsed_time(e))
     launches = lib.fvx_launch_count() - launches0
-    clk = stop_clock_sampler(clocks, local)
+    clk = stop_clock_sampler(clocks, device_uuid(device))
     events = step.field.sweep_events
     step.field.sweep_events = None
     ms = sum(step_ms) / len(step_ms)
@@ -432,9 +515,9 @@ def run_ours(args, rank, world):
         # with CUDA events around the launch inside the library
         tev = [e for e in step.field.tree_events if MODE_NAMES[e[0]] == mname]
         base = kern.split("/", 1)[1]
-        local = step.field.far_field in ("m2l", "learned")
+        has_local_exp = step.field.far_field in ("m2l", "learned")
         flop = sum(FLOP_PER_PAIR[(mname, base)] * e[2][6] + M2P_FLOP[mname] * e[2][7]
-                   + (L2P_FLOP[mname] * args.n if local else 0) for e in tev) / len(tev)
+                   + (L2P_FLOP[mname] * args.n if has_local_exp else 0) for e in tev) / len(tev)
         avg_ms = sum(e[3] for e in tev) / len(tev)
         kname = f"tree eval_kernel<{mname},{base}>"
         tree_stats = {"levels": int(tev[-1][2][0]), "leaves": int(tev[-1][2][1]),
@@ -448,13 +531,12 @@ def run_ours(args, rank, world):
             tree_stats["validation_per_step"] = vals[-1]
     achieved = flop / (avg_ms * 1e-3) / 1e12
     # DRAM bytes per launch of the stretching evaluation from one ncu capture
-    # (dram__bytes_read.sum + dram__bytes_write.sum = 109.9 + 24.6 MB) of the
-    # same kernel on 2^20 slab particles, leaf target 32; reported only for the
-    # workload that capture matches
-    traffic = None
+    # of the same kernel on the same workload (EVAL_TRAFFIC names the capture's
+    # summary); reported only for the workload that capture matches
+    traffic, traffic_source = None, None
     if (kname == "tree eval_kernel<stretch,winckelmans>" and args.n == 1 << 20
-            and args.leaf == 32 and args.precision == "f32c"):
-        traffic = 1.3454e8
+            and args.leaf == EVAL_TRAFFIC["leaf"] and args.precision == "f32c"):
+        traffic, traffic_source = EVAL_TRAFFIC["bytes"], EVAL_TRAFFIC["source"]
 
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -475,6 +557,7 @@ def run_ours(args, rank, world):
                      "achieved": achieved, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / (fp32_peak / 1e12), "traffic": traffic,
                      "traffic_unit": "bytes per launch (ncu capture)",
+                     "traffic_source": traffic_source,
                      "flop_per_launch": flop, "avg_launch_ms": avg_ms,
                      "peak_source": "measured FP32 FMA probe (fvx_probe_fp32_fma) on this GPU"},
         "sweep_ms": {f"{k[0]}/{k[1]}/{k[2]}x{k[3]}": sum(v) / len(v) for k, v in kinds.items()},
@@ -599,7 +682,9 @@ def main():
         backend = "gloo" if args.impl == "reference" else "nccl"
         dist.init_process_group(backend)
     try:
-        if args.impl == "reference":
+        if args.sweep_case:
+            run_sweep_case(args)
+        elif args.impl == "reference":
             run_reference(args, rank, world)
         else:
             run_ours(args, rank, world)

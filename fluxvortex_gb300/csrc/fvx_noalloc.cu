@@ -68,6 +68,12 @@ extern "C" int fvx_segments_collapsed_noalloc(const double* points, int64_t n_po
                                               const double* ages, double nu, int64_t n_vortices,
                                               int leg_set, double* out,
                                               int64_t* singularity_counts, void* stream) {
+  // Bad arguments are reported as such, before the size check can mistake
+  // them for a capacity problem.
+  FVX_ARG_CHECK(leg_set == FVX_LEGS_RING || leg_set == FVX_LEGS_CHORDWISE ||
+                    leg_set == FVX_LEGS_HORSESHOE,
+                "unknown leg set %d", leg_set);
+  FVX_ARG_CHECK(n_points >= 0 && n_vortices >= 0, "negative size");
   const size_t need = fvx::segments_collapsed_scratch(n_points, n_vortices);
   if (need > fvx::kScratchBytes) {
     fvx::set_last_error(

@@ -337,7 +337,9 @@ def make_population(ref_root):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the FLUXVortex reference tree>")
+    root = sys.argv[1]
     make_segments(root)
     make_particles(root)
     make_beam(root)

@@ -70,16 +70,28 @@ def test_no_alloc_matches_scratch_entry_on_two_calls(cuda, N, M):
         assert torch.equal(cnt, ref_cnt)
 
 
+def _oversize_points(lib, M):
+    """A target count whose partial sums exceed the limit on this device, or
+    None.  The scratch is 24 bytes x points x splits, and the split count
+    depends on the SM count, so every launch width is tried (host-side query,
+    128 points per CTA, up to the width at which one split fills the GPU)."""
+    for gx in range(1, 4097):
+        n = 128 * gx
+        nb = lib.fvx_segments_collapsed_scratch_bytes(n, M, _capi.LEGS_RING)
+        if nb > CAPACITY:
+            return n
+        if nb == 0:          # one split already fills the GPU: no scratch beyond here
+            return None
+    return None
+
+
 def test_no_alloc_rejects_problems_beyond_its_scratch(cuda):
     import torch
     lib = _capi.load()
-    # find a size whose partial sums exceed the 1 MiB limit (host-side query)
-    N, M = None, 200000
-    for n in range(4000, 40000, 500):
-        if lib.fvx_segments_collapsed_scratch_bytes(n, M, _capi.LEGS_RING) > CAPACITY:
-            N = n
-            break
-    assert N is not None
+    M = 200000
+    N = _oversize_points(lib, M)
+    if N is None:
+        pytest.skip("no problem size needs more than the fixed scratch on this device")
     P, V, s, rc, ages = _inputs(torch, cuda, N, M, seed=1)
     st, out, _ = _no_alloc(lib, torch, cuda, P, V, s, rc, ages, 0.0)
     assert st == _capi.FVX_ERR_CAPACITY
@@ -87,3 +99,20 @@ def test_no_alloc_rejects_problems_beyond_its_scratch(cuda):
     assert "scratch" in msg and "fvx_segments_collapsed" in msg
     torch.cuda.synchronize()
     assert torch.isnan(out).all()          # nothing was launched
+
+
+def test_no_alloc_reports_bad_arguments_before_capacity(cuda):
+    import torch
+    lib = _capi.load()
+    M = 200000
+    N = _oversize_points(lib, M) or 126
+    P, V, s, rc, ages = _inputs(torch, cuda, N, M, seed=2)
+    out = torch.full((N, 3), float("nan"), dtype=torch.float64, device=cuda)
+    st = lib.fvx_segments_collapsed_noalloc(
+        P.data_ptr(), N, *[v.data_ptr() for v in V], s.data_ptr(), rc.data_ptr(),
+        ages.data_ptr(), 0.0, M, 7, out.data_ptr(), None,
+        torch.cuda.current_stream(cuda).cuda_stream)
+    assert st == _capi.FVX_ERR_ARG
+    assert "leg set" in lib.fvx_last_error().decode()
+    torch.cuda.synchronize()
+    assert torch.isnan(out).all()
