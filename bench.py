@@ -53,7 +53,8 @@ FLOP_PER_PAIR = {
     ("stretch", "gaussianerf"): 67,
 }
 WORKLOAD = ("VPM+panel step: flapping NACA2412 wing + NACA0012 V-tail, 3 surfaces, 192 panels "
-            "+ {n} seeded wake particles, RK3 free wake with stretching")
+            "+ {n} seeded wake particles, RK3 free wake with stretching on, Pedrizzetti "
+            "relaxation off")
 # Algorithmic flop of one far-field (target particle, cell) evaluation of the
 # treecode's quadrupole expansion (same counting convention).
 M2P_FLOP = {"velocity": 166, "stretch": 355, "vorticity": 300}
@@ -104,9 +105,15 @@ def parse():
     p.add_argument("--leaf", type=int, default=32, help="treecode particles per leaf")
     p.add_argument("--no-flutter", dest="flutter", action="store_false",
                    help="skip the batched flutter-sweep measurement")
-    p.add_argument("--cl-steps", type=int, default=2,
-                   help="steps of the CL-history check against direct sweeps (0: off)")
-    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--cl-steps", type=int, default=43,
+                   help="steps of the CL-history check against direct sweeps (0: off; 43 = "
+                        "one flapping cycle)")
+    p.add_argument("--cl-particles", type=int, default=1 << 18,
+                   help="seeded particles of the CL-history check")
+    p.add_argument("--e2e-steps", type=int, default=5,
+                   help="steps of the end-to-end measurement (0: off)")
+    p.add_argument("--relax-steps", type=int, default=3,
+                   help="timed steps of the variant with the Pedrizzetti relaxation (0: off)")
     p.add_argument("--no-baselines", action="store_true")
     p.add_argument("--sweep-case", action="store_true",
                    help="instead of the step: one treecode velocity + stretching sweep pair of "
@@ -216,14 +223,15 @@ class Step:
     (CL, CDi), shedding, conversion, and one RK3 particle step with free wake
     and stretching (3 velocity + 3 stretching sweeps over all particles)."""
 
-    def __init__(self, n, precision, device, steps_hint=64, far_field="direct", leaf=64):
+    def __init__(self, n, precision, device, steps_hint=64, far_field="direct", leaf=64,
+                 rlxf=0.0):
         import torch
         from fluxvortex_gb300.geometry import flapping_aircraft
         from fluxvortex_gb300.hybrid import HybridStep
         from fluxvortex_gb300.workloads import AIRCRAFT_SLAB_X0, slab_wake
         pos, gam, sig, colloc = slab_wake(n, x0=AIRCRAFT_SLAB_X0)
         self.host = dict(pos=pos, gamma=gam, sigma=sig, colloc=colloc)
-        self.cfg = flapping_aircraft(n_keep=10, free_vpm=True, stretch=True, rlxf=0.0,
+        self.cfg = flapping_aircraft(n_keep=10, free_vpm=True, stretch=True, rlxf=rlxf,
                                      max_particles=n + 128 * (steps_hint + 8),
                                      far_field=None if far_field == "direct" else far_field)
         self.hs = HybridStep(self.cfg, precision=precision, device=device)
@@ -607,67 +615,114 @@ def run_ours(args, rank, world):
         progress("flutter sweep")
         result["flutter_sweep"] = flutter_sweep_measure(args)
 
-    if args.cl_steps > 0 and rank == 0 and args.far_field != "direct":
-        # CL / CDi history of the benchmarked form against direct all-pairs
-        # sweeps (FP32 compensated, within ~1e-7 of FP64) from the same seeded
-        # initial state, step by step
-        del flush
-        torch.cuda.empty_cache()
-        hist = {}
-        for ff in (args.far_field, "direct"):
-            progress(f"CL history, far field {ff}")
-            st2 = Step(args.n, args.precision, device, far_field=ff, leaf=args.leaf)
-            for _ in range(args.cl_steps):
-                st2.run()
-            hist[ff] = (st2.hs.cl.copy(), st2.hs.cdi.copy())
-            del st2
-            torch.cuda.empty_cache()
-        ca, da = hist[args.far_field]
-        cb, db = hist["direct"]
-        result["cl_history_vs_direct"] = {
-            "steps": args.cl_steps, "cl_rel_err_max": float(max(abs(ca - cb) / abs(cb))),
-            "cdi_rel_err_max": float(max(abs(da - db) / abs(db))),
-            "cl": [float(x) for x in cb], "reference": "direct sweeps, FP32 compensated"}
-
-    if not args.no_e2e:
-        # End to end through the host-facing API: the particle state in from
-        # pinned host memory, the step, the new state and CL / CDi out.
+    if args.e2e_steps > 0:
+        # End to end through the host-facing API, every step: the particle
+        # state (positions, strengths, cores) in from pinned host memory, the
+        # step, the new state and CL / CDi back out; the host holds the state
+        # between steps, so each step continues from the last one's output.
         progress("end to end")
         step.hs.restore(snap)
         f = step.field
-        n = f.np
-        hp = torch.empty((n, 3), dtype=torch.float64).pin_memory()
-        hg = torch.empty((n, 3), dtype=torch.float64).pin_memory()
-        hs = torch.empty(n, dtype=torch.float64).pin_memory()
-        hc = torch.empty(2, dtype=torch.float64).pin_memory()
-        hp.copy_(f._pos[:n])
-        hg.copy_(f._gamma[:n])
-        hs.copy_(f._sigma[:n])
+        n0 = f.np
+        cap = n0 + 128 * (args.e2e_steps + 1)
+        hp = torch.empty((cap, 3), dtype=torch.float64).pin_memory()
+        hg = torch.empty((cap, 3), dtype=torch.float64).pin_memory()
+        hs = torch.empty(cap, dtype=torch.float64).pin_memory()
+        hc = torch.empty((args.e2e_steps, 2), dtype=torch.float64).pin_memory()
+        hp[:n0].copy_(f._pos[:n0])
+        hg[:n0].copy_(f._gamma[:n0])
+        hs[:n0].copy_(f._sigma[:n0])
         torch.cuda.synchronize()
-        e2e_steps = 1
+        h2d = d2h = 0
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         barrier()
         s.record()
-        for _ in range(e2e_steps):
-            f._pos[:n].copy_(hp, non_blocking=True)
-            f._gamma[:n].copy_(hg, non_blocking=True)
-            f._sigma[:n].copy_(hs, non_blocking=True)
+        for k in range(args.e2e_steps):
+            n = f.np
+            f._pos[:n].copy_(hp[:n], non_blocking=True)
+            f._gamma[:n].copy_(hg[:n], non_blocking=True)
+            f._sigma[:n].copy_(hs[:n], non_blocking=True)
+            h2d += n * 7 * 8
             f.positions_changed()
             step.run()
             m = f.np
             kk = step.hs.k - 1
-            hp[:n].copy_(f._pos[:n], non_blocking=True)
-            hg[:n].copy_(f._gamma[:n], non_blocking=True)
-            hs[:n].copy_(f._sigma[:n], non_blocking=True)
-            hc[0:1].copy_(step.hs._cl[kk:kk + 1], non_blocking=True)
-            hc[1:2].copy_(step.hs._cdi[kk:kk + 1], non_blocking=True)
+            hp[:m].copy_(f._pos[:m], non_blocking=True)
+            hg[:m].copy_(f._gamma[:m], non_blocking=True)
+            hs[:m].copy_(f._sigma[:m], non_blocking=True)
+            hc[k, 0:1].copy_(step.hs._cl[kk:kk + 1], non_blocking=True)
+            hc[k, 1:2].copy_(step.hs._cdi[kk:kk + 1], non_blocking=True)
+            d2h += m * 7 * 8 + 16
         e.record()
         torch.cuda.synchronize()
-        e2e_ms = max_over_ranks(s.elapsed_time(e) / e2e_steps, world, device)
-        h2d = n * (3 + 3 + 1) * 8
-        d2h = n * (3 + 3 + 1) * 8 + 2 * 8
+        e2e_ms = max_over_ranks(s.elapsed_time(e) / args.e2e_steps, world, device)
         result["e2e"] = {"value": world * 1e3 / e2e_ms, "unit": UNIT,
-                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+                         "h2d_bytes_per_step": h2d // args.e2e_steps,
+                         "d2h_bytes_per_step": d2h // args.e2e_steps,
+                         "steps": args.e2e_steps, "ms_per_step": e2e_ms}
+
+    if args.relax_steps > 0 and rank == 0:
+        # the reference's hybrid solver runs the Pedrizzetti relaxation with
+        # rlxf = 0.3 (one more self-sweep per step, the Gaussian-erf vorticity);
+        # the same step with it on, timed alike
+        del step
+        torch.cuda.empty_cache()
+        progress("relaxation variant")
+        st3 = Step(args.n, args.precision, device, far_field=args.far_field, leaf=args.leaf,
+                   rlxf=0.3)
+        for _ in range(args.warmup):
+            st3.run()
+        snap3 = st3.hs.snapshot()
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+        ms3 = []
+        for _ in range(args.relax_steps):
+            st3.hs.restore(snap3)
+            flush.zero_()
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            st3.run()
+            e.record()
+            torch.cuda.synchronize()
+            ms3.append(s.elapsed_time(e))
+        result["relaxation_variant"] = {
+            "rlxf": 0.3, "ms_per_step": sum(ms3) / len(ms3),
+            "steps_per_s": 1e3 * len(ms3) / sum(ms3), "steps": len(ms3),
+            "note": "the benchmarked step plus the reference's Pedrizzetti relaxation "
+                    "(a Gaussian-erf vorticity self-sweep and the strength update)"}
+        del st3, flush
+        torch.cuda.empty_cache()
+
+    if args.cl_steps > 0 and rank == 0 and args.far_field != "direct":
+        # CL / CDi history of the benchmarked form against direct all-pairs
+        # sweeps (FP32 compensated, within ~1e-7 of FP64) from the same seeded
+        # initial state, step by step, over one flapping cycle (43 steps) at
+        # --cl-particles (the direct sweeps' N^2 cost bounds the size)
+        torch.cuda.empty_cache()
+        hist = {}
+        ncl = args.cl_particles
+        for ff in (args.far_field, "direct"):
+            progress(f"CL history, far field {ff}, {ncl} particles")
+            st2 = Step(ncl, args.precision, device, far_field=ff, leaf=args.leaf,
+                       steps_hint=args.cl_steps)
+            for _ in range(args.cl_steps):
+                st2.run()
+            hist[ff] = (st2.hs.cl.copy(), st2.hs.cdi.copy(), st2.field.np)
+            del st2
+            torch.cuda.empty_cache()
+        ca, da, na = hist[args.far_field]
+        cb, db, nb = hist["direct"]
+        result["cl_history_vs_direct"] = {
+            "steps": args.cl_steps, "particles_seeded": ncl, "particles_final": int(nb),
+            "cl_err_max_over_max": float(abs(ca - cb).max() / abs(cb).max()),
+            "cdi_err_max_over_max": float(abs(da - db).max() / abs(db).max()),
+            "cl_abs_err_max": float(abs(ca - cb).max()),
+            "cdi_abs_err_max": float(abs(da - db).max()),
+            "convention": "max_k |x_k - ref_k| / max_k |ref_k| over the history (the "
+                          "flapping CL crosses zero, so a per-step ratio is undefined there)",
+            "cl": [float(x) for x in cb], "cdi": [float(x) for x in db],
+            "reference": "direct all-pairs sweeps, FP32 compensated (within 1e-7 of FP64), "
+                         "same seeded state"}
 
     if rank == 0:
         print(json.dumps(result))

@@ -61,6 +61,7 @@ SIGNATURES = {
     "fvx_tree_hint_same_positions": (I32, [P]),
     "fvx_tree_set_list_slots": (I32, [P, I32, I32, I32]),
     "fvx_tree_last_validation": (I32, [P, P]),
+    "fvx_tree_last_judge": (I32, [P, P, I32]),
     "fvx_tree_sample_pairs": (I32, [P, I32, I32, P, P, P, P, P]),
     "fvx_mlp_forward": (I32, [P, I32, P, P, P, P, P, P]),
     "fvx_mlp_gemm": (I32, [P, I32, I32, P, I32, I32, P, I32, I32, I32, I32, I32, I32, P]),

@@ -27,6 +27,33 @@ struct FarPairs {
   int n;                     // pairs
 };
 
+// What the FP64 judge decided for each class of local-expansion pairs (see
+// fvx_tree.cu, judge_class): the translation and network kernels read a
+// pair's class from `cls` (row index over list 0, then list 1) and its action
+// from `act`: 0 = analytic translation + network residual, 1 = analytic
+// translation alone (the network is dropped for the class), 2 = no expansion
+// -- the translation kernel queues the pair, (target | list << 30, cell), in
+// `fb` for the FP64 direct sum.  cls == nullptr: every pair takes action 0.
+constexpr int kJudgeClasses = 16;
+struct FarJudge {
+  const uint8_t* cls = nullptr;
+  const uint8_t* act = nullptr;  // [kJudgeClasses]
+  int2* fb = nullptr;
+  int* nfb = nullptr;
+  int fb_cap = 0;
+};
+
+// The judge's stratified sample of local-expansion pairs: per list (0: the
+// leaves' own pairs, 1: the pairs shared through parents of leaves) `cap`
+// slots, of which the first cnt[list] are used.
+struct JudgeSampleView {
+  const int* cnt;            // [2] samples per list (device)
+  int cap;                   // slots per list
+  const int* cell[2];        // source cell of each sample
+  const uint32_t* key[2];    // Morton key of its target
+  float h[2];                // target size of each list
+};
+
 // Thread-local error message of the last failing C-ABI call.
 void set_last_error(const char* fmt, ...);
 

@@ -48,7 +48,7 @@ struct Smem {
   double Vind[2 * kMaxP][3];
   double W[kMaxRows + 1][kMaxNS + 1][3];
   double wgam[kMaxRows][kMaxNS], wage[kMaxRows];
-  double d[kMaxDof], v[kMaxDof], a[kMaxDof], F[kMaxDof], feff[kMaxDof];
+  double d[kMaxDof], v[kMaxDof], a[kMaxDof], F[kMaxDof], feff[kMaxDof], gd[kMaxDof];
   double tile[kTile][8];  // staged particles: x y z | a' (C-scaled) | sigma^2, 2.5 sigma^2
   double red[8];
   int piv;
@@ -139,6 +139,91 @@ __device__ void build_lattice(Smem& S, const FlutterParams& p) {
     S.area[k] = 0.5 * nrm;
     seg::prep_vortex<FVX_LEGS_RING>(S.bound[k], br, fr, fl, bl, 1.0, p.rc0, 0.0, p.nu);
   }
+}
+
+// The reference's panel deformation (coupling 1; aeroelastic_solver.py:150-221):
+// panel k of strip j moves with the heave w and twist th (nose-up) of the
+// displacements S.gd interpolated at the strip's collocation span station; its
+// corners and ring vertices by dz = w - (x - x_ea) sin th, dx = (x - x_ea)
+// (cos th - 1), its collocation point by dz only.  Normal and area from the
+// moved corners; no motion velocity.
+__device__ __forceinline__ void ref_motion(const FlutterParams& p, const Smem& S, int j,
+                                           double& w, double& s, double& c1) {
+  const int n = p.station_node[j];
+  const double xi = p.station_xi[j];
+  w = S.gd[3 * n] * (1.0 - xi) + S.gd[3 * (n + 1)] * xi;
+  const double th = S.gd[3 * n + 2] * (1.0 - xi) + S.gd[3 * (n + 1) + 2] * xi;
+  s = sin(th);
+  c1 = cos(th) - 1.0;
+}
+__device__ __forceinline__ void ref_move(const FlutterParams& p, double w, double s, double c1,
+                                         double* q) {
+  const double xr = q[0] - p.x_ea;
+  q[0] += xr * c1;
+  q[2] += w - xr * s;
+}
+__device__ void build_lattice_reference(Smem& S, const FlutterParams& p) {
+  const int P = p.nc * p.ns, s1 = p.ns + 1;
+  const double(*B)[3] = reinterpret_cast<const double(*)[3]>(p.base_verts);
+  for (int k = threadIdx.x; k < P; k += blockDim.x) {
+    const int i = k / p.ns, j = k % p.ns;
+    double w, sn, c1;
+    ref_motion(p, S, j, w, sn, c1);
+    double fl[3], fr[3], br[3], bl[3], v00[3], v01[3], v10[3], v11[3];
+    quarter(B, p.nc, p.ns, i, j, fl);
+    quarter(B, p.nc, p.ns, i, j + 1, fr);
+    quarter(B, p.nc, p.ns, i + 1, j + 1, br);
+    quarter(B, p.nc, p.ns, i + 1, j, bl);
+    for (int c = 0; c < 3; ++c) {
+      v00[c] = B[i * s1 + j][c];
+      v01[c] = B[i * s1 + j + 1][c];
+      v10[c] = B[(i + 1) * s1 + j][c];
+      v11[c] = B[(i + 1) * s1 + j + 1][c];
+      const double c0 = v00[c] + 0.75 * (v10[c] - v00[c]);
+      const double c1b = v01[c] + 0.75 * (v11[c] - v01[c]);
+      S.colloc[k][c] = 0.5 * (c0 + c1b);
+    }
+    S.colloc[k][2] += w - (S.colloc[k][0] - p.x_ea) * sn;
+    ref_move(p, w, sn, c1, fl);
+    ref_move(p, w, sn, c1, fr);
+    ref_move(p, w, sn, c1, br);
+    ref_move(p, w, sn, c1, bl);
+    ref_move(p, w, sn, c1, v00);
+    ref_move(p, w, sn, c1, v01);
+    ref_move(p, w, sn, c1, v10);
+    ref_move(p, w, sn, c1, v11);
+    double d1[3], d2[3];
+    for (int c = 0; c < 3; ++c) {
+      S.vcol[k][c] = 0.0;
+      S.vleg[k][c] = 0.0;
+      S.legc[k][c] = 0.5 * (fr[c] + fl[c]);
+      S.legv[k][c] = fl[c] - fr[c];
+      d1[c] = v11[c] - v00[c];
+      d2[c] = v01[c] - v10[c];
+    }
+    const double cx = d1[1] * d2[2] - d1[2] * d2[1];
+    const double cy = d1[2] * d2[0] - d1[0] * d2[2];
+    const double cz = d1[0] * d2[1] - d1[1] * d2[0];
+    const double nrm = sqrt(cx * cx + cy * cy + cz * cz);
+    S.normal[k][0] = cx / nrm;
+    S.normal[k][1] = cy / nrm;
+    S.normal[k][2] = cz / nrm;
+    S.area[k] = 0.5 * nrm;
+    seg::prep_vortex<FVX_LEGS_RING>(S.bound[k], br, fr, fl, bl, 1.0, p.rc0, 0.0, p.nu);
+  }
+}
+
+// The reference's trailing edge for the wake's new row (coupling 1): the back
+// vertices of the last chordwise rings, strip k's back-left one and the last
+// strip's back-right one, each moved with its strip's deformation.
+__device__ void trailing_edge_reference(const Smem& S, const FlutterParams& p, double* out,
+                                        int k) {
+  const double(*B)[3] = reinterpret_cast<const double(*)[3]>(p.base_verts);
+  const int j = k < p.ns ? k : p.ns - 1;
+  double w, sn, c1;
+  ref_motion(p, S, j, w, sn, c1);
+  quarter(B, p.nc, p.ns, p.nc, k, out);
+  ref_move(p, w, sn, c1, out);
 }
 
 // One wake ring at point p in FP32 on offsets taken in FP64 (the ring-vortex
@@ -368,10 +453,12 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
   const double ux = p.u_inf[3 * env], uy = p.u_inf[3 * env + 1], uz = p.u_inf[3 * env + 2];
   const double dt = p.dt;
   // load state
+  const bool ref = p.coupling == 1;
   for (int k = threadIdx.x; k < ndof; k += blockDim.x) {
     S.d[k] = st.d[env * ndof + k];
     S.v[k] = st.v[env * ndof + k];
     S.a[k] = st.a[env * ndof + k];
+    S.gd[k] = ref ? st.gd[env * ndof + k] : 0.0;
   }
   int R = st.nrows[env];
   for (int k = threadIdx.x; k < (R + 1) * s1 * 3; k += blockDim.x)
@@ -387,9 +474,13 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
   bool ok = true;
   for (; step < last && ok; ++step) {
     // 1. geometry and lattice
-    deform(S, p);
-    __syncthreads();
-    build_lattice(S, p);
+    if (ref) {
+      build_lattice_reference(S, p);
+    } else {
+      deform(S, p);
+      __syncthreads();
+      build_lattice(S, p);
+    }
     for (int k = threadIdx.x; k < R * p.ns; k += blockDim.x) {
       const int r = k / p.ns, j = k % p.ns;
       seg::prep_vortex<FVX_LEGS_RING>(S.wake[k], S.W[r + 1][j + 1], S.W[r][j + 1], S.W[r][j],
@@ -438,12 +529,18 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
       const double dg = has_prev ? (S.gam[k] - S.gprev[k]) / dt : 0.0;
       const double* l = S.legv[k];
       const double cz = Vx * l[1] - Vy * l[0];
-      Fz[k] = p.rho * geff * cz - p.rho * dg * S.area[k] * S.normal[k][2];
-      arm[k] = p.x_ea - S.legc[k][0];
+      const double fz = p.rho * geff * cz - p.rho * dg * S.area[k] * S.normal[k][2];
+      // physical: torque about the elastic axis with the bound leg's arm;
+      // reference: the lift's moment about x = 0 with the collocation
+      // point's arm (nose-up: -x_c F_z)
+      Fz[k] = fz;
+      arm[k] = ref ? -S.colloc[k][0] : p.x_ea - S.legc[k][0];
     }
     __syncthreads();
+    // the reference couples from step 1 to the step before the last
+    const bool couple = !ref || (step >= 1 && step < p.n_steps[env] - 1);
     // 6. station loads -> nodal forces (one thread, fixed order)
-    if (threadIdx.x == 0) {
+    if (couple && threadIdx.x == 0) {
       for (int k = 0; k < ndof; ++k) S.F[k] = 0.0;
       for (int j = 0; j < p.ns; ++j) {
         double lift = 0.0, torque = 0.0;
@@ -462,7 +559,7 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
     const double b = p.beta, g = p.gamma;
     const double a0 = 1.0 / (b * dt * dt), a1 = 1.0 / (b * dt), a2 = 1.0 / (2.0 * b) - 1.0;
     const double a3 = g / (b * dt), a4 = g / b - 1.0, a5 = dt * (g / (2.0 * b) - 1.0);
-    for (int r = threadIdx.x; r < nf; r += blockDim.x) {
+    for (int r = threadIdx.x; r < nf && couple; r += blockDim.x) {
       double fm = 0.0, fc = 0.0;
       for (int c = 0; c < nf; ++c) {
         const double dc = S.d[3 + c], vc = S.v[3 + c], ac = S.a[3 + c];
@@ -473,25 +570,37 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
     }
     __syncthreads();
     double dn = 0.0, an = 0.0, vn = 0.0;
-    for (int r = threadIdx.x; r < nf; r += blockDim.x) {
+    for (int r = threadIdx.x; r < nf && couple; r += blockDim.x) {
       for (int c = 0; c < nf; ++c) dn += p.kinv[r * nf + c] * S.feff[c];
       const double d0 = S.d[3 + r], v0 = S.v[3 + r], acc0 = S.a[3 + r];
       an = a0 * (dn - d0) - a1 * v0 - a2 * acc0;
       vn = v0 + dt * ((1.0 - g) * acc0 + g * an);
     }
     __syncthreads();
-    if (threadIdx.x < nf) {
+    if (couple && threadIdx.x < nf) {
       S.d[3 + threadIdx.x] = dn;
       S.v[3 + threadIdx.x] = vn;
       S.a[3 + threadIdx.x] = an;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      st.hist_w[static_cast<int64_t>(env) * p.max_steps + step] = S.d[ndof - 3];
-      st.hist_th[static_cast<int64_t>(env) * p.max_steps + step] = S.d[ndof - 1];
+    if (couple && threadIdx.x == 0) {
+      const int h = ref ? step - 1 : step;
+      st.hist_w[static_cast<int64_t>(env) * p.max_steps + h] = S.d[ndof - 3];
+      st.hist_th[static_cast<int64_t>(env) * p.max_steps + h] = S.d[ndof - 1];
     }
+    if (couple && st.hist_nodes != nullptr) {
+      const int h = ref ? step - 1 : step;
+      double* hn = st.hist_nodes + (static_cast<int64_t>(env) * p.max_steps + h) * p.nnodes * 2;
+      for (int n = threadIdx.x; n < p.nnodes; n += blockDim.x) {
+        hn[2 * n] = S.d[3 * n];
+        hn[2 * n + 1] = S.d[3 * n + 2];
+      }
+    }
+    // the coupling's displacements shape the next step (reference)
+    if (ref && couple)
+      for (int k = threadIdx.x; k < ndof; k += blockDim.x) S.gd[k] = S.d[k];
     // 8. wake: next geometry's trailing edge, convect rows and particles
-    deform(S, p);
+    if (!ref) deform(S, p);
     __syncthreads();
     const int Pm = p.max_particles;
     double* pp = st.ppos + static_cast<int64_t>(env) * Pm * 3;
@@ -517,8 +626,12 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
       if (threadIdx.x == 0) S.wage[r + 1] = S.wage[r] + dt;
       __syncthreads();
     }
-    for (int k = threadIdx.x; k < s1; k += blockDim.x)
-      quarter(S.verts, p.nc, p.ns, p.nc, k, S.W[0][k]);
+    for (int k = threadIdx.x; k < s1; k += blockDim.x) {
+      if (ref)
+        trailing_edge_reference(S, p, S.W[0][k], k);
+      else
+        quarter(S.verts, p.nc, p.ns, p.nc, k, S.W[0][k]);
+    }
     for (int k = threadIdx.x; k < p.ns; k += blockDim.x) S.wgam[0][k] = S.gam[(p.nc - 1) * p.ns + k];
     if (threadIdx.x == 0) S.wage[0] = 0.0;
     ++R;
@@ -585,6 +698,7 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
     st.d[env * ndof + k] = S.d[k];
     st.v[env * ndof + k] = S.v[k];
     st.a[env * ndof + k] = S.a[k];
+    if (ref) st.gd[env * ndof + k] = S.gd[k];
   }
   for (int k = threadIdx.x; k < (R + 1) * s1 * 3; k += blockDim.x)
     st.W[(static_cast<int64_t>(env) * (p.n_keep + 2)) * s1 * 3 + k] =
@@ -618,6 +732,8 @@ extern "C" int fvx_flutter_sweep(const FlutterParams* params, const FlutterState
   FVX_ARG_CHECK(3 * p.nnodes <= kMaxDof && p.nnodes >= 2, "beam too large");
   FVX_ARG_CHECK(p.max_particles >= 1 && p.max_steps >= 1, "bad capacities");
   FVX_ARG_CHECK(precision == FVX_PREC_F64 || precision == FVX_PREC_F32C, "bad precision");
+  FVX_ARG_CHECK(p.coupling == 0 || (p.coupling == 1 && state->gd != nullptr),
+                "coupling %d unknown (or its displacement array missing)", p.coupling);
   FVX_ARG_CHECK(threads >= 2 * P && threads <= 512 && threads % (2 * P) == 0 && threads % 32 == 0,
                 "threads must be a multiple of 2 x panels (and of 32), at most 512");
   FVX_ARG_CHECK((threads / (2 * P)) * 2 * P * 3 <= kMaxP * (kMaxP + 1),

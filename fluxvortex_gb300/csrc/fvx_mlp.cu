@@ -52,7 +52,7 @@ struct FwdSmem {
   __nv_bfloat16 act[kGroups][128 * H];
   float aux[kGroups][128][4];  // far field: the output scales m/d^2, m/d^3, m/d^4 of each row
   float bias[BN];
-  uint32_t hbias[3 * H / 2];  // F16 form: half the hidden layers' biases, packed F16 pairs
+  uint32_t hbias[3 * H / 2];  // inference form: half the hidden layers' biases, packed BF16 pairs
   uint64_t bar[kGroups];
   uint32_t tmem;
 };
@@ -67,17 +67,17 @@ __device__ __forceinline__ float silu(float z) {
   const float h = 0.5f * z;
   return fmaf(h, tanh_approx(h), h);
 }
-// Two SiLUs in packed F16 from two accumulator columns of the halved weights
+// Two SiLUs in packed BF16 from two accumulator columns of the halved weights
 // (acc = W x / 2) and the packed halved biases hb: h = z/2 = acc + b/2, then
-// one MUFU operation (tanh.approx.f16x2) and one packed FMA, h + h tanh(h) =
-// z sigmoid(z); the F16 result is the next layer's operand as it stands.
+// one MUFU operation (tanh.approx.bf16x2) and one packed FMA, h + h tanh(h) =
+// z sigmoid(z); the BF16 result is the next layer's operand as it stands.
 // Element 0 goes to the low half (the lower address in shared memory).
-__device__ __forceinline__ uint32_t silu_half2(float a0, float a1, uint32_t hb) {
+__device__ __forceinline__ uint32_t silu_bf16x2(float a0, float a1, uint32_t hb) {
   uint32_t h, t, s;
-  asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(a1), "f"(a0));
-  asm("add.rn.f16x2 %0, %1, %2;" : "=r"(h) : "r"(h), "r"(hb));
-  asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(h));
-  asm("fma.rn.f16x2 %0, %1, %2, %1;" : "=r"(s) : "r"(h), "r"(t));
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(a1), "f"(a0));
+  asm("add.rn.bf16x2 %0, %1, %2;" : "=r"(h) : "r"(h), "r"(hb));
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(h));
+  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(s) : "r"(h), "r"(t));
   return s;
 }
 __device__ __forceinline__ float silu_grad(float z) {
@@ -113,31 +113,21 @@ __device__ void stage_kmajor(__nv_bfloat16* dst, const __nv_bfloat16* src, int R
   }
 }
 
-// Eight BF16 values -> eight F16 values (round to nearest; every BF16 weight
-// of magnitude 6.1e-5 to 65504 is exact in F16, smaller ones keep an absolute
-// error below 3e-8).
-__device__ __forceinline__ uint4 bf16x8_to_f16x8(uint4 v, float scale = 1.f) {
-  const __nv_bfloat162* p = reinterpret_cast<const __nv_bfloat162*>(&v);
-  uint4 o;
-  __half2* q = reinterpret_cast<__half2*>(&o);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const float2 f = __bfloat1622float2(p[i]);
-    q[i] = __floats2half2_rn(f.x * scale, f.y * scale);
-  }
-  return o;
-}
-
-// As stage_kmajor, converting the BF16 matrix to F16 times `scale` (a power
-// of two: exact unless the product is an F16 subnormal) on the way.
-__device__ void stage_kmajor_f16(__nv_bfloat16* dst, const __nv_bfloat16* src, int R, int K,
-                                 float scale) {
+// As stage_kmajor, times `scale` (a power of two: exact in BF16, whose
+// exponent range is FP32's) on the way.
+__device__ void stage_kmajor_scaled(__nv_bfloat16* dst, const __nv_bfloat16* src, int R, int K,
+                                    float scale) {
   const int chunks = R * (K / 8);
   for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
     const int r = c / (K / 8), k8 = c % (K / 8);
-    const uint4 v = *reinterpret_cast<const uint4*>(src + static_cast<int64_t>(r) * K + 8 * k8);
-    *reinterpret_cast<uint4*>(reinterpret_cast<char*>(dst) + tc::kmajor_offset(r, 8 * k8, K)) =
-        bf16x8_to_f16x8(v, scale);
+    uint4 v = *reinterpret_cast<const uint4*>(src + static_cast<int64_t>(r) * K + 8 * k8);
+    __nv_bfloat162* p = reinterpret_cast<__nv_bfloat162*>(&v);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float2 f = __bfloat1622float2(p[i]);
+      p[i] = __floats2bfloat162_rn(f.x * scale, f.y * scale);
+    }
+    *reinterpret_cast<uint4*>(reinterpret_cast<char*>(dst) + tc::kmajor_offset(r, 8 * k8, K)) = v;
   }
 }
 
@@ -276,6 +266,7 @@ struct RowsIO {
 struct FarIO {
   FarPairs l0, l1;
   const float* rec;  // cell records
+  FarJudge judge;    // per-class actions of the FP64 judge (none by default)
 };
 
 template <bool FAR>
@@ -313,26 +304,26 @@ __device__ void epilogue_hidden(uint32_t tmem, int row, const float* bias, __nv_
   }
 }
 
-// Inference form of epilogue_hidden: F16 activations.  The layer's weights
-// are halved (acc = z/2 - b/2) and hbias holds its halved biases as packed F16
-// pairs, so each pair of columns is one silu_half2.
+// Inference form of epilogue_hidden: packed BF16 arithmetic.  The layer's
+// weights are halved (acc = z/2 - b/2) and hbias holds its halved biases as
+// packed BF16 pairs, so each pair of columns is one silu_bf16x2.
 // The TMEM loads are double-buffered: the next 16 columns load while the
 // current ones are processed.
-__device__ __forceinline__ void silu_chunk_f16(const uint32_t (&r)[16], const uint32_t* hbias,
-                                               char* base, int row, int c0) {
+__device__ __forceinline__ void silu_chunk_bf16(const uint32_t (&r)[16], const uint32_t* hbias,
+                                                char* base, int row, int c0) {
   __align__(16) uint32_t b[8];
   const uint4 h0 = *reinterpret_cast<const uint4*>(hbias + c0 / 2);
   const uint4 h1 = *reinterpret_cast<const uint4*>(hbias + c0 / 2 + 4);
   const uint32_t hb[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
 #pragma unroll
   for (int i = 0; i < 8; ++i)
-    b[i] = silu_half2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]), hb[i]);
+    b[i] = silu_bf16x2(__uint_as_float(r[2 * i]), __uint_as_float(r[2 * i + 1]), hb[i]);
   *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, c0, H)) =
       *reinterpret_cast<uint4*>(&b[0]);
   *reinterpret_cast<uint4*>(base + tc::kmajor_offset(row, c0 + 8, H)) =
       *reinterpret_cast<uint4*>(&b[4]);
 }
-__device__ void epilogue_hidden_f16(uint32_t tmem, int row, const uint32_t* hbias, void* act) {
+__device__ void epilogue_hidden_infer(uint32_t tmem, int row, const uint32_t* hbias, void* act) {
   const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * ((threadIdx.x >> 5) & 3)) << 16);
   char* base = reinterpret_cast<char*>(act);
   uint32_t ra[16], rb[16];
@@ -341,10 +332,10 @@ __device__ void epilogue_hidden_f16(uint32_t tmem, int row, const uint32_t* hbia
 #pragma unroll
   for (int c0 = 0; c0 < H; c0 += 32) {
     tc::tmem_ld16_issue(taddr + c0 + 16, rb);
-    silu_chunk_f16(ra, hbias, base, row, c0);
+    silu_chunk_bf16(ra, hbias, base, row, c0);
     tc::tmem_ld_wait(rb);
     if (c0 + 32 < H) tc::tmem_ld16_issue(taddr + c0 + 32, ra);
-    silu_chunk_f16(rb, hbias, base, row, c0 + 16);
+    silu_chunk_bf16(rb, hbias, base, row, c0 + 16);
     if (c0 + 32 < H) tc::tmem_ld_wait(ra);
   }
 }
@@ -378,11 +369,11 @@ __device__ __forceinline__ void group_handoff(int g) {
   tc::fence_after_sync();
 }
 
-// HALF: F16 operands and activations (weights converted while staged, the
-// packed SiLU of epilogue_hidden_f16) -- the inference form, always taken by
-// the treecode far field; the training forward (with stored pre-activations
-// and activations) keeps BF16, the type its backward GEMMs read.
-template <bool FAR, bool HALF>
+// INFER: the inference form -- BF16 operands, hidden weights and biases
+// halved while staged, the packed BF16 SiLU of epilogue_hidden_infer -- always
+// taken by the treecode far field; the training forward (with stored
+// pre-activations and activations) keeps the FP32 SiLU of epilogue_hidden.
+template <bool FAR, bool INFER>
 __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> A, int rows,
                                                            const __nv_bfloat16* __restrict__ W,
                                                            const float* __restrict__ bias) {
@@ -393,15 +384,15 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
     for (int g = 0; g < kGroups; ++g) mbar_init(&S.bar[g], 1);
     fence_mbar_init();
   }
-  static_assert(HALF || !FAR, "the far field runs the F16 form");
-  if constexpr (HALF) {
+  static_assert(INFER || !FAR, "the far field runs the inference form");
+  if constexpr (INFER) {
     // hidden layers halved: their accumulators are z/2, the tanh argument
-    stage_kmajor_f16(S.w1, W + W1o, H, IN, 0.5f);
-    stage_kmajor_f16(S.w2, W + W2o, H, H, 0.5f);
-    stage_kmajor_f16(S.w3, W + W3o, H, H, 0.5f);
-    stage_kmajor_f16(S.w4, W + W4o, OUT, H, 1.f);
+    stage_kmajor_scaled(S.w1, W + W1o, H, IN, 0.5f);
+    stage_kmajor_scaled(S.w2, W + W2o, H, H, 0.5f);
+    stage_kmajor_scaled(S.w3, W + W3o, H, H, 0.5f);
+    stage_kmajor(S.w4, W + W4o, OUT, H);
     for (int i = threadIdx.x; i < 3 * H / 2; i += blockDim.x) {
-      const __half2 hb = __floats2half2_rn(0.5f * bias[2 * i], 0.5f * bias[2 * i + 1]);
+      const __nv_bfloat162 hb = __floats2bfloat162_rn(0.5f * bias[2 * i], 0.5f * bias[2 * i + 1]);
       S.hbias[i] = *reinterpret_cast<const uint32_t*>(&hb);
     }
   } else {
@@ -430,6 +421,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
   // first MMA runs, the leaf key and the cell record while its third MMA
   // runs), so that the loads' latency leaves the tile's serial chain.
   int pf_leaf = 0, pf_cell = 0, pf_li = 0;
+  bool pf_keep = true;
   uint32_t pf_key = 0;
   RecRegs pf_rec;
   auto fetch_index = [&](int t) {
@@ -439,6 +431,8 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
       const int rr = pf_li ? r - A.f.l0.n : r;
       pf_leaf = (pf_li ? A.f.l1.pair_tgt : A.f.l0.pair_tgt)[rr];
       pf_cell = (pf_li ? A.f.l1.pair_cell : A.f.l0.pair_cell)[rr];
+      // the residual only for classes whose network the judge kept
+      pf_keep = A.f.judge.cls == nullptr || A.f.judge.act[A.f.judge.cls[r]] == 0;
     }
   };
   auto fetch_record = [&](int t) {
@@ -456,6 +450,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
     const int row = tile * 128 + lt;
     const bool act_row = row < rows;
     int leaf = 0, li = 0;
+    bool keep = true;
     // input tile (K = 48)
     {
       char* base = reinterpret_cast<char*>(act);
@@ -465,6 +460,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         if (act_row) {
           leaf = pf_leaf;
           li = pf_li;
+          keep = pf_keep;
           const float th = li ? A.f.l1.h : A.f.l0.h;
           const float3 cT = leaf_center(pf_key, th);
           const PairScale sc = pair_features(pf_rec.v, cT.x, cT.y, cT.z, th, f);
@@ -476,9 +472,10 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         }
 #pragma unroll
         for (int k8 = 0; k8 < IN / 8; ++k8) {
-          __align__(16) __half2 b[4];
+          __align__(16) __nv_bfloat162 b[4];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) b[q] = __floats2half2_rn(f[8 * k8 + 2 * q], f[8 * k8 + 2 * q + 1]);
+          for (int q = 0; q < 4; ++q)
+            b[q] = __floats2bfloat162_rn(f[8 * k8 + 2 * q], f[8 * k8 + 2 * q + 1]);
           *reinterpret_cast<uint4*>(base + tc::kmajor_offset(lt, 8 * k8, IN)) =
               *reinterpret_cast<uint4*>(b);
         }
@@ -487,7 +484,6 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
           uint4 v = make_uint4(0, 0, 0, 0);
           if (act_row)
             v = *reinterpret_cast<const uint4*>(A.r.X + static_cast<int64_t>(row) * IN + 8 * k8);
-          if constexpr (HALF) v = bf16x8_to_f16x8(v);
           *reinterpret_cast<uint4*>(base + tc::kmajor_offset(lt, 8 * k8, IN)) = v;
         }
       }
@@ -496,7 +492,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
       group_handoff(grp);
       if (lt == 0)
         tc::gemm_issue(tmem, act, l == 0 ? S.w1 : (l == 1 ? S.w2 : S.w3), l == 0 ? IN : H,
-                       HALF ? tc::idesc_f16(128, H) : tc::idesc_bf16(128, H), false, bar, 0);
+                       tc::idesc_bf16(128, H), false, bar, 0);
       if constexpr (FAR) {
         if (l == 0) fetch_index(tile + tile_step);
         if (l == 2) fetch_record(tile + tile_step);
@@ -511,16 +507,15 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         if (A.r.z_store && act_row) zo = A.r.z_store + (static_cast<int64_t>(l) * rows + row) * H;
         if (A.r.h_store && act_row) ho = A.r.h_store + (static_cast<int64_t>(l) * rows + row) * H;
       }
-      if constexpr (HALF)
-        epilogue_hidden_f16(tmem, lt, S.hbias + l * H / 2, act);
+      if constexpr (INFER)
+        epilogue_hidden_infer(tmem, lt, S.hbias + l * H / 2, act);
       else
         epilogue_hidden(tmem, lt, S.bias + l * H, act, zo, ho);
     }
     if (!ok) break;
     group_handoff(grp);
     if (lt == 0)
-      tc::gemm_issue(tmem, act, S.w4, H, HALF ? tc::idesc_f16(128, OUT) : tc::idesc_bf16(128, OUT),
-                     false, bar, 0);
+      tc::gemm_issue(tmem, act, S.w4, H, tc::idesc_bf16(128, OUT), false, bar, 0);
     if (!group_wait_mma(grp, bar, ph)) {
       ok = false;
       break;
@@ -537,7 +532,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         for (int i = 0; i < 16; ++i) {
           const int c = c0 + i;
           const float sc = c < 3 ? ax[0] : (c < 12 ? ax[1] : ax[2]);
-          x[c] = (act_row && c < NOUT) ? (v[i] + S.bias[B4o + c]) * sc : 0.f;
+          x[c] = (act_row && keep && c < NOUT) ? (v[i] + S.bias[B4o + c]) * sc : 0.f;
         }
       }
       const int lane = threadIdx.x & 31;
@@ -609,29 +604,18 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
 // a few very large cells still spread over the GPU); threads stride over the
 // slice, warps then the CTA reduce in a fixed order, and each slice writes its
 // own partial sums (no atomics: the result does not depend on timing).
-__global__ void pair_sums_kernel(int npairs, int stride, const int* __restrict__ pair_leaf,
-                                 const int* __restrict__ pair_cell,
-                                 const uint32_t* __restrict__ tgt_key, float h_tgt,
-                                 const uint32_t* __restrict__ leaf_key,
-                                 const int* __restrict__ cell_start,
-                                 const int* __restrict__ cell_count,
-                                 const float4* __restrict__ sp, const float4* __restrict__ sa,
-                                 const int* __restrict__ leaf_of_particle, float h,
-                                 double* __restrict__ partial) {
-  const int pr = blockIdx.x;
-  const int lane = threadIdx.x & 31;
-  __shared__ double red[kTargetsThreads / 32][NOUT];
-  if (pr >= npairs) return;
-  const int t = pair_leaf[static_cast<int64_t>(pr) * stride],
-            g = pair_cell[static_cast<int64_t>(pr) * stride];
-  const float3 cT = leaf_center(tgt_key[t], h_tgt);
-  double acc[NOUT];
+// One slice [s0, s0 + n) of a source cell's particles summed at cT into
+// acc[30]: the singular field u, its gradient and its second derivatives, in
+// FP64 (positions from the FP32 records relative to each particle's leaf
+// centre, the centre differences exact).
+__device__ __forceinline__ void exact_expansion_slice(float3 cT, int s0, int n,
+                                                      const uint32_t* __restrict__ leaf_key,
+                                                      const float4* __restrict__ sp,
+                                                      const float4* __restrict__ sa,
+                                                      const int* __restrict__ leaf_of_particle,
+                                                      float h, double (&acc)[NOUT]) {
 #pragma unroll
   for (int q = 0; q < NOUT; ++q) acc[q] = 0.0;
-  const int c0 = cell_start[g], cn = cell_count[g];
-  const int per = (cn + gridDim.y - 1) / gridDim.y;
-  const int s0 = c0 + static_cast<int>(blockIdx.y) * per;
-  const int n = max(0, min(per, c0 + cn - s0));
   for (int i = s0 + static_cast<int>(threadIdx.x); i < s0 + n; i += blockDim.x) {
     const float3 cs = leaf_center(leaf_key[leaf_of_particle[i] - 1], h);
     const float4 p = sp[i];
@@ -659,6 +643,12 @@ __global__ void pair_sums_kernel(int npairs, int stride, const int* __restrict__
         }
     }
   }
+}
+
+// The CTA's sums of acc, warps then the CTA in a fixed order, to `out` (30).
+__device__ __forceinline__ void reduce_expansion(double (&acc)[NOUT], double* out) {
+  __shared__ double red[kTargetsThreads / 32][NOUT];
+  const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int q = 0; q < NOUT; ++q)
     for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
@@ -668,8 +658,60 @@ __global__ void pair_sums_kernel(int npairs, int stride, const int* __restrict__
   if (threadIdx.x < NOUT) {
     double v = 0.0;
     for (int w = 0; w < kTargetsThreads / 32; ++w) v += red[w][threadIdx.x];
-    partial[(static_cast<int64_t>(pr) * gridDim.y + blockIdx.y) * NOUT + threadIdx.x] = v;
+    out[threadIdx.x] = v;
   }
+}
+
+// FP64 direct sums over the source cell's particles of the singular
+// Biot-Savart field and its first two derivatives at c_T.  blockIdx.x = the
+// pair, blockIdx.y = one of gridDim.y slices of the cell's particles (so that
+// a few very large cells still spread over the GPU); threads stride over the
+// slice, warps then the CTA reduce in a fixed order, and each slice writes its
+// own partial sums (no atomics: the result does not depend on timing).
+__global__ void pair_sums_kernel(int npairs, int stride, const int* __restrict__ pair_leaf,
+                                 const int* __restrict__ pair_cell,
+                                 const uint32_t* __restrict__ tgt_key, float h_tgt,
+                                 const uint32_t* __restrict__ leaf_key,
+                                 const int* __restrict__ cell_start,
+                                 const int* __restrict__ cell_count,
+                                 const float4* __restrict__ sp, const float4* __restrict__ sa,
+                                 const int* __restrict__ leaf_of_particle, float h,
+                                 double* __restrict__ partial) {
+  const int pr = blockIdx.x;
+  if (pr >= npairs) return;
+  const int t = pair_leaf[static_cast<int64_t>(pr) * stride],
+            g = pair_cell[static_cast<int64_t>(pr) * stride];
+  const float3 cT = leaf_center(tgt_key[t], h_tgt);
+  const int c0 = cell_start[g], cn = cell_count[g];
+  const int per = (cn + gridDim.y - 1) / gridDim.y;
+  const int s0 = c0 + static_cast<int>(blockIdx.y) * per;
+  const int n = max(0, min(per, c0 + cn - s0));
+  double acc[NOUT];
+  exact_expansion_slice(cT, s0, n, leaf_key, sp, sa, leaf_of_particle, h, acc);
+  reduce_expansion(acc, partial + (static_cast<int64_t>(pr) * gridDim.y + blockIdx.y) * NOUT);
+}
+
+// The same sums for the FP64 judge's samples: slot x of 2 x cap (list 0's
+// samples, then list 1's, cap slots each; slots past a list's count idle).
+__global__ void judge_sums_kernel(JudgeSampleView S, const uint32_t* __restrict__ leaf_key,
+                                  const int* __restrict__ cell_start,
+                                  const int* __restrict__ cell_count,
+                                  const float4* __restrict__ sp, const float4* __restrict__ sa,
+                                  const int* __restrict__ leaf_of_particle, float h,
+                                  double* __restrict__ partial) {
+  const int slot = blockIdx.x;
+  const int li = slot >= S.cap ? 1 : 0;
+  const int q = slot - li * S.cap;
+  if (q >= S.cnt[li]) return;
+  const float3 cT = leaf_center(S.key[li][q], S.h[li]);
+  const int g = S.cell[li][q];
+  const int c0 = cell_start[g], cn = cell_count[g];
+  const int per = (cn + gridDim.y - 1) / gridDim.y;
+  const int s0 = c0 + static_cast<int>(blockIdx.y) * per;
+  const int n = max(0, min(per, c0 + cn - s0));
+  double acc[NOUT];
+  exact_expansion_slice(cT, s0, n, leaf_key, sp, sa, leaf_of_particle, h, acc);
+  reduce_expansion(acc, partial + (static_cast<int64_t>(slot) * gridDim.y + blockIdx.y) * NOUT);
 }
 
 // Per pair: the slices' sums in order, the features (BF16), the output scales,
@@ -733,18 +775,40 @@ __global__ void __launch_bounds__(kM2lThreads) m2l_pairs_kernel(FarIO F) {
     PairScale sc{0.f, 0.f, 0.f};
     int leaf = 0, li = 0;
     float* L = nullptr;
+    bool queue = false;
+    int cell = 0;
     if (act_row) {
       li = row >= F.l0.n ? 1 : 0;
       const int rr_ = li ? row - F.l0.n : row;
       const FarPairs& fl = li ? F.l1 : F.l0;
       leaf = fl.pair_tgt[rr_];
+      cell = fl.pair_cell[rr_];
       L = fl.local + static_cast<int64_t>(leaf) * OUT;
-      const float3 cT = leaf_center(fl.tgt_key[leaf], fl.h);
-      const RecRegs rr = load_record(F.rec + static_cast<int64_t>(fl.pair_cell[rr_]) * kRecFloats);
-      const PairGeom g = pair_geom(rr.v, cT.x, cT.y, cT.z);
-      const RecordMoments src{rr.v, g.Rx * g.id, g.Ry * g.id, g.Rz * g.id, g.hS * g.id, g.im, g.ih};
-      m2l_tensor(src, a);
-      sc = pair_scale(g);
+      // a class the judge sent to the FP64 direct sum: no expansion, queued
+      queue = F.judge.cls != nullptr && F.judge.act[F.judge.cls[row]] == 2;
+      if (!queue) {
+        const float3 cT = leaf_center(fl.tgt_key[leaf], fl.h);
+        const RecRegs rr = load_record(F.rec + static_cast<int64_t>(cell) * kRecFloats);
+        const PairGeom g = pair_geom(rr.v, cT.x, cT.y, cT.z);
+        const RecordMoments src{rr.v, g.Rx * g.id, g.Ry * g.id, g.Rz * g.id, g.hS * g.id, g.im,
+                                g.ih};
+        m2l_tensor(src, a);
+        sc = pair_scale(g);
+      }
+    }
+    const unsigned qm = __ballot_sync(0xffffffffu, queue);
+    if (qm) {
+      // one atomic per warp for its queued pairs
+      int base_q = 0;
+      if (lane == 0) base_q = atomicAdd(F.judge.nfb, __popc(qm));
+      base_q = __shfl_sync(0xffffffffu, base_q, 0);
+      if (queue) {
+        const int q = base_q + __popc(qm & ((1u << lane) - 1u));
+        if (q < F.judge.fb_cap)
+          F.judge.fb[q] = make_int2(leaf | (li << 30), cell);
+        else
+          flag_status(kStatusCapacity);
+      }
     }
     const int my = act_row ? (leaf | (li << 30)) : -1 - lane;  // unique across the lists
     float x[32];
@@ -991,7 +1055,7 @@ int set_smem(K kernel, size_t bytes) {
 // The learned far field of both lists in one launch: local expansions added
 // into a.local / b.local (zeroed by the caller).
 int mlp_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, const void* W,
-                        const float* bias, cudaStream_t s) {
+                        const float* bias, cudaStream_t s, const FarJudge& judge) {
   using namespace mlp;
   const int npairs = a.n + b.n;
   if (npairs <= 0) return FVX_OK;
@@ -1003,7 +1067,7 @@ int mlp_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, 
   }
   FwdArgs<true> A;
   A.r = RowsIO{nullptr, nullptr, nullptr, nullptr};
-  A.f = FarIO{a, b, rec};
+  A.f = FarIO{a, b, rec, judge};
   const int nctas = ((npairs + 127) / 128 + kGroups - 1) / kGroups;
   const int grid = nctas < device_sm_count() ? nctas : device_sm_count();
   mlp_fwd_kernel<true, true><<<grid, kGroups * 128, sizeof(FwdSmem), s>>>(
@@ -1013,12 +1077,25 @@ int mlp_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, 
 }
 
 // The analytic multipole-to-local translation of both lists in one launch.
-int m2l_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, cudaStream_t s) {
+int m2l_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, cudaStream_t s,
+                        const FarJudge& judge) {
   const int npairs = a.n + b.n;
   if (npairs <= 0) return FVX_OK;
   const int blocks = (npairs + mlp::kM2lThreads - 1) / mlp::kM2lThreads;
   const int grid = blocks < 2 * device_sm_count() ? blocks : 2 * device_sm_count();
-  mlp::m2l_pairs_kernel<<<grid, mlp::kM2lThreads, 0, s>>>(mlp::FarIO{a, b, rec});
+  mlp::m2l_pairs_kernel<<<grid, mlp::kM2lThreads, 0, s>>>(mlp::FarIO{a, b, rec, judge});
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+// partial: scratch of 2 cap x slices x 30 doubles
+int judge_sums_launch(const JudgeSampleView& S, const uint32_t* leaf_key, const int* cell_start,
+                      const int* cell_count, const float4* sp, const float4* sa,
+                      const int* leaf_of_particle, float h, double* partial, int slices,
+                      cudaStream_t s) {
+  if (S.cap <= 0) return FVX_OK;
+  mlp::judge_sums_kernel<<<dim3(2 * S.cap, slices), mlp::kTargetsThreads, 0, s>>>(
+      S, leaf_key, cell_start, cell_count, sp, sa, leaf_of_particle, h, partial);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
@@ -1078,7 +1155,7 @@ int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, f
   A.f = FarIO{fvx::FarPairs{}, fvx::FarPairs{}, nullptr};
   const int nctas = ((rows + 127) / 128 + kGroups - 1) / kGroups;
   const int grid = nctas < fvx::device_sm_count() ? nctas : fvx::device_sm_count();
-  // without stores it is inference: the F16 form the treecode far field runs
+  // without stores it is inference: the form the treecode far field runs
   auto kern = (z_store || h_store) ? mlp_fwd_kernel<false, false> : mlp_fwd_kernel<false, true>;
   kern<<<grid, kGroups * 128, sizeof(FwdSmem), static_cast<cudaStream_t>(stream)>>>(
       A, rows, static_cast<const __nv_bfloat16*>(W), bias);

@@ -25,6 +25,10 @@
 #include <cstring>
 #include <type_traits>
 
+#include <algorithm>
+#include <cstddef>
+#include <cstring>
+
 #include "fvx_common.cuh"
 #include "fvx_pair_math.cuh"
 
@@ -1588,72 +1592,277 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
   }
 }
 
-// ---- validation of the local-expansion path against FP64 direct sums -------------
-// Row k checks list pair k*stride: exact normalised expansion T (FP64 sums),
-// analytic translation A and network residual Y (zero without a network).
-// The error is that of the expansion applied across the target leaf: with
-// rho = sqrt(3)/2 h_T/d (the leaf's half diagonal over the distance),
-//   e = (|du| + rho |dJ| + rho^2/2 |dH|) / (|u| + rho |J| + rho^2/2 |H|).
-// A pair with e > tol is taken out of its leaf's expansion (its A + Y, scaled
-// back, is subtracted) and queued for the FP64 direct fallback.  val[0] += 1
-// per checked pair, val[1] += e, val[2] = max e (as ordered bits of a
-// non-negative float).
-__global__ void validate_kernel(int K, int stride, const int* __restrict__ pair_leaf,
-                                const int* __restrict__ pair_cell, const float* __restrict__ Tn,
-                                const float* __restrict__ An, const float* __restrict__ Yn,
-                                const float* __restrict__ scale, float tol,
-                                float* __restrict__ leaf_local, int2* __restrict__ fallback,
-                                int* __restrict__ n_fallback, float* __restrict__ val,
-                                float* __restrict__ errs) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= K) return;
-  const float* t = Tn + static_cast<int64_t>(k) * 32;
-  const float* a = An + static_cast<int64_t>(k) * 32;
-  const float* y = Yn ? Yn + static_cast<int64_t>(k) * 32 : nullptr;
-  float dn[3] = {0.f, 0.f, 0.f}, tn[3] = {0.f, 0.f, 0.f};
-  for (int c = 0; c < 30; ++c) {
-    const float p = a[c] + (y ? y[c] : 0.f);
-    const int g = c < 3 ? 0 : (c < 12 ? 1 : 2);
-    dn[g] += (p - t[c]) * (p - t[c]);
-    tn[g] += t[c] * t[c];
+// ---- the FP64 judge of the local-expansion path ------------------------------------
+// Every local-expansion pair falls in one of kJudgeClasses classes: its list
+// (the leaves' own pairs, or the pairs shared through parents of leaves) x
+// whether the source cell is larger than the target x four bins of the
+// opening ratio mu = sqrt(3)/2 (h_T + h_S) / d against the path's theta (all
+// its pairs have mu < theta): mu/theta in [0.9, 1), [0.8, 0.9), [0.65, 0.8)
+// and below 0.65.  The truncation error grows with mu, so the classes keep
+// pairs of different error apart, and the judge samples each class on its own.
+__device__ __forceinline__ int judge_class(int list, float hT, float hS, float d2,
+                                           float inv_theta2) {
+  const float q = 0.75f * (hT + hS) * (hT + hS) * inv_theta2 / d2;  // (mu / theta)^2
+  const int bin = q >= 0.81f ? 0 : (q >= 0.64f ? 1 : (q >= 0.4225f ? 2 : 3));
+  return (list << 3) | (hS > hT ? 4 : 0) | bin;
+}
+
+// Both lists of local-expansion pairs (rows: list 0's, then list 1's).
+struct JudgeLists {
+  const int* tgt[2];
+  const int* cell[2];
+  const uint32_t* key[2];
+  float h[2];
+  int n0, n;
+};
+
+// Class of every pair (cls[row]) and the class sizes (hist, accumulated).
+__global__ void judge_classify_kernel(JudgeLists J, const float* __restrict__ rec,
+                                      float inv_theta2, uint8_t* __restrict__ cls,
+                                      unsigned* __restrict__ hist) {
+  __shared__ unsigned sh[kJudgeClasses];
+  if (threadIdx.x < kJudgeClasses) sh[threadIdx.x] = 0u;
+  __syncthreads();
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < J.n; r += gridDim.x * blockDim.x) {
+    const int li = r >= J.n0 ? 1 : 0;
+    const int i = r - li * J.n0;
+    const int t = J.tgt[li][i], c = J.cell[li][i];
+    const float3 cT = cell_center_rel(J.key[li][t], J.h[li]);
+    const float4 cs = __ldg(reinterpret_cast<const float4*>(rec + static_cast<int64_t>(c) * kRecFloats));
+    const float dx = cT.x - cs.x, dy = cT.y - cs.y, dz = cT.z - cs.z;
+    const int k = judge_class(li, J.h[li], cs.w, dx * dx + dy * dy + dz * dz, inv_theta2);
+    cls[r] = static_cast<uint8_t>(k);
+    atomicAdd(&sh[k], 1u);
   }
-  const float rho = 0.8660254f * scale[static_cast<int64_t>(k) * 4 + 3];
-  const float w1 = rho, w2 = 0.5f * rho * rho;
-  const float num = sqrtf(dn[0]) + w1 * sqrtf(dn[1]) + w2 * sqrtf(dn[2]);
-  const float den = sqrtf(tn[0]) + w1 * sqrtf(tn[1]) + w2 * sqrtf(tn[2]);
-  const float err = num / fmaxf(den, 1e-30f);
-  errs[k] = err;
-  atomicAdd(val, 1.f);
-  atomicAdd(val + 1, err);
-  atomicMax(reinterpret_cast<unsigned*>(val + 2), __float_as_uint(err));
-  if (!(err <= tol)) {
-    const int leaf = pair_leaf[static_cast<int64_t>(k) * stride];
-    const int cell = pair_cell[static_cast<int64_t>(k) * stride];
-    const float* sc = scale + static_cast<int64_t>(k) * 4;
-    float* L = leaf_local + static_cast<int64_t>(leaf) * 32;
-    for (int c = 0; c < 30; ++c) {
-      const float p = a[c] + (y ? y[c] : 0.f);
-      atomicAdd(L + c, -p * (c < 3 ? sc[0] : (c < 12 ? sc[1] : sc[2])));
-    }
-    const int q = atomicAdd(n_fallback, 1);
-    fallback[q] = make_int2(leaf, cell);
+  __syncthreads();
+  if (threadIdx.x < kJudgeClasses && sh[threadIdx.x]) atomicAdd(hist + threadIdx.x, sh[threadIdx.x]);
+}
+
+// Judge state on the device, one block of words (zeroed per judged sweep).
+struct JudgeWords {
+  unsigned checked, repaired, err_sum_bits, err_max_bits, applied;
+  unsigned class_pairs[kJudgeClasses], class_samples[kJudgeClasses];
+  unsigned fail_learned[kJudgeClasses], fail_analytic[kJudgeClasses];
+  unsigned action[kJudgeClasses], taken[kJudgeClasses];
+  int cnt[2];
+  float unrepaired;
+};
+
+struct JudgeSampleBufs {
+  int* row[2];       // index of the sampled pair in its list
+  int* tgt[2];       // its target (leaf or parent)
+  int* cell[2];
+  uint32_t* key[2];
+  uint8_t* cls[2];
+  int cap;
+};
+
+__host__ __device__ __forceinline__ uint32_t judge_hash(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+
+// Stratified random sample: a pair of class k (n_k pairs) is taken with
+// probability s_k / n_k, s_k = min(n_k, per_class) (every pair of a class with
+// at most per_class pairs), from a hash of (row, seed); at most 2 per_class
+// per class are kept.
+__global__ void judge_select_kernel(JudgeLists J, const uint8_t* __restrict__ cls,
+                                    const unsigned* __restrict__ hist, int per_class,
+                                    uint32_t seed, JudgeWords* W, JudgeSampleBufs B) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < J.n; r += gridDim.x * blockDim.x) {
+    const int k = cls[r];
+    const unsigned nk = hist[k];
+    const unsigned sk = nk < static_cast<unsigned>(per_class) ? nk : per_class;
+    if (judge_hash(static_cast<uint32_t>(r) ^ seed) % nk >= sk) continue;
+    if (atomicAdd(&W->taken[k], 1u) >= 2u * per_class) continue;
+    const int li = r >= J.n0 ? 1 : 0;
+    const int i = r - li * J.n0;
+    const int q = atomicAdd(&W->cnt[li], 1);
+    if (q >= B.cap) continue;  // cannot happen: 2 x per_class x 8 classes per list
+    const int t = J.tgt[li][i];
+    B.row[li][q] = i;
+    B.tgt[li][q] = t;
+    B.cell[li][q] = J.cell[li][i];
+    B.key[li][q] = J.key[li][t];
+    B.cls[li][q] = static_cast<uint8_t>(k);
   }
 }
 
-// FP64 direct sum of a queued (leaf, cell) pair at every target of the leaf,
-// added to the outputs: blockIdx.x = the queued pair, blockIdx.y = one of
-// gridDim.y slices of the cell's particles (so a few large cells still fill
-// the GPU), each slice at least kFallbackMinSlice particles (the surplus
-// CTAs of a small cell return at once).  Each warp takes whole targets: its
-// lanes stride over the slice, reduce by shuffles and add one atomic per
-// output component, with no block-wide barrier per target.
+// Unused slots get a valid pair (the list's first), so that the translation
+// and network kernels can run over all cap slots; pair_tgt is the identity.
+__global__ void judge_pad_kernel(JudgeLists J, JudgeWords* W, JudgeSampleBufs B, int* iota) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= B.cap) return;
+  iota[q] = q;
+  for (int li = 0; li < 2; ++li) {
+    const int nl = li ? J.n - J.n0 : J.n0;
+    if (nl <= 0) continue;
+    if (q < W->cnt[li]) continue;
+    const int t = J.tgt[li][0];
+    B.row[li][q] = 0;
+    B.tgt[li][q] = t;
+    B.cell[li][q] = J.cell[li][0];
+    B.key[li][q] = J.key[li][t];
+    B.cls[li][q] = 0;
+  }
+}
+
+__device__ __forceinline__ float expansion_error(const float* p, const double* t, float rho) {
+  float dn[3] = {0.f, 0.f, 0.f}, tn[3] = {0.f, 0.f, 0.f};
+  for (int c = 0; c < 30; ++c) {
+    const float tc = static_cast<float>(t[c]);
+    const int g = c < 3 ? 0 : (c < 12 ? 1 : 2);
+    dn[g] += (p[c] - tc) * (p[c] - tc);
+    tn[g] += tc * tc;
+  }
+  const float w1 = rho, w2 = 0.5f * rho * rho;
+  const float num = sqrtf(dn[0]) + w1 * sqrtf(dn[1]) + w2 * sqrtf(dn[2]);
+  const float den = sqrtf(tn[0]) + w1 * sqrtf(tn[1]) + w2 * sqrtf(tn[2]);
+  return num / fmaxf(den, 1e-30f);
+}
+
+// Per sample: the exact expansion T (FP64 sums, slices in order), the
+// analytic translation A and the network residual Y (physical units, from
+// the same kernels the sweep runs), and the error of the expansion applied
+// across the target: with rho = sqrt(3)/2 h_T / d (the target's half
+// diagonal over the distance),
+//   e = (|du| + rho |dJ| + rho^2/2 |dH|) / (|u| + rho |J| + rho^2/2 |H|),
+// for A + Y (err_l) and for A alone (err_a); failures counted per class.
+__global__ void judge_errors_kernel(JudgeSampleBufs B, const float* __restrict__ rec,
+                                    const double* __restrict__ partial, int slices,
+                                    const float* __restrict__ A, const float* __restrict__ Y,
+                                    float h0, float h1, float tol, JudgeWords* W,
+                                    float* __restrict__ err) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= 2 * B.cap) return;
+  const int li = slot >= B.cap ? 1 : 0;
+  const int q = slot - li * B.cap;
+  if (q >= W->cnt[li]) return;
+  double t[30];
+  for (int c = 0; c < 30; ++c) {
+    double v = 0.0;
+    for (int y = 0; y < slices; ++y) v += partial[(static_cast<int64_t>(slot) * slices + y) * 30 + c];
+    t[c] = v;
+  }
+  const float hT = li ? h1 : h0;
+  const float3 cT = cell_center_rel(B.key[li][q], hT);
+  const float* cs = rec + static_cast<int64_t>(B.cell[li][q]) * kRecFloats;
+  const float dx = cT.x - cs[0], dy = cT.y - cs[1], dz = cT.z - cs[2];
+  const float rho = 0.8660254f * hT * rsqrtf(dx * dx + dy * dy + dz * dz);
+  float pa[30], pl[30];
+  for (int c = 0; c < 30; ++c) {
+    pa[c] = A[static_cast<int64_t>(slot) * 32 + c];
+    pl[c] = pa[c] + (Y ? Y[static_cast<int64_t>(slot) * 32 + c] : 0.f);
+  }
+  const float el = expansion_error(pl, t, rho), ea = expansion_error(pa, t, rho);
+  err[2 * slot] = el;
+  err[2 * slot + 1] = ea;
+  const int k = B.cls[li][q];
+  atomicAdd(&W->checked, 1u);
+  atomicAdd(&W->class_samples[k], 1u);
+  if (!(el <= tol)) atomicAdd(&W->fail_learned[k], 1u);
+  if (!(ea <= tol)) atomicAdd(&W->fail_analytic[k], 1u);
+}
+
+// Per class, from its sampled failure fractions (f_l with the network, f_a
+// without): f_l <= kJudgeFailFraction keeps the network (action 0); else
+// f_a <= kJudgeFailFraction drops the network for the class (1); else every
+// pair of the class is summed directly in FP64 (2).  act is the table the
+// sweep's translation and network kernels read (kept for the sweeps that are
+// not judged).  unrepaired: the expected fraction of the pairs left above
+// the tolerance, sum over the expanded classes of n_k f_k over sum n_k.
+constexpr float kJudgeFailFraction = 0.25f;
+__global__ void judge_decide_kernel(JudgeWords* W, const unsigned* __restrict__ hist,
+                                    uint8_t* __restrict__ act, int learned) {
+  const int k = threadIdx.x;
+  float num = 0.f, den = 0.f;
+  if (k < kJudgeClasses) {
+    const unsigned ns = W->class_samples[k], nk = hist[k];
+    int a = 0;
+    float f = 0.f;
+    if (ns > 0) {
+      const float fl = static_cast<float>(W->fail_learned[k]) / ns;
+      const float fa = static_cast<float>(W->fail_analytic[k]) / ns;
+      if (fl <= kJudgeFailFraction) {
+        a = 0;
+        f = fl;
+      } else if (learned && fa <= kJudgeFailFraction) {
+        a = 1;
+        f = fa;
+      } else {
+        a = 2;
+      }
+    }
+    act[k] = static_cast<uint8_t>(a);
+    W->action[k] = a;
+    W->class_pairs[k] = nk;
+    num = f * nk;
+    den = static_cast<float>(nk);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    num += __shfl_xor_sync(0xffffffffu, num, o);
+    den += __shfl_xor_sync(0xffffffffu, den, o);
+  }
+  if (k == 0) W->unrepaired = den > 0.f ? num / den : 0.f;
+}
+
+// After the sweep's expansions: a sampled pair of an expanded class whose
+// applied expansion (A + Y, or A where the network was dropped) misses the
+// tolerance is taken out of its target's expansion and queued for the FP64
+// direct sum.  The applied error is summed for the report.
+__global__ void judge_repair_kernel(JudgeSampleBufs B, const float* __restrict__ A,
+                                    const float* __restrict__ Y, const float* __restrict__ err,
+                                    float tol, const uint8_t* __restrict__ act, float* local0,
+                                    float* local1, JudgeWords* W, FarJudge J) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= 2 * B.cap) return;
+  const int li = slot >= B.cap ? 1 : 0;
+  const int q = slot - li * B.cap;
+  if (q >= W->cnt[li]) return;
+  const int a = act[B.cls[li][q]];
+  if (a == 2) return;  // already queued whole by the translation kernel
+  const float e = err[2 * slot + (a == 0 ? 0 : 1)];
+  atomicAdd(&W->applied, 1u);
+  atomicAdd(reinterpret_cast<float*>(&W->err_sum_bits), e);
+  atomicMax(&W->err_max_bits, __float_as_uint(e));
+  if (e <= tol) return;
+  const int t = B.tgt[li][q];
+  float* L = (li ? local1 : local0) + static_cast<int64_t>(t) * 32;
+  for (int c = 0; c < 30; ++c) {
+    float p = A[static_cast<int64_t>(slot) * 32 + c];
+    if (a == 0 && Y) p += Y[static_cast<int64_t>(slot) * 32 + c];
+    atomicAdd(L + c, -p);
+  }
+  atomicAdd(&W->repaired, 1u);
+  const int f = atomicAdd(J.nfb, 1);
+  if (f < J.fb_cap)
+    J.fb[f] = make_int2(t | (li << 30), B.cell[li][q]);
+  else
+    flag_status(kStatusCapacity);
+}
+
+// FP64 direct sums of the queued (target, cell) pairs at every particle of
+// the target (a leaf, or a parent of leaves), added to the outputs.
+// Persistent CTAs stride over (pair, slice) items: kFallbackSlices slices of
+// the cell's particles per pair, each at least kFallbackMinSlice particles
+// (the surplus items of a small cell are skipped at once).  Each warp takes
+// whole targets: its lanes stride over the slice, reduce by shuffles and add
+// one atomic per output component, with no block-wide barrier per target.
 constexpr int kFallbackThreads = 256;
 constexpr int kFallbackMinSlice = 128;
+constexpr int kFallbackSlices = 8;
+struct FallbackTargets {
+  const int* start[2];
+  const int* count[2];
+};
 template <int MODE, int KERNEL>
 __global__ void __launch_bounds__(kFallbackThreads) fallback_kernel(
-    const int2* __restrict__ fallback, const int* __restrict__ n_fallback,
-    const int* __restrict__ leaf_start, const int* __restrict__ leaf_count,
-    const int* __restrict__ cell_start, const int* __restrict__ cell_count,
+    const int2* __restrict__ fallback, const int* __restrict__ n_fallback, int fb_cap,
+    FallbackTargets tg, const int* __restrict__ cell_start, const int* __restrict__ cell_count,
     const int* __restrict__ perm, const double* __restrict__ pos,
     const double* __restrict__ alpha, const double* __restrict__ sigma,
     const double* __restrict__ tgt_gamma, double* __restrict__ out_a,
@@ -1664,51 +1873,56 @@ __global__ void __launch_bounds__(kFallbackThreads) fallback_kernel(
   constexpr bool NEED_FPR = ModeInfo<MODE>::need_fpr;
   constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
   constexpr double kC = -0.07957747154594767;
-  if (static_cast<int>(blockIdx.x) >= *n_fallback) return;
-  const int2 pr = fallback[blockIdx.x];
-  const int t0 = leaf_start[pr.x], nt = leaf_count[pr.x];
-  const int c0 = cell_start[pr.y], cn = cell_count[pr.y];
-  const int per = max(kFallbackMinSlice, (cn + static_cast<int>(gridDim.y) - 1) /
-                                             static_cast<int>(gridDim.y));
-  const int64_t s0_64 = c0 + static_cast<int64_t>(blockIdx.y) * per;
-  if (s0_64 >= c0 + cn) return;
-  const int s0 = static_cast<int>(s0_64);
-  const int ns = min(per, c0 + cn - s0);
+  const int nq = min(*n_fallback, fb_cap);
+  const int64_t items = static_cast<int64_t>(nq) * kFallbackSlices;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int ti = wid; ti < nt; ti += kFallbackThreads / 32) {
-    const int i = perm[t0 + ti];
-    const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
-    double gx = 0.0, gy = 0.0, gz = 0.0;
-    if (NEED_TG) {
-      gx = tgt_gamma[3 * i];
-      gy = tgt_gamma[3 * i + 1];
-      gz = tgt_gamma[3 * i + 2];
-    }
-    double acc[NC];
+  for (int64_t w = blockIdx.x; w < items; w += gridDim.x) {
+    const int2 pr = fallback[w / kFallbackSlices];
+    const int sl = static_cast<int>(w % kFallbackSlices);
+    const int li = (pr.x >> 30) & 1, tgt = pr.x & ((1 << 30) - 1);
+    const int t0 = (li ? tg.start[1] : tg.start[0])[tgt];
+    const int nt = (li ? tg.count[1] : tg.count[0])[tgt];
+    const int c0 = cell_start[pr.y], cn = cell_count[pr.y];
+    const int per = max(kFallbackMinSlice, (cn + kFallbackSlices - 1) / kFallbackSlices);
+    const int64_t s0_64 = c0 + static_cast<int64_t>(sl) * per;
+    if (s0_64 >= c0 + cn) continue;
+    const int s0 = static_cast<int>(s0_64);
+    const int ns = min(per, c0 + cn - s0);
+    for (int ti = wid; ti < nt; ti += kFallbackThreads / 32) {
+      const int i = perm[t0 + ti];
+      const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+      double gx = 0.0, gy = 0.0, gz = 0.0;
+      if (NEED_TG) {
+        gx = tgt_gamma[3 * i];
+        gy = tgt_gamma[3 * i + 1];
+        gz = tgt_gamma[3 * i + 2];
+      }
+      double acc[NC];
 #pragma unroll
-    for (int c = 0; c < NC; ++c) acc[c] = 0.0;
-    for (int q = lane; q < ns; q += 32) {
-      const int j = perm[s0 + q];
-      const double dx = x - pos[3 * j], dy = y - pos[3 * j + 1], dz = z - pos[3 * j + 2];
-      const double r2 = dx * dx + dy * dy + dz * dz;
-      const double sg = sigma[j];
-      const double s2 = sg * sg;
-      const double k2 = KERNEL == FVX_KERNEL_WINCKELMANS ? 2.5 * s2 : 1.0 / sg;
-      double f, fpr = 0.0;
-      core_f64<KERNEL, NEED_FPR>(r2, s2, k2, f, fpr);
-      accumulate<MODE, double>(acc, dx, dy, dz, r2, kC * alpha[3 * j], kC * alpha[3 * j + 1],
-                               kC * alpha[3 * j + 2], f, fpr, gx, gy, gz);
-    }
+      for (int c = 0; c < NC; ++c) acc[c] = 0.0;
+      for (int q = lane; q < ns; q += 32) {
+        const int j = perm[s0 + q];
+        const double dx = x - pos[3 * j], dy = y - pos[3 * j + 1], dz = z - pos[3 * j + 2];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        const double sg = sigma[j];
+        const double s2 = sg * sg;
+        const double k2 = KERNEL == FVX_KERNEL_WINCKELMANS ? 2.5 * s2 : 1.0 / sg;
+        double f, fpr = 0.0;
+        core_f64<KERNEL, NEED_FPR>(r2, s2, k2, f, fpr);
+        accumulate<MODE, double>(acc, dx, dy, dz, r2, kC * alpha[3 * j], kC * alpha[3 * j + 1],
+                                 kC * alpha[3 * j + 2], f, fpr, gx, gy, gz);
+      }
 #pragma unroll
-    for (int c = 0; c < NC; ++c)
-      for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+      for (int c = 0; c < NC; ++c)
+        for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      if (lane != c) continue;
-      if (c < NA)
-        atomicAdd(out_a + static_cast<int64_t>(i) * NA + c, acc[c]);
-      else
-        atomicAdd(out_b + static_cast<int64_t>(i) * (NC - NA) + (c - NA), acc[c]);
+      for (int c = 0; c < NC; ++c) {
+        if (lane != c) continue;
+        if (c < NA)
+          atomicAdd(out_a + static_cast<int64_t>(i) * NA + c, acc[c]);
+        else
+          atomicAdd(out_b + static_cast<int64_t>(i) * (NC - NA) + (c - NA), acc[c]);
+      }
     }
   }
 }
@@ -1777,7 +1991,7 @@ void grid_params(const double lo[3], const double hi[3], int64_t n, int leaf_tar
 }  // namespace
 
 int mlp_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, const void* W,
-                        const float* bias, cudaStream_t s);
+                        const float* bias, cudaStream_t s, const FarJudge& judge = FarJudge{});
 int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const int* pair_cell,
                             const uint32_t* tgt_key, float h_tgt, const uint32_t* leaf_key,
                             const float* rec, const int* cell_start,
@@ -1785,7 +1999,12 @@ int mlp_pair_targets_launch(int npairs, int stride, const int* pair_leaf, const 
                             const int* leaf_of_particle, float h, void* X, float* T,
                             float* A, float* scale, double* partial, int slices,
                             cudaStream_t s);
-int m2l_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, cudaStream_t s);
+int m2l_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, cudaStream_t s,
+                        const FarJudge& judge = FarJudge{});
+int judge_sums_launch(const JudgeSampleView& S, const uint32_t* leaf_key, const int* cell_start,
+                      const int* cell_count, const float4* sp, const float4* sa,
+                      const int* leaf_of_particle, float h, double* partial, int slices,
+                      cudaStream_t s);
 
 }  // namespace fvx
 
@@ -1801,11 +2020,17 @@ struct fvx_tree {
   const float* mlp_b = nullptr;
   double theta_l = 0.0;
   cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // around the local-expansion stage
-  // per-sweep validation of the local-expansion path and its FP64 fallback
+  // the FP64 judge of the local-expansion path and its FP64 fallback: samples
+  // per judged sweep (spread over the classes), the tolerance, the per-mode
+  // class actions (kept between judged sweeps), the pair classes, the sample
+  // buffers, the fallback queue
   int val_samples = 256;
   double val_tol = 0.1;
-  fvx::DevBuf val_X, val_T, val_A, val_Y, val_scale, val_err, val_fb, val_stats;
-  int last_val_k = 0;
+  bool judge_armed = false;      // a judged sweep has set the action tables
+  uint32_t judge_seq = 0;        // seeds the samples of each judged sweep
+  fvx::DevBuf judge_act, judge_cls, judge_hist, judge_words, judge_samp, judge_A, judge_Y,
+      judge_err, fb_queue, fb_count;
+  int last_judged = 0;           // samples judged by the last judged sweep
   // two-level traversal: per-parent lists and expansions
   fvx::DevBuf dual_meta, par_par, par_cell, parent_local;
   fvx::DevBuf cen;  // cell centres in units of h/2 (dual traversal)
@@ -1909,17 +2134,17 @@ void launch_eval(int mode, int nleaf, int n, const tree::EvalArgs& A, cudaStream
 }
 
 template <int KERNEL>
-void launch_fallback(int mode, dim3 grid, const int2* fb, const int* nfb, const int* leaf_start,
-                     const int* leaf_count, const int* cell_start, const int* cell_count,
+void launch_fallback(int mode, int grid, const int2* fb, const int* nfb, int fb_cap,
+                     tree::FallbackTargets tgs, const int* cell_start, const int* cell_count,
                      const int* perm, const double* pos, const double* alpha,
                      const double* sigma, const double* tg, double* out_a, double* out_b,
                      cudaStream_t s) {
   using namespace tree;
-#define FVX_FB(M)                                                                          \
-  fallback_kernel<M, KERNEL><<<grid, kFallbackThreads, 0, s>>>(fb, nfb, leaf_start,        \
-                                                               leaf_count,                 \
-                                                  cell_start, cell_count, perm, pos, alpha, \
-                                                  sigma, tg, out_a, out_b)
+#define FVX_FB(M)                                                                        \
+  fallback_kernel<M, KERNEL><<<grid, kFallbackThreads, 0, s>>>(fb, nfb, fb_cap, tgs,     \
+                                                               cell_start, cell_count,   \
+                                                               perm, pos, alpha, sigma,  \
+                                                               tg, out_a, out_b)
   switch (mode) {
     case FVX_PAIR_VELOCITY:
       FVX_FB(FVX_PAIR_VELOCITY);
@@ -2407,17 +2632,131 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   A.parent_local = nullptr;
   A.leaf_parent = leaf_parent;
   const uint32_t* par_key = dual ? V.key + base[L - 1] : nullptr;
-  if (learned && lrn_total + par_total > 0) {
+  // ---- the FP64 judge of the local-expansion path --------------------------------
+  // A judged sweep (val_samples > 0) classifies every pair, samples each class,
+  // sums the samples' exact expansions in FP64, runs the sweep's own
+  // translation and network kernels on them and decides per class whether the
+  // network stays, is dropped, or the whole class is summed directly in FP64;
+  // the decision is kept (per mode) for the sweeps in between, which only
+  // classify their pairs.
+  const int64_t nloc = learned ? lrn_total + par_total : 0;
+  const bool network = T->far_method == FVX_FAR_LEARNED;
+  const bool judged = nloc > 0 && T->val_samples > 0;
+  const bool use_judge = nloc > 0 && (judged || T->judge_armed);
+  const int mslot = mode & 7;
+  FarJudge FJ{};
+  tree::JudgeLists JL{};
+  tree::JudgeSampleBufs JB{};
+  tree::JudgeWords* JW = nullptr;
+  int jcap = 0;
+  uint8_t* act = nullptr;
+  if (use_judge) {
+    const bool fresh_table = T->judge_act.p == nullptr;
+    if ((rc = grow(T->judge_act, 8 * kJudgeClasses)) || (rc = grow(T->judge_cls, size_t(nloc))) ||
+        (rc = grow(T->judge_hist, 4 * kJudgeClasses)) || (rc = grow(T->fb_count, 16)))
+      return rc;
+    if (fresh_table || !T->judge_armed)
+      FVX_CUDA_TRY(cudaMemsetAsync(T->judge_act.p, 0, 8 * kJudgeClasses, s));
+    act = P<uint8_t>(T->judge_act) + mslot * kJudgeClasses;
+    FVX_CUDA_TRY(cudaMemsetAsync(T->judge_hist.p, 0, 4 * kJudgeClasses, s));
+    FVX_CUDA_TRY(cudaMemsetAsync(T->fb_count.p, 0, 16, s));
+    JL.tgt[0] = P<int>(T->lrn_leaf);
+    JL.cell[0] = P<int>(T->lrn_cell);
+    JL.key[0] = leaves.key;
+    JL.h[0] = static_cast<float>(h);
+    JL.tgt[1] = dual ? P<int>(T->par_par) : JL.tgt[0];
+    JL.cell[1] = dual ? P<int>(T->par_cell) : JL.cell[0];
+    JL.key[1] = dual ? par_key : JL.key[0];
+    JL.h[1] = static_cast<float>(2.0 * h);
+    JL.n0 = static_cast<int>(lrn_total);
+    JL.n = static_cast<int>(nloc);
+    const int cgrid = static_cast<int>(std::min<int64_t>((nloc + 255) / 256, 8 * device_sm_count()));
+    tree::judge_classify_kernel<<<cgrid, 256, 0, s>>>(
+        JL, rec, static_cast<float>(1.0 / (T->theta_l * T->theta_l)), P<uint8_t>(T->judge_cls),
+        P<unsigned>(T->judge_hist));
+    FVX_LAUNCH_CHECK();
+  }
+  if (judged) {
+    const int per_class = std::max(1, T->val_samples / kJudgeClasses);
+    jcap = 16 * per_class;  // per list: 8 classes, at most 2 per_class samples each
+    const int slices = std::max(1, std::min(64, 8 * device_sm_count() / (2 * jcap)));
+    if ((rc = grow(T->judge_words, sizeof(tree::JudgeWords))) ||
+        (rc = grow(T->judge_samp, (9 * sizeof(int) + 2) * size_t(jcap) + 256)) ||
+        (rc = grow(T->judge_A, sizeof(float) * 64 * size_t(jcap))) ||
+        (rc = grow(T->judge_Y, sizeof(float) * 64 * size_t(jcap))) ||
+        (rc = grow(T->judge_err, sizeof(float) * 4 * size_t(jcap))) ||
+        (rc = grow(T->pair_partial, sizeof(double) * 30 * 2 * size_t(jcap) * slices)))
+      return rc;
+    JW = P<tree::JudgeWords>(T->judge_words);
+    FVX_CUDA_TRY(cudaMemsetAsync(JW, 0, sizeof(tree::JudgeWords), s));
+    FVX_CUDA_TRY(cudaMemsetAsync(T->judge_A.p, 0, sizeof(float) * 64 * size_t(jcap), s));
+    FVX_CUDA_TRY(cudaMemsetAsync(T->judge_Y.p, 0, sizeof(float) * 64 * size_t(jcap), s));
+    int* ib = P<int>(T->judge_samp);
+    for (int l = 0; l < 2; ++l) {
+      JB.row[l] = ib + (4 * l + 0) * jcap;
+      JB.tgt[l] = ib + (4 * l + 1) * jcap;
+      JB.cell[l] = ib + (4 * l + 2) * jcap;
+      JB.key[l] = reinterpret_cast<uint32_t*>(ib + (4 * l + 3) * jcap);
+      JB.cls[l] = reinterpret_cast<uint8_t*>(ib + 9 * jcap) + l * jcap;
+    }
+    int* iota = ib + 8 * jcap;
+    JB.cap = jcap;
+    const uint32_t seed = tree::judge_hash(0x9e3779b9u * (++T->judge_seq));
+    const int cgrid = static_cast<int>(std::min<int64_t>((nloc + 255) / 256, 8 * device_sm_count()));
+    tree::judge_select_kernel<<<cgrid, 256, 0, s>>>(JL, P<uint8_t>(T->judge_cls),
+                                                    P<unsigned>(T->judge_hist), per_class, seed,
+                                                    JW, JB);
+    FVX_LAUNCH_CHECK();
+    tree::judge_pad_kernel<<<(jcap + 127) / 128, 128, 0, s>>>(JL, JW, JB, iota);
+    FVX_LAUNCH_CHECK();
+    // exact FP64 expansions of the samples
+    const int* jcnt = reinterpret_cast<const int*>(reinterpret_cast<const char*>(JW) +
+                                                   offsetof(tree::JudgeWords, cnt));
+    JudgeSampleView SV{jcnt, jcap, {JB.cell[0], JB.cell[1]}, {JB.key[0], JB.key[1]},
+                       {JL.h[0], JL.h[1]}};
+    if ((rc = judge_sums_launch(SV, leaves.key, lvb, lvb + total_cells, sp, sa, cid,
+                                static_cast<float>(h), P<double>(T->pair_partial), slices, s)))
+      return rc;
+    // the sweep's own translation (and network) on the samples, one target each
+    float* jA = P<float>(T->judge_A);
+    float* jY = P<float>(T->judge_Y);
+    const int n1s = dual && par_total > 0 ? jcap : 0;
+    const int n0s = lrn_total > 0 ? jcap : 0;
+    FarPairs sa0{iota, JB.cell[0], JB.key[0], JL.h[0], jA, n0s};
+    FarPairs sa1{iota, JB.cell[1], JB.key[1], JL.h[1], jA + 32 * jcap, n1s};
+    if ((rc = m2l_farfield_launch(sa0, sa1, rec, s))) return rc;
+    if (network) {
+      FarPairs sy0{iota, JB.cell[0], JB.key[0], JL.h[0], jY, n0s};
+      FarPairs sy1{iota, JB.cell[1], JB.key[1], JL.h[1], jY + 32 * jcap, n1s};
+      if ((rc = mlp_farfield_launch(sy0, sy1, rec, T->mlp_W, T->mlp_b, s))) return rc;
+    }
+    tree::judge_errors_kernel<<<(2 * jcap + 127) / 128, 128, 0, s>>>(
+        JB, rec, P<double>(T->pair_partial), slices, jA, network ? jY : nullptr, JL.h[0],
+        JL.h[1], static_cast<float>(T->val_tol), JW, P<float>(T->judge_err));
+    FVX_LAUNCH_CHECK();
+    tree::judge_decide_kernel<<<1, 32, 0, s>>>(JW, P<unsigned>(T->judge_hist), act,
+                                               network ? 1 : 0);
+    FVX_LAUNCH_CHECK();
+    T->judge_armed = true;
+  }
+  if (use_judge) {
+    const int64_t cap = nloc + 2 * int64_t(jcap);
+    if ((rc = grow(T->fb_queue, sizeof(int2) * size_t(cap)))) return rc;
+    FJ.cls = P<uint8_t>(T->judge_cls);
+    FJ.act = act;
+    FJ.fb = P<int2>(T->fb_queue);
+    FJ.nfb = P<int>(T->fb_count);
+    FJ.fb_cap = static_cast<int>(cap);
+  }
+  if (learned && nloc > 0) {
     if (!T->ev2) {
       FVX_CUDA_TRY(cudaEventCreate(&T->ev2));
       FVX_CUDA_TRY(cudaEventCreate(&T->ev3));
     }
     FVX_CUDA_TRY(cudaEventRecord(T->ev2, s));
-    // the analytic translation, then (learned) the network's residual, for the
-    // leaves' own pairs and for the pairs shared through their parents
     // zeroed expansions of the leaves (and parents), then the analytic
     // translation and (learned) the network's residual of both lists, each in
-    // one launch
+    // one launch, under the judge's class actions
     auto zeroed = [&](DevBuf& buf, int ntgt) -> int {
       int r = grow(buf, sizeof(float) * 32 * size_t(ntgt));
       if (r) return r;
@@ -2433,72 +2772,21 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
       lb = FarPairs{P<int>(T->par_par), P<int>(T->par_cell), par_key, static_cast<float>(2.0 * h),
                     P<float>(T->parent_local), static_cast<int>(par_total)};
     }
-    if ((rc = m2l_farfield_launch(la, lb, rec, s))) return rc;
-    if (T->far_method == FVX_FAR_LEARNED &&
-        (rc = mlp_farfield_launch(la, lb, rec, T->mlp_W, T->mlp_b, s)))
-      return rc;
+    if ((rc = m2l_farfield_launch(la, lb, rec, s, FJ))) return rc;
+    if (network && (rc = mlp_farfield_launch(la, lb, rec, T->mlp_W, T->mlp_b, s, FJ))) return rc;
     A.leaf_local = P<float>(T->leaf_local);
     if (dual) A.parent_local = P<float>(T->parent_local);
     FVX_CUDA_TRY(cudaEventRecord(T->ev3, s));
   }
-  // validation sample: FP64 direct local expansions of evenly strided pairs of
-  // each list (leaves' own pairs; parents' pairs), half of the samples each
-  int val_k = 0, val_k_par = 0;
-  const int64_t val_cap = T->val_samples;
-  if (learned && lrn_total + par_total > 0 && T->val_samples > 0) {
-    const size_t K = static_cast<size_t>(T->val_samples);
-    if ((rc = grow(T->val_X, 2 * 48 * K)) || (rc = grow(T->val_T, 4 * 32 * K)) ||
-        (rc = grow(T->val_A, 4 * 32 * K)) || (rc = grow(T->val_Y, 4 * 32 * K)) ||
-        (rc = grow(T->val_scale, 4 * 4 * K)) || (rc = grow(T->val_err, 4 * K)) ||
-        (rc = grow(T->val_fb, 8 * 2 * K)) || (rc = grow(T->val_stats, 64)))
-      return rc;
-    FVX_CUDA_TRY(cudaMemsetAsync(T->val_stats.p, 0, 64, s));
-    auto validate = [&](int nlist, int samples, const int* tgt, const int* cell,
-                        const uint32_t* tkey, float th, float* local, int2* fb, int* nfb,
-                        int* k_out) -> int {
-      *k_out = 0;
-      if (nlist <= 0 || samples <= 0) return FVX_OK;
-      const int stride = nlist > samples ? nlist / samples : 1;
-      const int k = nlist / stride < samples ? nlist / stride : samples;
-      // slices: about eight CTAs per SM over the k sums (more slices cost more
-      // in their FP64 reductions than they save on the few large cells)
-      const int slices = max(1, min(64, 8 * device_sm_count() / k));
-      int r = grow(T->pair_partial, sizeof(double) * 30 * size_t(k) * slices);
-      if (r) return r;
-      r = mlp_pair_targets_launch(k, stride, tgt, cell, tkey, th, leaves.key, rec, lvb,
-                                  lvb + total_cells, sp, sa, cid, static_cast<float>(h),
-                                  T->val_X.p, P<float>(T->val_T), P<float>(T->val_A),
-                                  P<float>(T->val_scale), P<double>(T->pair_partial), slices, s);
-      if (r) return r;
-      const float* Y = nullptr;
-      if (T->far_method == FVX_FAR_LEARNED) {
-        if ((r = fvx_mlp_forward(T->val_X.p, k, T->mlp_W, T->mlp_b, P<float>(T->val_Y),
-                                 nullptr, nullptr, s)))
-          return r;
-        Y = P<float>(T->val_Y);
-      }
-      validate_kernel<<<(k + 127) / 128, 128, 0, s>>>(
-          k, stride, tgt, cell, P<float>(T->val_T), P<float>(T->val_A), Y,
-          P<float>(T->val_scale), static_cast<float>(T->val_tol), local, fb, nfb,
-          P<float>(T->val_stats), P<float>(T->val_err));
-      FVX_LAUNCH_CHECK();
-      *k_out = k;
-      return FVX_OK;
-    };
-    const int k_leaf = dual && par_total > 0 ? (T->val_samples + 1) / 2 : T->val_samples;
-    if ((rc = validate(static_cast<int>(lrn_total), k_leaf, P<int>(T->lrn_leaf),
-                       P<int>(T->lrn_cell), leaves.key, static_cast<float>(h),
-                       P<float>(T->leaf_local), P<int2>(T->val_fb), P<int>(T->val_stats) + 4,
-                       &val_k)))
-      return rc;
-    if (dual &&
-        (rc = validate(static_cast<int>(par_total), T->val_samples - k_leaf, P<int>(T->par_par),
-                       P<int>(T->par_cell), par_key, static_cast<float>(2.0 * h),
-                       P<float>(T->parent_local), P<int2>(T->val_fb) + val_cap,
-                       P<int>(T->val_stats) + 5, &val_k_par)))
-      return rc;
+  if (judged) {
+    // sampled pairs that miss the tolerance: out of their expansions, queued
+    tree::judge_repair_kernel<<<(2 * jcap + 127) / 128, 128, 0, s>>>(
+        JB, P<float>(T->judge_A), network ? P<float>(T->judge_Y) : nullptr,
+        P<float>(T->judge_err), static_cast<float>(T->val_tol), act, P<float>(T->leaf_local),
+        dual ? P<float>(T->parent_local) : nullptr, JW, FJ);
+    FVX_LAUNCH_CHECK();
+    T->last_judged = 2 * jcap;
   }
-  T->last_val_k = val_k + val_k_par;
   T->last_L = L;
   T->last_nleaf = nleaf;
   T->last_h = h;
@@ -2524,28 +2812,22 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
     launch_eval<FVX_KERNEL_GAUSSIANERF>(mode, nleaf, n, A, s);
   FVX_LAUNCH_CHECK();
   FVX_CUDA_TRY(cudaEventRecord(T->ev1, s));
-  // FP64 direct sums of the queued clusters at every target of their leaf / parent
-  auto fallback = [&](int k, const int2* fb, const int* nfb, const int* tstart,
-                      const int* tcount) {
-    if (k <= 0) return;
-    // queued pairs are at most k (few in practice): slice every cell so that
-    // all of them together span about four CTAs per SM
-    const int slices = max(1, min(64, 4 * device_sm_count() / max(1, k / 16)));
-    const dim3 fgrid(k, slices);
+  // FP64 direct sums of the queued pairs (whole classes and sampled repairs)
+  // at every particle of their leaf or parent
+  if (use_judge) {
+    tree::FallbackTargets tgs{{A.leaf_start, dual ? V.start + base[L - 1] : A.leaf_start},
+                              {A.leaf_count, dual ? V.count + base[L - 1] : A.leaf_count}};
+    const int fgrid = 4 * device_sm_count();
     if (kernel == FVX_KERNEL_WINCKELMANS)
-      launch_fallback<FVX_KERNEL_WINCKELMANS>(mode, fgrid, fb, nfb, tstart, tcount, lvb,
+      launch_fallback<FVX_KERNEL_WINCKELMANS>(mode, fgrid, FJ.fb, FJ.nfb, FJ.fb_cap, tgs, lvb,
                                               lvb + total_cells, perm, pos, alpha, sigma,
                                               tgt_gamma, out_a, out_b, s);
     else
-      launch_fallback<FVX_KERNEL_GAUSSIANERF>(mode, fgrid, fb, nfb, tstart, tcount, lvb,
+      launch_fallback<FVX_KERNEL_GAUSSIANERF>(mode, fgrid, FJ.fb, FJ.nfb, FJ.fb_cap, tgs, lvb,
                                               lvb + total_cells, perm, pos, alpha, sigma,
                                               tgt_gamma, out_a, out_b, s);
-  };
-  fallback(val_k, P<int2>(T->val_fb), P<int>(T->val_stats) + 4, A.leaf_start, A.leaf_count);
-  if (dual)
-    fallback(val_k_par, P<int2>(T->val_fb) + val_cap, P<int>(T->val_stats) + 5,
-             V.start + base[L - 1], V.count + base[L - 1]);
-  FVX_LAUNCH_CHECK();
+    FVX_LAUNCH_CHECK();
+  }
   unsigned ovf_h[6] = {0, 0, 0, 0, 0, 0};
   FVX_CUDA_TRY(cudaMemcpyAsync(ovf_h, ovf, 24, cudaMemcpyDeviceToHost, s));
   T->stats[0] = L;
@@ -2602,8 +2884,9 @@ void fvx_tree_destroy(fvx_tree* T) {
                          &T->scan_tmp, &T->flags,   &T->cid,      &T->levels,   &T->counts,
                          &T->rec,     &T->sp,       &T->sa,       &T->sg,       &T->lists_meta,
                          &T->near_list, &T->far_list, &T->bbox,   &T->lrn_meta, &T->lrn_leaf,
-                         &T->lrn_cell, &T->leaf_local, &T->val_X, &T->val_T, &T->val_A,
-                         &T->val_Y, &T->val_scale, &T->val_err, &T->val_fb, &T->val_stats,
+                         &T->lrn_cell, &T->leaf_local, &T->judge_act, &T->judge_cls,
+                         &T->judge_hist, &T->judge_words, &T->judge_samp, &T->judge_A,
+                         &T->judge_Y, &T->judge_err, &T->fb_queue, &T->fb_count,
                          &T->dual_meta, &T->par_par, &T->par_cell, &T->parent_local,
                          &T->cen, &T->res_slot, &T->res_cnt, &T->eval_next,
                          &T->leaf_order, &T->order_table,
@@ -2634,6 +2917,8 @@ int fvx_tree_set_far_field(fvx_tree* T, int method, const void* W, const float* 
   T->mlp_W = method == FVX_FAR_LEARNED ? W : nullptr;
   T->mlp_b = method == FVX_FAR_LEARNED ? b : nullptr;
   T->theta_l = method == FVX_FAR_M2P ? 0.0 : theta_local;
+  T->judge_armed = false;  // a new far field starts with every class expanded
+  T->last_judged = 0;
   return FVX_OK;
 }
 
@@ -2648,16 +2933,48 @@ int fvx_tree_set_validation(fvx_tree* T, int samples, double tol) {
 
 int fvx_tree_last_validation(fvx_tree* T, double* out) {
   FVX_ARG_CHECK(T && out, "null argument");
-  for (int k = 0; k < 4; ++k) out[k] = 0.0;
-  if (T->last_val_k <= 0) return FVX_OK;
-  float v[4];
-  int nfb[2] = {0, 0};
-  FVX_CUDA_TRY(cudaMemcpy(v, T->val_stats.p, 16, cudaMemcpyDeviceToHost));
-  FVX_CUDA_TRY(cudaMemcpy(nfb, fvx::P<int>(T->val_stats) + 4, 8, cudaMemcpyDeviceToHost));
-  out[0] = v[0];
-  out[1] = nfb[0] + nfb[1];
-  out[2] = v[0] > 0.f ? v[1] / v[0] : 0.0;
-  out[3] = v[2];
+  double rec[8 + 5 * fvx::kJudgeClasses];
+  int rc = fvx_tree_last_judge(T, rec, 8 + 5 * fvx::kJudgeClasses);
+  if (rc) return rc;
+  out[0] = rec[0];
+  out[1] = rec[2];
+  out[2] = rec[3];
+  out[3] = rec[4];
+  return FVX_OK;
+}
+
+int fvx_tree_last_judge(fvx_tree* T, double* out, int n_out) {
+  FVX_ARG_CHECK(T && out && n_out >= 0, "null argument");
+  const int n_rec = 8 + 5 * fvx::kJudgeClasses;
+  for (int k = 0; k < n_out; ++k) out[k] = 0.0;
+  if (T->last_judged <= 0) return FVX_OK;
+  fvx::tree::JudgeWords W;
+  int nfb = 0;
+  FVX_CUDA_TRY(cudaMemcpy(&W, T->judge_words.p, sizeof(W), cudaMemcpyDeviceToHost));
+  FVX_CUDA_TRY(cudaMemcpy(&nfb, T->fb_count.p, sizeof(int), cudaMemcpyDeviceToHost));
+  double rec[8 + 5 * fvx::kJudgeClasses];
+  float esum;
+  memcpy(&esum, &W.err_sum_bits, sizeof(float));
+  float emax;
+  memcpy(&emax, &W.err_max_bits, sizeof(float));
+  double pairs = 0.0;
+  for (int k = 0; k < fvx::kJudgeClasses; ++k) pairs += W.class_pairs[k];
+  rec[0] = W.checked;
+  rec[1] = W.repaired;
+  rec[2] = nfb;
+  rec[3] = W.applied ? esum / W.applied : 0.0;
+  rec[4] = emax;
+  rec[5] = W.unrepaired;
+  rec[6] = pairs;
+  rec[7] = 0.0;
+  for (int k = 0; k < fvx::kJudgeClasses; ++k) {
+    rec[8 + 5 * k + 0] = W.class_pairs[k];
+    rec[8 + 5 * k + 1] = W.class_samples[k];
+    rec[8 + 5 * k + 2] = W.fail_learned[k];
+    rec[8 + 5 * k + 3] = W.fail_analytic[k];
+    rec[8 + 5 * k + 4] = W.action[k];
+  }
+  for (int k = 0; k < n_out && k < n_rec; ++k) out[k] = rec[k];
   return FVX_OK;
 }
 

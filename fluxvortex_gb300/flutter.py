@@ -61,6 +61,13 @@ class FlutterConfig:
     max_particles: int = 2048
     tip_w: float = 0.05
     tip_theta_deg: float = 2.0
+    # "physical": the model above (motion velocity in the boundary condition,
+    # torque about the elastic axis, deformation at every vertex); "reference":
+    # the reference's own coupling (aeroelastic_solver.py:68-221): the station
+    # lift's moment about x = 0 with the collocation point's arm, vertices
+    # mutated per panel at its collocation span station, no motion velocity,
+    # coupling from step 1 on
+    coupling: str = "physical"
     beam: dict = field(default_factory=lambda: dict(
         length=6.096, n_elements=8, EI=9.773e6, GJ=0.988e6, m_per_length=35.72,
         Ip=35.72 * 1.8288 ** 2 / 24.0, x_ea_cg=0.10 * 1.8288, structural_damping=0.005))
@@ -132,7 +139,7 @@ class _Params(ctypes.Structure):
     _fields_ = [("n_env", ctypes.c_int), ("nc", ctypes.c_int), ("ns", ctypes.c_int),
                 ("nnodes", ctypes.c_int), ("n_keep", ctypes.c_int),
                 ("max_particles", ctypes.c_int), ("max_steps", ctypes.c_int),
-                ("pad0", ctypes.c_int),
+                ("coupling", ctypes.c_int),
                 ("x_ea", ctypes.c_double), ("rc0", ctypes.c_double), ("nu", ctypes.c_double),
                 ("rho", ctypes.c_double), ("dt", ctypes.c_double), ("beta", ctypes.c_double),
                 ("gamma", ctypes.c_double), ("pad1", ctypes.c_double)] + [
@@ -143,7 +150,10 @@ class _Params(ctypes.Structure):
 class _State(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in (
         "d", "v", "a", "W", "wgam", "wage", "nrows", "ppos", "palp", "psig", "phead", "pcount",
-        "gprev", "has_prev", "hist_w", "hist_th", "step")]
+        "gprev", "has_prev", "hist_w", "hist_th", "step", "gd", "hist_nodes")]
+
+
+COUPLINGS = {"physical": 0, "reference": 1}
 
 
 def deform_vertices(cfg, beam, d, base=None):
@@ -169,7 +179,7 @@ class FlutterSweep:
     histories on the host."""
 
     def __init__(self, cfg: FlutterConfig, velocities, precision="f64", threads=None,
-                 device="cuda"):
+                 device="cuda", node_histories=False):
         import torch
         from . import _capi
         from .geometry import lattice
@@ -204,16 +214,22 @@ class FlutterSweep:
         k = self._keep
         self.params = _Params(
             n_env=E, nc=nc, ns=ns, nnodes=beam.nnodes, n_keep=cfg.n_keep,
-            max_particles=cfg.max_particles, max_steps=self.max_steps, pad0=0,
+            max_particles=cfg.max_particles, max_steps=self.max_steps,
+            coupling=COUPLINGS[cfg.coupling],
             x_ea=cfg.x_ea * cfg.chord, rc0=cfg.rc0, nu=cfg.nu, rho=cfg.rho, dt=cfg.dt,
             beta=NEWMARK_BETA, gamma=NEWMARK_GAMMA, pad1=0.0,
             base_verts=k["base"].data_ptr(), vert_node=k["vn"].data_ptr(),
             vert_xi=k["vx"].data_ptr(), station_node=k["sn"].data_ptr(),
             station_xi=k["sx"].data_ptr(), kinv=k["kinv"].data_ptr(), mr=k["mr"].data_ptr(),
             cr=k["cr"].data_ptr(), u_inf=k["u"].data_ptr(), n_steps=k["ns"].data_ptr())
-        # initial state: tip perturbation, a0 = M^-1 (-K d0), first wake row at the TE
+        if cfg.coupling not in COUPLINGS:
+            raise ValueError(f"coupling must be one of {sorted(COUPLINGS)}, not {cfg.coupling!r}")
+        # initial state: tip perturbation, a0 = M^-1 (-K d0), first wake row at
+        # the TE (of the undeformed wing with the reference's coupling, which
+        # shapes the wing from the first coupling on)
         d0, v0, a0 = beam.initial_state(cfg.tip_w, np.radians(cfg.tip_theta_deg))
-        te = lattice(deform_vertices(cfg, beam, d0, base)).te_back
+        te = lattice(base if cfg.coupling == "reference"
+                     else deform_vertices(cfg, beam, d0, base)).te_back
         ndof = beam.ndof
         Pm = cfg.max_particles
         self._init = dict(d=np.tile(d0, (E, 1)), v=np.tile(v0, (E, 1)), a=np.tile(a0, (E, 1)),
@@ -225,7 +241,10 @@ class FlutterSweep:
                        wage=z(E, cfg.n_keep + 1), nrows=zi(E), ppos=z(E, Pm, 3),
                        palp=z(E, Pm, 3), psig=z(E, Pm), phead=zi(E), pcount=zi(E),
                        gprev=z(E, P), has_prev=zi(E), hist_w=z(E, self.max_steps),
-                       hist_th=z(E, self.max_steps), step=zi(E))
+                       hist_th=z(E, self.max_steps), step=zi(E), gd=z(E, ndof))
+        if node_histories:
+            # every beam node's heave and twist per recorded step
+            self.st["hist_nodes"] = z(E, self.max_steps, beam.nnodes, 2)
         self.state = _State(**{n: t.data_ptr() for n, t in self.st.items()})
         self._graph = None
         self.reset()
@@ -294,10 +313,22 @@ class FlutterSweep:
         self._graph.replay()
 
     def histories(self):
+        """Tip heave and twist per environment: one sample per step, or with
+        the reference's coupling one per coupled step (n_steps - 2)."""
         w = self.st["hist_w"].cpu().numpy()
         th = self.st["hist_th"].cpu().numpy()
-        return ([w[e, :self.steps[e]] for e in range(len(self.V))],
-                [th[e, :self.steps[e]] for e in range(len(self.V))])
+        n = self.steps - (2 if self.cfg.coupling == "reference" else 0)
+        return ([w[e, :n[e]] for e in range(len(self.V))],
+                [th[e, :n[e]] for e in range(len(self.V))])
+
+    def node_histories(self, env):
+        """(w, theta) of every beam node per recorded step of environment
+        ``env``: two (steps, nnodes) arrays (needs node_histories=True)."""
+        if "hist_nodes" not in self.st:
+            raise ValueError("the sweep was made without node_histories=True")
+        n = int(self.steps[env]) - (2 if self.cfg.coupling == "reference" else 0)
+        h = self.st["hist_nodes"][env, :n].cpu().numpy()
+        return h[..., 0].copy(), h[..., 1].copy()
 
     def sigma(self):
         w, _ = self.histories()

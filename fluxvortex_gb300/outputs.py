@@ -10,11 +10,12 @@
 - Particle snapshots: pos, alpha, sigma, age of the live particles and the
   time, one ``.npz`` per snapshot.
 - Flutter sweeps: the tip heave / twist histories of every airspeed with the
-  airspeeds, time step, growth rates and flutter speed.  The reference's
-  figures/flutter_data.npz holds all nine beam nodes at two airspeeds
-  (tests/animate_flutter.py:161); the device sweep records the tip only (what
-  the envelope growth rate needs), so its keys are named ``w_tip_<V>`` and
-  ``theta_tip_<V>`` instead of ``w_stable`` / ``w_flutter``.
+  airspeeds, time step, growth rates and flutter speed (``save_flutter_tips``);
+  and the layout of the reference's figures/flutter_data.npz
+  (tests/animate_flutter.py:161-168, ``save_flutter_data``): every beam node's
+  heave and twist per recorded step at a stable and a fluttering airspeed,
+  ``w_stable``, ``theta_stable``, ``w_flutter``, ``theta_flutter`` (steps x
+  nodes), the nodes' span stations ``y_nodes`` and the time step ``dt``.
 """
 from __future__ import annotations
 
@@ -83,3 +84,26 @@ def save_flutter_tips(path, sweep):
         out[f"w_tip_{V:.1f}"] = np.asarray(a, dtype=np.float64)
         out[f"theta_tip_{V:.1f}"] = np.asarray(b, dtype=np.float64)
     np.savez(path, **out)
+
+
+def save_flutter_data(path, sweep, v_stable, v_flutter):
+    """The reference's flutter_data.npz layout from a FlutterSweep made with
+    node_histories=True: the environments whose airspeeds are nearest
+    ``v_stable`` and ``v_flutter``."""
+    V = np.asarray(sweep.V, dtype=np.float64)
+    es = int(np.argmin(np.abs(V - v_stable)))
+    ef = int(np.argmin(np.abs(V - v_flutter)))
+    ws, ts = sweep.node_histories(es)
+    wf, tf = sweep.node_histories(ef)
+    np.savez_compressed(path, w_stable=ws, theta_stable=ts, w_flutter=wf, theta_flutter=tf,
+                        y_nodes=np.asarray(sweep.beam.y_nodes, dtype=np.float64),
+                        dt=np.float64(sweep.cfg.dt))
+
+
+def load_flutter_data(path):
+    """The two histories of a flutter_data.npz as the reference's animation
+    reads them: {"stable"|"flutter": {w_history, theta_history, y_nodes, dt}}."""
+    with np.load(path, allow_pickle=False) as z:
+        y, dt = z["y_nodes"], float(z["dt"])
+        return {tag: {"w_history": z[f"w_{tag}"], "theta_history": z[f"theta_{tag}"],
+                      "y_nodes": y, "dt": dt} for tag in ("stable", "flutter")}

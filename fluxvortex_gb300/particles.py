@@ -66,9 +66,10 @@ class VortexParticleField:
         # at other targets stay direct.
         self.tree = None
         self.far_field = far_field or "direct"
-        # per-step FP64 validation of the local-expansion far field: pairs
-        # checked on the step's first velocity sweep and the expansion error
-        # above which a checked cluster is summed directly in FP64 instead
+        # the per-step FP64 judge of the local-expansion far field: pairs
+        # judged on the step's first velocity and stretching sweeps, and the
+        # expansion error above which a pair counts as failed (see
+        # TreeSweeper.set_validation)
         self.validate_samples = 256
         self.validate_tol = 0.1
         self._validate_next = False
@@ -223,7 +224,7 @@ class VortexParticleField:
                 self.sweep_events.append((mode, "tree/" + (kernel or self.kernel), n_tgt, n,
                                           ev[0], ev[1]))
                 local = self.far_field in ("m2l", "learned")
-                val = self.tree.last_validation() if local else None
+                val = self.tree.last_judge() if local and self._validate_next else None
                 self.tree_events.append((mode, kernel or self.kernel, stats.copy(),
                                          self.tree.last_eval_ms(),
                                          self.tree.last_local_ms() if local else 0.0,
@@ -273,8 +274,9 @@ class VortexParticleField:
             inf_fn = None
         for stage, (a, b) in enumerate(RK3_COEFFS):
             if free_wake:
-                # the FP64 judge of the local-expansion far field runs once per
-                # step, on the first velocity sweep
+                # the FP64 judge of the local-expansion far field runs on the
+                # step's first velocity and first stretching sweeps; the sweeps
+                # in between keep its per-class decisions
                 self._validate_next = stage == 0
                 self._sweep(_capi.PAIR_VELOCITY, self._pos, None, n, self._u)
                 self._validate_next = False
@@ -289,7 +291,9 @@ class VortexParticleField:
                 self._rk_X.data_ptr(), st))
             self._pos_version += 1
             if stretch:
+                self._validate_next = stage == 0
                 self._sweep(_capi.PAIR_STRETCH, self._pos, self._gamma, n, self._S)
+                self._validate_next = False
                 _capi.check(lib.fvx_vpm_stage_strength(
                     n, a, b, dt, self.nu, self._S.data_ptr(), self._gamma.data_ptr(),
                     self._sigma.data_ptr(), self._rk_G.data_ptr(), self._rk_s.data_ptr(), st))

@@ -88,17 +88,40 @@ class TreeSweeper:
         _capi.check(self.lib.fvx_tree_set_list_slots(self.handle, int(near), int(lrn), int(par)))
 
     def set_validation(self, samples=256, tol=0.1):
-        """Per-sweep FP64 validation of the local-expansion path: ``samples``
-        strided (leaf, cell) pairs per sweep; a pair whose expansion error
-        exceeds ``tol`` is summed directly in FP64 instead (samples=0: off)."""
+        """The FP64 judge of the local-expansion path for the next sweeps:
+        ``samples`` pairs per judged sweep, stratified over the 16 pair classes
+        (list x cell larger than target x opening-ratio bin); per class the
+        network is kept, dropped, or the whole class is summed directly in FP64,
+        and sampled pairs above ``tol`` are summed directly in FP64
+        (fvx_tree_set_validation).  samples=0: the next sweeps are not judged
+        and keep the last judged sweep's class decisions."""
         _capi.check(self.lib.fvx_tree_set_validation(self.handle, int(samples), float(tol)))
 
     def last_validation(self):
-        """{checked, fallback, mean_err, max_err} of the last sweep."""
-        out = np.zeros(4, dtype=np.float64)
-        _capi.check(self.lib.fvx_tree_last_validation(self.handle, out.ctypes.data))
-        return {"checked": int(out[0]), "fallback": int(out[1]), "mean_err": float(out[2]),
-                "max_err": float(out[3])}
+        """{checked, fallback, mean_err, max_err} of the last judged sweep
+        (fallback: pairs summed directly in FP64, whole classes included)."""
+        j = self.last_judge()
+        return {"checked": j["checked"], "fallback": j["fp64_pairs"], "mean_err": j["mean_err"],
+                "max_err": j["max_err"]}
+
+    JUDGE_ACTIONS = ("network", "translation", "fp64")
+
+    def last_judge(self):
+        """The full record of the last judged sweep (fvx_tree_last_judge):
+        pairs judged and repaired, pairs summed directly in FP64, mean / max
+        applied error, the estimated fraction of the path's pairs left above
+        the tolerance, and per class its pairs, samples, failures with and
+        without the network and the action taken."""
+        out = np.zeros(8 + 5 * 16, dtype=np.float64)
+        _capi.check(self.lib.fvx_tree_last_judge(self.handle, out.ctypes.data, out.size))
+        cls = out[8:].reshape(16, 5)
+        return {"checked": int(out[0]), "repaired": int(out[1]), "fp64_pairs": int(out[2]),
+                "mean_err": float(out[3]), "max_err": float(out[4]),
+                "unrepaired_est": float(out[5]), "pairs": int(out[6]),
+                "classes": [{"class": k, "pairs": int(c[0]), "samples": int(c[1]),
+                             "fail_network": int(c[2]), "fail_translation": int(c[3]),
+                             "action": self.JUDGE_ACTIONS[int(c[4])]}
+                            for k, c in enumerate(cls) if c[0] > 0]}
 
     def last_local_ms(self):
         ms = ctypes.c_float(0.0)

@@ -228,16 +228,37 @@ int fvx_tree_last_eval_ms(fvx_tree* tree, float* ms);
 int fvx_tree_set_far_field(fvx_tree* tree, int method, const void* W, const float* b,
                            double theta_local);
 int fvx_tree_last_local_ms(fvx_tree* tree, float* ms);
-/* Per-sweep validation of the local-expansion path (on by default: 256
- * samples, tol 0.1).  Every sweep with FVX_FAR_M2L or FVX_FAR_LEARNED sums
- * `samples` evenly strided (leaf, cell) pairs of its list directly in FP64 at
- * the leaf centre and compares their expansions with it; the error is that
- * of the expansion across the leaf, e = (|du| + rho |dJ| + rho^2/2 |dH|) /
- * (|u| + rho |J| + rho^2/2 |H|), rho = sqrt(3)/2 h_T/d.  A pair with e > tol
- * leaves the expansion path: its cell is summed directly in FP64 at every
- * target particle of its leaf.  samples = 0 turns validation off.
- * fvx_tree_last_validation: out[4] = pairs checked, pairs sent to the FP64
- * fallback, mean e, max e of the last sweep (waits for it). */
+/* The FP64 judge of the local-expansion path and its FP64 fallback (new; no
+ * reference counterpart).  A sweep with FVX_FAR_M2L or FVX_FAR_LEARNED is
+ * judged when `samples` > 0.  Every (target, cell) pair of the path falls in
+ * one of 16 classes: its list (leaves' own pairs / pairs shared through
+ * parents of leaves) x whether the cell is larger than the target x four bins
+ * of the opening ratio mu = sqrt(3)/2 (h_T + h_S)/d against theta_local
+ * (mu/theta >= 0.9, 0.8, 0.65, below).  A judged sweep samples each class
+ * (samples/16 pairs per class, drawn at random anew every judged sweep, all
+ * pairs of smaller classes), sums each sampled cell directly in FP64 at its
+ * target's centre, and runs the sweep's own translation and network kernels
+ * on the samples.  The error of an expansion is that across the target,
+ * e = (|du| + rho |dJ| + rho^2/2 |dH|) / (|u| + rho |J| + rho^2/2 |H|), rho =
+ * sqrt(3)/2 h_T/d, for the translation plus the network (e_l) and the
+ * translation alone (e_a).  Per class, with f the fraction of its samples
+ * whose e exceeds tol: f_l <= 1/4 keeps the network; else f_a <= 1/4 drops the
+ * network for the class (translation alone); else every pair of the class is
+ * summed directly in FP64 at every particle of its target.  Sampled pairs of
+ * the expanded classes whose applied e exceeds tol are summed directly in
+ * FP64 as well.  The decision is kept per sweep mode for the sweeps that are
+ * not judged (samples = 0), until the next judged sweep; a new far-field
+ * method starts with every class expanded.  Defaults: 256 samples, tol 0.1.
+ * fvx_tree_last_validation: out[4] = pairs judged, pairs summed directly in
+ * FP64, mean applied e, max applied e of the last judged sweep (waits for it).
+ * fvx_tree_last_judge: the full record of the last judged sweep, up to n_out
+ * doubles of: [0] pairs judged, [1] sampled pairs repaired, [2] pairs summed
+ * directly in FP64 (whole classes + repairs), [3] mean and [4] max applied
+ * e, [5] estimated fraction of the path's pairs left above tol (sum over the
+ * expanded classes of n_k f_k / sum n_k), [6] pairs on the path, [7] 0, then
+ * per class k = 0..15 five values at 8 + 5k: pairs, samples, samples with
+ * e_l > tol, samples with e_a > tol, action (0 network, 1 translation alone,
+ * 2 FP64 direct).  Class k = 8 list + 4 (cell larger) + distance bin. */
 int fvx_tree_set_validation(fvx_tree* tree, int samples, double tol);
 /* fvx_tree_hint_same_positions: the next sweep's particle positions are those
  * of the last full build (the caller has not moved them): the grid, sort,
@@ -252,6 +273,7 @@ int fvx_tree_hint_same_positions(fvx_tree* tree);
  * a slot overflow falls back to counting; any 0 = always count. */
 int fvx_tree_set_list_slots(fvx_tree* tree, int near, int lrn, int par);
 int fvx_tree_last_validation(fvx_tree* tree, double* out);
+int fvx_tree_last_judge(fvx_tree* tree, double* out, int n_out);
 int fvx_tree_sample_pairs(fvx_tree* tree, int list, int max_pairs, void* X, float* T, float* A,
                           int* n_out, void* stream);
 
@@ -404,8 +426,17 @@ int fvx_vpm_merge_pass(int64_t n, double* pos, double* alpha, double* sigma, dou
  * wage[E][n_keep+1], nrows[E] (int); ppos, palp [E][max_particles][3],
  * psig[E][max_particles], phead, pcount [E] (int); gprev[E][nc ns],
  * has_prev[E] (int); hist_w, hist_th [E][max_steps]; step[E] (int). */
+/* coupling: 0 = the physical model (motion velocity in the boundary
+ * condition and the loads, torque about the elastic axis, deformation at every
+ * vertex); 1 = the reference's coupling (aeroelastic_solver.py:68-221): every
+ * panel moved with the beam's heave and twist at its collocation span station
+ * (corners, ring vertices, collocation height), no motion velocity, station
+ * lift and its moment about x = 0 with the collocation point's chordwise
+ * position as the arm, the beam coupled from step 1 to the step before the
+ * last, each coupling's displacements shaping the next step (state.gd);
+ * hist_* then hold n_steps - 2 entries. */
 typedef struct FlutterParams {
-  int n_env, nc, ns, nnodes, n_keep, max_particles, max_steps, pad0;
+  int n_env, nc, ns, nnodes, n_keep, max_particles, max_steps, coupling;
   double x_ea, rc0, nu, rho, dt, beta, gamma, pad1;
   const double* base_verts;
   const int* vert_node;
@@ -428,6 +459,10 @@ typedef struct FlutterState {
   int* has_prev;
   double *hist_w, *hist_th;
   int* step;
+  double* gd;  /* coupling 1: the displacements that shape the geometry */
+  /* optional (NULL: tip only): every node's (w, theta) per recorded step,
+   * [env][max_steps][nnodes][2] */
+  double* hist_nodes;
 } FlutterState;
 int fvx_flutter_sweep(const FlutterParams* params, const FlutterState* state, int step_end,
                       int precision, int threads, void* stream);
@@ -446,8 +481,9 @@ int fvx_flutter_sweep(const FlutterParams* params, const FlutterState* state, in
  * fvx_mlp_forward: Y[rows][32] FP32 from X[rows][48] BF16; z_store
  *   (3 x rows x 128 FP32) and h_store (3 x rows x 128 BF16), if not NULL,
  *   receive the hidden pre-activations and activations for training.  With
- *   both NULL (inference) the kernel runs the treecode far field's F16 form:
- *   weights converted to F16 in shared memory, F16 hidden activations.
+ *   both NULL (inference) the kernel runs the treecode far field's form: BF16
+ *   operands, the hidden layers' weights and biases halved while staged in
+ *   shared memory, each pair of SiLUs one packed BF16 add, tanh and FMA.
  * fvx_mlp_gemm: C[M][N] (+)= sum_k opA[m][k] opB[n][k], opA[m][k] = tA ?
  *   A[k*lda + m] : A[m*lda + k] (same for B), BF16 in, FP32 out, split over K
  *   into split_k slices added with atomics (accumulate != 0 adds into C).

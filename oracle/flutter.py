@@ -28,7 +28,7 @@ import math
 import numpy as np
 
 from fluxvortex_gb300.flutter import FlutterConfig
-from fluxvortex_gb300.geometry import lattice
+from fluxvortex_gb300.geometry import Lattice, lattice
 from oracle import oracle as O
 from oracle.beam import Beam, distribute
 
@@ -45,6 +45,46 @@ def lattice_point_velocities(vel):
     return col, leg
 
 
+def reference_panels(cfg, base, L0, w_nodes, th_nodes, y_nodes):
+    """The reference's panel deformation (aeroelastic_solver.py:150-221): every
+    panel moves with the beam's heave w and twist theta interpolated at its own
+    collocation span station |y_c| (no shared vertices: neighbouring panels
+    move apart at their common edges).  Each of its corners and ring-vortex
+    vertices moves by dz = w - (x - x_ea) sin(theta), dx = (x - x_ea)
+    (cos(theta) - 1) (theta nose-up here; the reference counts it nose-down,
+    dz = w + (x - x_ea) sin(theta_ref)); the collocation point by dz only.
+    Normals and areas follow from the moved corners.  The wake's first vertex
+    row is the back row of the last chordwise panels' rings (strip j's
+    back-left vertex, the last strip's back-right vertex)."""
+    nc, ns = cfg.nc, cfg.ns
+    x_ea = cfg.x_ea * cfg.chord
+    yc = np.abs(L0.colloc[:, 1])
+    w = np.interp(yc, y_nodes, w_nodes)
+    th = np.interp(yc, y_nodes, th_nodes)
+    s, c1 = np.sin(th)[:, None], (np.cos(th) - 1.0)[:, None]
+
+    def move(p):
+        xr = p[:, 0:1] - x_ea
+        out = p.copy()
+        out[:, 0:1] += xr * c1
+        out[:, 2:3] += w[:, None] - xr * s
+        return out
+
+    i, j = np.divmod(np.arange(nc * ns), ns)
+    c00, c01 = move(base[i, j]), move(base[i, j + 1])
+    c10, c11 = move(base[i + 1, j]), move(base[i + 1, j + 1])
+    cr = np.cross(c11 - c00, c01 - c10)
+    nrm = np.linalg.norm(cr, axis=1)
+    br, fr, fl, bl = move(L0.br), move(L0.fr), move(L0.fl), move(L0.bl)
+    colloc = L0.colloc.copy()
+    colloc[:, 2] += w - (colloc[:, 0] - x_ea) * np.sin(th)
+    last = np.arange((nc - 1) * ns, nc * ns)
+    te = np.vstack([bl[last], br[last[-1]][None]])
+    return Lattice(br=br, fr=fr, fl=fl, bl=bl, colloc=colloc, normal=cr / nrm[:, None],
+                   area=0.5 * nrm, leg_center=0.5 * (fr + fl), leg_vec=fl - fr, te_back=te,
+                   nc=nc, ns=ns)
+
+
 class FlutterOracle:
     def __init__(self, cfg: FlutterConfig, V):
         self.cfg = cfg
@@ -57,8 +97,18 @@ class FlutterOracle:
         self.beam.d[3 * tip + 2] = math.radians(cfg.tip_theta_deg)
         self.beam.init_acceleration()
         self.ns = cfg.ns
-        verts, _ = self.deform()
-        self.W = lattice(verts).te_back[None].copy()
+        self.reference = cfg.coupling == "reference"
+        if self.reference:
+            # the reference couples from step 1 on and applies each coupling's
+            # deformation to the next step's geometry: steps 0 and 1 run on
+            # the undeformed wing (aeroelastic_solver.py:63-66, :108-110)
+            self.L0 = lattice(self.base)
+            self.geom_d = np.zeros_like(self.beam.d)
+            self.n_total = cfg.n_steps(V)
+            self.W = self._ref_lattice(self.geom_d).te_back[None].copy()
+        else:
+            verts, _ = self.deform()
+            self.W = lattice(verts).te_back[None].copy()
         self.wgam = np.zeros((0, cfg.ns))
         self.wage = np.zeros(0)
         self.p_pos = np.zeros((0, 3))
@@ -85,6 +135,10 @@ class FlutterOracle:
         vel[..., 2] = wd - xr * np.cos(th) * thd
         return verts, vel
 
+    def _ref_lattice(self, d):
+        b = self.beam
+        return reference_panels(self.cfg, self.base, self.L0, d[0::3], d[2::3], b.y_nodes)
+
     def _rings(self):
         W, R, ns = self.W, self.wgam.shape[0], self.ns
         if R == 0:
@@ -108,9 +162,15 @@ class FlutterOracle:
 
     def step(self):
         cfg = self.cfg
-        verts, vel = self.deform()
-        L = lattice(verts)
-        v_col, v_leg = lattice_point_velocities(vel)
+        if self.reference:
+            # vertices mutated only: no motion velocity in the boundary
+            # condition or the loads
+            L = self._ref_lattice(self.geom_d)
+            v_col = v_leg = np.zeros((L.colloc.shape[0], 3))
+        else:
+            verts, vel = self.deform()
+            L = lattice(verts)
+            v_col, v_leg = lattice_point_velocities(vel)
         P = L.colloc.shape[0]
         rc_b = np.full(P, cfg.rc0)
         E = O.expanded_velocities_from_ring_vortices(L.colloc, L.br, L.fr, L.fl, L.bl,
@@ -132,17 +192,33 @@ class FlutterOracle:
         F = (cfg.rho * geff.reshape(-1)[:, None] * np.cross(V, L.leg_vec)
              - (cfg.rho * dgdt * L.area)[:, None] * L.normal)
         Fz = F[:, 2].reshape(L.nc, L.ns)
-        x_ea = cfg.x_ea * cfg.chord
-        arm = x_ea - L.leg_center[:, 0].reshape(L.nc, L.ns)
-        lift = Fz.sum(axis=0)
-        torque = (Fz * arm).sum(axis=0)
         y_st = (np.arange(L.ns) + 0.5) * cfg.semi_span / L.ns
-        self.beam.step(distribute(self.beam.y_nodes, y_st, lift, torque), cfg.dt)
-        self.tip_w.append(self.beam.d[-3])
-        self.tip_theta.append(self.beam.d[-1])
-        # wake: convect, shed at the next geometry, convert old rows
-        verts_n, _ = self.deform()
-        te = lattice(verts_n).te_back
+        if self.reference:
+            # station lift and its moment about x = 0 with the collocation
+            # point's chordwise position x_c as the arm (aeroelastic_solver.py:
+            # 126-138: lift -F_z in PteraSoftware's axes, moment x_c (-F_z)
+            # nose-down); here lift F_z and the nose-up moment -x_c F_z.
+            # Coupling from step 1 to the step before the last (:63-71); the
+            # next step's geometry from the new displacements
+            lift = Fz.sum(axis=0)
+            torque = (-self.L0.colloc[:, 0].reshape(L.nc, L.ns) * Fz).sum(axis=0)
+            if 1 <= self.k < self.n_total - 1:
+                self.beam.step(distribute(self.beam.y_nodes, y_st, lift, torque), cfg.dt)
+                self.tip_w.append(self.beam.d[-3])
+                self.tip_theta.append(self.beam.d[-1])
+                self.geom_d = self.beam.d.copy()
+            te = self._ref_lattice(self.geom_d).te_back
+        else:
+            x_ea = cfg.x_ea * cfg.chord
+            arm = x_ea - L.leg_center[:, 0].reshape(L.nc, L.ns)
+            lift = Fz.sum(axis=0)
+            torque = (Fz * arm).sum(axis=0)
+            self.beam.step(distribute(self.beam.y_nodes, y_st, lift, torque), cfg.dt)
+            self.tip_w.append(self.beam.d[-3])
+            self.tip_theta.append(self.beam.d[-1])
+            # wake: convect, shed at the next geometry, convert old rows
+            verts_n, _ = self.deform()
+            te = lattice(verts_n).te_back
         if self.p_pos.shape[0]:
             self.p_pos = self.p_pos + self.u_inf * cfg.dt
         self.W = np.concatenate([te[None], self.W + self.u_inf * cfg.dt], axis=0)

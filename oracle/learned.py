@@ -248,6 +248,24 @@ def forward(w, b, X, rounding=True):
     return Y, (Zs, Hs)
 
 
+def forward_inference(w, b, X):
+    """Y (rows, 32) of the far field's inference form, with the kernel's BF16
+    rounding points: BF16 inputs and weights, the hidden layers' weights and
+    biases halved (exact), each accumulator (z/2 - b/2, FP32 sums) rounded to
+    BF16, h = BF16(acc + BF16(b/2)), t = BF16(tanh h), the activation
+    BF16(h + h t) = SiLU(z) in one rounding; output layer BF16 weights, FP32
+    sums plus the bias.  The kernel's tanh is the hardware approximation, so
+    activations may differ by a BF16 unit in the last place."""
+    Ws, bs = unpack(w, b)
+    h = bf16(X)
+    for l in range(3):
+        acc = bf16(h @ (0.5 * bf16(Ws[l])).T)
+        hh = bf16(acc + bf16(0.5 * bs[l]))
+        t = bf16(np.tanh(hh))
+        h = bf16(hh + hh * t)
+    return h @ bf16(Ws[3]).T + bs[3]
+
+
 def gradients(w, b, X, T, rounding=True):
     """Loss sum over rows and the 30 used outputs of (Y - T)^2, and the packed
     gradients (gw, gb) of the mean loss sum / (rows * 30)."""

@@ -48,6 +48,39 @@ def _net(seed):
     return L.FarFieldMLP(w, b)
 
 
+def test_mlp_inference_form_matches_oracle(cuda):
+    """The far field's inference form (no stores: packed BF16 SiLU on halved
+    weights) against the oracle's restatement with the same BF16 rounding
+    points, with the trained weights on pair features of a slab wake; and its
+    distance from the unrounded FP64 network, the price of the BF16 form."""
+    from fluxvortex_gb300 import learned as L
+    from fluxvortex_gb300.tree import TreeSweeper
+    from fluxvortex_gb300.workloads import slab_wake
+    m = L.FarFieldMLP.load()
+    pos, gam, sig, _ = slab_wake(1 << 15, seed=31)
+    d = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")  # noqa: E731
+    ts = TreeSweeper(theta=0.5, leaf_target=32)
+    X, T, A = L.harvest(ts, d(pos), d(gam), d(sig), 1 << 15, 4000)
+    rows = X.shape[0]
+    assert rows >= 1000
+    Y = m.forward(X).cpu().numpy()
+    w, b = m.weights_numpy()
+    Xh = X.float().cpu().numpy()
+    Yo = OL.forward_inference(w, b, Xh)
+    Y64, _ = OL.forward(w, b, Xh, rounding=False)
+    scale = np.abs(Yo[:, :L.NOUT]).max()
+    err = np.abs(Y[:, :L.NOUT] - Yo[:, :L.NOUT]).max() / scale
+    e64 = np.abs(Y[:, :L.NOUT] - Y64[:, :L.NOUT]).max() / scale
+    # the residual's share of the expansion it corrects
+    share = float((torch.tensor(Y[:, :L.NOUT]).norm(dim=1)
+                   / T[:, :L.NOUT].cpu().norm(dim=1).clamp_min(1e-30)).median())
+    print(f"inference form vs oracle {err:.3e}, vs unrounded FP64 network {e64:.3e}; "
+          f"median |residual| / |expansion| {share:.3e}")
+    assert err < 2e-2, err
+    assert e64 < 5e-2, e64
+    assert _lib().status_read_and_clear() == 0
+
+
 def test_mlp_forward_matches_oracle(cuda):
     from fluxvortex_gb300 import learned as L
     m = _net(11)

@@ -1,0 +1,59 @@
+"""The metric's accuracy bar over a real run: the benchmarked form of the step
+(treecode self-sweeps with the learned far field, FP32-compensated sweeps)
+against the FP64 direct step (every sweep an FP64 all-pairs sum), both from
+the same seeded state, over one full flapping cycle (43 steps) of the large
+flapping configuration.
+
+The wake holds a seeded slab of 2^15 particles behind the tail
+(``workloads.slab_wake`` at ``AIRCRAFT_SLAB_X0``) plus the particles the three
+surfaces convert from their ring rows every step (128 per step), so the
+wing sees particles that the learned far field convected.  CL and CDi must
+stay within 1e-4 of the FP64 step, as max_k |x_k - ref_k| / max_k |ref_k|
+(the reference's tolerance convention; the flapping CL crosses zero, where a
+per-step ratio is undefined)."""
+import numpy as np
+import pytest
+
+from fluxvortex_gb300.geometry import flapping_aircraft
+from fluxvortex_gb300.hybrid import HybridStep
+from fluxvortex_gb300.workloads import AIRCRAFT_SLAB_X0, slab_wake
+from tests.conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+STEPS = 43          # one flapping cycle (period 1 s, dt = 1/43 s)
+N_SLAB = 1 << 15
+TOL = 1e-4
+
+
+def _step(far_field, precision, pos, gam, sig):
+    cfg = flapping_aircraft(n_keep=10, free_vpm=True, stretch=True, rlxf=0.0,
+                            max_particles=N_SLAB + 128 * (STEPS + 4), far_field=far_field)
+    hs = HybridStep(cfg, precision=precision)
+    if hs.field.tree is not None:
+        hs.field.tree.leaf_target = 32
+    hs.field.add_particles_batch(pos, gam, sig)
+    return hs
+
+
+def test_learned_step_cl_cdi_within_1e4_of_fp64_over_one_flapping_cycle(cuda):
+    pos, gam, sig, _ = slab_wake(N_SLAB, x0=AIRCRAFT_SLAB_X0)
+    ref = _step(None, "f64", pos, gam, sig)
+    lrn = _step("learned", "f32c", pos, gam, sig)
+    for k in range(STEPS):
+        if k == STEPS - 1:
+            lrn.field.sweep_events = []       # per-sweep tree statistics of the last step
+        ref.step()
+        lrn.step()
+    assert lrn.field.np == ref.field.np == N_SLAB + 128 * (STEPS - 10)
+    # the learned far field really ran: local-expansion pairs were formed, and
+    # the FP64 judge checked clusters
+    ev = lrn.field.tree_events
+    assert ev and all(int(e[2][4]) > 0 for e in ev)
+    assert any(e[5] and e[5]["checked"] > 0 for e in ev)
+    e_cl = rel_err(lrn.cl, ref.cl)
+    e_cdi = rel_err(lrn.cdi, ref.cdi)
+    print(f"learned vs FP64 over {STEPS} steps: CL {e_cl:.3e}, CDi {e_cdi:.3e}")
+    assert np.all(np.isfinite(lrn.cl)) and np.all(np.isfinite(lrn.cdi))
+    assert e_cl < TOL, f"CL history {e_cl:.3e}"
+    assert e_cdi < TOL, f"CDi history {e_cdi:.3e}"

@@ -35,8 +35,9 @@ def _sweep(ts, mode, P, G, S, n, tg=None):
 
 @pytest.mark.parametrize("mode", ["velocity", "stretch"])
 def test_fallback_of_every_pair_is_the_fp64_direct_sum(cuda, mode):
-    """tol ~ 0 with every pair sampled: each far pair is summed in FP64 at
-    every target, so only the FP32 near field differs from the direct sum."""
+    """tol ~ 0: every sampled pair fails, so the judge sends every class to
+    the FP64 direct sum and each far pair is summed in FP64 at every target;
+    only the FP32 near field differs from the direct sum."""
     from fluxvortex_gb300 import _capi
     from fluxvortex_gb300.tree import TreeSweeper
     m = _capi.PAIR_VELOCITY if mode == "velocity" else _capi.PAIR_STRETCH
@@ -51,10 +52,87 @@ def test_fallback_of_every_pair_is_the_fp64_direct_sum(cuda, mode):
     ts.set_validation(samples=65536, tol=1e-30)
     out, stats = _sweep(ts, m, P, G, S, n, tg)
     v = ts.last_validation()
-    assert v["checked"] == int(stats[4]) > 0 and v["fallback"] == v["checked"]
+    assert 0 < v["checked"] <= int(stats[4]) and v["fallback"] == int(stats[4])
+    j = ts.last_judge()
+    assert j["pairs"] == int(stats[4]) and j["unrepaired_est"] == 0.0
+    assert all(c["action"] == "fp64" for c in j["classes"] if c["samples"])
     e_fb = float((out - ref).abs().max() / ref.abs().max())
     e_tree = float((out_tree - ref).abs().max() / ref.abs().max())
     assert e_fb < 2e-5 and e_fb < 0.2 * e_tree, (e_fb, e_tree)
+    assert _capi.status_read_and_clear() == 0
+
+
+@pytest.mark.parametrize("mode", ["velocity", "stretch"])
+def test_judge_repairs_a_biased_network(cuda, mode):
+    """Fault injection on the host: the network's output biases are shifted
+    (a perturbation of its weights before they reach the device), so every
+    learned expansion is wrong.  Unjudged, the sweep's error is far above the
+    analytic path's; judged, every class's samples fail with the network and
+    pass without it, the judge drops the network for them, and the sweep is
+    as accurate as the analytic path again."""
+    from fluxvortex_gb300 import _capi, learned as L
+    from fluxvortex_gb300.tree import TreeSweeper
+    from fluxvortex_gb300.workloads import slab_wake
+    m = _capi.PAIR_VELOCITY if mode == "velocity" else _capi.PAIR_STRETCH
+    n = 1 << 15
+    pos, alpha, sigma, _ = slab_wake(n, seed=91)
+    P, G, S = _dev(pos), _dev(alpha), _dev(sigma)
+    tg = G if mode == "stretch" else None
+    ref = _direct(m, P, G, S, tg)
+    good = L.FarFieldMLP.load()
+    w, b = good.weights_numpy()
+    b = b.copy()
+    b[3 * L.HID:3 * L.HID + L.NOUT] += 0.5          # output layer, normalised units
+    bad = L.FarFieldMLP(good.w32.cpu().numpy(), b)
+
+    def run(method, mlp, samples):
+        ts = TreeSweeper(theta=0.5, leaf_target=32)
+        ts.set_far_field(method, mlp=mlp)
+        ts.set_validation(samples, 0.1)
+        out, _ = _sweep(ts, m, P, G, S, n, tg)
+        return float((out - ref).abs().max() / ref.abs().max()), ts
+
+    e_m2l, _ = run("m2l", None, 0)
+    e_bad, _ = run("learned", bad, 0)
+    e_fix, ts = run("learned", bad, 256)
+    j = ts.last_judge()
+    print(f"{mode}: analytic {e_m2l:.3e}, biased network unjudged {e_bad:.3e}, judged "
+          f"{e_fix:.3e}; actions {[c['action'] for c in j['classes']]}")
+    assert e_bad > 20 * e_m2l
+    sampled = [c for c in j["classes"] if c["samples"]]
+    assert sampled and all(c["fail_network"] > c["samples"] // 4 for c in sampled)
+    assert all(c["action"] != "network" for c in sampled)
+    assert e_fix < 1.5 * e_m2l + 1e-6
+    assert j["unrepaired_est"] < 0.1
+    assert _capi.status_read_and_clear() == 0
+
+
+def test_judge_record_of_the_trained_network(cuda):
+    """With the trained network the judge keeps it for the classes it passes:
+    the record covers every class of the sweep, and the estimated fraction of
+    pairs above the tolerance is small."""
+    from fluxvortex_gb300 import _capi, learned as L
+    from fluxvortex_gb300.tree import TreeSweeper
+    from fluxvortex_gb300.workloads import slab_wake
+    n = 1 << 16
+    pos, alpha, sigma, _ = slab_wake(n, seed=93)
+    P, G, S = _dev(pos), _dev(alpha), _dev(sigma)
+    ts = TreeSweeper(theta=0.5, leaf_target=32)
+    ts.set_far_field("learned", mlp=L.FarFieldMLP.load())
+    ts.set_validation(512, 0.1)
+    _, stats = _sweep(ts, _capi.PAIR_VELOCITY, P, G, S, n)
+    j = ts.last_judge()
+    assert j["pairs"] == int(stats[4]) > 0
+    assert sum(c["pairs"] for c in j["classes"]) == j["pairs"]
+    assert j["checked"] == sum(c["samples"] for c in j["classes"])
+    # every class with pairs was sampled, at most 2 x 32 samples each
+    assert all(0 < c["samples"] <= 64 for c in j["classes"])
+    assert j["unrepaired_est"] < 0.05
+    assert sum(c["action"] == "network" for c in j["classes"]) >= len(j["classes"]) // 2
+    print("judge:", {k: j[k] for k in ("checked", "repaired", "fp64_pairs", "mean_err",
+                                       "max_err", "unrepaired_est", "pairs")})
+    for c in j["classes"]:
+        print("  ", c)
     assert _capi.status_read_and_clear() == 0
 
 

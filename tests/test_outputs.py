@@ -43,3 +43,33 @@ def test_flutter_tips_and_particle_snapshot(tmp_path):
     OUT.save_particles(str(tmp_path / "p.npz"), field, t=0.5)
     p = np.load(tmp_path / "p.npz", allow_pickle=False)
     assert int(p["np"]) == 3 and float(p["t"]) == 0.5 and p["pos"].shape == (3, 3)
+
+
+def test_flutter_data_layout_round_trip(tmp_path):
+    """save_flutter_data writes the reference's figures/flutter_data.npz
+    layout (tests/animate_flutter.py:161-168): per-node (steps x nodes) heave
+    and twist at a stable and a fluttering airspeed, y_nodes, dt.  The
+    reference's file (60 chords at 100 and 160 m/s, its coupling records
+    n_steps - 2 steps) holds (364, 9) and (227, 9) arrays."""
+    from fluxvortex_gb300.flutter import goland
+    cfg = goland(num_chords=60.0, coupling="reference")
+    steps = {100.0: cfg.n_steps(100.0) - 2, 160.0: cfg.n_steps(160.0) - 2}
+    assert steps == {100.0: 364, 160.0: 227}
+    y = np.linspace(0.0, 6.096, 9)
+    hist = {e: (np.random.default_rng(e).standard_normal((n, 9)),
+                np.random.default_rng(10 + e).standard_normal((n, 9)))
+            for e, n in enumerate(steps.values())}
+    sweep = types.SimpleNamespace(V=np.array([100.0, 160.0]), cfg=cfg,
+                                  beam=types.SimpleNamespace(y_nodes=y),
+                                  node_histories=lambda e: hist[e])
+    OUT.save_flutter_data(str(tmp_path / "flutter_data.npz"), sweep, 100.0, 160.0)
+    z = np.load(tmp_path / "flutter_data.npz", allow_pickle=False)
+    assert sorted(z.files) == sorted(["w_stable", "theta_stable", "w_flutter", "theta_flutter",
+                                      "y_nodes", "dt"])
+    assert z["w_stable"].shape == z["theta_stable"].shape == (364, 9)
+    assert z["w_flutter"].shape == z["theta_flutter"].shape == (227, 9)
+    assert z["y_nodes"].shape == (9,) and float(z["dt"]) == 0.003
+    d = OUT.load_flutter_data(str(tmp_path / "flutter_data.npz"))
+    assert np.array_equal(d["stable"]["w_history"], hist[0][0])
+    assert np.array_equal(d["flutter"]["theta_history"], hist[1][1])
+    assert np.array_equal(d["flutter"]["y_nodes"], y) and d["stable"]["dt"] == 0.003
