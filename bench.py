@@ -53,8 +53,8 @@ FLOP_PER_PAIR = {
     ("stretch", "gaussianerf"): 67,
 }
 WORKLOAD = ("VPM+panel step: flapping NACA2412 wing + NACA0012 V-tail, 3 surfaces, 192 panels "
-            "+ {n} seeded wake particles, RK3 free wake with stretching on, Pedrizzetti "
-            "relaxation off")
+            "+ {n} seeded wake particles (cores 1.3 x spacing), RK3 free wake with stretching "
+            "on, Pedrizzetti relaxation off, converted cores 1.3 x mean ring edge")
 # Algorithmic flop of one far-field (target particle, cell) evaluation of the
 # treecode's quadrupole expansion (same counting convention).
 M2P_FLOP = {"velocity": 166, "stretch": 355, "vorticity": 300}
@@ -113,7 +113,8 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=5,
                    help="steps of the end-to-end measurement (0: off)")
     p.add_argument("--relax-steps", type=int, default=3,
-                   help="timed steps of the variant with the Pedrizzetti relaxation (0: off)")
+                   help="timed steps of each variant of the step: with the Pedrizzetti "
+                        "relaxation, and without the stretching term (0: off)")
     p.add_argument("--no-baselines", action="store_true")
     p.add_argument("--sweep-case", action="store_true",
                    help="instead of the step: one treecode velocity + stretching sweep pair of "
@@ -224,14 +225,21 @@ class Step:
     and stretching (3 velocity + 3 stretching sweeps over all particles)."""
 
     def __init__(self, n, precision, device, steps_hint=64, far_field="direct", leaf=64,
-                 rlxf=0.0):
+                 rlxf=0.0, stretch=True):
         import torch
         from fluxvortex_gb300.geometry import flapping_aircraft
         from fluxvortex_gb300.hybrid import HybridStep
-        from fluxvortex_gb300.workloads import AIRCRAFT_SLAB_X0, slab_wake
-        pos, gam, sig, colloc = slab_wake(n, x0=AIRCRAFT_SLAB_X0)
+        from fluxvortex_gb300.workloads import AIRCRAFT_SLAB_X0, resolved_core, slab_wake
+        # the seeded slab stands in for the grown wake: cores of 1.3 x the
+        # particle spacing, like the converted particles' (resolved_core)
+        pos, gam, sig, colloc = slab_wake(n, x0=AIRCRAFT_SLAB_X0, sigma=resolved_core(n))
         self.host = dict(pos=pos, gamma=gam, sigma=sig, colloc=colloc)
-        self.cfg = flapping_aircraft(n_keep=10, free_vpm=True, stretch=True, rlxf=rlxf,
+        # converted particles take the core 1.3 x the ring's mean edge, the
+        # hybrid configurations' rule (the core |V| dt sits below the particle
+        # spacing, and the converted wake is then chaotic: a 1e-12 change of
+        # the state reaches the CL history within a cycle)
+        self.cfg = flapping_aircraft(n_keep=10, free_vpm=True, stretch=stretch, rlxf=rlxf,
+                                     sigma_rule="edge",
                                      max_particles=n + 128 * (steps_hint + 8),
                                      far_field=None if far_field == "direct" else far_field)
         self.hs = HybridStep(self.cfg, precision=precision, device=device)
@@ -413,8 +421,8 @@ def max_over_ranks(value, world, device=None):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    from fluxvortex_gb300.workloads import AIRCRAFT_SLAB_X0, slab_wake
-    pos, gam, sig, colloc = slab_wake(args.n, x0=AIRCRAFT_SLAB_X0)
+    from fluxvortex_gb300.workloads import AIRCRAFT_SLAB_X0, resolved_core, slab_wake
+    pos, gam, sig, colloc = slab_wake(args.n, x0=AIRCRAFT_SLAB_X0, sigma=resolved_core(args.n))
     host = dict(pos=pos, gamma=gam, sigma=sig)
     cores = os.cpu_count() or 1
     n_t = max(16, int(64 * (1 << 20) / args.n))
@@ -428,6 +436,19 @@ def run_reference(args, rank, world):
     v = 1.0 / step_s
     sample = (f"{n_t} targets x {args.n} sources per sweep kind (velocity, velocity+stretching),"
               f" scaled to the full step by N/targets")
+    # the reference's own NumPy particle path (kernel.py, one thread), restated
+    # with its block structure, at 2^14 and 2^16 particles on 512 targets,
+    # scaled by N/targets and then to the benchmarked N by (N / n)^2
+    from oracle import numpy_reference as NR
+    numpy_ref = {"kind": "port of the reference's NumPy kernels (kernel.py:69-190), "
+                         "blocks of 512, FP64", "cores": 1, "sizes": {}}
+    for n_np in (1 << 14, 1 << 16):
+        p, g, sgm, _ = slab_wake(n_np, x0=AIRCRAFT_SLAB_X0, sigma=resolved_core(n_np))
+        s_np, det = NR.step_seconds(p, g, sgm, min(512, n_np))
+        numpy_ref["sizes"][str(n_np)] = {
+            "step_s": s_np, **det,
+            "step_s_extrapolated_to_n": s_np * (args.n / n_np) ** 2,
+            "extrapolation": f"N^2 from {n_np} to {args.n} particles (extrapolated, not run)"}
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
@@ -437,6 +458,7 @@ def run_reference(args, rank, world):
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "numpy_reference": numpy_ref,
     }))
 
 
@@ -662,67 +684,80 @@ def run_ours(args, rank, world):
                          "steps": args.e2e_steps, "ms_per_step": e2e_ms}
 
     if args.relax_steps > 0 and rank == 0:
-        # the reference's hybrid solver runs the Pedrizzetti relaxation with
-        # rlxf = 0.3 (one more self-sweep per step, the Gaussian-erf vorticity);
-        # the same step with it on, timed alike
+        # the same step in two other forms, timed alike: with the reference's
+        # Pedrizzetti relaxation (rlxf = 0.3: one Gaussian-erf vorticity
+        # self-sweep and the strength update more), and as the reference's
+        # hybrid solver runs its free wake, without the stretching term
+        # (experiment_hybrid_panel_particle.py:140-143: three velocity sweeps)
         del step
         torch.cuda.empty_cache()
-        progress("relaxation variant")
-        st3 = Step(args.n, args.precision, device, far_field=args.far_field, leaf=args.leaf,
-                   rlxf=0.3)
-        for _ in range(args.warmup):
-            st3.run()
-        snap3 = st3.hs.snapshot()
         flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
-        ms3 = []
-        for _ in range(args.relax_steps):
-            st3.hs.restore(snap3)
-            flush.zero_()
-            torch.cuda.synchronize()
-            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s.record()
-            st3.run()
-            e.record()
-            torch.cuda.synchronize()
-            ms3.append(s.elapsed_time(e))
-        result["relaxation_variant"] = {
-            "rlxf": 0.3, "ms_per_step": sum(ms3) / len(ms3),
-            "steps_per_s": 1e3 * len(ms3) / sum(ms3), "steps": len(ms3),
-            "note": "the benchmarked step plus the reference's Pedrizzetti relaxation "
-                    "(a Gaussian-erf vorticity self-sweep and the strength update)"}
-        del st3, flush
-        torch.cuda.empty_cache()
+        for key, kw, note in (
+                ("relaxation_variant", dict(rlxf=0.3),
+                 "the benchmarked step plus the reference's Pedrizzetti relaxation (a "
+                 "Gaussian-erf vorticity self-sweep and the strength update)"),
+                ("stretching_off_variant", dict(stretch=False),
+                 "the benchmarked step without the stretching term, as the reference's "
+                 "hybrid solver runs its free wake (3 velocity self-sweeps per step)")):
+            progress(key)
+            st3 = Step(args.n, args.precision, device, far_field=args.far_field, leaf=args.leaf,
+                       **kw)
+            for _ in range(args.warmup):
+                st3.run()
+            snap3 = st3.hs.snapshot()
+            ms3 = []
+            for _ in range(args.relax_steps):
+                st3.hs.restore(snap3)
+                flush.zero_()
+                torch.cuda.synchronize()
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record()
+                st3.run()
+                e.record()
+                torch.cuda.synchronize()
+                ms3.append(s.elapsed_time(e))
+            result[key] = {**kw, "ms_per_step": sum(ms3) / len(ms3),
+                           "steps_per_s": 1e3 * len(ms3) / sum(ms3), "steps": len(ms3),
+                           "note": note}
+            del st3
+            torch.cuda.empty_cache()
+        del flush
 
     if args.cl_steps > 0 and rank == 0 and args.far_field != "direct":
         # CL / CDi history of the benchmarked form against direct all-pairs
-        # sweeps (FP32 compensated, within ~1e-7 of FP64) from the same seeded
-        # initial state, step by step, over one flapping cycle (43 steps) at
-        # --cl-particles (the direct sweeps' N^2 cost bounds the size)
+        # sweeps (FP32 compensated, within ~1e-7 of FP64 per sweep) from the
+        # same seeded initial state, step by step, over one flapping cycle
+        # (43 steps) at --cl-particles (the direct sweeps' N^2 cost bounds the
+        # size): with the stretching term (the timed step) and without it (the
+        # reference's hybrid solver, experiment_hybrid_panel_particle.py:140-143)
         torch.cuda.empty_cache()
-        hist = {}
         ncl = args.cl_particles
-        for ff in (args.far_field, "direct"):
-            progress(f"CL history, far field {ff}, {ncl} particles")
-            st2 = Step(ncl, args.precision, device, far_field=ff, leaf=args.leaf,
-                       steps_hint=args.cl_steps)
-            for _ in range(args.cl_steps):
-                st2.run()
-            hist[ff] = (st2.hs.cl.copy(), st2.hs.cdi.copy(), st2.field.np)
-            del st2
-            torch.cuda.empty_cache()
-        ca, da, na = hist[args.far_field]
-        cb, db, nb = hist["direct"]
-        result["cl_history_vs_direct"] = {
-            "steps": args.cl_steps, "particles_seeded": ncl, "particles_final": int(nb),
-            "cl_err_max_over_max": float(abs(ca - cb).max() / abs(cb).max()),
-            "cdi_err_max_over_max": float(abs(da - db).max() / abs(db).max()),
-            "cl_abs_err_max": float(abs(ca - cb).max()),
-            "cdi_abs_err_max": float(abs(da - db).max()),
-            "convention": "max_k |x_k - ref_k| / max_k |ref_k| over the history (the "
-                          "flapping CL crosses zero, so a per-step ratio is undefined there)",
-            "cl": [float(x) for x in cb], "cdi": [float(x) for x in db],
-            "reference": "direct all-pairs sweeps, FP32 compensated (within 1e-7 of FP64), "
-                         "same seeded state"}
+        result["cl_history_vs_direct"] = {}
+        for stretch in (True, False):
+            hist = {}
+            for ff in (args.far_field, "direct"):
+                progress(f"CL history, far field {ff}, {ncl} particles, stretching {stretch}")
+                st2 = Step(ncl, args.precision, device, far_field=ff, leaf=args.leaf,
+                           steps_hint=args.cl_steps, stretch=stretch)
+                for _ in range(args.cl_steps):
+                    st2.run()
+                hist[ff] = (st2.hs.cl.copy(), st2.hs.cdi.copy(), st2.field.np)
+                del st2
+                torch.cuda.empty_cache()
+            ca, da, na = hist[args.far_field]
+            cb, db, nb = hist["direct"]
+            result["cl_history_vs_direct"]["stretching_on" if stretch else "stretching_off"] = {
+                "steps": args.cl_steps, "particles_seeded": ncl, "particles_final": int(nb),
+                "cl_err_max_over_max": float(abs(ca - cb).max() / abs(cb).max()),
+                "cdi_err_max_over_max": float(abs(da - db).max() / abs(db).max()),
+                "cl_abs_err_max": float(abs(ca - cb).max()),
+                "cdi_abs_err_max": float(abs(da - db).max()),
+                "cl": [float(x) for x in cb], "cdi": [float(x) for x in db]}
+        result["cl_history_vs_direct"]["convention"] = (
+            "max_k |x_k - ref_k| / max_k |ref_k| over the history (the flapping CL crosses "
+            "zero, where a per-step ratio is undefined)")
+        result["cl_history_vs_direct"]["reference"] = (
+            "direct all-pairs sweeps, FP32 compensated, same seeded state")
 
     if rank == 0:
         print(json.dumps(result))

@@ -27,17 +27,30 @@ struct FarPairs {
   int n;                     // pairs
 };
 
-// What the FP64 judge decided for each class of local-expansion pairs (see
-// fvx_tree.cu, judge_class): the translation and network kernels read a
-// pair's class from `cls` (row index over list 0, then list 1) and its action
-// from `act`: 0 = analytic translation + network residual, 1 = analytic
-// translation alone (the network is dropped for the class), 2 = no expansion
-// -- the translation kernel queues the pair, (target | list << 30, cell), in
-// `fb` for the FP64 direct sum.  cls == nullptr: every pair takes action 0.
+// Classes of the local-expansion pairs for the FP64 judge: the pair's list
+// (0: the leaves' own pairs, 1: the pairs shared through parents of leaves)
+// x whether the source cell is larger than the target x four bins of the
+// opening ratio mu = sqrt(3)/2 (h_T + h_S) / d against the path's theta
+// (every pair on the path has mu < theta): mu/theta in [0.9, 1), [0.8, 0.9),
+// [0.65, 0.8) and below 0.65.  The truncation error grows with mu, so the
+// classes keep pairs of different error apart.
 constexpr int kJudgeClasses = 16;
+__host__ __device__ __forceinline__ int judge_class(int list, float hT, float hS, float d2,
+                                                    float inv_theta2) {
+  const float q = 0.75f * (hT + hS) * (hT + hS) * inv_theta2 / d2;  // (mu / theta)^2
+  const int bin = q >= 0.81f ? 0 : (q >= 0.64f ? 1 : (q >= 0.4225f ? 2 : 3));
+  return (list << 3) | (hS > hT ? 4 : 0) | bin;
+}
+
+// What the FP64 judge decided for each class: the translation and network
+// kernels work out each pair's class and read its action from `act`:
+// 0 = analytic translation + network residual, 1 = analytic translation
+// alone (the network is dropped for the class), 2 = no expansion -- the
+// translation kernel queues the pair, (target | list << 30, cell), in `fb`
+// for the FP64 direct sum.  act == nullptr: every pair takes action 0.
 struct FarJudge {
-  const uint8_t* cls = nullptr;
   const uint8_t* act = nullptr;  // [kJudgeClasses]
+  float inv_theta2 = 0.f;        // 1 / theta^2 of the path
   int2* fb = nullptr;
   int* nfb = nullptr;
   int fb_cap = 0;

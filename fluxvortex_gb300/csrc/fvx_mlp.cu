@@ -421,7 +421,6 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
   // first MMA runs, the leaf key and the cell record while its third MMA
   // runs), so that the loads' latency leaves the tile's serial chain.
   int pf_leaf = 0, pf_cell = 0, pf_li = 0;
-  bool pf_keep = true;
   uint32_t pf_key = 0;
   RecRegs pf_rec;
   auto fetch_index = [&](int t) {
@@ -431,8 +430,6 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
       const int rr = pf_li ? r - A.f.l0.n : r;
       pf_leaf = (pf_li ? A.f.l1.pair_tgt : A.f.l0.pair_tgt)[rr];
       pf_cell = (pf_li ? A.f.l1.pair_cell : A.f.l0.pair_cell)[rr];
-      // the residual only for classes whose network the judge kept
-      pf_keep = A.f.judge.cls == nullptr || A.f.judge.act[A.f.judge.cls[r]] == 0;
     }
   };
   auto fetch_record = [&](int t) {
@@ -460,9 +457,14 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         if (act_row) {
           leaf = pf_leaf;
           li = pf_li;
-          keep = pf_keep;
           const float th = li ? A.f.l1.h : A.f.l0.h;
           const float3 cT = leaf_center(pf_key, th);
+          if (A.f.judge.act != nullptr) {
+            // the residual only for the classes whose network the judge kept
+            const float dx = cT.x - pf_rec.v[0], dy = cT.y - pf_rec.v[1], dz = cT.z - pf_rec.v[2];
+            keep = A.f.judge.act[judge_class(li, th, pf_rec.v[3], dx * dx + dy * dy + dz * dz,
+                                             A.f.judge.inv_theta2)] == 0;
+          }
           const PairScale sc = pair_features(pf_rec.v, cT.x, cT.y, cT.z, th, f);
           ax[0] = sc.s2;
           ax[1] = sc.s3;
@@ -691,27 +693,75 @@ __global__ void pair_sums_kernel(int npairs, int stride, const int* __restrict__
   reduce_expansion(acc, partial + (static_cast<int64_t>(pr) * gridDim.y + blockIdx.y) * NOUT);
 }
 
-// The same sums for the FP64 judge's samples: slot x of 2 x cap (list 0's
-// samples, then list 1's, cap slots each; slots past a list's count idle).
-__global__ void judge_sums_kernel(JudgeSampleView S, const uint32_t* __restrict__ leaf_key,
-                                  const int* __restrict__ cell_start,
-                                  const int* __restrict__ cell_count,
-                                  const float4* __restrict__ sp, const float4* __restrict__ sa,
-                                  const int* __restrict__ leaf_of_particle, float h,
-                                  double* __restrict__ partial) {
-  const int slot = blockIdx.x;
-  const int li = slot >= S.cap ? 1 : 0;
-  const int q = slot - li * S.cap;
-  if (q >= S.cnt[li]) return;
-  const float3 cT = leaf_center(S.key[li][q], S.h[li]);
-  const int g = S.cell[li][q];
-  const int c0 = cell_start[g], cn = cell_count[g];
-  const int per = (cn + gridDim.y - 1) / gridDim.y;
-  const int s0 = c0 + static_cast<int>(blockIdx.y) * per;
-  const int n = max(0, min(per, c0 + cn - s0));
-  double acc[NOUT];
-  exact_expansion_slice(cT, s0, n, leaf_key, sp, sa, leaf_of_particle, h, acc);
-  reduce_expansion(acc, partial + (static_cast<int64_t>(slot) * gridDim.y + blockIdx.y) * NOUT);
+// The same sums for the FP64 judge's samples, balanced over the GPU whatever
+// the cells' sizes: each sample's cell is cut into chunks of kTargetsThreads
+// particles, item offsets per slot come from judge_chunks_kernel, and
+// resident CTAs stride over the items (one particle per thread), adding each
+// chunk's 30 sums into the slot's with FP64 atomics (the order of those
+// additions varies from run to run in the last bits).  Slots: list 0's
+// samples, then list 1's, cap each; slots past a list's count take no items.
+__global__ void judge_chunks_kernel(JudgeSampleView S, const int* __restrict__ cell_count,
+                                    int* __restrict__ off) {
+  __shared__ int sc[1024];
+  __shared__ int carry;
+  const int n = 2 * S.cap;
+  if (threadIdx.x == 0) {
+    carry = 0;
+    off[0] = 0;
+  }
+  for (int base = 0; base < n; base += 1024) {
+    const int i = base + threadIdx.x;
+    int c = 0;
+    if (i < n) {
+      const int li = i >= S.cap ? 1 : 0;
+      const int q = i - li * S.cap;
+      if (q < S.cnt[li]) c = (cell_count[S.cell[li][q]] + kTargetsThreads - 1) / kTargetsThreads;
+    }
+    __syncthreads();
+    sc[threadIdx.x] = c;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      const int v = threadIdx.x >= static_cast<unsigned>(o) ? sc[threadIdx.x - o] : 0;
+      __syncthreads();
+      sc[threadIdx.x] += v;
+      __syncthreads();
+    }
+    if (i < n) off[i + 1] = carry + sc[threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 1023) carry += sc[1023];
+  }
+}
+
+__global__ void __launch_bounds__(kTargetsThreads) judge_sums_kernel(
+    JudgeSampleView S, const int* __restrict__ off, const uint32_t* __restrict__ leaf_key,
+    const int* __restrict__ cell_start, const int* __restrict__ cell_count,
+    const float4* __restrict__ sp, const float4* __restrict__ sa,
+    const int* __restrict__ leaf_of_particle, float h, double* __restrict__ sums) {
+  __shared__ double s_out[NOUT];
+  const int n = 2 * S.cap;
+  const int total = off[n];
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int lo = 0, hi = n;  // the slot: off[slot] <= item < off[slot + 1]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (off[mid] <= item) lo = mid; else hi = mid;
+    }
+    const int slot = lo;
+    const int li = slot >= S.cap ? 1 : 0;
+    const int q = slot - li * S.cap;
+    const float3 cT = leaf_center(S.key[li][q], S.h[li]);
+    const int g = S.cell[li][q];
+    const int c0 = cell_start[g], cn = cell_count[g];
+    const int s0 = c0 + (item - off[slot]) * kTargetsThreads;
+    const int m = min(kTargetsThreads, c0 + cn - s0);
+    double acc[NOUT];
+    exact_expansion_slice(cT, s0, m, leaf_key, sp, sa, leaf_of_particle, h, acc);
+    reduce_expansion(acc, s_out);
+    __syncthreads();
+    if (threadIdx.x < NOUT) atomicAdd(sums + static_cast<int64_t>(slot) * NOUT + threadIdx.x,
+                                      s_out[threadIdx.x]);
+    __syncthreads();
+  }
 }
 
 // Per pair: the slices' sums in order, the features (BF16), the output scales,
@@ -784,11 +834,15 @@ __global__ void __launch_bounds__(kM2lThreads) m2l_pairs_kernel(FarIO F) {
       leaf = fl.pair_tgt[rr_];
       cell = fl.pair_cell[rr_];
       L = fl.local + static_cast<int64_t>(leaf) * OUT;
-      // a class the judge sent to the FP64 direct sum: no expansion, queued
-      queue = F.judge.cls != nullptr && F.judge.act[F.judge.cls[row]] == 2;
+      const float3 cT = leaf_center(fl.tgt_key[leaf], fl.h);
+      const RecRegs rr = load_record(F.rec + static_cast<int64_t>(cell) * kRecFloats);
+      if (F.judge.act != nullptr) {
+        // a class the judge sent to the FP64 direct sum: no expansion, queued
+        const float dx = cT.x - rr.v[0], dy = cT.y - rr.v[1], dz = cT.z - rr.v[2];
+        queue = F.judge.act[judge_class(li, fl.h, rr.v[3], dx * dx + dy * dy + dz * dz,
+                                        F.judge.inv_theta2)] == 2;
+      }
       if (!queue) {
-        const float3 cT = leaf_center(fl.tgt_key[leaf], fl.h);
-        const RecRegs rr = load_record(F.rec + static_cast<int64_t>(cell) * kRecFloats);
         const PairGeom g = pair_geom(rr.v, cT.x, cT.y, cT.z);
         const RecordMoments src{rr.v, g.Rx * g.id, g.Ry * g.id, g.Rz * g.id, g.hS * g.id, g.im,
                                 g.ih};
@@ -1088,14 +1142,17 @@ int m2l_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, 
   return FVX_OK;
 }
 
-// partial: scratch of 2 cap x slices x 30 doubles
+// sums: 2 cap x 30 doubles (zeroed here); off: 2 cap + 1 ints of scratch
 int judge_sums_launch(const JudgeSampleView& S, const uint32_t* leaf_key, const int* cell_start,
                       const int* cell_count, const float4* sp, const float4* sa,
-                      const int* leaf_of_particle, float h, double* partial, int slices,
+                      const int* leaf_of_particle, float h, double* sums, int* off,
                       cudaStream_t s) {
   if (S.cap <= 0) return FVX_OK;
-  mlp::judge_sums_kernel<<<dim3(2 * S.cap, slices), mlp::kTargetsThreads, 0, s>>>(
-      S, leaf_key, cell_start, cell_count, sp, sa, leaf_of_particle, h, partial);
+  FVX_CUDA_TRY(cudaMemsetAsync(sums, 0, sizeof(double) * 30 * 2 * size_t(S.cap), s));
+  mlp::judge_chunks_kernel<<<1, 1024, 0, s>>>(S, cell_count, off);
+  FVX_LAUNCH_CHECK();
+  mlp::judge_sums_kernel<<<4 * device_sm_count(), mlp::kTargetsThreads, 0, s>>>(
+      S, off, leaf_key, cell_start, cell_count, sp, sa, leaf_of_particle, h, sums);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }

@@ -1593,19 +1593,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
 }
 
 // ---- the FP64 judge of the local-expansion path ------------------------------------
-// Every local-expansion pair falls in one of kJudgeClasses classes: its list
-// (the leaves' own pairs, or the pairs shared through parents of leaves) x
-// whether the source cell is larger than the target x four bins of the
-// opening ratio mu = sqrt(3)/2 (h_T + h_S) / d against the path's theta (all
-// its pairs have mu < theta): mu/theta in [0.9, 1), [0.8, 0.9), [0.65, 0.8)
-// and below 0.65.  The truncation error grows with mu, so the classes keep
-// pairs of different error apart, and the judge samples each class on its own.
-__device__ __forceinline__ int judge_class(int list, float hT, float hS, float d2,
-                                           float inv_theta2) {
-  const float q = 0.75f * (hT + hS) * (hT + hS) * inv_theta2 / d2;  // (mu / theta)^2
-  const int bin = q >= 0.81f ? 0 : (q >= 0.64f ? 1 : (q >= 0.4225f ? 2 : 3));
-  return (list << 3) | (hS > hT ? 4 : 0) | bin;
-}
+// (pair classes: judge_class in fvx_common.cuh)
 
 // Both lists of local-expansion pairs (rows: list 0's, then list 1's).
 struct JudgeLists {
@@ -1725,7 +1713,7 @@ __device__ __forceinline__ float expansion_error(const float* p, const double* t
   return num / fmaxf(den, 1e-30f);
 }
 
-// Per sample: the exact expansion T (FP64 sums, slices in order), the
+// Per sample: the exact expansion T (FP64 sums), the
 // analytic translation A and the network residual Y (physical units, from
 // the same kernels the sweep runs), and the error of the expansion applied
 // across the target: with rho = sqrt(3)/2 h_T / d (the target's half
@@ -1733,7 +1721,7 @@ __device__ __forceinline__ float expansion_error(const float* p, const double* t
 //   e = (|du| + rho |dJ| + rho^2/2 |dH|) / (|u| + rho |J| + rho^2/2 |H|),
 // for A + Y (err_l) and for A alone (err_a); failures counted per class.
 __global__ void judge_errors_kernel(JudgeSampleBufs B, const float* __restrict__ rec,
-                                    const double* __restrict__ partial, int slices,
+                                    const double* __restrict__ sums,
                                     const float* __restrict__ A, const float* __restrict__ Y,
                                     float h0, float h1, float tol, JudgeWords* W,
                                     float* __restrict__ err) {
@@ -1743,11 +1731,7 @@ __global__ void judge_errors_kernel(JudgeSampleBufs B, const float* __restrict__
   const int q = slot - li * B.cap;
   if (q >= W->cnt[li]) return;
   double t[30];
-  for (int c = 0; c < 30; ++c) {
-    double v = 0.0;
-    for (int y = 0; y < slices; ++y) v += partial[(static_cast<int64_t>(slot) * slices + y) * 30 + c];
-    t[c] = v;
-  }
+  for (int c = 0; c < 30; ++c) t[c] = sums[static_cast<int64_t>(slot) * 30 + c];
   const float hT = li ? h1 : h0;
   const float3 cT = cell_center_rel(B.key[li][q], hT);
   const float* cs = rec + static_cast<int64_t>(B.cell[li][q]) * kRecFloats;
@@ -2003,7 +1987,7 @@ int m2l_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, 
                         const FarJudge& judge = FarJudge{});
 int judge_sums_launch(const JudgeSampleView& S, const uint32_t* leaf_key, const int* cell_start,
                       const int* cell_count, const float4* sp, const float4* sa,
-                      const int* leaf_of_particle, float h, double* partial, int slices,
+                      const int* leaf_of_particle, float h, double* sums, int* off,
                       cudaStream_t s);
 
 }  // namespace fvx
@@ -2652,14 +2636,18 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   uint8_t* act = nullptr;
   if (use_judge) {
     const bool fresh_table = T->judge_act.p == nullptr;
-    if ((rc = grow(T->judge_act, 8 * kJudgeClasses)) || (rc = grow(T->judge_cls, size_t(nloc))) ||
-        (rc = grow(T->judge_hist, 4 * kJudgeClasses)) || (rc = grow(T->fb_count, 16)))
-      return rc;
+    if ((rc = grow(T->judge_act, 8 * kJudgeClasses)) || (rc = grow(T->fb_count, 16))) return rc;
     if (fresh_table || !T->judge_armed)
       FVX_CUDA_TRY(cudaMemsetAsync(T->judge_act.p, 0, 8 * kJudgeClasses, s));
     act = P<uint8_t>(T->judge_act) + mslot * kJudgeClasses;
-    FVX_CUDA_TRY(cudaMemsetAsync(T->judge_hist.p, 0, 4 * kJudgeClasses, s));
     FVX_CUDA_TRY(cudaMemsetAsync(T->fb_count.p, 0, 16, s));
+  }
+  if (judged) {
+    // every pair's class and the class sizes (the sweep's kernels work the
+    // class out again themselves; the judge needs the sizes and the sample)
+    if ((rc = grow(T->judge_cls, size_t(nloc))) || (rc = grow(T->judge_hist, 4 * kJudgeClasses)))
+      return rc;
+    FVX_CUDA_TRY(cudaMemsetAsync(T->judge_hist.p, 0, 4 * kJudgeClasses, s));
     JL.tgt[0] = P<int>(T->lrn_leaf);
     JL.cell[0] = P<int>(T->lrn_cell);
     JL.key[0] = leaves.key;
@@ -2679,13 +2667,12 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   if (judged) {
     const int per_class = std::max(1, T->val_samples / kJudgeClasses);
     jcap = 16 * per_class;  // per list: 8 classes, at most 2 per_class samples each
-    const int slices = std::max(1, std::min(64, 8 * device_sm_count() / (2 * jcap)));
     if ((rc = grow(T->judge_words, sizeof(tree::JudgeWords))) ||
         (rc = grow(T->judge_samp, (9 * sizeof(int) + 2) * size_t(jcap) + 256)) ||
         (rc = grow(T->judge_A, sizeof(float) * 64 * size_t(jcap))) ||
         (rc = grow(T->judge_Y, sizeof(float) * 64 * size_t(jcap))) ||
         (rc = grow(T->judge_err, sizeof(float) * 4 * size_t(jcap))) ||
-        (rc = grow(T->pair_partial, sizeof(double) * 30 * 2 * size_t(jcap) * slices)))
+        (rc = grow(T->pair_partial, sizeof(double) * 30 * 2 * size_t(jcap) + 8 * size_t(jcap) + 64)))
       return rc;
     JW = P<tree::JudgeWords>(T->judge_words);
     FVX_CUDA_TRY(cudaMemsetAsync(JW, 0, sizeof(tree::JudgeWords), s));
@@ -2714,8 +2701,9 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
                                                    offsetof(tree::JudgeWords, cnt));
     JudgeSampleView SV{jcnt, jcap, {JB.cell[0], JB.cell[1]}, {JB.key[0], JB.key[1]},
                        {JL.h[0], JL.h[1]}};
+    int* joff = reinterpret_cast<int*>(P<double>(T->pair_partial) + 30 * 2 * size_t(jcap));
     if ((rc = judge_sums_launch(SV, leaves.key, lvb, lvb + total_cells, sp, sa, cid,
-                                static_cast<float>(h), P<double>(T->pair_partial), slices, s)))
+                                static_cast<float>(h), P<double>(T->pair_partial), joff, s)))
       return rc;
     // the sweep's own translation (and network) on the samples, one target each
     float* jA = P<float>(T->judge_A);
@@ -2731,7 +2719,7 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
       if ((rc = mlp_farfield_launch(sy0, sy1, rec, T->mlp_W, T->mlp_b, s))) return rc;
     }
     tree::judge_errors_kernel<<<(2 * jcap + 127) / 128, 128, 0, s>>>(
-        JB, rec, P<double>(T->pair_partial), slices, jA, network ? jY : nullptr, JL.h[0],
+        JB, rec, P<double>(T->pair_partial), jA, network ? jY : nullptr, JL.h[0],
         JL.h[1], static_cast<float>(T->val_tol), JW, P<float>(T->judge_err));
     FVX_LAUNCH_CHECK();
     tree::judge_decide_kernel<<<1, 32, 0, s>>>(JW, P<unsigned>(T->judge_hist), act,
@@ -2742,8 +2730,8 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   if (use_judge) {
     const int64_t cap = nloc + 2 * int64_t(jcap);
     if ((rc = grow(T->fb_queue, sizeof(int2) * size_t(cap)))) return rc;
-    FJ.cls = P<uint8_t>(T->judge_cls);
     FJ.act = act;
+    FJ.inv_theta2 = static_cast<float>(1.0 / (T->theta_l * T->theta_l));
     FJ.fb = P<int2>(T->fb_queue);
     FJ.nfb = P<int>(T->fb_count);
     FJ.fb_cap = static_cast<int>(cap);

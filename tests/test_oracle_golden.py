@@ -183,3 +183,18 @@ def test_population_drop_keeps_the_newest():
     assert np.array_equal(out[2], [6.0, 7.0, 8.0, 9.0])
     same = POP.drop_oldest(pos, pos, np.arange(n, dtype=float), np.arange(n, dtype=float), 20)
     assert same[0].shape[0] == n
+
+
+@pytest.mark.parametrize("kernel", ["winckelmans", "gaussianerf"])
+def test_numpy_restatement_of_the_reference_kernels(golden, kernel):
+    """The NumPy restatement timed as the reference's CPU path gives the
+    reference's own outputs (blocks of 512 over 300 targets x 700 sources:
+    two source blocks, one partial)."""
+    from oracle import numpy_reference as NR
+    z = golden("particles_kernel.npz")
+    u = NR.velocity_from_particles(z["tgt_pos"], z["src_pos"], z["src_gamma"], z["src_sigma"],
+                                   kernel)
+    assert rel_err(u, z[f"velocity_{kernel}"]) < 1e-13
+    J = NR.jacobian_from_particles(z["tgt_pos"], z["src_pos"], z["src_gamma"], z["src_sigma"],
+                                   kernel)
+    assert rel_err(J, z[f"jacobian_{kernel}"]) < 1e-12
