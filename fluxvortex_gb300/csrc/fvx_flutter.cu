@@ -22,6 +22,8 @@
 // Reference: src/fluxvortex/aeroelastic_solver.py:68-221 and beam_fe.py:231-351
 // around PteraSoftware's ring-vortex UVLM; the PteraSoftware-free model is
 // described in fluxvortex_gb300/flutter.py.
+#include <cooperative_groups.h>
+
 #include "fvx_common.cuh"
 #include "fvx_pair_math.cuh"
 #include "fvx_segment_math.cuh"
@@ -46,6 +48,7 @@ struct Smem {
   double A[kMaxP][kMaxP + 1];
   double rhs[kMaxP], gam[kMaxP], gprev[kMaxP];
   double Vind[2 * kMaxP][3];
+  double Vsum[2 * kMaxP][3];  // cluster form: both CTAs' partial inductions summed
   double W[kMaxRows + 1][kMaxNS + 1][3];
   double wgam[kMaxRows][kMaxNS], wage[kMaxRows];
   double d[kMaxDof], v[kMaxDof], a[kMaxDof], F[kMaxDof], feff[kMaxDof], gd[kMaxDof];
@@ -263,9 +266,13 @@ __device__ __forceinline__ void ring_velocity_f32(const seg::VortexRec& R, doubl
 
 // Induced velocity of the wake rings and particles at the 2P points
 // (collocation points, then bound-leg centres) into S.Vind.
-template <bool F32>
+// CL > 1: the environment runs on a cluster of CL CTAs; CTA `crank` takes
+// every CL-th ring (by slice) and every CL-th particle tile, and the partial
+// inductions are summed in rank order through distributed shared memory, so
+// both CTAs hold the same total.
+template <bool F32, int CL>
 __device__ void wake_induction(Smem& S, const FlutterParams& p, const FlutterState& st, int env,
-                               int R, int head, int count) {
+                               int R, int head, int count, int crank) {
   const int P = p.nc * p.ns, T2 = 2 * P;
   const int slices = blockDim.x / T2;
   const int tgt = threadIdx.x % T2, sl = threadIdx.x / T2;
@@ -283,13 +290,13 @@ __device__ void wake_induction(Smem& S, const FlutterParams& p, const FlutterSta
   if (active) {
     if constexpr (F32) {
       float fx = 0.f, fy = 0.f, fz = 0.f;
-      for (int r = sl; r < R * p.ns; r += slices)
+      for (int r = sl + crank * slices; r < R * p.ns; r += slices * CL)
         ring_velocity_f32(S.wake[r], px, py, pz, fx, fy, fz);
       vx = fx;
       vy = fy;
       vz = fz;
     } else {
-      for (int r = sl; r < R * p.ns; r += slices)
+      for (int r = sl + crank * slices; r < R * p.ns; r += slices * CL)
         seg::vortex_velocity<FVX_LEGS_RING>(S.wake[r], px, py, pz, vx, vy, vz, cnt);
     }
   }
@@ -299,7 +306,7 @@ __device__ void wake_induction(Smem& S, const FlutterParams& p, const FlutterSta
   const double* pa = st.palp + static_cast<int64_t>(env) * Pm * 3;
   const double* ps = st.psig + static_cast<int64_t>(env) * Pm;
   float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
-  for (int t0 = 0; t0 < count; t0 += kTile) {
+  for (int t0 = crank * kTile; t0 < count; t0 += kTile * CL) {
     const int nt = min(kTile, count - t0);
     __syncthreads();
     for (int e = threadIdx.x; e < nt; e += blockDim.x) {
@@ -377,6 +384,27 @@ __device__ void wake_induction(Smem& S, const FlutterParams& p, const FlutterSta
     S.Vind[k][2] = z;
   }
   __syncthreads();
+  if constexpr (CL > 1) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    cl.sync();  // every CTA's partial is complete
+    for (int k = threadIdx.x; k < T2; k += blockDim.x) {
+      double x = 0.0, y = 0.0, z = 0.0;
+      for (int r = 0; r < CL; ++r) {
+        const double(*V)[3] = r == crank ? S.Vind : cl.map_shared_rank(S.Vind, r);
+        x += V[k][0];
+        y += V[k][1];
+        z += V[k][2];
+      }
+      S.Vsum[k][0] = x;
+      S.Vsum[k][1] = y;
+      S.Vsum[k][2] = z;
+    }
+    cl.sync();  // every CTA has read the others' partials
+    for (int k = threadIdx.x; k < T2; k += blockDim.x)
+      for (int c = 0; c < 3; ++c) S.Vind[k][c] = S.Vsum[k][c];
+    __syncthreads();
+  }
 }
 
 // In-place LU solve of S.A x = S.rhs (partial pivoting, first largest |pivot|).
@@ -441,11 +469,19 @@ __device__ bool lu_solve(Smem& S, int P) {
   return true;
 }
 
-template <bool F32>
+// CL CTAs per environment (a cluster, launched with that cluster size): they
+// run the same step redundantly, except the wake induction, which they share
+// (wake_induction); rank 0 alone writes the environment's global state, and a
+// cluster barrier at the start of every step makes its particle writes of
+// the last step visible to the others.
+template <bool F32, int CL>
 __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterState st, int step_end) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem& S = *reinterpret_cast<Smem*>(smem_raw);
-  const int env = blockIdx.x;
+  int crank = 0;
+  if constexpr (CL > 1) crank = static_cast<int>(cooperative_groups::this_cluster().block_rank());
+  const bool writer = crank == 0;
+  const int env = blockIdx.x / CL;
   const int P = p.nc * p.ns, s1 = p.ns + 1, ndof = 3 * p.nnodes, nf = ndof - 3;
   const int last = min(step_end, p.n_steps[env]);
   int step = st.step[env];
@@ -473,6 +509,10 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
   __syncthreads();
   bool ok = true;
   for (; step < last && ok; ++step) {
+    if constexpr (CL > 1) {
+      __threadfence();
+      cooperative_groups::this_cluster().sync();  // rank 0's particle writes visible
+    }
     // 1. geometry and lattice
     if (ref) {
       build_lattice_reference(S, p);
@@ -488,7 +528,7 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
     }
     __syncthreads();
     // 2. wake + particles at collocation points and bound-leg centres
-    wake_induction<F32>(S, p, st, env, R, head, count);
+    wake_induction<F32, CL>(S, p, st, env, R, head, count, crank);
     // 3. AIC (written after the induction, whose scratch overlaps it) and rhs
     for (int e = threadIdx.x; e < P * P; e += blockDim.x) {
       const int i = e / P, j = e % P;
@@ -583,12 +623,12 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
       S.a[3 + threadIdx.x] = an;
     }
     __syncthreads();
-    if (couple && threadIdx.x == 0) {
+    if (couple && writer && threadIdx.x == 0) {
       const int h = ref ? step - 1 : step;
       st.hist_w[static_cast<int64_t>(env) * p.max_steps + h] = S.d[ndof - 3];
       st.hist_th[static_cast<int64_t>(env) * p.max_steps + h] = S.d[ndof - 1];
     }
-    if (couple && st.hist_nodes != nullptr) {
+    if (couple && writer && st.hist_nodes != nullptr) {
       const int h = ref ? step - 1 : step;
       double* hn = st.hist_nodes + (static_cast<int64_t>(env) * p.max_steps + h) * p.nnodes * 2;
       for (int n = threadIdx.x; n < p.nnodes; n += blockDim.x) {
@@ -606,7 +646,7 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
     double* pp = st.ppos + static_cast<int64_t>(env) * Pm * 3;
     double* pa = st.palp + static_cast<int64_t>(env) * Pm * 3;
     double* ps = st.psig + static_cast<int64_t>(env) * Pm;
-    for (int e = threadIdx.x; e < count; e += blockDim.x) {
+    for (int e = threadIdx.x; e < (writer ? count : 0); e += blockDim.x) {
       const int q = (head + e) % Pm;
       pp[3 * q] += ux * dt;
       pp[3 * q + 1] += uy * dt;
@@ -668,13 +708,15 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
                 q = head;  // drop the oldest
                 head = (head + 1) % Pm;
               }
-              pp[3 * q] = 0.5 * (a[0] + bb[0]);
-              pp[3 * q + 1] = 0.5 * (a[1] + bb[1]);
-              pp[3 * q + 2] = 0.5 * (a[2] + bb[2]);
-              pa[3 * q] = alx;
-              pa[3 * q + 1] = aly;
-              pa[3 * q + 2] = alz;
-              ps[q] = sg;
+              if (writer) {
+                pp[3 * q] = 0.5 * (a[0] + bb[0]);
+                pp[3 * q + 1] = 0.5 * (a[1] + bb[1]);
+                pp[3 * q + 2] = 0.5 * (a[2] + bb[2]);
+                pa[3 * q] = alx;
+                pa[3 * q + 1] = aly;
+                pa[3 * q + 2] = alz;
+                ps[q] = sg;
+              }
             }
           }
         }
@@ -693,7 +735,8 @@ __global__ void __launch_bounds__(512) sweep_kernel(FlutterParams p, FlutterStat
   if (!ok) {
     if (threadIdx.x == 0) flag_status(kStatusNonFinite);
   }
-  // store state
+  // store state (rank 0)
+  if (!writer) return;
   for (int k = threadIdx.x; k < ndof; k += blockDim.x) {
     st.d[env * ndof + k] = S.d[k];
     st.v[env * ndof + k] = S.v[k];
@@ -739,17 +782,36 @@ extern "C" int fvx_flutter_sweep(const FlutterParams* params, const FlutterState
   FVX_ARG_CHECK((threads / (2 * P)) * 2 * P * 3 <= kMaxP * (kMaxP + 1),
                 "too many slices for the reduction scratch");
   const size_t smem = sizeof(Smem);
-  static bool attr_done[2] = {false, false};
+  // two CTAs per environment (a cluster sharing its wake induction) when the
+  // sweep leaves half of the SMs idle with one
+  const int cl = 2 * p.n_env <= fvx::device_sm_count() ? 2 : 1;
+  static bool attr_done[4] = {false, false, false, false};
   auto launch = [&](auto kernel, int idx) -> int {
     if (!attr_done[idx]) {
       FVX_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(smem)));
       attr_done[idx] = true;
     }
-    kernel<<<p.n_env, threads, smem, static_cast<cudaStream_t>(stream)>>>(p, *state, step_end);
-    FVX_LAUNCH_CHECK();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(p.n_env * cl));
+    cfg.blockDim = dim3(static_cast<unsigned>(threads));
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = static_cast<cudaStream_t>(stream);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = static_cast<unsigned>(cl);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    FVX_CUDA_TRY(cudaLaunchKernelEx(&cfg, kernel, p, *state, step_end));
+    fvx::note_launch();
     return FVX_OK;
   };
-  if (precision == FVX_PREC_F32C) return launch(sweep_kernel<true>, 1);
-  return launch(sweep_kernel<false>, 0);
+  if (cl == 2) {
+    if (precision == FVX_PREC_F32C) return launch(sweep_kernel<true, 2>, 3);
+    return launch(sweep_kernel<false, 2>, 2);
+  }
+  if (precision == FVX_PREC_F32C) return launch(sweep_kernel<true, 1>, 1);
+  return launch(sweep_kernel<false, 1>, 0);
 }

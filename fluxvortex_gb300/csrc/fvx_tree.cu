@@ -1831,14 +1831,16 @@ __global__ void judge_repair_kernel(JudgeSampleBufs B, const float* __restrict__
 
 // FP64 direct sums of the queued (target, cell) pairs at every particle of
 // the target (a leaf, or a parent of leaves), added to the outputs.
-// Persistent CTAs stride over (pair, slice) items: kFallbackSlices slices of
-// the cell's particles per pair, each at least kFallbackMinSlice particles
-// (the surplus items of a small cell are skipped at once).  Each warp takes
-// whole targets: its lanes stride over the slice, reduce by shuffles and add
-// one atomic per output component, with no block-wide barrier per target.
+// Persistent CTAs stride over (pair, slice) items: each pair's cell is cut
+// into S slices of at least kFallbackMinSlice particles (the surplus items of
+// a small cell are skipped at once), S = 64 for a short queue (the judge's
+// repairs: a few pairs, some of them parents against cells of thousands of
+// particles) and 8 for a long one (whole classes).  Each warp takes whole
+// targets: its lanes stride over the slice, reduce by shuffles and add one
+// atomic per output component, with no block-wide barrier per target.
 constexpr int kFallbackThreads = 256;
 constexpr int kFallbackMinSlice = 128;
-constexpr int kFallbackSlices = 8;
+constexpr int kFallbackSlicesShort = 64, kFallbackSlicesLong = 8, kFallbackShortQueue = 2048;
 struct FallbackTargets {
   const int* start[2];
   const int* count[2];
@@ -1858,16 +1860,17 @@ __global__ void __launch_bounds__(kFallbackThreads) fallback_kernel(
   constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
   constexpr double kC = -0.07957747154594767;
   const int nq = min(*n_fallback, fb_cap);
-  const int64_t items = static_cast<int64_t>(nq) * kFallbackSlices;
+  const int S = nq < kFallbackShortQueue ? kFallbackSlicesShort : kFallbackSlicesLong;
+  const int64_t items = static_cast<int64_t>(nq) * S;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int64_t w = blockIdx.x; w < items; w += gridDim.x) {
-    const int2 pr = fallback[w / kFallbackSlices];
-    const int sl = static_cast<int>(w % kFallbackSlices);
+    const int2 pr = fallback[w / S];
+    const int sl = static_cast<int>(w % S);
     const int li = (pr.x >> 30) & 1, tgt = pr.x & ((1 << 30) - 1);
     const int t0 = (li ? tg.start[1] : tg.start[0])[tgt];
     const int nt = (li ? tg.count[1] : tg.count[0])[tgt];
     const int c0 = cell_start[pr.y], cn = cell_count[pr.y];
-    const int per = max(kFallbackMinSlice, (cn + kFallbackSlices - 1) / kFallbackSlices);
+    const int per = max(kFallbackMinSlice, (cn + S - 1) / S);
     const int64_t s0_64 = c0 + static_cast<int64_t>(sl) * per;
     if (s0_64 >= c0 + cn) continue;
     const int s0 = static_cast<int>(s0_64);
