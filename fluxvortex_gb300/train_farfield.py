@@ -56,11 +56,11 @@ def hybrid_field(n_seed, steps, seed):
             f._sigma[:n].clone(), n)
 
 
-def collect(fields, per_field, leaves, log=print):
+def collect(fields, per_field, leaves, log=print, theta=0.5):
     Xs, Ts, As = [], [], []
     for name, pos, gam, sig, n in fields:
         for leaf in leaves:
-            ts = TreeSweeper(theta=0.5, leaf_target=leaf)
+            ts = TreeSweeper(theta=theta, leaf_target=leaf)
             X, T, A = L.harvest(ts, pos, gam, sig, n, per_field)
             Xs.append(X)
             Ts.append(T)
@@ -85,6 +85,8 @@ def main(argv=None):
     p.add_argument("--hybrid-steps", type=int, default=6)
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--quick", action="store_true", help="small data and few steps")
+    p.add_argument("--theta", type=float, default=0.5,
+                   help="opening angle of the treecode whose accepted pairs are trained on")
     a = p.parse_args(argv)
     t0 = time.time()
     sizes = (1 << 14, 1 << 16) if a.quick else (1 << 16, 1 << 18, 1 << 20)
@@ -92,12 +94,12 @@ def main(argv=None):
     train = list(slab_fields(sizes, (101, 102)))
     train.append(hybrid_field(sizes[-1] // 4, a.hybrid_steps, 103))
     print("training fields:")
-    X, T, A = collect(train, a.per_field, leaves)
+    X, T, A = collect(train, a.per_field, leaves, theta=a.theta)
     del train
     print("validation fields:")
     Xv, Tv, Av = collect(list(slab_fields(sizes[-1:], (201,))) +
                      [hybrid_field(sizes[-1] // 4, a.hybrid_steps, 202)],
-                     a.per_field // 2, leaves)
+                     a.per_field // 2, leaves, theta=a.theta)
     print(f"{X.shape[0]} training / {Xv.shape[0]} validation pairs ({time.time() - t0:.1f} s)")
     m = L.FarFieldMLP(seed=a.seed)
     steps = 300 if a.quick else a.steps
@@ -110,7 +112,7 @@ def main(argv=None):
     print("train relative error (analytic + learned)", tr)
     print("validation relative error (analytic + learned)", va)
     print("validation relative error (analytic alone)", an)
-    m.save(a.out, n_train=X.shape[0], steps=steps, batch=a.batch, lr=a.lr,
+    m.save(a.out, n_train=X.shape[0], steps=steps, batch=a.batch, lr=a.lr, theta=a.theta,
            val_median=va["median"], val_p90=va["p90"], val_p99=va["p99"], val_max=va["max"],
            val_analytic_median=an["median"], val_analytic_p90=an["p90"],
            val_analytic_p99=an["p99"], train_median=tr["median"])
