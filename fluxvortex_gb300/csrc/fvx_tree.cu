@@ -1207,11 +1207,11 @@ __device__ __forceinline__ uint64_t fma(uint64_t a, uint64_t b, uint64_t c) {
 }  // namespace x2
 
 // One row of the packed near tile: {-x, -y}, {-z, s2}, {c1, ax}, {ay, az},
-// {-ax, -ay}, {-az, c2} with c1 = 1.5 s2, c2 = -7.5 s2 (the negated values
-// turn each cross-product and stretching component into two fused
-// multiply-adds), each a 64-bit pair whose halves hold either one source
-// twice (two targets per lane) or two consecutive sources (one target per
-// lane, two source phases).
+// {cx, cy}, {cz, c2} with c1 = 1.5 s2, c2 = -7.5 s2 and c = x_s x a (x_s the
+// source relative to the target leaf's centre, so that the cross product
+// d x a = t x a - c needs no per-pair product), each a 64-bit pair whose
+// halves hold either one source twice (two targets per lane) or two
+// consecutive sources (one target per lane, two source phases).
 struct NearX2 {
   ulonglong2 q[6];
 };
@@ -1232,6 +1232,11 @@ __device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, in
                                              uint64_t TX, uint64_t TY, uint64_t TZ, uint64_t GX,
                                              uint64_t GY, uint64_t GZ, uint64_t* acc) {
   const uint64_t ONE = x2::pack(1.f, 1.f), CM3 = x2::pack(-3.f, -3.f);
+  // d x a = t x a - x_s x a, with c = x_s x a staged per source: the tile's
+  // sums of f a, f c (velocity) or f a, w a, w c (stretching) are formed per
+  // pair, and t x (sum f a) - sum f c, or G x (sum f a) + t x (sum w a) -
+  // sum w c, once per tile
+  uint64_t FA[3] = {0ull, 0ull, 0ull}, FC[3] = {0ull, 0ull, 0ull}, WA[3] = {0ull, 0ull, 0ull};
 #pragma unroll 8
   for (int i = 0; i < nt; ++i) {
     const int k = i * NG;
@@ -1248,26 +1253,47 @@ __device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, in
     const uint64_t T3 = x2::mul(T2, T);
     const uint64_t F = x2::mul(T3, x2::fma(q2.x, T2, ONE));
     const ulonglong2 q4 = tile[k].q[4], q5 = tile[k].q[5];
-    const uint64_t AX = q2.y, AY = q3.x, AZ = q3.y, NAX = q4.x, NAY = q4.y, NAZ = q5.x;
+    const uint64_t AX = q2.y, AY = q3.x, AZ = q3.y, CX = q4.x, CY = q4.y, CZ = q5.x;
     if (MODE == FVX_PAIR_VELOCITY) {
-      const uint64_t EX = x2::mul(F, DX), EY = x2::mul(F, DY), EZ = x2::mul(F, DZ);
-      acc[0] = x2::fma(EZ, NAY, x2::fma(EY, AZ, acc[0]));
-      acc[1] = x2::fma(EX, NAZ, x2::fma(EZ, AX, acc[1]));
-      acc[2] = x2::fma(EY, NAX, x2::fma(EX, AY, acc[2]));
+      FA[0] = x2::fma(F, AX, FA[0]);
+      FA[1] = x2::fma(F, AY, FA[1]);
+      FA[2] = x2::fma(F, AZ, FA[2]);
+      FC[0] = x2::fma(F, CX, FC[0]);
+      FC[1] = x2::fma(F, CY, FC[1]);
+      FC[2] = x2::fma(F, CZ, FC[2]);
     } else {
-      // S += (f G + w d) x a, w = fpr (d . G)
       uint64_t DG = x2::mul(DX, GX);
       DG = x2::fma(DY, GY, DG);
       DG = x2::fma(DZ, GZ, DG);
       const uint64_t T5 = x2::mul(T3, T2);
       const uint64_t W = x2::mul(x2::mul(x2::fma(q5.y, T2, CM3), T5), DG);
-      const uint64_t VX = x2::fma(W, DX, x2::mul(F, GX));
-      const uint64_t VY = x2::fma(W, DY, x2::mul(F, GY));
-      const uint64_t VZ = x2::fma(W, DZ, x2::mul(F, GZ));
-      acc[0] = x2::fma(VZ, NAY, x2::fma(VY, AZ, acc[0]));
-      acc[1] = x2::fma(VX, NAZ, x2::fma(VZ, AX, acc[1]));
-      acc[2] = x2::fma(VY, NAX, x2::fma(VX, AY, acc[2]));
+      FA[0] = x2::fma(F, AX, FA[0]);
+      FA[1] = x2::fma(F, AY, FA[1]);
+      FA[2] = x2::fma(F, AZ, FA[2]);
+      WA[0] = x2::fma(W, AX, WA[0]);
+      WA[1] = x2::fma(W, AY, WA[1]);
+      WA[2] = x2::fma(W, AZ, WA[2]);
+      FC[0] = x2::fma(W, CX, FC[0]);
+      FC[1] = x2::fma(W, CY, FC[1]);
+      FC[2] = x2::fma(W, CZ, FC[2]);
     }
+  }
+  // velocity: sum f (d x a) = t x FA - FC; stretching: sum (f G + w d) x a =
+  // G x FA + t x WA - FC
+  const uint64_t U[3] = {x2::sub(x2::mul(TY, FA[2]), x2::fma(TZ, FA[1], FC[0])),
+                         x2::sub(x2::mul(TZ, FA[0]), x2::fma(TX, FA[2], FC[1])),
+                         x2::sub(x2::mul(TX, FA[1]), x2::fma(TY, FA[0], FC[2]))};
+  if (MODE == FVX_PAIR_VELOCITY) {
+    acc[0] = U[0];
+    acc[1] = U[1];
+    acc[2] = U[2];
+  } else {
+    acc[0] = x2::add(x2::sub(x2::mul(GY, FA[2]), x2::mul(GZ, FA[1])),
+                     x2::sub(x2::sub(x2::mul(TY, WA[2]), x2::mul(TZ, WA[1])), FC[0]));
+    acc[1] = x2::add(x2::sub(x2::mul(GZ, FA[0]), x2::mul(GX, FA[2])),
+                     x2::sub(x2::sub(x2::mul(TZ, WA[0]), x2::mul(TX, WA[2])), FC[1]));
+    acc[2] = x2::add(x2::sub(x2::mul(GX, FA[1]), x2::mul(GY, FA[0])),
+                     x2::sub(x2::sub(x2::mul(TX, WA[1]), x2::mul(TY, WA[0])), FC[2]));
   }
 }
 
@@ -1394,17 +1420,24 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
           for (int r0 = 0; r0 < rows; r0 += kEvalThreads) {
             const int k = r0 + lane;
             float4 p[2], a[2];
+            // each staged source's near leaf, from the leaves' start offsets in
+            // this window of 32 (G = 1) or 64 sources: one bit per start
+            // (near leaves are never empty, so starts are distinct), and a
+            // source's leaf is the number of starts up to it, minus one
+            const int g0 = b0 + (G == 1 ? r0 : 2 * r0);
+            const int pl = excl - g0;
+            const unsigned blo = __reduce_or_sync(full, (pl >= 0 && pl < 32) ? 1u << pl : 0u);
+            const unsigned bhi =
+                __reduce_or_sync(full, (pl >= 32 && pl < 64) ? 1u << (pl - 32) : 0u);
+            const int before = __popc(__ballot_sync(full, pl < 0));
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
               const int sk = G == 1 ? k : 2 * k + h;  // source of this half
               const int g = b0 + (sk < nt ? sk : 0);
-              // near leaf of source g: the lanes whose inclusive prefix is <= g
-              int li = 0;
-#pragma unroll
-              for (int step = 16; step >= 1; step >>= 1) {
-                const int v = __shfl_sync(full, incl, li + step - 1);
-                if (v <= g) li += step;
-              }
+              const int o = G == 1 ? lane : 2 * lane + h;
+              const unsigned m_lo = o >= 31 ? 0xffffffffu : ((2u << o) - 1u);
+              const unsigned m_hi = o >= 63 ? 0xffffffffu : (o >= 32 ? ((2u << (o - 32)) - 1u) : 0u);
+              const int li = before + __popc(blo & m_lo) + __popc(bhi & m_hi) - 1;
               const int lss = __shfl_sync(full, mss, li), lex = __shfl_sync(full, excl, li);
               const float ldx = __shfl_sync(full, mdx, li), ldy = __shfl_sync(full, mdy, li),
                           ldz = __shfl_sync(full, mdz, li);
@@ -1423,8 +1456,16 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
               e.q[2] = make_ulonglong2(x2::pack(1.5f * p[0].w, 1.5f * p[1].w),
                                        x2::pack(a[0].x, a[1].x));
               e.q[3] = make_ulonglong2(x2::pack(a[0].y, a[1].y), x2::pack(a[0].z, a[1].z));
-              e.q[4] = make_ulonglong2(x2::pack(-a[0].x, -a[1].x), x2::pack(-a[0].y, -a[1].y));
-              e.q[5] = make_ulonglong2(x2::pack(-a[0].z, -a[1].z),
+              // c = x_s x a with x_s relative to the target leaf's centre
+              float cx[2], cy[2], cz[2];
+#pragma unroll
+              for (int h = 0; h < 2; ++h) {
+                cx[h] = p[h].y * a[h].z - p[h].z * a[h].y;
+                cy[h] = p[h].z * a[h].x - p[h].x * a[h].z;
+                cz[h] = p[h].x * a[h].y - p[h].y * a[h].x;
+              }
+              e.q[4] = make_ulonglong2(x2::pack(cx[0], cx[1]), x2::pack(cy[0], cy[1]));
+              e.q[5] = make_ulonglong2(x2::pack(cz[0], cz[1]),
                                        x2::pack(-7.5f * p[0].w, -7.5f * p[1].w));
               s_x2[k] = e;
             }
