@@ -108,10 +108,13 @@ namespace tree {
 // ---- bounding box -------------------------------------------------------------
 // Bounding box of the finite positions; particles with a non-finite
 // coordinate are counted into *nonfinite (the sweep refuses them).
+// Bounding box of the positions and the smallest core (7 values per block:
+// lo xyz, hi xyz, min sigma), and the count of non-finite positions.
 __global__ void bbox_partial_kernel(int64_t n, const double* __restrict__ pos,
+                                    const double* __restrict__ sigma,
                                     double* __restrict__ partial,
                                     unsigned* __restrict__ nonfinite) {
-  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, smin = 1e300;
   unsigned bad = 0;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -122,24 +125,28 @@ __global__ void bbox_partial_kernel(int64_t n, const double* __restrict__ pos,
       lo[c] = fmin(lo[c], v);
       hi[c] = fmax(hi[c], v);
     }
+    smin = fmin(smin, sigma[i]);
     bad += fin ? 0u : 1u;
   }
   if (bad) atomicAdd(nonfinite, bad);
-  __shared__ double s[6][256];
+  __shared__ double s[7][256];
   for (int c = 0; c < 3; ++c) {
     s[c][threadIdx.x] = lo[c];
     s[3 + c][threadIdx.x] = hi[c];
   }
+  s[6][threadIdx.x] = smin;
   __syncthreads();
   for (int st = blockDim.x / 2; st > 0; st >>= 1) {
-    if (threadIdx.x < st)
+    if (threadIdx.x < st) {
       for (int c = 0; c < 3; ++c) {
         s[c][threadIdx.x] = fmin(s[c][threadIdx.x], s[c][threadIdx.x + st]);
         s[3 + c][threadIdx.x] = fmax(s[3 + c][threadIdx.x], s[3 + c][threadIdx.x + st]);
       }
+      s[6][threadIdx.x] = fmin(s[6][threadIdx.x], s[6][threadIdx.x + st]);
+    }
     __syncthreads();
   }
-  if (threadIdx.x < 6) partial[blockIdx.x * 6 + threadIdx.x] = s[threadIdx.x][0];
+  if (threadIdx.x < 7) partial[blockIdx.x * 7 + threadIdx.x] = s[threadIdx.x][0];
 }
 
 // One CTA of kBboxFinalThreads: each thread folds a strided share of the
@@ -147,27 +154,32 @@ __global__ void bbox_partial_kernel(int64_t n, const double* __restrict__ pos,
 constexpr int kBboxFinalThreads = 256;
 __global__ void __launch_bounds__(kBboxFinalThreads) bbox_final_kernel(
     int nb, const double* __restrict__ partial, double* __restrict__ out) {
-  double r[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
-  for (int b = threadIdx.x; b < nb; b += kBboxFinalThreads)
+  double r[7] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300, 1e300};
+  for (int b = threadIdx.x; b < nb; b += kBboxFinalThreads) {
     for (int c = 0; c < 3; ++c) {
-      r[c] = fmin(r[c], partial[b * 6 + c]);
-      r[3 + c] = fmax(r[3 + c], partial[b * 6 + 3 + c]);
+      r[c] = fmin(r[c], partial[b * 7 + c]);
+      r[3 + c] = fmax(r[3 + c], partial[b * 7 + 3 + c]);
     }
+    r[6] = fmin(r[6], partial[b * 7 + 6]);
+  }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1)
+  for (int o = 16; o > 0; o >>= 1) {
     for (int c = 0; c < 3; ++c) {
       r[c] = fmin(r[c], __shfl_xor_sync(0xffffffffu, r[c], o));
       r[3 + c] = fmax(r[3 + c], __shfl_xor_sync(0xffffffffu, r[3 + c], o));
     }
-  __shared__ double s[kBboxFinalThreads / 32][6];
+    r[6] = fmin(r[6], __shfl_xor_sync(0xffffffffu, r[6], o));
+  }
+  __shared__ double s[kBboxFinalThreads / 32][7];
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0)
-    for (int c = 0; c < 6; ++c) s[w][c] = r[c];
+    for (int c = 0; c < 7; ++c) s[w][c] = r[c];
   __syncthreads();
-  if (threadIdx.x < 6) {
+  if (threadIdx.x < 7) {
     const int c = threadIdx.x;
     double v = s[0][c];
-    for (int k = 1; k < kBboxFinalThreads / 32; ++k) v = c < 3 ? fmin(v, s[k][c]) : fmax(v, s[k][c]);
+    for (int k = 1; k < kBboxFinalThreads / 32; ++k)
+      v = (c < 3 || c == 6) ? fmin(v, s[k][c]) : fmax(v, s[k][c]);
     out[c] = v;
   }
 }
@@ -1207,11 +1219,13 @@ __device__ __forceinline__ uint64_t fma(uint64_t a, uint64_t b, uint64_t c) {
 }  // namespace x2
 
 // One row of the packed near tile: {-x, -y}, {-z, s2}, {c1, ax}, {ay, az},
-// {cx, cy}, {cz, c2} with c1 = 1.5 s2, c2 = -7.5 s2 and c = x_s x a (x_s the
-// source relative to the target leaf's centre, so that the cross product
-// d x a = t x a - c needs no per-pair product), each a 64-bit pair whose
-// halves hold either one source twice (two targets per lane) or two
-// consecutive sources (one target per lane, two source phases).
+// {-ax, -ay}, {-az, c2} with c1 = 1.5 s2, c2 = -7.5 s2 (the negated values
+// turn each cross-product and stretching component into two fused
+// multiply-adds); in the factored form the fifth and sixth pairs hold
+// {cx, cy}, {cz, c2} instead, c = x_s x a with x_s the source relative to the
+// target leaf's centre.  Each is a 64-bit pair whose halves hold either one
+// source twice (two targets per lane) or two consecutive sources (one target
+// per lane, two source phases).
 struct NearX2 {
   ulonglong2 q[6];
 };
@@ -1228,7 +1242,57 @@ struct NearX2 {
 // small leaves interleave), a compile-time constant so that the unrolled loop
 // addresses its rows by immediate offsets.
 template <int MODE, int NG>
-__device__ __forceinline__ void near_tile_x2(const NearX2* __restrict__ tile, int nt,
+__device__ __forceinline__ void near_tile_x2_direct(const NearX2* __restrict__ tile, int nt,
+                                             uint64_t TX, uint64_t TY, uint64_t TZ, uint64_t GX,
+                                             uint64_t GY, uint64_t GZ, uint64_t* acc) {
+  const uint64_t ONE = x2::pack(1.f, 1.f), CM3 = x2::pack(-3.f, -3.f);
+#pragma unroll 8
+  for (int i = 0; i < nt; ++i) {
+    const int k = i * NG;
+    const ulonglong2 q0 = tile[k].q[0], q1 = tile[k].q[1], q2 = tile[k].q[2],
+                     q3 = tile[k].q[3];
+    const uint64_t DX = x2::add(TX, q0.x), DY = x2::add(TY, q0.y), DZ = x2::add(TZ, q1.x);
+    uint64_t Q = x2::fma(DX, DX, q1.y);
+    Q = x2::fma(DY, DY, Q);
+    Q = x2::fma(DZ, DZ, Q);
+    float qa, qb;
+    x2::unpack(Q, qa, qb);
+    const uint64_t T = x2::pack(rsqrt_ftz(qa), rsqrt_ftz(qb));
+    const uint64_t T2 = x2::mul(T, T);
+    const uint64_t T3 = x2::mul(T2, T);
+    const uint64_t F = x2::mul(T3, x2::fma(q2.x, T2, ONE));
+    const ulonglong2 q4 = tile[k].q[4], q5 = tile[k].q[5];
+    const uint64_t AX = q2.y, AY = q3.x, AZ = q3.y, NAX = q4.x, NAY = q4.y, NAZ = q5.x;
+    if (MODE == FVX_PAIR_VELOCITY) {
+      const uint64_t EX = x2::mul(F, DX), EY = x2::mul(F, DY), EZ = x2::mul(F, DZ);
+      acc[0] = x2::fma(EZ, NAY, x2::fma(EY, AZ, acc[0]));
+      acc[1] = x2::fma(EX, NAZ, x2::fma(EZ, AX, acc[1]));
+      acc[2] = x2::fma(EY, NAX, x2::fma(EX, AY, acc[2]));
+    } else {
+      // S += (f G + w d) x a, w = fpr (d . G)
+      uint64_t DG = x2::mul(DX, GX);
+      DG = x2::fma(DY, GY, DG);
+      DG = x2::fma(DZ, GZ, DG);
+      const uint64_t T5 = x2::mul(T3, T2);
+      const uint64_t W = x2::mul(x2::mul(x2::fma(q5.y, T2, CM3), T5), DG);
+      const uint64_t VX = x2::fma(W, DX, x2::mul(F, GX));
+      const uint64_t VY = x2::fma(W, DY, x2::mul(F, GY));
+      const uint64_t VZ = x2::fma(W, DZ, x2::mul(F, GZ));
+      acc[0] = x2::fma(VZ, NAY, x2::fma(VY, AZ, acc[0]));
+      acc[1] = x2::fma(VX, NAZ, x2::fma(VZ, AX, acc[1]));
+      acc[2] = x2::fma(VY, NAX, x2::fma(VX, AY, acc[2]));
+    }
+  }
+}
+
+// The same sums in the factored form (FACT): d x a = t x a - x_s x a with
+// c = x_s x a staged per source.  Fewer paired operations per row (16 / 26
+// instead of 19 / 29), but t x (sum f a) and sum f c cancel where |d| is far
+// below |x_s|, so the sweep takes this form only when the leaf size is at
+// most 4 times the smallest core (|x_s| <= ~2 h, and the rounding stays
+// within a few FP32 units of a source's peak contribution).
+template <int MODE, int NG>
+__device__ __forceinline__ void near_tile_x2_factored(const NearX2* __restrict__ tile, int nt,
                                              uint64_t TX, uint64_t TY, uint64_t TZ, uint64_t GX,
                                              uint64_t GY, uint64_t GZ, uint64_t* acc) {
   const uint64_t ONE = x2::pack(1.f, 1.f), CM3 = x2::pack(-3.f, -3.f);
@@ -1312,7 +1376,7 @@ struct EvalSmem {
 
 // Leaf t: its targets against its near leaves and far cells, plus the local
 // expansions (one warp).
-template <int MODE, int KERNEL, int TPT>
+template <int MODE, int KERNEL, int TPT, bool FACT>
 __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned char* s_raw) {
   using namespace pair;
   constexpr int NC = ModeInfo<MODE>::ncomp;
@@ -1456,13 +1520,20 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
               e.q[2] = make_ulonglong2(x2::pack(1.5f * p[0].w, 1.5f * p[1].w),
                                        x2::pack(a[0].x, a[1].x));
               e.q[3] = make_ulonglong2(x2::pack(a[0].y, a[1].y), x2::pack(a[0].z, a[1].z));
-              // c = x_s x a with x_s relative to the target leaf's centre
+              // factored form: c = x_s x a, x_s relative to the target
+              // leaf's centre; direct form: the negated strengths
               float cx[2], cy[2], cz[2];
 #pragma unroll
               for (int h = 0; h < 2; ++h) {
-                cx[h] = p[h].y * a[h].z - p[h].z * a[h].y;
-                cy[h] = p[h].z * a[h].x - p[h].x * a[h].z;
-                cz[h] = p[h].x * a[h].y - p[h].y * a[h].x;
+                if constexpr (FACT) {
+                  cx[h] = p[h].y * a[h].z - p[h].z * a[h].y;
+                  cy[h] = p[h].z * a[h].x - p[h].x * a[h].z;
+                  cz[h] = p[h].x * a[h].y - p[h].y * a[h].x;
+                } else {
+                  cx[h] = -a[h].x;
+                  cy[h] = -a[h].y;
+                  cz[h] = -a[h].z;
+                }
               }
               e.q[4] = make_ulonglong2(x2::pack(cx[0], cx[1]), x2::pack(cy[0], cy[1]));
               e.q[5] = make_ulonglong2(x2::pack(cz[0], cz[1]),
@@ -1473,12 +1544,21 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
           __syncthreads();
           uint64_t acc2[3] = {0ull, 0ull, 0ull};
           const NearX2* tile = s_x2 + (G == 1 ? 0 : grp);
-          if (ng == 1)
-            near_tile_x2<MODE, 1>(tile, rows, TX, TY, TZ, GX, GY, GZ, acc2);
-          else if (ng == 2)
-            near_tile_x2<MODE, 2>(tile, rows / 2, TX, TY, TZ, GX, GY, GZ, acc2);
-          else
-            near_tile_x2<MODE, 4>(tile, rows / 4, TX, TY, TZ, GX, GY, GZ, acc2);
+          if constexpr (FACT) {
+            if (ng == 1)
+              near_tile_x2_factored<MODE, 1>(tile, rows, TX, TY, TZ, GX, GY, GZ, acc2);
+            else if (ng == 2)
+              near_tile_x2_factored<MODE, 2>(tile, rows / 2, TX, TY, TZ, GX, GY, GZ, acc2);
+            else
+              near_tile_x2_factored<MODE, 4>(tile, rows / 4, TX, TY, TZ, GX, GY, GZ, acc2);
+          } else {
+            if (ng == 1)
+              near_tile_x2_direct<MODE, 1>(tile, rows, TX, TY, TZ, GX, GY, GZ, acc2);
+            else if (ng == 2)
+              near_tile_x2_direct<MODE, 2>(tile, rows / 2, TX, TY, TZ, GX, GY, GZ, acc2);
+            else
+              near_tile_x2_direct<MODE, 4>(tile, rows / 4, TX, TY, TZ, GX, GY, GZ, acc2);
+          }
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             float a0, a1;
@@ -1620,7 +1700,7 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
 // until none are left: the SMs stay at their occupancy limit to the end, and
 // no CTA is launched per leaf.  The leaves come in decreasing order of their
 // near-field work, so the last ones taken are the shortest.
-template <int MODE, int KERNEL, int TPT>
+template <int MODE, int KERNEL, int TPT, bool FACT = false>
 __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
   __shared__ __align__(16) unsigned char s_raw[EvalSmem<MODE, KERNEL, TPT>::bytes];
   for (;;) {
@@ -1628,7 +1708,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
     if (threadIdx.x == 0) c = atomicAdd(A.leaf_next, 1);
     c = __shfl_sync(0xffffffffu, c, 0);
     if (c >= A.nleaf) break;
-    eval_leaf<MODE, KERNEL, TPT>(A, A.leaf_order[c], s_raw);
+    eval_leaf<MODE, KERNEL, TPT, FACT>(A, A.leaf_order[c], s_raw);
     __syncthreads();  // the next leaf restages the shared buffer
   }
 }
@@ -2044,6 +2124,7 @@ struct fvx_tree {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // around the last evaluation launch
   // far-field method of the pairs beyond theta_l (FVX_FAR_*)
   int far_method = FVX_FAR_M2P;
+  double sigma_min = 0.0;  // smallest core at the last full build
   const void* mlp_W = nullptr;
   const float* mlp_b = nullptr;
   double theta_l = 0.0;
@@ -2121,16 +2202,20 @@ int resident_grid(K kernel, int nleaf) {
 // Targets per thread: leaves of at most ~40 particles on average fill one
 // 32-target chunk per warp better than two.
 template <int KERNEL, int TPT>
-void launch_eval_tpt(int mode, int nleaf, const tree::EvalArgs& A, cudaStream_t s) {
+void launch_eval_tpt(int mode, int nleaf, const tree::EvalArgs& A, bool factored,
+                     cudaStream_t s) {
   using namespace tree;
+  constexpr bool F = KERNEL == FVX_KERNEL_WINCKELMANS && TPT == 2;  // the paired kernels
   switch (mode) {
     case FVX_PAIR_VELOCITY: {
-      auto k = eval_kernel<FVX_PAIR_VELOCITY, KERNEL, TPT>;
+      auto k = F && factored ? eval_kernel<FVX_PAIR_VELOCITY, KERNEL, TPT, F>
+                             : eval_kernel<FVX_PAIR_VELOCITY, KERNEL, TPT>;
       k<<<resident_grid(k, nleaf), kEvalThreads, 0, s>>>(A);
       break;
     }
     case FVX_PAIR_STRETCH: {
-      auto k = eval_kernel<FVX_PAIR_STRETCH, KERNEL, TPT>;
+      auto k = F && factored ? eval_kernel<FVX_PAIR_STRETCH, KERNEL, TPT, F>
+                             : eval_kernel<FVX_PAIR_STRETCH, KERNEL, TPT>;
       k<<<resident_grid(k, nleaf), kEvalThreads, 0, s>>>(A);
       break;
     }
@@ -2148,7 +2233,8 @@ void launch_eval_tpt(int mode, int nleaf, const tree::EvalArgs& A, cudaStream_t 
 }
 
 template <int KERNEL>
-void launch_eval(int mode, int nleaf, int n, const tree::EvalArgs& A, cudaStream_t s) {
+void launch_eval(int mode, int nleaf, int n, const tree::EvalArgs& A, bool factored,
+                 cudaStream_t s) {
   // Winckelmans velocity and stretching: the paired f32x2 kernel, whose
   // source phases keep small leaves' slots busy.  Otherwise two targets per
   // thread once leaves average more than ~40 particles; at fewer, one target
@@ -2156,9 +2242,9 @@ void launch_eval(int mode, int nleaf, int n, const tree::EvalArgs& A, cudaStream
   const bool paired = KERNEL == FVX_KERNEL_WINCKELMANS &&
                       (mode == FVX_PAIR_VELOCITY || mode == FVX_PAIR_STRETCH);
   if (!paired && n <= 40 * nleaf)
-    launch_eval_tpt<KERNEL, 1>(mode, nleaf, A, s);
+    launch_eval_tpt<KERNEL, 1>(mode, nleaf, A, false, s);
   else
-    launch_eval_tpt<KERNEL, 2>(mode, nleaf, A, s);
+    launch_eval_tpt<KERNEL, 2>(mode, nleaf, A, factored, s);
 }
 
 template <int KERNEL>
@@ -2251,17 +2337,17 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   ST.valid = false;
   // 1. bounding box -> grid
   const int nbb = 256;
-  if ((rc = grow(T->bbox, sizeof(double) * (6 * nbb + 7)))) return rc;
-  unsigned* nonfinite = reinterpret_cast<unsigned*>(P<double>(T->bbox) + 6 * nbb + 6);
+  if ((rc = grow(T->bbox, sizeof(double) * (7 * nbb + 8)))) return rc;
+  unsigned* nonfinite = reinterpret_cast<unsigned*>(P<double>(T->bbox) + 7 * nbb + 7);
   FVX_CUDA_TRY(cudaMemsetAsync(nonfinite, 0, sizeof(unsigned), s));
-  bbox_partial_kernel<<<nbb, 256, 0, s>>>(n, pos, P<double>(T->bbox), nonfinite);
+  bbox_partial_kernel<<<nbb, 256, 0, s>>>(n, pos, sigma, P<double>(T->bbox), nonfinite);
   FVX_LAUNCH_CHECK();
   bbox_final_kernel<<<1, kBboxFinalThreads, 0, s>>>(nbb, P<double>(T->bbox),
-                                                    P<double>(T->bbox) + 6 * nbb);
+                                                    P<double>(T->bbox) + 7 * nbb);
   FVX_LAUNCH_CHECK();
-  double lohi[6];
+  double lohi[7];
   unsigned nbad = 0;
-  FVX_CUDA_TRY(cudaMemcpyAsync(lohi, P<double>(T->bbox) + 6 * nbb, sizeof(lohi),
+  FVX_CUDA_TRY(cudaMemcpyAsync(lohi, P<double>(T->bbox) + 7 * nbb, sizeof(lohi),
                                cudaMemcpyDeviceToHost, s));
   FVX_CUDA_TRY(cudaMemcpyAsync(&nbad, nonfinite, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   FVX_CUDA_TRY(cudaStreamSynchronize(s));
@@ -2269,6 +2355,7 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   // cell) and turn the sweep into an all-pairs sum on a few CTAs
   FVX_ARG_CHECK(nbad == 0, "treecode: %u particles with non-finite positions", nbad);
   grid_params(lohi, lohi + 3, n, leaf_target, &L, &h, origin);
+  T->sigma_min = lohi[6];
   // level capacities and bases
   cap[L] = n;
   for (int l = L - 1; l >= 0; --l) {
@@ -2838,10 +2925,13 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   A.leaf_next = P<int>(T->eval_next);
   A.leaf_order = P<int>(T->leaf_order);
   FVX_CUDA_TRY(cudaEventRecord(T->ev0, s));
+  // the factored near loop where leaves are at most 4 smallest cores wide (the
+  // cores of the last full build; see near_tile_x2_factored)
+  const bool factored = h <= 4.0 * T->sigma_min;
   if (kernel == FVX_KERNEL_WINCKELMANS)
-    launch_eval<FVX_KERNEL_WINCKELMANS>(mode, nleaf, n, A, s);
+    launch_eval<FVX_KERNEL_WINCKELMANS>(mode, nleaf, n, A, factored, s);
   else
-    launch_eval<FVX_KERNEL_GAUSSIANERF>(mode, nleaf, n, A, s);
+    launch_eval<FVX_KERNEL_GAUSSIANERF>(mode, nleaf, n, A, factored, s);
   FVX_LAUNCH_CHECK();
   FVX_CUDA_TRY(cudaEventRecord(T->ev1, s));
   // FP64 direct sums of the queued pairs (whole classes and sampled repairs)
