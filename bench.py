@@ -121,6 +121,9 @@ def parse():
                         "the seeded slab (the profiling case of the evaluation and network "
                         "kernels); --repeat R more pairs print median kernel times")
     p.add_argument("--repeat", type=int, default=0)
+    p.add_argument("--sweep-core", choices=("thin", "resolved"), default="thin",
+                   help="--sweep-case cores: 0.02c (the slab sweep case) or 1.3 x the "
+                        "particle spacing (the benchmarked step's slab)")
     return p.parse_args()
 
 
@@ -363,7 +366,9 @@ def flutter_sweep_measure(args):
 def run_sweep_case(args):
     """One treecode self-sweep pair (velocity, then stretching) of the seeded
     slab wake (``workloads.slab_wake``: uniform in a 20c x 10c x 2c slab,
-    sigma 0.02c) with the chosen far field and FP64 validation off: the
+    sigma 0.02c, or with ``--sweep-core resolved`` 1.3 x the particle spacing
+    as in the benchmarked step) with the chosen far field and FP64 validation
+    off: the
     smallest complete invocation of the particle hot path, used as the
     profiling case of the evaluation, translation and network kernels.
     ``--repeat R`` runs R more sweep pairs at the same positions and prints the
@@ -372,9 +377,10 @@ def run_sweep_case(args):
     import torch
     from fluxvortex_gb300 import _capi
     from fluxvortex_gb300.tree import TreeSweeper
-    from fluxvortex_gb300.workloads import slab_wake
+    from fluxvortex_gb300.workloads import resolved_core, slab_wake
     ff = {"tree": "m2p", "direct": "m2p"}.get(args.far_field, args.far_field)
-    pos, gam, sig, _ = slab_wake(args.n)
+    core = resolved_core(args.n) if args.sweep_core == "resolved" else None
+    pos, gam, sig, _ = slab_wake(args.n, sigma=core)
     d = lambda x: torch.as_tensor(x, dtype=torch.float64, device="cuda")  # noqa: E731
     P, G, S = d(pos), d(gam), d(sig)
     ts = TreeSweeper(theta=0.5, leaf_target=args.leaf)

@@ -40,7 +40,6 @@ constexpr int kSortItems = 1024;   // keys per radix-sort block (256 threads x 4
 constexpr int kEvalThreads = 32;   // eval CTA (one warp); 1 or 2 targets per thread
 constexpr int kFarTile = 32;       // far cells staged per tile
 constexpr int kNearTile = 128;     // source particles staged per tile
-constexpr int kNearRows = 64;      // paired path: staged rows per tile (2 sources each, G > 1)
 constexpr int kRecFloats = 40;     // far-cell record
 constexpr double kC = -0.07957747154594767;  // -1/(4 pi)
 
@@ -1193,6 +1192,7 @@ __device__ __forceinline__ uint64_t pack(float a, float b) {
   asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
   return r;
 }
+__device__ __forceinline__ uint64_t dup(float a) { return pack(a, a); }
 __device__ __forceinline__ void unpack(uint64_t v, float& a, float& b) {
   asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
 }
@@ -1218,41 +1218,45 @@ __device__ __forceinline__ uint64_t fma(uint64_t a, uint64_t b, uint64_t c) {
 }
 }  // namespace x2
 
-// One row of the packed near tile: {-x, -y}, {-z, s2}, {c1, ax}, {ay, az},
-// {-ax, -ay}, {-az, c2} with c1 = 1.5 s2, c2 = -7.5 s2 (the negated values
-// turn each cross-product and stretching component into two fused
-// multiply-adds); in the factored form the fifth and sixth pairs hold
-// {cx, cy}, {cz, c2} instead, c = x_s x a with x_s the source relative to the
-// target leaf's centre.  Each is a 64-bit pair whose halves hold either one
-// source twice (two targets per lane) or two consecutive sources (one target
-// per lane, two source phases).
-struct NearX2 {
-  ulonglong2 q[6];
-};
+// The packed near tile: kNearTile staged sources, one per row, in planes of
+// 16-byte words (plane w of row k at w * kNearTile + k), so that a warp
+// staging consecutive rows writes consecutive words without bank conflicts:
+//   direct:   {-x, -y, -z, s2}, {c1, ax, ay, az}
+//   factored: {x, y, z, S},     {c1, ax, ay, az}, {cx, cy, cz, 0}
+// with c1 = 1.5 s2, x_s = (x, y, z) the source relative to the target leaf's
+// centre, S = |x_s|^2 + s2 and c = x_s x a.  Each lane holds two targets in
+// the halves of its paired registers and reads one row per step, duplicating
+// each value into both halves: a broadcast 16-byte load costs the
+// shared-memory pipe two wavefronts, so one source for two targets per load
+// takes half the wavefronts of two sources for one target.
+constexpr int kPlanes = 3;
 
-// Near pairs of one staged tile for the thread's two target slots (Winckelmans
-// core, velocity or stretching) with paired FP32 instructions.  With
-// q = r^2 + s^2 and t = q^-1/2 the core terms are written in q alone,
-//   f   = (r^2 + 2.5 s^2) t^5  = t^3 (1 + 1.5 s^2 t^2),
-//   fpr = -(3 r^2 + 10.5 s^2) t^7 = t^5 (-3 - 7.5 s^2 t^2),
+// Near pairs of one staged tile (rows grp, grp + g, ... : nit of them) for the
+// thread's two targets (Winckelmans core, velocity or stretching) in paired
+// FP32 arithmetic.  With q = r^2 + s^2, t = q^-1/2 and u = 1.5 s^2 t^2,
+//   f   = (r^2 + 2.5 s^2) t^5  = t^3 (1 + u),
+//   fpr = -(3 r^2 + 10.5 s^2) t^7 = -5 t^5 (u + 0.6),
 // so q comes from three fused multiply-adds seeded with s^2, r^2 is never
 // formed, and every factor stays bounded (no FP32 overflow for cores down to
-// the integrator's 1e-6 floor).
-// NG: rows between a lane group's consecutive rows (the G/2 lane groups of
-// small leaves interleave), a compile-time constant so that the unrolled loop
-// addresses its rows by immediate offsets.
-template <int MODE, int NG>
-__device__ __forceinline__ void near_tile_x2_direct(const NearX2* __restrict__ tile, int nt,
-                                             uint64_t TX, uint64_t TY, uint64_t TZ, uint64_t GX,
-                                             uint64_t GY, uint64_t GZ, uint64_t* acc) {
-  const uint64_t ONE = x2::pack(1.f, 1.f), CM3 = x2::pack(-3.f, -3.f);
-#pragma unroll 8
-  for (int i = 0; i < nt; ++i) {
-    const int k = i * NG;
-    const ulonglong2 q0 = tile[k].q[0], q1 = tile[k].q[1], q2 = tile[k].q[2],
-                     q3 = tile[k].q[3];
-    const uint64_t DX = x2::add(TX, q0.x), DY = x2::add(TY, q0.y), DZ = x2::add(TZ, q1.x);
-    uint64_t Q = x2::fma(DX, DX, q1.y);
+// the integrator's 1e-6 floor).  The cross products with the strengths are
+// summed as two sums per component (sum e_y a_z and sum e_z a_y, ...),
+// subtracted once per tile.
+// Per-target constants: T = t, G = the target's strength, G5 = -5 G.
+template <int MODE>
+__device__ __forceinline__ void near_tile_direct(const float4* __restrict__ row, int nit, int g,
+                                                 uint64_t TX, uint64_t TY, uint64_t TZ,
+                                                 uint64_t GX, uint64_t GY, uint64_t GZ,
+                                                 uint64_t G5X, uint64_t G5Y, uint64_t G5Z,
+                                                 uint64_t* acc) {
+  const uint64_t ONE = x2::pack(1.f, 1.f), C06 = x2::pack(0.6f, 0.6f);
+  uint64_t PS[3] = {0ull, 0ull, 0ull}, MS[3] = {0ull, 0ull, 0ull};
+#pragma unroll 4
+  for (int i = 0; i < nit; ++i) {
+    const float4* r = row + i * g;
+    const float4 u0 = r[0], u1 = r[kNearTile];
+    const uint64_t DX = x2::add(TX, x2::dup(u0.x)), DY = x2::add(TY, x2::dup(u0.y)),
+                   DZ = x2::add(TZ, x2::dup(u0.z));
+    uint64_t Q = x2::fma(DX, DX, x2::dup(u0.w));
     Q = x2::fma(DY, DY, Q);
     Q = x2::fma(DZ, DZ, Q);
     float qa, qb;
@@ -1260,104 +1264,119 @@ __device__ __forceinline__ void near_tile_x2_direct(const NearX2* __restrict__ t
     const uint64_t T = x2::pack(rsqrt_ftz(qa), rsqrt_ftz(qb));
     const uint64_t T2 = x2::mul(T, T);
     const uint64_t T3 = x2::mul(T2, T);
-    const uint64_t F = x2::mul(T3, x2::fma(q2.x, T2, ONE));
-    const ulonglong2 q4 = tile[k].q[4], q5 = tile[k].q[5];
-    const uint64_t AX = q2.y, AY = q3.x, AZ = q3.y, NAX = q4.x, NAY = q4.y, NAZ = q5.x;
+    const uint64_t C1 = x2::dup(u1.x);
+    const uint64_t AX = x2::dup(u1.y), AY = x2::dup(u1.z), AZ = x2::dup(u1.w);
+    uint64_t EX, EY, EZ;
     if (MODE == FVX_PAIR_VELOCITY) {
-      const uint64_t EX = x2::mul(F, DX), EY = x2::mul(F, DY), EZ = x2::mul(F, DZ);
-      acc[0] = x2::fma(EZ, NAY, x2::fma(EY, AZ, acc[0]));
-      acc[1] = x2::fma(EX, NAZ, x2::fma(EZ, AX, acc[1]));
-      acc[2] = x2::fma(EY, NAX, x2::fma(EX, AY, acc[2]));
+      const uint64_t F = x2::mul(T3, x2::fma(C1, T2, ONE));
+      EX = x2::mul(F, DX);
+      EY = x2::mul(F, DY);
+      EZ = x2::mul(F, DZ);
     } else {
-      // S += (f G + w d) x a, w = fpr (d . G)
-      uint64_t DG = x2::mul(DX, GX);
-      DG = x2::fma(DY, GY, DG);
-      DG = x2::fma(DZ, GZ, DG);
+      // e = f G + w d, w = fpr (d . G)
       const uint64_t T5 = x2::mul(T3, T2);
-      const uint64_t W = x2::mul(x2::mul(x2::fma(q5.y, T2, CM3), T5), DG);
-      const uint64_t VX = x2::fma(W, DX, x2::mul(F, GX));
-      const uint64_t VY = x2::fma(W, DY, x2::mul(F, GY));
-      const uint64_t VZ = x2::fma(W, DZ, x2::mul(F, GZ));
-      acc[0] = x2::fma(VZ, NAY, x2::fma(VY, AZ, acc[0]));
-      acc[1] = x2::fma(VX, NAZ, x2::fma(VZ, AX, acc[1]));
-      acc[2] = x2::fma(VY, NAX, x2::fma(VX, AY, acc[2]));
+      const uint64_t F = x2::fma(C1, T5, T3);
+      uint64_t DG5 = x2::mul(DX, G5X);
+      DG5 = x2::fma(DY, G5Y, DG5);
+      DG5 = x2::fma(DZ, G5Z, DG5);
+      const uint64_t W = x2::mul(x2::mul(x2::fma(C1, T2, C06), T5), DG5);
+      EX = x2::fma(W, DX, x2::mul(F, GX));
+      EY = x2::fma(W, DY, x2::mul(F, GY));
+      EZ = x2::fma(W, DZ, x2::mul(F, GZ));
     }
+    PS[0] = x2::fma(EY, AZ, PS[0]);
+    MS[0] = x2::fma(EZ, AY, MS[0]);
+    PS[1] = x2::fma(EZ, AX, PS[1]);
+    MS[1] = x2::fma(EX, AZ, MS[1]);
+    PS[2] = x2::fma(EX, AY, PS[2]);
+    MS[2] = x2::fma(EY, AX, MS[2]);
   }
+  acc[0] = x2::sub(PS[0], MS[0]);
+  acc[1] = x2::sub(PS[1], MS[1]);
+  acc[2] = x2::sub(PS[2], MS[2]);
 }
 
 // The same sums in the factored form (FACT): d x a = t x a - x_s x a with
-// c = x_s x a staged per source.  Fewer paired operations per row (16 / 26
-// instead of 19 / 29), but t x (sum f a) and sum f c cancel where |d| is far
-// below |x_s|, so the sweep takes this form only when the leaf size is at
-// most 4 times the smallest core (|x_s| <= ~2 h, and the rounding stays
-// within a few FP32 units of a source's peak contribution).
-template <int MODE, int NG>
-__device__ __forceinline__ void near_tile_x2_factored(const NearX2* __restrict__ tile, int nt,
-                                             uint64_t TX, uint64_t TY, uint64_t TZ, uint64_t GX,
-                                             uint64_t GY, uint64_t GZ, uint64_t* acc) {
-  const uint64_t ONE = x2::pack(1.f, 1.f), CM3 = x2::pack(-3.f, -3.f);
-  // d x a = t x a - x_s x a, with c = x_s x a staged per source: the tile's
-  // sums of f a, f c (velocity) or f a, w a, w c (stretching) are formed per
-  // pair, and t x (sum f a) - sum f c, or G x (sum f a) + t x (sum w a) -
-  // sum w c, once per tile
-  uint64_t FA[3] = {0ull, 0ull, 0ull}, FC[3] = {0ull, 0ull, 0ull}, WA[3] = {0ull, 0ull, 0ull};
-#pragma unroll 8
-  for (int i = 0; i < nt; ++i) {
-    const int k = i * NG;
-    const ulonglong2 q0 = tile[k].q[0], q1 = tile[k].q[1], q2 = tile[k].q[2],
-                     q3 = tile[k].q[3];
-    const uint64_t DX = x2::add(TX, q0.x), DY = x2::add(TY, q0.y), DZ = x2::add(TZ, q1.x);
-    uint64_t Q = x2::fma(DX, DX, q1.y);
-    Q = x2::fma(DY, DY, Q);
-    Q = x2::fma(DZ, DZ, Q);
+// c = x_s x a staged per source, and d never formed: q = |t|^2 + S - 2 t . x_s
+// and d . G = t . G - x_s . G take three fused multiply-adds each from
+// per-target constants.  Velocity sums f a and f c (14 paired operations per
+// pair of pairs, 19 in the direct form), stretching f a, w' a and w' c with
+// w = -5 w' (23, 28 in the direct form); the factor -5 and the cross products
+// with t and G are applied once per tile.  The sums cancel where |d| is far
+// below |x_s| or |t|, so a sweep takes this form only when the leaf size is
+// at most 4 times the smallest core (|t|, |x_s| of order h, q >= s^2 >=
+// h^2 / 16, and the rounding stays within a few tens of FP32 units of q and
+// of a source's peak contribution).
+// Per-target constants: M2 = -2 t, TT = |t|^2, NG = -G, TG = t . G.
+template <int MODE>
+__device__ __forceinline__ void near_tile_factored(const float4* __restrict__ row, int nit, int g,
+                                                   uint64_t M2X, uint64_t M2Y, uint64_t M2Z,
+                                                   uint64_t TT, uint64_t NGX, uint64_t NGY,
+                                                   uint64_t NGZ, uint64_t TG, uint64_t* acc) {
+  const uint64_t ONE = x2::pack(1.f, 1.f), C06 = x2::pack(0.6f, 0.6f);
+  uint64_t FA[3] = {0ull, 0ull, 0ull}, WA[3] = {0ull, 0ull, 0ull}, WC[3] = {0ull, 0ull, 0ull};
+#pragma unroll 4
+  for (int i = 0; i < nit; ++i) {
+    const float4* r = row + i * g;
+    const float4 u0 = r[0], u1 = r[kNearTile], u2 = r[2 * kNearTile];
+    const uint64_t X = x2::dup(u0.x), Y = x2::dup(u0.y), Z = x2::dup(u0.z);
+    uint64_t Q = x2::add(TT, x2::dup(u0.w));
+    Q = x2::fma(M2X, X, Q);
+    Q = x2::fma(M2Y, Y, Q);
+    Q = x2::fma(M2Z, Z, Q);
     float qa, qb;
     x2::unpack(Q, qa, qb);
     const uint64_t T = x2::pack(rsqrt_ftz(qa), rsqrt_ftz(qb));
     const uint64_t T2 = x2::mul(T, T);
     const uint64_t T3 = x2::mul(T2, T);
-    const uint64_t F = x2::mul(T3, x2::fma(q2.x, T2, ONE));
-    const ulonglong2 q4 = tile[k].q[4], q5 = tile[k].q[5];
-    const uint64_t AX = q2.y, AY = q3.x, AZ = q3.y, CX = q4.x, CY = q4.y, CZ = q5.x;
+    const uint64_t C1 = x2::dup(u1.x);
+    const uint64_t AX = x2::dup(u1.y), AY = x2::dup(u1.z), AZ = x2::dup(u1.w);
+    const uint64_t CX = x2::dup(u2.x), CY = x2::dup(u2.y), CZ = x2::dup(u2.z);
     if (MODE == FVX_PAIR_VELOCITY) {
+      const uint64_t F = x2::mul(T3, x2::fma(C1, T2, ONE));
       FA[0] = x2::fma(F, AX, FA[0]);
       FA[1] = x2::fma(F, AY, FA[1]);
       FA[2] = x2::fma(F, AZ, FA[2]);
-      FC[0] = x2::fma(F, CX, FC[0]);
-      FC[1] = x2::fma(F, CY, FC[1]);
-      FC[2] = x2::fma(F, CZ, FC[2]);
+      WC[0] = x2::fma(F, CX, WC[0]);
+      WC[1] = x2::fma(F, CY, WC[1]);
+      WC[2] = x2::fma(F, CZ, WC[2]);
     } else {
-      uint64_t DG = x2::mul(DX, GX);
-      DG = x2::fma(DY, GY, DG);
-      DG = x2::fma(DZ, GZ, DG);
       const uint64_t T5 = x2::mul(T3, T2);
-      const uint64_t W = x2::mul(x2::mul(x2::fma(q5.y, T2, CM3), T5), DG);
+      const uint64_t F = x2::fma(C1, T5, T3);
+      uint64_t DG = x2::fma(NGX, X, TG);
+      DG = x2::fma(NGY, Y, DG);
+      DG = x2::fma(NGZ, Z, DG);
+      const uint64_t W = x2::mul(x2::mul(x2::fma(C1, T2, C06), T5), DG);
       FA[0] = x2::fma(F, AX, FA[0]);
       FA[1] = x2::fma(F, AY, FA[1]);
       FA[2] = x2::fma(F, AZ, FA[2]);
       WA[0] = x2::fma(W, AX, WA[0]);
       WA[1] = x2::fma(W, AY, WA[1]);
       WA[2] = x2::fma(W, AZ, WA[2]);
-      FC[0] = x2::fma(W, CX, FC[0]);
-      FC[1] = x2::fma(W, CY, FC[1]);
-      FC[2] = x2::fma(W, CZ, FC[2]);
+      WC[0] = x2::fma(W, CX, WC[0]);
+      WC[1] = x2::fma(W, CY, WC[1]);
+      WC[2] = x2::fma(W, CZ, WC[2]);
     }
   }
-  // velocity: sum f (d x a) = t x FA - FC; stretching: sum (f G + w d) x a =
-  // G x FA + t x WA - FC
-  const uint64_t U[3] = {x2::sub(x2::mul(TY, FA[2]), x2::fma(TZ, FA[1], FC[0])),
-                         x2::sub(x2::mul(TZ, FA[0]), x2::fma(TX, FA[2], FC[1])),
-                         x2::sub(x2::mul(TX, FA[1]), x2::fma(TY, FA[0], FC[2]))};
   if (MODE == FVX_PAIR_VELOCITY) {
-    acc[0] = U[0];
-    acc[1] = U[1];
-    acc[2] = U[2];
+    // sum f (d x a) = t x FA - sum f c, t = -M2 / 2 (exact)
+    const uint64_t MH = x2::pack(-0.5f, -0.5f);
+    const uint64_t TX = x2::mul(M2X, MH), TY = x2::mul(M2Y, MH), TZ = x2::mul(M2Z, MH);
+    acc[0] = x2::sub(x2::mul(TY, FA[2]), x2::fma(TZ, FA[1], WC[0]));
+    acc[1] = x2::sub(x2::mul(TZ, FA[0]), x2::fma(TX, FA[2], WC[1]));
+    acc[2] = x2::sub(x2::mul(TX, FA[1]), x2::fma(TY, FA[0], WC[2]));
   } else {
+    // G x FA + t x (sum w a) - sum w c = -(NG x FA) + 2.5 (M2 x WA) + 5 WC
+    const uint64_t MONE = x2::pack(-1.f, -1.f), P25 = x2::pack(2.5f, 2.5f),
+                   P5 = x2::pack(5.f, 5.f);
+    const uint64_t GX = x2::mul(NGX, MONE), GY = x2::mul(NGY, MONE), GZ = x2::mul(NGZ, MONE);
+    const uint64_t HX = x2::mul(M2X, P25), HY = x2::mul(M2Y, P25), HZ = x2::mul(M2Z, P25);
     acc[0] = x2::add(x2::sub(x2::mul(GY, FA[2]), x2::mul(GZ, FA[1])),
-                     x2::sub(x2::sub(x2::mul(TY, WA[2]), x2::mul(TZ, WA[1])), FC[0]));
+                     x2::fma(P5, WC[0], x2::sub(x2::mul(HY, WA[2]), x2::mul(HZ, WA[1]))));
     acc[1] = x2::add(x2::sub(x2::mul(GZ, FA[0]), x2::mul(GX, FA[2])),
-                     x2::sub(x2::sub(x2::mul(TZ, WA[0]), x2::mul(TX, WA[2])), FC[1]));
+                     x2::fma(P5, WC[1], x2::sub(x2::mul(HZ, WA[0]), x2::mul(HX, WA[2]))));
     acc[2] = x2::add(x2::sub(x2::mul(GX, FA[1]), x2::mul(GY, FA[0])),
-                     x2::sub(x2::sub(x2::mul(TX, WA[1]), x2::mul(TY, WA[0])), FC[2]));
+                     x2::fma(P5, WC[2], x2::sub(x2::mul(HX, WA[1]), x2::mul(HY, WA[0]))));
   }
 }
 
@@ -1368,7 +1387,9 @@ struct EvalSmem {
   // paired path: Winckelmans velocity / stretching with two targets per thread
   static constexpr bool PACKED = TPT == 2 && KERNEL == FVX_KERNEL_WINCKELMANS &&
                                  (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_STRETCH);
-  static constexpr int kNearBytes = PACKED ? kNearRows * static_cast<int>(sizeof(NearX2))
+  // paired: the tile's planes, then the lanes' running near-field sums
+  // (hi, lo of two targets x three components, 12 x 32 floats)
+  static constexpr int kNearBytes = PACKED ? kPlanes * kNearTile * 16 + 12 * kEvalThreads * 4
                                            : kNearTile * 2 * static_cast<int>(sizeof(float4));
   static constexpr int kFarBytes = kFarTile * kRecFloats * 4;
   static constexpr int bytes = kNearBytes > kFarBytes ? kNearBytes : kFarBytes;
@@ -1386,55 +1407,64 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
   constexpr bool PACKED = EvalSmem<MODE, KERNEL, TPT>::PACKED;
   float4* s_p = reinterpret_cast<float4*>(s_raw);
   float4* s_a = s_p + kNearTile;
-  NearX2* s_x2 = reinterpret_cast<NearX2*>(s_raw);
+  ulonglong2* s_q = reinterpret_cast<ulonglong2*>(s_raw);
   float* s_rec = reinterpret_cast<float*>(s_raw);
 
   const int tstart = A.leaf_start[t], tcount = A.leaf_count[t];
   const float3 cT = cell_center_rel(A.leaf_key[t], A.h);
   const int nno = A.near_off[t], nnc = A.near_cnt[t];
   const int fno = A.far_off[t], fnc = A.far_cnt[t];
-  // Source phases (paired path): the leaf's targets go in chunks of 32, one
-  // target per lane, and each target of a chunk of c gets G = 2, 4 or 8
-  // workers (c > 16, > 8, <= 8) -- the two halves of the paired registers
-  // times G/2 groups of lanes -- each summing every G-th source, so that the
-  // 64 paired slots stay busy for chunks of 32, 16 or 8 targets.  (Two
-  // targets per lane over 64 slots would leave a leaf of 33..63 targets
-  // 48..2 % idle; a chunk of 32 plus a smaller one with more phases costs
-  // fewer rows.)  The other paths take TPT targets per lane, G = 1.
+  // Paired path: the leaf's targets go in chunks of at most 32.  A chunk of c
+  // targets puts two in each of m = ceil(c/2) lanes (the halves of the paired
+  // registers) and splits the sources over g = floor(32/m) groups of m lanes
+  // (group j sums rows j, j + g, ...); the groups' partial sums are added into
+  // group 0 at the end of the near field.  Lanes past the g groups mirror
+  // group 0 and are not counted.  The other paths take TPT targets per lane.
   const int chunk_step = PACKED ? kEvalThreads : kEvalThreads * TPT;
+  const int lane = threadIdx.x;
 
   for (int chunk = 0; chunk < tcount; chunk += chunk_step) {
-    int G = 1;
+    const int cend = min(tcount, chunk + chunk_step);
+    int m = kEvalThreads, g = 1, grp = 0, tl = lane;
+    bool spare = false;
     if constexpr (PACKED) {
-      const int cnt = min(kEvalThreads, tcount - chunk);
-      G = cnt > 16 ? 2 : (cnt > 8 ? 4 : 8);
+      m = (cend - chunk + 1) >> 1;
+      g = kEvalThreads / m;
+      grp = lane / m;
+      tl = lane - grp * m;
+      spare = grp >= g;
+      if (spare) grp = 0;
     }
-    const int gl = G == 1 ? kEvalThreads : 2 * kEvalThreads / G;  // lanes per group
-    const int grp = threadIdx.x / gl, tl = threadIdx.x - grp * gl;
     float ox[TPT], oy[TPT], oz[TPT], gx[TPT], gy[TPT], gz[TPT];
     float hi[TPT][NC], lo[TPT][NC];
     bool act[TPT];
     int kk[TPT];
+    // the lane's targets (reloaded after the paired near field rather than
+    // held through it)
+    auto load_targets = [&]() {
+#pragma unroll
+      for (int j = 0; j < TPT; ++j) {
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f), gv = p;
+        if (kk[j] < cend) {
+          p = A.sp[tstart + kk[j]];
+          if (NEED_TG) gv = A.sg[tstart + kk[j]];
+        }
+        ox[j] = p.x;
+        oy[j] = p.y;
+        oz[j] = p.z;
+        gx[j] = gv.x;
+        gy[j] = gv.y;
+        gz[j] = gv.z;
+      }
+    };
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      // G > 1: both slots hold the lane's one target; only group 0 writes it
-      const int k = G == 1 ? chunk + threadIdx.x + j * kEvalThreads : chunk + tl;
-      kk[j] = k;
-      act[j] = k < tcount && (G == 1 || (j == 0 && grp == 0));
-      float4 p = make_float4(0.f, 0.f, 0.f, 0.f), g = p;
-      if (k < tcount) {
-        p = A.sp[tstart + k];
-        if (NEED_TG) g = A.sg[tstart + k];
-      }
-      ox[j] = p.x;
-      oy[j] = p.y;
-      oz[j] = p.z;
-      gx[j] = g.x;
-      gy[j] = g.y;
-      gz[j] = g.z;
+      kk[j] = chunk + tl + j * m;
+      act[j] = kk[j] < cend && grp == 0 && !spare;
 #pragma unroll
       for (int c = 0; c < NC; ++c) hi[j][c] = lo[j][c] = 0.f;
     }
+    load_targets();
     // near field: direct pairs with every near leaf
     if constexpr (PACKED) {
       // Tiles of up to kNearTile sources filled from up to 32 near leaves at
@@ -1446,12 +1476,30 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
       // leaf), so one tile mixes leaves and its barriers, loads and fold are
       // paid per 128 sources instead of per near leaf.
       const unsigned full = 0xffffffffu;
-      const int lane = threadIdx.x;
-      const uint64_t TX = x2::pack(ox[0], ox[TPT - 1]), TY = x2::pack(oy[0], oy[TPT - 1]),
-                     TZ = x2::pack(oz[0], oz[TPT - 1]);
-      const uint64_t GX = x2::pack(gx[0], gx[TPT - 1]), GY = x2::pack(gy[0], gy[TPT - 1]),
-                     GZ = x2::pack(gz[0], gz[TPT - 1]);
-      const int ng = G == 1 ? 1 : G / 2;
+      const uint64_t TX = x2::pack(ox[0], ox[1]), TY = x2::pack(oy[0], oy[1]),
+                     TZ = x2::pack(oz[0], oz[1]);
+      const uint64_t GX = x2::pack(gx[0], gx[1]), GY = x2::pack(gy[0], gy[1]),
+                     GZ = x2::pack(gz[0], gz[1]);
+      const float m5 = -5.f, m2 = -2.f;
+      const uint64_t G5X = x2::pack(m5 * gx[0], m5 * gx[1]),
+                     G5Y = x2::pack(m5 * gy[0], m5 * gy[1]),
+                     G5Z = x2::pack(m5 * gz[0], m5 * gz[1]);
+      // per-target constants of the factored form: -2 t, |t|^2, -G, t . G
+      const uint64_t M2X = x2::pack(m2 * ox[0], m2 * ox[1]),
+                     M2Y = x2::pack(m2 * oy[0], m2 * oy[1]),
+                     M2Z = x2::pack(m2 * oz[0], m2 * oz[1]);
+      const uint64_t TT = x2::pack(fmaf(ox[0], ox[0], fmaf(oy[0], oy[0], oz[0] * oz[0])),
+                                   fmaf(ox[1], ox[1], fmaf(oy[1], oy[1], oz[1] * oz[1])));
+      const uint64_t NGX = x2::pack(-gx[0], -gx[1]), NGY = x2::pack(-gy[0], -gy[1]),
+                     NGZ = x2::pack(-gz[0], -gz[1]);
+      const uint64_t TG = x2::pack(fmaf(ox[0], gx[0], fmaf(oy[0], gy[0], oz[0] * gz[0])),
+                                   fmaf(ox[1], gx[1], fmaf(oy[1], gy[1], oz[1] * gz[1])));
+      float4* s_r = reinterpret_cast<float4*>(s_raw);
+      // the running sums stay in shared memory through the near field (each
+      // lane its own column), not in registers
+      float* s_sum = reinterpret_cast<float*>(s_raw + kPlanes * kNearTile * 16) + lane;
+#pragma unroll
+      for (int e = 0; e < 12; ++e) s_sum[e * kEvalThreads] = 0.f;
       for (int q0 = 0; q0 < nnc; q0 += kEvalThreads) {
         int mss = 0, msn = 0;
         float mdx = 0.f, mdy = 0.f, mdz = 0.f;
@@ -1472,109 +1520,100 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
         }
         const int total = __shfl_sync(full, incl, kEvalThreads - 1);
         const int excl = incl - msn;
-        // a tile is kNearRows staged rows: as many sources (G = 1), or twice
-        // as many (G > 1, two per row)
-        const int tile_src = G == 1 ? kNearRows : 2 * kNearRows;
+        // a tile holds a multiple of g sources (at most kNearTile), so that
+        // padding its last one to a multiple of g stays within the planes
+        const int tile_src = kNearTile / g * g;
         for (int b0 = 0; b0 < total; b0 += tile_src) {
           const int nt = min(tile_src, total - b0);
-          // rows: nt sources (G = 1), or ceil(nt/2) source pairs padded with
-          // zero-strength sources to a multiple of the G/2 lane groups
-          const int rows = G == 1 ? nt : ((nt + 1) / 2 + ng - 1) / ng * ng;
+          // rows: nt sources padded with zero-strength ones to a multiple of g
+          const int rows = (nt + g - 1) / g * g;
           __syncthreads();
           for (int r0 = 0; r0 < rows; r0 += kEvalThreads) {
             const int k = r0 + lane;
-            float4 p[2], a[2];
             // each staged source's near leaf, from the leaves' start offsets in
-            // this window of 32 (G = 1) or 64 sources: one bit per start
-            // (near leaves are never empty, so starts are distinct), and a
-            // source's leaf is the number of starts up to it, minus one
-            const int g0 = b0 + (G == 1 ? r0 : 2 * r0);
-            const int pl = excl - g0;
-            const unsigned blo = __reduce_or_sync(full, (pl >= 0 && pl < 32) ? 1u << pl : 0u);
-            const unsigned bhi =
-                __reduce_or_sync(full, (pl >= 32 && pl < 64) ? 1u << (pl - 32) : 0u);
+            // this window of 32 sources: one bit per start (near leaves are
+            // never empty, so starts are distinct), and a source's leaf is the
+            // number of starts up to it, minus one
+            const int pl = excl - (b0 + r0);
+            const unsigned bits = __reduce_or_sync(full, (pl >= 0 && pl < 32) ? 1u << pl : 0u);
             const int before = __popc(__ballot_sync(full, pl < 0));
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const int sk = G == 1 ? k : 2 * k + h;  // source of this half
-              const int g = b0 + (sk < nt ? sk : 0);
-              const int o = G == 1 ? lane : 2 * lane + h;
-              const unsigned m_lo = o >= 31 ? 0xffffffffu : ((2u << o) - 1u);
-              const unsigned m_hi = o >= 63 ? 0xffffffffu : (o >= 32 ? ((2u << (o - 32)) - 1u) : 0u);
-              const int li = before + __popc(blo & m_lo) + __popc(bhi & m_hi) - 1;
-              const int lss = __shfl_sync(full, mss, li), lex = __shfl_sync(full, excl, li);
-              const float ldx = __shfl_sync(full, mdx, li), ldy = __shfl_sync(full, mdy, li),
-                          ldz = __shfl_sync(full, mdz, li);
-              p[h] = make_float4(0.f, 0.f, 0.f, 1.f);
-              a[h] = make_float4(0.f, 0.f, 0.f, 0.f);
-              if (k < rows && sk < nt) {
-                const float4 pv = A.sp[lss + g - lex];
-                p[h] = make_float4(pv.x - ldx, pv.y - ldy, pv.z - ldz, pv.w);
-                a[h] = A.sa[lss + g - lex];
-              }
+            const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+            const int li = before + __popc(bits & upto) - 1;
+            const int lss = __shfl_sync(full, mss, li), lex = __shfl_sync(full, excl, li);
+            const float ldx = __shfl_sync(full, mdx, li), ldy = __shfl_sync(full, mdy, li),
+                        ldz = __shfl_sync(full, mdz, li);
+            float4 p = make_float4(0.f, 0.f, 0.f, 1.f), av = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k < nt) {
+              const int src = lss + b0 + k - lex;
+              const float4 pv = A.sp[src];
+              p = make_float4(pv.x - ldx, pv.y - ldy, pv.z - ldz, pv.w);
+              av = A.sa[src];
             }
             if (k < rows) {
-              NearX2 e;
-              e.q[0] = make_ulonglong2(x2::pack(-p[0].x, -p[1].x), x2::pack(-p[0].y, -p[1].y));
-              e.q[1] = make_ulonglong2(x2::pack(-p[0].z, -p[1].z), x2::pack(p[0].w, p[1].w));
-              e.q[2] = make_ulonglong2(x2::pack(1.5f * p[0].w, 1.5f * p[1].w),
-                                       x2::pack(a[0].x, a[1].x));
-              e.q[3] = make_ulonglong2(x2::pack(a[0].y, a[1].y), x2::pack(a[0].z, a[1].z));
-              // factored form: c = x_s x a, x_s relative to the target
-              // leaf's centre; direct form: the negated strengths
-              float cx[2], cy[2], cz[2];
-#pragma unroll
-              for (int h = 0; h < 2; ++h) {
-                if constexpr (FACT) {
-                  cx[h] = p[h].y * a[h].z - p[h].z * a[h].y;
-                  cy[h] = p[h].z * a[h].x - p[h].x * a[h].z;
-                  cz[h] = p[h].x * a[h].y - p[h].y * a[h].x;
-                } else {
-                  cx[h] = -a[h].x;
-                  cy[h] = -a[h].y;
-                  cz[h] = -a[h].z;
-                }
+              float4* row = s_r + k;
+              if constexpr (FACT) {
+                const float S2 = fmaf(p.x, p.x, fmaf(p.y, p.y, fmaf(p.z, p.z, p.w)));
+                row[0] = make_float4(p.x, p.y, p.z, S2);
+                row[2 * kNearTile] =
+                    make_float4(p.y * av.z - p.z * av.y, p.z * av.x - p.x * av.z,
+                                p.x * av.y - p.y * av.x, 0.f);
+              } else {
+                row[0] = make_float4(-p.x, -p.y, -p.z, p.w);
               }
-              e.q[4] = make_ulonglong2(x2::pack(cx[0], cx[1]), x2::pack(cy[0], cy[1]));
-              e.q[5] = make_ulonglong2(x2::pack(cz[0], cz[1]),
-                                       x2::pack(-7.5f * p[0].w, -7.5f * p[1].w));
-              s_x2[k] = e;
+              row[kNearTile] = make_float4(1.5f * p.w, av.x, av.y, av.z);
             }
           }
           __syncthreads();
-          uint64_t acc2[3] = {0ull, 0ull, 0ull};
-          const NearX2* tile = s_x2 + (G == 1 ? 0 : grp);
-          if constexpr (FACT) {
-            if (ng == 1)
-              near_tile_x2_factored<MODE, 1>(tile, rows, TX, TY, TZ, GX, GY, GZ, acc2);
-            else if (ng == 2)
-              near_tile_x2_factored<MODE, 2>(tile, rows / 2, TX, TY, TZ, GX, GY, GZ, acc2);
-            else
-              near_tile_x2_factored<MODE, 4>(tile, rows / 4, TX, TY, TZ, GX, GY, GZ, acc2);
-          } else {
-            if (ng == 1)
-              near_tile_x2_direct<MODE, 1>(tile, rows, TX, TY, TZ, GX, GY, GZ, acc2);
-            else if (ng == 2)
-              near_tile_x2_direct<MODE, 2>(tile, rows / 2, TX, TY, TZ, GX, GY, GZ, acc2);
-            else
-              near_tile_x2_direct<MODE, 4>(tile, rows / 4, TX, TY, TZ, GX, GY, GZ, acc2);
-          }
+          uint64_t acc2[3];
+          const float4* row = s_r + grp;
+          if constexpr (FACT)
+            near_tile_factored<MODE>(row, rows / g, g, M2X, M2Y, M2Z, TT, NGX, NGY, NGZ, TG, acc2);
+          else
+            near_tile_direct<MODE>(row, rows / g, g, TX, TY, TZ, GX, GY, GZ, G5X, G5Y, G5Z, acc2);
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            float a0, a1;
-            x2::unpack(acc2[c], a0, a1);
-            if (G == 1) {
-              fold(hi[0][c], lo[0][c], a0);
-              fold(hi[TPT - 1][c], lo[TPT - 1][c], a1);
-            } else {
-              // the target's G partial sums: the two halves, then the groups
-              float v = a0 + a1;
-              if (G == 8) v += __shfl_xor_sync(full, v, 8);
-              if (G >= 4) v += __shfl_xor_sync(full, v, 16);
-              fold(hi[0][c], lo[0][c], v);
+            float a[2];
+            x2::unpack(acc2[c], a[0], a[1]);
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+              float* e = s_sum + (4 * c + 2 * j) * kEvalThreads;
+              float h = e[0], l = e[kEvalThreads];
+              fold(h, l, a[j]);
+              e[0] = h;
+              e[kEvalThreads] = l;
             }
           }
         }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          hi[j][c] = s_sum[(4 * c + 2 * j) * kEvalThreads];
+          lo[j][c] = s_sum[(4 * c + 2 * j + 1) * kEvalThreads];
+        }
+      load_targets();
+      // the groups' partial sums into group 0 (lanes tl + j m, j < g), read
+      // from copies: every lane updates its own sums while others read them
+      float ph[2][3], pq[2][3];
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          ph[s2][c] = hi[s2][c];
+          pq[s2][c] = lo[s2][c];
+        }
+      for (int j = 1; j < g; ++j) {
+        const int src = tl + j * m;
+#pragma unroll
+        for (int s2 = 0; s2 < 2; ++s2)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const float vh = __shfl_sync(full, ph[s2][c], src);
+            const float vl = __shfl_sync(full, pq[s2][c], src);
+            fold(hi[s2][c], lo[s2][c], vh);
+            lo[s2][c] += vl;
+          }
       }
     }
     for (int q = 0; q < (PACKED ? 0 : nnc); ++q) {
@@ -1700,8 +1739,8 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
 // until none are left: the SMs stay at their occupancy limit to the end, and
 // no CTA is launched per leaf.  The leaves come in decreasing order of their
 // near-field work, so the last ones taken are the shortest.
-template <int MODE, int KERNEL, int TPT, bool FACT = false>
-__global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
+template <int MODE, int KERNEL, int TPT, bool FACT>
+__device__ __forceinline__ void eval_leaves(const EvalArgs& A) {
   __shared__ __align__(16) unsigned char s_raw[EvalSmem<MODE, KERNEL, TPT>::bytes];
   for (;;) {
     int c = 0;
@@ -1711,6 +1750,20 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
     eval_leaf<MODE, KERNEL, TPT, FACT>(A, A.leaf_order[c], s_raw);
     __syncthreads();  // the next leaf restages the shared buffer
   }
+}
+
+template <int MODE, int KERNEL, int TPT>
+__global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
+  eval_leaves<MODE, KERNEL, TPT, false>(A);
+}
+
+// The factored stretching loop (paired Winckelmans), held to 24 resident
+// warps per SM, i.e. at most 80 registers: more warps in flight than its
+// unbounded register count allows.
+template <int MODE, int KERNEL, int TPT>
+__global__ void __launch_bounds__(kEvalThreads, 24)
+    eval_kernel_factored(EvalArgs A) {
+  eval_leaves<MODE, KERNEL, TPT, true>(A);
 }
 
 // ---- the FP64 judge of the local-expansion path ------------------------------------
@@ -2208,14 +2261,16 @@ void launch_eval_tpt(int mode, int nleaf, const tree::EvalArgs& A, bool factored
   constexpr bool F = KERNEL == FVX_KERNEL_WINCKELMANS && TPT == 2;  // the paired kernels
   switch (mode) {
     case FVX_PAIR_VELOCITY: {
-      auto k = F && factored ? eval_kernel<FVX_PAIR_VELOCITY, KERNEL, TPT, F>
-                             : eval_kernel<FVX_PAIR_VELOCITY, KERNEL, TPT>;
+      auto k = eval_kernel<FVX_PAIR_VELOCITY, KERNEL, TPT>;
+      if constexpr (F)
+        if (factored) k = eval_kernel_factored<FVX_PAIR_VELOCITY, KERNEL, TPT>;
       k<<<resident_grid(k, nleaf), kEvalThreads, 0, s>>>(A);
       break;
     }
     case FVX_PAIR_STRETCH: {
-      auto k = F && factored ? eval_kernel<FVX_PAIR_STRETCH, KERNEL, TPT, F>
-                             : eval_kernel<FVX_PAIR_STRETCH, KERNEL, TPT>;
+      auto k = eval_kernel<FVX_PAIR_STRETCH, KERNEL, TPT>;
+      if constexpr (F)
+        if (factored) k = eval_kernel_factored<FVX_PAIR_STRETCH, KERNEL, TPT>;
       k<<<resident_grid(k, nleaf), kEvalThreads, 0, s>>>(A);
       break;
     }
@@ -2925,8 +2980,8 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   A.leaf_next = P<int>(T->eval_next);
   A.leaf_order = P<int>(T->leaf_order);
   FVX_CUDA_TRY(cudaEventRecord(T->ev0, s));
-  // the factored near loop where leaves are at most 4 smallest cores wide (the
-  // cores of the last full build; see near_tile_x2_factored)
+  // the factored stretching loop where leaves are at most 4 smallest cores
+  // wide (the cores of the last full build; see near_tile_x2_factored)
   const bool factored = h <= 4.0 * T->sigma_min;
   if (kernel == FVX_KERNEL_WINCKELMANS)
     launch_eval<FVX_KERNEL_WINCKELMANS>(mode, nleaf, n, A, factored, s);
