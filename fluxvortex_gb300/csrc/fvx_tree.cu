@@ -2005,16 +2005,19 @@ __global__ void judge_repair_kernel(JudgeSampleBufs B, const float* __restrict__
 
 // FP64 direct sums of the queued (target, cell) pairs at every particle of
 // the target (a leaf, or a parent of leaves), added to the outputs.
-// Persistent CTAs stride over (pair, slice) items: each pair's cell is cut
-// into S slices of at least kFallbackMinSlice particles (the surplus items of
-// a small cell are skipped at once), S = 64 for a short queue (the judge's
-// repairs: a few pairs, some of them parents against cells of thousands of
-// particles) and 8 for a long one (whole classes).  Each warp takes whole
-// targets: its lanes stride over the slice, reduce by shuffles and add one
-// atomic per output component, with no block-wide barrier per target.
+// Persistent CTAs stride over (pair, slice, target phase) items: each pair's
+// cell is cut into S slices of at least a minimum size (the surplus items of
+// a small cell are skipped at once), and its targets into TP phases of eight
+// (one per warp).  A short queue (the judge's repairs: a few pairs, some of
+// them parents of hundreds of particles against cells of thousands) takes
+// S = 64 slices of at least 32 particles and TP = 8 phases, so that a single
+// pair spreads over hundreds of CTAs: FP64 runs at 1/64 of the FP32 rate, and
+// one CTA per slice left a parent pair at ~0.2 ms.  A long queue (whole
+// classes) takes S = 8 slices of at least 128 and one phase.  Each warp takes
+// whole targets: its lanes stride over the slice, reduce by shuffles and add
+// one atomic per output component, with no block-wide barrier per target.
 constexpr int kFallbackThreads = 256;
-constexpr int kFallbackMinSlice = 128;
-constexpr int kFallbackSlicesShort = 64, kFallbackSlicesLong = 8, kFallbackShortQueue = 2048;
+constexpr int kFallbackShortQueue = 2048;
 struct FallbackTargets {
   const int* start[2];
   const int* count[2];
@@ -2034,22 +2037,25 @@ __global__ void __launch_bounds__(kFallbackThreads) fallback_kernel(
   constexpr bool NEED_TG = ModeInfo<MODE>::need_tg;
   constexpr double kC = -0.07957747154594767;
   const int nq = min(*n_fallback, fb_cap);
-  const int S = nq < kFallbackShortQueue ? kFallbackSlicesShort : kFallbackSlicesLong;
-  const int64_t items = static_cast<int64_t>(nq) * S;
+  const bool short_q = nq < kFallbackShortQueue;
+  const int S = short_q ? 64 : 8, TP = short_q ? 8 : 1, min_slice = short_q ? 32 : 128;
+  const int64_t items = static_cast<int64_t>(nq) * S * TP;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int kWarps = kFallbackThreads / 32;
   for (int64_t w = blockIdx.x; w < items; w += gridDim.x) {
-    const int2 pr = fallback[w / S];
-    const int sl = static_cast<int>(w % S);
+    const int2 pr = fallback[w / (S * TP)];
+    const int rem = static_cast<int>(w % (S * TP));
+    const int sl = rem / TP, tp = rem - sl * TP;
     const int li = (pr.x >> 30) & 1, tgt = pr.x & ((1 << 30) - 1);
     const int t0 = (li ? tg.start[1] : tg.start[0])[tgt];
     const int nt = (li ? tg.count[1] : tg.count[0])[tgt];
     const int c0 = cell_start[pr.y], cn = cell_count[pr.y];
-    const int per = max(kFallbackMinSlice, (cn + S - 1) / S);
+    const int per = max(min_slice, (cn + S - 1) / S);
     const int64_t s0_64 = c0 + static_cast<int64_t>(sl) * per;
     if (s0_64 >= c0 + cn) continue;
     const int s0 = static_cast<int>(s0_64);
     const int ns = min(per, c0 + cn - s0);
-    for (int ti = wid; ti < nt; ti += kFallbackThreads / 32) {
+    for (int ti = tp * kWarps + wid; ti < nt; ti += kWarps * TP) {
       const int i = perm[t0 + ti];
       const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
       double gx = 0.0, gy = 0.0, gz = 0.0;
