@@ -59,8 +59,7 @@ def test_fallback_of_every_pair_is_the_fp64_direct_sum(cuda, mode):
     e_fb = float((out - ref).abs().max() / ref.abs().max())
     e_tree = float((out_tree - ref).abs().max() / ref.abs().max())
     # only the FP32 near field remains: within the FP32-compensated tolerance,
-    # and well below the treecode's own error (the near loop forms d x a as
-    # t x a - x_s x a, whose rounding is a few times FP32's for close pairs)
+    # and well below the treecode's own error
     assert e_fb < 2e-5 and e_fb < 0.5 * e_tree, (e_fb, e_tree)
     assert _capi.status_read_and_clear() == 0
 

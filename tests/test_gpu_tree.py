@@ -158,3 +158,54 @@ def test_one_pass_lists_and_their_overflow_fallback(cuda):
     for o, st in outs[:2]:
         assert np.abs(o - ref).max() <= 1e-5 * np.abs(ref).max()
         assert np.array_equal(st[:5], outs[2][1][:5])
+
+
+def _factored_case(n=3000, leaf=16, seed=5):
+    """A slab whose cores are 1.3 x the particle spacing (the benchmarked
+    step's), so that the leaves are at most four cores wide and the sweep
+    takes the factored near loop (d x a = t x a - x_s x a)."""
+    from fluxvortex_gb300.tree_params import grid_params
+    from fluxvortex_gb300.workloads import resolved_core
+    pos, gam, sig, _ = slab_wake(n, seed=seed, sigma=resolved_core(n))
+    h = grid_params(pos.min(0), pos.max(0), n, leaf)["h"]
+    assert h <= 4.0 * sig.min(), (h, sig.min())
+    return pos, gam, sig
+
+
+def test_factored_near_loop_matches_oracle_algorithm(cuda):
+    """The factored velocity and stretching loops against the oracle's FP64
+    restatement of the same treecode: the difference is the FP32 rounding
+    (3.9e-7 measured for both; the bar is ten times that)."""
+    pos, gam, sig = _factored_case()
+    tr = OT.build(pos, theta=0.5, leaf_target=16)
+    OT.moments(tr, pos, gam)
+    u, J = OT.evaluate(tr, pos, gam, sig, kernel="winckelmans")
+    S = np.einsum("tij,tj->ti", J, gam)
+    gu, _, _ = _tree(_capi.PAIR_VELOCITY, "winckelmans", pos, gam, sig, cuda, 16)
+    gs, _, _ = _tree(_capi.PAIR_STRETCH, "winckelmans", pos, gam, sig, cuda, 16, tg=gam)
+    eu, es = rel_err(gu, u), rel_err(gs, S)
+    print(f"factored loop vs oracle: velocity {eu:.2e}, stretching {es:.2e}")
+    assert eu < 4e-6 and es < 4e-6
+
+
+@pytest.mark.parametrize("mode", ["velocity", "stretch"])
+def test_factored_near_field_with_fp64_far_field(cuda, mode):
+    """Every far pair sent to the FP64 fallback (judge tolerance ~ 0), so only
+    the factored FP32 near field differs from the FP64 direct sum (5.7e-7 /
+    3.5e-7 measured for velocity / stretching)."""
+    pos, gam, sig = _factored_case(2500, 16, 51)
+    n = pos.shape[0]
+    m = _capi.PAIR_VELOCITY if mode == "velocity" else _capi.PAIR_STRETCH
+    P, G, S = _dev(pos, cuda), _dev(gam, cuda), _dev(sig, cuda)
+    tg = G if mode == "stretch" else None
+    ref, _ = K.particle_pairs(m, P, tg, P, G, S, "winckelmans", "f64")
+    ts = TreeSweeper(theta=0.5, leaf_target=16)
+    ts.set_far_field("m2l")
+    ts.set_validation(samples=65536, tol=1e-30)
+    out = torch.empty((n, 3), dtype=torch.float64, device=cuda)
+    stats = ts.sweep(m, "winckelmans", P, G, S, n, out, tgt_gamma=tg, check=True)
+    assert ts.last_validation()["fallback"] == int(stats[4]) > 0
+    e = rel_err(out.cpu().numpy(), ref.cpu().numpy())
+    print(f"factored near field, {mode}: {e:.2e} of the FP64 direct sum")
+    assert e < 4e-6
+    assert _capi.status_read_and_clear() == 0
