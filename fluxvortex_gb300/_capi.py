@@ -78,6 +78,9 @@ SIGNATURES = {
     "fvx_uvlm_aic": (I32, [I32, I32, P, P, P, P, P, P, D, D, P, P]),
     "fvx_uvlm_rhs": (I32, [I32, P, P, P, P, P, P, D, P, P]),
     "fvx_lu_solve_batched": (I32, [I32, I32, P, P, P]),
+    "fvx_lu_workspace_bytes": (I64, [I32]),
+    "fvx_lu_factor_batched": (I32, [I32, I32, P, P, P]),
+    "fvx_lu_solve_factored_batched": (I32, [I32, I32, P, P, P]),
     "fvx_uvlm_loads": (I32, [I32, P, P, P, P, P, P, P, P, P, P, P, D, D, D, D, P, P, P, P]),
     "fvx_uvlm_wake_rings": (I32, [I32, P, P, P, P, D, P, P, P, P, P, P, P, P]),
     "fvx_uvlm_shed": (I32, [I32, I32, P, P, P, P, P, P, P, D, P, P, P, P, P, P, P]),

@@ -426,16 +426,49 @@ constexpr int kLuCtas = 8;
 constexpr int kLuClusterThreads = 256;
 constexpr int kLuClusterMaxP = 192;  // packed U, P (P + 1) / 2 doubles, in CTA 0
 
+// doubles of one system's factorisation workspace: multipliers P x P, pivots
+// P, packed U P (P + 1) / 2
+__host__ __device__ constexpr int64_t lu_workspace_doubles(int P) {
+  return static_cast<int64_t>(P) * P + P + static_cast<int64_t>(P) * (P + 1) / 2;
+}
+
+// Back substitution with the packed upper triangle (column j's rows 0..j at
+// j (j + 1) / 2), x in place; every thread of the CTA takes part.
+__device__ __forceinline__ void back_substitute(int P, const double* s_u, double* s_x, int tid,
+                                                int NT) {
+  for (int k = P - 1; k >= 0; --k) {
+    const int base = k * (k + 1) / 2;
+    const double xk = s_x[k] / s_u[base + k];
+    for (int r = tid; r < k; r += NT) s_x[r] -= s_u[base + r] * xk;
+    __syncthreads();
+    if (tid == 0) s_x[k] = xk;
+    __syncthreads();
+  }
+}
+
 // Dynamic shared memory per CTA: panel[ceil(P/kLuCtas)][P] (column-major),
 // s_l[2][P], s_x[P], packed U[P (P + 1) / 2] (used in CTA 0).
+// FACTOR: the factorisation alone, no right-hand side: step k's multipliers
+// (as formed at step k), its pivot and the packed upper triangle go to the
+// workspace W (lu_workspace), from which lu_solve_factored_kernel replays the
+// same elimination on a right-hand side later (same operations, same order:
+// the same solution bit for bit), so the factorisation can run while the
+// right-hand side is still being formed.
+template <bool FACTOR>
 __global__ void __cluster_dims__(kLuCtas, 1, 1) __launch_bounds__(kLuClusterThreads)
-    lu_solve_cluster_kernel(int P, double* __restrict__ A, double* __restrict__ b) {
+    lu_cluster_kernel(int P, double* __restrict__ A, double* __restrict__ b,
+                      double* __restrict__ W) {
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ double lc_smem[];
   const int rank = static_cast<int>(cl.block_rank());
   const int sys = blockIdx.x / kLuCtas;
   double* a = A + static_cast<int64_t>(sys) * P * P;
-  double* xg = b + static_cast<int64_t>(sys) * P;
+  double* xg = FACTOR ? nullptr : b + static_cast<int64_t>(sys) * P;
+  // workspace of this system: multipliers L[k][r] (row k: step k's, r > k),
+  // pivots (as doubles), packed U
+  double* wl = FACTOR ? W + static_cast<int64_t>(sys) * lu_workspace_doubles(P) : nullptr;
+  double* wp = FACTOR ? wl + static_cast<int64_t>(P) * P : nullptr;
+  double* wu = FACTOR ? wp + P : nullptr;
   const int ncmax = (P + kLuCtas - 1) / kLuCtas;
   const int ncol = rank < P ? (P - rank + kLuCtas - 1) / kLuCtas : 0;
   double* panel = lc_smem;
@@ -451,7 +484,8 @@ __global__ void __cluster_dims__(kLuCtas, 1, 1) __launch_bounds__(kLuClusterThre
     const int q = e / P, r = e - q * P;
     panel[q * P + r] = a[static_cast<int64_t>(r) * P + rank + kLuCtas * q];
   }
-  for (int r = tid; r < P; r += NT) s_x[r] = xg[r];
+  if (!FACTOR)
+    for (int r = tid; r < P; r += NT) s_x[r] = xg[r];
   __syncthreads();
   for (int k = 0; k < P; ++k) {
     const int o = k % kLuCtas, par = k & 1;
@@ -500,6 +534,10 @@ __global__ void __cluster_dims__(kLuCtas, 1, 1) __launch_bounds__(kLuClusterThre
       __syncthreads();
       const double akk = col[k];
       for (int r = k + 1 + tid; r < P; r += NT) l_own[r] = col[r] / akk;
+      if (FACTOR) {
+        for (int r = k + 1 + tid; r < P; r += NT) wl[static_cast<int64_t>(k) * P + r] = l_own[r];
+        if (tid == 0) wp[k] = static_cast<double>(s_piv[par]);
+      }
     }
     cl.sync();
     const double* l_src = cl.map_shared_rank(l_own, o);
@@ -516,14 +554,16 @@ __global__ void __cluster_dims__(kLuCtas, 1, 1) __launch_bounds__(kLuClusterThre
         c[k] = c[piv];
         c[piv] = t;
       }
-    if (tid == 0 && piv != k && piv < P) {
+    if (!FACTOR && tid == 0 && piv != k && piv < P) {
       const double t = s_x[k];
       s_x[k] = s_x[piv];
       s_x[piv] = t;
     }
     __syncthreads();
-    const double xk = s_x[k];
-    for (int r = k + 1 + tid; r < P; r += NT) s_x[r] -= l_own[r] * xk;
+    if (!FACTOR) {
+      const double xk = s_x[k];
+      for (int r = k + 1 + tid; r < P; r += NT) s_x[r] -= l_own[r] * xk;
+    }
     // trailing update of this CTA's columns j > k, rows r > k
     const int nq = ncol - q0, nr = P - k - 1;
     for (int e = tid; e < nq * nr; e += NT) {
@@ -542,16 +582,50 @@ __global__ void __cluster_dims__(kLuCtas, 1, 1) __launch_bounds__(kLuClusterThre
   }
   cl.sync();
   if (rank == 0) {
-    for (int k = P - 1; k >= 0; --k) {
-      const int base = k * (k + 1) / 2;
-      const double xk = s_x[k] / s_u[base + k];
-      for (int r = tid; r < k; r += NT) s_x[r] -= s_u[base + r] * xk;
-      __syncthreads();
-      if (tid == 0) s_x[k] = xk;
-      __syncthreads();
+    if (FACTOR) {
+      for (int e = tid; e < P * (P + 1) / 2; e += NT) wu[e] = s_u[e];
+      return;
     }
+    back_substitute(P, s_u, s_x, tid, NT);
     for (int r = tid; r < P; r += NT) xg[r] = s_x[r];
   }
+}
+
+// The solve of a factorisation left by lu_cluster_kernel<true> in W: the
+// fused kernel's right-hand-side operations replayed in its order (the pivot
+// swap and the multipliers of step k, k = 0..P-1, then the back
+// substitution), one CTA per system.  Dynamic shared memory: s_x[P], packed
+// U[P (P + 1) / 2].
+__global__ void __launch_bounds__(kLuClusterThreads)
+    lu_solve_factored_kernel(int P, const double* __restrict__ W, double* __restrict__ b) {
+  extern __shared__ double sf_smem[];
+  const int sys = blockIdx.x;
+  const double* wl = W + static_cast<int64_t>(sys) * lu_workspace_doubles(P);
+  const double* wp = wl + static_cast<int64_t>(P) * P;
+  const double* wu = wp + P;
+  double* xg = b + static_cast<int64_t>(sys) * P;
+  double* s_x = sf_smem;
+  double* s_u = s_x + P;
+  const int tid = threadIdx.x;
+  constexpr int NT = kLuClusterThreads;
+  for (int r = tid; r < P; r += NT) s_x[r] = xg[r];
+  for (int e = tid; e < P * (P + 1) / 2; e += NT) s_u[e] = wu[e];
+  __syncthreads();
+  for (int k = 0; k < P; ++k) {
+    const int piv = static_cast<int>(wp[k]);
+    if (tid == 0 && piv != k && piv < P) {
+      const double t = s_x[k];
+      s_x[k] = s_x[piv];
+      s_x[piv] = t;
+    }
+    __syncthreads();
+    const double xk = s_x[k];
+    const double* l_own = wl + static_cast<int64_t>(k) * P;
+    for (int r = k + 1 + tid; r < P; r += NT) s_x[r] -= l_own[r] * xk;
+    __syncthreads();
+  }
+  back_substitute(P, s_u, s_x, tid, NT);
+  for (int r = tid; r < P; r += NT) xg[r] = s_x[r];
 }
 
 struct LoadsArgs {
@@ -954,11 +1028,11 @@ int fvx_lu_solve_batched(int n_systems, int P, double* A, double* b, void* strea
     const int ncmax = (P + fvx::kLuCtas - 1) / fvx::kLuCtas;
     const size_t smem =
         8 * (static_cast<size_t>(ncmax) * P + 3 * static_cast<size_t>(P) + P * (P + 1) / 2);
-    FVX_CUDA_TRY(cudaFuncSetAttribute(fvx::lu_solve_cluster_kernel,
+    FVX_CUDA_TRY(cudaFuncSetAttribute(fvx::lu_cluster_kernel<false>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(smem)));
-    fvx::lu_solve_cluster_kernel<<<n_systems * fvx::kLuCtas, fvx::kLuClusterThreads, smem,
-                                   static_cast<cudaStream_t>(stream)>>>(P, A, b);
+    fvx::lu_cluster_kernel<false><<<n_systems * fvx::kLuCtas, fvx::kLuClusterThreads, smem,
+                                    static_cast<cudaStream_t>(stream)>>>(P, A, b, nullptr);
     FVX_LAUNCH_CHECK();
     return FVX_OK;
   }
@@ -973,6 +1047,39 @@ int fvx_lu_solve_batched(int n_systems, int P, double* A, double* b, void* strea
                                     static_cast<int>(smem)));
   fvx::lu_solve_kernel<<<n_systems, fvx::kLuThreads, smem, static_cast<cudaStream_t>(stream)>>>(
       P, T, A, b);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int64_t fvx_lu_workspace_bytes(int P) {
+  return P >= 1 && P <= fvx::kLuClusterMaxP ? 8 * fvx::lu_workspace_doubles(P) : 0;
+}
+
+int fvx_lu_factor_batched(int n_systems, int P, double* A, double* work, void* stream) {
+  FVX_ARG_CHECK(n_systems >= 1 && P >= 1 && P <= fvx::kLuClusterMaxP && A && work,
+                "bad factor arguments (P must be 1..%d)", fvx::kLuClusterMaxP);
+  const int ncmax = (P + fvx::kLuCtas - 1) / fvx::kLuCtas;
+  const size_t smem =
+      8 * (static_cast<size_t>(ncmax) * P + 3 * static_cast<size_t>(P) + P * (P + 1) / 2);
+  FVX_CUDA_TRY(cudaFuncSetAttribute(fvx::lu_cluster_kernel<true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)));
+  fvx::lu_cluster_kernel<true><<<n_systems * fvx::kLuCtas, fvx::kLuClusterThreads, smem,
+                                 static_cast<cudaStream_t>(stream)>>>(P, A, nullptr, work);
+  FVX_LAUNCH_CHECK();
+  return FVX_OK;
+}
+
+int fvx_lu_solve_factored_batched(int n_systems, int P, const double* work, double* b,
+                                  void* stream) {
+  FVX_ARG_CHECK(n_systems >= 1 && P >= 1 && P <= fvx::kLuClusterMaxP && work && b,
+                "bad solve arguments (P must be 1..%d)", fvx::kLuClusterMaxP);
+  const size_t smem = 8 * (static_cast<size_t>(P) + static_cast<size_t>(P) * (P + 1) / 2);
+  FVX_CUDA_TRY(cudaFuncSetAttribute(fvx::lu_solve_factored_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)));
+  fvx::lu_solve_factored_kernel<<<n_systems, fvx::kLuClusterThreads, smem,
+                                  static_cast<cudaStream_t>(stream)>>>(P, work, b);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }

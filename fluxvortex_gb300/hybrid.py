@@ -61,6 +61,12 @@ class HybridStep:
         self.Ln = {k: z3(P) for k in self.L if k != "area"}
         self.Ln["area"] = torch.zeros(P, **d)
         self.aic = torch.zeros((P, P), **d)
+        # P <= 192: the AIC is factorised on a side stream while the wake and
+        # the particles are swept at the collocation points, and the solve
+        # waits for it (the same strengths bit for bit as the fused solve)
+        wb = int(self.lib.fvx_lu_workspace_bytes(P))
+        self._lu_work = torch.empty(wb // 8, **d) if wb > 0 else None
+        self._lu_side = torch.cuda.Stream(self.device) if wb > 0 else None
         self.rhs = torch.zeros(P, **d)
         self.gamma = torch.zeros(P, **d)
         self.gamma_prev = torch.zeros(P, **d)
@@ -173,6 +179,16 @@ class HybridStep:
         _capi.check(lib.fvx_uvlm_aic(1, P, L["colloc"].data_ptr(), L["normal"].data_ptr(),
                                      L["br"].data_ptr(), L["fr"].data_ptr(), L["fl"].data_ptr(),
                                      L["bl"].data_ptr(), cfg.rc0, cfg.nu, self.aic.data_ptr(), st))
+        fac_done = None
+        if self._lu_work is not None:
+            aic_ready = torch.cuda.Event()
+            aic_ready.record(torch.cuda.current_stream(self.device))
+            self._lu_side.wait_event(aic_ready)
+            _capi.check(lib.fvx_lu_factor_batched(1, P, self.aic.data_ptr(),
+                                                  self._lu_work.data_ptr(),
+                                                  self._lu_side.cuda_stream))
+            fac_done = torch.cuda.Event()
+            fac_done.record(self._lu_side)
         # 2-3. wake on collocation: ring rows + particles
         R = self.R
         Wc, gc, ac = self.W[self.cur], self.wg[self.cur], self.wa[self.cur]
@@ -199,7 +215,13 @@ class HybridStep:
                                      self.u_inf.ctypes.data, t, self.rhs.data_ptr(), st))
         # 4. strengths (in place: rhs -> Gamma)
         self.gamma.copy_(self.rhs)
-        _capi.check(lib.fvx_lu_solve_batched(1, P, self.aic.data_ptr(), self.gamma.data_ptr(), st))
+        if fac_done is not None:
+            torch.cuda.current_stream(self.device).wait_event(fac_done)
+            _capi.check(lib.fvx_lu_solve_factored_batched(1, P, self._lu_work.data_ptr(),
+                                                          self.gamma.data_ptr(), st))
+        else:
+            _capi.check(lib.fvx_lu_solve_batched(1, P, self.aic.data_ptr(),
+                                                 self.gamma.data_ptr(), st))
         # 5. loads at the bound-leg centres (wake and particles swept above)
         k = self.k
         cl_p = self._cl[k:].data_ptr() if out2 is None else out2[0:].data_ptr()

@@ -306,6 +306,14 @@ int fvx_tree_sample_pairs(fvx_tree* tree, int list, int max_pairs, void* X, floa
  *   on a cluster of 8 CTAs per system (thread-block clusters), larger P on
  *   one CTA per system; both give the same results.  A's contents afterwards
  *   are unspecified (the one-CTA form works in it).
+ * lu_factor_batched / lu_solve_factored_batched (P <= 192): the same solve in
+ *   two launches, so that the factorisation of A can overlap the work that
+ *   forms b.  lu_factor_batched reads A and leaves the factorisation in
+ *   `work` (lu_workspace_bytes(P) bytes per system, back to back); A is not
+ *   written.  lu_solve_factored_batched then solves in place (x -> b) by
+ *   replaying the fused kernel's elimination in its order, so x is the same
+ *   bit for bit as lu_solve_batched's.  lu_workspace_bytes returns 0 for P
+ *   outside 1..192.
  * loads: Kutta-Joukowski force on each bound leg, rho (G_ij - G_i-1,j) (V x l),
  *   V = u_inf - v_body + v1 + v2 + v3, minus rho dG/dt A n (gamma_prev NULL:
  *   no unsteady term); writes CL and CDi (device scalars) on the reference
@@ -351,6 +359,10 @@ int fvx_uvlm_rhs(int nc, const FvxSurfaces* s, const double* colloc, const doubl
                  const double* v1, const double* v2, const double* u_inf, double t, double* rhs,
                  void* stream);
 int fvx_lu_solve_batched(int n_systems, int P, double* A, double* b, void* stream);
+int64_t fvx_lu_workspace_bytes(int P);
+int fvx_lu_factor_batched(int n_systems, int P, double* A, double* work, void* stream);
+int fvx_lu_solve_factored_batched(int n_systems, int P, const double* work, double* b,
+                                  void* stream);
 int fvx_uvlm_loads(int nc, const FvxSurfaces* s, const double* gamma, const double* gamma_prev,
                    const double* leg_center, const double* leg_vec, const double* area,
                    const double* normal, const double* v1, const double* v2, const double* v3,

@@ -135,6 +135,37 @@ def test_lu_solve_batched_matches_numpy(cuda, P, nsys):
     assert np.abs(got - x).max() <= 1e-9 * np.abs(x).max()
 
 
+@pytest.mark.parametrize("P,nsys", [(1, 1), (7, 3), (120, 2), (192, 3)])
+def test_lu_factor_then_solve_is_the_fused_solve_bit_for_bit(cuda, P, nsys):
+    """The factorisation on its own (A left unchanged) and the replayed solve
+    give the fused solve's solution bit for bit; sizes past 192 are refused."""
+    import torch
+    from fluxvortex_gb300 import _capi
+    lib = _capi.load()
+    rng = np.random.default_rng(100 + P)
+    A = rng.standard_normal((nsys, P, P)) + 0.5 * np.eye(P)
+    if P > 1:
+        A[:, 0, 0] = 0.0
+    b = rng.standard_normal((nsys, P))
+    dA = torch.as_tensor(A, device="cuda").contiguous()
+    db = torch.as_tensor(b, device="cuda").contiguous()
+    fused_A, fused_b = dA.clone(), db.clone()
+    _capi.check(lib.fvx_lu_solve_batched(nsys, P, fused_A.data_ptr(), fused_b.data_ptr(), None))
+    wb = int(lib.fvx_lu_workspace_bytes(P))
+    assert wb == 8 * (P * P + P + P * (P + 1) // 2)
+    work = torch.empty(nsys * wb // 8, dtype=torch.float64, device="cuda")
+    A0 = dA.clone()
+    _capi.check(lib.fvx_lu_factor_batched(nsys, P, dA.data_ptr(), work.data_ptr(), None))
+    _capi.check(lib.fvx_lu_solve_factored_batched(nsys, P, work.data_ptr(), db.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert _capi.status_read_and_clear() == 0
+    assert torch.equal(dA, A0)
+    assert torch.equal(db, fused_b)
+    assert lib.fvx_lu_workspace_bytes(193) == 0
+    with pytest.raises(_capi.FvxError):
+        _capi.check(lib.fvx_lu_factor_batched(1, 193, dA.data_ptr(), work.data_ptr(), None))
+
+
 def test_lu_solve_flags_a_singular_system_and_refuses_oversize(cuda):
     import torch
     from fluxvortex_gb300 import _capi
