@@ -425,6 +425,7 @@ namespace cg = cooperative_groups;
 constexpr int kLuCtas = 8;
 constexpr int kLuClusterThreads = 256;
 constexpr int kLuClusterMaxP = 192;  // packed U, P (P + 1) / 2 doubles, in CTA 0
+static_assert(kLuClusterThreads >= kLuClusterMaxP, "the replayed solve takes one row per thread");
 
 // doubles of one system's factorisation workspace: multipliers P x P, pivots
 // P, packed U P (P + 1) / 2
@@ -595,7 +596,7 @@ __global__ void __cluster_dims__(kLuCtas, 1, 1) __launch_bounds__(kLuClusterThre
 // fused kernel's right-hand-side operations replayed in its order (the pivot
 // swap and the multipliers of step k, k = 0..P-1, then the back
 // substitution), one CTA per system.  Dynamic shared memory: s_x[P], packed
-// U[P (P + 1) / 2].
+// U[P (P + 1) / 2], the pivots[P].
 __global__ void __launch_bounds__(kLuClusterThreads)
     lu_solve_factored_kernel(int P, const double* __restrict__ W, double* __restrict__ b) {
   extern __shared__ double sf_smem[];
@@ -606,13 +607,20 @@ __global__ void __launch_bounds__(kLuClusterThreads)
   double* xg = b + static_cast<int64_t>(sys) * P;
   double* s_x = sf_smem;
   double* s_u = s_x + P;
+  double* s_p = s_u + P * (P + 1) / 2;  // pivots
   const int tid = threadIdx.x;
-  constexpr int NT = kLuClusterThreads;
-  for (int r = tid; r < P; r += NT) s_x[r] = xg[r];
+  constexpr int NT = kLuClusterThreads;  // >= P: one row per thread and step
+  for (int r = tid; r < P; r += NT) {
+    s_x[r] = xg[r];
+    s_p[r] = wp[r];
+  }
   for (int e = tid; e < P * (P + 1) / 2; e += NT) s_u[e] = wu[e];
   __syncthreads();
+  // step k updates row k + 1 + tid with step k's multiplier for that row; the
+  // next step's multiplier is loaded while this step's barrier waits
+  double lcur = 1 + tid < P ? wl[1 + tid] : 0.0;
   for (int k = 0; k < P; ++k) {
-    const int piv = static_cast<int>(wp[k]);
+    const int piv = static_cast<int>(s_p[k]);
     if (tid == 0 && piv != k && piv < P) {
       const double t = s_x[k];
       s_x[k] = s_x[piv];
@@ -620,8 +628,11 @@ __global__ void __launch_bounds__(kLuClusterThreads)
     }
     __syncthreads();
     const double xk = s_x[k];
-    const double* l_own = wl + static_cast<int64_t>(k) * P;
-    for (int r = k + 1 + tid; r < P; r += NT) s_x[r] -= l_own[r] * xk;
+    const int rn = k + 2 + tid;
+    const double lnext = rn < P ? wl[static_cast<int64_t>(k + 1) * P + rn] : 0.0;
+    const int r = k + 1 + tid;
+    if (r < P) s_x[r] -= lcur * xk;
+    lcur = lnext;
     __syncthreads();
   }
   back_substitute(P, s_u, s_x, tid, NT);
@@ -1074,7 +1085,7 @@ int fvx_lu_solve_factored_batched(int n_systems, int P, const double* work, doub
                                   void* stream) {
   FVX_ARG_CHECK(n_systems >= 1 && P >= 1 && P <= fvx::kLuClusterMaxP && work && b,
                 "bad solve arguments (P must be 1..%d)", fvx::kLuClusterMaxP);
-  const size_t smem = 8 * (static_cast<size_t>(P) + static_cast<size_t>(P) * (P + 1) / 2);
+  const size_t smem = 8 * (2 * static_cast<size_t>(P) + static_cast<size_t>(P) * (P + 1) / 2);
   FVX_CUDA_TRY(cudaFuncSetAttribute(fvx::lu_solve_factored_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     static_cast<int>(smem)));
