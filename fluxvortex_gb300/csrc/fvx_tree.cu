@@ -1308,78 +1308,93 @@ __device__ __forceinline__ void near_tile_direct(const float4* __restrict__ row,
 // h^2 / 16, and the rounding stays within a few tens of FP32 units of q and
 // of a source's peak contribution).
 // Per-target constants: M2 = -2 t, TT = |t|^2, NG = -G, TG = t . G.
-template <int MODE>
+template <int MODE, int NP>
 __device__ __forceinline__ void near_tile_factored(const float4* __restrict__ row, int nit, int g,
-                                                   uint64_t M2X, uint64_t M2Y, uint64_t M2Z,
-                                                   uint64_t TT, uint64_t NGX, uint64_t NGY,
-                                                   uint64_t NGZ, uint64_t TG, uint64_t* acc) {
+                                                   const uint64_t* M2X, const uint64_t* M2Y,
+                                                   const uint64_t* M2Z, const uint64_t* TT,
+                                                   const uint64_t* NGX, const uint64_t* NGY,
+                                                   const uint64_t* NGZ, const uint64_t* TG,
+                                                   uint64_t (*acc)[3]) {
   const uint64_t ONE = x2::pack(1.f, 1.f), C06 = x2::pack(0.6f, 0.6f);
-  uint64_t FA[3] = {0ull, 0ull, 0ull}, WA[3] = {0ull, 0ull, 0ull}, WC[3] = {0ull, 0ull, 0ull};
-  // unrolled 4 x for velocity, 2 x for the longer stretching body (4.61 ->
-  // 4.49 ms per sweep at 2^20; 1 x and 8 x are no better)
-  constexpr int kUnroll = MODE == FVX_PAIR_STRETCH ? 2 : 4;
+  uint64_t FA[NP][3], WA[NP][3], WC[NP][3];
+#pragma unroll
+  for (int p = 0; p < NP; ++p)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) FA[p][c] = WA[p][c] = WC[p][c] = 0ull;
+  // unrolled 4 x for one pair of velocity targets, 2 x for two pairs and for
+  // the longer stretching body (4.61 -> 4.49 ms per sweep at 2^20; 1 x and
+  // 8 x are no better)
+  constexpr int kUnroll = MODE == FVX_PAIR_STRETCH || NP > 1 ? 2 : 4;
 #pragma unroll kUnroll
   for (int i = 0; i < nit; ++i) {
     const float4* r = row + i * g;
     const float4 u0 = r[0], u1 = r[kNearTile], u2 = r[2 * kNearTile];
-    const uint64_t X = x2::dup(u0.x), Y = x2::dup(u0.y), Z = x2::dup(u0.z);
-    uint64_t Q = x2::add(TT, x2::dup(u0.w));
-    Q = x2::fma(M2X, X, Q);
-    Q = x2::fma(M2Y, Y, Q);
-    Q = x2::fma(M2Z, Z, Q);
-    float qa, qb;
-    x2::unpack(Q, qa, qb);
-    const uint64_t T = x2::pack(rsqrt_ftz(qa), rsqrt_ftz(qb));
-    const uint64_t T2 = x2::mul(T, T);
-    const uint64_t T3 = x2::mul(T2, T);
+    const uint64_t X = x2::dup(u0.x), Y = x2::dup(u0.y), Z = x2::dup(u0.z), S = x2::dup(u0.w);
     const uint64_t C1 = x2::dup(u1.x);
     const uint64_t AX = x2::dup(u1.y), AY = x2::dup(u1.z), AZ = x2::dup(u1.w);
     const uint64_t CX = x2::dup(u2.x), CY = x2::dup(u2.y), CZ = x2::dup(u2.z);
-    if (MODE == FVX_PAIR_VELOCITY) {
-      const uint64_t F = x2::mul(T3, x2::fma(C1, T2, ONE));
-      FA[0] = x2::fma(F, AX, FA[0]);
-      FA[1] = x2::fma(F, AY, FA[1]);
-      FA[2] = x2::fma(F, AZ, FA[2]);
-      WC[0] = x2::fma(F, CX, WC[0]);
-      WC[1] = x2::fma(F, CY, WC[1]);
-      WC[2] = x2::fma(F, CZ, WC[2]);
-    } else {
-      const uint64_t T5 = x2::mul(T3, T2);
-      const uint64_t F = x2::fma(C1, T5, T3);
-      uint64_t DG = x2::fma(NGX, X, TG);
-      DG = x2::fma(NGY, Y, DG);
-      DG = x2::fma(NGZ, Z, DG);
-      const uint64_t W = x2::mul(x2::mul(x2::fma(C1, T2, C06), T5), DG);
-      FA[0] = x2::fma(F, AX, FA[0]);
-      FA[1] = x2::fma(F, AY, FA[1]);
-      FA[2] = x2::fma(F, AZ, FA[2]);
-      WA[0] = x2::fma(W, AX, WA[0]);
-      WA[1] = x2::fma(W, AY, WA[1]);
-      WA[2] = x2::fma(W, AZ, WA[2]);
-      WC[0] = x2::fma(W, CX, WC[0]);
-      WC[1] = x2::fma(W, CY, WC[1]);
-      WC[2] = x2::fma(W, CZ, WC[2]);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      uint64_t Q = x2::add(TT[p], S);
+      Q = x2::fma(M2X[p], X, Q);
+      Q = x2::fma(M2Y[p], Y, Q);
+      Q = x2::fma(M2Z[p], Z, Q);
+      float qa, qb;
+      x2::unpack(Q, qa, qb);
+      const uint64_t T = x2::pack(rsqrt_ftz(qa), rsqrt_ftz(qb));
+      const uint64_t T2 = x2::mul(T, T);
+      const uint64_t T3 = x2::mul(T2, T);
+      if (MODE == FVX_PAIR_VELOCITY) {
+        const uint64_t F = x2::mul(T3, x2::fma(C1, T2, ONE));
+        FA[p][0] = x2::fma(F, AX, FA[p][0]);
+        FA[p][1] = x2::fma(F, AY, FA[p][1]);
+        FA[p][2] = x2::fma(F, AZ, FA[p][2]);
+        WC[p][0] = x2::fma(F, CX, WC[p][0]);
+        WC[p][1] = x2::fma(F, CY, WC[p][1]);
+        WC[p][2] = x2::fma(F, CZ, WC[p][2]);
+      } else {
+        const uint64_t T5 = x2::mul(T3, T2);
+        const uint64_t F = x2::fma(C1, T5, T3);
+        uint64_t DG = x2::fma(NGX[p], X, TG[p]);
+        DG = x2::fma(NGY[p], Y, DG);
+        DG = x2::fma(NGZ[p], Z, DG);
+        const uint64_t W = x2::mul(x2::mul(x2::fma(C1, T2, C06), T5), DG);
+        FA[p][0] = x2::fma(F, AX, FA[p][0]);
+        FA[p][1] = x2::fma(F, AY, FA[p][1]);
+        FA[p][2] = x2::fma(F, AZ, FA[p][2]);
+        WA[p][0] = x2::fma(W, AX, WA[p][0]);
+        WA[p][1] = x2::fma(W, AY, WA[p][1]);
+        WA[p][2] = x2::fma(W, AZ, WA[p][2]);
+        WC[p][0] = x2::fma(W, CX, WC[p][0]);
+        WC[p][1] = x2::fma(W, CY, WC[p][1]);
+        WC[p][2] = x2::fma(W, CZ, WC[p][2]);
+      }
     }
   }
-  if (MODE == FVX_PAIR_VELOCITY) {
-    // sum f (d x a) = t x FA - sum f c, t = -M2 / 2 (exact)
-    const uint64_t MH = x2::pack(-0.5f, -0.5f);
-    const uint64_t TX = x2::mul(M2X, MH), TY = x2::mul(M2Y, MH), TZ = x2::mul(M2Z, MH);
-    acc[0] = x2::sub(x2::mul(TY, FA[2]), x2::fma(TZ, FA[1], WC[0]));
-    acc[1] = x2::sub(x2::mul(TZ, FA[0]), x2::fma(TX, FA[2], WC[1]));
-    acc[2] = x2::sub(x2::mul(TX, FA[1]), x2::fma(TY, FA[0], WC[2]));
-  } else {
-    // G x FA + t x (sum w a) - sum w c = -(NG x FA) + 2.5 (M2 x WA) + 5 WC
-    const uint64_t MONE = x2::pack(-1.f, -1.f), P25 = x2::pack(2.5f, 2.5f),
-                   P5 = x2::pack(5.f, 5.f);
-    const uint64_t GX = x2::mul(NGX, MONE), GY = x2::mul(NGY, MONE), GZ = x2::mul(NGZ, MONE);
-    const uint64_t HX = x2::mul(M2X, P25), HY = x2::mul(M2Y, P25), HZ = x2::mul(M2Z, P25);
-    acc[0] = x2::add(x2::sub(x2::mul(GY, FA[2]), x2::mul(GZ, FA[1])),
-                     x2::fma(P5, WC[0], x2::sub(x2::mul(HY, WA[2]), x2::mul(HZ, WA[1]))));
-    acc[1] = x2::add(x2::sub(x2::mul(GZ, FA[0]), x2::mul(GX, FA[2])),
-                     x2::fma(P5, WC[1], x2::sub(x2::mul(HZ, WA[0]), x2::mul(HX, WA[2]))));
-    acc[2] = x2::add(x2::sub(x2::mul(GX, FA[1]), x2::mul(GY, FA[0])),
-                     x2::fma(P5, WC[2], x2::sub(x2::mul(HX, WA[1]), x2::mul(HY, WA[0]))));
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    if (MODE == FVX_PAIR_VELOCITY) {
+      // sum f (d x a) = t x FA - sum f c, t = -M2 / 2 (exact)
+      const uint64_t MH = x2::pack(-0.5f, -0.5f);
+      const uint64_t TX = x2::mul(M2X[p], MH), TY = x2::mul(M2Y[p], MH), TZ = x2::mul(M2Z[p], MH);
+      acc[p][0] = x2::sub(x2::mul(TY, FA[p][2]), x2::fma(TZ, FA[p][1], WC[p][0]));
+      acc[p][1] = x2::sub(x2::mul(TZ, FA[p][0]), x2::fma(TX, FA[p][2], WC[p][1]));
+      acc[p][2] = x2::sub(x2::mul(TX, FA[p][1]), x2::fma(TY, FA[p][0], WC[p][2]));
+    } else {
+      // G x FA + t x (sum w a) - sum w c = -(NG x FA) + 2.5 (M2 x WA) + 5 WC
+      const uint64_t MONE = x2::pack(-1.f, -1.f), P25 = x2::pack(2.5f, 2.5f),
+                     P5 = x2::pack(5.f, 5.f);
+      const uint64_t GX = x2::mul(NGX[p], MONE), GY = x2::mul(NGY[p], MONE),
+                     GZ = x2::mul(NGZ[p], MONE);
+      const uint64_t HX = x2::mul(M2X[p], P25), HY = x2::mul(M2Y[p], P25),
+                     HZ = x2::mul(M2Z[p], P25);
+      acc[p][0] = x2::add(x2::sub(x2::mul(GY, FA[p][2]), x2::mul(GZ, FA[p][1])),
+                          x2::fma(P5, WC[p][0], x2::sub(x2::mul(HY, WA[p][2]), x2::mul(HZ, WA[p][1]))));
+      acc[p][1] = x2::add(x2::sub(x2::mul(GZ, FA[p][0]), x2::mul(GX, FA[p][2])),
+                          x2::fma(P5, WC[p][1], x2::sub(x2::mul(HZ, WA[p][0]), x2::mul(HX, WA[p][2]))));
+      acc[p][2] = x2::add(x2::sub(x2::mul(GX, FA[p][1]), x2::mul(GY, FA[p][0])),
+                          x2::fma(P5, WC[p][2], x2::sub(x2::mul(HX, WA[p][1]), x2::mul(HY, WA[p][0]))));
+    }
   }
 }
 
@@ -1388,11 +1403,11 @@ __device__ __forceinline__ void near_tile_factored(const float4* __restrict__ ro
 template <int MODE, int KERNEL, int TPT>
 struct EvalSmem {
   // paired path: Winckelmans velocity / stretching with two targets per thread
-  static constexpr bool PACKED = TPT == 2 && KERNEL == FVX_KERNEL_WINCKELMANS &&
+  static constexpr bool PACKED = (TPT == 2 || TPT == 4) && KERNEL == FVX_KERNEL_WINCKELMANS &&
                                  (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_STRETCH);
   // paired: the tile's planes, then the lanes' running near-field sums
   // (hi, lo of two targets x three components, 12 x 32 floats)
-  static constexpr int kNearBytes = PACKED ? kPlanes * kNearTile * 16 + 12 * kEvalThreads * 4
+  static constexpr int kNearBytes = PACKED ? kPlanes * kNearTile * 16 + 6 * TPT * kEvalThreads * 4
                                            : kNearTile * 2 * static_cast<int>(sizeof(float4));
   static constexpr int kFarBytes = kFarTile * kRecFloats * 4;
   static constexpr int bytes = kNearBytes > kFarBytes ? kNearBytes : kFarBytes;
@@ -1416,13 +1431,15 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
   const float3 cT = cell_center_rel(A.leaf_key[t], A.h);
   const int nno = A.near_off[t], nnc = A.near_cnt[t];
   const int fno = A.far_off[t], fnc = A.far_cnt[t];
-  // Paired path: the leaf's targets go in chunks of at most 32.  A chunk of c
-  // targets puts two in each of m = ceil(c/2) lanes (the halves of the paired
-  // registers) and splits the sources over g = floor(32/m) groups of m lanes
-  // (group j sums rows j, j + g, ...); the groups' partial sums are added into
-  // group 0 at the end of the near field.  Lanes past the g groups mirror
-  // group 0 and are not counted.  The other paths take TPT targets per lane.
-  const int chunk_step = PACKED ? kEvalThreads : kEvalThreads * TPT;
+  // Paired path: TPT = 2 or 4 targets per lane (one or two pairs of paired
+  // registers), the leaf's targets in chunks of at most 16 TPT.  A chunk of c
+  // targets puts TPT in each of m = ceil(c/TPT) lanes and splits the sources
+  // over g = floor(32/m) groups of m lanes (group j sums rows j, j + g, ...);
+  // the groups' partial sums are added into group 0 at the end of the near
+  // field.  Lanes past the g groups mirror group 0 and are not counted.  The
+  // other paths take TPT targets per lane.
+  constexpr int NP = TPT / 2;  // pairs of targets per lane (paired path)
+  const int chunk_step = PACKED ? (kEvalThreads / 2) * TPT : kEvalThreads * TPT;
   const int lane = threadIdx.x;
 
   for (int chunk = 0; chunk < tcount; chunk += chunk_step) {
@@ -1430,7 +1447,7 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
     int m = kEvalThreads, g = 1, grp = 0, tl = lane;
     bool spare = false;
     if constexpr (PACKED) {
-      m = (cend - chunk + 1) >> 1;
+      m = (cend - chunk + TPT - 1) / TPT;
       g = kEvalThreads / m;
       grp = lane / m;
       tl = lane - grp * m;
@@ -1478,30 +1495,40 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
       // leaf), so one tile mixes leaves and its barriers, loads and fold are
       // paid per 128 sources instead of per near leaf.
       const unsigned full = 0xffffffffu;
-      const uint64_t TX = x2::pack(ox[0], ox[1]), TY = x2::pack(oy[0], oy[1]),
-                     TZ = x2::pack(oz[0], oz[1]);
-      const uint64_t GX = x2::pack(gx[0], gx[1]), GY = x2::pack(gy[0], gy[1]),
-                     GZ = x2::pack(gz[0], gz[1]);
+      // per-target constants, pair p holding the lane's targets 2p and 2p + 1:
+      // direct form t, G, -5 G; factored form -2 t, |t|^2, -G, t . G
+      uint64_t TX[NP], TY[NP], TZ[NP], GX[NP], GY[NP], GZ[NP], G5X[NP], G5Y[NP], G5Z[NP];
+      uint64_t M2X[NP], M2Y[NP], M2Z[NP], TT[NP], NGX[NP], NGY[NP], NGZ[NP], TG[NP];
       const float m5 = -5.f, m2 = -2.f;
-      const uint64_t G5X = x2::pack(m5 * gx[0], m5 * gx[1]),
-                     G5Y = x2::pack(m5 * gy[0], m5 * gy[1]),
-                     G5Z = x2::pack(m5 * gz[0], m5 * gz[1]);
-      // per-target constants of the factored form: -2 t, |t|^2, -G, t . G
-      const uint64_t M2X = x2::pack(m2 * ox[0], m2 * ox[1]),
-                     M2Y = x2::pack(m2 * oy[0], m2 * oy[1]),
-                     M2Z = x2::pack(m2 * oz[0], m2 * oz[1]);
-      const uint64_t TT = x2::pack(fmaf(ox[0], ox[0], fmaf(oy[0], oy[0], oz[0] * oz[0])),
-                                   fmaf(ox[1], ox[1], fmaf(oy[1], oy[1], oz[1] * oz[1])));
-      const uint64_t NGX = x2::pack(-gx[0], -gx[1]), NGY = x2::pack(-gy[0], -gy[1]),
-                     NGZ = x2::pack(-gz[0], -gz[1]);
-      const uint64_t TG = x2::pack(fmaf(ox[0], gx[0], fmaf(oy[0], gy[0], oz[0] * gz[0])),
-                                   fmaf(ox[1], gx[1], fmaf(oy[1], gy[1], oz[1] * gz[1])));
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        const int a = 2 * p, b = 2 * p + 1;
+        TX[p] = x2::pack(ox[a], ox[b]);
+        TY[p] = x2::pack(oy[a], oy[b]);
+        TZ[p] = x2::pack(oz[a], oz[b]);
+        GX[p] = x2::pack(gx[a], gx[b]);
+        GY[p] = x2::pack(gy[a], gy[b]);
+        GZ[p] = x2::pack(gz[a], gz[b]);
+        G5X[p] = x2::pack(m5 * gx[a], m5 * gx[b]);
+        G5Y[p] = x2::pack(m5 * gy[a], m5 * gy[b]);
+        G5Z[p] = x2::pack(m5 * gz[a], m5 * gz[b]);
+        M2X[p] = x2::pack(m2 * ox[a], m2 * ox[b]);
+        M2Y[p] = x2::pack(m2 * oy[a], m2 * oy[b]);
+        M2Z[p] = x2::pack(m2 * oz[a], m2 * oz[b]);
+        TT[p] = x2::pack(fmaf(ox[a], ox[a], fmaf(oy[a], oy[a], oz[a] * oz[a])),
+                         fmaf(ox[b], ox[b], fmaf(oy[b], oy[b], oz[b] * oz[b])));
+        NGX[p] = x2::pack(-gx[a], -gx[b]);
+        NGY[p] = x2::pack(-gy[a], -gy[b]);
+        NGZ[p] = x2::pack(-gz[a], -gz[b]);
+        TG[p] = x2::pack(fmaf(ox[a], gx[a], fmaf(oy[a], gy[a], oz[a] * gz[a])),
+                         fmaf(ox[b], gx[b], fmaf(oy[b], gy[b], oz[b] * gz[b])));
+      }
       float4* s_r = reinterpret_cast<float4*>(s_raw);
       // the running sums stay in shared memory through the near field (each
       // lane its own column), not in registers
       float* s_sum = reinterpret_cast<float*>(s_raw + kPlanes * kNearTile * 16) + lane;
 #pragma unroll
-      for (int e = 0; e < 12; ++e) s_sum[e * kEvalThreads] = 0.f;
+      for (int e = 0; e < 6 * TPT; ++e) s_sum[e * kEvalThreads] = 0.f;
       for (int q0 = 0; q0 < nnc; q0 += kEvalThreads) {
         int mss = 0, msn = 0;
         float mdx = 0.f, mdy = 0.f, mdz = 0.f;
@@ -1566,40 +1593,46 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
             }
           }
           __syncthreads();
-          uint64_t acc2[3];
+          uint64_t acc2[NP][3];
           const float4* row = s_r + grp;
-          if constexpr (FACT)
-            near_tile_factored<MODE>(row, rows / g, g, M2X, M2Y, M2Z, TT, NGX, NGY, NGZ, TG, acc2);
-          else
-            near_tile_direct<MODE>(row, rows / g, g, TX, TY, TZ, GX, GY, GZ, G5X, G5Y, G5Z, acc2);
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            float a[2];
-            x2::unpack(acc2[c], a[0], a[1]);
-#pragma unroll
-            for (int j = 0; j < 2; ++j) {
-              float* e = s_sum + (4 * c + 2 * j) * kEvalThreads;
-              float h = e[0], l = e[kEvalThreads];
-              fold(h, l, a[j]);
-              e[0] = h;
-              e[kEvalThreads] = l;
-            }
+          if constexpr (FACT) {
+            near_tile_factored<MODE, NP>(row, rows / g, g, M2X, M2Y, M2Z, TT, NGX, NGY, NGZ, TG,
+                                         acc2);
+          } else {
+            static_assert(FACT || NP == 1, "the direct form takes two targets per lane");
+            near_tile_direct<MODE>(row, rows / g, g, TX[0], TY[0], TZ[0], GX[0], GY[0], GZ[0],
+                                   G5X[0], G5Y[0], G5Z[0], acc2[0]);
           }
+#pragma unroll
+          for (int p = 0; p < NP; ++p)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              float a[2];
+              x2::unpack(acc2[p][c], a[0], a[1]);
+#pragma unroll
+              for (int h2 = 0; h2 < 2; ++h2) {
+                float* e = s_sum + (2 * (c * TPT + 2 * p + h2)) * kEvalThreads;
+                float hv = e[0], lv = e[kEvalThreads];
+                fold(hv, lv, a[h2]);
+                e[0] = hv;
+                e[kEvalThreads] = lv;
+              }
+            }
         }
       }
 #pragma unroll
       for (int c = 0; c < 3; ++c)
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
-          hi[j][c] = s_sum[(4 * c + 2 * j) * kEvalThreads];
-          lo[j][c] = s_sum[(4 * c + 2 * j + 1) * kEvalThreads];
+        for (int j = 0; j < TPT; ++j) {
+          hi[j][c] = s_sum[(2 * (c * TPT + j)) * kEvalThreads];
+          lo[j][c] = s_sum[(2 * (c * TPT + j) + 1) * kEvalThreads];
         }
       load_targets();
       // the groups' partial sums into group 0 (lanes tl + j m, j < g), read
       // from copies: every lane updates its own sums while others read them
-      float ph[2][3], pq[2][3];
+      float ph[TPT][3], pq[TPT][3];
 #pragma unroll
-      for (int s2 = 0; s2 < 2; ++s2)
+      for (int s2 = 0; s2 < TPT; ++s2)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           ph[s2][c] = hi[s2][c];
@@ -1608,7 +1641,7 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
       for (int j = 1; j < g; ++j) {
         const int src = tl + j * m;
 #pragma unroll
-        for (int s2 = 0; s2 < 2; ++s2)
+        for (int s2 = 0; s2 < TPT; ++s2)
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             const float vh = __shfl_sync(full, ph[s2][c], src);
@@ -1759,11 +1792,13 @@ __global__ void __launch_bounds__(kEvalThreads) eval_kernel(EvalArgs A) {
   eval_leaves<MODE, KERNEL, TPT, false>(A);
 }
 
-// The factored stretching loop (paired Winckelmans), held to 24 resident
-// warps per SM, i.e. at most 80 registers: more warps in flight than its
-// unbounded register count allows.
+// The factored loops (paired Winckelmans): stretching with two targets per
+// lane held to 24 resident warps per SM (at most 80 registers); velocity with
+// four targets per lane, so that each staged value serves four pairs (the
+// velocity loop was bound by the shared-memory pipe: 3.09 -> 2.93 ms per sweep
+// at 2^20), held to 20 warps (96 registers; 16 and 24 warps are no faster).
 template <int MODE, int KERNEL, int TPT>
-__global__ void __launch_bounds__(kEvalThreads, 24)
+__global__ void __launch_bounds__(kEvalThreads, TPT == 4 ? 20 : 24)
     eval_kernel_factored(EvalArgs A) {
   eval_leaves<MODE, KERNEL, TPT, true>(A);
 }
@@ -2271,7 +2306,7 @@ void launch_eval_tpt(int mode, int nleaf, const tree::EvalArgs& A, bool factored
     case FVX_PAIR_VELOCITY: {
       auto k = eval_kernel<FVX_PAIR_VELOCITY, KERNEL, TPT>;
       if constexpr (F)
-        if (factored) k = eval_kernel_factored<FVX_PAIR_VELOCITY, KERNEL, TPT>;
+        if (factored) k = eval_kernel_factored<FVX_PAIR_VELOCITY, KERNEL, 4>;
       k<<<resident_grid(k, nleaf), kEvalThreads, 0, s>>>(A);
       break;
     }
