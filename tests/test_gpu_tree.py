@@ -172,17 +172,23 @@ def _factored_case(n=3000, leaf=16, seed=5):
     return pos, gam, sig
 
 
-def test_factored_near_loop_matches_oracle_algorithm(cuda):
+@pytest.mark.parametrize("n,leaf", [(3000, 16), (12000, 64)])
+def test_factored_near_loop_matches_oracle_algorithm(cuda, n, leaf):
     """The factored velocity and stretching loops against the oracle's FP64
     restatement of the same treecode: the difference is the FP32 rounding
-    (3.9e-7 measured for both; the bar is ten times that)."""
-    pos, gam, sig = _factored_case()
-    tr = OT.build(pos, theta=0.5, leaf_target=16)
+    (3.9e-7 measured for both; the bar is ten times that).  Leaf target 64
+    gives leaves of more than 64 particles, which the velocity loop (four
+    targets per lane, chunks of up to 64) takes in two chunks."""
+    pos, gam, sig = _factored_case(n=n, leaf=leaf)
+    tr = OT.build(pos, theta=0.5, leaf_target=leaf)
     OT.moments(tr, pos, gam)
     u, J = OT.evaluate(tr, pos, gam, sig, kernel="winckelmans")
     S = np.einsum("tij,tj->ti", J, gam)
-    gu, _, _ = _tree(_capi.PAIR_VELOCITY, "winckelmans", pos, gam, sig, cuda, 16)
-    gs, _, _ = _tree(_capi.PAIR_STRETCH, "winckelmans", pos, gam, sig, cuda, 16, tg=gam)
+    if leaf == 64:
+        counts = np.asarray(tr["levels"][-1]["end"]) - np.asarray(tr["levels"][-1]["start"])
+        assert counts.max() > 64
+    gu, _, _ = _tree(_capi.PAIR_VELOCITY, "winckelmans", pos, gam, sig, cuda, leaf)
+    gs, _, _ = _tree(_capi.PAIR_STRETCH, "winckelmans", pos, gam, sig, cuda, leaf, tg=gam)
     eu, es = rel_err(gu, u), rel_err(gs, S)
     print(f"factored loop vs oracle: velocity {eu:.2e}, stretching {es:.2e}")
     assert eu < 4e-6 and es < 4e-6
