@@ -37,7 +37,7 @@ namespace tree {
 
 constexpr int kScanBlock = 2048;   // elements per scan block (1024 threads x 2)
 constexpr int kSortItems = 1024;   // keys per radix-sort block (256 threads x 4)
-constexpr int kEvalThreads = 32;   // eval CTA (one warp); 1 or 2 targets per thread
+constexpr int kEvalThreads = 32;   // eval CTA (one warp); 1, 2 or 4 targets per thread
 constexpr int kFarTile = 32;       // far cells staged per tile
 constexpr int kNearTile = 128;     // source particles staged per tile
 constexpr int kRecFloats = 40;     // far-cell record
@@ -1402,11 +1402,12 @@ __device__ __forceinline__ void near_tile_factored(const float4* __restrict__ ro
 // and the far-cell records share the storage.
 template <int MODE, int KERNEL, int TPT>
 struct EvalSmem {
-  // paired path: Winckelmans velocity / stretching with two targets per thread
+  // paired path: Winckelmans velocity / stretching with two or four targets
+  // per thread
   static constexpr bool PACKED = (TPT == 2 || TPT == 4) && KERNEL == FVX_KERNEL_WINCKELMANS &&
                                  (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_STRETCH);
   // paired: the tile's planes, then the lanes' running near-field sums
-  // (hi, lo of two targets x three components, 12 x 32 floats)
+  // (hi, lo of TPT targets x three components, 6 TPT x 32 floats)
   static constexpr int kNearBytes = PACKED ? kPlanes * kNearTile * 16 + 6 * TPT * kEvalThreads * 4
                                            : kNearTile * 2 * static_cast<int>(sizeof(float4));
   static constexpr int kFarBytes = kFarTile * kRecFloats * 4;
