@@ -8,14 +8,14 @@
 //     tile at a time and chains the four layers through its quarter of the
 //     tensor memory: MMA into TMEM -> tcgen05.ld -> bias + SiLU in registers
 //     -> the group's shared activation tile -> next MMA, so one group's
-//     epilogue overlaps the others' MMAs.  Inference runs on F16 operands
-//     (weights converted while staged), training on BF16 (the type its
-//     backward GEMMs read).  Two input/output policies: plain rows
-//     (X -> Y, with the hidden pre-activations / activations kept for
-//     training), and the treecode's learned far field (features computed
-//     in-kernel from the (target leaf, source cell) pair list, outputs scaled
-//     back to physical local-expansion coefficients and added to the leaf's
-//     local expansion);
+//     epilogue overlaps the others' MMAs.  Inference runs with the hidden
+//     weights and biases halved while staged and a packed BF16 SiLU; training
+//     with the FP32 SiLU.  Two kernels: mlp_fwd_kernel on plain rows (X -> Y,
+//     with the hidden pre-activations / activations kept for training), and
+//     farfield_kernel, the treecode's learned far field, in which two more
+//     warpgroups form the inputs of every tile from the (target leaf, source
+//     cell) pair lists and reduce its outputs, scaled back to physical
+//     local-expansion coefficients, into the leaves' expansions;
 //   * training: a generic tile GEMM C = op(A) op(B)^T on tcgen05 (operands
 //     staged transposed as needed by the threads, split over K with FP32
 //     atomics) for dW = dZ^T H and dH = dZ W, plus element-wise kernels for
@@ -50,7 +50,6 @@ struct FwdSmem {
   __nv_bfloat16 w3[H * H];
   __nv_bfloat16 w4[OUT * H];
   __nv_bfloat16 act[kGroups][128 * H];
-  float aux[kGroups][128][4];  // far field: the output scales m/d^2, m/d^3, m/d^4 of each row
   float bias[BN];
   uint32_t hbias[3 * H / 2];  // inference form: half the hidden layers' biases, packed BF16 pairs
   uint64_t bar[kGroups];
@@ -269,12 +268,6 @@ struct FarIO {
   FarJudge judge;    // per-class actions of the FP64 judge (none by default)
 };
 
-template <bool FAR>
-struct FwdArgs {
-  RowsIO r;
-  FarIO f;
-};
-
 // row `row` of a 128 x H accumulator -> bias + SiLU -> BF16 activation tile
 __device__ void epilogue_hidden(uint32_t tmem, int row, const float* bias, __nv_bfloat16* act,
                                 float* z_out, __nv_bfloat16* h_out) {
@@ -360,6 +353,23 @@ __device__ __forceinline__ bool group_wait_mma(int g, uint64_t* bar, uint32_t& p
   return ok;
 }
 
+// As group_wait_mma, with the first thread's `issued` (false when it did not
+// issue the MMA): the group's warp 0 polls only for an issued MMA, and every
+// thread learns the AND.
+__device__ __forceinline__ bool group_wait_mma_if(int g, uint64_t* bar, uint32_t& ph, bool issued) {
+  bool w = issued;
+  if ((threadIdx.x & 127) < 32) {
+    const bool any = __shfl_sync(0xffffffffu, issued ? 1 : 0, 0) != 0;
+    if (any) w = w && mbar_wait(bar, ph);
+    else w = false;
+  }
+  ph ^= 1u;
+  tc::fence_before_sync();
+  const bool ok = group_sync_and(g, w);
+  tc::fence_after_sync();
+  return ok;
+}
+
 // Group-local fence + barrier before an MMA: the group's shared-memory writes
 // made visible to the tensor core (async proxy) and its TMEM reads done.
 __device__ __forceinline__ void group_handoff(int g) {
@@ -369,12 +379,13 @@ __device__ __forceinline__ void group_handoff(int g) {
   tc::fence_after_sync();
 }
 
-// INFER: the inference form -- BF16 operands, hidden weights and biases
-// halved while staged, the packed BF16 SiLU of epilogue_hidden_infer -- always
-// taken by the treecode far field; the training forward (with stored
-// pre-activations and activations) keeps the FP32 SiLU of epilogue_hidden.
-template <bool FAR, bool INFER>
-__global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> A, int rows,
+// The network on rows of inputs: Y[rows][32] from X[rows][48].  INFER: the
+// inference form -- BF16 operands, hidden weights and biases halved while
+// staged, the packed BF16 SiLU of epilogue_hidden_infer (the far-field
+// kernel's arithmetic); the training forward (with stored pre-activations and
+// activations) keeps the FP32 SiLU of epilogue_hidden.
+template <bool INFER>
+__global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(RowsIO A, int rows,
                                                            const __nv_bfloat16* __restrict__ W,
                                                            const float* __restrict__ bias) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -384,7 +395,6 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
     for (int g = 0; g < kGroups; ++g) mbar_init(&S.bar[g], 1);
     fence_mbar_init();
   }
-  static_assert(INFER || !FAR, "the far field runs the inference form");
   if constexpr (INFER) {
     // hidden layers halved: their accumulators are z/2, the tanh argument
     stage_kmajor_scaled(S.w1, W + W1o, H, IN, 0.5f);
@@ -416,78 +426,17 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
   bool ok = true;
   const int ntiles = (rows + 127) / 128;
   const int tile_step = kGroups * gridDim.x;
-  // Far field: the pair inputs of a row are loaded one tile ahead, in two
-  // dependent levels (the pair's leaf and cell indices while the next tile's
-  // first MMA runs, the leaf key and the cell record while its third MMA
-  // runs), so that the loads' latency leaves the tile's serial chain.
-  int pf_leaf = 0, pf_cell = 0, pf_li = 0;
-  uint32_t pf_key = 0;
-  RecRegs pf_rec;
-  auto fetch_index = [&](int t) {
-    const int r = t * 128 + lt;
-    if (t < ntiles && r < rows) {
-      pf_li = r >= A.f.l0.n ? 1 : 0;
-      const int rr = pf_li ? r - A.f.l0.n : r;
-      pf_leaf = (pf_li ? A.f.l1.pair_tgt : A.f.l0.pair_tgt)[rr];
-      pf_cell = (pf_li ? A.f.l1.pair_cell : A.f.l0.pair_cell)[rr];
-    }
-  };
-  auto fetch_record = [&](int t) {
-    const int r = t * 128 + lt;
-    if (t < ntiles && r < rows) {
-      pf_key = (pf_li ? A.f.l1.tgt_key : A.f.l0.tgt_key)[pf_leaf];
-      pf_rec = load_record(A.f.rec + static_cast<int64_t>(pf_cell) * kRecFloats);
-    }
-  };
-  if constexpr (FAR) {
-    fetch_index(kGroups * blockIdx.x + grp);
-    fetch_record(kGroups * blockIdx.x + grp);
-  }
   for (int tile = kGroups * blockIdx.x + grp; tile < ntiles && ok; tile += tile_step) {
     const int row = tile * 128 + lt;
     const bool act_row = row < rows;
-    int leaf = 0, li = 0;
-    bool keep = true;
     // input tile (K = 48)
     {
       char* base = reinterpret_cast<char*>(act);
-      if constexpr (FAR) {
-        float f[IN];
-        float* ax = S.aux[grp][lt];
-        if (act_row) {
-          leaf = pf_leaf;
-          li = pf_li;
-          const float th = li ? A.f.l1.h : A.f.l0.h;
-          const float3 cT = leaf_center(pf_key, th);
-          if (A.f.judge.act != nullptr) {
-            // the residual only for the classes whose network the judge kept
-            const float dx = cT.x - pf_rec.v[0], dy = cT.y - pf_rec.v[1], dz = cT.z - pf_rec.v[2];
-            keep = A.f.judge.act[judge_class(li, th, pf_rec.v[3], dx * dx + dy * dy + dz * dz,
-                                             A.f.judge.inv_theta2)] == 0;
-          }
-          const PairScale sc = pair_features(pf_rec.v, cT.x, cT.y, cT.z, th, f);
-          ax[0] = sc.s2;
-          ax[1] = sc.s3;
-          ax[2] = sc.s4;
-        } else {
-          for (int q = 0; q < IN; ++q) f[q] = 0.f;
-        }
-#pragma unroll
-        for (int k8 = 0; k8 < IN / 8; ++k8) {
-          __align__(16) __nv_bfloat162 b[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-            b[q] = __floats2bfloat162_rn(f[8 * k8 + 2 * q], f[8 * k8 + 2 * q + 1]);
-          *reinterpret_cast<uint4*>(base + tc::kmajor_offset(lt, 8 * k8, IN)) =
-              *reinterpret_cast<uint4*>(b);
-        }
-      } else {
-        for (int k8 = 0; k8 < IN / 8; ++k8) {
-          uint4 v = make_uint4(0, 0, 0, 0);
-          if (act_row)
-            v = *reinterpret_cast<const uint4*>(A.r.X + static_cast<int64_t>(row) * IN + 8 * k8);
-          *reinterpret_cast<uint4*>(base + tc::kmajor_offset(lt, 8 * k8, IN)) = v;
-        }
+      for (int k8 = 0; k8 < IN / 8; ++k8) {
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (act_row)
+          v = *reinterpret_cast<const uint4*>(A.X + static_cast<int64_t>(row) * IN + 8 * k8);
+        *reinterpret_cast<uint4*>(base + tc::kmajor_offset(lt, 8 * k8, IN)) = v;
       }
     }
     for (int l = 0; l < 3; ++l) {
@@ -495,20 +444,14 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
       if (lt == 0)
         tc::gemm_issue(tmem, act, l == 0 ? S.w1 : (l == 1 ? S.w2 : S.w3), l == 0 ? IN : H,
                        tc::idesc_bf16(128, H), false, bar, 0);
-      if constexpr (FAR) {
-        if (l == 0) fetch_index(tile + tile_step);
-        if (l == 2) fetch_record(tile + tile_step);
-      }
       if (!group_wait_mma(grp, bar, ph)) {
         ok = false;
         break;
       }
       float* zo = nullptr;
       __nv_bfloat16* ho = nullptr;
-      if constexpr (!FAR) {
-        if (A.r.z_store && act_row) zo = A.r.z_store + (static_cast<int64_t>(l) * rows + row) * H;
-        if (A.r.h_store && act_row) ho = A.r.h_store + (static_cast<int64_t>(l) * rows + row) * H;
-      }
+      if (A.z_store && act_row) zo = A.z_store + (static_cast<int64_t>(l) * rows + row) * H;
+      if (A.h_store && act_row) ho = A.h_store + (static_cast<int64_t>(l) * rows + row) * H;
       if constexpr (INFER)
         epilogue_hidden_infer(tmem, lt, S.hbias + l * H / 2, act);
       else
@@ -522,38 +465,299 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
       ok = false;
       break;
     }
-    if constexpr (FAR) {
-      // the learned residual of this row, back to physical units (the analytic
-      // translation is added by its own kernel)
+    for (int c0 = 0; c0 < OUT; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(tmem + lane_base + c0, v);
+      if (!act_row) continue;
+      float4* y = reinterpret_cast<float4*>(A.Y + static_cast<int64_t>(row) * OUT + c0);
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        y[q] = make_float4(v[4 * q] + S.bias[B4o + c0 + 4 * q],
+                           v[4 * q + 1] + S.bias[B4o + c0 + 4 * q + 1],
+                           v[4 * q + 2] + S.bias[B4o + c0 + 4 * q + 2],
+                           v[4 * q + 3] + S.bias[B4o + c0 + 4 * q + 3]);
+    }
+    // no barrier here: the next tile's first handoff orders this tile's TMEM
+    // reads before the MMA that overwrites them
+  }
+  if (!ok && lt == 0) flag_status(kStatusTimeout);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32) tc::tmem_dealloc(S.tmem, 128 * kGroups);
+}
+
+// ---- the learned far field: consumer warpgroups and a producer warpgroup ----------------
+// Warpgroups 0..3 (consumers) chain the network's layers through their quarter
+// of the tensor memory as in mlp_fwd_kernel: MMA -> epilogue -> next MMA.
+// Warpgroups 4 and 5 (producers, two consumer groups each) form every tile's
+// inputs (the pair features into the group's activation tile, the output
+// scales and targets into aux) and reduce every tile's outputs into the
+// leaves' expansions, so that neither stage sits on a consumer's chain.  A
+// producer's warp q serves rows 32q..32q+31 of every tile (the TMEM lanes warp
+// q may read) and loads the pair indices and cell records one step ahead.
+// Per group g:
+//   feat_bar[g] (4 arrivals, one per producer warp) completes once per tile
+//     when its inputs are written and the previous tile's output accumulator
+//     has been read (so the activation tile and TMEM are free);
+//   out_bar[g] (tcgen05.commit of the tile's last MMA) completes when the
+//     tile's outputs are in TMEM and the activation tile has been read.
+// A producer visits its groups' tiles in increasing order: its step j is tile
+// j / 2 of its group j % 2.  Registers move from the consumers to the
+// producers by setmaxnreg; the host checks that the launch holds them.
+constexpr int kProducers = 2;
+constexpr int kGroupsPerProducer = kGroups / kProducers;
+constexpr int kFarThreads = (kGroups + kProducers) * 128;
+constexpr int kConsumerRegs = 56, kProducerRegs = 128;
+constexpr int kFarRegsNeeded = (kGroups * kConsumerRegs + kProducers * kProducerRegs) * 128;
+
+struct FarSmem {
+  __nv_bfloat16 w1[H * IN];
+  __nv_bfloat16 w2[H * H];
+  __nv_bfloat16 w3[H * H];
+  __nv_bfloat16 w4[OUT * H];
+  __nv_bfloat16 act[kGroups][128 * H];
+  // per row: the output scales m/d^2, m/d^3, m/d^4 (zero for a row without a
+  // pair or whose class dropped the network) and the target id
+  float aux[kGroups][128][4];
+  float bias4[OUT];
+  uint32_t hbias[3 * H / 2];  // half the hidden layers' biases, packed BF16 pairs
+  uint64_t bar[kGroups], feat_bar[kGroups], out_bar[kGroups];
+  uint32_t tmem;
+};
+
+// The producer's view of a pair ahead of its use: the index level (leaf, cell,
+// list), then the record level (the leaf key and the cell record as well).
+struct PairIndex {
+  int leaf = 0, cell = 0, li = 0;
+  bool act = false;
+};
+struct PairFetch {
+  PairIndex i;
+  uint32_t key = 0;
+  RecRegs rec;
+};
+
+__global__ void __launch_bounds__(kFarThreads, 1) farfield_kernel(FarIO F, int rows,
+                                                                  const __nv_bfloat16* __restrict__ W,
+                                                                  const float* __restrict__ bias) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  FarSmem& S = *reinterpret_cast<FarSmem*>(smem_raw);
+  if (threadIdx.x < 32) tc::tmem_alloc(&S.tmem, 128 * kGroups);
+  if (threadIdx.x == 0) {
+    for (int g = 0; g < kGroups; ++g) {
+      mbar_init(&S.bar[g], 1);
+      mbar_init(&S.feat_bar[g], 4);
+      mbar_init(&S.out_bar[g], 1);
+    }
+    fence_mbar_init();
+  }
+  // hidden layers halved: their accumulators are z/2, the tanh argument
+  stage_kmajor_scaled(S.w1, W + W1o, H, IN, 0.5f);
+  stage_kmajor_scaled(S.w2, W + W2o, H, H, 0.5f);
+  stage_kmajor_scaled(S.w3, W + W3o, H, H, 0.5f);
+  stage_kmajor(S.w4, W + W4o, OUT, H);
+  for (int i = threadIdx.x; i < 3 * H / 2; i += blockDim.x) {
+    const __nv_bfloat162 hb = __floats2bfloat162_rn(0.5f * bias[2 * i], 0.5f * bias[2 * i + 1]);
+    S.hbias[i] = *reinterpret_cast<const uint32_t*>(&hb);
+  }
+  for (int i = threadIdx.x; i < OUT; i += blockDim.x) S.bias4[i] = bias[B4o + i];
+  tc::fence_smem_to_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const int grp = threadIdx.x >> 7;
+  const int lt = threadIdx.x & 127;
+  const int ntiles = (rows + 127) / 128;
+  const int tile_step = kGroups * gridDim.x;
+  bool ok = true;
+  if (grp < kGroups) {
+    // ---- consumer: the four layers of the group's tiles ----
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kConsumerRegs));
+    const uint32_t tmem = S.tmem + static_cast<uint32_t>(128 * grp);
+    __nv_bfloat16* act = S.act[grp];
+    uint64_t* bar = &S.bar[grp];
+    uint32_t ph = 0, fph = 0;
+    for (int tile = kGroups * blockIdx.x + grp; tile < ntiles; tile += tile_step) {
+      // the tile's inputs written and the previous tile's outputs read: only
+      // the issuing thread waits; the group learns the outcome with the first
+      // MMA's wait
+      bool fed = true;
+      if (lt == 0) {
+        fed = mbar_wait(&S.feat_bar[grp], fph);
+        tc::fence_after_sync();
+      }
+      fph ^= 1u;
+      for (int l = 0; l < 3; ++l) {
+        if (l > 0) group_handoff(grp);
+        if (lt == 0 && fed)
+          tc::gemm_issue(tmem, act, l == 0 ? S.w1 : (l == 1 ? S.w2 : S.w3), l == 0 ? IN : H,
+                         tc::idesc_bf16(128, H), false, bar, 0);
+        if (!group_wait_mma_if(grp, bar, ph, l > 0 || fed)) {
+          ok = false;
+          break;
+        }
+        epilogue_hidden_infer(tmem, lt, S.hbias + l * H / 2, act);
+      }
+      if (!ok) break;
+      group_handoff(grp);
+      if (lt == 0)
+        tc::gemm_issue(tmem, act, S.w4, H, tc::idesc_bf16(128, OUT), false, &S.out_bar[grp], 0);
+    }
+  } else {
+    // ---- producer: inputs and outputs of its groups' tiles, rows 32q..32q+31 ----
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kProducerRegs));
+    const int g0 = (grp - kGroups) * kGroupsPerProducer;  // the first group served
+    const int q = (threadIdx.x >> 5) & 3;
+    const int lane = threadIdx.x & 31;
+    const int r = 32 * q + lane;  // the row of every tile this thread serves
+    const uint32_t lane_base = static_cast<uint32_t>(32 * q) << 16;
+    auto tile_of = [&](int j) {
+      return kGroups * blockIdx.x + g0 + j % kGroupsPerProducer + j / kGroupsPerProducer * tile_step;
+    };
+    auto fetch_index = [&](PairIndex& I, int j) {
+      const int row = tile_of(j) * 128 + r;
+      I.act = tile_of(j) < ntiles && row < rows;
+      if (I.act) {
+        I.li = row >= F.l0.n ? 1 : 0;
+        const int rr = I.li ? row - F.l0.n : row;
+        I.leaf = (I.li ? F.l1.pair_tgt : F.l0.pair_tgt)[rr];
+        I.cell = (I.li ? F.l1.pair_cell : F.l0.pair_cell)[rr];
+      }
+    };
+    auto fetch_record = [&](PairFetch& P, const PairIndex& I) {
+      P.i = I;
+      if (I.act) {
+        P.key = (I.li ? F.l1.tgt_key : F.l0.tgt_key)[I.leaf];
+        P.rec = load_record(F.rec + static_cast<int64_t>(I.cell) * kRecFloats);
+      }
+    };
+    // the features of a fetched pair, packed BF16 pairs, and its aux row
+    uint32_t fp[IN / 2];
+    float faux[4];
+    auto features = [&](const PairFetch& P) {
+      float f[IN];
+      faux[0] = faux[1] = faux[2] = 0.f;
+      faux[3] = __int_as_float(-1 - r);  // a row without a pair: an id of its own
+      if (P.i.act) {
+        const float th = P.i.li ? F.l1.h : F.l0.h;
+        const float3 cT = leaf_center(P.key, th);
+        bool keep = true;
+        if (F.judge.act != nullptr) {
+          // the residual only for the classes whose network the judge kept
+          const float dx = cT.x - P.rec.v[0], dy = cT.y - P.rec.v[1], dz = cT.z - P.rec.v[2];
+          keep = F.judge.act[judge_class(P.i.li, th, P.rec.v[3], dx * dx + dy * dy + dz * dz,
+                                         F.judge.inv_theta2)] == 0;
+        }
+        const PairScale sc = pair_features(P.rec.v, cT.x, cT.y, cT.z, th, f);
+        if (keep) {
+          faux[0] = sc.s2;
+          faux[1] = sc.s3;
+          faux[2] = sc.s4;
+        }
+        faux[3] = __int_as_float(P.i.leaf | (P.i.li << 30));
+      } else {
+#pragma unroll
+        for (int k = 0; k < IN; ++k) f[k] = 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < IN / 2; ++k) {
+        const __nv_bfloat162 b = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+        fp[k] = *reinterpret_cast<const uint32_t*>(&b);
+      }
+    };
+    auto write_inputs = [&](int g) {
+      char* base = reinterpret_cast<char*>(S.act[g]);
+#pragma unroll
+      for (int k8 = 0; k8 < IN / 8; ++k8)
+        *reinterpret_cast<uint4*>(base + tc::kmajor_offset(r, 8 * k8, IN)) =
+            make_uint4(fp[4 * k8], fp[4 * k8 + 1], fp[4 * k8 + 2], fp[4 * k8 + 3]);
+      *reinterpret_cast<float4*>(S.aux[g][r]) = make_float4(faux[0], faux[1], faux[2], faux[3]);
+    };
+    // inputs of the first tile of each group served: nothing to wait for
+    PairFetch cur;
+    PairIndex nxt;
+    fetch_index(nxt, 0);
+    for (int j = 0; j < kGroupsPerProducer; ++j) {
+      fetch_record(cur, nxt);
+      fetch_index(nxt, j + 1);
+      if (tile_of(j) < ntiles) {
+        features(cur);
+        write_inputs(g0 + j);
+        tc::fence_smem_to_async();
+        __syncwarp();
+        if (lane == 0)
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                           smem_u32(&S.feat_bar[g0 + j]))
+                       : "memory");
+      }
+    }
+    // the record of step kGroupsPerProducer's tile, then the next step's index
+    fetch_record(cur, nxt);
+    fetch_index(nxt, kGroupsPerProducer + 1);
+    uint32_t oph = 0u;  // bit g: the parity of group g's next out_bar phase
+    for (int j = 0; tile_of(j) < ntiles && ok; ++j) {
+      const int g = g0 + j % kGroupsPerProducer;
+      // the inputs of this group's next tile (step j + kGroupsPerProducer), from cur
+      const bool has_next = tile_of(j + kGroupsPerProducer) < ntiles;
+      if (has_next) features(cur);
+      // one step ahead: the next step's record, the one after's index
+      fetch_record(cur, nxt);
+      fetch_index(nxt, j + kGroupsPerProducer + 2);
+      // tile j's outputs
+      bool w = true;
+      if (lane == 0) w = mbar_wait(&S.out_bar[g], (oph >> g) & 1u);
+      oph ^= 1u << g;
+      if (!__shfl_sync(0xffffffffu, w ? 1 : 0, 0)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after_sync();
       float x[OUT];
-      for (int c0 = 0; c0 < OUT; c0 += 16) {
-        float v[16];
-        tc::tmem_ld16(tmem + lane_base + c0, v);
-        const float* ax = S.aux[grp][lt];
+      {
+        uint32_t v0[16], v1[16];
+        tc::tmem_ld16_issue(S.tmem + static_cast<uint32_t>(128 * g) + lane_base, v0);
+        tc::tmem_ld16_issue(S.tmem + static_cast<uint32_t>(128 * g) + lane_base + 16, v1);
+        tc::tmem_ld_wait(v0);
+        tc::tmem_ld_wait(v1);
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-          const int c = c0 + i;
-          const float sc = c < 3 ? ax[0] : (c < 12 ? ax[1] : ax[2]);
-          x[c] = (act_row && keep && c < NOUT) ? (v[i] + S.bias[B4o + c]) * sc : 0.f;
+          x[i] = __uint_as_float(v0[i]);
+          x[16 + i] = __uint_as_float(v1[i]);
         }
       }
-      const int lane = threadIdx.x & 31;
-      // the target, unique across the two lists
-      const int my = act_row ? (leaf | (li << 30)) : -1 - lane;
-      float* L = act_row ? (li ? A.f.l1.local : A.f.l0.local) + static_cast<int64_t>(leaf) * OUT
+      const float4 ax = *reinterpret_cast<const float4*>(S.aux[g][r]);
+      if (has_next) {
+        write_inputs(g);
+        tc::fence_smem_to_async();
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (has_next && lane == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&S.feat_bar[g]))
+                     : "memory");
+      // the learned residual of this row, back to physical units (the analytic
+      // translation is added by its own kernel)
+#pragma unroll
+      for (int c = 0; c < OUT; ++c) {
+        const float sc = c < 3 ? ax.x : (c < 12 ? ax.y : ax.z);
+        x[c] = c < NOUT ? (x[c] + S.bias4[c]) * sc : 0.f;
+      }
+      const int my = __float_as_int(ax.w);  // unique across the two lists
+      const bool act_row = my >= 0;
+      float* L = act_row ? ((my >> 30) ? F.l1.local : F.l0.local) +
+                               static_cast<int64_t>(my & ((1 << 30) - 1)) * OUT
                          : nullptr;
       if (__all_sync(0xffffffffu, my == __shfl_sync(0xffffffffu, my, 0))) {
-        // one target for the whole warp (pairs are ordered by target, runs are
-        // long): reduce-scatter by recursive halving, 31 shuffles for the 32
-        // columns; lane c ends with the warp's sum of column c
+        // one target for the whole warp: reduce-scatter by recursive halving,
+        // 31 shuffles for the 32 columns; lane c ends with column c's sum
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) {
           const bool upper = (lane & off) != 0;
 #pragma unroll
-          for (int j = 0; j < off; ++j) {
-            const float send = upper ? x[j] : x[j + off];
-            const float keep = upper ? x[j + off] : x[j];
-            x[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+          for (int i = 0; i < off; ++i) {
+            const float send = upper ? x[i] : x[i + off];
+            const float kept = upper ? x[i + off] : x[i];
+            x[i] = kept + __shfl_xor_sync(0xffffffffu, send, off);
           }
         }
         if (lane < NOUT) atomicAdd(L + lane, x[0]);
@@ -575,25 +779,8 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(FwdArgs<FAR> 
         }
       }
     }
-    for (int c0 = 0; c0 < OUT && !FAR; c0 += 16) {
-      float v[16];
-      tc::tmem_ld16(tmem + lane_base + c0, v);
-      if constexpr (FAR) continue;
-      if (!act_row) continue;
-      {
-        float4* y = reinterpret_cast<float4*>(A.r.Y + static_cast<int64_t>(row) * OUT + c0);
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-          y[q] = make_float4(v[4 * q] + S.bias[B4o + c0 + 4 * q],
-                             v[4 * q + 1] + S.bias[B4o + c0 + 4 * q + 1],
-                             v[4 * q + 2] + S.bias[B4o + c0 + 4 * q + 2],
-                             v[4 * q + 3] + S.bias[B4o + c0 + 4 * q + 3]);
-      }
-    }
-    // no barrier here: the next tile's first handoff orders this tile's TMEM
-    // reads before the MMA that overwrites them
   }
-  if (!ok && lt == 0) flag_status(kStatusTimeout);
+  if (!ok && (threadIdx.x & 31) == 0) flag_status(kStatusTimeout);
   tc::fence_before_sync();
   __syncthreads();
   if (threadIdx.x < 32) tc::tmem_dealloc(S.tmem, 128 * kGroups);
@@ -1115,17 +1302,22 @@ int mlp_farfield_launch(const FarPairs& a, const FarPairs& b, const float* rec, 
   if (npairs <= 0) return FVX_OK;
   static int done = 0;
   if (!done) {
-    int rc = set_smem(mlp_fwd_kernel<true, true>, sizeof(FwdSmem));
+    // setmaxnreg moves registers between the warpgroups within what the launch
+    // holds: refuse to run a build whose launch would hold fewer
+    cudaFuncAttributes fa{};
+    FVX_CUDA_TRY(cudaFuncGetAttributes(&fa, farfield_kernel));
+    const int per_thread = (fa.numRegs + 7) / 8 * 8;
+    FVX_ARG_CHECK(per_thread * kFarThreads >= kFarRegsNeeded,
+                  "far-field kernel built with %d registers per thread; its warpgroups need %d",
+                  fa.numRegs, kFarRegsNeeded / kFarThreads);
+    int rc = set_smem(farfield_kernel, sizeof(FarSmem));
     if (rc) return rc;
     done = 1;
   }
-  FwdArgs<true> A;
-  A.r = RowsIO{nullptr, nullptr, nullptr, nullptr};
-  A.f = FarIO{a, b, rec, judge};
   const int nctas = ((npairs + 127) / 128 + kGroups - 1) / kGroups;
   const int grid = nctas < device_sm_count() ? nctas : device_sm_count();
-  mlp_fwd_kernel<true, true><<<grid, kGroups * 128, sizeof(FwdSmem), s>>>(
-      A, npairs, static_cast<const __nv_bfloat16*>(W), bias);
+  farfield_kernel<<<grid, kFarThreads, sizeof(FarSmem), s>>>(
+      FarIO{a, b, rec, judge}, npairs, static_cast<const __nv_bfloat16*>(W), bias);
   FVX_LAUNCH_CHECK();
   return FVX_OK;
 }
@@ -1201,19 +1393,17 @@ int fvx_mlp_forward(const void* X, int rows, const void* W, const float* bias, f
   if (rows == 0) return FVX_OK;
   static int done = 0;
   if (!done) {
-    int rc = set_smem(mlp_fwd_kernel<false, false>, sizeof(FwdSmem));
-    if (!rc) rc = set_smem(mlp_fwd_kernel<false, true>, sizeof(FwdSmem));
+    int rc = set_smem(mlp_fwd_kernel<false>, sizeof(FwdSmem));
+    if (!rc) rc = set_smem(mlp_fwd_kernel<true>, sizeof(FwdSmem));
     if (rc) return rc;
     done = 1;
   }
-  FwdArgs<false> A;
-  A.r = RowsIO{static_cast<const __nv_bfloat16*>(X), Y, z_store,
-               static_cast<__nv_bfloat16*>(h_store)};
-  A.f = FarIO{fvx::FarPairs{}, fvx::FarPairs{}, nullptr};
+  const RowsIO A{static_cast<const __nv_bfloat16*>(X), Y, z_store,
+                 static_cast<__nv_bfloat16*>(h_store)};
   const int nctas = ((rows + 127) / 128 + kGroups - 1) / kGroups;
   const int grid = nctas < fvx::device_sm_count() ? nctas : fvx::device_sm_count();
-  // without stores it is inference: the form the treecode far field runs
-  auto kern = (z_store || h_store) ? mlp_fwd_kernel<false, false> : mlp_fwd_kernel<false, true>;
+  // without stores it is inference: the arithmetic the treecode far field runs
+  auto kern = (z_store || h_store) ? mlp_fwd_kernel<false> : mlp_fwd_kernel<true>;
   kern<<<grid, kGroups * 128, sizeof(FwdSmem), static_cast<cudaStream_t>(stream)>>>(
       A, rows, static_cast<const __nv_bfloat16*>(W), bias);
   FVX_LAUNCH_CHECK();
