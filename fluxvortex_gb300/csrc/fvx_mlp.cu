@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(RowsIO A, int
   if (threadIdx.x < 32) tc::tmem_dealloc(S.tmem, 128 * kGroups);
 }
 
-// ---- the learned far field: consumer warpgroups and a producer warpgroup ----------------
+// ---- the learned far field: consumer and producer warpgroups ----------------------------
 // Warpgroups 0..3 (consumers) chain the network's layers through their quarter
 // of the tensor memory as in mlp_fwd_kernel: MMA -> epilogue -> next MMA.
 // Warpgroups 4 and 5 (producers, two consumer groups each) form every tile's
@@ -506,6 +506,7 @@ __global__ void __launch_bounds__(kGroups * 128, 1) mlp_fwd_kernel(RowsIO A, int
 // producers by setmaxnreg; the host checks that the launch holds them.
 constexpr int kProducers = 2;
 constexpr int kGroupsPerProducer = kGroups / kProducers;
+static_assert(kGroups % kProducers == 0, "each producer serves the same number of groups");
 constexpr int kFarThreads = (kGroups + kProducers) * 128;
 constexpr int kConsumerRegs = 56, kProducerRegs = 128;
 constexpr int kFarRegsNeeded = (kGroups * kConsumerRegs + kProducers * kProducerRegs) * 128;
