@@ -1296,6 +1296,130 @@ __device__ __forceinline__ void near_tile_direct(const float4* __restrict__ row,
   acc[2] = x2::sub(PS[2], MS[2]);
 }
 
+// Gaussian-erf vorticity of one staged tile (rows {-x, -y, -z, 1/s},
+// {a, 1/s^2}) for the thread's two targets, in paired FP32:
+//   omega += d (fpr (d . a)) - a (fpr r^2 + 2 f)
+// with the core of core_f32<GAUSSIANERF>: x = r^2 / s^2 = rho^2,
+// e = exp(-x / 2), g = erf(rho / sqrt2) - sqrt(2/pi) rho e, f = g / r^3,
+// fpr = (sqrt(2/pi) x e / s - 3 g / r) / r^4.  erf takes the rational form of
+// Abramowitz & Stegun (Handbook of Mathematical Functions, 7.1.26; absolute
+// error <= 1.5e-7): erf(z) = 1 - t (a1 + t (a2 + ... + t a5)) exp(-z^2),
+// t = 1 / (1 + p z), whose exponential at z = rho / sqrt2 is the same e, so a
+// pair takes one ex2, one reciprocal and one reciprocal square root on the
+// MUFU.  A row in which any lane has a pair with x < 0.25 (the self pair and
+// close neighbours, where g cancels) also takes core_f32's series there,
+// selected per target.  Sums d s1 and a s2 are kept apart and subtracted
+// once per tile.
+__device__ __forceinline__ float ex2_ftz(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ void near_tile_vort_gauss(const float4* __restrict__ row, int nit,
+                                                     int g, uint64_t TX, uint64_t TY,
+                                                     uint64_t TZ, uint64_t* acc) {
+  using namespace pair;
+  const uint64_t ONE = x2::dup(1.f);
+  const uint64_t KP = x2::dup(static_cast<float>(0.3275911 * kInvSqrt2));  // p on rho
+  // -a1..-a5: the polynomial enters as 1 - t P e
+  const uint64_t NA1 = x2::dup(-0.254829592f), NA2 = x2::dup(0.284496736f),
+                 NA3 = x2::dup(-1.421413741f), NA4 = x2::dup(1.453152027f),
+                 NA5 = x2::dup(-1.061405429f);
+  const uint64_t NHL2E = x2::dup(static_cast<float>(-0.5 * 1.4426950408889634));  // -log2(e)/2
+  const uint64_t CS = x2::dup(static_cast<float>(kSqrt2OverPi)),
+                 NCS = x2::dup(static_cast<float>(-kSqrt2OverPi)), M3 = x2::dup(-3.f),
+                 TWO = x2::dup(2.f);
+  uint64_t PS[3] = {0ull, 0ull, 0ull}, QS[3] = {0ull, 0ull, 0ull};
+#pragma unroll 2
+  for (int i = 0; i < nit; ++i) {
+    const float4* r = row + i * g;
+    const float4 u0 = r[0], u1 = r[kNearTile];
+    const uint64_t DX = x2::add(TX, x2::dup(u0.x)), DY = x2::add(TY, x2::dup(u0.y)),
+                   DZ = x2::add(TZ, x2::dup(u0.z));
+    const uint64_t IS = x2::dup(u0.w), IS2 = x2::dup(u1.w);
+    const uint64_t AX = x2::dup(u1.x), AY = x2::dup(u1.y), AZ = x2::dup(u1.z);
+    uint64_t R2 = x2::mul(DZ, DZ);
+    R2 = x2::fma(DY, DY, R2);
+    R2 = x2::fma(DX, DX, R2);
+    uint64_t DA = x2::mul(DZ, AZ);
+    DA = x2::fma(DY, AY, DA);
+    DA = x2::fma(DX, AX, DA);
+    const uint64_t X = x2::mul(R2, IS2);
+    float r2a, r2b;
+    x2::unpack(R2, r2a, r2b);
+    const uint64_t IR = x2::pack(rsqrt_ftz(r2a), rsqrt_ftz(r2b));
+    const uint64_t RHO = x2::mul(x2::mul(R2, IR), IS);
+    float ea, eb;
+    x2::unpack(x2::mul(X, NHL2E), ea, eb);
+    const uint64_t E = x2::pack(ex2_ftz(ea), ex2_ftz(eb));
+    float ta, tb;
+    x2::unpack(x2::fma(RHO, KP, ONE), ta, tb);
+    const uint64_t T = x2::pack(rcp_ftz(ta), rcp_ftz(tb));
+    uint64_t P = x2::fma(NA5, T, NA4);
+    P = x2::fma(P, T, NA3);
+    P = x2::fma(P, T, NA2);
+    P = x2::fma(P, T, NA1);
+    P = x2::mul(P, T);
+    const uint64_t G = x2::fma(x2::mul(RHO, E), NCS, x2::fma(P, E, ONE));
+    const uint64_t IR2 = x2::mul(IR, IR), IR3 = x2::mul(IR2, IR);
+    uint64_t F = x2::mul(G, IR3);
+    uint64_t FPR = x2::mul(x2::fma(x2::mul(x2::mul(X, E), IS), CS, x2::mul(x2::mul(G, IR), M3)),
+                           x2::mul(IR3, IR));
+    float xa, xb;
+    x2::unpack(X, xa, xb);
+    if (__any_sync(0xffffffffu, xa < 0.25f || xb < 0.25f)) {
+      // the series of core_f32 for x < 0.25
+      uint64_t H = x2::fma(x2::dup(static_cast<float>(FVX_GA6)), X,
+                           x2::dup(static_cast<float>(FVX_GA5)));
+      H = x2::fma(H, X, x2::dup(static_cast<float>(FVX_GA4)));
+      H = x2::fma(H, X, x2::dup(static_cast<float>(FVX_GA3)));
+      H = x2::fma(H, X, x2::dup(static_cast<float>(FVX_GA2)));
+      H = x2::fma(H, X, x2::dup(static_cast<float>(FVX_GA1)));
+      H = x2::fma(H, X, x2::dup(static_cast<float>(FVX_GA0)));
+      uint64_t DD = x2::fma(x2::dup(static_cast<float>(12.0 * FVX_GA6)), X,
+                            x2::dup(static_cast<float>(10.0 * FVX_GA5)));
+      DD = x2::fma(DD, X, x2::dup(static_cast<float>(8.0 * FVX_GA4)));
+      DD = x2::fma(DD, X, x2::dup(static_cast<float>(6.0 * FVX_GA3)));
+      DD = x2::fma(DD, X, x2::dup(static_cast<float>(4.0 * FVX_GA2)));
+      DD = x2::fma(DD, X, x2::dup(static_cast<float>(2.0 * FVX_GA1)));
+      const uint64_t IS3 = x2::mul(x2::mul(IS, IS), IS);
+      const uint64_t FS = x2::mul(x2::mul(CS, H), IS3);
+      const uint64_t FPRS = x2::mul(x2::mul(x2::mul(x2::mul(CS, DD), IS3), IS), IS);
+      float fa, fb, pa, pb, sa, sb, qa, qb;
+      x2::unpack(F, fa, fb);
+      x2::unpack(FPR, pa, pb);
+      x2::unpack(FS, sa, sb);
+      x2::unpack(FPRS, qa, qb);
+      if (xa < 0.25f) {
+        fa = sa;
+        pa = qa;
+      }
+      if (xb < 0.25f) {
+        fb = sb;
+        pb = qb;
+      }
+      F = x2::pack(fa, fb);
+      FPR = x2::pack(pa, pb);
+    }
+    const uint64_t S1 = x2::mul(FPR, DA);
+    const uint64_t S2 = x2::fma(FPR, R2, x2::mul(F, TWO));
+    PS[0] = x2::fma(DX, S1, PS[0]);
+    PS[1] = x2::fma(DY, S1, PS[1]);
+    PS[2] = x2::fma(DZ, S1, PS[2]);
+    QS[0] = x2::fma(AX, S2, QS[0]);
+    QS[1] = x2::fma(AY, S2, QS[1]);
+    QS[2] = x2::fma(AZ, S2, QS[2]);
+  }
+  acc[0] = x2::sub(PS[0], QS[0]);
+  acc[1] = x2::sub(PS[1], QS[1]);
+  acc[2] = x2::sub(PS[2], QS[2]);
+}
+
 // The same sums in the factored form (FACT): d x a = t x a - x_s x a with
 // c = x_s x a staged per source, and d never formed: q = |t|^2 + S - 2 t . x_s
 // and d . G = t . G - x_s . G take three fused multiply-adds each from
@@ -1403,9 +1527,12 @@ __device__ __forceinline__ void near_tile_factored(const float4* __restrict__ ro
 template <int MODE, int KERNEL, int TPT>
 struct EvalSmem {
   // paired path: Winckelmans velocity / stretching with two or four targets
-  // per thread
-  static constexpr bool PACKED = (TPT == 2 || TPT == 4) && KERNEL == FVX_KERNEL_WINCKELMANS &&
-                                 (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_STRETCH);
+  // per thread, the Gaussian-erf vorticity with two
+  static constexpr bool VORT_GAUSS = KERNEL == FVX_KERNEL_GAUSSIANERF && MODE == FVX_PAIR_VORTICITY;
+  static constexpr bool PACKED =
+      ((TPT == 2 || TPT == 4) && KERNEL == FVX_KERNEL_WINCKELMANS &&
+       (MODE == FVX_PAIR_VELOCITY || MODE == FVX_PAIR_STRETCH)) ||
+      (TPT == 2 && VORT_GAUSS);
   // paired: the tile's planes, then the lanes' running near-field sums
   // (hi, lo of TPT targets x three components, 6 TPT x 32 floats)
   static constexpr int kNearBytes = PACKED ? kPlanes * kNearTile * 16 + 6 * TPT * kEvalThreads * 4
@@ -1581,16 +1708,22 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
             }
             if (k < rows) {
               float4* row = s_r + k;
-              if constexpr (FACT) {
-                const float S2 = fmaf(p.x, p.x, fmaf(p.y, p.y, fmaf(p.z, p.z, p.w)));
-                row[0] = make_float4(p.x, p.y, p.z, S2);
-                row[2 * kNearTile] =
-                    make_float4(p.y * av.z - p.z * av.y, p.z * av.x - p.x * av.z,
-                                p.x * av.y - p.y * av.x, 0.f);
+              if constexpr (EvalSmem<MODE, KERNEL, TPT>::VORT_GAUSS) {
+                // {-x, 1/s}, {a, 1/s^2} (a padding row: 1/s = 0, no strength)
+                row[0] = make_float4(-p.x, -p.y, -p.z, av.w);
+                row[kNearTile] = make_float4(av.x, av.y, av.z, av.w * av.w);
               } else {
-                row[0] = make_float4(-p.x, -p.y, -p.z, p.w);
+                if constexpr (FACT) {
+                  const float S2 = fmaf(p.x, p.x, fmaf(p.y, p.y, fmaf(p.z, p.z, p.w)));
+                  row[0] = make_float4(p.x, p.y, p.z, S2);
+                  row[2 * kNearTile] =
+                      make_float4(p.y * av.z - p.z * av.y, p.z * av.x - p.x * av.z,
+                                  p.x * av.y - p.y * av.x, 0.f);
+                } else {
+                  row[0] = make_float4(-p.x, -p.y, -p.z, p.w);
+                }
+                row[kNearTile] = make_float4(1.5f * p.w, av.x, av.y, av.z);
               }
-              row[kNearTile] = make_float4(1.5f * p.w, av.x, av.y, av.z);
             }
           }
           __syncthreads();
@@ -1599,6 +1732,8 @@ __device__ __forceinline__ void eval_leaf(const EvalArgs& A, int t, unsigned cha
           if constexpr (FACT) {
             near_tile_factored<MODE, NP>(row, rows / g, g, M2X, M2Y, M2Z, TT, NGX, NGY, NGZ, TG,
                                          acc2);
+          } else if constexpr (EvalSmem<MODE, KERNEL, TPT>::VORT_GAUSS) {
+            near_tile_vort_gauss(row, rows / g, g, TX[0], TY[0], TZ[0], acc2[0]);
           } else {
             static_assert(FACT || NP == 1, "the direct form takes two targets per lane");
             near_tile_direct<MODE>(row, rows / g, g, TX[0], TY[0], TZ[0], GX[0], GY[0], GZ[0],
@@ -2334,12 +2469,13 @@ void launch_eval_tpt(int mode, int nleaf, const tree::EvalArgs& A, bool factored
 template <int KERNEL>
 void launch_eval(int mode, int nleaf, int n, const tree::EvalArgs& A, bool factored,
                  cudaStream_t s) {
-  // Winckelmans velocity and stretching: the paired f32x2 kernel, whose
-  // source phases keep small leaves' slots busy.  Otherwise two targets per
-  // thread once leaves average more than ~40 particles; at fewer, one target
-  // per thread wastes fewer lanes.
-  const bool paired = KERNEL == FVX_KERNEL_WINCKELMANS &&
-                      (mode == FVX_PAIR_VELOCITY || mode == FVX_PAIR_STRETCH);
+  // Winckelmans velocity and stretching and the Gaussian-erf vorticity: the
+  // paired f32x2 kernels, whose source phases keep small leaves' slots busy.
+  // Otherwise two targets per thread once leaves average more than ~40
+  // particles; at fewer, one target per thread wastes fewer lanes.
+  const bool paired = (KERNEL == FVX_KERNEL_WINCKELMANS &&
+                       (mode == FVX_PAIR_VELOCITY || mode == FVX_PAIR_STRETCH)) ||
+                      (KERNEL == FVX_KERNEL_GAUSSIANERF && mode == FVX_PAIR_VORTICITY);
   if (!paired && n <= 40 * nleaf)
     launch_eval_tpt<KERNEL, 1>(mode, nleaf, A, false, s);
   else

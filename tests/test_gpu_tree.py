@@ -194,6 +194,27 @@ def test_factored_near_loop_matches_oracle_algorithm(cuda, n, leaf):
     assert eu < 4e-6 and es < 4e-6
 
 
+@pytest.mark.parametrize("n,leaf", [(3000, 16), (12000, 64)])
+def test_paired_gaussian_vorticity_matches_oracle_algorithm(cuda, n, leaf):
+    """The Gaussian-erf vorticity sweep (the Pedrizzetti relaxation's) in its
+    paired loop -- erf from Abramowitz & Stegun 7.1.26 sharing the core's
+    exponential, the series below rho^2 = 0.25 -- with cores 1.3 x the particle
+    spacing, so that every target's self pair and its close neighbours take
+    the series, against the oracle's FP64 restatement of the same treecode.
+    The difference is the FP32 arithmetic and the rational erf (both well
+    under the bar of the other sweeps' oracle test)."""
+    pos, gam, sig = _factored_case(n=n, leaf=leaf)
+    tr = OT.build(pos, theta=0.5, leaf_target=leaf)
+    OT.moments(tr, pos, gam)
+    _, J = OT.evaluate(tr, pos, gam, sig, kernel="gaussianerf")
+    w = np.stack([J[:, 2, 1] - J[:, 1, 2], J[:, 0, 2] - J[:, 2, 0], J[:, 1, 0] - J[:, 0, 1]], 1)
+    gw, _, _ = _tree(_capi.PAIR_VORTICITY, "gaussianerf", pos, gam, sig, cuda, leaf)
+    e = rel_err(gw, w)
+    print(f"paired Gaussian-erf vorticity vs oracle: {e:.2e}")
+    assert e < 2e-5
+    assert _capi.status_read_and_clear() == 0
+
+
 @pytest.mark.parametrize("mode", ["velocity", "stretch"])
 def test_factored_near_field_with_fp64_far_field(cuda, mode):
     """Every far pair sent to the FP64 fallback (judge tolerance ~ 0), so only
