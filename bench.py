@@ -124,6 +124,10 @@ def parse():
     p.add_argument("--sweep-core", choices=("thin", "resolved"), default="thin",
                    help="--sweep-case cores: 0.02c (the slab sweep case) or 1.3 x the "
                         "particle spacing (the benchmarked step's slab)")
+    p.add_argument("--sweep-kind", choices=("velocity-stretch", "vorticity"),
+                   default="velocity-stretch",
+                   help="--sweep-case sweeps: the Winckelmans velocity + stretching pair, or "
+                        "the Gaussian-erf vorticity sweep of the Pedrizzetti relaxation")
     return p.parse_args()
 
 
@@ -373,7 +377,8 @@ def run_sweep_case(args):
     profiling case of the evaluation, translation and network kernels.
     ``--repeat R`` runs R more sweep pairs at the same positions and prints the
     median times of the evaluation kernel and of the local-expansion stage
-    (CUDA events inside the library)."""
+    (CUDA events inside the library).  ``--sweep-kind vorticity`` runs the
+    Gaussian-erf vorticity sweep of the relaxation instead of the pair."""
     import torch
     from fluxvortex_gb300 import _capi
     from fluxvortex_gb300.tree import TreeSweeper
@@ -391,13 +396,17 @@ def run_sweep_case(args):
     ts.set_far_field(ff, mlp=mlp)
     ts.set_validation(0, 0.1)
     out = torch.empty((args.n, 3), dtype=torch.float64, device="cuda")
-    ts.sweep(_capi.PAIR_VELOCITY, "winckelmans", P, G, S, args.n, out)
-    ts.sweep(_capi.PAIR_STRETCH, "winckelmans", P, G, S, args.n, out, tgt_gamma=G)
-    times = {"velocity": [], "stretch": []}
+    if args.sweep_kind == "vorticity":
+        kinds = (("vorticity", _capi.PAIR_VORTICITY, None, "gaussianerf"),)
+    else:
+        kinds = (("velocity", _capi.PAIR_VELOCITY, None, "winckelmans"),
+                 ("stretch", _capi.PAIR_STRETCH, G, "winckelmans"))
+    for _, mode, tg, kern in kinds:
+        ts.sweep(mode, kern, P, G, S, args.n, out, tgt_gamma=tg)
+    times = {k[0]: [] for k in kinds}
     for _ in range(args.repeat):
-        for name, mode, tg in (("velocity", _capi.PAIR_VELOCITY, None),
-                               ("stretch", _capi.PAIR_STRETCH, G)):
-            ts.sweep(mode, "winckelmans", P, G, S, args.n, out, tgt_gamma=tg, check=True,
+        for name, mode, tg, kern in kinds:
+            ts.sweep(mode, kern, P, G, S, args.n, out, tgt_gamma=tg, check=True,
                      same_positions=True)
             loc = ts.last_local_ms() if ff != "m2p" else 0.0
             times[name].append((ts.last_eval_ms(), loc))
@@ -409,7 +418,7 @@ def run_sweep_case(args):
             print(f"{name}: evaluation {ev:.3f} ms, local-expansion stage {lo:.3f} ms "
                   f"(median of {len(t)})", file=sys.stderr)
     st = _capi.status_read_and_clear()
-    print(f"sweep case ok: max |S| = {float(out.abs().max())}, status {st}", file=sys.stderr)
+    print(f"sweep case ok: max |out| = {float(out.abs().max())}, status {st}", file=sys.stderr)
     if st:
         raise SystemExit(f"device status {st}")
 
