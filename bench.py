@@ -713,7 +713,8 @@ def run_ours(args, rank, world):
         # self-sweep and the strength update more); as the reference's hybrid
         # solver runs its free wake, without the stretching term
         # (experiment_hybrid_panel_particle.py:140-143: three velocity sweeps);
-        # and with the analytic translation alone as the far field
+        # both, as that solver is set up (rlxf = 0.3 at :111); and with the
+        # analytic translation alone as the far field
         del step
         torch.cuda.empty_cache()
         flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
@@ -724,6 +725,10 @@ def run_ours(args, rank, world):
                 ("stretching_off_variant", dict(stretch=False),
                  "the benchmarked step without the stretching term, as the reference's "
                  "hybrid solver runs its free wake (3 velocity self-sweeps per step)"),
+                ("reference_solver_variant", dict(stretch=False, rlxf=0.3),
+                 "the step as the reference's hybrid solver sets it up: no stretching "
+                 "term, Pedrizzetti relaxation at rlxf = 0.3 (3 velocity self-sweeps and "
+                 "one Gaussian-erf vorticity self-sweep per step)"),
                 ("translation_only_variant", dict(far_field="m2l"),
                  "the benchmarked step with the analytic multipole-to-local translation "
                  "alone as the far field (no network residual), judged alike: the method "
