@@ -269,14 +269,22 @@ __global__ void __launch_bounds__(kThreads) pairs_kernel(PairArgs A) {
   }
 }
 
+// The split partial sums of every output value, in a fixed order: a warp per
+// value, lane l adding splits l, l + 32, ... in turn, then a fixed shuffle
+// tree over the lanes.  (A thread per value would leave a few hundred values
+// to a handful of CTAs, each thread waiting on one dependent load per split.)
 __global__ void reduce_pairs_kernel(const double* __restrict__ partial, int64_t n_tgt, int nc,
                                     int na, int splits, double* __restrict__ out_a,
                                     double* __restrict__ out_b) {
-  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t idx = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   const int64_t n_vals = n_tgt * nc;
-  if (idx >= n_vals) return;
+  if (idx >= n_vals) return;  // the whole warp: idx is the warp's
   double s = 0.0;
-  for (int k = 0; k < splits; ++k) s += partial[static_cast<int64_t>(k) * n_vals + idx];
+  for (int k = lane; k < splits; k += 32) s += partial[static_cast<int64_t>(k) * n_vals + idx];
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  if (lane != 0) return;
   const int64_t i = idx / nc;
   const int c = static_cast<int>(idx - i * nc);
   if (c < na)
@@ -418,8 +426,9 @@ int particle_pairs_launch(int mode, int kernel, int precision, const double* tgt
     launch_kernel<FVX_KERNEL_GAUSSIANERF>(mode, precision, grid, stream, A);
   FVX_LAUNCH_CHECK();
   if (splits > 1) {
-    const int64_t nv = n_tgt * nc;
-    reduce_pairs_kernel<<<static_cast<unsigned>((nv + 255) / 256), 256, 0, stream>>>(
+    const int64_t nv = n_tgt * nc;  // a warp per value
+    FVX_ARG_CHECK((nv * 32 + 255) / 256 < (1LL << 31), "too many output values");
+    reduce_pairs_kernel<<<static_cast<unsigned>((nv * 32 + 255) / 256), 256, 0, stream>>>(
         static_cast<const double*>(scratch), n_tgt, nc, na, splits, out_a, out_b);
     FVX_LAUNCH_CHECK();
   }
