@@ -38,6 +38,10 @@ constexpr int W1o = 0, W2o = W1o + H * IN, W3o = W2o + H * H, W4o = W3o + H * H,
 constexpr int B1o = 0, B2o = H, B3o = 2 * H, B4o = 3 * H, BN = 3 * H + OUT;
 constexpr int kRecFloats = 40;  // treecode cell record (fvx_tree.cu)
 constexpr int kTargetsThreads = 256;  // FP64 exact-expansion sums: threads per pair
+// The judge's FP64 sums take their cells in chunks of four particles per thread:
+// each chunk ends in a block reduction of 30 FP64 values, which on this GPU's
+// FP64 pipe costs about as much as one particle per thread.
+constexpr int kJudgeChunk = 4 * kTargetsThreads;
 
 // Four 128-row tiles are in flight per CTA (one per warpgroup, each with a
 // quarter of the tensor memory): while some groups run their epilogues on the
@@ -882,9 +886,9 @@ __global__ void pair_sums_kernel(int npairs, int stride, const int* __restrict__
 }
 
 // The same sums for the FP64 judge's samples, balanced over the GPU whatever
-// the cells' sizes: each sample's cell is cut into chunks of kTargetsThreads
+// the cells' sizes: each sample's cell is cut into chunks of kJudgeChunk
 // particles, item offsets per slot come from judge_chunks_kernel, and
-// resident CTAs stride over the items (one particle per thread), adding each
+// resident CTAs stride over the items (four particles per thread), adding each
 // chunk's 30 sums into the slot's with FP64 atomics (the order of those
 // additions varies from run to run in the last bits).  Slots: list 0's
 // samples, then list 1's, cap each; slots past a list's count take no items.
@@ -903,7 +907,7 @@ __global__ void judge_chunks_kernel(JudgeSampleView S, const int* __restrict__ c
     if (i < n) {
       const int li = i >= S.cap ? 1 : 0;
       const int q = i - li * S.cap;
-      if (q < S.cnt[li]) c = (cell_count[S.cell[li][q]] + kTargetsThreads - 1) / kTargetsThreads;
+      if (q < S.cnt[li]) c = (cell_count[S.cell[li][q]] + kJudgeChunk - 1) / kJudgeChunk;
     }
     __syncthreads();
     sc[threadIdx.x] = c;
@@ -940,8 +944,8 @@ __global__ void __launch_bounds__(kTargetsThreads) judge_sums_kernel(
     const float3 cT = leaf_center(S.key[li][q], S.h[li]);
     const int g = S.cell[li][q];
     const int c0 = cell_start[g], cn = cell_count[g];
-    const int s0 = c0 + (item - off[slot]) * kTargetsThreads;
-    const int m = min(kTargetsThreads, c0 + cn - s0);
+    const int s0 = c0 + (item - off[slot]) * kJudgeChunk;
+    const int m = min(kJudgeChunk, c0 + cn - s0);
     double acc[NOUT];
     exact_expansion_slice(cT, s0, m, leaf_key, sp, sa, leaf_of_particle, h, acc);
     reduce_expansion(acc, s_out);
