@@ -2612,7 +2612,8 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
       (rc = grow(T->sp, 16 * size_t(n))) || (rc = grow(T->sa, 16 * size_t(n))) ||
       (rc = grow(T->sg, 16 * size_t(n))))
     return rc;
-  // 2. keys + stable radix sort (4 passes: result back in keys0/idx0)
+  // 2. keys + stable radix sort: a pass per 8 bits of the 3L-bit keys (the result in
+  //    ka / ia, the other pair free)
   keys_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, pos, origin[0], origin[1], origin[2], 1.0 / h, L,
                                               P<uint32_t>(T->keys0), P<int>(T->idx0));
   FVX_LAUNCH_CHECK();
@@ -2620,7 +2621,8 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   int *ia = P<int>(T->idx0), *ib = P<int>(T->idx1);
   int* table = P<int>(T->table);
   int* table_ex = table + 256 * nblk;
-  for (int pass = 0; pass < 4; ++pass) {
+  const int passes = (3 * L + 7) / 8;
+  for (int pass = 0; pass < passes; ++pass) {
     const int shift = 8 * pass;
     radix_hist_kernel<<<nblk, 256, 0, s>>>(ka, n, shift, nblk, table);
     FVX_LAUNCH_CHECK();
@@ -2651,8 +2653,8 @@ int tree_sweep(fvx_tree* T, int mode, int kernel, const double* pos, const doubl
   FVX_LAUNCH_CHECK();
   // parent levels reuse flag (as flags) and the scan buffer; the leaf ids of
   // the particles (cid) are kept for the gather
-  int* pflag = P<int>(T->keys1);  // free after the sort
-  int* pid = P<int>(T->idx1);
+  int* pflag = reinterpret_cast<int*>(kb);  // the sort's free pair
+  int* pid = ib;
   for (int l = L - 1; l >= 0; --l) {
     Level ch = level(l + 1), par = level(l);
     const int cc = cap[l + 1];
